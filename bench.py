@@ -1,0 +1,395 @@
+#!/usr/bin/env python
+"""Benchmark of the XPBD cloth substep on GB300.
+
+Workload (default ``drape256``): a 256 x 256 cloth (65536 vertices, 130050
+faces) over a static 20480-face sphere; per frame 10 substeps, each with a
+cell-grid LBVH rebuild of both meshes, 30 Jacobi spring/bending iterations,
+broad phase in the first iteration, vertex-triangle contact projection in every
+iteration, velocity and position update.  One step = one frame.  The metric is
+cloth vertex-substeps per second (vertices x substeps / time).
+
+Timing: W untimed warm-up frames, then K timed frames; before each timed frame a
+256 MiB buffer is written to flush L2 (the frame's own working set, a few MB,
+is smaller than L2); each frame is bracketed by CUDA events on the solver's
+stream.  ``e2e`` repeats the measurement through the public API with the
+state uploaded from pinned host memory and downloaded again inside the timed
+region.  ``roofline`` reports the dominant kernel (the Jacobi sweep) timed with
+CUDA events over a separate instrumented pass.  ``cpu_baseline`` times the CPU
+oracle (a port of the reference algorithm, OpenMP on all host cores) on one
+substep of the same scene.
+
+``--impl reference`` times that CPU port alone as the reference arm.
+Multi-GPU (torchrun): every rank runs an independent replica of the workload
+(the substep has no cross-cloth exchange); the value is the sum of the
+replicas' work divided by the slowest rank's time.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "cloth vertex-substeps/s (256x256 self-collision drape, 10 substeps x 30 Jacobi iterations)"
+UNIT = "vertex-substeps/s"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", choices=["drape256", "plain64"], default="drape256")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(n_gpus):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(v, world):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def build_scene(name):
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    if name == "drape256":
+        return pkg, pkg.scenes.drape256()
+    return pkg, pkg.scenes.plain64()
+
+
+def workload_config(scene, name, sim=None):
+    return {
+        "workload": f"{name}: {scene.meta.get('grid')}x{scene.meta.get('grid')} cloth, "
+                    f"{len(scene.cloth_faces)} faces, obstacle {0 if scene.obstacle_faces is None else len(scene.obstacle_faces)} faces",
+        "vertices": int(scene.cloth_x.shape[0]),
+        "substeps_per_step": scene.n_substeps,
+        "jacobi_iterations": scene.n_iter,
+        "bvh_rebuild": scene.rebuild,
+        "contact": "vertex-triangle (static + self), dHat=thickness^2",
+        "bending_on": "y",
+        "l2": "flushed before every timed step (256 MiB write); working set < L2",
+    }
+
+
+class ClockSampler:
+    """nvidia-smi clocks/throttle sampling in the background (200 ms)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append((float(parts[1]), float(parts[2]), parts[5:9]))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(r[0] for r in rows)
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i, v in enumerate(r[2]) if v.lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": rows[0][1], "reasons": reasons, "samples": len(rows)}
+
+
+def measured_peak():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel_file):
+    """Per-launch DRAM bytes of the dominant kernel from its committed ncu summary."""
+    p = os.path.join(ROOT, "profiles", kernel_file)
+    try:
+        for line in open(p):
+            if line.startswith("traffic_bytes_per_launch:"):
+                return float(line.split(":", 1)[1].split()[0])
+    except OSError:
+        pass
+    return None
+
+
+def cpu_baseline(scene, rank):
+    """Oracle port on all host cores, one substep of the same scene."""
+    import numpy as np  # noqa: F401
+
+    from oracle import pyoracle as po
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    from starlab_physics_gb300 import mesh as M
+
+    cl = M.TriMesh(scene.cloth_x, scene.cloth_faces, device="cpu")
+    ob = M.TriMesh(scene.obstacle_x, scene.obstacle_faces, device="cpu") if scene.obstacle_x is not None else None
+    if len(scene.pinned):
+        cl.fixed[scene.pinned] = 0.0
+    cores = os.cpu_count() or 1
+    orc = po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob) if ob else None, dt=scene.dt,
+                          g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
+                          k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
+                          padding=scene.padding, n_iter=scene.n_iter, collisions=scene.collisions,
+                          rebuild=scene.rebuild, cap=scene.cap, nthreads=cores, bending_on="y")
+    dt_sub = scene.dt / scene.n_substeps
+    orc.substep(dt_sub)  # warm-up
+    n = 0
+    t0 = time.perf_counter()
+    while True:
+        orc.substep(dt_sub)
+        n += 1
+        el = time.perf_counter() - t0
+        if el > 8.0 or n >= 10:
+            break
+    V = scene.cloth_x.shape[0]
+    return {"value": V * n / el, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{n} substep(s) of the same scene on the CPU oracle (OpenMP, {cores} threads), "
+                      f"{el:.2f} s"}
+
+
+def run_reference(args):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    pkg, scene = build_scene(args.workload)
+    from oracle import pyoracle as po
+    from starlab_physics_gb300 import mesh as M
+
+    cl = M.TriMesh(scene.cloth_x, scene.cloth_faces, device="cpu")
+    ob = M.TriMesh(scene.obstacle_x, scene.obstacle_faces, device="cpu") if scene.obstacle_x is not None else None
+    if len(scene.pinned):
+        cl.fixed[scene.pinned] = 0.0
+    cores = os.cpu_count() or 1
+    orc = po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob) if ob else None, dt=scene.dt,
+                          g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
+                          k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
+                          padding=scene.padding, n_iter=scene.n_iter, collisions=scene.collisions,
+                          rebuild=scene.rebuild, cap=scene.cap, nthreads=cores, bending_on="y")
+    dt_sub = scene.dt / scene.n_substeps
+    for _ in range(max(1, min(args.warmup, 2))):
+        orc.substep(dt_sub)
+    times = []
+    budget = 150.0
+    t_all = time.perf_counter()
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        orc.substep(dt_sub)
+        times.append(time.perf_counter() - t0)
+        if time.perf_counter() - t_all > budget:
+            break
+    V = scene.cloth_x.shape[0]
+    tot = sum(times)
+    val = V * len(times) / tot
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_config(scene, args.workload) | {"step": "one substep (bounded CPU sample)"},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
+                         "sample": f"{len(times)} substeps of the same scene on the CPU oracle, {cores} threads "
+                                   "(the reference's Taichi path cannot run here)"},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+
+    world, rank, local = dist_setup(args.gpus)
+    pkg, scene = build_scene(args.workload)
+    from starlab_physics_gb300 import _lib
+
+    _lib.load()
+    sim = pkg.scenes.make_solver(scene, device="cuda")
+    sim.bending_on = "y"
+    V = sim.mesh_dy.num_verts
+    S = scene.n_substeps
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    x0 = sim.mesh_dy.x4.clone()
+    v0 = sim.mesh_dy.v4.clone()
+    for _ in range(args.warmup):
+        sim.forward(S)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region ----
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    lib = _lib.load()
+    l0 = lib.sx_kernel_launches()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            sim.forward(S)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    launches = lib.sx_kernel_launches() - l0
+    barrier(world)
+    ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    ms = max_over_ranks(ms, world)
+    value = world * V * S * args.steps / (ms / 1e3)
+    status = sim.status_flags()
+
+    # ---- end-to-end through the public API with host buffers ----
+    xh = x0.cpu().pin_memory()
+    vh = v0.cpu().pin_memory()
+    xo = torch.empty_like(xh).pin_memory()
+    vo = torch.empty_like(vh).pin_memory()
+    e_st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    e_en = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk2:
+        for k in range(args.steps):
+            flush.zero_()
+            e_st[k].record(stream)
+            sim.mesh_dy.x4.copy_(xh, non_blocking=True)
+            sim.mesh_dy.v4.copy_(vh, non_blocking=True)
+            sim.forward(S)
+            xo.copy_(sim.mesh_dy.x4, non_blocking=True)
+            vo.copy_(sim.mesh_dy.v4, non_blocking=True)
+            e_en[k].record(stream)
+        torch.cuda.synchronize()
+    ms_e2e = max_over_ranks(sum(s.elapsed_time(e) for s, e in zip(e_st, e_en)), world)
+    e2e_val = world * V * S * args.steps / (ms_e2e / 1e3)
+    bytes_io = 2 * V * 16
+
+    # ---- dominant kernel: Jacobi sweep, instrumented pass ----
+    sweeps = []
+    orig = sim.spring_sweep
+
+    def timed_sweep(dt):
+        a = torch.cuda.Event(enable_timing=True)
+        b = torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        orig(dt)
+        b.record(stream)
+        sweeps.append((a, b))
+
+    sim.spring_sweep = timed_sweep
+    n_inst = max(1, min(args.steps, 5))
+    for _ in range(n_inst):
+        sim.forward(S)
+    torch.cuda.synchronize()
+    sim.spring_sweep = orig
+    sweep_ms = sum(a.elapsed_time(b) for a, b in sweeps) / len(sweeps)
+    m = sim.mesh_dy
+    E, B = m.num_edges, m.bending_constraint_count
+    alg_bytes = 12 * (E + B) + 28 * V
+    achieved = alg_bytes / (sweep_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    frame_ms = ms / args.steps
+    roofline = {"kernel": "jacobi_sweep_kernel", "bound": "hbm", "achieved": round(achieved, 1),
+                "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                "traffic": ncu_traffic("jacobi_sweep_kernel_drape256.md"),
+                "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": round(sweep_ms * 1e3, 3),
+                "launches_per_step": len(sweeps) // n_inst,
+                "share_of_step": round(sweep_ms * (len(sweeps) / n_inst) / frame_ms, 4),
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": frame_ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generators)",
+        "config": workload_config(scene, args.workload),
+        "gpu_launches": int(launches),
+        "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},
+        "roofline": roofline,
+        "clocks": clk.summary(),
+        "status_flags": status,
+    }
+    line["clocks_e2e"] = clk2.summary()
+    if rank == 0 and world >= 1 and not args.no_cpu_baseline and world == 1:
+        line["cpu_baseline"] = cpu_baseline(scene, rank)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

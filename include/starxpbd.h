@@ -1,0 +1,180 @@
+/*
+ * starxpbd -- C ABI of the GB300 (sm_103a) XPBD cloth substep library.
+ *
+ * Every entry point takes raw device pointers, element counts and a CUDA
+ * stream (cudaStream_t passed as void*; NULL = legacy default stream).  Calls
+ * are enqueued on that stream and return without synchronising, except where
+ * noted.  No entry point allocates or frees memory: scratch space comes from
+ * caller-provided workspaces whose size is given by the *_workspace_bytes
+ * functions.  Errors are returned as negative codes (below); the message of the
+ * last error on the calling thread is available from sx_last_error().  No C++
+ * exception crosses this boundary.
+ *
+ * Layout conventions
+ *   positions / velocities : float4 per vertex (xyz + w).  For x4 and y4 the w
+ *                            lane holds wf = fixed * m_inv; for v4 it is unused.
+ *   face AABBs             : float4 per face for min and for max (w unused).
+ *   boxes                  : box6 = {min x, min y, min z, max x, max y, max z}.
+ *   indices                : int32.
+ *   BVH nodes              : 2n-1 nodes; internal nodes 0..n-2, leaves n-1..2n-2.
+ *
+ * Each declaration cites the reference (medialab-ku/starlab-physics) function
+ * it replaces, as path:line within that project.
+ */
+#ifndef STARXPBD_H
+#define STARXPBD_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SX_OK 0
+#define SX_ERR_ARG (-1)      /* bad argument (null pointer, size, workspace)      */
+#define SX_ERR_CAPACITY (-2) /* a fixed-capacity list overflowed (see status word) */
+#define SX_ERR_TIMEOUT (-3)  /* a bounded device-side wait gave up                */
+#define SX_ERR_CUDA (-4)     /* a CUDA runtime call failed                          */
+
+/* status-word bits written by traversal / contact kernels (int32, device) */
+#define SX_STATUS_CAND_OVERFLOW 1  /* a query found more candidates than `cap`     */
+#define SX_STATUS_STACK_OVERFLOW 2 /* a traversal stack (64 entries) overflowed     */
+#define SX_STATUS_FIXED_RANGE 4    /* a contact term was NaN or out of fixed range  */
+#define SX_STATUS_CLIMB_LIMIT 8    /* a bottom-up refit walk exceeded n steps        */
+
+int sx_version(void);
+const char* sx_last_error(void);
+/* Number of CUDA kernels this library has launched in the process so far
+ * (all threads); benchmarks difference it around a timed region. */
+long long sx_kernel_launches(void);
+
+/* ---- cloth state (framework/physics/XPBD.py) ------------------------------ */
+
+/* compute_y, XPBD.py:116-118: y = x + fixed*v*dt + g*dt*dt; y.w = x.w */
+int sx_predict(const float* x4, const float* v4, const float* fixed, float* y4, int n_verts, float dt,
+               float gx, float gy, float gz, void* stream);
+
+/* One Jacobi sweep: init_variables + solve_spring_constraints_x + update_dx,
+ * XPBD.py:345-348, :141-184, :384-387.  Springs read y_in4; bending pairs read
+ * x4 as in the reference (XPBD.py:169) when bend_on_y == 0, or y_in4 when
+ * bend_on_y == 1.  Vertex-centric gather over adj_ptr[n_verts+1] /
+ * adj[2*nnz] = (neighbour | 0x80000000 for bending, float bits of rest length)
+ * in ascending constraint index; writes y_out4 (must not alias y_in4).
+ * k_spring, k_bend = stiffness * dt^2 of the two constraint types. */
+int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
+                    const int* adj, int n_verts, float k_spring, float k_bend, int bend_on_y, void* stream);
+
+/* compute_velocity + update_x, XPBD.py:341-343 and :333-337:
+ * v = (1-damping)*fixed*(y-x)/dt ; x += dt*v */
+int sx_velocity_update(float* x4, const float* y4, float* v4, const float* fixed, int n_verts, float damping,
+                       float dt, void* stream);
+
+/* computeAABB_faces, meshTaichiWrapper.py:351-365 (positions p4) */
+int sx_face_aabbs(const float* p4, const int* faces, int n_faces, float padding, float* aabb_min4,
+                  float* aabb_max4, void* stream);
+
+/* computeAABB, meshTaichiWrapper.py:335-347: box6 (device) = vertex AABB +- padding.
+ * The reference returns the box to the host; here it stays on the device. */
+int sx_scene_aabb(const float* p4, int n_verts, float padding, float* box6, void* stream);
+
+/* ---- LBVH over the 32^3 cell grid (framework/collision/lbvh_cell.py) ------- */
+
+/* LBVH_CELL.__init__, lbvh_cell.py:78-80: Morton codes of the 32768 cell
+ * centres (assign_cell_morton :123-152), radix sort (radix_sort_cells
+ * :553-562) and Karras build (assign_internal_nodes_Karras12_cells :408-430).
+ * Outputs are 32768 (codes, ids) and 32767 internal nodes; parent has 65535. */
+size_t sx_cell_bvh_workspace_bytes(int n_faces);
+int sx_cell_bvh_init(int* sorted_codes, int* sorted_ids, int* child_a, int* child_b, int* range_l, int* range_r,
+                     int* parent, void* ws, size_t ws_bytes, void* stream);
+
+/* LBVH_CELL.build, lbvh_cell.py:637-653: cell size from box6
+ * (assign_cell_centers :105-120), faces binned by AABB centre
+ * (assign_face_cell_ids :577-586), inclusive scan, stable counting sort
+ * (counting_sort_cells :589-598), leaves = row-major cells with
+ * AABB = centre U faces (assign_leaf_cell_nodes :602-634) and a single-launch
+ * bottom-up refit with the rules of compute_cell_node_aabbs :491-522.
+ * Outputs: sorted_face_ids[n_faces], prefix[32768] (inclusive),
+ * num_faces[65535], nmin4/nmax4[65535], cell_size3[3]. */
+int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_faces, const float* box6, const int* child_a,
+                      const int* child_b, const int* parent, int* sorted_face_ids, int* prefix, int* num_faces,
+                      float* nmin4, float* nmax4, float* cell_size3, void* ws, size_t ws_bytes, void* stream);
+
+/* traverse_cell_bvh_single, lbvh_cell.py:656-714, for query boxes
+ * p4[i] +- padding (Solver.broadphase_lbvh, XPBD.py:187-215).  origin = box6 of
+ * the build (its min corner is the grid origin).  cand[q*cap + j] for j < cap;
+ * num[q] = total overlaps found (num > cap: list truncated, status bit 1). */
+int sx_cell_bvh_traverse(const float* p4, int n_queries, float padding, const float* cell_size3,
+                         const float* origin_box6, const int* child_a, const int* child_b, const int* num_faces,
+                         const float* nmin4, const float* nmax4, const int* prefix, const int* sorted_face_ids,
+                         const float* fmin4, const float* fmax4, int cap, int* cand, int* num, int* status,
+                         void* stream);
+
+/* ---- face-level LBVH (standalone broad phase) ------------------------------ */
+
+/* Morton codes of face-AABB centres normalised by box6 (intended form of
+ * LBVH_CELL.assign_morton, lbvh_cell.py:196-232; morton_3d :87-102). ids[i]=i */
+int sx_face_morton(const float* fmin4, const float* fmax4, int n_faces, const float* box6, unsigned* codes,
+                   int* ids, void* stream);
+
+/* Stable LSD radix sort of (key, value) pairs on the low `bits` key bits
+ * (radix_sort_cells, lbvh_cell.py:525-562: the reference uses 6-bit digits and
+ * a serialised scatter; here 8-bit digits, per-block histograms and a
+ * warp-ranked stable scatter give the same permutation). In place. */
+size_t sx_radix_sort_workspace_bytes(int n);
+int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, void* ws, size_t ws_bytes, void* stream);
+
+/* Karras 2012 hierarchy over sorted codes (assign_internal_nodes_Karras12,
+ * lbvh_cell.py:384-405, with delta/find_split/determine_range :256-336).
+ * tie = 0: the reference's rule (equal codes give delta = 32, split at the
+ * midpoint); tie = 1: equal codes compare by index (always a valid tree).
+ * parent has 2n-1 entries; parent[0] = -1. */
+int sx_karras_build(const unsigned* codes, int n, int tie, int* child_a, int* child_b, int* range_l,
+                    int* range_r, int* parent, void* stream);
+
+/* Bottom-up refit of a face-level LBVH (one face per leaf; leaf n-1+j holds
+ * face sorted_ids[j]): node box = union of children, single launch with
+ * per-node arrival counters (flags: n-1 ints scratch, zero on entry, left
+ * zero on exit). */
+int sx_face_bvh_refit(int n, const int* sorted_ids, const float* fmin4, const float* fmax4, const int* child_a,
+                      const int* child_b, const int* parent, float* nmin4, float* nmax4, int* flags, int* status,
+                      void* stream);
+
+/* Stack traversal of a face-level LBVH for query boxes p4[i] +- padding, same
+ * visiting order as traverse_cell_bvh_single (lbvh_cell.py:662-714). */
+int sx_face_bvh_traverse(int n, const float* p4, int n_queries, float padding, const int* child_a,
+                         const int* child_b, const int* sorted_ids, const float* nmin4, const float* nmax4, int cap,
+                         int* cand, int* num, int* status, void* stream);
+
+/* ---- narrow phase + contact projection ------------------------------------ */
+
+/* solve_collision_constraints_x (XPBD.py:237-264) -> __vt_st / __vt_dy /
+ * __tv_st (collision_constraints_x.py:6-310; distance.py:5-47, :102-184,
+ * :413-459), then update_dx (XPBD.py:384-387) on the dynamic mesh y4.
+ * Candidate blocks: vt_st and vt_dy are n_dy x cap, tv_st is n_st x cap.
+ * Corrections are accumulated in 64-bit fixed point (40 fractional bits) in
+ * dx_fix[3*n_dy] and nc[n_dy], which must be zero on entry and are zero again
+ * on return.  Pair records (pair[2], pair_g[16 floats], pair_schur, pair_num;
+ * blocks vt_st | vt_dy | tv_st, each query x cap) are optional: pass NULL. */
+int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const int* faces_st, float* y4, const float* xs4,
+                       const float* fixed, const float* m_inv, float dHat, float compliance, int cap,
+                       const int* vt_st_cand, const int* vt_st_num, const int* vt_dy_cand, const int* vt_dy_num,
+                       const int* tv_st_cand, const int* tv_st_num, long long* dx_fix, int* nc, int* pair,
+                       float* pair_g, float* pair_schur, int* pair_num, int* status, void* stream);
+
+/* ---- constraint-graph colouring (framework/utilities/graph_coloring.py) --- */
+
+/* initAdjEdges + colorEdgesGreedy + colorCountingSort, graph_coloring.py:112-201:
+ * colour = first-fit over edges in id order (edges sharing a vertex are
+ * adjacent; all max_colors forbidden -> 0), computed in parallel rounds in
+ * which an edge is coloured once all its lower-id neighbours are; then a
+ * stable sort by colour.  prefix[max_colors] = start offset of each colour.
+ * Synchronises `stream` (it polls the number of uncoloured edges). */
+size_t sx_color_workspace_bytes(int n_verts, int n_edges);
+int sx_color_edges_greedy(const int* edges, int n_edges, int n_verts, int max_colors, int* color, int* sorted_edges,
+                          int* prefix, void* ws, size_t ws_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* STARXPBD_H */

@@ -1,0 +1,929 @@
+// CPU restatement of the reference XPBD cloth substep -- TEST INFRASTRUCTURE ONLY.
+//
+// This library is the correctness oracle and the timed CPU baseline.  It is
+// loaded only by tests/, by __graft_entry__.smoke() and by bench.py's CPU
+// baseline leg; the product path (the CUDA library) never calls it.
+//
+// Parity status: the reference (Python + Taichi 1.7.1) cannot run in this
+// environment, so nothing here is checked against reference outputs.  Each
+// function below restates the reference file:line it follows, and is pinned
+// against known-answer tests and brute-force checks in tests/ (parity against
+// the reference itself is "unpinned").
+//
+// Numeric conventions shared with the CUDA kernels (documented, not taken from
+// the reference, whose Taichi build uses float atomics and fast math):
+//   * IEEE float32, no FMA contraction (compile with -ffp-contract=off),
+//     correctly rounded sqrt and division;
+//   * spring/bending accumulation in ascending constraint index per vertex
+//     (= a serial execution of the reference loop);
+//   * contact corrections accumulated in 64-bit fixed point with 40 fractional
+//     bits (order independent, so the serial and parallel orders agree);
+//   * float -> int conversions truncate toward zero and saturate; NaN -> 0.
+//
+// nthreads > 1 runs the loops with OpenMP the way the reference's Taichi
+// ti.cpu backend would: parallel loops, float atomics for the spring
+// accumulation (so the spring result is then order dependent) -- used only for
+// timing.
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define API extern "C" __attribute__((visibility("default")))
+
+namespace {
+
+struct V3 {
+    float x, y, z;
+};
+inline V3 v3(const float* p) { return V3{p[0], p[1], p[2]}; }
+inline V3 sub(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3 add(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline V3 scale(float s, V3 a) { return V3{s * a.x, s * a.y, s * a.z}; }
+inline V3 neg(V3 a) { return V3{-a.x, -a.y, -a.z}; }
+inline float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+inline V3 cross(V3 a, V3 b) {
+    return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+inline V3 vmin(V3 a, V3 b) { return V3{std::min(a.x, b.x), std::min(a.y, b.y), std::min(a.z, b.z)}; }
+inline V3 vmax(V3 a, V3 b) { return V3{std::max(a.x, b.x), std::max(a.y, b.y), std::max(a.z, b.z)}; }
+
+// float -> int32, truncation toward zero, saturating, NaN -> 0
+inline int32_t f2i_sat(float f) {
+    if (f != f) return 0;
+    if (f >= 2147483648.0f) return INT32_MAX;
+    if (f <= -2147483648.0f) return INT32_MIN;
+    return (int32_t)f;
+}
+
+// contact fixed point: 40 fractional bits, saturating at +-2^62
+constexpr double kFixScale = 1099511627776.0;        // 2^40
+constexpr double kFixInv = 1.0 / 1099511627776.0;    // 2^-40
+constexpr double kFixMax = 4611686018427387904.0;    // 2^62
+inline int64_t to_fix(float c, int* bad) {
+    double d = (double)c * kFixScale;
+    if (d != d) { *bad = 1; return 0; }
+    if (d >= kFixMax) { *bad = 1; return (int64_t)4611686018427387904LL; }
+    if (d <= -kFixMax) { *bad = 1; return -(int64_t)4611686018427387904LL; }
+    return (int64_t)std::nearbyint(d);
+}
+inline float from_fix(int64_t a) { return (float)((double)a * kFixInv); }
+
+inline void atomic_addf(float* p, float v, bool par) {
+    if (par) {
+#pragma omp atomic
+        *p += v;
+    } else {
+        *p += v;
+    }
+}
+
+int set_threads(int nthreads) {
+#ifdef _OPENMP
+    if (nthreads > 0) omp_set_num_threads(nthreads);
+    return nthreads > 1;
+#else
+    (void)nthreads;
+    return 0;
+#endif
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// cloth state kernels  (framework/physics/XPBD.py)
+// ---------------------------------------------------------------------------
+
+// XPBD.py:116-118 compute_y: y = x + fixed*v*dt + g*dt*dt ; y.w = x.w
+API int or_predict(int V, const float* x4, const float* v4, const float* fixed, float* y4,
+                   float dt, float gx, float gy, float gz, int nthreads) {
+    int par = set_threads(nthreads);
+    const float g[3] = {gx, gy, gz};
+#pragma omp parallel for if (par)
+    for (int i = 0; i < V; ++i) {
+        for (int k = 0; k < 3; ++k)
+            y4[4 * i + k] = (x4[4 * i + k] + (fixed[i] * v4[4 * i + k]) * dt) + (g[k] * dt) * dt;
+        y4[4 * i + 3] = x4[4 * i + 3];
+    }
+    return 0;
+}
+
+// XPBD.py:141-184 solve_spring_constraints_x + XPBD.py:384-387 update_dx, with
+// XPBD.py:345-348 init_variables in front.  Springs read y; bending pairs read x
+// as in the reference (XPBD.py:169) when bend_on_y == 0, or the current y when
+// bend_on_y == 1 (iterated Jacobi: every sweep evaluates all constraints on the
+// current iterate).  k_spring / k_bend are the two "compliance" arguments
+// (stiffness * dt^2) already assigned to their constraint types.
+// dx3 (3V floats) and nc (V floats) are scratch.
+API int or_spring_sweep(int V, int E, int B, const float* x4, float* y4, const float* fixed,
+                        const float* m_inv, const int* edges, const float* l0, const int* bend,
+                        const float* bend_l0, float k_spring, float k_bend, int bend_on_y, float* dx3, float* nc,
+                        int nthreads) {
+    int par = set_threads(nthreads);
+    std::memset(dx3, 0, sizeof(float) * 3 * (size_t)V);
+    std::memset(nc, 0, sizeof(float) * (size_t)V);
+#pragma omp parallel for if (par)
+    for (int i = 0; i < E + B; ++i) {
+        int v0, v1;
+        float rest, k;
+        const float* P;
+        if (i < E) {
+            v0 = edges[2 * i];
+            v1 = edges[2 * i + 1];
+            rest = l0[i];
+            k = k_spring;
+            P = y4;
+        } else {
+            int b = i - E;
+            v0 = bend[2 * b];
+            v1 = bend[2 * b + 1];
+            rest = bend_l0[b];
+            k = k_bend;
+            P = bend_on_y ? y4 : x4;
+        }
+        V3 x10 = sub(v3(P + 4 * v0), v3(P + 4 * v1));
+        float lij = std::sqrt(dot(x10, x10));
+        float C = lij - rest;
+        float inv = 1.0f / lij;
+        V3 n = scale(inv, x10);
+        float w0 = fixed[v0] * m_inv[v0];
+        float w1 = fixed[v1] * m_inv[v1];
+        float schur = (w0 + w1) * dot(n, n);
+        float ld = (k * C) / (k * schur + 1.0f);
+        float a0 = w0 * ld, a1 = w1 * ld;
+        atomic_addf(&dx3[3 * v0 + 0], -(a0 * n.x), par);
+        atomic_addf(&dx3[3 * v0 + 1], -(a0 * n.y), par);
+        atomic_addf(&dx3[3 * v0 + 2], -(a0 * n.z), par);
+        atomic_addf(&dx3[3 * v1 + 0], a1 * n.x, par);
+        atomic_addf(&dx3[3 * v1 + 1], a1 * n.y, par);
+        atomic_addf(&dx3[3 * v1 + 2], a1 * n.z, par);
+        atomic_addf(&nc[v0], 1.0f, par);
+        atomic_addf(&nc[v1], 1.0f, par);
+    }
+#pragma omp parallel for if (par)
+    for (int v = 0; v < V; ++v) {
+        if (nc[v] > 0.0f) {
+            for (int k = 0; k < 3; ++k) y4[4 * v + k] = y4[4 * v + k] + fixed[v] * (dx3[3 * v + k] / nc[v]);
+        }
+    }
+    return 0;
+}
+
+// XPBD.py:341-343 compute_velocity then XPBD.py:333-337 update_x
+API int or_velocity_update(int V, float* x4, const float* y4, float* v4, const float* fixed,
+                           float damping, float dt, int nthreads) {
+    int par = set_threads(nthreads);
+    float s0 = 1.0f - damping;
+#pragma omp parallel for if (par)
+    for (int i = 0; i < V; ++i) {
+        float s = s0 * fixed[i];
+        for (int k = 0; k < 3; ++k) {
+            float vel = (s * (y4[4 * i + k] - x4[4 * i + k])) / dt;
+            v4[4 * i + k] = vel;
+            x4[4 * i + k] = x4[4 * i + k] + dt * vel;
+        }
+    }
+    return 0;
+}
+
+// meshTaichiWrapper.py:351-365 computeAABB_faces on a position array P (x4 layout)
+API int or_face_aabbs(int F, const float* P4, const int* faces, float padding, float* mn4, float* mx4) {
+    for (int f = 0; f < F; ++f) {
+        V3 a = v3(P4 + 4 * faces[3 * f]), b = v3(P4 + 4 * faces[3 * f + 1]), c = v3(P4 + 4 * faces[3 * f + 2]);
+        V3 lo = vmin(vmin(a, b), c), hi = vmax(vmax(a, b), c);
+        mn4[4 * f + 0] = lo.x - padding; mn4[4 * f + 1] = lo.y - padding; mn4[4 * f + 2] = lo.z - padding; mn4[4 * f + 3] = 0.f;
+        mx4[4 * f + 0] = hi.x + padding; mx4[4 * f + 1] = hi.y + padding; mx4[4 * f + 2] = hi.z + padding; mx4[4 * f + 3] = 0.f;
+    }
+    return 0;
+}
+
+// meshTaichiWrapper.py:335-347 computeAABB -> out6 = (min xyz, max xyz)
+API int or_scene_aabb(int V, const float* P4, float padding, float* out6) {
+    V3 lo{1e5f, 1e5f, 1e5f}, hi{-1e5f, -1e5f, -1e5f};
+    for (int i = 0; i < V; ++i) {
+        V3 p = v3(P4 + 4 * i);
+        lo = vmin(lo, p);
+        hi = vmax(hi, p);
+    }
+    out6[0] = lo.x - padding; out6[1] = lo.y - padding; out6[2] = lo.z - padding;
+    out6[3] = hi.x + padding; out6[4] = hi.y + padding; out6[5] = hi.z + padding;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Morton codes, radix sort, Karras hierarchy  (framework/collision/lbvh_cell.py)
+// ---------------------------------------------------------------------------
+namespace {
+// lbvh_cell.py:87-92
+inline uint64_t expand_bits(uint64_t v) {
+    v = (v | (v << 16)) & 0x030000FFull;
+    v = (v | (v << 8)) & 0x0300F00Full;
+    v = (v | (v << 4)) & 0x030C30C3ull;
+    v = (v | (v << 2)) & 0x09249249ull;
+    return v;
+}
+inline float clampf(float v, float lo, float hi) { return std::min(std::max(v, lo), hi); }
+// lbvh_cell.py:95-102 (input already normalised and clamped to [0,1])
+inline int32_t morton3d(float x, float y, float z) {
+    x = clampf(x * 1024.0f, 0.0f, 1023.0f);
+    y = clampf(y * 1024.0f, 0.0f, 1023.0f);
+    z = clampf(z * 1024.0f, 0.0f, 1023.0f);
+    uint64_t xx = expand_bits((uint64_t)x), yy = expand_bits((uint64_t)y), zz = expand_bits((uint64_t)z);
+    return (int32_t)(uint32_t)(xx | (yy << 1) | (zz << 2));
+}
+// lbvh_cell.py:139-148: normalise a point by the box, clamp, encode
+inline int32_t morton_of(V3 p, V3 lo, V3 hi) {
+    float x = (p.x - lo.x) / (hi.x - lo.x);
+    float y = (p.y - lo.y) / (hi.y - lo.y);
+    float z = (p.z - lo.z) / (hi.z - lo.z);
+    return morton3d(clampf(x, 0.f, 1.f), clampf(y, 0.f, 1.f), clampf(z, 0.f, 1.f));
+}
+inline int clz32(uint32_t v) { return v == 0 ? 32 : __builtin_clz(v); }
+}  // namespace
+
+API int or_morton3d(int n, const float* xyz, int32_t* codes) {
+    for (int i = 0; i < n; ++i) codes[i] = morton3d(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]);
+    return 0;
+}
+
+// Face-centre Morton codes for the face-level LBVH, following the intended form
+// lbvh_cell.py:196-232: centre = 0.5*(aabb_max + aabb_min), normalised by the
+// scene box, clamped, encoded.  ids[i] = i.
+API int or_face_morton(int F, const float* mn4, const float* mx4, const float* box6, int32_t* codes, int32_t* ids) {
+    V3 lo{box6[0], box6[1], box6[2]}, hi{box6[3], box6[4], box6[5]};
+    for (int f = 0; f < F; ++f) {
+        V3 c = scale(0.5f, add(v3(mx4 + 4 * f), v3(mn4 + 4 * f)));
+        codes[f] = morton_of(c, lo, hi);
+        ids[f] = f;
+    }
+    return 0;
+}
+
+// lbvh_cell.py:525-562: LSD radix sort, 6-bit digits, atomic histogram,
+// inclusive scan, serialized back-to-front scatter.  Sorts (keys, vals) in place
+// over the low `bits` key bits (keys treated as unsigned).
+API int or_radix_sort(int n, uint32_t* keys, int32_t* vals, int bits) {
+    const int BPP = 6, R = 1 << BPP;
+    int passes = (bits + BPP - 1) / BPP;
+    std::vector<uint32_t> k2(n);
+    std::vector<int32_t> v2(n);
+    for (int p = 0; p < passes; ++p) {
+        int ps[R] = {0};
+        for (int i = 0; i < n; ++i) ps[(keys[i] >> (p * BPP)) & (R - 1)] += 1;
+        for (int d = 1; d < R; ++d) ps[d] += ps[d - 1];
+        for (int i = 0; i < n; ++i) {
+            int I = n - 1 - i;
+            int d = (keys[I] >> (p * BPP)) & (R - 1);
+            int idx = ps[d] - 1;
+            k2[idx] = keys[I];
+            v2[idx] = vals[I];
+            ps[d] -= 1;
+        }
+        std::memcpy(keys, k2.data(), sizeof(uint32_t) * n);
+        std::memcpy(vals, v2.data(), sizeof(int32_t) * n);
+    }
+    return 0;
+}
+
+namespace {
+// lbvh_cell.py:256-264 delta.  tie==1 adds the index tie-break of Karras 2012
+// (equal codes compare by index), which the reference does not have.
+inline int kdelta(int i, int j, int n, const int32_t* c, int tie) {
+    if (j > n - 1 || j < 0) return -1;
+    uint32_t x = (uint32_t)(c[i] ^ c[j]);
+    if (x == 0) return tie ? 32 + clz32((uint32_t)(i ^ j)) : 32;
+    return clz32(x);
+}
+// lbvh_cell.py:273-298 find_split
+inline int find_split(int l, int r, const int32_t* c, int n, int tie) {
+    int32_t first = c[l], last = c[r];
+    if (first == last && !tie) return (l + r) / 2;
+    int common = kdelta(l, r, n, c, tie);
+    int split = l, step = r - l;
+    while (step > 1) {
+        step = (step + 1) / 2;
+        int ns = split + step;
+        if (ns < r) {
+            if (kdelta(l, ns, n, c, tie) > common) split = ns;
+        }
+    }
+    return split;
+}
+// lbvh_cell.py:302-336 determine_range (note the exponential step l_max <<= 2)
+inline void determine_range(int i, int n, const int32_t* c, int tie, int* start, int* end) {
+    int dl = kdelta(i, i - 1, n, c, tie), dr = kdelta(i, i + 1, n, c, tie);
+    int d = 1, dmin = dl;
+    if (dr < dl) { d = -1; dmin = dr; }
+    int64_t lmax = 2;
+    while (lmax < (int64_t)4 * n) {
+        int64_t j = i + lmax * d;
+        if (j < INT32_MIN || j > INT32_MAX) break;
+        if (kdelta(i, (int)j, n, c, tie) > dmin) lmax <<= 2; else break;
+    }
+    int64_t l = 0, t = lmax / 2;
+    while (t > 0) {
+        int64_t j = i + (l + t) * d;
+        int dd = -1;
+        if (j >= 0 && j < n) dd = kdelta(i, (int)j, n, c, tie);
+        if (dd > dmin) l += t;
+        t /= 2;
+    }
+    *start = i; *end = (int)(i + l * d);
+    if (d == -1) { *start = (int)(i + l * d); *end = i; }
+}
+}  // namespace
+
+// lbvh_cell.py:384-430 assign_internal_nodes_Karras12(_cells).  Writes, for
+// internal node i in [0, n-1): child_a, child_b, range_l, range_r; parent[] for
+// all 2n-1 nodes is written in node order (the last writer wins, as a serial run
+// of the reference would leave it); parent[0] = -1 here.
+API int or_karras(int n, const int32_t* codes, int tie, int32_t* child_a, int32_t* child_b,
+                  int32_t* range_l, int32_t* range_r, int32_t* parent) {
+    for (int i = 0; i < 2 * n - 1; ++i) parent[i] = -1;
+    for (int i = 0; i < n - 1; ++i) {
+        int s, e;
+        determine_range(i, n, codes, tie, &s, &e);
+        int split = find_split(s, e, codes, n, tie);
+        int left = split;
+        if (split == s) left += n - 1;
+        int right = split + 1;
+        if (right == e) right += n - 1;
+        child_a[i] = left; child_b[i] = right;
+        range_l[i] = s; range_r[i] = e;
+        parent[left] = i; parent[right] = i;
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Cell-grid LBVH (LBVH_CELL, lbvh_cell.py:16-714)
+// Node arrays cover 2n-1 nodes: internal 0..n-2, leaves n-1..2n-2.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int GR = 32;
+constexpr int NC = GR * GR * GR;
+inline V3 cell_size_of(const float* box6) {
+    return V3{(box6[3] - box6[0]) / (float)GR, (box6[4] - box6[1]) / (float)GR, (box6[5] - box6[2]) / (float)GR};
+}
+inline V3 cell_center(int i, V3 cs, V3 lo) {
+    int x0 = i / (GR * GR), y0 = (i % (GR * GR)) / GR, z0 = i % GR;
+    V3 p{cs.x * (float)x0 + 0.5f * cs.x, cs.y * (float)y0 + 0.5f * cs.y, cs.z * (float)z0 + 0.5f * cs.z};
+    return add(p, lo);
+}
+// lbvh_cell.py:565-574 (truncating float->int cast, then x*1024 + y*32 + z in
+// wrapping int32 arithmetic)
+inline int32_t flat_cell(V3 pos, V3 cs, V3 org) {
+    int32_t ix = f2i_sat((pos.x - org.x) / cs.x);
+    int32_t iy = f2i_sat((pos.y - org.y) / cs.y);
+    int32_t iz = f2i_sat((pos.z - org.z) / cs.z);
+    uint32_t r = (uint32_t)ix * (uint32_t)(GR * GR) + (uint32_t)iy * (uint32_t)GR + (uint32_t)iz;
+    return (int32_t)r;
+}
+inline bool overlap(V3 a0, V3 a1, V3 b0, V3 b1) {
+    return a0.x <= b1.x && a1.x >= b0.x && a0.y <= b1.y && a1.y >= b0.y && a0.z <= b1.z && a1.z >= b0.z;
+}
+}  // namespace
+
+// LBVH_CELL.__init__ (lbvh_cell.py:78-80): cell Morton codes over the box
+// (0,0,0)-(1e3,1e3,1e3), 6-bit radix sort, Karras build.  Outputs the sorted
+// codes and ids and the internal-node topology.
+API int or_cell_bvh_init(int32_t* sorted_codes, int32_t* sorted_ids, int32_t* child_a, int32_t* child_b,
+                         int32_t* range_l, int32_t* range_r, int32_t* parent) {
+    float box[6] = {0.f, 0.f, 0.f, 1e3f, 1e3f, 1e3f};
+    V3 lo{0.f, 0.f, 0.f}, hi{1e3f, 1e3f, 1e3f};
+    V3 cs = cell_size_of(box);
+    std::vector<uint32_t> k(NC);
+    for (int i = 0; i < NC; ++i) {
+        V3 p = cell_center(i, cs, lo);
+        k[i] = (uint32_t)morton_of(p, lo, hi);
+        sorted_ids[i] = i;
+    }
+    or_radix_sort(NC, k.data(), sorted_ids, 30);
+    for (int i = 0; i < NC; ++i) sorted_codes[i] = (int32_t)k[i];
+    return or_karras(NC, sorted_codes, 0, child_a, child_b, range_l, range_r, parent);
+}
+
+// LBVH_CELL.build (lbvh_cell.py:637-653) for one mesh whose face AABBs are given.
+// In:  topology from or_cell_bvh_init; face AABBs mn4/mx4 (F); box6 = scene AABB.
+// Out: sorted_face_ids[F], prefix[NC] (inclusive), node num_faces/aabb for 2n-1
+//      nodes (nmin4/nmax4 float4 each), cell_size3.
+// Faces whose centre cell coordinate falls outside [0,32) are clamped into the
+// grid (the reference would index out of bounds there).
+API int or_cell_bvh_build(int F, const float* mn4, const float* mx4, const float* box6, const int32_t* child_a,
+                          const int32_t* child_b, const int32_t* parent, int32_t* sorted_face_ids, int32_t* prefix,
+                          int32_t* num_faces, float* nmin4, float* nmax4, float* cell_size3) {
+    V3 lo{box6[0], box6[1], box6[2]};
+    V3 cs = cell_size_of(box6);
+    cell_size3[0] = cs.x; cell_size3[1] = cs.y; cell_size3[2] = cs.z;
+    std::vector<int32_t> fcell(F);
+    std::fill(prefix, prefix + NC, 0);
+    for (int f = 0; f < F; ++f) {  // assign_face_cell_ids :577-586
+        V3 c = scale(0.5f, add(v3(mn4 + 4 * f), v3(mx4 + 4 * f)));
+        int ix = std::min(std::max(f2i_sat((c.x - lo.x) / cs.x), 0), GR - 1);
+        int iy = std::min(std::max(f2i_sat((c.y - lo.y) / cs.y), 0), GR - 1);
+        int iz = std::min(std::max(f2i_sat((c.z - lo.z) / cs.z), 0), GR - 1);
+        int cell = ix * GR * GR + iy * GR + iz;
+        fcell[f] = cell;
+        prefix[cell] += 1;
+    }
+    for (int i = 1; i < NC; ++i) prefix[i] += prefix[i - 1];  // PrefixSumExecutor (inclusive)
+    std::vector<int32_t> tmp(prefix, prefix + NC);
+    for (int fid = 0; fid < F; ++fid) {  // counting_sort_cells :589-598, serial order
+        int I = F - 1 - fid;
+        int idx = --tmp[fcell[I]];
+        sorted_face_ids[idx] = I;
+    }
+    const int N = 2 * NC - 1;
+    std::vector<int32_t> visited(N, 0);
+    std::fill(num_faces, num_faces + N, 0);
+    for (int i = 0; i < NC; ++i) {  // assign_leaf_cell_nodes :602-634
+        int leaf = i + NC - 1;
+        int rl = i == 0 ? 0 : prefix[i - 1];
+        int rr = prefix[i] - 1;
+        int size = rr - rl + 1;
+        V3 c = cell_center(i, cs, lo);
+        V3 a = c, b = c;
+        num_faces[leaf] = size;
+        for (int j = 0; j < size; ++j) {
+            int fid = sorted_face_ids[j + rl];
+            a = vmin(a, v3(mn4 + 4 * fid));
+            b = vmax(b, v3(mx4 + 4 * fid));
+        }
+        nmin4[4 * leaf] = a.x; nmin4[4 * leaf + 1] = a.y; nmin4[4 * leaf + 2] = a.z; nmin4[4 * leaf + 3] = 0.f;
+        nmax4[4 * leaf] = b.x; nmax4[4 * leaf + 1] = b.y; nmax4[4 * leaf + 2] = b.z; nmax4[4 * leaf + 3] = 0.f;
+        visited[parent[leaf]] += 1;
+    }
+    for (;;) {  // compute_bvh_aabbs_cells :481-522
+        int cnt = 0;
+        for (int i = 0; i < NC - 1; ++i) {
+            if (visited[i] != 2) continue;
+            int l = child_a[i], r = child_b[i];
+            V3 min0 = v3(nmin4 + 4 * l), min1 = v3(nmin4 + 4 * r), max0 = v3(nmax4 + 4 * l), max1 = v3(nmax4 + 4 * r);
+            num_faces[i] = num_faces[l] + num_faces[r];
+            V3 a, b;
+            if (num_faces[l] > 0 && num_faces[r] > 0) { a = vmin(min0, min1); b = vmax(max0, max1); }
+            else if (num_faces[l] > 0) { a = min0; b = max0; }
+            else if (num_faces[r] > 0) { a = min1; b = max1; }
+            else { a = scale(0.25f, add(add(add(min0, max0), min1), max1)); b = a; }
+            nmin4[4 * i] = a.x; nmin4[4 * i + 1] = a.y; nmin4[4 * i + 2] = a.z; nmin4[4 * i + 3] = 0.f;
+            nmax4[4 * i] = b.x; nmax4[4 * i + 1] = b.y; nmax4[4 * i + 2] = b.z; nmax4[4 * i + 3] = 0.f;
+            int p = parent[i];
+            visited[i] += 1;
+            if (p >= 0) visited[p] += 1;
+            cnt += 1;
+        }
+        if (cnt == 0) break;
+    }
+    return 0;
+}
+
+// traverse_cell_bvh_single (lbvh_cell.py:662-714) for Q queries with AABBs
+// qmin4/qmax4.  Candidates go to cand[q*cap + j] for j < cap; num[q] counts all
+// overlaps (num > cap marks a truncated list).  Stack depth 64; a push beyond it
+// sets *status |= 2 and drops the node.
+API int or_cell_bvh_traverse(int Q, const float* qmin4, const float* qmax4, const float* cell_size3,
+                             const float* origin3, const int32_t* child_a, const int32_t* child_b,
+                             const int32_t* num_faces, const float* nmin4, const float* nmax4,
+                             const int32_t* prefix, const int32_t* sorted_face_ids, const float* fmn4,
+                             const float* fmx4, int cap, int32_t* cand, int32_t* num, int32_t* status) {
+    V3 cs{cell_size3[0], cell_size3[1], cell_size3[2]}, org{origin3[0], origin3[1], origin3[2]};
+    for (int q = 0; q < Q; ++q) {
+        V3 a = v3(qmin4 + 4 * q), b = v3(qmax4 + 4 * q);
+        num[q] = 0;
+        V3 pos = scale(0.5f, add(a, b));
+        int32_t cid = flat_cell(pos, cs, org);
+        if (cid > NC - 1) continue;
+        int stack[64];
+        int sc = 0;
+        stack[sc++] = 0;
+        long long pops = 0;
+        while (sc > 0) {
+            if (++pops > 2LL * NC) { *status |= 2; break; }
+            int idx = stack[--sc];
+            if (num_faces[idx] <= 0) continue;
+            if (!overlap(a, b, v3(nmin4 + 4 * idx), v3(nmax4 + 4 * idx))) continue;
+            if (idx >= NC - 1) {
+                int i = idx - (NC - 1);
+                int rl = i == 0 ? 0 : prefix[i - 1];
+                int size = prefix[i] - rl;
+                for (int j = 0; j < size; ++j) {
+                    int fid = sorted_face_ids[j + rl];
+                    if (overlap(a, b, v3(fmn4 + 4 * fid), v3(fmx4 + 4 * fid))) {
+                        if (num[q] < cap) cand[(size_t)q * cap + num[q]] = fid;
+                        num[q] += 1;
+                    }
+                }
+            } else {
+                int l = child_a[idx], r = child_b[idx];
+                if (num_faces[l] > 0) { if (sc < 64) stack[sc++] = l; else *status |= 2; }
+                if (num_faces[r] > 0) { if (sc < 64) stack[sc++] = r; else *status |= 2; }
+            }
+        }
+        if (num[q] > cap) *status |= 1;
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Face-level LBVH (standalone broad phase)
+// ---------------------------------------------------------------------------
+// Leaves hold one face each (leaf n-1+j = sorted face j); refit with the
+// compute_cell_node_aabbs rules (lbvh_cell.py:491-522), every leaf holding one
+// face, so each internal box is the union of its children.  Bottom-up by
+// repeated passes like the reference; nodes never reached stay untouched.
+API int or_face_bvh_refit(int n, const int32_t* sorted_ids, const float* fmn4, const float* fmx4,
+                          const int32_t* child_a, const int32_t* child_b, const int32_t* parent, float* nmin4,
+                          float* nmax4) {
+    const int N = 2 * n - 1;
+    std::vector<int32_t> visited(N, 0);
+    for (int j = 0; j < n; ++j) {
+        int leaf = n - 1 + j, f = sorted_ids[j];
+        std::memcpy(nmin4 + 4 * leaf, fmn4 + 4 * f, 16);
+        std::memcpy(nmax4 + 4 * leaf, fmx4 + 4 * f, 16);
+        if (parent[leaf] >= 0) visited[parent[leaf]] += 1;
+    }
+    for (;;) {
+        int cnt = 0;
+        for (int i = 0; i < n - 1; ++i) {
+            if (visited[i] != 2) continue;
+            int l = child_a[i], r = child_b[i];
+            V3 a = vmin(v3(nmin4 + 4 * l), v3(nmin4 + 4 * r)), b = vmax(v3(nmax4 + 4 * l), v3(nmax4 + 4 * r));
+            nmin4[4 * i] = a.x; nmin4[4 * i + 1] = a.y; nmin4[4 * i + 2] = a.z; nmin4[4 * i + 3] = 0.f;
+            nmax4[4 * i] = b.x; nmax4[4 * i + 1] = b.y; nmax4[4 * i + 2] = b.z; nmax4[4 * i + 3] = 0.f;
+            visited[i] += 1;
+            if (parent[i] >= 0) visited[parent[i]] += 1;
+            cnt += 1;
+        }
+        if (cnt == 0) break;
+    }
+    return 0;
+}
+
+// Stack traversal of the face-level LBVH (same visiting order as
+// traverse_cell_bvh_single: pop, test, push child_a then child_b).
+API int or_face_bvh_traverse(int n, int Q, const float* qmin4, const float* qmax4, const int32_t* child_a,
+                             const int32_t* child_b, const int32_t* sorted_ids, const float* nmin4,
+                             const float* nmax4, int cap, int32_t* cand, int32_t* num, int32_t* status) {
+    for (int q = 0; q < Q; ++q) {
+        V3 a = v3(qmin4 + 4 * q), b = v3(qmax4 + 4 * q);
+        num[q] = 0;
+        int stack[64];
+        int sc = 0;
+        stack[sc++] = 0;
+        if (n == 1) stack[0] = 0;
+        long long pops = 0;
+        while (sc > 0) {
+            if (++pops > 2LL * n) { *status |= 2; break; }
+            int idx = stack[--sc];
+            if (!overlap(a, b, v3(nmin4 + 4 * idx), v3(nmax4 + 4 * idx))) continue;
+            if (idx >= n - 1) {
+                int fid = sorted_ids[idx - (n - 1)];
+                if (num[q] < cap) cand[(size_t)q * cap + num[q]] = fid;
+                num[q] += 1;
+            } else {
+                int l = child_a[idx], r = child_b[idx];
+                if (sc < 64) stack[sc++] = l; else *status |= 2;
+                if (sc < 64) stack[sc++] = r; else *status |= 2;
+            }
+        }
+        if (num[q] > cap) *status |= 1;
+    }
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Narrow phase  (framework/collision/distance.py,
+//                framework/physics/collision_constraints_x.py)
+// ---------------------------------------------------------------------------
+namespace {
+// distance.py:5-47 d_type_PT: region of the closest feature of triangle
+// (v1,v2,v3) to v0, via three 2x2 solves A^{-1} b with
+// A^{-1} = (1/det) [[a11, -a01], [-a10, a00]].
+inline void solve2(float a00, float a01, float a10, float a11, float b0, float b1, float* p0, float* p1) {
+    float det = a00 * a11 - a01 * a10;
+    float id = 1.0f / det;
+    float m00 = id * a11, m01 = id * (-a01), m10 = id * (-a10), m11 = id * a00;
+    *p0 = m00 * b0 + m01 * b1;
+    *p1 = m10 * b0 + m11 * b1;
+}
+int d_type_PT(V3 v0, V3 v1, V3 v2, V3 v3) {
+    V3 v12 = sub(v2, v1), v13 = sub(v3, v1);
+    V3 n = cross(v12, v13);
+    V3 v13n = cross(v12, n);
+    V3 v10 = sub(v0, v1);
+    float p00, p01;
+    solve2(dot(v12, v12), dot(v12, v13n), dot(v13n, v12), dot(v13n, v13n), dot(v12, v10), dot(v13n, v10), &p00, &p01);
+    if (p00 > 0.0f && p00 < 1.0f && p01 >= 0.0f) return 3;
+    V3 v32 = sub(v3, v2), v32n = cross(v32, n), v20 = sub(v0, v2);
+    float p10, p11;
+    solve2(dot(v32, v32), dot(v32, v32n), dot(v32n, v32), dot(v32n, v32n), dot(v32, v20), dot(v32n, v20), &p10, &p11);
+    if (p10 > 0.0f && p10 < 1.0f && p11 >= 0.0f) return 4;
+    V3 v31 = sub(v1, v3), v31n = cross(v31, n), v30 = sub(v0, v3);
+    float p20, p21;
+    solve2(dot(v31, v31), dot(v31, v31n), dot(v31n, v31), dot(v31n, v31n), dot(v31, v30), dot(v31n, v30), &p20, &p21);
+    if (p20 > 0.0f && p20 < 1.0f && p21 >= 0.0f) return 5;
+    if (p00 <= 0.0f && p20 >= 1.0f) return 0;
+    if (p10 <= 0.0f && p00 >= 1.0f) return 1;
+    if (p20 <= 0.0f && p10 >= 1.0f) return 2;
+    return 6;
+}
+// squared distances, distance.py:102-116
+inline float d_PP(V3 a, V3 b) { V3 d = sub(a, b); return dot(d, d); }
+inline float d_PE(V3 p, V3 e0, V3 e1) {
+    V3 c = cross(sub(e0, p), sub(e1, p));
+    V3 e = sub(e1, e0);
+    return dot(c, c) / dot(e, e);
+}
+inline float d_PT(V3 p, V3 t0, V3 t1, V3 t2) {
+    V3 b = cross(sub(t1, t0), sub(t2, t0));
+    float s = dot(sub(p, t0), b);
+    return s * s / dot(b, b);
+}
+// Gradients of the squared distances (the quantities of distance.py g_PP :127,
+// g_PE :145-184, g_PT :413-459), written from the closed-form derivatives:
+//  PP: d=|a-b|^2                      g_a = 2(a-b), g_b = -g_a
+//  PE: c=(e0-p)x(e1-p), L=|e1-e0|^2, d=c.c/L
+//      g_e0 = (2 (e1-p)xc + 2 d (e1-e0)) / L
+//      g_e1 = (2 cx(e0-p) - 2 d (e1-e0)) / L,   g_p = -(g_e0 + g_e1)
+//  PT: n=(t1-t0)x(t2-t0), r=p-t0, s=r.n, N=n.n, d=s^2/N
+//      g_p  = 2 s n / N
+//      g_t1 = (2 s (t2-t0)xr - 2 d (t2-t0)xn) / N
+//      g_t2 = (2 s rx(t1-t0) - 2 d nx(t1-t0)) / N,   g_t0 = -(g_p + g_t1 + g_t2)
+inline void g_PP(V3 a, V3 b, V3* ga, V3* gb) {
+    V3 d = sub(a, b);
+    *ga = scale(2.0f, d);
+    *gb = neg(*ga);
+}
+inline void g_PE(V3 p, V3 e0, V3 e1, V3* gp, V3* g0, V3* g1) {
+    V3 a = sub(e0, p), b = sub(e1, p);
+    V3 c = cross(a, b);
+    V3 e = sub(e1, e0);
+    float L = dot(e, e);
+    float iL = 1.0f / L;
+    float d = dot(c, c) * iL;
+    V3 bc = cross(b, c), ca = cross(c, a);
+    float td = 2.0f * d;
+    V3 t0 = add(scale(2.0f, bc), scale(td, e));
+    V3 t1 = sub(scale(2.0f, ca), scale(td, e));
+    *g0 = scale(iL, t0);
+    *g1 = scale(iL, t1);
+    *gp = neg(add(*g0, *g1));
+}
+inline void g_PT(V3 p, V3 t0, V3 t1, V3 t2, V3* gp, V3* g0, V3* g1, V3* g2) {
+    V3 u = sub(t1, t0), w = sub(t2, t0);
+    V3 n = cross(u, w);
+    V3 r = sub(p, t0);
+    float s = dot(r, n);
+    float N = dot(n, n);
+    float iN = 1.0f / N;
+    float d = (s * s) * iN;
+    float ts = 2.0f * s, td = 2.0f * d;
+    *gp = scale(ts * iN, n);
+    V3 a1 = sub(scale(ts, cross(w, r)), scale(td, cross(w, n)));
+    V3 a2 = sub(scale(ts, cross(r, u)), scale(td, cross(n, u)));
+    *g1 = scale(iN, a1);
+    *g2 = scale(iN, a2);
+    *g0 = neg(add(add(*gp, *g1), *g2));
+}
+
+// Evaluate the point-triangle distance by region.  g[0] is the point's gradient,
+// g[1..3] the triangle vertices' (zero where the feature excludes the vertex).
+inline float pt_distance(int dtype, V3 x0, V3 x1, V3 x2, V3 x3, V3 g[4], bool want_grad, float dflt) {
+    float d = dflt;
+    switch (dtype) {
+        case 0: d = d_PP(x0, x1); if (want_grad) g_PP(x0, x1, &g[0], &g[1]); break;
+        case 1: d = d_PP(x0, x2); if (want_grad) g_PP(x0, x2, &g[0], &g[2]); break;
+        case 2: d = d_PP(x0, x3); if (want_grad) g_PP(x0, x3, &g[0], &g[3]); break;
+        case 3: d = d_PE(x0, x1, x2); if (want_grad) g_PE(x0, x1, x2, &g[0], &g[1], &g[2]); break;
+        case 4: d = d_PE(x0, x2, x3); if (want_grad) g_PE(x0, x2, x3, &g[0], &g[2], &g[3]); break;
+        case 5: d = d_PE(x0, x1, x3); if (want_grad) g_PE(x0, x1, x3, &g[0], &g[1], &g[3]); break;
+        case 6: d = d_PT(x0, x1, x2, x3); if (want_grad) g_PT(x0, x1, x2, x3, &g[0], &g[1], &g[2], &g[3]); break;
+        default: break;
+    }
+    return d;
+}
+// vertex mask per region: which of (x0..x3) the feature involves
+inline int region_mask(int dtype) {
+    static const int m[7] = {0x3, 0x5, 0x9, 0x7, 0xD, 0xB, 0xF};
+    return (dtype >= 0 && dtype < 7) ? m[dtype] : 0;
+}
+
+struct Acc {
+    int64_t* dx;  // 3 per vertex
+    int32_t* nc;
+    int* bad;
+    bool par;
+    void add(int v, float a, V3 g) {
+        int64_t c0 = to_fix(a * g.x, bad), c1 = to_fix(a * g.y, bad), c2 = to_fix(a * g.z, bad);
+        if (par) {
+#pragma omp atomic
+            dx[3 * v] += c0;
+#pragma omp atomic
+            dx[3 * v + 1] += c1;
+#pragma omp atomic
+            dx[3 * v + 2] += c2;
+#pragma omp atomic
+            nc[v] += 1;
+        } else {
+            dx[3 * v] += c0; dx[3 * v + 1] += c1; dx[3 * v + 2] += c2; nc[v] += 1;
+        }
+    }
+};
+
+struct Pairs {  // optional pair records: pair[(q*cap+j)*2 + {0,1}] = (face, dtype)
+    int32_t* pair;
+    float* g;       // (q*cap+j)*16 : 4 gradients as float4
+    float* schur;
+    int32_t* num;
+    int cap;
+    void rec(int q, int face, int dtype, const V3 gg[4], float s) {
+        if (!num) return;
+        int j = num[q];
+        if (j >= cap) return;
+        size_t o = (size_t)q * cap + j;
+        pair[2 * o] = face; pair[2 * o + 1] = dtype;
+        for (int k = 0; k < 4; ++k) { g[16 * o + 4 * k] = gg[k].x; g[16 * o + 4 * k + 1] = gg[k].y; g[16 * o + 4 * k + 2] = gg[k].z; g[16 * o + 4 * k + 3] = 0.f; }
+        schur[o] = s;
+        num[q] = j + 1;
+    }
+};
+}  // namespace
+
+// solve_collision_constraints_x (XPBD.py:237-264) -> __vt_st / __vt_dy / __tv_st
+// (collision_constraints_x.py:6-310) with fixed-point accumulation, then
+// update_dx (XPBD.py:384-387) on the dynamic mesh (y4).
+//   dynamic mesh: y4 (positions; .w unused here), fixed, m_inv, faces_dy
+//   static mesh:  xs4 (positions), faces_st
+//   candidates:   vt_st (Vd x cap), vt_dy (Vd x cap), tv_st (Vs x cap), counts
+// Optional pair records (pass NULL to skip): three blocks, same layout.
+API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_t* faces_st, float* y4,
+                           const float* xs4, const float* fixed, const float* m_inv, float dHat, float compliance,
+                           int cap, const int32_t* vt_st_c, const int32_t* vt_st_n, const int32_t* vt_dy_c,
+                           const int32_t* vt_dy_n, const int32_t* tv_st_c, const int32_t* tv_st_n,
+                           int64_t* dx_fix, int32_t* nc, int32_t* pair, float* pair_g, float* pair_schur,
+                           int32_t* pair_num, int32_t* status, int nthreads) {
+    int par = set_threads(nthreads);
+    std::memset(dx_fix, 0, sizeof(int64_t) * 3 * (size_t)Vd);
+    std::memset(nc, 0, sizeof(int32_t) * (size_t)Vd);
+    int bad = 0;
+    Acc acc{dx_fix, nc, &bad, par != 0};
+    Pairs P[3];
+    for (int s = 0; s < 3; ++s) {
+        size_t qoff = s == 2 ? 2 * (size_t)Vd : s * (size_t)Vd;
+        P[s].cap = cap;
+        P[s].num = pair_num ? pair_num + qoff : nullptr;
+        P[s].pair = pair ? pair + 2 * qoff * cap : nullptr;
+        P[s].g = pair_g ? pair_g + 16 * qoff * cap : nullptr;
+        P[s].schur = pair_schur ? pair_schur + qoff * cap : nullptr;
+    }
+    if (pair_num) std::memset(pair_num, 0, sizeof(int32_t) * (2 * (size_t)Vd + Vs));
+    const int total = 2 * Vd + Vs;
+#pragma omp parallel for if (par) schedule(dynamic, 64)
+    for (int i = 0; i < total; ++i) {
+        if (i < Vd) {  // __vt_st: dynamic vertex (y) vs static triangle (x)
+            int vid = i;
+            int n = std::min(vt_st_n[vid], cap);
+            for (int j = 0; j < n; ++j) {
+                int fs = vt_st_c[(size_t)vid * cap + j];
+                V3 x0 = v3(y4 + 4 * vid);
+                V3 x1 = v3(xs4 + 4 * faces_st[3 * fs]), x2 = v3(xs4 + 4 * faces_st[3 * fs + 1]), x3 = v3(xs4 + 4 * faces_st[3 * fs + 2]);
+                V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                int dt = d_type_PT(x0, x1, x2, x3);
+                float d = pt_distance(dt, x0, x1, x2, x3, g, true, dHat);
+                if (d < dHat) {
+                    float schur = m_inv[vid] * dot(g[0], g[0]);
+                    float ld = (compliance * (dHat - d)) / (compliance * schur + 1.0f);
+                    acc.add(vid, m_inv[vid] * ld, g[0]);  // no `fixed` factor (collision_constraints_x.py:58)
+                    P[0].rec(vid, fs, dt, g, schur);
+                }
+            }
+        } else if (i < 2 * Vd) {  // __vt_dy: self collision, incident faces skipped (XPBD.py:121-127)
+            int vid = i - Vd;
+            int n = std::min(vt_dy_n[vid], cap);
+            for (int j = 0; j < n; ++j) {
+                int fd = vt_dy_c[(size_t)vid * cap + j];
+                int a = faces_dy[3 * fd], b = faces_dy[3 * fd + 1], c = faces_dy[3 * fd + 2];
+                if (a == vid || b == vid || c == vid) continue;
+                int vv[4] = {vid, a, b, c};
+                V3 x[4] = {v3(y4 + 4 * vid), v3(y4 + 4 * a), v3(y4 + 4 * b), v3(y4 + 4 * c)};
+                V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                int dt = d_type_PT(x[0], x[1], x[2], x[3]);
+                float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);
+                float schur = 0.0f;
+                if (d < dHat) {
+                    pt_distance(dt, x[0], x[1], x[2], x[3], g, true, dHat);
+                    int m = region_mask(dt);
+                    float s = 0.0f;
+                    bool first = true;
+                    for (int k = 0; k < 4; ++k) {
+                        if (!(m & (1 << k))) continue;
+                        float t = (fixed[vv[k]] * m_inv[vv[k]]) * dot(g[k], g[k]);
+                        s = first ? t : s + t;
+                        first = false;
+                    }
+                    schur = s + 1e-4f;
+                    float ld = (dHat - d) / schur;
+                    for (int k = 0; k < 4; ++k) {
+                        if (!(m & (1 << k))) continue;
+                        // dtype 0 applies m_inv without `fixed` (collision_constraints_x.py:199-200)
+                        float w = dt == 0 ? m_inv[vv[k]] : fixed[vv[k]] * m_inv[vv[k]];
+                        acc.add(vv[k], w * ld, g[k]);
+                    }
+                }
+                P[1].rec(vid, fd, dt, g, schur);
+            }
+        } else {  // __tv_st: static vertex (x) vs dynamic triangle (y)
+            int vis = i - 2 * Vd;
+            int n = std::min(tv_st_n[vis], cap);
+            for (int j = 0; j < n; ++j) {
+                int fd = tv_st_c[(size_t)vis * cap + j];
+                int vv[4] = {-1, faces_dy[3 * fd], faces_dy[3 * fd + 1], faces_dy[3 * fd + 2]};
+                V3 x[4] = {v3(xs4 + 4 * vis), v3(y4 + 4 * vv[1]), v3(y4 + 4 * vv[2]), v3(y4 + 4 * vv[3])};
+                V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                int dt = d_type_PT(x[0], x[1], x[2], x[3]);
+                float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);
+                float schur = 0.0f;
+                if (d < dHat) {
+                    pt_distance(dt, x[0], x[1], x[2], x[3], g, true, dHat);
+                    int m = region_mask(dt) & ~1;
+                    float s = 0.0f;
+                    bool first = true;
+                    for (int k = 1; k < 4; ++k) {
+                        if (!(m & (1 << k))) continue;
+                        float t = (fixed[vv[k]] * m_inv[vv[k]]) * dot(g[k], g[k]);
+                        s = first ? t : s + t;
+                        first = false;
+                    }
+                    schur = s;
+                    float ld = (compliance * (dHat - d)) / (compliance * schur + 1.0f);
+                    for (int k = 1; k < 4; ++k) {
+                        if (!(m & (1 << k))) continue;
+                        acc.add(vv[k], (fixed[vv[k]] * m_inv[vv[k]]) * ld, g[k]);
+                    }
+                }
+                P[2].rec(vis, fd, dt, g, schur);
+            }
+        }
+    }
+    // update_dx on the dynamic mesh
+#pragma omp parallel for if (par)
+    for (int v = 0; v < Vd; ++v) {
+        if (nc[v] > 0) {
+            float c = (float)nc[v];
+            for (int k = 0; k < 3; ++k) y4[4 * v + k] = y4[4 * v + k] + fixed[v] * (from_fix(dx_fix[3 * v + k]) / c);
+        }
+    }
+    if (bad && status) *status |= 4;
+    return 0;
+}
+
+// The region classifier, distance and gradient for one point-triangle query
+// (used by tests: known-answer and finite-difference checks).
+API int or_point_triangle(const float* p12, float* d_out, float* g12) {
+    V3 x0 = v3(p12), x1 = v3(p12 + 3), x2 = v3(p12 + 6), x3 = v3(p12 + 9);
+    V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    int dt = d_type_PT(x0, x1, x2, x3);
+    *d_out = pt_distance(dt, x0, x1, x2, x3, g, true, 0.0f);
+    for (int k = 0; k < 4; ++k) { g12[3 * k] = g[k].x; g12[3 * k + 1] = g[k].y; g12[3 * k + 2] = g[k].z; }
+    return dt;
+}
+
+// ---------------------------------------------------------------------------
+// Graph colouring (framework/utilities/graph_coloring.py)
+// ---------------------------------------------------------------------------
+// initAdjEdges (:112-129) + colorEdgesGreedy (:131-149): sequential first-fit in
+// edge-id order; two edges are adjacent when they share a vertex; the colour is
+// argmax of the 0/1 availability vector over max_colors entries (all forbidden
+// -> colour 0).  colorCountingSort (:172-201): stable counting sort, back to
+// front; prefix[c] = start offset of colour c (E for colours past the last).
+API int or_color_edges(int V, int E, const int32_t* edges, int max_colors, int32_t* color, int32_t* sorted_edges,
+                       int32_t* prefix) {
+    std::vector<std::vector<int>> inc(V);
+    for (int e = 0; e < E; ++e) { inc[edges[2 * e]].push_back(e); inc[edges[2 * e + 1]].push_back(e); }
+    for (int e = 0; e < E; ++e) color[e] = -1;
+    std::vector<char> avail(max_colors);
+    for (int e = 0; e < E; ++e) {
+        std::fill(avail.begin(), avail.end(), 1);
+        for (int s = 0; s < 2; ++s)
+            for (int o : inc[edges[2 * e + s]])
+                if (o != e && color[o] != -1) avail[color[o]] = 0;
+        int c = 0;
+        for (int k = 0; k < max_colors; ++k) if (avail[k]) { c = k; break; }
+        color[e] = c;
+    }
+    std::fill(prefix, prefix + max_colors, 0);
+    for (int e = 0; e < E; ++e) prefix[color[e]] += 1;
+    for (int i = 1; i < max_colors; ++i) prefix[i] += prefix[i - 1];
+    for (int i = E - 1; i >= 0; --i) {
+        int c = color[i];
+        prefix[c] -= 1;
+        sorted_edges[prefix[c]] = i;
+    }
+    return 0;
+}
+
+API int or_version(void) { return 1; }

@@ -1,0 +1,384 @@
+"""numpy front end of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Loaded by tests/, by ``__graft_entry__.smoke()`` and by the CPU-baseline leg of
+``bench.py``; never by the product.  Wraps ``oracle/_build/liboracle.so`` (a CPU
+restatement of the reference algorithms, see oracle.cpp for the file:line each
+function follows) and provides :class:`OracleSolver`, which strings the pieces
+together exactly like ``Solver.forward`` (``framework/physics/XPBD.py:443-469``)
+with the iteration and rebuild options of the GPU solver.
+
+Parity status: unpinned against the reference itself (Taichi is not available);
+pinned by known-answer and brute-force checks in tests/.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+_lib = None
+
+P = C.c_void_p
+I = C.c_int
+F = C.c_float
+
+_SIGS = {
+    "or_predict": [I, P, P, P, P, F, F, F, F, I],
+    "or_spring_sweep": [I, I, I, P, P, P, P, P, P, P, P, F, F, I, P, P, I],
+    "or_velocity_update": [I, P, P, P, P, F, F, I],
+    "or_face_aabbs": [I, P, P, F, P, P],
+    "or_scene_aabb": [I, P, F, P],
+    "or_morton3d": [I, P, P],
+    "or_face_morton": [I, P, P, P, P, P],
+    "or_radix_sort": [I, P, P, I],
+    "or_karras": [I, P, I, P, P, P, P, P],
+    "or_cell_bvh_init": [P, P, P, P, P, P, P],
+    "or_cell_bvh_build": [I, P, P, P, P, P, P, P, P, P, P, P, P],
+    "or_cell_bvh_traverse": [I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, P, P, P],
+    "or_face_bvh_refit": [I, P, P, P, P, P, P, P, P],
+    "or_face_bvh_traverse": [I, I, P, P, P, P, P, P, P, I, P, P, P],
+    "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I],
+    "or_point_triangle": [P, P, P],
+    "or_color_edges": [I, I, P, I, P, P, P],
+    "or_version": [],
+}
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = _build.build_oracle()
+        L = C.CDLL(path)
+        for name, args in _SIGS.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def f32(a, shape=None):
+    a = np.ascontiguousarray(a, dtype=np.float32)
+    return a if shape is None else a.reshape(shape)
+
+
+def i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+NUM_CELLS = 32 * 32 * 32
+
+
+# ---- cloth ------------------------------------------------------------------
+def predict(x4, v4, fixed, dt, g, nthreads=1):
+    y4 = np.empty_like(x4)
+    lib().or_predict(x4.shape[0], _p(x4), _p(v4), _p(fixed), _p(y4), dt, g[0], g[1], g[2], nthreads)
+    return y4
+
+
+def spring_sweep(x4, y4, fixed, m_inv, edges, l0, bend, bl0, k_spring, k_bend, nthreads=1, bend_on_y=0):
+    """One Jacobi sweep; updates y4 in place."""
+    V = x4.shape[0]
+    dx = np.empty(3 * V, np.float32)
+    nc = np.empty(V, np.float32)
+    lib().or_spring_sweep(V, edges.shape[0], bend.shape[0], _p(x4), _p(y4), _p(fixed), _p(m_inv), _p(edges),
+                          _p(l0), _p(bend), _p(bl0), k_spring, k_bend, int(bend_on_y), _p(dx), _p(nc), nthreads)
+    return y4
+
+
+def velocity_update(x4, y4, v4, fixed, damping, dt, nthreads=1):
+    lib().or_velocity_update(x4.shape[0], _p(x4), _p(y4), _p(v4), _p(fixed), damping, dt, nthreads)
+
+
+def face_aabbs(p4, faces, padding):
+    F_ = faces.shape[0]
+    mn = np.empty((F_, 4), np.float32)
+    mx = np.empty((F_, 4), np.float32)
+    lib().or_face_aabbs(F_, _p(p4), _p(i32(faces)), padding, _p(mn), _p(mx))
+    return mn, mx
+
+
+def scene_aabb(p4, padding):
+    out = np.empty(6, np.float32)
+    lib().or_scene_aabb(p4.shape[0], _p(p4), padding, _p(out))
+    return out
+
+
+# ---- LBVH -------------------------------------------------------------------
+def morton3d(xyz):
+    xyz = f32(xyz, (-1, 3))
+    out = np.empty(xyz.shape[0], np.int32)
+    lib().or_morton3d(xyz.shape[0], _p(xyz), _p(out))
+    return out
+
+
+def face_morton(mn4, mx4, box6):
+    n = mn4.shape[0]
+    codes = np.empty(n, np.int32)
+    ids = np.empty(n, np.int32)
+    lib().or_face_morton(n, _p(mn4), _p(mx4), _p(f32(box6)), _p(codes), _p(ids))
+    return codes, ids
+
+
+def radix_sort(keys, vals, bits):
+    k = np.ascontiguousarray(keys, dtype=np.uint32).copy()
+    v = i32(vals).copy()
+    lib().or_radix_sort(k.shape[0], _p(k), _p(v), bits)
+    return k, v
+
+
+def karras(codes, tie=0):
+    codes = i32(codes)
+    n = codes.shape[0]
+    ca = np.zeros(max(n - 1, 1), np.int32)
+    cb = np.zeros_like(ca)
+    rl = np.zeros_like(ca)
+    rr = np.zeros_like(ca)
+    par = np.zeros(2 * n - 1, np.int32)
+    lib().or_karras(n, _p(codes), tie, _p(ca), _p(cb), _p(rl), _p(rr), _p(par))
+    return ca[: n - 1], cb[: n - 1], rl[: n - 1], rr[: n - 1], par
+
+
+class CellBVH:
+    """Oracle of LBVH_CELL (lbvh_cell.py:16-714)."""
+
+    def __init__(self):
+        n = NUM_CELLS
+        self.codes = np.empty(n, np.int32)
+        self.ids = np.empty(n, np.int32)
+        self.child_a = np.empty(n - 1, np.int32)
+        self.child_b = np.empty(n - 1, np.int32)
+        self.range_l = np.empty(n - 1, np.int32)
+        self.range_r = np.empty(n - 1, np.int32)
+        self.parent = np.empty(2 * n - 1, np.int32)
+        lib().or_cell_bvh_init(_p(self.codes), _p(self.ids), _p(self.child_a), _p(self.child_b), _p(self.range_l),
+                               _p(self.range_r), _p(self.parent))
+
+    def build(self, fmn4, fmx4, box6):
+        F_ = fmn4.shape[0]
+        N = 2 * NUM_CELLS - 1
+        self.box6 = f32(box6).copy()
+        self.fmn4, self.fmx4 = fmn4, fmx4
+        self.sorted_face_ids = np.empty(max(F_, 1), np.int32)
+        self.prefix = np.empty(NUM_CELLS, np.int32)
+        self.num_faces = np.empty(N, np.int32)
+        self.nmin4 = np.zeros((N, 4), np.float32)
+        self.nmax4 = np.zeros((N, 4), np.float32)
+        self.cell_size = np.empty(3, np.float32)
+        lib().or_cell_bvh_build(F_, _p(fmn4), _p(fmx4), _p(self.box6), _p(self.child_a), _p(self.child_b),
+                                _p(self.parent), _p(self.sorted_face_ids), _p(self.prefix), _p(self.num_faces),
+                                _p(self.nmin4), _p(self.nmax4), _p(self.cell_size))
+        self.sorted_face_ids = self.sorted_face_ids[:F_]
+
+    def traverse(self, qmin4, qmax4, cap):
+        Q = qmin4.shape[0]
+        cand = np.full((Q, cap), -1, np.int32)
+        num = np.zeros(Q, np.int32)
+        status = np.zeros(1, np.int32)
+        sfi = self.sorted_face_ids if self.sorted_face_ids.size else np.zeros(1, np.int32)
+        lib().or_cell_bvh_traverse(Q, _p(qmin4), _p(qmax4), _p(self.cell_size), _p(self.box6), _p(self.child_a),
+                                   _p(self.child_b), _p(self.num_faces), _p(self.nmin4), _p(self.nmax4),
+                                   _p(self.prefix), _p(sfi), _p(self.fmn4), _p(self.fmx4), cap, _p(cand), _p(num),
+                                   _p(status))
+        return cand, num, int(status[0])
+
+
+def query_boxes(p4, padding):
+    p = f32(p4)[:, :3]
+    pad = np.float32(padding)
+    mn = np.zeros((p.shape[0], 4), np.float32)
+    mx = np.zeros((p.shape[0], 4), np.float32)
+    mn[:, :3] = p - pad
+    mx[:, :3] = p + pad
+    return mn, mx
+
+
+class FaceBVH:
+    """Oracle of the face-level LBVH (Morton -> radix sort -> Karras -> refit)."""
+
+    def __init__(self, fmn4, fmx4, box6, tie=1):
+        n = fmn4.shape[0]
+        self.n = n
+        codes, ids = face_morton(fmn4, fmx4, box6)
+        self.codes_unsorted = codes
+        k, v = radix_sort(codes.view(np.uint32), ids, 32)
+        self.sorted_codes = k.view(np.int32)
+        self.sorted_ids = v
+        self.child_a, self.child_b, self.range_l, self.range_r, self.parent = karras(self.sorted_codes, tie)
+        self.nmin4 = np.zeros((2 * n - 1, 4), np.float32)
+        self.nmax4 = np.zeros((2 * n - 1, 4), np.float32)
+        ca = self.child_a if n > 1 else np.zeros(1, np.int32)
+        cb = self.child_b if n > 1 else np.zeros(1, np.int32)
+        lib().or_face_bvh_refit(n, _p(self.sorted_ids), _p(fmn4), _p(fmx4), _p(ca), _p(cb), _p(self.parent),
+                                _p(self.nmin4), _p(self.nmax4))
+
+    def traverse(self, qmin4, qmax4, cap):
+        Q = qmin4.shape[0]
+        cand = np.full((Q, cap), -1, np.int32)
+        num = np.zeros(Q, np.int32)
+        status = np.zeros(1, np.int32)
+        ca = self.child_a if self.n > 1 else np.zeros(1, np.int32)
+        cb = self.child_b if self.n > 1 else np.zeros(1, np.int32)
+        lib().or_face_bvh_traverse(self.n, Q, _p(qmin4), _p(qmax4), _p(ca), _p(cb), _p(self.sorted_ids),
+                                   _p(self.nmin4), _p(self.nmax4), cap, _p(cand), _p(num), _p(status))
+        return cand, num, int(status[0])
+
+
+# ---- narrow phase -----------------------------------------------------------
+def point_triangle(p, t0, t1, t2):
+    buf = f32(np.concatenate([p, t0, t1, t2]))
+    d = np.zeros(1, np.float32)
+    g = np.zeros(12, np.float32)
+    dt = lib().or_point_triangle(_p(buf), _p(d), _p(g))
+    return dt, float(d[0]), g.reshape(4, 3)
+
+
+def collision_sweep(faces_dy, faces_st, y4, xs4, fixed, m_inv, dHat, compliance, cap, vt_st, vt_dy, tv_st,
+                    want_pairs=False, nthreads=1):
+    """Narrow phase + update_dx; updates y4 in place.  vt_st etc. = (cand, num)."""
+    Vd = y4.shape[0]
+    Vs = xs4.shape[0] if xs4 is not None else 0
+    dx = np.zeros(3 * Vd, np.int64)
+    nc = np.zeros(Vd, np.int32)
+    status = np.zeros(1, np.int32)
+    pair = pair_g = pair_schur = pair_num = None
+    if want_pairs:
+        Q = 2 * Vd + Vs
+        pair = np.zeros((Q, cap, 2), np.int32)
+        pair_g = np.zeros((Q, cap, 4, 4), np.float32)
+        pair_schur = np.zeros((Q, cap), np.float32)
+        pair_num = np.zeros(Q, np.int32)
+    fs = i32(faces_st) if faces_st is not None else np.zeros(3, np.int32)
+    xs = xs4 if xs4 is not None else np.zeros((1, 4), np.float32)
+    lib().or_collision_sweep(Vd, Vs, _p(i32(faces_dy)), _p(fs), _p(y4), _p(xs), _p(fixed), _p(m_inv), dHat,
+                             compliance, cap, _p(vt_st[0]), _p(vt_st[1]), _p(vt_dy[0]), _p(vt_dy[1]),
+                             _p(tv_st[0]), _p(tv_st[1]), _p(dx), _p(nc), _p(pair), _p(pair_g), _p(pair_schur),
+                             _p(pair_num), _p(status), nthreads)
+    out = {"status": int(status[0])}
+    if want_pairs:
+        out.update(pair=pair, pair_g=pair_g, pair_schur=pair_schur, pair_num=pair_num)
+    return out
+
+
+# ---- colouring --------------------------------------------------------------
+def color_edges(n_verts, edges, max_colors=100):
+    edges = i32(edges)
+    E = edges.shape[0]
+    color = np.empty(max(E, 1), np.int32)
+    sorted_edges = np.empty(max(E, 1), np.int32)
+    prefix = np.empty(max_colors, np.int32)
+    lib().or_color_edges(n_verts, E, _p(edges), max_colors, _p(color), _p(sorted_edges), _p(prefix))
+    return color[:E], sorted_edges[:E], prefix
+
+
+# ---- whole-solver driver -----------------------------------------------------
+class OracleSolver:
+    """CPU restatement of ``Solver.forward`` (XPBD.py:443-469).
+
+    Per frame: if collisions are on and ``rebuild == "frame"``, build both cell
+    BVHs on ``x`` (XPBD.py:448-458).  Per substep: compute_y; ``n_iter`` times
+    [spring sweep + update_dx; if collisions: (first iteration: broad phase on y)
+    narrow phase + update_dx]; compute_velocity; update_x.  With
+    ``rebuild == "substep"`` the BVHs are rebuilt on ``x`` at the start of every
+    substep.  With n_iter = 1 this is exactly the reference's substep.
+    """
+
+    def __init__(self, mesh_dy, mesh_st=None, *, dt, g, k_stretch_stiffness, k_bend_stiffness, dHat=4e-3,
+                 damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
+                 compliance_collision=1e8, nthreads=1, bending_on="x"):
+        self.d = mesh_dy
+        self.s = mesh_st
+        self.dt = float(dt)
+        self.g = np.asarray(g, np.float32)
+        self.kss = k_stretch_stiffness
+        self.kbs = k_bend_stiffness
+        self.dHat = np.float32(dHat)
+        self.damping = np.float32(damping)
+        self.padding = np.float32(padding)
+        self.n_iter = n_iter
+        self.collisions = collisions
+        self.rebuild = rebuild
+        self.cap = cap
+        self.compliance = np.float32(compliance_collision)
+        self.nthreads = nthreads
+        self.bend_on_y = 1 if bending_on == "y" else 0
+        V = mesh_dy["x"].shape[0]
+        self.x4 = np.zeros((V, 4), np.float32)
+        self.x4[:, :3] = mesh_dy["x"]
+        self.fixed = f32(mesh_dy["fixed"])
+        self.m_inv = f32(mesh_dy["m_inv"])
+        self.x4[:, 3] = self.fixed * self.m_inv
+        self.v4 = np.zeros((V, 4), np.float32)
+        self.edges = i32(mesh_dy["edges"])
+        self.l0 = f32(mesh_dy["l0"])
+        self.bend = i32(mesh_dy["bend"]).reshape(-1, 2)
+        self.bl0 = f32(mesh_dy["bend_l0"])
+        self.faces = i32(mesh_dy["faces"])
+        if collisions:
+            self.bvh_dy = CellBVH()
+            if mesh_st is not None:
+                self.bvh_st = CellBVH()
+                self.xs4 = np.zeros((mesh_st["x"].shape[0], 4), np.float32)
+                self.xs4[:, :3] = mesh_st["x"]
+                self.faces_st = i32(mesh_st["faces"])
+        self.last_status = 0
+
+    def _build(self):
+        mn, mx = face_aabbs(self.x4, self.faces, self.padding)
+        self.bvh_dy.build(mn, mx, scene_aabb(self.x4, self.padding))
+        if self.s is not None:
+            mn, mx = face_aabbs(self.xs4, self.faces_st, self.padding)
+            self.bvh_st.build(mn, mx, scene_aabb(self.xs4, self.padding))
+
+    def _broad(self, y4):
+        qmn, qmx = query_boxes(y4, self.padding)
+        Vd = y4.shape[0]
+        if self.s is not None:
+            vt_st = self.bvh_st.traverse(qmn, qmx, self.cap)
+            smn, smx = query_boxes(self.xs4, self.padding)
+            tv_st = self.bvh_dy.traverse(smn, smx, self.cap)
+        else:
+            vt_st = (np.zeros((Vd, self.cap), np.int32), np.zeros(Vd, np.int32), 0)
+            tv_st = (np.zeros((0, self.cap), np.int32), np.zeros(0, np.int32), 0)
+        vt_dy = self.bvh_dy.traverse(qmn, qmx, self.cap)
+        self.last_status |= vt_st[2] | vt_dy[2] | tv_st[2]
+        return vt_st, vt_dy, tv_st
+
+    def substep(self, dt_sub):
+        # dt_sub and the stiffness products are Python doubles, rounded to float32
+        # when passed to the kernels, as the reference's kernel arguments are.
+        dt_sub = float(dt_sub)
+        if self.collisions and self.rebuild == "substep":
+            self._build()
+        y4 = predict(self.x4, self.v4, self.fixed, dt_sub, self.g, self.nthreads)
+        k_spring = float(self.kbs) * dt_sub * dt_sub   # XPBD.py:354 (names swapped)
+        k_bend = float(self.kss) * dt_sub * dt_sub     # XPBD.py:355
+        cands = None
+        for it in range(self.n_iter):
+            spring_sweep(self.x4, y4, self.fixed, self.m_inv, self.edges, self.l0, self.bend, self.bl0, k_spring,
+                         k_bend, self.nthreads, self.bend_on_y)
+            if self.collisions:
+                if it == 0:
+                    cands = self._broad(y4)
+                vt_st, vt_dy, tv_st = cands
+                r = collision_sweep(self.faces, self.faces_st if self.s is not None else None, y4,
+                                    self.xs4 if self.s is not None else None, self.fixed, self.m_inv, self.dHat,
+                                    self.compliance, self.cap, vt_st[:2], vt_dy[:2], tv_st[:2],
+                                    nthreads=self.nthreads)
+                self.last_status |= r["status"]
+        velocity_update(self.x4, y4, self.v4, self.fixed, self.damping, dt_sub, self.nthreads)
+        self.y4 = y4
+
+    def forward(self, n_substeps):
+        dt_sub = self.dt / n_substeps
+        if self.collisions and self.rebuild == "frame":
+            self._build()
+        for _ in range(n_substeps):
+            self.substep(dt_sub)

@@ -1,0 +1,18 @@
+"""starxpbd: GB300-native (sm_103a) XPBD cloth substep.
+
+A drop-in for the Taichi hot path of medialab-ku/starlab-physics
+(``framework/physics/XPBD.py`` Solver, ``framework/collision/lbvh_cell.py``
+LBVH_CELL, ``framework/utilities/graph_coloring.py`` GraphColoring): state in
+torch CUDA tensors, hand-written CUDA kernels behind the C ABI of
+``include/starxpbd.h`` (``libstarxpbd.so``), no CPU fallback.
+"""
+from . import _lib
+from ._lib import SxError, load as load_library, library_path
+from .coloring import GraphColoring
+from .lbvh import LBVH, LBVH_CELL
+from .mesh import TriMesh, box_mesh, grid_cloth, icosphere
+from .solver import Solver
+from . import scenes
+
+__all__ = ["Solver", "LBVH_CELL", "LBVH", "GraphColoring", "TriMesh", "grid_cloth", "box_mesh", "icosphere",
+           "scenes", "SxError", "load_library", "library_path"]

@@ -1,0 +1,123 @@
+"""ctypes binding of ``libstarxpbd.so`` (declared in include/starxpbd.h).
+
+Every wrapper passes raw device pointers (``tensor.data_ptr()``), sizes and the
+current CUDA stream, and raises :class:`SxError` when the C ABI returns a
+nonzero code.  There is no CPU fallback: if the library is missing it is built
+with nvcc, and if that fails, or no CUDA device is present, calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+
+from . import build as _build
+
+P = C.c_void_p
+I = C.c_int
+F = C.c_float
+Z = C.c_size_t
+
+SX_OK = 0
+SX_ERR_ARG = -1
+SX_ERR_CAPACITY = -2
+SX_ERR_TIMEOUT = -3
+SX_ERR_CUDA = -4
+
+STATUS_CAND_OVERFLOW = 1
+STATUS_STACK_OVERFLOW = 2
+STATUS_FIXED_RANGE = 4
+STATUS_CLIMB_LIMIT = 8
+
+# name -> (argtypes, restype)
+SIGNATURES = {
+    "sx_version": ([], I),
+    "sx_last_error": ([], C.c_char_p),
+    "sx_kernel_launches": ([], C.c_longlong),
+    "sx_predict": ([P, P, P, P, I, F, F, F, F, P], I),
+    "sx_jacobi_sweep": ([P, P, P, P, P, P, I, F, F, I, P], I),
+    "sx_velocity_update": ([P, P, P, P, I, F, F, P], I),
+    "sx_face_aabbs": ([P, P, I, F, P, P, P], I),
+    "sx_scene_aabb": ([P, I, F, P, P], I),
+    "sx_cell_bvh_workspace_bytes": ([I], Z),
+    "sx_cell_bvh_init": ([P, P, P, P, P, P, P, P, Z, P], I),
+    "sx_cell_bvh_build": ([P, P, I, P, P, P, P, P, P, P, P, P, P, P, Z, P], I),
+    "sx_cell_bvh_traverse": ([P, I, F, P, P, P, P, P, P, P, P, P, P, P, I, P, P, P, P], I),
+    "sx_face_morton": ([P, P, I, P, P, P, P], I),
+    "sx_radix_sort_workspace_bytes": ([I], Z),
+    "sx_radix_sort_pairs": ([P, P, I, I, P, Z, P], I),
+    "sx_karras_build": ([P, I, I, P, P, P, P, P, P], I),
+    "sx_face_bvh_refit": ([I, P, P, P, P, P, P, P, P, P, P, P], I),
+    "sx_face_bvh_traverse": ([I, P, I, F, P, P, P, P, P, I, P, P, P, P], I),
+    "sx_collision_sweep": ([I, I, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P], I),
+    "sx_color_workspace_bytes": ([I, I], Z),
+    "sx_color_edges_greedy": ([P, I, I, I, P, P, P, P, Z, P], I),
+}
+
+
+class SxError(RuntimeError):
+    def __init__(self, fn, code, msg):
+        super().__init__(f"{fn} failed with code {code}: {msg}")
+        self.code = code
+
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path() -> str:
+    return _build.LIB
+
+
+def load(build_if_missing: bool = True):
+    """Load (building first if needed) the CUDA library and bind signatures."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if build_if_missing:
+            path = _build.build_library()
+        if not os.path.exists(path):
+            raise RuntimeError(f"starxpbd CUDA library missing: {path}")
+        L = C.CDLL(path)
+        for name, (args, res) in SIGNATURES.items():
+            fn = getattr(L, name)
+            fn.argtypes = args
+            fn.restype = res
+        _lib = L
+        return _lib
+
+
+def _call(name, *args):
+    L = load()
+    rc = getattr(L, name)(*args)
+    if rc != SX_OK:
+        raise SxError(name, rc, L.sx_last_error().decode(errors="replace"))
+    return rc
+
+
+def ptr(t) -> int | None:
+    """Device pointer of a tensor (None for None)."""
+    return None if t is None else t.data_ptr()
+
+
+def stream_handle(stream=None) -> int:
+    import torch
+
+    s = stream if stream is not None else torch.cuda.current_stream()
+    return s.cuda_stream
+
+
+class _Calls:
+    """Attribute access returns a checked caller: ``sx.sx_predict(...)``."""
+
+    def __getattr__(self, name):
+        if name not in SIGNATURES:
+            raise AttributeError(name)
+        if SIGNATURES[name][1] is I and name != "sx_version":
+            return lambda *a: _call(name, *a)
+        return getattr(load(), name)
+
+
+sx = _Calls()

@@ -1,0 +1,90 @@
+// Shared device helpers for the starxpbd CUDA library (sm_103a).
+//
+// Numerics: the library is compiled with -fmad=false, -prec-div=true and
+// -prec-sqrt=true, so every float expression below is evaluated as written in
+// IEEE float32 (no FMA contraction, correctly rounded '/' and sqrtf).  Vector
+// helpers fix the evaluation order: dot = (x*x' + y*y') + z*z'.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+
+#include "../../include/starxpbd.h"
+
+namespace sx {
+
+// ---- error plumbing ---------------------------------------------------------
+void set_error(const char* fmt, ...);
+int cuda_status(cudaError_t e, const char* what);
+inline cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+int check_launch(const char* what);
+
+#define SX_REQUIRE(cond, ...)              \
+    do {                                   \
+        if (!(cond)) {                     \
+            ::sx::set_error(__VA_ARGS__);  \
+            return SX_ERR_ARG;             \
+        }                                  \
+    } while (0)
+
+#define SX_CUDA(call)                                                 \
+    do {                                                              \
+        cudaError_t _e = (call);                                      \
+        if (_e != cudaSuccess) return ::sx::cuda_status(_e, #call);   \
+    } while (0)
+
+inline int grid_for(long long n, int block) {
+    long long g = (n + block - 1) / block;
+    return (int)(g < 1 ? 1 : g);
+}
+
+// Every kernel launch of the library goes through launch(), which counts it
+// (sx_kernel_launches() reports the running total for benchmarks).
+void note_launch();
+template <typename K, typename... A>
+inline void launch(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t s, A... args) {
+    kernel<<<grid, block, smem, s>>>(args...);
+    note_launch();
+}
+
+// ---- float3 arithmetic with fixed evaluation order ----------------------------
+struct V3 {
+    float x, y, z;
+};
+__device__ __forceinline__ V3 mk(float4 a) { return V3{a.x, a.y, a.z}; }
+__device__ __forceinline__ V3 sub(V3 a, V3 b) { return V3{a.x - b.x, a.y - b.y, a.z - b.z}; }
+__device__ __forceinline__ V3 add(V3 a, V3 b) { return V3{a.x + b.x, a.y + b.y, a.z + b.z}; }
+__device__ __forceinline__ V3 scale(float s, V3 a) { return V3{s * a.x, s * a.y, s * a.z}; }
+__device__ __forceinline__ V3 neg(V3 a) { return V3{-a.x, -a.y, -a.z}; }
+__device__ __forceinline__ float dot(V3 a, V3 b) { return (a.x * b.x + a.y * b.y) + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+    return V3{a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+__device__ __forceinline__ V3 vmin(V3 a, V3 b) { return V3{fminf(a.x, b.x), fminf(a.y, b.y), fminf(a.z, b.z)}; }
+__device__ __forceinline__ V3 vmax(V3 a, V3 b) { return V3{fmaxf(a.x, b.x), fmaxf(a.y, b.y), fmaxf(a.z, b.z)}; }
+__device__ __forceinline__ bool overlap(V3 a0, V3 a1, V3 b0, V3 b1) {
+    return a0.x <= b1.x && a1.x >= b0.x && a0.y <= b1.y && a1.y >= b0.y && a0.z <= b1.z && a1.z >= b0.z;
+}
+
+// float -> int32: truncate toward zero, saturate, NaN -> 0 (cvt.rzi.s32.f32)
+__device__ __forceinline__ int f2i_sat(float f) { return __float2int_rz(f); }
+
+// ---- contact accumulation in 64-bit fixed point (40 fractional bits) -----------
+constexpr double kFixScale = 1099511627776.0;      // 2^40
+constexpr double kFixInv = 1.0 / 1099511627776.0;  // 2^-40
+constexpr double kFixMax = 4611686018427387904.0;  // 2^62
+__device__ __forceinline__ long long to_fix(float c, int* bad) {
+    double d = (double)c * kFixScale;
+    if (d != d) { *bad = 1; return 0; }
+    if (d >= kFixMax) { *bad = 1; return 4611686018427387904LL; }
+    if (d <= -kFixMax) { *bad = 1; return -4611686018427387904LL; }
+    return __double2ll_rn(d);
+}
+__device__ __forceinline__ float from_fix(long long a) { return __double2float_rn(__ll2double_rn(a) * kFixInv); }
+
+// ---- cell grid ----------------------------------------------------------------
+constexpr int kGridRes = 32;
+constexpr int kNumCells = kGridRes * kGridRes * kGridRes;
+
+}  // namespace sx

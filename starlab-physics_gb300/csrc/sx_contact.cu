@@ -1,0 +1,311 @@
+// Vertex-triangle narrow phase and non-penetration projection
+// (framework/physics/collision_constraints_x.py __vt_st / __vt_dy / __tv_st,
+// framework/collision/distance.py d_type_PT, d_PP/d_PE/d_PT and gradients),
+// followed by update_dx (XPBD.py:384-387).
+//
+// Corrections are accumulated in 64-bit fixed point (40 fractional bits) with
+// integer atomics, so the sum does not depend on the order in which threads
+// arrive (the reference uses float atomics, whose result does).
+#include "sx_common.cuh"
+
+namespace sx {
+
+// 2x2 solve A^{-1} b with A^{-1} = (1/det) [[a11, -a01], [-a10, a00]]
+__device__ __forceinline__ void solve2(float a00, float a01, float a10, float a11, float b0, float b1, float* p0,
+                                       float* p1) {
+    float det = a00 * a11 - a01 * a10;
+    float id = 1.0f / det;
+    float m00 = id * a11, m01 = id * (-a01), m10 = id * (-a10), m11 = id * a00;
+    *p0 = m00 * b0 + m01 * b1;
+    *p1 = m10 * b0 + m11 * b1;
+}
+
+// distance.py:5-47
+__device__ int d_type_PT(V3 v0, V3 v1, V3 v2, V3 v3) {
+    V3 v12 = sub(v2, v1), v13 = sub(v3, v1);
+    V3 n = cross(v12, v13);
+    V3 v13n = cross(v12, n);
+    V3 v10 = sub(v0, v1);
+    float p00, p01;
+    solve2(dot(v12, v12), dot(v12, v13n), dot(v13n, v12), dot(v13n, v13n), dot(v12, v10), dot(v13n, v10), &p00,
+           &p01);
+    if (p00 > 0.0f && p00 < 1.0f && p01 >= 0.0f) return 3;
+    V3 v32 = sub(v3, v2), v32n = cross(v32, n), v20 = sub(v0, v2);
+    float p10, p11;
+    solve2(dot(v32, v32), dot(v32, v32n), dot(v32n, v32), dot(v32n, v32n), dot(v32, v20), dot(v32n, v20), &p10,
+           &p11);
+    if (p10 > 0.0f && p10 < 1.0f && p11 >= 0.0f) return 4;
+    V3 v31 = sub(v1, v3), v31n = cross(v31, n), v30 = sub(v0, v3);
+    float p20, p21;
+    solve2(dot(v31, v31), dot(v31, v31n), dot(v31n, v31), dot(v31n, v31n), dot(v31, v30), dot(v31n, v30), &p20,
+           &p21);
+    if (p20 > 0.0f && p20 < 1.0f && p21 >= 0.0f) return 5;
+    if (p00 <= 0.0f && p20 >= 1.0f) return 0;
+    if (p10 <= 0.0f && p00 >= 1.0f) return 1;
+    if (p20 <= 0.0f && p10 >= 1.0f) return 2;
+    return 6;
+}
+
+__device__ __forceinline__ float d_PP(V3 a, V3 b) {
+    V3 d = sub(a, b);
+    return dot(d, d);
+}
+__device__ __forceinline__ float d_PE(V3 p, V3 e0, V3 e1) {
+    V3 c = cross(sub(e0, p), sub(e1, p));
+    V3 e = sub(e1, e0);
+    return dot(c, c) / dot(e, e);
+}
+__device__ __forceinline__ float d_PT(V3 p, V3 t0, V3 t1, V3 t2) {
+    V3 b = cross(sub(t1, t0), sub(t2, t0));
+    float s = dot(sub(p, t0), b);
+    return s * s / dot(b, b);
+}
+// Closed-form gradients of the squared distances:
+//  PP: g_a = 2(a-b), g_b = -g_a
+//  PE: c=(e0-p)x(e1-p), L=|e1-e0|^2, d=c.c/L;
+//      g_e0 = (2 (e1-p)xc + 2d (e1-e0))/L, g_e1 = (2 cx(e0-p) - 2d (e1-e0))/L,
+//      g_p = -(g_e0 + g_e1)
+//  PT: n=(t1-t0)x(t2-t0), r=p-t0, s=r.n, N=n.n, d=s^2/N;
+//      g_p = 2sn/N, g_t1 = (2s (t2-t0)xr - 2d (t2-t0)xn)/N,
+//      g_t2 = (2s rx(t1-t0) - 2d nx(t1-t0))/N, g_t0 = -(g_p + g_t1 + g_t2)
+__device__ __forceinline__ void g_PP(V3 a, V3 b, V3* ga, V3* gb) {
+    *ga = scale(2.0f, sub(a, b));
+    *gb = neg(*ga);
+}
+__device__ __forceinline__ void g_PE(V3 p, V3 e0, V3 e1, V3* gp, V3* g0, V3* g1) {
+    V3 a = sub(e0, p), b = sub(e1, p);
+    V3 c = cross(a, b);
+    V3 e = sub(e1, e0);
+    float L = dot(e, e);
+    float iL = 1.0f / L;
+    float d = dot(c, c) * iL;
+    V3 bc = cross(b, c), ca = cross(c, a);
+    float td = 2.0f * d;
+    V3 t0 = add(scale(2.0f, bc), scale(td, e));
+    V3 t1 = sub(scale(2.0f, ca), scale(td, e));
+    *g0 = scale(iL, t0);
+    *g1 = scale(iL, t1);
+    *gp = neg(add(*g0, *g1));
+}
+__device__ __forceinline__ void g_PT(V3 p, V3 t0, V3 t1, V3 t2, V3* gp, V3* g0, V3* g1, V3* g2) {
+    V3 u = sub(t1, t0), w = sub(t2, t0);
+    V3 n = cross(u, w);
+    V3 r = sub(p, t0);
+    float s = dot(r, n);
+    float N = dot(n, n);
+    float iN = 1.0f / N;
+    float d = (s * s) * iN;
+    float ts = 2.0f * s, td = 2.0f * d;
+    *gp = scale(ts * iN, n);
+    V3 a1 = sub(scale(ts, cross(w, r)), scale(td, cross(w, n)));
+    V3 a2 = sub(scale(ts, cross(r, u)), scale(td, cross(n, u)));
+    *g1 = scale(iN, a1);
+    *g2 = scale(iN, a2);
+    *g0 = neg(add(add(*gp, *g1), *g2));
+}
+
+__device__ float pt_distance(int dtype, V3 x0, V3 x1, V3 x2, V3 x3, V3 g[4], bool want_grad, float dflt) {
+    float d = dflt;
+    switch (dtype) {
+        case 0: d = d_PP(x0, x1); if (want_grad) g_PP(x0, x1, &g[0], &g[1]); break;
+        case 1: d = d_PP(x0, x2); if (want_grad) g_PP(x0, x2, &g[0], &g[2]); break;
+        case 2: d = d_PP(x0, x3); if (want_grad) g_PP(x0, x3, &g[0], &g[3]); break;
+        case 3: d = d_PE(x0, x1, x2); if (want_grad) g_PE(x0, x1, x2, &g[0], &g[1], &g[2]); break;
+        case 4: d = d_PE(x0, x2, x3); if (want_grad) g_PE(x0, x2, x3, &g[0], &g[2], &g[3]); break;
+        case 5: d = d_PE(x0, x1, x3); if (want_grad) g_PE(x0, x1, x3, &g[0], &g[1], &g[3]); break;
+        case 6: d = d_PT(x0, x1, x2, x3); if (want_grad) g_PT(x0, x1, x2, x3, &g[0], &g[1], &g[2], &g[3]); break;
+        default: break;
+    }
+    return d;
+}
+__device__ __forceinline__ int region_mask(int dtype) {
+    // bit k set: vertex k (0 = query point, 1..3 = triangle) takes part
+    return dtype == 0 ? 0x3 : dtype == 1 ? 0x5 : dtype == 2 ? 0x9 : dtype == 3 ? 0x7 : dtype == 4 ? 0xD
+         : dtype == 5 ? 0xB : dtype == 6 ? 0xF : 0;
+}
+
+__device__ __forceinline__ void acc_add(long long* dx, int* nc, int v, float a, V3 g, int* bad) {
+    long long c0 = to_fix(a * g.x, bad), c1 = to_fix(a * g.y, bad), c2 = to_fix(a * g.z, bad);
+    atomicAdd((unsigned long long*)(dx + 3 * v), (unsigned long long)c0);
+    atomicAdd((unsigned long long*)(dx + 3 * v + 1), (unsigned long long)c1);
+    atomicAdd((unsigned long long*)(dx + 3 * v + 2), (unsigned long long)c2);
+    atomicAdd(nc + v, 1);
+}
+
+struct PairOut {
+    int* pair;
+    float* g;
+    float* schur;
+    int* num;
+    int cap;
+    __device__ __forceinline__ void rec(size_t q, int& cnt, int face, int dtype, const V3 gg[4], float s) {
+        if (!num || cnt >= cap) return;
+        size_t o = q * cap + cnt;
+        pair[2 * o] = face;
+        pair[2 * o + 1] = dtype;
+        float4* g4 = reinterpret_cast<float4*>(g) + 4 * o;
+        for (int k = 0; k < 4; ++k) g4[k] = make_float4(gg[k].x, gg[k].y, gg[k].z, 0.0f);
+        schur[o] = s;
+        ++cnt;
+    }
+};
+
+__global__ void __launch_bounds__(128) collision_project_kernel(
+    int Vd, int Vs, const int* __restrict__ faces_dy, const int* __restrict__ faces_st,
+    const float4* __restrict__ y4, const float4* __restrict__ xs4, const float* __restrict__ fixed,
+    const float* __restrict__ m_inv, float dHat, float compliance, int cap, const int* __restrict__ vt_st_c,
+    const int* __restrict__ vt_st_n, const int* __restrict__ vt_dy_c, const int* __restrict__ vt_dy_n,
+    const int* __restrict__ tv_st_c, const int* __restrict__ tv_st_n, long long* dx, int* nc, PairOut po,
+    int* status) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * Vd + Vs) return;
+    int bad = 0;
+    int cnt = 0;
+    if (i < Vd) {  // __vt_st (collision_constraints_x.py:6-69)
+        const int vid = i;
+        const int n = min(vt_st_n[vid], cap);
+        const V3 x0 = mk(y4[vid]);
+        const float wv = m_inv[vid];
+        for (int j = 0; j < n; ++j) {
+            const int fs = vt_st_c[(size_t)vid * cap + j];
+            const V3 x1 = mk(xs4[faces_st[3 * fs]]), x2 = mk(xs4[faces_st[3 * fs + 1]]),
+                     x3 = mk(xs4[faces_st[3 * fs + 2]]);
+            V3 g[4] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+            const int dt = d_type_PT(x0, x1, x2, x3);
+            const float d = pt_distance(dt, x0, x1, x2, x3, g, true, dHat);
+            if (d < dHat) {
+                const float schur = wv * dot(g[0], g[0]);
+                const float ld = (compliance * (dHat - d)) / (compliance * schur + 1.0f);
+                acc_add(dx, nc, vid, wv * ld, g[0], &bad);
+                po.rec((size_t)vid, cnt, fs, dt, g, schur);
+            }
+        }
+        if (po.num) po.num[vid] = cnt;
+    } else if (i < 2 * Vd) {  // __vt_dy (collision_constraints_x.py:176-310)
+        const int vid = i - Vd;
+        const int n = min(vt_dy_n[vid], cap);
+        for (int j = 0; j < n; ++j) {
+            const int fd = vt_dy_c[(size_t)vid * cap + j];
+            const int a = faces_dy[3 * fd], b = faces_dy[3 * fd + 1], c = faces_dy[3 * fd + 2];
+            if (a == vid || b == vid || c == vid) continue;  // Solver.is_in_face, XPBD.py:121-127
+            const int vv[4] = {vid, a, b, c};
+            const V3 x[4] = {mk(y4[vid]), mk(y4[a]), mk(y4[b]), mk(y4[c])};
+            V3 g[4] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+            const int dt = d_type_PT(x[0], x[1], x[2], x[3]);
+            const float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);
+            float schur = 0.0f;
+            if (d < dHat) {
+                pt_distance(dt, x[0], x[1], x[2], x[3], g, true, dHat);
+                const int m = region_mask(dt);
+                float s = 0.0f;
+                bool first = true;
+                for (int k = 0; k < 4; ++k) {
+                    if (!(m & (1 << k))) continue;
+                    const float t = (fixed[vv[k]] * m_inv[vv[k]]) * dot(g[k], g[k]);
+                    s = first ? t : s + t;
+                    first = false;
+                }
+                schur = s + 1e-4f;
+                const float ld = (dHat - d) / schur;
+                for (int k = 0; k < 4; ++k) {
+                    if (!(m & (1 << k))) continue;
+                    // region 0 applies m_inv without `fixed` (collision_constraints_x.py:199-200)
+                    const float w = dt == 0 ? m_inv[vv[k]] : fixed[vv[k]] * m_inv[vv[k]];
+                    acc_add(dx, nc, vv[k], w * ld, g[k], &bad);
+                }
+            }
+            po.rec((size_t)Vd + vid, cnt, fd, dt, g, schur);
+        }
+        if (po.num) po.num[Vd + vid] = cnt;
+    } else {  // __tv_st (collision_constraints_x.py:72-173)
+        const int vis = i - 2 * Vd;
+        const int n = min(tv_st_n[vis], cap);
+        for (int j = 0; j < n; ++j) {
+            const int fd = tv_st_c[(size_t)vis * cap + j];
+            const int vv[4] = {-1, faces_dy[3 * fd], faces_dy[3 * fd + 1], faces_dy[3 * fd + 2]};
+            const V3 x[4] = {mk(xs4[vis]), mk(y4[vv[1]]), mk(y4[vv[2]]), mk(y4[vv[3]])};
+            V3 g[4] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
+            const int dt = d_type_PT(x[0], x[1], x[2], x[3]);
+            const float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);
+            float schur = 0.0f;
+            if (d < dHat) {
+                pt_distance(dt, x[0], x[1], x[2], x[3], g, true, dHat);
+                const int m = region_mask(dt) & ~1;
+                float s = 0.0f;
+                bool first = true;
+                for (int k = 1; k < 4; ++k) {
+                    if (!(m & (1 << k))) continue;
+                    const float t = (fixed[vv[k]] * m_inv[vv[k]]) * dot(g[k], g[k]);
+                    s = first ? t : s + t;
+                    first = false;
+                }
+                schur = s;
+                const float ld = (compliance * (dHat - d)) / (compliance * schur + 1.0f);
+                for (int k = 1; k < 4; ++k) {
+                    if (!(m & (1 << k))) continue;
+                    acc_add(dx, nc, vv[k], (fixed[vv[k]] * m_inv[vv[k]]) * ld, g[k], &bad);
+                }
+            }
+            po.rec((size_t)2 * Vd + vis, cnt, fd, dt, g, schur);
+        }
+        if (po.num) po.num[2 * Vd + vis] = cnt;
+    }
+    if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
+}
+
+// update_dx (XPBD.py:384-387) from the fixed-point accumulators; clears them.
+__global__ void collision_apply_kernel(int V, float4* __restrict__ y4, const float* __restrict__ fixed,
+                                       long long* __restrict__ dx, int* __restrict__ nc) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    const int c = nc[v];
+    if (c > 0) {
+        const float cf = (float)c;
+        const float f = fixed[v];
+        float4 y = y4[v];
+        y.x = y.x + f * (from_fix(dx[3 * v]) / cf);
+        y.y = y.y + f * (from_fix(dx[3 * v + 1]) / cf);
+        y.z = y.z + f * (from_fix(dx[3 * v + 2]) / cf);
+        y4[v] = y;
+        dx[3 * v] = 0;
+        dx[3 * v + 1] = 0;
+        dx[3 * v + 2] = 0;
+        nc[v] = 0;
+    }
+}
+
+}  // namespace sx
+
+using namespace sx;
+
+extern "C" int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const int* faces_st, float* y4,
+                                  const float* xs4, const float* fixed, const float* m_inv, float dHat,
+                                  float compliance, int cap, const int* vt_st_cand, const int* vt_st_num,
+                                  const int* vt_dy_cand, const int* vt_dy_num, const int* tv_st_cand,
+                                  const int* tv_st_num, long long* dx_fix, int* nc, int* pair, float* pair_g,
+                                  float* pair_schur, int* pair_num, int* status, void* stream) {
+    SX_REQUIRE(n_dy >= 0 && n_st >= 0 && cap >= 1, "sx_collision_sweep: bad sizes");
+    if (n_dy == 0) return SX_OK;
+    SX_REQUIRE(faces_dy && y4 && fixed && m_inv && vt_dy_cand && vt_dy_num && dx_fix && nc && status,
+               "sx_collision_sweep: null pointer");
+    SX_REQUIRE(n_st == 0 || (faces_st && xs4 && vt_st_cand && vt_st_num && tv_st_cand && tv_st_num),
+               "sx_collision_sweep: null static-mesh pointer");
+    SX_REQUIRE(!pair_num || (pair && pair_g && pair_schur), "sx_collision_sweep: partial pair outputs");
+    cudaStream_t s = as_stream(stream);
+    PairOut po{pair, pair_g, pair_schur, pair_num, cap};
+    const int total = 2 * n_dy + n_st;
+    // with no static mesh the vt_st block has no candidates: point it at the
+    // vt_dy block but force its counts to zero by passing n_st == 0 paths only
+    const int* vsn = vt_st_num;
+    const int* vsc = vt_st_cand;
+    if (n_st == 0) {
+        SX_REQUIRE(vt_st_num && vt_st_cand, "sx_collision_sweep: vt_st arrays required (may be zero counts)");
+    }
+    launch(collision_project_kernel, grid_for(total, 128), 128, 0, s, 
+        n_dy, n_st, faces_dy, faces_st, (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, cap,
+        vsc, vsn, vt_dy_cand, vt_dy_num, tv_st_cand, tv_st_num, dx_fix, nc, po, status);
+    int rc = check_launch("collision_project_kernel");
+    if (rc) return rc;
+    launch(collision_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)y4, fixed, dx_fix, nc);
+    return check_launch("collision_apply_kernel");
+}

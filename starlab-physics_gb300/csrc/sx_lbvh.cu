@@ -1,0 +1,616 @@
+// LBVH broad phase: Morton codes, stable LSD radix sort, Karras 2012 hierarchy,
+// single-launch bottom-up refit and stack traversal, for the reference's 32^3
+// cell-grid BVH (framework/collision/lbvh_cell.py, class LBVH_CELL) and for a
+// face-level LBVH over triangle soups.
+#include "sx_common.cuh"
+
+namespace sx {
+
+// ---------------------------------------------------------------------------
+// Morton codes (lbvh_cell.py:87-102, :139-148)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long expand_bits(unsigned long long v) {
+    v = (v | (v << 16)) & 0x030000FFull;
+    v = (v | (v << 8)) & 0x0300F00Full;
+    v = (v | (v << 4)) & 0x030C30C3ull;
+    v = (v | (v << 2)) & 0x09249249ull;
+    return v;
+}
+__device__ __forceinline__ float clampf(float v, float lo, float hi) { return fminf(fmaxf(v, lo), hi); }
+__device__ __forceinline__ unsigned morton3d(float x, float y, float z) {
+    x = clampf(x * 1024.0f, 0.0f, 1023.0f);
+    y = clampf(y * 1024.0f, 0.0f, 1023.0f);
+    z = clampf(z * 1024.0f, 0.0f, 1023.0f);
+    unsigned long long xx = expand_bits((unsigned long long)x), yy = expand_bits((unsigned long long)y),
+                       zz = expand_bits((unsigned long long)z);
+    return (unsigned)(xx | (yy << 1) | (zz << 2));
+}
+__device__ __forceinline__ unsigned morton_of(V3 p, V3 lo, V3 hi) {
+    float x = (p.x - lo.x) / (hi.x - lo.x);
+    float y = (p.y - lo.y) / (hi.y - lo.y);
+    float z = (p.z - lo.z) / (hi.z - lo.z);
+    return morton3d(clampf(x, 0.f, 1.f), clampf(y, 0.f, 1.f), clampf(z, 0.f, 1.f));
+}
+
+__device__ __forceinline__ V3 cell_size_of(const float* box6) {
+    return V3{(box6[3] - box6[0]) / (float)kGridRes, (box6[4] - box6[1]) / (float)kGridRes,
+              (box6[5] - box6[2]) / (float)kGridRes};
+}
+// assign_cell_centers (lbvh_cell.py:105-120)
+__device__ __forceinline__ V3 cell_center(int i, V3 cs, V3 lo) {
+    int x0 = i / (kGridRes * kGridRes), y0 = (i % (kGridRes * kGridRes)) / kGridRes, z0 = i % kGridRes;
+    V3 p{cs.x * (float)x0 + 0.5f * cs.x, cs.y * (float)y0 + 0.5f * cs.y, cs.z * (float)z0 + 0.5f * cs.z};
+    return add(p, lo);
+}
+
+__global__ void cell_morton_kernel(unsigned* codes, int* ids) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kNumCells) return;
+    const float box[6] = {0.f, 0.f, 0.f, 1e3f, 1e3f, 1e3f};
+    V3 lo{0.f, 0.f, 0.f}, hi{1e3f, 1e3f, 1e3f};
+    V3 cs = cell_size_of(box);
+    codes[i] = morton_of(cell_center(i, cs, lo), lo, hi);
+    ids[i] = i;
+}
+
+__global__ void face_morton_kernel(int F, const float4* __restrict__ mn4, const float4* __restrict__ mx4,
+                                   const float* __restrict__ box6, unsigned* codes, int* ids) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    if (f >= F) return;
+    V3 lo{box6[0], box6[1], box6[2]}, hi{box6[3], box6[4], box6[5]};
+    V3 c = scale(0.5f, add(mk(mx4[f]), mk(mn4[f])));
+    codes[f] = morton_of(c, lo, hi);
+    ids[f] = f;
+}
+
+// ---------------------------------------------------------------------------
+// Stable LSD radix sort, 8-bit digits.
+//   upsweep : per-tile digit histogram -> hist[digit * nblocks + block]
+//   scan    : exclusive scan of hist (digit-major => stable across tiles)
+//   scatter : per tile, keys ranked within their digit in input order with
+//             __match_any_sync + per-warp counts, written to their final slots.
+// ---------------------------------------------------------------------------
+constexpr int RS_BLOCK = 256;
+constexpr int RS_ITEMS = 8;
+constexpr int RS_TILE = RS_BLOCK * RS_ITEMS;
+constexpr int RS_WARPS = RS_BLOCK / 32;
+
+__global__ void __launch_bounds__(RS_BLOCK) rs_upsweep(const unsigned* __restrict__ keys, int n, int shift,
+                                                       unsigned* __restrict__ hist, int nblocks) {
+    __shared__ unsigned cnt[256];
+    const int tid = threadIdx.x;
+    cnt[tid] = 0;
+    __syncthreads();
+    const long long base = (long long)blockIdx.x * RS_TILE;
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        long long idx = base + r * RS_BLOCK + tid;
+        if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    hist[(size_t)tid * nblocks + blockIdx.x] = cnt[tid];
+}
+
+// single-block scan over n entries (exclusive or inclusive), 1024 threads
+__global__ void __launch_bounds__(1024) scan_single_block(unsigned* data, int n, int inclusive) {
+    __shared__ unsigned s[1024];
+    const int tid = threadIdx.x;
+    const int per = (n + 1023) / 1024;
+    const int beg = min(tid * per, n), end = min(beg + per, n);
+    unsigned sum = 0;
+    for (int i = beg; i < end; ++i) sum += data[i];
+    s[tid] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        unsigned v = tid >= off ? s[tid - off] : 0u;
+        __syncthreads();
+        s[tid] += v;
+        __syncthreads();
+    }
+    unsigned run = tid ? s[tid - 1] : 0u;
+    for (int i = beg; i < end; ++i) {
+        unsigned t = data[i];
+        if (inclusive) {
+            run += t;
+            data[i] = run;
+        } else {
+            data[i] = run;
+            run += t;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(RS_BLOCK) rs_scatter(const unsigned* __restrict__ kin,
+                                                       const int* __restrict__ vin, unsigned* __restrict__ kout,
+                                                       int* __restrict__ vout, int n, int shift,
+                                                       const unsigned* __restrict__ hist, int nblocks) {
+    __shared__ unsigned s_base[256];
+    __shared__ unsigned s_wcnt[RS_WARPS][256];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    s_base[tid] = hist[(size_t)tid * nblocks + blockIdx.x];
+    const long long base = (long long)blockIdx.x * RS_TILE;
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const long long idx = base + r * RS_BLOCK + tid;
+        const bool valid = idx < n;
+        unsigned key = 0;
+        int val = 0;
+        if (valid) {
+            key = kin[idx];
+            val = vin[idx];
+        }
+        const unsigned digit = valid ? ((key >> shift) & 255u) : 256u;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) s_wcnt[w][tid] = 0;
+        __syncthreads();
+        const unsigned peers = __match_any_sync(0xffffffffu, digit);
+        const unsigned rank = __popc(peers & lt_mask);
+        if (valid && (__ffs(peers) - 1) == lane) s_wcnt[warp][digit] = __popc(peers);
+        __syncthreads();
+        if (valid) {
+            unsigned off = s_base[digit];
+            for (int w = 0; w < warp; ++w) off += s_wcnt[w][digit];
+            const unsigned pos = off + rank;
+            kout[pos] = key;
+            vout[pos] = val;
+        }
+        __syncthreads();
+        unsigned tot = 0;
+#pragma unroll
+        for (int w = 0; w < RS_WARPS; ++w) tot += s_wcnt[w][tid];
+        s_base[tid] += tot;
+    }
+}
+
+static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
+static inline int rs_nblocks(int n) { return n <= 0 ? 1 : (n + RS_TILE - 1) / RS_TILE; }
+static size_t rs_ws_bytes(int n) {
+    size_t nn = (size_t)(n > 0 ? n : 1);
+    return align256(nn * 4) * 2 + align256((size_t)256 * rs_nblocks(n) * 4);
+}
+
+static int radix_sort(unsigned* keys, int* vals, int n, int bits, void* ws, size_t ws_bytes, cudaStream_t s) {
+    SX_REQUIRE(bits >= 1 && bits <= 32, "radix sort: bits must be in [1, 32]");
+    if (n <= 1) return SX_OK;
+    SX_REQUIRE(ws && ws_bytes >= rs_ws_bytes(n), "radix sort: workspace too small (%zu < %zu)", ws_bytes,
+               rs_ws_bytes(n));
+    char* p = (char*)ws;
+    unsigned* kalt = (unsigned*)p;
+    p += align256((size_t)n * 4);
+    int* valt = (int*)p;
+    p += align256((size_t)n * 4);
+    unsigned* hist = (unsigned*)p;
+    const int nb = rs_nblocks(n);
+    const int passes = (bits + 7) / 8;
+    unsigned* ki = keys;
+    int* vi = vals;
+    unsigned* ko = kalt;
+    int* vo = valt;
+    for (int pass = 0; pass < passes; ++pass) {
+        const int shift = 8 * pass;
+        launch(rs_upsweep, nb, RS_BLOCK, 0, s, ki, n, shift, hist, nb);
+        launch(scan_single_block, 1, 1024, 0, s, hist, 256 * nb, 0);
+        launch(rs_scatter, nb, RS_BLOCK, 0, s, ki, vi, ko, vo, n, shift, hist, nb);
+        unsigned* tk = ki; ki = ko; ko = tk;
+        int* tv = vi; vi = vo; vo = tv;
+    }
+    if (ki != keys) {
+        SX_CUDA(cudaMemcpyAsync(keys, ki, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+        SX_CUDA(cudaMemcpyAsync(vals, vi, (size_t)n * 4, cudaMemcpyDeviceToDevice, s));
+    }
+    return check_launch("radix_sort");
+}
+
+// ---------------------------------------------------------------------------
+// Karras 2012 hierarchy (lbvh_cell.py:256-336, :384-430)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int kdelta(int i, long long j, int n, const unsigned* c, int tie) {
+    if (j > n - 1 || j < 0) return -1;
+    unsigned x = c[i] ^ c[(int)j];
+    if (x == 0) return tie ? 32 + __clz(i ^ (int)j) : 32;
+    return __clz(x);
+}
+
+__global__ void karras_kernel(int n, const unsigned* __restrict__ c, int tie, int* child_a, int* child_b,
+                              int* range_l, int* range_r, int* parent) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) parent[0] = -1;
+    if (i >= n - 1) return;
+    // determine_range
+    int dl = kdelta(i, (long long)i - 1, n, c, tie), dr = kdelta(i, (long long)i + 1, n, c, tie);
+    int d = 1, dmin = dl;
+    if (dr < dl) { d = -1; dmin = dr; }
+    long long lmax = 2;
+    while (lmax < 4LL * n && kdelta(i, (long long)i + lmax * d, n, c, tie) > dmin) lmax <<= 2;
+    long long l = 0;
+    for (long long t = lmax / 2; t > 0; t /= 2) {
+        long long j = (long long)i + (l + t) * d;
+        int dd = (j >= 0 && j < n) ? kdelta(i, j, n, c, tie) : -1;
+        if (dd > dmin) l += t;
+    }
+    int s = i, e = (int)(i + l * d);
+    if (d == -1) { s = (int)(i + l * d); e = i; }
+    // find_split
+    int split;
+    if (c[s] == c[e] && !tie) {
+        split = (s + e) / 2;
+    } else {
+        int common = kdelta(s, e, n, c, tie);
+        split = s;
+        int step = e - s;
+        while (step > 1) {
+            step = (step + 1) / 2;
+            int ns = split + step;
+            if (ns < e && kdelta(s, ns, n, c, tie) > common) split = ns;
+        }
+    }
+    int left = split, right = split + 1;
+    if (split == s) left += n - 1;
+    if (right == e) right += n - 1;
+    child_a[i] = left;
+    child_b[i] = right;
+    range_l[i] = s;
+    range_r[i] = e;
+    parent[left] = i;
+    parent[right] = i;
+}
+
+// ---------------------------------------------------------------------------
+// Cell-grid BVH build (LBVH_CELL.build, lbvh_cell.py:637-653)
+// ---------------------------------------------------------------------------
+__global__ void face_cell_kernel(int F, const float4* __restrict__ mn4, const float4* __restrict__ mx4,
+                                 const float* __restrict__ box6, unsigned* keys, int* ids, unsigned* counts,
+                                 float* cell_size3) {
+    int f = blockIdx.x * blockDim.x + threadIdx.x;
+    V3 lo{box6[0], box6[1], box6[2]};
+    V3 cs = cell_size_of(box6);
+    if (f == 0) {
+        cell_size3[0] = cs.x;
+        cell_size3[1] = cs.y;
+        cell_size3[2] = cs.z;
+    }
+    if (f >= F) return;
+    V3 c = scale(0.5f, add(mk(mn4[f]), mk(mx4[f])));
+    int ix = min(max(f2i_sat((c.x - lo.x) / cs.x), 0), kGridRes - 1);
+    int iy = min(max(f2i_sat((c.y - lo.y) / cs.y), 0), kGridRes - 1);
+    int iz = min(max(f2i_sat((c.z - lo.z) / cs.z), 0), kGridRes - 1);
+    int cell = ix * kGridRes * kGridRes + iy * kGridRes + iz;
+    keys[f] = (unsigned)cell;
+    ids[f] = f;
+    atomicAdd(counts + cell, 1u);
+}
+
+__device__ __forceinline__ void store_box(float4* nmin4, float4* nmax4, int i, V3 a, V3 b) {
+    nmin4[i] = make_float4(a.x, a.y, a.z, 0.0f);
+    nmax4[i] = make_float4(b.x, b.y, b.z, 0.0f);
+}
+__device__ __forceinline__ V3 load_cg(const float4* p) {
+    float4 v = __ldcg(p);
+    return V3{v.x, v.y, v.z};
+}
+
+// assign_leaf_cell_nodes (:602-634) fused with a bottom-up refit that applies
+// the rules of compute_cell_node_aabbs (:491-522).  The second thread to reach
+// an internal node computes it from both (finished) children.
+__global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int* __restrict__ prefix,
+                                       const int* __restrict__ sorted_face_ids, const float4* __restrict__ fmn4,
+                                       const float4* __restrict__ fmx4, const int* __restrict__ child_a,
+                                       const int* __restrict__ child_b, const int* __restrict__ parent,
+                                       int* num_faces, float4* nmin4, float4* nmax4, int* flags, int* status) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= kNumCells) return;
+    V3 lo{box6[0], box6[1], box6[2]};
+    V3 cs = cell_size_of(box6);
+    const int leaf = i + kNumCells - 1;
+    const int rl = i == 0 ? 0 : prefix[i - 1];
+    const int size = prefix[i] - rl;
+    V3 c = cell_center(i, cs, lo);
+    V3 a = c, b = c;
+    for (int j = 0; j < size; ++j) {
+        int fid = sorted_face_ids[rl + j];
+        a = vmin(a, mk(fmn4[fid]));
+        b = vmax(b, mk(fmx4[fid]));
+    }
+    num_faces[leaf] = size;
+    store_box(nmin4, nmax4, leaf, a, b);
+    int node = parent[leaf];
+    for (int steps = 0; node >= 0; ++steps) {
+        if (steps > kNumCells) {
+            atomicOr(status, SX_STATUS_CLIMB_LIMIT);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(flags + node, 1) == 0) return;
+        flags[node] = 0;
+        const int l = child_a[node], r = child_b[node];
+        const int nl = __ldcg(num_faces + l), nr = __ldcg(num_faces + r);
+        V3 min0 = load_cg(nmin4 + l), max0 = load_cg(nmax4 + l), min1 = load_cg(nmin4 + r), max1 = load_cg(nmax4 + r);
+        V3 na, nb;
+        if (nl > 0 && nr > 0) {
+            na = vmin(min0, min1);
+            nb = vmax(max0, max1);
+        } else if (nl > 0) {
+            na = min0;
+            nb = max0;
+        } else if (nr > 0) {
+            na = min1;
+            nb = max1;
+        } else {
+            na = scale(0.25f, add(add(add(min0, max0), min1), max1));
+            nb = na;
+        }
+        num_faces[node] = nl + nr;
+        store_box(nmin4, nmax4, node, na, nb);
+        node = parent[node];
+    }
+}
+
+// traverse_cell_bvh_single (lbvh_cell.py:662-714)
+__global__ void __launch_bounds__(128) cell_traverse_kernel(
+    int Q, const float4* __restrict__ p4, float pad, const float* __restrict__ cs3, const float* __restrict__ box6,
+    const int* __restrict__ child_a, const int* __restrict__ child_b, const int* __restrict__ num_faces,
+    const float4* __restrict__ nmin4, const float4* __restrict__ nmax4, const int* __restrict__ prefix,
+    const int* __restrict__ sorted_face_ids, const float4* __restrict__ fmn4, const float4* __restrict__ fmx4,
+    int cap, int* __restrict__ cand, int* __restrict__ num, int* status) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= Q) return;
+    V3 p = mk(p4[q]);
+    V3 a{p.x - pad, p.y - pad, p.z - pad}, b{p.x + pad, p.y + pad, p.z + pad};
+    V3 pos = scale(0.5f, add(a, b));
+    V3 cs{cs3[0], cs3[1], cs3[2]}, org{box6[0], box6[1], box6[2]};
+    int ix = f2i_sat((pos.x - org.x) / cs.x), iy = f2i_sat((pos.y - org.y) / cs.y),
+        iz = f2i_sat((pos.z - org.z) / cs.z);
+    int cid = (int)((unsigned)ix * (unsigned)(kGridRes * kGridRes) + (unsigned)iy * (unsigned)kGridRes + (unsigned)iz);
+    int count = 0;
+    int flags = 0;
+    int* out = cand + (size_t)q * cap;
+    if (cid <= kNumCells - 1) {
+        int stack[64];
+        int sc = 0;
+        stack[sc++] = 0;
+        long long pops = 0;
+        while (sc > 0) {
+            if (++pops > 2LL * kNumCells) {
+                flags |= SX_STATUS_STACK_OVERFLOW;
+                break;
+            }
+            const int idx = stack[--sc];
+            if (num_faces[idx] <= 0) continue;
+            if (!overlap(a, b, mk(nmin4[idx]), mk(nmax4[idx]))) continue;
+            if (idx >= kNumCells - 1) {
+                const int i = idx - (kNumCells - 1);
+                const int rl = i == 0 ? 0 : prefix[i - 1];
+                const int size = prefix[i] - rl;
+                for (int j = 0; j < size; ++j) {
+                    const int fid = sorted_face_ids[rl + j];
+                    if (overlap(a, b, mk(fmn4[fid]), mk(fmx4[fid]))) {
+                        if (count < cap) out[count] = fid;
+                        ++count;
+                    }
+                }
+            } else {
+                const int l = child_a[idx], r = child_b[idx];
+                if (num_faces[l] > 0) {
+                    if (sc < 64) stack[sc++] = l; else flags |= SX_STATUS_STACK_OVERFLOW;
+                }
+                if (num_faces[r] > 0) {
+                    if (sc < 64) stack[sc++] = r; else flags |= SX_STATUS_STACK_OVERFLOW;
+                }
+            }
+        }
+    }
+    num[q] = count;
+    if (count > cap) flags |= SX_STATUS_CAND_OVERFLOW;
+    if (flags) atomicOr(status, flags);
+}
+
+// ---------------------------------------------------------------------------
+// Face-level LBVH refit and traversal
+// ---------------------------------------------------------------------------
+__global__ void face_refit_kernel(int n, const int* __restrict__ sorted_ids, const float4* __restrict__ fmn4,
+                                  const float4* __restrict__ fmx4, const int* __restrict__ child_a,
+                                  const int* __restrict__ child_b, const int* __restrict__ parent, float4* nmin4,
+                                  float4* nmax4, int* flags, int* status) {
+    int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int leaf = n - 1 + j, f = sorted_ids[j];
+    nmin4[leaf] = fmn4[f];
+    nmax4[leaf] = fmx4[f];
+    if (n == 1) return;
+    int node = parent[leaf];
+    for (int steps = 0; node >= 0; ++steps) {
+        if (steps > n) {
+            atomicOr(status, SX_STATUS_CLIMB_LIMIT);
+            return;
+        }
+        __threadfence();
+        if (atomicAdd(flags + node, 1) == 0) return;
+        flags[node] = 0;
+        const int l = child_a[node], r = child_b[node];
+        V3 a = vmin(load_cg(nmin4 + l), load_cg(nmin4 + r));
+        V3 b = vmax(load_cg(nmax4 + l), load_cg(nmax4 + r));
+        store_box(nmin4, nmax4, node, a, b);
+        node = parent[node];
+    }
+}
+
+__global__ void __launch_bounds__(128) face_traverse_kernel(int n, int Q, const float4* __restrict__ p4, float pad,
+                                                            const int* __restrict__ child_a,
+                                                            const int* __restrict__ child_b,
+                                                            const int* __restrict__ sorted_ids,
+                                                            const float4* __restrict__ nmin4,
+                                                            const float4* __restrict__ nmax4, int cap,
+                                                            int* __restrict__ cand, int* __restrict__ num,
+                                                            int* status) {
+    int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= Q) return;
+    V3 p = mk(p4[q]);
+    V3 a{p.x - pad, p.y - pad, p.z - pad}, b{p.x + pad, p.y + pad, p.z + pad};
+    int count = 0, flags = 0;
+    int* out = cand + (size_t)q * cap;
+    int stack[64];
+    int sc = 0;
+    stack[sc++] = 0;
+    // A well-formed tree pops each of its 2n-1 nodes at most once; the bound
+    // stops the walk on a malformed hierarchy (reference tie rule with repeated
+    // codes can create cycles).
+    long long pops = 0;
+    const long long max_pops = 2LL * n;
+    while (sc > 0) {
+        if (++pops > max_pops) {
+            flags |= SX_STATUS_STACK_OVERFLOW;
+            break;
+        }
+        const int idx = stack[--sc];
+        if (!overlap(a, b, mk(nmin4[idx]), mk(nmax4[idx]))) continue;
+        if (idx >= n - 1) {
+            if (count < cap) out[count] = sorted_ids[idx - (n - 1)];
+            ++count;
+        } else {
+            const int l = child_a[idx], r = child_b[idx];
+            if (sc < 64) stack[sc++] = l; else flags |= SX_STATUS_STACK_OVERFLOW;
+            if (sc < 64) stack[sc++] = r; else flags |= SX_STATUS_STACK_OVERFLOW;
+        }
+    }
+    num[q] = count;
+    if (count > cap) flags |= SX_STATUS_CAND_OVERFLOW;
+    if (flags) atomicOr(status, flags);
+}
+
+}  // namespace sx
+
+using namespace sx;
+
+// ---- workspace layouts --------------------------------------------------------
+// cell BVH: [keys F][radix ws F][flags NC] ; init uses [codes NC][radix ws NC]
+extern "C" size_t sx_radix_sort_workspace_bytes(int n) { return rs_ws_bytes(n); }
+
+extern "C" size_t sx_cell_bvh_workspace_bytes(int n_faces) {
+    size_t build = align256((size_t)(n_faces > 0 ? n_faces : 1) * 4) + rs_ws_bytes(n_faces) +
+                   align256((size_t)kNumCells * 4);
+    size_t init = align256((size_t)kNumCells * 4) + rs_ws_bytes(kNumCells);
+    return build > init ? build : init;
+}
+
+extern "C" int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, void* ws, size_t ws_bytes,
+                                   void* stream) {
+    SX_REQUIRE(n >= 0, "sx_radix_sort_pairs: n < 0");
+    if (n <= 1) return SX_OK;
+    SX_REQUIRE(keys && vals, "sx_radix_sort_pairs: null pointer");
+    return radix_sort(keys, vals, n, bits, ws, ws_bytes, as_stream(stream));
+}
+
+extern "C" int sx_face_morton(const float* fmin4, const float* fmax4, int n_faces, const float* box6,
+                              unsigned* codes, int* ids, void* stream) {
+    SX_REQUIRE(n_faces >= 0, "sx_face_morton: n_faces < 0");
+    if (n_faces == 0) return SX_OK;
+    SX_REQUIRE(fmin4 && fmax4 && box6 && codes && ids, "sx_face_morton: null pointer");
+    launch(face_morton_kernel, grid_for(n_faces, 256), 256, 0, as_stream(stream), 
+        n_faces, (const float4*)fmin4, (const float4*)fmax4, box6, codes, ids);
+    return check_launch("face_morton_kernel");
+}
+
+extern "C" int sx_karras_build(const unsigned* codes, int n, int tie, int* child_a, int* child_b, int* range_l,
+                               int* range_r, int* parent, void* stream) {
+    SX_REQUIRE(n >= 1, "sx_karras_build: n must be >= 1");
+    SX_REQUIRE(codes && parent && (n == 1 || (child_a && child_b && range_l && range_r)),
+               "sx_karras_build: null pointer");
+    launch(karras_kernel, grid_for(n, 256), 256, 0, as_stream(stream), n, codes, tie ? 1 : 0, child_a, child_b,
+                                                                    range_l, range_r, parent);
+    return check_launch("karras_kernel");
+}
+
+extern "C" int sx_cell_bvh_init(int* sorted_codes, int* sorted_ids, int* child_a, int* child_b, int* range_l,
+                                int* range_r, int* parent, void* ws, size_t ws_bytes, void* stream) {
+    SX_REQUIRE(sorted_codes && sorted_ids && child_a && child_b && range_l && range_r && parent,
+               "sx_cell_bvh_init: null pointer");
+    SX_REQUIRE(ws && ws_bytes >= sx_cell_bvh_workspace_bytes(0), "sx_cell_bvh_init: workspace too small");
+    cudaStream_t s = as_stream(stream);
+    launch(cell_morton_kernel, grid_for(kNumCells, 256), 256, 0, s, (unsigned*)sorted_codes, sorted_ids);
+    int rc = check_launch("cell_morton_kernel");
+    if (rc) return rc;
+    rc = radix_sort((unsigned*)sorted_codes, sorted_ids, kNumCells, 30, ws, ws_bytes, s);
+    if (rc) return rc;
+    launch(karras_kernel, grid_for(kNumCells, 256), 256, 0, s, kNumCells, (const unsigned*)sorted_codes, 0, child_a,
+                                                           child_b, range_l, range_r, parent);
+    return check_launch("karras_kernel(cells)");
+}
+
+extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_faces, const float* box6,
+                                 const int* child_a, const int* child_b, const int* parent, int* sorted_face_ids,
+                                 int* prefix, int* num_faces, float* nmin4, float* nmax4, float* cell_size3,
+                                 void* ws, size_t ws_bytes, void* stream) {
+    SX_REQUIRE(n_faces >= 0, "sx_cell_bvh_build: n_faces < 0");
+    SX_REQUIRE(box6 && child_a && child_b && parent && prefix && num_faces && nmin4 && nmax4 && cell_size3,
+               "sx_cell_bvh_build: null pointer");
+    SX_REQUIRE(n_faces == 0 || (fmin4 && fmax4 && sorted_face_ids), "sx_cell_bvh_build: null face arrays");
+    SX_REQUIRE(ws && ws_bytes >= sx_cell_bvh_workspace_bytes(n_faces), "sx_cell_bvh_build: workspace too small");
+    cudaStream_t s = as_stream(stream);
+    char* p = (char*)ws;
+    unsigned* keys = (unsigned*)p;
+    p += align256((size_t)(n_faces > 0 ? n_faces : 1) * 4);
+    void* rws = p;
+    p += rs_ws_bytes(n_faces);
+    int* flags = (int*)p;
+    SX_CUDA(cudaMemsetAsync(prefix, 0, sizeof(int) * kNumCells, s));
+    SX_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * kNumCells, s));
+    launch(face_cell_kernel, grid_for(n_faces, 256), 256, 0, s, n_faces, (const float4*)fmin4, (const float4*)fmax4,
+                                                            box6, keys, sorted_face_ids, (unsigned*)prefix,
+                                                            cell_size3);
+    int rc = check_launch("face_cell_kernel");
+    if (rc) return rc;
+    launch(scan_single_block, 1, 1024, 0, s, (unsigned*)prefix, kNumCells, 1);
+    if (n_faces > 1) {
+        rc = radix_sort(keys, sorted_face_ids, n_faces, 15, rws, rs_ws_bytes(n_faces), s);
+        if (rc) return rc;
+    }
+    // the status word lives in the flags scratch tail (flags[NC-1] is never a node)
+    int* status = flags + (kNumCells - 1);
+    launch(cell_leaf_refit_kernel, grid_for(kNumCells, 256), 256, 0, s, 
+        box6, prefix, sorted_face_ids, (const float4*)fmin4, (const float4*)fmax4, child_a, child_b, parent,
+        num_faces, (float4*)nmin4, (float4*)nmax4, flags, status);
+    return check_launch("cell_leaf_refit_kernel");
+}
+
+extern "C" int sx_cell_bvh_traverse(const float* p4, int n_queries, float padding, const float* cell_size3,
+                                    const float* origin_box6, const int* child_a, const int* child_b,
+                                    const int* num_faces, const float* nmin4, const float* nmax4, const int* prefix,
+                                    const int* sorted_face_ids, const float* fmin4, const float* fmax4, int cap,
+                                    int* cand, int* num, int* status, void* stream) {
+    SX_REQUIRE(n_queries >= 0 && cap >= 1, "sx_cell_bvh_traverse: bad sizes");
+    if (n_queries == 0) return SX_OK;
+    SX_REQUIRE(p4 && cell_size3 && origin_box6 && child_a && child_b && num_faces && nmin4 && nmax4 && prefix &&
+                   sorted_face_ids && fmin4 && fmax4 && cand && num && status,
+               "sx_cell_bvh_traverse: null pointer");
+    launch(cell_traverse_kernel, grid_for(n_queries, 128), 128, 0, as_stream(stream), 
+        n_queries, (const float4*)p4, padding, cell_size3, origin_box6, child_a, child_b, num_faces,
+        (const float4*)nmin4, (const float4*)nmax4, prefix, sorted_face_ids, (const float4*)fmin4,
+        (const float4*)fmax4, cap, cand, num, status);
+    return check_launch("cell_traverse_kernel");
+}
+
+extern "C" int sx_face_bvh_refit(int n, const int* sorted_ids, const float* fmin4, const float* fmax4,
+                                 const int* child_a, const int* child_b, const int* parent, float* nmin4,
+                                 float* nmax4, int* flags, int* status, void* stream) {
+    SX_REQUIRE(n >= 1, "sx_face_bvh_refit: n must be >= 1");
+    SX_REQUIRE(sorted_ids && fmin4 && fmax4 && parent && nmin4 && nmax4 && status &&
+                   (n == 1 || (child_a && child_b && flags)),
+               "sx_face_bvh_refit: null pointer");
+    launch(face_refit_kernel, grid_for(n, 256), 256, 0, as_stream(stream), 
+        n, sorted_ids, (const float4*)fmin4, (const float4*)fmax4, child_a, child_b, parent, (float4*)nmin4,
+        (float4*)nmax4, flags, status);
+    return check_launch("face_refit_kernel");
+}
+
+extern "C" int sx_face_bvh_traverse(int n, const float* p4, int n_queries, float padding, const int* child_a,
+                                    const int* child_b, const int* sorted_ids, const float* nmin4,
+                                    const float* nmax4, int cap, int* cand, int* num, int* status, void* stream) {
+    SX_REQUIRE(n >= 1 && n_queries >= 0 && cap >= 1, "sx_face_bvh_traverse: bad sizes");
+    if (n_queries == 0) return SX_OK;
+    SX_REQUIRE(p4 && sorted_ids && nmin4 && nmax4 && cand && num && status && (n == 1 || (child_a && child_b)),
+               "sx_face_bvh_traverse: null pointer");
+    launch(face_traverse_kernel, grid_for(n_queries, 128), 128, 0, as_stream(stream), 
+        n, n_queries, (const float4*)p4, padding, child_a, child_b, sorted_ids, (const float4*)nmin4,
+        (const float4*)nmax4, cap, cand, num, status);
+    return check_launch("face_traverse_kernel");
+}

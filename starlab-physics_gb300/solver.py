@@ -1,0 +1,214 @@
+"""XPBD cloth solver (mirrors ``framework/physics/XPBD.py`` class ``Solver``).
+
+Same constructor arguments, attributes and methods as the reference
+(``XPBD.py:9-106``): ``dt, dHat, damping, mu, padding,
+enable_collision_handling, enable_velocity_update``; ``forward(n_substeps)``,
+``reset()``, ``set_fixed_vertices(mask)``.  Each substep runs on the GPU through
+the starxpbd C ABI on the current torch stream; nothing is read back to the
+host inside :meth:`forward`.
+
+Options beyond the reference (keyword-only, defaults reproduce the reference):
+
+* ``n_iter`` -- Jacobi iterations per substep.  Each iteration is the
+  reference's ``solve_constraints_jacobi_x`` (spring/bending sweep + update, and
+  with collisions a contact sweep + update); the broad phase runs in the first
+  iteration only and its candidate lists are reused by later iterations.
+* ``rebuild`` -- ``"frame"`` builds both cell BVHs on ``x`` once per
+  :meth:`forward` call (``XPBD.py:448-458``); ``"substep"`` rebuilds them on ``x``
+  at the start of every substep.
+* ``bending_on`` -- ``"x"`` evaluates bending pairs on the start-of-substep
+  positions as the reference does (``XPBD.py:169``); ``"y"`` evaluates them on
+  the current iterate.  With ``n_iter > 1``, ``"x"`` re-applies the same bending
+  correction in every iteration, which diverges for stiff bending; iterated
+  solves use ``"y"``.
+* ``cap`` -- candidate / pair list capacity per query (the reference's 40,
+  ``XPBD.py:51``).  Longer lists are truncated and flagged in :attr:`status`.
+
+Reference quirks kept on purpose: the stretch springs use
+``stiffness_bending * dt^2`` and the bending pairs ``stiffness_stretch * dt^2``
+(``XPBD.py:354-355``); bending reads ``x`` not ``y`` (``XPBD.py:169``); ``dHat``
+is compared with squared distances; the collision compliance is the constant
+``1e8`` (``XPBD.py:367``).
+"""
+from __future__ import annotations
+
+import torch
+
+from ._lib import ptr, stream_handle, sx
+from .lbvh import LBVH_CELL
+
+
+class Solver:
+    def __init__(self, mesh_dy, mesh_st, dHat, stiffness_stretch, stiffness_bending, g, dt, *, n_iter: int = 1,
+                 rebuild: str = "frame", cap: int = 40, record_pairs: bool = False, bending_on: str = "x"):
+        if rebuild not in ("frame", "substep"):
+            raise ValueError("rebuild must be 'frame' or 'substep'")
+        if bending_on not in ("x", "y"):
+            raise ValueError("bending_on must be 'x' or 'y'")
+        if n_iter < 1:
+            raise ValueError("n_iter must be >= 1")
+        self.mesh_dy = mesh_dy
+        self.mesh_st = mesh_st
+        self.g = tuple(float(c) for c in g)
+        self.dt = float(dt)
+        self.dHat = float(dHat)
+        self.stiffness_stretch = float(stiffness_stretch)
+        self.stiffness_bending = float(stiffness_bending)
+        self.damping = 0.001
+        self.mu = 0.8
+        self.padding = 0.05
+        self.enable_velocity_update = False
+        self.enable_collision_handling = False
+        self.n_iter = int(n_iter)
+        self.rebuild = rebuild
+        self.compliance_collision = 1e8
+        self.bending_on = bending_on
+
+        self.max_num_verts_dy = mesh_dy.num_verts
+        self.max_num_edges_dy = mesh_dy.num_edges
+        self.max_num_faces_dy = mesh_dy.num_faces
+        self.max_num_verts_st = mesh_st.num_verts if mesh_st is not None else 0
+        self.max_num_edges_st = mesh_st.num_edges if mesh_st is not None else 0
+        self.max_num_faces_st = mesh_st.num_faces if mesh_st is not None else 0
+
+        dev = mesh_dy.device
+        self.device = dev
+        self.lbvh_dy = LBVH_CELL(mesh_dy.num_faces, dev)
+        self.lbvh_st = LBVH_CELL(mesh_st.num_faces, dev) if mesh_st is not None else None
+
+        Vd, Vs = self.max_num_verts_dy, self.max_num_verts_st
+        self.cache_size = int(cap)
+        i32 = dict(dtype=torch.int32, device=dev)
+        self.vt_st_candidates = torch.zeros((Vd, cap), **i32)
+        self.vt_st_candidates_num = torch.zeros(Vd, **i32)
+        self.vt_dy_candidates = torch.zeros((Vd, cap), **i32)
+        self.vt_dy_candidates_num = torch.zeros(Vd, **i32)
+        self.tv_st_candidates = torch.zeros((max(Vs, 1), cap), **i32)
+        self.tv_st_candidates_num = torch.zeros(max(Vs, 1), **i32)
+        self.status = torch.zeros(1, **i32)
+        self._dx_fix = torch.zeros(3 * Vd, dtype=torch.int64, device=dev)
+        self._nc = torch.zeros(Vd, **i32)
+        self._y_other = torch.zeros_like(mesh_dy.y4)
+        self.record_pairs = record_pairs
+        if record_pairs:
+            Q = 2 * Vd + Vs
+            self.pair = torch.zeros((Q, cap, 2), **i32)
+            self.pair_g = torch.zeros((Q, cap, 4, 4), dtype=torch.float32, device=dev)
+            self.pair_schur = torch.zeros((Q, cap), dtype=torch.float32, device=dev)
+            self.pair_num = torch.zeros(Q, **i32)
+        else:
+            self.pair = self.pair_g = self.pair_schur = self.pair_num = None
+
+    # -- reference surface ------------------------------------------------------
+    def reset(self):
+        """``Solver.reset`` (XPBD.py:108-112)."""
+        self.mesh_dy.reset()
+        if self.mesh_st is not None:
+            self.mesh_st.reset()
+
+    def set_fixed_vertices(self, fixed_vertices):
+        """``Solver.set_fixed_vertices`` (XPBD.py:390-395): ``fixed = 0`` where the
+        mask is >= 1 (pinned), else 1."""
+        m = torch.as_tensor(fixed_vertices, device=self.device)
+        self.mesh_dy.fixed.copy_(torch.where(m >= 1, 0.0, 1.0).to(torch.float32))
+        self.mesh_dy.refresh_weights()
+
+    def compute_y(self, dt):
+        """XPBD.py:116-118."""
+        m = self.mesh_dy
+        g = self.g
+        sx.sx_predict(ptr(m.x4), ptr(m.v4), ptr(m.fixed), ptr(m.y4), m.num_verts, float(dt), g[0], g[1], g[2],
+                      stream_handle())
+
+    def spring_sweep(self, dt):
+        """init_variables + solve_spring_constraints_x + update_dx
+        (XPBD.py:345-348, :141-184, :384-387); ping-pongs ``y``."""
+        m = self.mesh_dy
+        k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
+        k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
+        sx.sx_jacobi_sweep(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj),
+                           m.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0, stream_handle())
+        self._swap_y()
+
+    def _swap_y(self):
+        m = self.mesh_dy
+        m.y4, self._y_other = self._y_other, m.y4
+        m.verts.y = m.y4[:, :3]
+
+    def build_bvhs(self):
+        """XPBD.py:448-458: face AABBs and scene box on ``x``, then both builds."""
+        m = self.mesh_dy
+        m.computeAABB_faces(self.padding)
+        m.computeAABB(self.padding)
+        self.lbvh_dy.build(m, m.box6)
+        if self.mesh_st is not None:
+            s = self.mesh_st
+            s.computeAABB_faces(self.padding)
+            s.computeAABB(self.padding)
+            self.lbvh_st.build(s, s.box6)
+
+    def broadphase_lbvh(self):
+        """XPBD.py:187-215: three query sets."""
+        m = self.mesh_dy
+        cap = self.cache_size
+        if self.mesh_st is not None:
+            self.lbvh_st.traverse(m.y4, self.padding, cap, self.vt_st_candidates, self.vt_st_candidates_num,
+                                  self.status)
+            self.lbvh_dy.traverse(self.mesh_st.x4, self.padding, cap, self.tv_st_candidates,
+                                  self.tv_st_candidates_num, self.status)
+        self.lbvh_dy.traverse(m.y4, self.padding, cap, self.vt_dy_candidates, self.vt_dy_candidates_num,
+                              self.status)
+
+    def solve_collision_constraints_x(self, compliance_col=None):
+        """XPBD.py:237-264 followed by update_dx (XPBD.py:384-387)."""
+        m = self.mesh_dy
+        s = self.mesh_st
+        c = self.compliance_collision if compliance_col is None else compliance_col
+        sx.sx_collision_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(m.face_indices),
+                              ptr(s.face_indices) if s is not None else None, ptr(m.y4),
+                              ptr(s.x4) if s is not None else None, ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c),
+                              self.cache_size, ptr(self.vt_st_candidates), ptr(self.vt_st_candidates_num),
+                              ptr(self.vt_dy_candidates), ptr(self.vt_dy_candidates_num),
+                              ptr(self.tv_st_candidates), ptr(self.tv_st_candidates_num), ptr(self._dx_fix),
+                              ptr(self._nc), ptr(self.pair), ptr(self.pair_g), ptr(self.pair_schur),
+                              ptr(self.pair_num), ptr(self.status), stream_handle())
+
+    def solve_constraints_jacobi_x(self, dt, first_iteration: bool = True):
+        """XPBD.py:350-369 (broad phase only in the first iteration of a substep)."""
+        self.spring_sweep(dt)
+        if self.enable_collision_handling:
+            if self.mesh_st is None:
+                # the reference always has a static mesh when collisions are on
+                self.vt_st_candidates_num.zero_()
+            if first_iteration:
+                self.broadphase_lbvh()
+            self.solve_collision_constraints_x()
+
+    def compute_velocity_update_x(self, dt):
+        """compute_velocity (XPBD.py:341-343) then update_x (XPBD.py:333-337)."""
+        m = self.mesh_dy
+        sx.sx_velocity_update(ptr(m.x4), ptr(m.y4), ptr(m.v4), ptr(m.fixed), m.num_verts, self.damping, float(dt),
+                              stream_handle())
+
+    def substep(self, dt_sub):
+        if self.enable_collision_handling and self.rebuild == "substep":
+            self.build_bvhs()
+        self.compute_y(dt_sub)
+        for it in range(self.n_iter):
+            self.solve_constraints_jacobi_x(dt_sub, first_iteration=(it == 0))
+        if self.enable_velocity_update:
+            raise NotImplementedError("the velocity-level contact pass is not part of this build")
+        self.compute_velocity_update_x(dt_sub)
+
+    def forward(self, n_substeps: int):
+        """``Solver.forward`` (XPBD.py:443-469)."""
+        dt_sub = self.dt / n_substeps
+        if self.enable_collision_handling and self.rebuild == "frame":
+            self.build_bvhs()
+        for _ in range(n_substeps):
+            self.substep(dt_sub)
+
+    # -- diagnostics ---------------------------------------------------------------
+    def status_flags(self) -> int:
+        """Accumulated device status bits (host sync)."""
+        return int(self.status.item())

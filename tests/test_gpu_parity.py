@@ -1,0 +1,277 @@
+"""GPU parity: every CUDA entry point against the CPU oracle, through the C ABI.
+
+Integer outputs (Morton codes, sort order, BVH topology, candidate lists,
+colourings) must match bit for bit.  Float outputs are compared bit for bit as
+well: kernels and oracle evaluate the same expressions in the same order with
+no FMA contraction, so any difference is a bug.  End-to-end solver runs are
+additionally held to the benchmark spec's tolerance 1e-4 x bounding-box diagonal.
+"""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+DEV = "cuda"
+
+
+def _t(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).to(DEV)
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.fixture(scope="module")
+def sxm(pkg):
+    from starlab_physics_gb300 import _lib
+
+    _lib.load()
+    return _lib
+
+
+def _cloth(pkg, n=16, seed=3, pinned=True):
+    sc = pkg.scenes.plain64(n=n, seed=seed)
+    m = pkg.TriMesh(sc.cloth_x, sc.cloth_faces, device=DEV)
+    if pinned:
+        m.fixed[sc.pinned] = 0.0
+        m.refresh_weights()
+    return sc, m
+
+
+def _state(m, rng):
+    V = m.num_verts
+    x4 = _np(m.x4).copy()
+    x4[:, :3] += rng.normal(0, 2e-3, (V, 3)).astype(np.float32)
+    v4 = np.zeros((V, 4), np.float32)
+    v4[:, :3] = rng.normal(0, 0.3, (V, 3)).astype(np.float32)
+    return x4, v4
+
+
+def test_predict_sweep_velocity_bit_exact(pkg, po, sxm):
+    sc, m = _cloth(pkg)
+    rng = np.random.default_rng(0)
+    x4, v4 = _state(m, rng)
+    fixed = _np(m.fixed)
+    m_inv = _np(m.m_inv)
+    dt = 1.0 / 600.0
+    g = (0.0, 0.0, -9.81)
+    s = torch.cuda.current_stream().cuda_stream
+    X, Vv, Y, Y2 = _t(x4), _t(v4), torch.empty_like(m.x4), torch.empty_like(m.x4)
+    sxm.sx.sx_predict(X.data_ptr(), Vv.data_ptr(), m.fixed.data_ptr(), Y.data_ptr(), m.num_verts, dt, *g, s)
+    y_ref = po.predict(x4, v4, fixed, dt, g)
+    assert np.array_equal(_np(Y), y_ref)
+    for bend_on_y in (0, 1):
+        yin = _t(y_ref)
+        ks, kb = 1e8 * dt * dt, 1e5 * dt * dt
+        sxm.sx.sx_jacobi_sweep(X.data_ptr(), yin.data_ptr(), Y2.data_ptr(), m.fixed.data_ptr(),
+                               m.adj_ptr.data_ptr(), m.adj.data_ptr(), m.num_verts, ks, kb, bend_on_y, s)
+        yo = y_ref.copy()
+        po.spring_sweep(x4, yo, fixed, m_inv, m.eid_np, m.l0_np, m.bending_np, m.bending_l0_np, ks, kb,
+                        bend_on_y=bend_on_y)
+        got = _np(Y2)
+        assert np.array_equal(got[:, :3], yo[:, :3]), f"bend_on_y={bend_on_y} max diff {np.abs(got - yo).max()}"
+    xo, vo = x4.copy(), v4.copy()
+    po.velocity_update(xo, yo, vo, fixed, 0.001, dt)
+    Yt = _t(yo)
+    sxm.sx.sx_velocity_update(X.data_ptr(), Yt.data_ptr(), Vv.data_ptr(), m.fixed.data_ptr(), m.num_verts, 0.001,
+                              dt, s)
+    assert np.array_equal(_np(X)[:, :3], xo[:, :3])
+    assert np.array_equal(_np(Vv)[:, :3], vo[:, :3])
+
+
+def test_aabbs(pkg, po, sxm):
+    sc, m = _cloth(pkg, n=20)
+    x4 = _np(m.x4)
+    m.computeAABB_faces(0.01)
+    mn, mx = po.face_aabbs(x4, m.fid_np, 0.01)
+    assert np.array_equal(_np(m.aabb_min4), mn) and np.array_equal(_np(m.aabb_max4), mx)
+    m.computeAABB(0.02)
+    assert np.array_equal(_np(m.box6), po.scene_aabb(x4, 0.02))
+
+
+@pytest.mark.parametrize("n,bits", [(1, 30), (7, 30), (2047, 30), (2048, 30), (2049, 15), (100003, 32),
+                                    (65536, 8), (300000, 30)])
+def test_radix_sort(pkg, sxm, n, bits):
+    rng = np.random.default_rng(n)
+    hi = (1 << bits) if bits < 32 else (1 << 32)
+    keys = rng.integers(0, hi, n, dtype=np.uint64).astype(np.uint32)
+    if n > 10:
+        keys[: n // 3] = keys[n // 3: 2 * (n // 3)]  # many duplicates: stability matters
+    vals = np.arange(n, dtype=np.int32)
+    K, Vt = _t(keys.view(np.int32)), _t(vals)
+    ws = torch.empty(int(sxm.load().sx_radix_sort_workspace_bytes(n)), dtype=torch.uint8, device=DEV)
+    sxm.sx.sx_radix_sort_pairs(K.data_ptr(), Vt.data_ptr(), n, bits, ws.data_ptr(), ws.numel(),
+                               torch.cuda.current_stream().cuda_stream)
+    order = np.argsort(keys, kind="stable")
+    assert np.array_equal(_np(Vt), order)
+    assert np.array_equal(_np(K).view(np.uint32), keys[order])
+
+
+def test_cell_bvh_init(pkg, po):
+    bvh = pkg.LBVH_CELL(10, DEV)
+    ref = po.CellBVH()
+    assert np.array_equal(_np(bvh.cell_morton_codes), ref.codes)
+    assert np.array_equal(_np(bvh.cell_ids), ref.ids)
+    for a, b in [(bvh.child_a, ref.child_a), (bvh.child_b, ref.child_b), (bvh.range_l, ref.range_l),
+                 (bvh.range_r, ref.range_r), (bvh.parent, ref.parent)]:
+        assert np.array_equal(_np(a), b)
+
+
+def _drape(pkg, n=48):
+    sc = pkg.scenes.drape256(n=n, sphere_subdiv=3)
+    cl = pkg.TriMesh(sc.cloth_x, sc.cloth_faces, device=DEV)
+    sp = pkg.TriMesh(sc.obstacle_x, sc.obstacle_faces, device=DEV, is_static=True)
+    return sc, cl, sp
+
+
+def test_cell_bvh_build_and_traverse(pkg, po):
+    sc, cl, sp = _drape(pkg)
+    pad = 0.01
+    for mesh in (cl, sp):
+        mesh.computeAABB_faces(pad)
+        mesh.computeAABB(pad)
+        bvh = pkg.LBVH_CELL(mesh.num_faces, DEV)
+        bvh.build(mesh, mesh.box6)
+        ref = po.CellBVH()
+        ref.build(_np(mesh.aabb_min4), _np(mesh.aabb_max4), _np(mesh.box6))
+        assert np.array_equal(_np(bvh.prefix_sum_cell), ref.prefix)
+        assert np.array_equal(_np(bvh.sorted_face_ids)[: mesh.num_faces], ref.sorted_face_ids)
+        assert np.array_equal(_np(bvh.num_faces), ref.num_faces)
+        assert np.array_equal(_np(bvh.node_min4), ref.nmin4)
+        assert np.array_equal(_np(bvh.node_max4), ref.nmax4)
+        assert np.array_equal(_np(bvh.cell_size), ref.cell_size)
+        # queries: the cloth vertices
+        pts = _np(cl.x4).copy()
+        pts[:, :3] += np.random.default_rng(1).normal(0, 0.01, (pts.shape[0], 3)).astype(np.float32)
+        P = _t(pts)
+        cap = 40
+        cand = torch.full((pts.shape[0], cap), -1, dtype=torch.int32, device=DEV)
+        num = torch.zeros(pts.shape[0], dtype=torch.int32, device=DEV)
+        status = torch.zeros(1, dtype=torch.int32, device=DEV)
+        bvh.traverse(P, pad, cap, cand, num, status)
+        qmn, qmx = po.query_boxes(pts, pad)
+        rc, rn, rs = ref.traverse(qmn, qmx, cap)
+        gn = _np(num)
+        assert np.array_equal(gn, rn)
+        gc = _np(cand)
+        for q in range(pts.shape[0]):
+            k = min(rn[q], cap)
+            assert np.array_equal(gc[q, :k], rc[q, :k])
+        assert int(status.item()) == rs
+
+
+def test_face_lbvh_small_soup(pkg, po):
+    verts, faces, queries = pkg.scenes.triangle_soup(1 << 14, seed=5)
+    V4 = np.zeros((verts.shape[0], 4), np.float32)
+    V4[:, :3] = verts
+    mn, mx = po.face_aabbs(V4, faces, 0.0)
+    box = po.scene_aabb(V4, 0.0)
+    for tie in (0, 1):
+        bvh = pkg.LBVH(faces.shape[0], DEV, tie=tie)
+        bvh.build(_t(mn), _t(mx), _t(box))
+        ref = po.FaceBVH(mn, mx, box, tie=tie)
+        assert np.array_equal(_np(bvh.codes), ref.sorted_codes)
+        assert np.array_equal(_np(bvh.sorted_ids), ref.sorted_ids)
+        n = faces.shape[0]
+        assert np.array_equal(_np(bvh.child_a)[: n - 1], ref.child_a)
+        assert np.array_equal(_np(bvh.child_b)[: n - 1], ref.child_b)
+        assert np.array_equal(_np(bvh.range_l)[: n - 1], ref.range_l)
+        assert np.array_equal(_np(bvh.range_r)[: n - 1], ref.range_r)
+        if tie == 1 or len(np.unique(ref.sorted_codes)) == n:
+            assert np.array_equal(_np(bvh.parent), ref.parent)
+            assert np.array_equal(_np(bvh.node_min4), ref.nmin4)
+            assert np.array_equal(_np(bvh.node_max4), ref.nmax4)
+            Q = np.zeros((queries.shape[0], 4), np.float32)
+            Q[:, :3] = queries
+            cand, num = bvh.query(_t(Q), 2e-3, 64)
+            qmn, qmx = po.query_boxes(Q, 2e-3)
+            rc, rn, _ = ref.traverse(qmn, qmx, 64)
+            assert np.array_equal(_np(num), rn)
+            gc = _np(cand)
+            for q in range(0, Q.shape[0], 7):
+                k = min(rn[q], 64)
+                assert np.array_equal(gc[q, :k], rc[q, :k])
+
+
+def test_collision_sweep_bit_exact(pkg, po):
+    sc, cl, sp = _drape(pkg, n=40)
+    sim = pkg.Solver(cl, sp, dHat=(4e-2) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8, g=(0, 0, -9.81),
+                     dt=1 / 60, record_pairs=True)
+    sim.padding = 0.04
+    sim.enable_collision_handling = True
+    # squash the cloth onto the sphere so that many contacts are active
+    x = _np(cl.x4).copy()
+    x[:, 2] = 0.5 + 0.3 + 0.01 * np.sin(13 * x[:, 0]) * np.cos(7 * x[:, 1])
+    cl.x4.copy_(_t(x))
+    sim.build_bvhs()
+    sim.compute_y(1 / 600)
+    sim.broadphase_lbvh()
+    y_before = _np(cl.y4).copy()
+    cap = sim.cache_size
+    vt_st = (_np(sim.vt_st_candidates), _np(sim.vt_st_candidates_num))
+    vt_dy = (_np(sim.vt_dy_candidates), _np(sim.vt_dy_candidates_num))
+    tv_st = (_np(sim.tv_st_candidates), _np(sim.tv_st_candidates_num))
+    sim.solve_collision_constraints_x()
+    yo = y_before.copy()
+    r = po.collision_sweep(cl.fid_np, sp.fid_np, yo, _np(sp.x4), _np(cl.fixed), _np(cl.m_inv), np.float32(sim.dHat),
+                           np.float32(1e8), cap, vt_st, vt_dy, tv_st, want_pairs=True)
+    got = _np(cl.y4)
+    assert (r["pair_num"] > 0).sum() > 10, "test scene produced too few contacts"
+    assert np.array_equal(got[:, :3], yo[:, :3]), f"max diff {np.abs(got[:, :3] - yo[:, :3]).max()}"
+    assert np.array_equal(_np(sim.pair_num), r["pair_num"])
+    pn = r["pair_num"]
+    gp, gg, gs = _np(sim.pair), _np(sim.pair_g), _np(sim.pair_schur)
+    for q in np.flatnonzero(pn):
+        k = pn[q]
+        assert np.array_equal(gp[q, :k], r["pair"][q, :k])
+        assert np.array_equal(gg[q, :k], r["pair_g"][q, :k])
+        assert np.array_equal(gs[q, :k], r["pair_schur"][q, :k])
+    assert np.count_nonzero(_np(sim._dx_fix)) == 0 and np.count_nonzero(_np(sim._nc)) == 0
+
+
+def _run_pair(pkg, po, scene, frames, **solver_kw):
+    sim = pkg.scenes.make_solver(scene, device=DEV)
+    for k, v in solver_kw.items():
+        setattr(sim, k, v)
+    orc = po.OracleSolver(pkg.scenes.oracle_inputs(sim.mesh_dy),
+                          pkg.scenes.oracle_inputs(sim.mesh_st) if sim.mesh_st is not None else None,
+                          dt=scene.dt, g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
+                          k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
+                          padding=scene.padding, n_iter=scene.n_iter, collisions=scene.collisions,
+                          rebuild=scene.rebuild, cap=scene.cap, bending_on=sim.bending_on)
+    for _ in range(frames):
+        sim.forward(scene.n_substeps)
+        orc.forward(scene.n_substeps)
+    torch.cuda.synchronize()
+    return sim, orc
+
+
+@pytest.mark.parametrize("mode", ["reference", "iterated"])
+def test_solver_end_to_end(pkg, po, mode):
+    scene = pkg.scenes.plain64(n=24, seed=2)
+    if mode == "reference":
+        scene.n_iter, scene.rebuild, scene.padding = 1, "frame", 0.03
+        sim_kw = {}
+    else:
+        scene.n_iter = 4
+        sim_kw = {"bending_on": "y"}
+    sim, orc = _run_pair(pkg, po, scene, 6, **sim_kw)
+    gx = _np(sim.mesh_dy.x4)
+    diag = sim.mesh_dy.bbox_diagonal()
+    assert np.isfinite(gx).all()
+    diff = np.abs(gx[:, :3] - orc.x4[:, :3]).max()
+    assert diff <= 1e-4 * diag
+    assert np.array_equal(gx[:, :3], orc.x4[:, :3]), f"not bit-exact: max diff {diff}"
+
+
+def test_coloring(pkg, po):
+    for n in (9, 33):
+        x, f = pkg.grid_cloth(n)
+        e = pkg.mesh.edges_from_faces(f)
+        gc = pkg.GraphColoring(n * n, e, device=DEV)
+        color, sorted_e, prefix = po.color_edges(n * n, e)
+        assert np.array_equal(_np(gc.edges_color)[: e.shape[0]], color)
+        assert np.array_equal(_np(gc.sorted_edges_sequence_for_color)[: e.shape[0]], sorted_e)
+        assert np.array_equal(_np(gc.color_prefix_sum), prefix)
