@@ -95,20 +95,24 @@ int sx_cell_bvh_init(int* sorted_codes, int* sorted_ids, int* child_a, int* chil
  * AABB = centre U faces (assign_leaf_cell_nodes :602-634) and a single-launch
  * bottom-up refit with the rules of compute_cell_node_aabbs :491-522.
  * Outputs: sorted_face_ids[n_faces], prefix[32768] (inclusive),
- * num_faces[65535], nmin4/nmax4[65535], cell_size3[3]. */
+ * num_faces[65535], nmin4/nmax4[65535] (nmin4.w = the node's face count as
+ * int bits), face_rec8[8*n_faces] (per sorted face: min xyz + face id bits,
+ * max xyz + 0; what the traversal scans), cell_size3[3]. */
 int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_faces, const float* box6, const int* child_a,
                       const int* child_b, const int* parent, int* sorted_face_ids, int* prefix, int* num_faces,
-                      float* nmin4, float* nmax4, float* cell_size3, void* ws, size_t ws_bytes, void* stream);
+                      float* nmin4, float* nmax4, float* face_rec8, float* cell_size3, void* ws, size_t ws_bytes,
+                      void* stream);
 
 /* traverse_cell_bvh_single, lbvh_cell.py:656-714, for query boxes
- * p4[i] +- padding (Solver.broadphase_lbvh, XPBD.py:187-215).  origin = box6 of
- * the build (its min corner is the grid origin).  cand[q*cap + j] for j < cap;
- * num[q] = total overlaps found (num > cap: list truncated, status bit 1). */
+ * p4[i] +- padding (Solver.broadphase_lbvh, XPBD.py:187-215), over a build's
+ * nodes and face records.  origin = box6 of the build (its min corner is the
+ * grid origin).  cand[q*cap + j] for j < cap; num[q] = total overlaps found
+ * (num > cap: list truncated, status bit 1).  Candidates come out in the
+ * reference's visiting order. */
 int sx_cell_bvh_traverse(const float* p4, int n_queries, float padding, const float* cell_size3,
-                         const float* origin_box6, const int* child_a, const int* child_b, const int* num_faces,
-                         const float* nmin4, const float* nmax4, const int* prefix, const int* sorted_face_ids,
-                         const float* fmin4, const float* fmax4, int cap, int* cand, int* num, int* status,
-                         void* stream);
+                         const float* origin_box6, const int* child_a, const int* child_b, const float* nmin4,
+                         const float* nmax4, const int* prefix, const float* face_rec8, int cap, int* cand, int* num,
+                         int* status, void* stream);
 
 /* ---- face-level LBVH (standalone broad phase) ------------------------------ */
 
@@ -161,6 +165,24 @@ int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const int* faces
                        const int* vt_st_cand, const int* vt_st_num, const int* vt_dy_cand, const int* vt_dy_num,
                        const int* tv_st_cand, const int* tv_st_num, long long* dx_fix, int* nc, int* pair,
                        float* pair_g, float* pair_schur, int* pair_num, int* status, void* stream);
+
+/* The same contact projection over a dense pair list.  The candidate lists do
+ * not change between the Jacobi iterations of a substep (the broad phase runs
+ * once per substep), so sx_contact_pairs_build flattens them once -- in query
+ * order, dropping the incident faces __vt_dy skips (XPBD.py:258) -- into
+ * pairs[max_pairs] (int4: query vertex, triangle vertices;
+ * max_pairs >= (2*n_dy + n_st) * cap), and sx_contact_pairs_sweep then runs
+ * one thread per pair followed by update_dx.  Same arithmetic and the same
+ * order-independent accumulation as sx_collision_sweep, hence the same result;
+ * pair records are only available from sx_collision_sweep. */
+size_t sx_contact_pairs_workspace_bytes(int n_dy, int n_st);
+int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* faces_st, int cap,
+                           const int* vt_st_cand, const int* vt_st_num, const int* vt_dy_cand, const int* vt_dy_num,
+                           const int* tv_st_cand, const int* tv_st_num, int* pairs, long long max_pairs, void* ws,
+                           size_t ws_bytes, void* stream);
+int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4, const float* xs4,
+                           const float* fixed, const float* m_inv, float dHat, float compliance, long long* dx_fix,
+                           int* nc, int* status, void* stream);
 
 /* ---- constraint-graph colouring (framework/utilities/graph_coloring.py) --- */
 

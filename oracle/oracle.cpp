@@ -453,7 +453,8 @@ API int or_cell_bvh_build(int F, const float* mn4, const float* mx4, const float
             a = vmin(a, v3(mn4 + 4 * fid));
             b = vmax(b, v3(mx4 + 4 * fid));
         }
-        nmin4[4 * leaf] = a.x; nmin4[4 * leaf + 1] = a.y; nmin4[4 * leaf + 2] = a.z; nmin4[4 * leaf + 3] = 0.f;
+        nmin4[4 * leaf] = a.x; nmin4[4 * leaf + 1] = a.y; nmin4[4 * leaf + 2] = a.z;
+        std::memcpy(nmin4 + 4 * leaf + 3, &size, 4);  // node layout: min.w = face count (int bits)
         nmax4[4 * leaf] = b.x; nmax4[4 * leaf + 1] = b.y; nmax4[4 * leaf + 2] = b.z; nmax4[4 * leaf + 3] = 0.f;
         visited[parent[leaf]] += 1;
     }
@@ -469,7 +470,8 @@ API int or_cell_bvh_build(int F, const float* mn4, const float* mx4, const float
             else if (num_faces[l] > 0) { a = min0; b = max0; }
             else if (num_faces[r] > 0) { a = min1; b = max1; }
             else { a = scale(0.25f, add(add(add(min0, max0), min1), max1)); b = a; }
-            nmin4[4 * i] = a.x; nmin4[4 * i + 1] = a.y; nmin4[4 * i + 2] = a.z; nmin4[4 * i + 3] = 0.f;
+            nmin4[4 * i] = a.x; nmin4[4 * i + 1] = a.y; nmin4[4 * i + 2] = a.z;
+            std::memcpy(nmin4 + 4 * i + 3, &num_faces[i], 4);
             nmax4[4 * i] = b.x; nmax4[4 * i + 1] = b.y; nmax4[4 * i + 2] = b.z; nmax4[4 * i + 3] = 0.f;
             int p = parent[i];
             visited[i] += 1;

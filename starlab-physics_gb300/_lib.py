@@ -41,8 +41,8 @@ SIGNATURES = {
     "sx_scene_aabb": ([P, I, F, P, P], I),
     "sx_cell_bvh_workspace_bytes": ([I], Z),
     "sx_cell_bvh_init": ([P, P, P, P, P, P, P, P, Z, P], I),
-    "sx_cell_bvh_build": ([P, P, I, P, P, P, P, P, P, P, P, P, P, P, Z, P], I),
-    "sx_cell_bvh_traverse": ([P, I, F, P, P, P, P, P, P, P, P, P, P, P, I, P, P, P, P], I),
+    "sx_cell_bvh_build": ([P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, Z, P], I),
+    "sx_cell_bvh_traverse": ([P, I, F, P, P, P, P, P, P, P, P, I, P, P, P, P], I),
     "sx_face_morton": ([P, P, I, P, P, P, P], I),
     "sx_radix_sort_workspace_bytes": ([I], Z),
     "sx_radix_sort_pairs": ([P, P, I, I, P, Z, P], I),
@@ -50,6 +50,9 @@ SIGNATURES = {
     "sx_face_bvh_refit": ([I, P, P, P, P, P, P, P, P, P, P, P], I),
     "sx_face_bvh_traverse": ([I, P, I, F, P, P, P, P, P, I, P, P, P, P], I),
     "sx_collision_sweep": ([I, I, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P], I),
+    "sx_contact_pairs_workspace_bytes": ([I, I], Z),
+    "sx_contact_pairs_build": ([I, I, P, P, I, P, P, P, P, P, P, P, C.c_longlong, P, Z, P], I),
+    "sx_contact_pairs_sweep": ([I, I, P, P, P, P, P, P, F, F, P, P, P, P], I),
     "sx_color_workspace_bytes": ([I, I], Z),
     "sx_color_edges_greedy": ([P, I, I, I, P, P, P, P, Z, P], I),
 }

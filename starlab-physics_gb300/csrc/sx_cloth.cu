@@ -63,40 +63,72 @@ __global__ void predict_kernel(int V, const float4* __restrict__ x4, const float
 // dx -= (w_self*ld) * normalize(p_self - p_other) over its incident constraints
 // in ascending constraint index, which equals a serial run of the reference.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
+__global__ void __launch_bounds__(128) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
                                                            const float4* __restrict__ yin,
                                                            float4* __restrict__ yout,
                                                            const float* __restrict__ fixed,
                                                            const int* __restrict__ ptr,
                                                            const int2* __restrict__ adj, float ks, float kb,
                                                            int bend_y) {
-    int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= V) return;
-    const float4 ps = yin[v];
-    const float4 xs = x4[v];
-    float dx = 0.0f, dy = 0.0f, dz = 0.0f;
-    const int b = ptr[v], e = ptr[v + 1];
-    for (int k = b; k < e; ++k) {
-        const int2 a = __ldg(adj + k);
-        const bool bend = a.x < 0;
-        const int nb = a.x & 0x7fffffff;
-        const float rest = __int_as_float(a.y);
-        const bool use_x = bend && !bend_y;
-        const float4 self = use_x ? xs : ps;
-        const float4 other = use_x ? __ldg(x4 + nb) : yin[nb];
-        const float kk = bend ? kb : ks;
-        const float ex = self.x - other.x, ey = self.y - other.y, ez = self.z - other.z;
-        const float lij = sqrtf((ex * ex + ey * ey) + ez * ez);
-        const float C = lij - rest;
-        const float inv = 1.0f / lij;
-        const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
-        const float schur = (self.w + other.w) * ((nx * nx + ny * ny) + nz * nz);
-        const float ld = (kk * C) / (kk * schur + 1.0f);
-        const float a0 = self.w * ld;
-        dx = dx - a0 * nx;
-        dy = dy - a0 * ny;
-        dz = dz - a0 * nz;
+    // Four lanes per vertex: in round r lane j evaluates entry b + 4r + j, then
+    // every lane of the quad adds the four terms in ascending entry order
+    // (shuffles), so the sum is the serial one while the loads, square roots and
+    // divisions run four-wide.
+    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+    const int lane = threadIdx.x & 31;
+    const int j = gt & 3;
+    const int v = gt >> 2;
+    const bool valid = v < V;
+    float4 ps = make_float4(0.f, 0.f, 0.f, 0.f), xs = ps;
+    int b = 0, e = 0;
+    if (valid) {
+        ps = __ldg(yin + v);
+        xs = __ldg(x4 + v);
+        b = __ldg(ptr + v);
+        e = __ldg(ptr + v + 1);
     }
+    const int rounds = (e - b + 3) >> 2;
+    int rmax = rounds;
+    for (int o = 4; o < 32; o <<= 1) rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+    const int qbase = lane & ~3;
+    float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+    for (int r = 0; r < rmax; ++r) {
+        const int k = b + 4 * r + j;
+        float tx = 0.0f, ty = 0.0f, tz = 0.0f;
+        if (k < e) {
+            const int2 a = __ldg(adj + k);
+            const bool bend = a.x < 0;
+            const int nb = a.x & 0x7fffffff;
+            const float rest = __int_as_float(a.y);
+            const bool use_x = bend && !bend_y;
+            const float4 self = use_x ? xs : ps;
+            const float4 other = __ldg((use_x ? x4 : yin) + nb);
+            const float kk = bend ? kb : ks;
+            const float ex = self.x - other.x, ey = self.y - other.y, ez = self.z - other.z;
+            const float lij = sqrtf((ex * ex + ey * ey) + ez * ez);
+            const float C = lij - rest;
+            const float inv = 1.0f / lij;
+            const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
+            const float schur = (self.w + other.w) * ((nx * nx + ny * ny) + nz * nz);
+            const float ld = (kk * C) / (kk * schur + 1.0f);
+            const float a0 = self.w * ld;
+            tx = a0 * nx;
+            ty = a0 * ny;
+            tz = a0 * nz;
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+            const float sx_ = __shfl_sync(0xffffffffu, tx, qbase + u);
+            const float sy_ = __shfl_sync(0xffffffffu, ty, qbase + u);
+            const float sz_ = __shfl_sync(0xffffffffu, tz, qbase + u);
+            if (b + 4 * r + u < e) {
+                dx = dx - sx_;
+                dy = dy - sy_;
+                dz = dz - sz_;
+            }
+        }
+    }
+    if (!valid || j != 0) return;
     float4 out = ps;
     const float nc = (float)(e - b);
     if (nc > 0.0f) {
@@ -215,7 +247,7 @@ extern "C" int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out
     if (n_verts == 0) return SX_OK;
     SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj, "sx_jacobi_sweep: null pointer");
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep: y_in4 and y_out4 must not alias");
-    launch(jacobi_sweep_kernel, grid_for(n_verts, 256), 256, 0, as_stream(stream), 
+    launch(jacobi_sweep_kernel, grid_for(4LL * n_verts, 128), 128, 0, as_stream(stream), 
         n_verts, (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj,
         k_spring, k_bend, bend_on_y ? 1 : 0);
     return check_launch("jacobi_sweep_kernel");

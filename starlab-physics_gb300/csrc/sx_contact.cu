@@ -150,6 +150,90 @@ struct PairOut {
     }
 };
 
+// One candidate of each kind.  g receives the four gradients (zero where the
+// feature excludes a vertex); *schur_out the value the reference records.
+// __vt_st (collision_constraints_x.py:6-69): dynamic vertex y vs static triangle x
+__device__ __forceinline__ bool project_vt_st(int vid, V3 x0, V3 x1, V3 x2, V3 x3, float wv, float dHat,
+                                              float compliance, long long* dx, int* nc, int* bad, V3 g[4],
+                                              int* dtype, float* schur_out) {
+    const int dt = d_type_PT(x0, x1, x2, x3);
+    *dtype = dt;
+    const float d = pt_distance(dt, x0, x1, x2, x3, g, true, dHat);
+    if (d < dHat) {
+        const float schur = wv * dot(g[0], g[0]);
+        const float ld = (compliance * (dHat - d)) / (compliance * schur + 1.0f);
+        acc_add(dx, nc, vid, wv * ld, g[0], bad);  // no `fixed` factor (collision_constraints_x.py:58)
+        *schur_out = schur;
+        return true;
+    }
+    return false;
+}
+
+// __vt_dy (collision_constraints_x.py:176-310): self contact, all four on y
+__device__ __forceinline__ void project_vt_dy(const int vv[4], const V3 x[4], const float* __restrict__ fixed,
+                                              const float* __restrict__ m_inv, float dHat, long long* dx, int* nc,
+                                              int* bad, V3 g[4], int* dtype, float* schur_out) {
+    const int dt = d_type_PT(x[0], x[1], x[2], x[3]);
+    *dtype = dt;
+    const float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);
+    float schur = 0.0f;
+    if (d < dHat) {
+        pt_distance(dt, x[0], x[1], x[2], x[3], g, true, dHat);
+        const int m = region_mask(dt);
+        float s = 0.0f;
+        bool first = true;
+        for (int k = 0; k < 4; ++k) {
+            if (!(m & (1 << k))) continue;
+            const float t = (fixed[vv[k]] * m_inv[vv[k]]) * dot(g[k], g[k]);
+            s = first ? t : s + t;
+            first = false;
+        }
+        schur = s + 1e-4f;
+        const float ld = (dHat - d) / schur;
+        for (int k = 0; k < 4; ++k) {
+            if (!(m & (1 << k))) continue;
+            // region 0 applies m_inv without `fixed` (collision_constraints_x.py:199-200)
+            const float w = dt == 0 ? m_inv[vv[k]] : fixed[vv[k]] * m_inv[vv[k]];
+            acc_add(dx, nc, vv[k], w * ld, g[k], bad);
+        }
+    }
+    *schur_out = schur;
+}
+
+// __tv_st (collision_constraints_x.py:72-173): static vertex x vs dynamic triangle y
+__device__ __forceinline__ void project_tv_st(const int vv[4], const V3 x[4], const float* __restrict__ fixed,
+                                              const float* __restrict__ m_inv, float dHat, float compliance,
+                                              long long* dx, int* nc, int* bad, V3 g[4], int* dtype,
+                                              float* schur_out) {
+    const int dt = d_type_PT(x[0], x[1], x[2], x[3]);
+    *dtype = dt;
+    const float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);
+    float schur = 0.0f;
+    if (d < dHat) {
+        pt_distance(dt, x[0], x[1], x[2], x[3], g, true, dHat);
+        const int m = region_mask(dt) & ~1;
+        float s = 0.0f;
+        bool first = true;
+        for (int k = 1; k < 4; ++k) {
+            if (!(m & (1 << k))) continue;
+            const float t = (fixed[vv[k]] * m_inv[vv[k]]) * dot(g[k], g[k]);
+            s = first ? t : s + t;
+            first = false;
+        }
+        schur = s;
+        const float ld = (compliance * (dHat - d)) / (compliance * schur + 1.0f);
+        for (int k = 1; k < 4; ++k) {
+            if (!(m & (1 << k))) continue;
+            acc_add(dx, nc, vv[k], (fixed[vv[k]] * m_inv[vv[k]]) * ld, g[k], bad);
+        }
+    }
+    *schur_out = schur;
+}
+
+#define SX_ZERO_G {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}}
+
+// Candidate lists walked per query, in list order, as the reference does; the
+// only variant that can write pair records (their slot order is list order).
 __global__ void __launch_bounds__(128) collision_project_kernel(
     int Vd, int Vs, const int* __restrict__ faces_dy, const int* __restrict__ faces_st,
     const float4* __restrict__ y4, const float4* __restrict__ xs4, const float* __restrict__ fixed,
@@ -161,7 +245,7 @@ __global__ void __launch_bounds__(128) collision_project_kernel(
     if (i >= 2 * Vd + Vs) return;
     int bad = 0;
     int cnt = 0;
-    if (i < Vd) {  // __vt_st (collision_constraints_x.py:6-69)
+    if (i < Vd) {
         const int vid = i;
         const int n = min(vt_st_n[vid], cap);
         const V3 x0 = mk(y4[vid]);
@@ -170,18 +254,14 @@ __global__ void __launch_bounds__(128) collision_project_kernel(
             const int fs = vt_st_c[(size_t)vid * cap + j];
             const V3 x1 = mk(xs4[faces_st[3 * fs]]), x2 = mk(xs4[faces_st[3 * fs + 1]]),
                      x3 = mk(xs4[faces_st[3 * fs + 2]]);
-            V3 g[4] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-            const int dt = d_type_PT(x0, x1, x2, x3);
-            const float d = pt_distance(dt, x0, x1, x2, x3, g, true, dHat);
-            if (d < dHat) {
-                const float schur = wv * dot(g[0], g[0]);
-                const float ld = (compliance * (dHat - d)) / (compliance * schur + 1.0f);
-                acc_add(dx, nc, vid, wv * ld, g[0], &bad);
+            V3 g[4] = SX_ZERO_G;
+            int dt;
+            float schur;
+            if (project_vt_st(vid, x0, x1, x2, x3, wv, dHat, compliance, dx, nc, &bad, g, &dt, &schur))
                 po.rec((size_t)vid, cnt, fs, dt, g, schur);
-            }
         }
         if (po.num) po.num[vid] = cnt;
-    } else if (i < 2 * Vd) {  // __vt_dy (collision_constraints_x.py:176-310)
+    } else if (i < 2 * Vd) {
         const int vid = i - Vd;
         const int n = min(vt_dy_n[vid], cap);
         for (int j = 0; j < n; ++j) {
@@ -190,65 +270,184 @@ __global__ void __launch_bounds__(128) collision_project_kernel(
             if (a == vid || b == vid || c == vid) continue;  // Solver.is_in_face, XPBD.py:121-127
             const int vv[4] = {vid, a, b, c};
             const V3 x[4] = {mk(y4[vid]), mk(y4[a]), mk(y4[b]), mk(y4[c])};
-            V3 g[4] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-            const int dt = d_type_PT(x[0], x[1], x[2], x[3]);
-            const float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);
-            float schur = 0.0f;
-            if (d < dHat) {
-                pt_distance(dt, x[0], x[1], x[2], x[3], g, true, dHat);
-                const int m = region_mask(dt);
-                float s = 0.0f;
-                bool first = true;
-                for (int k = 0; k < 4; ++k) {
-                    if (!(m & (1 << k))) continue;
-                    const float t = (fixed[vv[k]] * m_inv[vv[k]]) * dot(g[k], g[k]);
-                    s = first ? t : s + t;
-                    first = false;
-                }
-                schur = s + 1e-4f;
-                const float ld = (dHat - d) / schur;
-                for (int k = 0; k < 4; ++k) {
-                    if (!(m & (1 << k))) continue;
-                    // region 0 applies m_inv without `fixed` (collision_constraints_x.py:199-200)
-                    const float w = dt == 0 ? m_inv[vv[k]] : fixed[vv[k]] * m_inv[vv[k]];
-                    acc_add(dx, nc, vv[k], w * ld, g[k], &bad);
-                }
-            }
+            V3 g[4] = SX_ZERO_G;
+            int dt;
+            float schur;
+            project_vt_dy(vv, x, fixed, m_inv, dHat, dx, nc, &bad, g, &dt, &schur);
             po.rec((size_t)Vd + vid, cnt, fd, dt, g, schur);
         }
         if (po.num) po.num[Vd + vid] = cnt;
-    } else {  // __tv_st (collision_constraints_x.py:72-173)
+    } else {
         const int vis = i - 2 * Vd;
         const int n = min(tv_st_n[vis], cap);
         for (int j = 0; j < n; ++j) {
             const int fd = tv_st_c[(size_t)vis * cap + j];
             const int vv[4] = {-1, faces_dy[3 * fd], faces_dy[3 * fd + 1], faces_dy[3 * fd + 2]};
             const V3 x[4] = {mk(xs4[vis]), mk(y4[vv[1]]), mk(y4[vv[2]]), mk(y4[vv[3]])};
-            V3 g[4] = {{0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}, {0.f, 0.f, 0.f}};
-            const int dt = d_type_PT(x[0], x[1], x[2], x[3]);
-            const float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);
-            float schur = 0.0f;
-            if (d < dHat) {
-                pt_distance(dt, x[0], x[1], x[2], x[3], g, true, dHat);
-                const int m = region_mask(dt) & ~1;
-                float s = 0.0f;
-                bool first = true;
-                for (int k = 1; k < 4; ++k) {
-                    if (!(m & (1 << k))) continue;
-                    const float t = (fixed[vv[k]] * m_inv[vv[k]]) * dot(g[k], g[k]);
-                    s = first ? t : s + t;
-                    first = false;
-                }
-                schur = s;
-                const float ld = (compliance * (dHat - d)) / (compliance * schur + 1.0f);
-                for (int k = 1; k < 4; ++k) {
-                    if (!(m & (1 << k))) continue;
-                    acc_add(dx, nc, vv[k], (fixed[vv[k]] * m_inv[vv[k]]) * ld, g[k], &bad);
-                }
-            }
+            V3 g[4] = SX_ZERO_G;
+            int dt;
+            float schur;
+            project_tv_st(vv, x, fixed, m_inv, dHat, compliance, dx, nc, &bad, g, &dt, &schur);
             po.rec((size_t)2 * Vd + vis, cnt, fd, dt, g, schur);
         }
         if (po.num) po.num[2 * Vd + vis] = cnt;
+    }
+    if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
+}
+
+// ---------------------------------------------------------------------------
+// Compacted pair list.  The candidate lists do not change between the Jacobi
+// iterations of a substep, so once per substep they are flattened into one
+// dense array of (query vertex, triangle vertices) quads, in query order,
+// without the faces __vt_dy skips (incident ones); every iteration then runs
+// one thread per pair.  The per-pair arithmetic is the same code as above and
+// accumulation is order independent, so the result equals the per-query walk.
+// Workspace: block totals, then meta[4] = {end of vt_st pairs, end of vt_dy
+// pairs, total pairs, unused}.
+// ---------------------------------------------------------------------------
+constexpr int PB = 256;
+
+__device__ __forceinline__ int query_pairs(int q, int Vd, int cap, const int* __restrict__ faces_dy,
+                                           const int* __restrict__ vt_st_n, const int* __restrict__ vt_dy_c,
+                                           const int* __restrict__ vt_dy_n, const int* __restrict__ tv_st_n) {
+    if (q < Vd) return min(vt_st_n[q], cap);
+    if (q < 2 * Vd) {
+        const int vid = q - Vd;
+        const int n = min(vt_dy_n[vid], cap);
+        int c = 0;
+        for (int j = 0; j < n; ++j) {
+            const int fd = vt_dy_c[(size_t)vid * cap + j];
+            c += !(faces_dy[3 * fd] == vid || faces_dy[3 * fd + 1] == vid || faces_dy[3 * fd + 2] == vid);
+        }
+        return c;
+    }
+    return min(tv_st_n[q - 2 * Vd], cap);
+}
+
+__device__ __forceinline__ int block_excl_scan(int v, int* total) {
+    __shared__ int warp_tot[PB / 32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = v;
+    for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    int base = 0, tot = 0;
+    for (int k = 0; k < PB / 32; ++k) {
+        if (k < w) base += warp_tot[k];
+        tot += warp_tot[k];
+    }
+    __syncthreads();
+    *total = tot;
+    return base + incl - v;
+}
+
+__global__ void __launch_bounds__(PB) pairs_count_kernel(int Vd, int Vs, int cap, const int* __restrict__ faces_dy,
+                                                          const int* __restrict__ vt_st_n,
+                                                          const int* __restrict__ vt_dy_c,
+                                                          const int* __restrict__ vt_dy_n,
+                                                          const int* __restrict__ tv_st_n, int* block_tot) {
+    const int q = blockIdx.x * PB + threadIdx.x;
+    const int c = q < 2 * Vd + Vs ? query_pairs(q, Vd, cap, faces_dy, vt_st_n, vt_dy_c, vt_dy_n, tv_st_n) : 0;
+    int tot;
+    block_excl_scan(c, &tot);
+    if (threadIdx.x == 0) block_tot[blockIdx.x] = tot;
+}
+
+__global__ void __launch_bounds__(1024) pairs_scan_kernel(int nb, int* block_tot) {
+    __shared__ int s[1024];
+    const int tid = threadIdx.x;
+    const int per = (nb + 1023) / 1024;
+    const int beg = min(tid * per, nb), end = min(beg + per, nb);
+    int sum = 0;
+    for (int i = beg; i < end; ++i) sum += block_tot[i];
+    s[tid] = sum;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        int v = tid >= off ? s[tid - off] : 0;
+        __syncthreads();
+        s[tid] += v;
+        __syncthreads();
+    }
+    int run = tid ? s[tid - 1] : 0;
+    for (int i = beg; i < end; ++i) {
+        int t = block_tot[i];
+        block_tot[i] = run;
+        run += t;
+    }
+}
+
+__global__ void __launch_bounds__(PB) pairs_fill_kernel(int Vd, int Vs, int cap, const int* __restrict__ faces_dy,
+                                                         const int* __restrict__ faces_st,
+                                                         const int* __restrict__ vt_st_c,
+                                                         const int* __restrict__ vt_st_n,
+                                                         const int* __restrict__ vt_dy_c,
+                                                         const int* __restrict__ vt_dy_n,
+                                                         const int* __restrict__ tv_st_c,
+                                                         const int* __restrict__ tv_st_n,
+                                                         const int* __restrict__ block_off, int4* pairs, int* meta) {
+    const int Q = 2 * Vd + Vs;
+    const int q = blockIdx.x * PB + threadIdx.x;
+    const int c = q < Q ? query_pairs(q, Vd, cap, faces_dy, vt_st_n, vt_dy_c, vt_dy_n, tv_st_n) : 0;
+    int tot;
+    const int off = block_off[blockIdx.x] + block_excl_scan(c, &tot);
+    if (q == Vd) meta[0] = off;
+    if (q == 2 * Vd) meta[1] = off;
+    if (q == Q) meta[2] = off;
+    if (q >= Q || c == 0) return;
+    int k = off;
+    if (q < Vd) {
+        for (int j = 0; j < c; ++j) {
+            const int fs = vt_st_c[(size_t)q * cap + j];
+            pairs[k++] = make_int4(q, faces_st[3 * fs], faces_st[3 * fs + 1], faces_st[3 * fs + 2]);
+        }
+    } else if (q < 2 * Vd) {
+        const int vid = q - Vd;
+        const int n = min(vt_dy_n[vid], cap);
+        for (int j = 0; j < n; ++j) {
+            const int fd = vt_dy_c[(size_t)vid * cap + j];
+            const int a = faces_dy[3 * fd], b = faces_dy[3 * fd + 1], cc = faces_dy[3 * fd + 2];
+            if (a == vid || b == vid || cc == vid) continue;
+            pairs[k++] = make_int4(vid, a, b, cc);
+        }
+    } else {
+        const int vis = q - 2 * Vd;
+        for (int j = 0; j < c; ++j) {
+            const int fd = tv_st_c[(size_t)vis * cap + j];
+            pairs[k++] = make_int4(vis, faces_dy[3 * fd], faces_dy[3 * fd + 1], faces_dy[3 * fd + 2]);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) pairs_project_kernel(const int* __restrict__ meta,
+                                                             const int4* __restrict__ pairs,
+                                                             const float4* __restrict__ y4,
+                                                             const float4* __restrict__ xs4,
+                                                             const float* __restrict__ fixed,
+                                                             const float* __restrict__ m_inv, float dHat,
+                                                             float compliance, long long* dx, int* nc,
+                                                             int* status) {
+    const int st_end = meta[0], dy_end = meta[1], P = meta[2];
+    int bad = 0;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
+        const int4 pr = pairs[t];
+        V3 g[4] = SX_ZERO_G;
+        int dt;
+        float schur;
+        if (t < st_end) {
+            project_vt_st(pr.x, mk(y4[pr.x]), mk(xs4[pr.y]), mk(xs4[pr.z]), mk(xs4[pr.w]), m_inv[pr.x], dHat,
+                          compliance, dx, nc, &bad, g, &dt, &schur);
+        } else if (t < dy_end) {
+            const int vv[4] = {pr.x, pr.y, pr.z, pr.w};
+            const V3 x[4] = {mk(y4[pr.x]), mk(y4[pr.y]), mk(y4[pr.z]), mk(y4[pr.w])};
+            project_vt_dy(vv, x, fixed, m_inv, dHat, dx, nc, &bad, g, &dt, &schur);
+        } else {
+            const int vv[4] = {-1, pr.y, pr.z, pr.w};
+            const V3 x[4] = {mk(xs4[pr.x]), mk(y4[pr.y]), mk(y4[pr.z]), mk(y4[pr.w])};
+            project_tv_st(vv, x, fixed, m_inv, dHat, compliance, dx, nc, &bad, g, &dt, &schur);
+        }
     }
     if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
 }
@@ -305,6 +504,65 @@ extern "C" int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const
         n_dy, n_st, faces_dy, faces_st, (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, cap,
         vsc, vsn, vt_dy_cand, vt_dy_num, tv_st_cand, tv_st_num, dx_fix, nc, po, status);
     int rc = check_launch("collision_project_kernel");
+    if (rc) return rc;
+    launch(collision_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)y4, fixed, dx_fix, nc);
+    return check_launch("collision_apply_kernel");
+}
+
+static inline size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
+static inline int pairs_blocks(int n_dy, int n_st) { return (2 * n_dy + n_st + 1 + PB - 1) / PB; }
+
+extern "C" size_t sx_contact_pairs_workspace_bytes(int n_dy, int n_st) {
+    return a256((size_t)pairs_blocks(n_dy, n_st) * 4) + 256;
+}
+
+extern "C" int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* faces_st, int cap,
+                                      const int* vt_st_cand, const int* vt_st_num, const int* vt_dy_cand,
+                                      const int* vt_dy_num, const int* tv_st_cand, const int* tv_st_num, int* pairs,
+                                      long long max_pairs, void* ws, size_t ws_bytes, void* stream) {
+    SX_REQUIRE(n_dy >= 0 && n_st >= 0 && cap >= 1, "sx_contact_pairs_build: bad sizes");
+    SX_REQUIRE(max_pairs >= (long long)(2 * n_dy + n_st) * cap,
+               "sx_contact_pairs_build: pair buffer must hold (2*n_dy + n_st) * cap entries");
+    SX_REQUIRE(ws && ws_bytes >= sx_contact_pairs_workspace_bytes(n_dy, n_st),
+               "sx_contact_pairs_build: workspace too small");
+    SX_REQUIRE(faces_dy && vt_st_cand && vt_st_num && vt_dy_cand && vt_dy_num && pairs,
+               "sx_contact_pairs_build: null pointer");
+    SX_REQUIRE(n_st == 0 || (faces_st && tv_st_cand && tv_st_num), "sx_contact_pairs_build: null static pointer");
+    cudaStream_t s = as_stream(stream);
+    const int nb = pairs_blocks(n_dy, n_st);
+    int* block_tot = (int*)ws;
+    int* meta = (int*)((char*)ws + a256((size_t)nb * 4));
+    launch(pairs_count_kernel, nb, PB, 0, s, n_dy, n_st, cap, faces_dy, vt_st_num, vt_dy_cand, vt_dy_num, tv_st_num,
+           block_tot);
+    launch(pairs_scan_kernel, 1, 1024, 0, s, nb, block_tot);
+    launch(pairs_fill_kernel, nb, PB, 0, s, n_dy, n_st, cap, faces_dy, faces_st, vt_st_cand, vt_st_num, vt_dy_cand,
+           vt_dy_num, tv_st_cand, tv_st_num, (const int*)block_tot, (int4*)pairs, meta);
+    return check_launch("sx_contact_pairs_build");
+}
+
+static int sm_count() {
+    static int n = 0;
+    if (n == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            n = 132;
+    }
+    return n;
+}
+
+extern "C" int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4,
+                                      const float* xs4, const float* fixed, const float* m_inv, float dHat,
+                                      float compliance, long long* dx_fix, int* nc, int* status, void* stream) {
+    SX_REQUIRE(n_dy >= 0 && n_st >= 0, "sx_contact_pairs_sweep: bad sizes");
+    if (n_dy == 0) return SX_OK;
+    SX_REQUIRE(pairs && ws && y4 && fixed && m_inv && dx_fix && nc && status, "sx_contact_pairs_sweep: null pointer");
+    SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_sweep: null static positions");
+    cudaStream_t s = as_stream(stream);
+    const int nb = pairs_blocks(n_dy, n_st);
+    const int* meta = (const int*)((const char*)ws + a256((size_t)nb * 4));
+    launch(pairs_project_kernel, sm_count() * 8, 256, 0, s, meta, (const int4*)pairs, (const float4*)y4,
+           (const float4*)xs4, fixed, m_inv, dHat, compliance, dx_fix, nc, status);
+    int rc = check_launch("pairs_project_kernel");
     if (rc) return rc;
     launch(collision_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)y4, fixed, dx_fix, nc);
     return check_launch("collision_apply_kernel");

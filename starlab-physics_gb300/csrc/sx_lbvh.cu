@@ -91,32 +91,32 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_upsweep(const unsigned* __restric
     hist[(size_t)tid * nblocks + blockIdx.x] = cnt[tid];
 }
 
-// single-block scan over n entries (exclusive or inclusive), 1024 threads
+// Single-block scan over n entries (exclusive or inclusive), 1024 threads.
+// Each warp owns a contiguous chunk that its lanes read 32 consecutive
+// elements at a time (coalesced); a shuffle scan combines each group of 32 and
+// the warp chunk totals are scanned across warps in shared memory.
 __global__ void __launch_bounds__(1024) scan_single_block(unsigned* data, int n, int inclusive) {
-    __shared__ unsigned s[1024];
-    const int tid = threadIdx.x;
-    const int per = (n + 1023) / 1024;
-    const int beg = min(tid * per, n), end = min(beg + per, n);
-    unsigned sum = 0;
-    for (int i = beg; i < end; ++i) sum += data[i];
-    s[tid] = sum;
+    __shared__ unsigned wsum[32];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    const int chunk = ((n + 31) / 32 + 31) / 32 * 32;
+    const int beg = min(w * chunk, n), end = min(beg + chunk, n);
+    unsigned tot = 0;
+    for (int i = beg + lane; i < end; i += 32) tot += data[i];
+    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    if (lane == 0) wsum[w] = tot;
     __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        unsigned v = tid >= off ? s[tid - off] : 0u;
-        __syncthreads();
-        s[tid] += v;
-        __syncthreads();
-    }
-    unsigned run = tid ? s[tid - 1] : 0u;
-    for (int i = beg; i < end; ++i) {
-        unsigned t = data[i];
-        if (inclusive) {
-            run += t;
-            data[i] = run;
-        } else {
-            data[i] = run;
-            run += t;
+    unsigned run = 0;
+    for (int k = 0; k < w; ++k) run += wsum[k];
+    for (int i0 = beg; i0 < end; i0 += 32) {
+        const int i = i0 + lane;
+        const unsigned v = i < end ? data[i] : 0u;
+        unsigned incl = v;
+        for (int o = 1; o < 32; o <<= 1) {
+            unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+            if (lane >= o) incl += t;
         }
+        if (i < end) data[i] = run + (inclusive ? incl : incl - v);
+        run += __shfl_sync(0xffffffffu, incl, 31);
     }
 }
 
@@ -280,8 +280,10 @@ __global__ void face_cell_kernel(int F, const float4* __restrict__ mn4, const fl
     atomicAdd(counts + cell, 1u);
 }
 
-__device__ __forceinline__ void store_box(float4* nmin4, float4* nmax4, int i, V3 a, V3 b) {
-    nmin4[i] = make_float4(a.x, a.y, a.z, 0.0f);
+// Node boxes are float4 pairs; min.w carries the node's face count (int bits)
+// so that one 16-byte load gives a child's box corner and whether it is empty.
+__device__ __forceinline__ void store_box(float4* nmin4, float4* nmax4, int i, V3 a, V3 b, int nf = 0) {
+    nmin4[i] = make_float4(a.x, a.y, a.z, __int_as_float(nf));
     nmax4[i] = make_float4(b.x, b.y, b.z, 0.0f);
 }
 __device__ __forceinline__ V3 load_cg(const float4* p) {
@@ -291,12 +293,15 @@ __device__ __forceinline__ V3 load_cg(const float4* p) {
 
 // assign_leaf_cell_nodes (:602-634) fused with a bottom-up refit that applies
 // the rules of compute_cell_node_aabbs (:491-522).  The second thread to reach
-// an internal node computes it from both (finished) children.
+// an internal node computes it from both (finished) children.  Each leaf also
+// writes its faces' records (min.xyz + face id, max.xyz) in sorted order, the
+// contiguous array the traversal scans.
 __global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int* __restrict__ prefix,
                                        const int* __restrict__ sorted_face_ids, const float4* __restrict__ fmn4,
                                        const float4* __restrict__ fmx4, const int* __restrict__ child_a,
                                        const int* __restrict__ child_b, const int* __restrict__ parent,
-                                       int* num_faces, float4* nmin4, float4* nmax4, int* flags, int* status) {
+                                       int* num_faces, float4* nmin4, float4* nmax4, float4* frec, int* flags,
+                                       int* status) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kNumCells) return;
     V3 lo{box6[0], box6[1], box6[2]};
@@ -307,12 +312,15 @@ __global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int
     V3 c = cell_center(i, cs, lo);
     V3 a = c, b = c;
     for (int j = 0; j < size; ++j) {
-        int fid = sorted_face_ids[rl + j];
-        a = vmin(a, mk(fmn4[fid]));
-        b = vmax(b, mk(fmx4[fid]));
+        const int fid = sorted_face_ids[rl + j];
+        const float4 fa = fmn4[fid], fb = fmx4[fid];
+        a = vmin(a, mk(fa));
+        b = vmax(b, mk(fb));
+        frec[2 * (rl + j)] = make_float4(fa.x, fa.y, fa.z, __int_as_float(fid));
+        frec[2 * (rl + j) + 1] = make_float4(fb.x, fb.y, fb.z, 0.0f);
     }
     num_faces[leaf] = size;
-    store_box(nmin4, nmax4, leaf, a, b);
+    store_box(nmin4, nmax4, leaf, a, b, size);
     int node = parent[leaf];
     for (int steps = 0; node >= 0; ++steps) {
         if (steps > kNumCells) {
@@ -340,18 +348,22 @@ __global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int
             nb = na;
         }
         num_faces[node] = nl + nr;
-        store_box(nmin4, nmax4, node, na, nb);
+        store_box(nmin4, nmax4, node, na, nb, nl + nr);
         node = parent[node];
     }
 }
 
-// traverse_cell_bvh_single (lbvh_cell.py:662-714)
+// traverse_cell_bvh_single (lbvh_cell.py:662-714).  The reference pops a node,
+// skips it when empty or not overlapping, and otherwise either scans the
+// leaf's faces or pushes child_a then child_b.  Testing a child's emptiness and
+// overlap before pushing it instead of after popping it visits the overlapping
+// nodes in the same order, so the candidate list is the same, with fewer
+// stack operations and one float4 pair per child.
 __global__ void __launch_bounds__(128) cell_traverse_kernel(
     int Q, const float4* __restrict__ p4, float pad, const float* __restrict__ cs3, const float* __restrict__ box6,
-    const int* __restrict__ child_a, const int* __restrict__ child_b, const int* __restrict__ num_faces,
-    const float4* __restrict__ nmin4, const float4* __restrict__ nmax4, const int* __restrict__ prefix,
-    const int* __restrict__ sorted_face_ids, const float4* __restrict__ fmn4, const float4* __restrict__ fmx4,
-    int cap, int* __restrict__ cand, int* __restrict__ num, int* status) {
+    const int* __restrict__ child_a, const int* __restrict__ child_b, const float4* __restrict__ nmin4,
+    const float4* __restrict__ nmax4, const int* __restrict__ prefix, const float4* __restrict__ frec, int cap,
+    int* __restrict__ cand, int* __restrict__ num, int* status) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= Q) return;
     V3 p = mk(p4[q]);
@@ -367,7 +379,8 @@ __global__ void __launch_bounds__(128) cell_traverse_kernel(
     if (cid <= kNumCells - 1) {
         int stack[64];
         int sc = 0;
-        stack[sc++] = 0;
+        const float4 rmn = nmin4[0], rmx = nmax4[0];
+        if (__float_as_int(rmn.w) > 0 && overlap(a, b, mk(rmn), mk(rmx))) stack[sc++] = 0;
         long long pops = 0;
         while (sc > 0) {
             if (++pops > 2LL * kNumCells) {
@@ -375,25 +388,24 @@ __global__ void __launch_bounds__(128) cell_traverse_kernel(
                 break;
             }
             const int idx = stack[--sc];
-            if (num_faces[idx] <= 0) continue;
-            if (!overlap(a, b, mk(nmin4[idx]), mk(nmax4[idx]))) continue;
             if (idx >= kNumCells - 1) {
                 const int i = idx - (kNumCells - 1);
                 const int rl = i == 0 ? 0 : prefix[i - 1];
-                const int size = prefix[i] - rl;
-                for (int j = 0; j < size; ++j) {
-                    const int fid = sorted_face_ids[rl + j];
-                    if (overlap(a, b, mk(fmn4[fid]), mk(fmx4[fid]))) {
-                        if (count < cap) out[count] = fid;
+                const int re = prefix[i];
+                for (int j = rl; j < re; ++j) {
+                    const float4 fa = frec[2 * j], fb = frec[2 * j + 1];
+                    if (overlap(a, b, mk(fa), mk(fb))) {
+                        if (count < cap) out[count] = __float_as_int(fa.w);
                         ++count;
                     }
                 }
             } else {
                 const int l = child_a[idx], r = child_b[idx];
-                if (num_faces[l] > 0) {
+                const float4 lmn = nmin4[l], lmx = nmax4[l], rmn2 = nmin4[r], rmx2 = nmax4[r];
+                if (__float_as_int(lmn.w) > 0 && overlap(a, b, mk(lmn), mk(lmx))) {
                     if (sc < 64) stack[sc++] = l; else flags |= SX_STATUS_STACK_OVERFLOW;
                 }
-                if (num_faces[r] > 0) {
+                if (__float_as_int(rmn2.w) > 0 && overlap(a, b, mk(rmn2), mk(rmx2))) {
                     if (sc < 64) stack[sc++] = r; else flags |= SX_STATUS_STACK_OVERFLOW;
                 }
             }
@@ -450,7 +462,9 @@ __global__ void __launch_bounds__(128) face_traverse_kernel(int n, int Q, const 
     int* out = cand + (size_t)q * cap;
     int stack[64];
     int sc = 0;
-    stack[sc++] = 0;
+    // Children are tested before they are pushed (same visiting order as a
+    // pop-time test, see cell_traverse_kernel).
+    if (overlap(a, b, mk(nmin4[0]), mk(nmax4[0]))) stack[sc++] = 0;
     // A well-formed tree pops each of its 2n-1 nodes at most once; the bound
     // stops the walk on a malformed hierarchy (reference tie rule with repeated
     // codes can create cycles).
@@ -462,14 +476,17 @@ __global__ void __launch_bounds__(128) face_traverse_kernel(int n, int Q, const 
             break;
         }
         const int idx = stack[--sc];
-        if (!overlap(a, b, mk(nmin4[idx]), mk(nmax4[idx]))) continue;
         if (idx >= n - 1) {
             if (count < cap) out[count] = sorted_ids[idx - (n - 1)];
             ++count;
         } else {
             const int l = child_a[idx], r = child_b[idx];
-            if (sc < 64) stack[sc++] = l; else flags |= SX_STATUS_STACK_OVERFLOW;
-            if (sc < 64) stack[sc++] = r; else flags |= SX_STATUS_STACK_OVERFLOW;
+            if (overlap(a, b, mk(nmin4[l]), mk(nmax4[l]))) {
+                if (sc < 64) stack[sc++] = l; else flags |= SX_STATUS_STACK_OVERFLOW;
+            }
+            if (overlap(a, b, mk(nmin4[r]), mk(nmax4[r]))) {
+                if (sc < 64) stack[sc++] = r; else flags |= SX_STATUS_STACK_OVERFLOW;
+            }
         }
     }
     num[q] = count;
@@ -538,12 +555,13 @@ extern "C" int sx_cell_bvh_init(int* sorted_codes, int* sorted_ids, int* child_a
 
 extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_faces, const float* box6,
                                  const int* child_a, const int* child_b, const int* parent, int* sorted_face_ids,
-                                 int* prefix, int* num_faces, float* nmin4, float* nmax4, float* cell_size3,
-                                 void* ws, size_t ws_bytes, void* stream) {
+                                 int* prefix, int* num_faces, float* nmin4, float* nmax4, float* face_rec8,
+                                 float* cell_size3, void* ws, size_t ws_bytes, void* stream) {
     SX_REQUIRE(n_faces >= 0, "sx_cell_bvh_build: n_faces < 0");
     SX_REQUIRE(box6 && child_a && child_b && parent && prefix && num_faces && nmin4 && nmax4 && cell_size3,
                "sx_cell_bvh_build: null pointer");
-    SX_REQUIRE(n_faces == 0 || (fmin4 && fmax4 && sorted_face_ids), "sx_cell_bvh_build: null face arrays");
+    SX_REQUIRE(n_faces == 0 || (fmin4 && fmax4 && sorted_face_ids && face_rec8),
+               "sx_cell_bvh_build: null face arrays");
     SX_REQUIRE(ws && ws_bytes >= sx_cell_bvh_workspace_bytes(n_faces), "sx_cell_bvh_build: workspace too small");
     cudaStream_t s = as_stream(stream);
     char* p = (char*)ws;
@@ -555,8 +573,7 @@ extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_f
     SX_CUDA(cudaMemsetAsync(prefix, 0, sizeof(int) * kNumCells, s));
     SX_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * kNumCells, s));
     launch(face_cell_kernel, grid_for(n_faces, 256), 256, 0, s, n_faces, (const float4*)fmin4, (const float4*)fmax4,
-                                                            box6, keys, sorted_face_ids, (unsigned*)prefix,
-                                                            cell_size3);
+           box6, keys, sorted_face_ids, (unsigned*)prefix, cell_size3);
     int rc = check_launch("face_cell_kernel");
     if (rc) return rc;
     launch(scan_single_block, 1, 1024, 0, s, (unsigned*)prefix, kNumCells, 1);
@@ -566,26 +583,25 @@ extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_f
     }
     // the status word lives in the flags scratch tail (flags[NC-1] is never a node)
     int* status = flags + (kNumCells - 1);
-    launch(cell_leaf_refit_kernel, grid_for(kNumCells, 256), 256, 0, s, 
-        box6, prefix, sorted_face_ids, (const float4*)fmin4, (const float4*)fmax4, child_a, child_b, parent,
-        num_faces, (float4*)nmin4, (float4*)nmax4, flags, status);
+    launch(cell_leaf_refit_kernel, grid_for(kNumCells, 256), 256, 0, s, box6, (const int*)prefix,
+           (const int*)sorted_face_ids, (const float4*)fmin4, (const float4*)fmax4, child_a, child_b, parent,
+           num_faces, (float4*)nmin4, (float4*)nmax4, (float4*)face_rec8, flags, status);
     return check_launch("cell_leaf_refit_kernel");
 }
 
 extern "C" int sx_cell_bvh_traverse(const float* p4, int n_queries, float padding, const float* cell_size3,
                                     const float* origin_box6, const int* child_a, const int* child_b,
-                                    const int* num_faces, const float* nmin4, const float* nmax4, const int* prefix,
-                                    const int* sorted_face_ids, const float* fmin4, const float* fmax4, int cap,
-                                    int* cand, int* num, int* status, void* stream) {
+                                    const float* nmin4, const float* nmax4, const int* prefix,
+                                    const float* face_rec8, int cap, int* cand, int* num, int* status,
+                                    void* stream) {
     SX_REQUIRE(n_queries >= 0 && cap >= 1, "sx_cell_bvh_traverse: bad sizes");
     if (n_queries == 0) return SX_OK;
-    SX_REQUIRE(p4 && cell_size3 && origin_box6 && child_a && child_b && num_faces && nmin4 && nmax4 && prefix &&
-                   sorted_face_ids && fmin4 && fmax4 && cand && num && status,
+    SX_REQUIRE(p4 && cell_size3 && origin_box6 && child_a && child_b && nmin4 && nmax4 && prefix && face_rec8 &&
+                   cand && num && status,
                "sx_cell_bvh_traverse: null pointer");
-    launch(cell_traverse_kernel, grid_for(n_queries, 128), 128, 0, as_stream(stream), 
-        n_queries, (const float4*)p4, padding, cell_size3, origin_box6, child_a, child_b, num_faces,
-        (const float4*)nmin4, (const float4*)nmax4, prefix, sorted_face_ids, (const float4*)fmin4,
-        (const float4*)fmax4, cap, cand, num, status);
+    launch(cell_traverse_kernel, grid_for(n_queries, 128), 128, 0, as_stream(stream), n_queries, (const float4*)p4,
+           padding, cell_size3, origin_box6, child_a, child_b, (const float4*)nmin4, (const float4*)nmax4, prefix,
+           (const float4*)face_rec8, cap, cand, num, status);
     return check_launch("cell_traverse_kernel");
 }
 

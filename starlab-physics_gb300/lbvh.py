@@ -52,6 +52,7 @@ class LBVH_CELL:
         self.num_faces = torch.zeros(2 * n - 1, **i32)
         self.node_min4 = torch.zeros((2 * n - 1, 4), dtype=torch.float32, device=dev)
         self.node_max4 = torch.zeros((2 * n - 1, 4), dtype=torch.float32, device=dev)
+        self.face_rec8 = torch.zeros((max(self.num_leafs, 1), 8), dtype=torch.float32, device=dev)
         self.cell_size = torch.zeros(3, dtype=torch.float32, device=dev)
         self.box6 = torch.zeros(6, dtype=torch.float32, device=dev)
         ws = int(sx.sx_cell_bvh_workspace_bytes(self.num_leafs))
@@ -84,16 +85,15 @@ class LBVH_CELL:
         self.face_aabb_min4, self.face_aabb_max4 = fmn, fmx
         sx.sx_cell_bvh_build(ptr(fmn), ptr(fmx), nf, ptr(self.box6), ptr(self.child_a), ptr(self.child_b),
                              ptr(self.parent), ptr(self.sorted_face_ids), ptr(self.prefix_sum_cell),
-                             ptr(self.num_faces), ptr(self.node_min4), ptr(self.node_max4), ptr(self.cell_size),
-                             ptr(self.workspace), self.workspace.numel(), stream_handle())
+                             ptr(self.num_faces), ptr(self.node_min4), ptr(self.node_max4), ptr(self.face_rec8),
+                             ptr(self.cell_size), ptr(self.workspace), self.workspace.numel(), stream_handle())
 
     def traverse(self, points4, padding: float, cap: int, cand, num, status, n_queries=None):
         """``traverse_cell_bvh_single`` for boxes ``points4[i] +- padding``."""
         q = points4.shape[0] if n_queries is None else n_queries
         sx.sx_cell_bvh_traverse(ptr(points4), q, float(padding), ptr(self.cell_size), ptr(self.box6),
-                                ptr(self.child_a), ptr(self.child_b), ptr(self.num_faces), ptr(self.node_min4),
-                                ptr(self.node_max4), ptr(self.prefix_sum_cell), ptr(self.sorted_face_ids),
-                                ptr(self.face_aabb_min4), ptr(self.face_aabb_max4), int(cap), ptr(cand), ptr(num),
+                                ptr(self.child_a), ptr(self.child_b), ptr(self.node_min4), ptr(self.node_max4),
+                                ptr(self.prefix_sum_cell), ptr(self.face_rec8), int(cap), ptr(cand), ptr(num),
                                 ptr(status), stream_handle())
 
 

@@ -9,7 +9,7 @@ with the shapes, sizes and parameters of the benchmark configurations:
   +-1e-4 jitter, over a static box (side 0.5, centre (0.5, 0.5, 0.3), 12 faces);
   dt = 1/60, 10 substeps, 20 Jacobi iterations; springs 1e8 (compliance 1e-8),
   bending 1e5 (compliance 1e-5); gravity (0, 0, -9.81).
-* ``drape256``  -- 256 x 256 cloth (65536 vertices, 130050 faces) 0.02 above a
+* ``drape256``  -- 256 x 256 cloth (65536 vertices, 130050 faces) 5 mm above a
   static icosphere of 20480 faces, radius 0.3; Gaussian sigma 1e-3 normal (z)
   offsets; contact thickness 2e-3 (dHat = thickness^2, since the reference
   compares squared distances); 10 substeps, 30 iterations; BVHs rebuilt every
@@ -68,11 +68,11 @@ def plain64(n: int = 64, seed: int = 0, collisions: bool = True) -> Scene:
                  meta={"grid": n, "thickness": thickness})
 
 
-def drape256(n: int = 256, seed: int = 0, sphere_subdiv: int = 5) -> Scene:
+def drape256(n: int = 256, seed: int = 0, sphere_subdiv: int = 5, gap: float = 0.005) -> Scene:
     rng = np.random.default_rng(seed)
     radius = 0.3
     center = (0.5, 0.5, 0.5)
-    x, f = grid_cloth(n, height=center[2] + radius + 0.02)
+    x, f = grid_cloth(n, height=center[2] + radius + gap)
     x[:, 2] = (x[:, 2] + rng.normal(0.0, 1e-3, size=x.shape[0]).astype(np.float32)).astype(np.float32)
     sx_, sf = icosphere(sphere_subdiv, radius, center)
     thickness = 2e-3

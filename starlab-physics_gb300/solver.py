@@ -34,7 +34,7 @@ from __future__ import annotations
 
 import torch
 
-from ._lib import ptr, stream_handle, sx
+from ._lib import load, ptr, stream_handle, sx
 from .lbvh import LBVH_CELL
 
 
@@ -89,6 +89,14 @@ class Solver:
         self._dx_fix = torch.zeros(3 * Vd, dtype=torch.int64, device=dev)
         self._nc = torch.zeros(Vd, **i32)
         self._y_other = torch.zeros_like(mesh_dy.y4)
+        # dense contact-pair list (int4 per pair, worst case every candidate slot)
+        self._pairs = torch.empty(((2 * Vd + Vs) * cap, 4), **i32)
+        self._pairs_ws = torch.zeros(int(sx.sx_contact_pairs_workspace_bytes(Vd, Vs)), dtype=torch.uint8,
+                                     device=dev)
+        self._static_built_for = None
+        self.use_graph = False
+        self._graphs = {}
+        self.graph_kernel_launches = 0  # library kernels in the last captured frame
         self.record_pairs = record_pairs
         if record_pairs:
             Q = 2 * Vd + Vs
@@ -136,16 +144,27 @@ class Solver:
         m.verts.y = m.y4[:, :3]
 
     def build_bvhs(self):
-        """XPBD.py:448-458: face AABBs and scene box on ``x``, then both builds."""
+        """XPBD.py:448-458: face AABBs and scene box on ``x``, then both builds.
+
+        The static mesh does not move, so its build is the same every time: it
+        runs on the first call and again only after :meth:`mark_static_moved`
+        (or when ``padding`` changes)."""
         m = self.mesh_dy
         m.computeAABB_faces(self.padding)
         m.computeAABB(self.padding)
         self.lbvh_dy.build(m, m.box6)
-        if self.mesh_st is not None:
+        if self.mesh_st is not None and self._static_built_for != self.padding:
             s = self.mesh_st
             s.computeAABB_faces(self.padding)
             s.computeAABB(self.padding)
             self.lbvh_st.build(s, s.box6)
+            self._static_built_for = self.padding
+
+    def mark_static_moved(self):
+        """The static mesh's positions changed: rebuild its BVH at the next build
+        and drop captured graphs."""
+        self._static_built_for = None
+        self._graphs.clear()
 
     def broadphase_lbvh(self):
         """XPBD.py:187-215: three query sets."""
@@ -159,11 +178,30 @@ class Solver:
         self.lbvh_dy.traverse(m.y4, self.padding, cap, self.vt_dy_candidates, self.vt_dy_candidates_num,
                               self.status)
 
+    def build_contact_pairs(self):
+        """Flatten this substep's candidate lists into the dense pair list used by
+        every iteration's contact sweep (not needed when pair records are kept)."""
+        m = self.mesh_dy
+        s = self.mesh_st
+        sx.sx_contact_pairs_build(m.num_verts, s.num_verts if s is not None else 0, ptr(m.face_indices),
+                                  ptr(s.face_indices) if s is not None else None, self.cache_size,
+                                  ptr(self.vt_st_candidates), ptr(self.vt_st_candidates_num),
+                                  ptr(self.vt_dy_candidates), ptr(self.vt_dy_candidates_num),
+                                  ptr(self.tv_st_candidates), ptr(self.tv_st_candidates_num), ptr(self._pairs),
+                                  self._pairs.shape[0], ptr(self._pairs_ws), self._pairs_ws.numel(),
+                                  stream_handle())
+
     def solve_collision_constraints_x(self, compliance_col=None):
         """XPBD.py:237-264 followed by update_dx (XPBD.py:384-387)."""
         m = self.mesh_dy
         s = self.mesh_st
         c = self.compliance_collision if compliance_col is None else compliance_col
+        if not self.record_pairs:
+            sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
+                                      ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
+                                      ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c), ptr(self._dx_fix),
+                                      ptr(self._nc), ptr(self.status), stream_handle())
+            return
         sx.sx_collision_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(m.face_indices),
                               ptr(s.face_indices) if s is not None else None, ptr(m.y4),
                               ptr(s.x4) if s is not None else None, ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c),
@@ -182,6 +220,8 @@ class Solver:
                 self.vt_st_candidates_num.zero_()
             if first_iteration:
                 self.broadphase_lbvh()
+                if not self.record_pairs:
+                    self.build_contact_pairs()
             self.solve_collision_constraints_x()
 
     def compute_velocity_update_x(self, dt):
@@ -201,12 +241,53 @@ class Solver:
         self.compute_velocity_update_x(dt_sub)
 
     def forward(self, n_substeps: int):
-        """``Solver.forward`` (XPBD.py:443-469)."""
+        """``Solver.forward`` (XPBD.py:443-469).
+
+        With ``use_graph = True`` the whole frame is captured once into a CUDA
+        graph (per set of parameters that the kernels receive by value) and
+        replayed on later calls; results are identical to the eager path."""
+        if not self.use_graph:
+            self._forward_eager(n_substeps)
+            return
+        key = self._graph_key(n_substeps)
+        g = self._graphs.get(key)
+        if g is None:
+            g = self._capture(n_substeps)
+            self._graphs[key] = g
+        g.replay()
+
+    def _forward_eager(self, n_substeps: int):
         dt_sub = self.dt / n_substeps
         if self.enable_collision_handling and self.rebuild == "frame":
             self.build_bvhs()
         for _ in range(n_substeps):
             self.substep(dt_sub)
+
+    def _graph_key(self, n_substeps):
+        return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
+                self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
+                self.compliance_collision, self.mesh_dy.y4.data_ptr())
+
+    def _capture(self, n_substeps):
+        m = self.mesh_dy
+        y_start = m.y4
+        if self.enable_collision_handling and self.mesh_st is not None and self._static_built_for != self.padding:
+            self.build_bvhs()  # the static build happens once, outside the graph
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream(device=self.device)
+        side.wait_stream(torch.cuda.current_stream(self.device))
+        lib = load()
+        n0 = lib.sx_kernel_launches()
+        with torch.cuda.graph(g, stream=side):
+            self._forward_eager(n_substeps)
+            if m.y4 is not y_start:
+                # an odd number of sweeps left y in the other buffer: copy it back
+                # so that every replay starts from the same buffer assignment
+                y_start.copy_(m.y4)
+                self._swap_y()
+        torch.cuda.current_stream(self.device).wait_stream(side)
+        self.graph_kernel_launches = lib.sx_kernel_launches() - n0
+        return g
 
     # -- diagnostics ---------------------------------------------------------------
     def status_flags(self) -> int:

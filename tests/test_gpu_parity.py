@@ -275,3 +275,43 @@ def test_coloring(pkg, po):
         assert np.array_equal(_np(gc.edges_color)[: e.shape[0]], color)
         assert np.array_equal(_np(gc.sorted_edges_sequence_for_color)[: e.shape[0]], sorted_e)
         assert np.array_equal(_np(gc.color_prefix_sum), prefix)
+
+
+def test_pair_list_sweep_equals_per_query_sweep(pkg):
+    """The compacted pair list gives the same positions as the per-query walk."""
+    outs = []
+    for record in (True, False):
+        sc, cl, sp = _drape(pkg, n=40)
+        sim = pkg.Solver(cl, sp, dHat=(4e-2) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8, g=(0, 0, -9.81),
+                         dt=1 / 60, record_pairs=record)
+        sim.padding = 0.04
+        sim.enable_collision_handling = True
+        x = _np(cl.x4).copy()
+        x[:, 2] = 0.5 + 0.3 + 0.01 * np.sin(13 * x[:, 0]) * np.cos(7 * x[:, 1])
+        cl.x4.copy_(_t(x))
+        sim.build_bvhs()
+        sim.compute_y(1 / 600)
+        sim.broadphase_lbvh()
+        if not record:
+            sim.build_contact_pairs()
+        for _ in range(3):
+            sim.solve_collision_constraints_x()
+        outs.append(_np(cl.y4).copy())
+    assert np.array_equal(outs[0], outs[1])
+
+
+@pytest.mark.parametrize("n_iter", [3, 4])
+def test_graph_replay_equals_eager(pkg, n_iter):
+    res = []
+    for use_graph in (False, True):
+        scene = pkg.scenes.plain64(n=20, seed=6)
+        scene.n_iter = n_iter
+        sim = pkg.scenes.make_solver(scene, device=DEV)
+        sim.bending_on = "y"
+        sim.use_graph = use_graph
+        for _ in range(4):
+            sim.forward(scene.n_substeps)
+        torch.cuda.synchronize()
+        res.append((_np(sim.mesh_dy.x4), _np(sim.mesh_dy.v4), _np(sim.mesh_dy.y4)))
+    for a, b in zip(*res):
+        assert np.array_equal(a, b)
