@@ -50,6 +50,7 @@ def parse_args():
     ap.add_argument("--workload", choices=["drape256", "plain64"], default="drape256")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of replaying a graph")
+    ap.add_argument("--no-lbvh", action="store_true", help="skip the standalone 2^20-triangle LBVH measurement")
     return ap.parse_args()
 
 
@@ -218,6 +219,76 @@ def cpu_baseline(scene, rank):
     return {"value": V * n / el, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{n} substep(s) of the same scene on the CPU oracle (OpenMP, {cores} threads), "
                       f"{el:.2f} s"}
+
+
+def lbvh_soup(pkg, reps=10, with_cpu=True):
+    """Standalone broad phase on 2^20 random triangles: build ms (scene box,
+    Morton codes, 32-bit key/index radix sort, Karras hierarchy, refit) and query
+    ms for 2^20 vertex boxes with padding 2e-3, each the mean of `reps` runs
+    timed with CUDA events (L2 flushed before each)."""
+    import numpy as np
+    import torch
+
+    n = 1 << 20
+    verts, faces, queries = pkg.scenes.triangle_soup(n, seed=0)
+    V4 = torch.zeros((verts.shape[0], 4), dtype=torch.float32, device="cuda")
+    V4[:, :3] = torch.from_numpy(verts).cuda()
+    Q4 = torch.zeros((n, 4), dtype=torch.float32, device="cuda")
+    Q4[:, :3] = torch.from_numpy(queries).cuda()
+    F = torch.from_numpy(faces.reshape(-1)).cuda()
+    from starlab_physics_gb300._lib import ptr, stream_handle, sx
+
+    fmn = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+    fmx = torch.empty_like(fmn)
+    box = torch.empty(6, dtype=torch.float32, device="cuda")
+    sx.sx_face_aabbs(ptr(V4), ptr(F), n, 0.0, ptr(fmn), ptr(fmx), stream_handle())
+    bvh = pkg.LBVH(n, "cuda", tie=1)
+    cap = 32
+    cand = torch.empty((n, cap), dtype=torch.int32, device="cuda")
+    num = torch.empty(n, dtype=torch.int32, device="cuda")
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    stream = torch.cuda.current_stream()
+
+    def build():
+        sx.sx_scene_aabb(ptr(V4), V4.shape[0], 0.0, ptr(box), stream_handle())
+        bvh.build(fmn, fmx, box)
+
+    build()
+    bvh.query(Q4, 2e-3, cap, cand, num)
+    torch.cuda.synchronize()
+    tb, tq = [], []
+    for _ in range(reps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        build()
+        b.record(stream)
+        flush.zero_()
+        c, d = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        c.record(stream)
+        bvh.query(Q4, 2e-3, cap, cand, num)
+        d.record(stream)
+        torch.cuda.synchronize()
+        tb.append(a.elapsed_time(b))
+        tq.append(c.elapsed_time(d))
+    out = {"workload": "2^20-triangle soup, 2^20 queries, padding 2e-3", "build_ms": round(sum(tb) / reps, 4),
+           "query_ms": round(sum(tq) / reps, 4), "candidates": int(num.sum().item()),
+           "sort_bytes_per_build": n * 64}
+    if with_cpu:
+        from oracle import pyoracle as po
+
+        vv = np.zeros((verts.shape[0], 4), np.float32)
+        vv[:, :3] = verts
+        mn, mx = po.face_aabbs(vv, faces, 0.0)
+        t0 = time.perf_counter()
+        fb = po.FaceBVH(mn, mx, po.scene_aabb(vv, 0.0), tie=1)
+        t1 = time.perf_counter()
+        ok = bool(np.array_equal(bvh.sorted_ids.cpu().numpy(), fb.sorted_ids)
+                  and np.array_equal(bvh.child_a.cpu().numpy(), fb.child_a))
+        out["cpu_baseline_build_ms"] = round(1e3 * (t1 - t0), 1)
+        out["cpu_baseline_kind"] = "port (serial oracle)"
+        out["matches_oracle"] = ok
+    return out
 
 
 def run_reference(args):
@@ -392,6 +463,8 @@ def main():
         "status_flags": status,
     }
     line["clocks_e2e"] = clk2.summary()
+    if rank == 0 and not args.no_lbvh:
+        line["lbvh_soup"] = lbvh_soup(pkg, with_cpu=not args.no_cpu_baseline)
     if rank == 0 and world >= 1 and not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(scene, rank)
     if rank == 0:

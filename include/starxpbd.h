@@ -97,22 +97,24 @@ int sx_cell_bvh_init(int* sorted_codes, int* sorted_ids, int* child_a, int* chil
  * Outputs: sorted_face_ids[n_faces], prefix[32768] (inclusive),
  * num_faces[65535], nmin4/nmax4[65535] (nmin4.w = the node's face count as
  * int bits), face_rec8[8*n_faces] (per sorted face: min xyz + face id bits,
- * max xyz + 0; what the traversal scans), cell_size3[3]. */
+ * max xyz + 0; what the traversal scans), grid8[8] = {cell size xyz, the
+ * largest distance any leaf box reaches beyond its cell per axis, 0, 0}. */
 int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_faces, const float* box6, const int* child_a,
                       const int* child_b, const int* parent, int* sorted_face_ids, int* prefix, int* num_faces,
-                      float* nmin4, float* nmax4, float* face_rec8, float* cell_size3, void* ws, size_t ws_bytes,
+                      float* nmin4, float* nmax4, float* face_rec8, float* grid8, void* ws, size_t ws_bytes,
                       void* stream);
 
 /* traverse_cell_bvh_single, lbvh_cell.py:656-714, for query boxes
  * p4[i] +- padding (Solver.broadphase_lbvh, XPBD.py:187-215), over a build's
- * nodes and face records.  origin = box6 of the build (its min corner is the
- * grid origin).  cand[q*cap + j] for j < cap; num[q] = total overlaps found
- * (num > cap: list truncated, status bit 1).  Candidates come out in the
- * reference's visiting order. */
-int sx_cell_bvh_traverse(const float* p4, int n_queries, float padding, const float* cell_size3,
-                         const float* origin_box6, const int* child_a, const int* child_b, const float* nmin4,
-                         const float* nmax4, const int* prefix, const float* face_rec8, int cap, int* cand, int* num,
-                         int* status, void* stream);
+ * nodes, grid8 and face records.  origin = box6 of the build (its min corner is
+ * the grid origin).  cand[q*cap + j] for j < cap; num[q] = total overlaps
+ * found (num > cap: list truncated, status bit 1).  Candidates come out in
+ * the reference's depth-first visiting order, which for the cell tree is
+ * descending cell index; the walk visits the cells within the leaves' reach of
+ * each query box in that order. */
+int sx_cell_bvh_traverse(const float* p4, int n_queries, float padding, const float* grid8, const float* origin_box6,
+                         const float* nmin4, const float* nmax4, const int* prefix, const float* face_rec8, int cap,
+                         int* cand, int* num, int* status, void* stream);
 
 /* ---- face-level LBVH (standalone broad phase) ------------------------------ */
 
@@ -127,6 +129,7 @@ int sx_face_morton(const float* fmin4, const float* fmax4, int n_faces, const fl
  * warp-ranked stable scatter give the same permutation). In place. */
 size_t sx_radix_sort_workspace_bytes(int n);
 int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, void* ws, size_t ws_bytes, void* stream);
+
 
 /* Karras 2012 hierarchy over sorted codes (assign_internal_nodes_Karras12,
  * lbvh_cell.py:384-405, with delta/find_split/determine_range :256-336).

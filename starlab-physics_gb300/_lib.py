@@ -42,7 +42,7 @@ SIGNATURES = {
     "sx_cell_bvh_workspace_bytes": ([I], Z),
     "sx_cell_bvh_init": ([P, P, P, P, P, P, P, P, Z, P], I),
     "sx_cell_bvh_build": ([P, P, I, P, P, P, P, P, P, P, P, P, P, P, P, Z, P], I),
-    "sx_cell_bvh_traverse": ([P, I, F, P, P, P, P, P, P, P, P, I, P, P, P, P], I),
+    "sx_cell_bvh_traverse": ([P, I, F, P, P, P, P, P, P, I, P, P, P, P], I),
     "sx_face_morton": ([P, P, I, P, P, P, P], I),
     "sx_radix_sort_workspace_bytes": ([I], Z),
     "sx_radix_sort_pairs": ([P, P, I, I, P, Z, P], I),

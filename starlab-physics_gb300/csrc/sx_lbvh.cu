@@ -260,14 +260,16 @@ __global__ void karras_kernel(int n, const unsigned* __restrict__ c, int tie, in
 // ---------------------------------------------------------------------------
 __global__ void face_cell_kernel(int F, const float4* __restrict__ mn4, const float4* __restrict__ mx4,
                                  const float* __restrict__ box6, unsigned* keys, int* ids, unsigned* counts,
-                                 float* cell_size3) {
+                                 float* grid8) {
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     V3 lo{box6[0], box6[1], box6[2]};
     V3 cs = cell_size_of(box6);
     if (f == 0) {
-        cell_size3[0] = cs.x;
-        cell_size3[1] = cs.y;
-        cell_size3[2] = cs.z;
+        grid8[0] = cs.x;
+        grid8[1] = cs.y;
+        grid8[2] = cs.z;
+        grid8[3] = grid8[4] = grid8[5] = 0.0f;  // max leaf overhang, raised by the leaf kernel
+        grid8[6] = grid8[7] = 0.0f;
     }
     if (f >= F) return;
     V3 c = scale(0.5f, add(mk(mn4[f]), mk(mx4[f])));
@@ -301,7 +303,7 @@ __global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int
                                        const float4* __restrict__ fmx4, const int* __restrict__ child_a,
                                        const int* __restrict__ child_b, const int* __restrict__ parent,
                                        int* num_faces, float4* nmin4, float4* nmax4, float4* frec, int* flags,
-                                       int* status) {
+                                       int* status, float* grid8) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kNumCells) return;
     V3 lo{box6[0], box6[1], box6[2]};
@@ -321,6 +323,21 @@ __global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int
     }
     num_faces[leaf] = size;
     store_box(nmin4, nmax4, leaf, a, b, size);
+    // How far this leaf's box reaches beyond its cell (>= 0), maximised over the
+    // grid: the traversal scans the cells within that reach of a query box.
+    {
+        const int x0 = i / (kGridRes * kGridRes), y0 = (i % (kGridRes * kGridRes)) / kGridRes, z0 = i % kGridRes;
+        const float clo[3] = {lo.x + cs.x * (float)x0, lo.y + cs.y * (float)y0, lo.z + cs.z * (float)z0};
+        const float chi[3] = {lo.x + cs.x * (float)(x0 + 1), lo.y + cs.y * (float)(y0 + 1),
+                              lo.z + cs.z * (float)(z0 + 1)};
+        const float am[3] = {a.x, a.y, a.z}, bm[3] = {b.x, b.y, b.z};
+        for (int k = 0; k < 3; ++k) {
+            float ext = size > 0 ? fmaxf(fmaxf(clo[k] - am[k], bm[k] - chi[k]), 0.0f) : 0.0f;
+            for (int o = 16; o > 0; o >>= 1) ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
+            if ((threadIdx.x & 31) == 0 && ext > 0.0f)
+                atomicMax(reinterpret_cast<unsigned*>(grid8) + 3 + k, __float_as_uint(ext));
+        }
+    }
     int node = parent[leaf];
     for (int steps = 0; node >= 0; ++steps) {
         if (steps > kNumCells) {
@@ -353,67 +370,70 @@ __global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int
     }
 }
 
-// traverse_cell_bvh_single (lbvh_cell.py:662-714).  The reference pops a node,
-// skips it when empty or not overlapping, and otherwise either scans the
-// leaf's faces or pushes child_a then child_b.  Testing a child's emptiness and
-// overlap before pushing it instead of after popping it visits the overlapping
-// nodes in the same order, so the candidate list is the same, with fewer
-// stack operations and one float4 pair per child.
+// traverse_cell_bvh_single (lbvh_cell.py:662-714) as a walk over grid cells.
+//
+// The reference pops a node, skips it when empty or not overlapping, and
+// otherwise scans a leaf's faces or pushes child_a then child_b.  The cell tree
+// is always the perfect tree that the Karras build makes over the 32^3
+// distinct cell codes, child_a covering the lower half of a node's leaf slots,
+// and leaf slot i holds row-major cell i (lbvh_cell.py:604-634).  Its
+// depth-first walk therefore reaches exactly the non-empty leaves whose boxes
+// overlap the query (every ancestor of such a leaf contains its box), in
+// descending slot = descending cell index.  A leaf's box is its cell grown by
+// at most the build's maximum overhang (grid8[3..5]), so scanning the cells
+// within that reach of the query box, in descending index, and applying the
+// same leaf and face tests produces the same candidate list in the same order,
+// with independent loads instead of a chain of dependent node fetches.
+__device__ __forceinline__ void cell_range(float qa, float qb, float o, float c, float e, int* i0, int* i1) {
+    // one extra cell on each side absorbs rounding in the divisions
+    const float f0 = floorf((qa - e - o) / c) - 1.0f, f1 = floorf((qb + e - o) / c) + 1.0f;
+    *i0 = (int)fmaxf(f0, 0.0f);
+    *i1 = (int)fminf(f1, (float)(kGridRes - 1));
+}
+
 __global__ void __launch_bounds__(128) cell_traverse_kernel(
-    int Q, const float4* __restrict__ p4, float pad, const float* __restrict__ cs3, const float* __restrict__ box6,
-    const int* __restrict__ child_a, const int* __restrict__ child_b, const float4* __restrict__ nmin4,
-    const float4* __restrict__ nmax4, const int* __restrict__ prefix, const float4* __restrict__ frec, int cap,
-    int* __restrict__ cand, int* __restrict__ num, int* status) {
+    int Q, const float4* __restrict__ p4, float pad, const float* __restrict__ grid8, const float* __restrict__ box6,
+    const float4* __restrict__ nmin4, const float4* __restrict__ nmax4, const int* __restrict__ prefix,
+    const float4* __restrict__ frec, int cap, int* __restrict__ cand, int* __restrict__ num, int* status) {
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= Q) return;
     V3 p = mk(p4[q]);
     V3 a{p.x - pad, p.y - pad, p.z - pad}, b{p.x + pad, p.y + pad, p.z + pad};
     V3 pos = scale(0.5f, add(a, b));
-    V3 cs{cs3[0], cs3[1], cs3[2]}, org{box6[0], box6[1], box6[2]};
+    V3 cs{grid8[0], grid8[1], grid8[2]}, org{box6[0], box6[1], box6[2]};
     int ix = f2i_sat((pos.x - org.x) / cs.x), iy = f2i_sat((pos.y - org.y) / cs.y),
         iz = f2i_sat((pos.z - org.z) / cs.z);
     int cid = (int)((unsigned)ix * (unsigned)(kGridRes * kGridRes) + (unsigned)iy * (unsigned)kGridRes + (unsigned)iz);
     int count = 0;
-    int flags = 0;
     int* out = cand + (size_t)q * cap;
-    if (cid <= kNumCells - 1) {
-        int stack[64];
-        int sc = 0;
-        const float4 rmn = nmin4[0], rmx = nmax4[0];
-        if (__float_as_int(rmn.w) > 0 && overlap(a, b, mk(rmn), mk(rmx))) stack[sc++] = 0;
-        long long pops = 0;
-        while (sc > 0) {
-            if (++pops > 2LL * kNumCells) {
-                flags |= SX_STATUS_STACK_OVERFLOW;
-                break;
-            }
-            const int idx = stack[--sc];
-            if (idx >= kNumCells - 1) {
-                const int i = idx - (kNumCells - 1);
-                const int rl = i == 0 ? 0 : prefix[i - 1];
-                const int re = prefix[i];
-                for (int j = rl; j < re; ++j) {
-                    const float4 fa = frec[2 * j], fb = frec[2 * j + 1];
-                    if (overlap(a, b, mk(fa), mk(fb))) {
-                        if (count < cap) out[count] = __float_as_int(fa.w);
-                        ++count;
+    if (cid <= kNumCells - 1) {  // the reference's skip rule (lbvh_cell.py:665)
+        int x0, x1, y0, y1, z0, z1;
+        cell_range(a.x, b.x, org.x, cs.x, grid8[3], &x0, &x1);
+        cell_range(a.y, b.y, org.y, cs.y, grid8[4], &y0, &y1);
+        cell_range(a.z, b.z, org.z, cs.z, grid8[5], &z0, &z1);
+        for (int cx = x1; cx >= x0; --cx) {
+            for (int cy = y1; cy >= y0; --cy) {
+                for (int cz = z1; cz >= z0; --cz) {
+                    const int i = cx * kGridRes * kGridRes + cy * kGridRes + cz;
+                    const int leaf = i + kNumCells - 1;
+                    const float4 lmn = nmin4[leaf];
+                    if (__float_as_int(lmn.w) <= 0) continue;
+                    if (!overlap(a, b, mk(lmn), mk(nmax4[leaf]))) continue;
+                    const int rl = i == 0 ? 0 : prefix[i - 1];
+                    const int re = prefix[i];
+                    for (int j = rl; j < re; ++j) {
+                        const float4 fa = frec[2 * j], fb = frec[2 * j + 1];
+                        if (overlap(a, b, mk(fa), mk(fb))) {
+                            if (count < cap) out[count] = __float_as_int(fa.w);
+                            ++count;
+                        }
                     }
-                }
-            } else {
-                const int l = child_a[idx], r = child_b[idx];
-                const float4 lmn = nmin4[l], lmx = nmax4[l], rmn2 = nmin4[r], rmx2 = nmax4[r];
-                if (__float_as_int(lmn.w) > 0 && overlap(a, b, mk(lmn), mk(lmx))) {
-                    if (sc < 64) stack[sc++] = l; else flags |= SX_STATUS_STACK_OVERFLOW;
-                }
-                if (__float_as_int(rmn2.w) > 0 && overlap(a, b, mk(rmn2), mk(rmx2))) {
-                    if (sc < 64) stack[sc++] = r; else flags |= SX_STATUS_STACK_OVERFLOW;
                 }
             }
         }
     }
     num[q] = count;
-    if (count > cap) flags |= SX_STATUS_CAND_OVERFLOW;
-    if (flags) atomicOr(status, flags);
+    if (count > cap) atomicOr(status, SX_STATUS_CAND_OVERFLOW);
 }
 
 // ---------------------------------------------------------------------------
@@ -556,9 +576,9 @@ extern "C" int sx_cell_bvh_init(int* sorted_codes, int* sorted_ids, int* child_a
 extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_faces, const float* box6,
                                  const int* child_a, const int* child_b, const int* parent, int* sorted_face_ids,
                                  int* prefix, int* num_faces, float* nmin4, float* nmax4, float* face_rec8,
-                                 float* cell_size3, void* ws, size_t ws_bytes, void* stream) {
+                                 float* grid8, void* ws, size_t ws_bytes, void* stream) {
     SX_REQUIRE(n_faces >= 0, "sx_cell_bvh_build: n_faces < 0");
-    SX_REQUIRE(box6 && child_a && child_b && parent && prefix && num_faces && nmin4 && nmax4 && cell_size3,
+    SX_REQUIRE(box6 && child_a && child_b && parent && prefix && num_faces && nmin4 && nmax4 && grid8,
                "sx_cell_bvh_build: null pointer");
     SX_REQUIRE(n_faces == 0 || (fmin4 && fmax4 && sorted_face_ids && face_rec8),
                "sx_cell_bvh_build: null face arrays");
@@ -573,7 +593,7 @@ extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_f
     SX_CUDA(cudaMemsetAsync(prefix, 0, sizeof(int) * kNumCells, s));
     SX_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * kNumCells, s));
     launch(face_cell_kernel, grid_for(n_faces, 256), 256, 0, s, n_faces, (const float4*)fmin4, (const float4*)fmax4,
-           box6, keys, sorted_face_ids, (unsigned*)prefix, cell_size3);
+           box6, keys, sorted_face_ids, (unsigned*)prefix, grid8);
     int rc = check_launch("face_cell_kernel");
     if (rc) return rc;
     launch(scan_single_block, 1, 1024, 0, s, (unsigned*)prefix, kNumCells, 1);
@@ -585,22 +605,22 @@ extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_f
     int* status = flags + (kNumCells - 1);
     launch(cell_leaf_refit_kernel, grid_for(kNumCells, 256), 256, 0, s, box6, (const int*)prefix,
            (const int*)sorted_face_ids, (const float4*)fmin4, (const float4*)fmax4, child_a, child_b, parent,
-           num_faces, (float4*)nmin4, (float4*)nmax4, (float4*)face_rec8, flags, status);
+           num_faces, (float4*)nmin4, (float4*)nmax4, (float4*)face_rec8, flags, status, grid8);
     return check_launch("cell_leaf_refit_kernel");
 }
 
-extern "C" int sx_cell_bvh_traverse(const float* p4, int n_queries, float padding, const float* cell_size3,
-                                    const float* origin_box6, const int* child_a, const int* child_b,
-                                    const float* nmin4, const float* nmax4, const int* prefix,
+extern "C" int sx_cell_bvh_traverse(const float* p4, int n_queries, float padding, const float* grid8,
+                                    const float* origin_box6, const float* nmin4, const float* nmax4,
+                                    const int* prefix,
                                     const float* face_rec8, int cap, int* cand, int* num, int* status,
                                     void* stream) {
     SX_REQUIRE(n_queries >= 0 && cap >= 1, "sx_cell_bvh_traverse: bad sizes");
     if (n_queries == 0) return SX_OK;
-    SX_REQUIRE(p4 && cell_size3 && origin_box6 && child_a && child_b && nmin4 && nmax4 && prefix && face_rec8 &&
+    SX_REQUIRE(p4 && grid8 && origin_box6 && nmin4 && nmax4 && prefix && face_rec8 &&
                    cand && num && status,
                "sx_cell_bvh_traverse: null pointer");
     launch(cell_traverse_kernel, grid_for(n_queries, 128), 128, 0, as_stream(stream), n_queries, (const float4*)p4,
-           padding, cell_size3, origin_box6, child_a, child_b, (const float4*)nmin4, (const float4*)nmax4, prefix,
+           padding, grid8, origin_box6, (const float4*)nmin4, (const float4*)nmax4, prefix,
            (const float4*)face_rec8, cap, cand, num, status);
     return check_launch("cell_traverse_kernel");
 }

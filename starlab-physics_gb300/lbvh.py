@@ -53,7 +53,8 @@ class LBVH_CELL:
         self.node_min4 = torch.zeros((2 * n - 1, 4), dtype=torch.float32, device=dev)
         self.node_max4 = torch.zeros((2 * n - 1, 4), dtype=torch.float32, device=dev)
         self.face_rec8 = torch.zeros((max(self.num_leafs, 1), 8), dtype=torch.float32, device=dev)
-        self.cell_size = torch.zeros(3, dtype=torch.float32, device=dev)
+        # grid8 = cell size xyz, largest leaf overhang beyond its cell xyz, 0, 0
+        self.grid8 = torch.zeros(8, dtype=torch.float32, device=dev)
         self.box6 = torch.zeros(6, dtype=torch.float32, device=dev)
         ws = int(sx.sx_cell_bvh_workspace_bytes(self.num_leafs))
         self.workspace = torch.empty(ws, dtype=torch.uint8, device=dev)
@@ -67,6 +68,11 @@ class LBVH_CELL:
     def origin(self):
         """Grid origin (device tensor view of the build box's min corner)."""
         return self.box6[:3]
+
+    @property
+    def cell_size(self):
+        """Cell size of the last build (device tensor view)."""
+        return self.grid8[:3]
 
     def build(self, mesh, aabb_min_g=None, aabb_max_g=None, *, face_min4=None, face_max4=None):
         """``LBVH_CELL.build`` (lbvh_cell.py:637-653).
@@ -86,15 +92,14 @@ class LBVH_CELL:
         sx.sx_cell_bvh_build(ptr(fmn), ptr(fmx), nf, ptr(self.box6), ptr(self.child_a), ptr(self.child_b),
                              ptr(self.parent), ptr(self.sorted_face_ids), ptr(self.prefix_sum_cell),
                              ptr(self.num_faces), ptr(self.node_min4), ptr(self.node_max4), ptr(self.face_rec8),
-                             ptr(self.cell_size), ptr(self.workspace), self.workspace.numel(), stream_handle())
+                             ptr(self.grid8), ptr(self.workspace), self.workspace.numel(), stream_handle())
 
     def traverse(self, points4, padding: float, cap: int, cand, num, status, n_queries=None):
         """``traverse_cell_bvh_single`` for boxes ``points4[i] +- padding``."""
         q = points4.shape[0] if n_queries is None else n_queries
-        sx.sx_cell_bvh_traverse(ptr(points4), q, float(padding), ptr(self.cell_size), ptr(self.box6),
-                                ptr(self.child_a), ptr(self.child_b), ptr(self.node_min4), ptr(self.node_max4),
-                                ptr(self.prefix_sum_cell), ptr(self.face_rec8), int(cap), ptr(cand), ptr(num),
-                                ptr(status), stream_handle())
+        sx.sx_cell_bvh_traverse(ptr(points4), q, float(padding), ptr(self.grid8), ptr(self.box6),
+                                ptr(self.node_min4), ptr(self.node_max4), ptr(self.prefix_sum_cell),
+                                ptr(self.face_rec8), int(cap), ptr(cand), ptr(num), ptr(status), stream_handle())
 
 
 class LBVH:

@@ -162,6 +162,41 @@ def test_cell_bvh_build_and_traverse(pkg, po):
         assert int(status.item()) == rs
 
 
+@pytest.mark.parametrize("size,seed", [(0.004, 1), (0.08, 2), (0.3, 3)])
+def test_cell_traverse_adversarial(pkg, po, size, seed):
+    """Faces that overhang many cells and queries inside, outside and on the edge
+    of the grid: the cell walk must reproduce the reference's depth-first list."""
+    rng = np.random.default_rng(seed)
+    F = 20000
+    c = rng.uniform(0, 1, (F, 3)).astype(np.float32)
+    e = (rng.uniform(0, size, (F, 3)) * rng.uniform(0, 1, (F, 1)) ** 4).astype(np.float32)
+    mn = np.zeros((F, 4), np.float32)
+    mx = np.zeros((F, 4), np.float32)
+    mn[:, :3], mx[:, :3] = c - e, c + e
+    box = np.array([-0.05, -0.05, -0.05, 1.05, 1.05, 1.05], np.float32)
+    bvh = pkg.LBVH_CELL(F, DEV)
+    bvh.build(None, _t(box), face_min4=_t(mn), face_max4=_t(mx))
+    ref = po.CellBVH()
+    ref.build(mn, mx, box)
+    assert np.array_equal(_np(bvh.node_min4), ref.nmin4) and np.array_equal(_np(bvh.node_max4), ref.nmax4)
+    pts = np.zeros((30000, 4), np.float32)
+    pts[:, :3] = rng.uniform(-0.2, 1.2, (30000, 3))
+    pts[:100, :3] = np.array([1.05, 0.5, 0.5], np.float32)   # on the upper face of the grid
+    cap = 64
+    cand = torch.full((pts.shape[0], cap), -1, dtype=torch.int32, device=DEV)
+    num = torch.zeros(pts.shape[0], dtype=torch.int32, device=DEV)
+    status = torch.zeros(1, dtype=torch.int32, device=DEV)
+    for pad in (0.002, 0.05):
+        bvh.traverse(_t(pts), pad, cap, cand, num, status)
+        qmn, qmx = po.query_boxes(pts, pad)
+        rc, rn, rs = ref.traverse(qmn, qmx, cap)
+        assert np.array_equal(_np(num), rn)
+        gc = _np(cand)
+        for q in range(pts.shape[0]):
+            k = min(rn[q], cap)
+            assert np.array_equal(gc[q, :k], rc[q, :k]), q
+
+
 def test_face_lbvh_small_soup(pkg, po):
     verts, faces, queries = pkg.scenes.triangle_soup(1 << 14, seed=5)
     V4 = np.zeros((verts.shape[0], 4), np.float32)
