@@ -130,6 +130,18 @@ int sx_face_morton(const float* fmin4, const float* fmax4, int n_faces, const fl
 size_t sx_radix_sort_workspace_bytes(int n);
 int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, void* ws, size_t ws_bytes, void* stream);
 
+/* The same sort for callers that cannot allocate device memory when they
+ * sort -- e.g. hosts whose device memory belongs to another allocator with a
+ * fixed budget, or real-time loops that cannot take the synchronisation a
+ * cudaMalloc may cause.  It takes no workspace and allocates nothing: its
+ * scratch is a fixed array in the library's own device memory (about 2.1 MB,
+ * held on every GPU that loads the library until the process exits).
+ * n is limited to 262144 (2^18) keys; larger n returns SX_ERR_ARG.  The first
+ * call on a device looks up the array's device address with that device
+ * current; make that first call before any stream capture.  All calls share
+ * the array, so calls that overlap on the GPU race and must be ordered by the
+ * caller.  This entry point has no counterpart in the reference. */
+int sx_radix_sort_pairs_noalloc(unsigned* keys, int* vals, int n, int bits, void* stream);
 
 /* Karras 2012 hierarchy over sorted codes (assign_internal_nodes_Karras12,
  * lbvh_cell.py:384-405, with delta/find_split/determine_range :256-336).

@@ -46,6 +46,7 @@ SIGNATURES = {
     "sx_face_morton": ([P, P, I, P, P, P, P], I),
     "sx_radix_sort_workspace_bytes": ([I], Z),
     "sx_radix_sort_pairs": ([P, P, I, I, P, Z, P], I),
+    "sx_radix_sort_pairs_noalloc": ([P, P, I, I, P], I),
     "sx_karras_build": ([P, I, I, P, P, P, P, P, P], I),
     "sx_face_bvh_refit": ([I, P, P, P, P, P, P, P, P, P, P, P], I),
     "sx_face_bvh_traverse": ([I, P, I, F, P, P, P, P, P, I, P, P, P, P], I),

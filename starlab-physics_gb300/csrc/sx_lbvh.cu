@@ -2,6 +2,8 @@
 // single-launch bottom-up refit and stack traversal, for the reference's 32^3
 // cell-grid BVH (framework/collision/lbvh_cell.py, class LBVH_CELL) and for a
 // face-level LBVH over triangle soups.
+#include <mutex>
+
 #include "sx_common.cuh"
 
 namespace sx {
@@ -535,6 +537,68 @@ extern "C" int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, v
     if (n <= 1) return SX_OK;
     SX_REQUIRE(keys && vals, "sx_radix_sort_pairs: null pointer");
     return radix_sort(keys, vals, n, bits, ws, ws_bytes, as_stream(stream));
+}
+
+// ---------------------------------------------------------------------------
+// Radix sort without a caller-provided workspace.
+//
+// Some callers cannot allocate device memory when they need to sort: hosts
+// whose device memory belongs to another allocator with a fixed budget (a
+// framework's caching pool, an engine's arena), where an extra cudaMalloc can
+// fail or fragment the pool, and real-time loops that cannot afford the
+// device-wide synchronisation cudaMalloc/cudaFree may cause.  For them the
+// sort's scratch (two key/value ping-pong buffers and the digit histograms)
+// lives in one fixed array in this library's device memory, sized for at most
+// kNoAllocMaxKeys keys.  Every GPU that loads the library keeps the array
+// (about 2.1 MB) until the process exits.
+//
+// In host code the array's name is only a host-side stand-in for the symbol, so
+// its device address is looked up once per device, on the first call made with
+// that device current, with cudaGetSymbolAddress; that first call should come
+// before any stream capture.  All calls share the array: calls that overlap on
+// the GPU (different streams, or threads) race on it and must be ordered by the
+// caller.  Nothing in it needs clearing: every pass overwrites the histogram
+// and both ping-pong buffers before reading them.
+// ---------------------------------------------------------------------------
+constexpr int kNoAllocMaxKeys = 1 << 18;
+constexpr size_t kNoAllocScratchBytes =
+    2 * (((size_t)kNoAllocMaxKeys * 4 + 255) & ~(size_t)255) +
+    (((size_t)256 * ((kNoAllocMaxKeys + RS_TILE - 1) / RS_TILE) * 4 + 255) & ~(size_t)255);
+static __device__ __align__(256) unsigned char g_sort_scratch[kNoAllocScratchBytes];
+
+constexpr int kMaxDevices = 64;
+static std::mutex g_scratch_mutex;
+static void* g_scratch_addr[kMaxDevices] = {};
+
+static int sort_scratch_for_current_device(void** out) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_status(e, "cudaGetDevice");
+    SX_REQUIRE(dev >= 0 && dev < kMaxDevices, "sx_radix_sort_pairs_noalloc: device %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (g_scratch_addr[dev] == nullptr) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_sort_scratch);
+        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_sort_scratch)");
+        g_scratch_addr[dev] = p;
+    }
+    *out = g_scratch_addr[dev];
+    return SX_OK;
+}
+
+extern "C" int sx_radix_sort_pairs_noalloc(unsigned* keys, int* vals, int n, int bits, void* stream) {
+    SX_REQUIRE(n >= 0, "sx_radix_sort_pairs_noalloc: n < 0");
+    SX_REQUIRE(n <= kNoAllocMaxKeys,
+               "sx_radix_sort_pairs_noalloc: %d keys exceed the fixed scratch capacity of %d keys; "
+               "use sx_radix_sort_pairs with a workspace",
+               n, kNoAllocMaxKeys);
+    if (n <= 1) return SX_OK;
+    SX_REQUIRE(keys && vals, "sx_radix_sort_pairs_noalloc: null pointer");
+    SX_REQUIRE(rs_ws_bytes(n) <= kNoAllocScratchBytes, "sx_radix_sort_pairs_noalloc: scratch layout mismatch");
+    void* scratch = nullptr;
+    int rc = sort_scratch_for_current_device(&scratch);
+    if (rc) return rc;
+    return radix_sort(keys, vals, n, bits, scratch, kNoAllocScratchBytes, as_stream(stream));
 }
 
 extern "C" int sx_face_morton(const float* fmin4, const float* fmax4, int n_faces, const float* box6,

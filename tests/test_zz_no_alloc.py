@@ -1,0 +1,55 @@
+"""The allocation-free radix sort (sx_radix_sort_pairs_noalloc), for callers
+that cannot allocate device memory when they sort -- hosts whose device memory
+belongs to another allocator with a fixed budget, or loops that cannot take the
+synchronisation a cudaMalloc may cause.  It is called through the C ABI and
+compared with the workspace-taking sort on two calls in a row (the second call
+reuses the library's fixed scratch array left over from the first)."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+MAX_KEYS = 1 << 18
+
+
+def _keys(n, bits, seed):
+    rng = np.random.default_rng(seed)
+    hi = (1 << bits) if bits < 32 else (1 << 32)
+    k = rng.integers(0, hi, n, dtype=np.uint64).astype(np.uint32)
+    k[: n // 3] = k[n // 3: 2 * (n // 3)]   # repeated keys: the sort must stay stable
+    return k
+
+
+def test_noalloc_sort_matches_workspace_sort(pkg):
+    from starlab_physics_gb300 import _lib
+
+    L = _lib.load()
+    stream = torch.cuda.current_stream().cuda_stream
+    for call, (n, bits) in enumerate([(200003, 30), (MAX_KEYS, 32)]):
+        keys = _keys(n, bits, seed=call)
+        vals = np.arange(n, dtype=np.int32)
+        k_ws = torch.from_numpy(keys.view(np.int32)).cuda()
+        v_ws = torch.from_numpy(vals).cuda()
+        k_na, v_na = k_ws.clone(), v_ws.clone()
+        ws = torch.empty(int(L.sx_radix_sort_workspace_bytes(n)), dtype=torch.uint8, device="cuda")
+        assert L.sx_radix_sort_pairs(k_ws.data_ptr(), v_ws.data_ptr(), n, bits, ws.data_ptr(), ws.numel(),
+                                     stream) == 0
+        rc = L.sx_radix_sort_pairs_noalloc(k_na.data_ptr(), v_na.data_ptr(), n, bits, stream)
+        assert rc == 0, L.sx_last_error()
+        torch.cuda.synchronize()
+        assert torch.equal(k_na, k_ws) and torch.equal(v_na, v_ws)       # integer outputs: exact
+        order = np.argsort(keys, kind="stable")
+        assert np.array_equal(v_na.cpu().numpy(), order)
+
+
+def test_noalloc_sort_rejects_oversize(pkg):
+    from starlab_physics_gb300 import _lib
+
+    L = _lib.load()
+    k = torch.zeros(MAX_KEYS + 1, dtype=torch.int32, device="cuda")
+    v = torch.zeros_like(k)
+    rc = L.sx_radix_sort_pairs_noalloc(k.data_ptr(), v.data_ptr(), MAX_KEYS + 1, 30,
+                                       torch.cuda.current_stream().cuda_stream)
+    assert rc == _lib.SX_ERR_ARG
+    assert b"capacity" in L.sx_last_error()
