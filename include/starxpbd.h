@@ -97,8 +97,10 @@ int sx_cell_bvh_init(int* sorted_codes, int* sorted_ids, int* child_a, int* chil
  * Outputs: sorted_face_ids[n_faces], prefix[32768] (inclusive),
  * num_faces[65535], nmin4/nmax4[65535] (nmin4.w = the node's face count as
  * int bits), face_rec8[8*n_faces] (per sorted face: min xyz + face id bits,
- * max xyz + 0; what the traversal scans), grid8[8] = {cell size xyz, the
- * largest distance any leaf box reaches beyond its cell per axis, 0, 0}. */
+ * max xyz + 0; what the traversal scans), grid8[1032] = {cell size xyz, the
+ * largest distance any leaf box reaches beyond its cell per axis, 0, 0,
+ * then 1024 uint32 occupancy words: bit z of word x*32 + y set when cell
+ * (x, y, z) holds faces}. */
 int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_faces, const float* box6, const int* child_a,
                       const int* child_b, const int* parent, int* sorted_face_ids, int* prefix, int* num_faces,
                       float* nmin4, float* nmax4, float* face_rec8, float* grid8, void* ws, size_t ws_bytes,
@@ -186,18 +188,50 @@ int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const int* faces
  * once per substep), so sx_contact_pairs_build flattens them once -- in query
  * order, dropping the incident faces __vt_dy skips (XPBD.py:258) -- into
  * pairs[max_pairs] (int4: query vertex, triangle vertices;
- * max_pairs >= (2*n_dy + n_st) * cap), and sx_contact_pairs_sweep then runs
- * one thread per pair followed by update_dx.  Same arithmetic and the same
- * order-independent accumulation as sx_collision_sweep, hence the same result;
- * pair records are only available from sx_collision_sweep. */
-size_t sx_contact_pairs_workspace_bytes(int n_dy, int n_st);
-int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* faces_st, int cap,
+ * max_pairs >= (2*n_dy + n_st) * cap) and, for self contact, also groups the
+ * pairs by triangle in the workspace.  sx_contact_pairs_sweep then evaluates
+ * per iteration each dynamic triangle's classifier terms once (a 192-byte
+ * record per triangle) and runs one thread per pair, followed by update_dx.
+ * Same values, decisions and order-independent accumulation as
+ * sx_collision_sweep, hence the same result; pair records are only available
+ * from sx_collision_sweep.  n_faces_dy = number of dynamic-mesh faces. */
+size_t sx_contact_pairs_workspace_bytes(int n_dy, int n_st, int n_faces_dy, int cap);
+int sx_contact_pairs_build(int n_dy, int n_st, int n_faces_dy, const int* faces_dy, const int* faces_st, int cap,
                            const int* vt_st_cand, const int* vt_st_num, const int* vt_dy_cand, const int* vt_dy_num,
                            const int* tv_st_cand, const int* tv_st_num, int* pairs, long long max_pairs, void* ws,
                            size_t ws_bytes, void* stream);
-int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4, const float* xs4,
-                           const float* fixed, const float* m_inv, float dHat, float compliance, long long* dx_fix,
-                           int* nc, int* status, void* stream);
+int sx_contact_pairs_sweep(int n_dy, int n_st, int n_faces_dy, const int* faces_dy, int cap, const int* pairs,
+                           void* ws, float* y4, const float* xs4, const float* fixed, const float* m_inv, float dHat,
+                           float compliance, long long* dx_fix, int* nc, int* status, void* stream);
+
+/* ---- batched independent cloths with obstacles ---------------------------- */
+
+/* computeAABB (meshTaichiWrapper.py:335-347) for each segment
+ * [seg_ptr[s], seg_ptr[s+1]) of a point array: box6[6*s..] = AABB +- padding. */
+int sx_segment_aabbs(const float* p4, const int* seg_ptr, int n_seg, float padding, float* box6, void* stream);
+
+/* Broad phase of the obstacle contacts of a batch (Solver.broadphase_lbvh,
+ * XPBD.py:187-215, restricted to each instance): for cloth vertex v of
+ * instance vinst[v], vmask[v] bit k = obstacle face ob_fptr[inst] + k is a
+ * candidate (padded boxes overlap, and the query is not skipped by the rule of
+ * lbvh_cell.py:665 on the obstacle's grid ob_box6[inst]); for obstacle vertex
+ * s of instance svinst[s], tv_cand[s*cap..] lists its cloth faces in
+ * [cl_fptr[inst], cl_fptr[inst+1]) (ascending, grid cl_box6[inst]).  These are
+ * the candidate sets the reference's cell-BVH traversal returns.  At most 32
+ * obstacle faces per instance. */
+int sx_batched_obstacle_broadphase(int n_verts, const float* y4, const int* vinst, const float* ob_box6,
+                                   const int* ob_fptr, const float* ob_fmin4, const float* ob_fmax4, float padding,
+                                   unsigned* vmask, int n_ob_verts, const float* xs4, const int* svinst,
+                                   const float* cl_box6, const int* cl_fptr, const float* cl_fmin4,
+                                   const float* cl_fmax4, int cap, int* tv_cand, int* tv_num, int* status,
+                                   void* stream);
+
+/* __vt_st / __tv_st (collision_constraints_x.py:6-173) over those candidates,
+ * fixed-point accumulation, then update_dx (XPBD.py:384-387). */
+int sx_batched_obstacle_contacts(int n_verts, float* y4, const float* fixed, const float* m_inv, const int* vinst,
+                                 const int* ob_fptr, const int* ob_faces, const float* xs4, const unsigned* vmask,
+                                 int n_ob_verts, const int* tv_cand, const int* tv_num, int cap, const int* cl_faces,
+                                 float dHat, float compliance, long long* dx_fix, int* nc, int* status, void* stream);
 
 /* ---- constraint-graph colouring (framework/utilities/graph_coloring.py) --- */
 

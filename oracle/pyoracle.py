@@ -292,8 +292,9 @@ class OracleSolver:
 
     def __init__(self, mesh_dy, mesh_st=None, *, dt, g, k_stretch_stiffness, k_bend_stiffness, dHat=4e-3,
                  damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
-                 compliance_collision=1e8, nthreads=1, bending_on="x"):
+                 compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True):
         self.d = mesh_dy
+        self.self_collision = self_collision
         self.s = mesh_st
         self.dt = float(dt)
         self.g = np.asarray(g, np.float32)
@@ -347,7 +348,10 @@ class OracleSolver:
         else:
             vt_st = (np.zeros((Vd, self.cap), np.int32), np.zeros(Vd, np.int32), 0)
             tv_st = (np.zeros((0, self.cap), np.int32), np.zeros(0, np.int32), 0)
-        vt_dy = self.bvh_dy.traverse(qmn, qmx, self.cap)
+        if self.self_collision:
+            vt_dy = self.bvh_dy.traverse(qmn, qmx, self.cap)
+        else:
+            vt_dy = (np.zeros((Vd, self.cap), np.int32), np.zeros(Vd, np.int32), 0)
         self.last_status |= vt_st[2] | vt_dy[2] | tv_st[2]
         return vt_st, vt_dy, tv_st
 

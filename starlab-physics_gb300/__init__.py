@@ -12,7 +12,8 @@ from .coloring import GraphColoring
 from .lbvh import LBVH, LBVH_CELL
 from .mesh import TriMesh, box_mesh, grid_cloth, icosphere
 from .solver import Solver
+from .batched import BatchedSolver, Instance, batched_scene
 from . import scenes
 
-__all__ = ["Solver", "LBVH_CELL", "LBVH", "GraphColoring", "TriMesh", "grid_cloth", "box_mesh", "icosphere",
-           "scenes", "SxError", "load_library", "library_path"]
+__all__ = ["Solver", "BatchedSolver", "Instance", "batched_scene", "LBVH_CELL", "LBVH", "GraphColoring", "TriMesh",
+           "grid_cloth", "box_mesh", "icosphere", "scenes", "SxError", "load_library", "library_path"]

@@ -1,0 +1,240 @@
+"""Many independent cloths, each with its own static obstacle, in one solver.
+
+The reference batches by concatenating meshes into one (``concat.py:11-58``,
+``Scenes/concat_test.py:20-41``), sharing one BVH.  Here instances are
+concatenated with per-instance offset tables (vertices, faces, obstacle
+vertices and faces) while every instance keeps the candidate semantics of its
+own pair of cell BVHs.  One launch per kernel covers every instance:
+
+* the Jacobi sweep runs over the concatenated vertex-centric adjacency (a
+  vertex only has neighbours in its own instance);
+* obstacle contacts (``__vt_st`` and ``__tv_st``) use per-instance grids and
+  brute-force candidate tests, which give the candidate sets the reference's
+  traversal gives (``sx_batched_obstacle_broadphase``);
+* self contact between a cloth and itself (``__vt_dy``) is not part of the
+  batched workload (obstacle contacts only).
+
+Each instance's result equals that instance alone in :class:`Solver` with
+``self_collision = False`` and ``rebuild = "substep"``.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+import torch
+
+from ._lib import load, ptr, stream_handle, sx
+from .mesh import bending_pairs, box_mesh, constraint_adjacency, edges_from_faces, grid_cloth, inverse_masses, \
+    rest_lengths
+
+
+@dataclass
+class Instance:
+    x: np.ndarray          # float32[V,3] rest positions
+    faces: np.ndarray      # int32[F,3]
+    pinned: np.ndarray     # vertex ids (local) with fixed = 0
+    obstacle_x: np.ndarray
+    obstacle_faces: np.ndarray
+
+
+def batched_scene(n_instances: int = 512, seed: int = 0, n_min: int = 16, n_max: int = 128, spacing: float = 1.5):
+    """Seeded batch: instance i is an N_i x N_i cloth (N_i uniform in [n_min, n_max])
+    on the unit square at height 1, jittered +-1e-4, corners at y = 1 pinned,
+    over its own box (side 0.5, centre randomised around (0.5, 0.5, 0.3)); the
+    instances sit on a grid of `spacing` so that they never touch."""
+    rng = np.random.default_rng(seed)
+    cols = int(np.ceil(np.sqrt(n_instances)))
+    out = []
+    for i in range(n_instances):
+        n = int(rng.integers(n_min, n_max + 1))
+        ox, oy = spacing * (i % cols), spacing * (i // cols)
+        x, f = grid_cloth(n, origin=(ox, oy), height=1.0)
+        x = (x + rng.uniform(-1e-4, 1e-4, size=x.shape).astype(np.float32)).astype(np.float32)
+        c = (ox + 0.5 + rng.uniform(-0.2, 0.2), oy + 0.5 + rng.uniform(-0.2, 0.2), 0.3 + rng.uniform(0.0, 0.3))
+        bx, bf = box_mesh(0.5, center=c)
+        out.append(Instance(x, f, np.array([(n - 1) * n, n * n - 1]), bx, bf))
+    return out
+
+
+class BatchedSolver:
+    """XPBD substep for a batch of independent cloths with obstacles."""
+
+    def __init__(self, instances, dHat, stiffness_stretch, stiffness_bending, g, dt, *, n_iter=20, cap=40,
+                 bending_on="y", padding=8e-3, damping=0.001, device="cuda"):
+        dev = torch.device(device)
+        self.device = dev
+        self.n_instances = len(instances)
+        self.dHat = float(dHat)
+        self.stiffness_stretch = float(stiffness_stretch)
+        self.stiffness_bending = float(stiffness_bending)
+        self.g = tuple(float(c) for c in g)
+        self.dt = float(dt)
+        self.n_iter = int(n_iter)
+        self.cap = int(cap)
+        self.bending_on = bending_on
+        self.padding = float(padding)
+        self.damping = float(damping)
+        self.compliance_collision = 1e8
+        self.use_graph = False
+        self._graphs = {}
+        self.graph_kernel_launches = 0
+
+        xs, fs, es, l0s, bs, bl0s, minvs, fixeds = [], [], [], [], [], [], [], []
+        oxs, ofs = [], []
+        vptr, fptr, optr, ofptr = [0], [0], [0], [0]
+        for inst in instances:
+            x = np.asarray(inst.x, np.float32)
+            f = np.asarray(inst.faces, np.int32)
+            e = edges_from_faces(f)
+            l0 = rest_lengths(x, e)
+            b = bending_pairs(f)
+            bl0 = rest_lengths(x, b) if b.shape[0] else np.zeros(0, np.float32)
+            v0 = vptr[-1]
+            xs.append(x)
+            fs.append(f + v0)
+            es.append(e + v0)
+            l0s.append(l0)
+            bs.append(b + v0)
+            bl0s.append(bl0)
+            minvs.append(inverse_masses(x.shape[0], e, l0))
+            fx = np.ones(x.shape[0], np.float32)
+            fx[np.asarray(inst.pinned, np.int64)] = 0.0
+            fixeds.append(fx)
+            vptr.append(v0 + x.shape[0])
+            fptr.append(fptr[-1] + f.shape[0])
+            ox = np.asarray(inst.obstacle_x, np.float32)
+            of = np.asarray(inst.obstacle_faces, np.int32)
+            if of.shape[0] > 32:
+                raise ValueError("an obstacle may have at most 32 faces")
+            ofs.append(of + optr[-1])
+            oxs.append(ox)
+            optr.append(optr[-1] + ox.shape[0])
+            ofptr.append(ofptr[-1] + of.shape[0])
+        x = np.concatenate(xs)
+        faces = np.concatenate(fs)
+        edges = np.concatenate(es)
+        l0 = np.concatenate(l0s)
+        bend = np.concatenate(bs)
+        bl0 = np.concatenate(bl0s)
+        m_inv = np.concatenate(minvs)
+        fixed = np.concatenate(fixeds)
+        V = x.shape[0]
+        self.num_verts = V
+        self.num_faces = faces.shape[0]
+        adj_ptr, adj = constraint_adjacency(V, edges, l0, bend, bl0)
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+        self.vptr_np = np.asarray(vptr, np.int32)
+        self.fptr_np = np.asarray(fptr, np.int32)
+        self.vptr, self.fptr = t(self.vptr_np), t(self.fptr_np)
+        self.vinst = t(np.repeat(np.arange(self.n_instances, dtype=np.int32), np.diff(self.vptr_np)))
+        self.faces = t(faces.reshape(-1))
+        self.adj_ptr, self.adj = t(adj_ptr), t(adj)
+        self.fixed, self.m_inv = t(fixed), t(m_inv)
+        self.x4 = torch.zeros((V, 4), dtype=torch.float32, device=dev)
+        self.x4[:, :3] = t(x)
+        wf = self.fixed * self.m_inv
+        self.x4[:, 3] = wf
+        self.y4 = self.x4.clone()
+        self._y_other = torch.zeros_like(self.x4)
+        self.v4 = torch.zeros_like(self.x4)
+        self.fmin4 = torch.zeros((self.num_faces, 4), dtype=torch.float32, device=dev)
+        self.fmax4 = torch.zeros_like(self.fmin4)
+        self.cl_box6 = torch.zeros((self.n_instances, 6), dtype=torch.float32, device=dev)
+        # obstacles: static; their face boxes and grids are computed once
+        ox = np.concatenate(oxs)
+        self.n_ob_verts = ox.shape[0]
+        self.xs4 = torch.zeros((self.n_ob_verts, 4), dtype=torch.float32, device=dev)
+        self.xs4[:, :3] = t(ox)
+        self.ob_faces = t(np.concatenate(ofs).reshape(-1))
+        self.optr = t(np.asarray(optr, np.int32))
+        self.ob_fptr = t(np.asarray(ofptr, np.int32))
+        self.svinst = t(np.repeat(np.arange(self.n_instances, dtype=np.int32), np.diff(np.asarray(optr))))
+        self.ob_fmin4 = torch.zeros((int(ofptr[-1]), 4), dtype=torch.float32, device=dev)
+        self.ob_fmax4 = torch.zeros_like(self.ob_fmin4)
+        self.ob_box6 = torch.zeros((self.n_instances, 6), dtype=torch.float32, device=dev)
+        self._ob_built_for = None
+        self.vmask = torch.zeros(V, dtype=torch.int32, device=dev)
+        self.tv_cand = torch.zeros((max(self.n_ob_verts, 1), cap), dtype=torch.int32, device=dev)
+        self.tv_num = torch.zeros(max(self.n_ob_verts, 1), dtype=torch.int32, device=dev)
+        self.status = torch.zeros(1, dtype=torch.int32, device=dev)
+        self._dx_fix = torch.zeros(3 * V, dtype=torch.int64, device=dev)
+        self._nc = torch.zeros(V, dtype=torch.int32, device=dev)
+
+    # -- pieces ------------------------------------------------------------------
+    def _static_obstacles(self):
+        s = stream_handle()
+        sx.sx_face_aabbs(ptr(self.xs4), ptr(self.ob_faces), self.ob_fmin4.shape[0], self.padding, ptr(self.ob_fmin4),
+                         ptr(self.ob_fmax4), s)
+        sx.sx_segment_aabbs(ptr(self.xs4), ptr(self.optr), self.n_instances, self.padding, ptr(self.ob_box6), s)
+        self._ob_built_for = self.padding
+
+    def _swap_y(self):
+        self.y4, self._y_other = self._y_other, self.y4
+
+    def substep(self, dt):
+        s = stream_handle()
+        # per-instance cloth grids and face boxes on x (the substep's BVH build)
+        sx.sx_face_aabbs(ptr(self.x4), ptr(self.faces), self.num_faces, self.padding, ptr(self.fmin4),
+                         ptr(self.fmax4), s)
+        sx.sx_segment_aabbs(ptr(self.x4), ptr(self.vptr), self.n_instances, self.padding, ptr(self.cl_box6), s)
+        g = self.g
+        sx.sx_predict(ptr(self.x4), ptr(self.v4), ptr(self.fixed), ptr(self.y4), self.num_verts, float(dt), g[0], g[1],
+                      g[2], s)
+        k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
+        k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
+        for it in range(self.n_iter):
+            sx.sx_jacobi_sweep(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed), ptr(self.adj_ptr),
+                               ptr(self.adj), self.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0, s)
+            self._swap_y()
+            if it == 0:
+                sx.sx_batched_obstacle_broadphase(
+                    self.num_verts, ptr(self.y4), ptr(self.vinst), ptr(self.ob_box6), ptr(self.ob_fptr),
+                    ptr(self.ob_fmin4), ptr(self.ob_fmax4), self.padding, ptr(self.vmask), self.n_ob_verts,
+                    ptr(self.xs4), ptr(self.svinst), ptr(self.cl_box6), ptr(self.fptr), ptr(self.fmin4),
+                    ptr(self.fmax4), self.cap, ptr(self.tv_cand), ptr(self.tv_num), ptr(self.status), s)
+            sx.sx_batched_obstacle_contacts(
+                self.num_verts, ptr(self.y4), ptr(self.fixed), ptr(self.m_inv), ptr(self.vinst), ptr(self.ob_fptr),
+                ptr(self.ob_faces), ptr(self.xs4), ptr(self.vmask), self.n_ob_verts, ptr(self.tv_cand),
+                ptr(self.tv_num), self.cap, ptr(self.faces), self.dHat, self.compliance_collision, ptr(self._dx_fix),
+                ptr(self._nc), ptr(self.status), s)
+        sx.sx_velocity_update(ptr(self.x4), ptr(self.y4), ptr(self.v4), ptr(self.fixed), self.num_verts, self.damping,
+                              float(dt), s)
+
+    def _forward_eager(self, n_substeps):
+        if self._ob_built_for != self.padding:
+            self._static_obstacles()
+        dt_sub = self.dt / n_substeps
+        for _ in range(n_substeps):
+            self.substep(dt_sub)
+
+    def forward(self, n_substeps: int):
+        """One frame for every instance (a CUDA graph per frame with
+        ``use_graph``)."""
+        if not self.use_graph:
+            self._forward_eager(n_substeps)
+            return
+        key = (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
+               self.stiffness_bending, self.n_iter, self.bending_on, self.y4.data_ptr())
+        gr = self._graphs.get(key)
+        if gr is None:
+            if self._ob_built_for != self.padding:
+                self._static_obstacles()
+            y_start = self.y4
+            gr = torch.cuda.CUDAGraph()
+            side = torch.cuda.Stream(device=self.device)
+            side.wait_stream(torch.cuda.current_stream(self.device))
+            lib = load()
+            n0 = lib.sx_kernel_launches()
+            with torch.cuda.graph(gr, stream=side):
+                self._forward_eager(n_substeps)
+                if self.y4 is not y_start:
+                    y_start.copy_(self.y4)
+                    self._swap_y()
+            torch.cuda.current_stream(self.device).wait_stream(side)
+            self.graph_kernel_launches = lib.sx_kernel_launches() - n0
+            self._graphs[key] = gr
+        gr.replay()
+
+    def instance_positions(self, i):
+        return self.x4[self.vptr_np[i]:self.vptr_np[i + 1], :3]

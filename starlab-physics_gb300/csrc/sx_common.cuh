@@ -83,8 +83,16 @@ __device__ __forceinline__ long long to_fix(float c, int* bad) {
 }
 __device__ __forceinline__ float from_fix(long long a) { return __double2float_rn(__ll2double_rn(a) * kFixInv); }
 
+// In-place scan (exclusive or inclusive) of n uint32 on one block (sx_lbvh.cu).
+int scan_u32(unsigned* data, int n, int inclusive, cudaStream_t s);
+
 // ---- cell grid ----------------------------------------------------------------
 constexpr int kGridRes = 32;
 constexpr int kNumCells = kGridRes * kGridRes * kGridRes;
+// grid descriptor of a cell-BVH build: 8 floats (cell size xyz, max leaf
+// overhang xyz, 2 unused) then 1024 occupancy words (bit z of word x*32 + y:
+// cell (x, y, z) holds faces)
+constexpr int kGridHeader = 8;
+constexpr int kGridWords = kGridHeader + kGridRes * kGridRes;
 
 }  // namespace sx

@@ -164,6 +164,12 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_scatter(const unsigned* __restric
     }
 }
 
+int scan_u32(unsigned* data, int n, int inclusive, cudaStream_t s) {
+    if (n <= 0) return SX_OK;
+    launch(scan_single_block, 1, 1024, 0, s, data, n, inclusive);
+    return check_launch("scan_single_block");
+}
+
 static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 static inline int rs_nblocks(int n) { return n <= 0 ? 1 : (n + RS_TILE - 1) / RS_TILE; }
 static size_t rs_ws_bytes(int n) {
@@ -339,6 +345,9 @@ __global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int
             if ((threadIdx.x & 31) == 0 && ext > 0.0f)
                 atomicMax(reinterpret_cast<unsigned*>(grid8) + 3 + k, __float_as_uint(ext));
         }
+        // occupancy: the 32 cells of a warp are one z-column (x, y fixed, z = 0..31)
+        const unsigned occ = __ballot_sync(0xffffffffu, size > 0);
+        if ((threadIdx.x & 31) == 0) reinterpret_cast<unsigned*>(grid8)[kGridHeader + (i >> 5)] = occ;
     }
     int node = parent[leaf];
     for (int steps = 0; node >= 0; ++steps) {
@@ -397,6 +406,11 @@ __global__ void __launch_bounds__(128) cell_traverse_kernel(
     int Q, const float4* __restrict__ p4, float pad, const float* __restrict__ grid8, const float* __restrict__ box6,
     const float4* __restrict__ nmin4, const float4* __restrict__ nmax4, const int* __restrict__ prefix,
     const float4* __restrict__ frec, int cap, int* __restrict__ cand, int* __restrict__ num, int* status) {
+    // occupancy words: bit z of word x*32 + y = cell (x, y, z) holds faces
+    __shared__ unsigned occ[kGridRes * kGridRes];
+    const unsigned* gocc = reinterpret_cast<const unsigned*>(grid8) + kGridHeader;
+    for (int k = threadIdx.x; k < kGridRes * kGridRes; k += blockDim.x) occ[k] = gocc[k];
+    __syncthreads();
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= Q) return;
     V3 p = mk(p4[q]);
@@ -413,21 +427,25 @@ __global__ void __launch_bounds__(128) cell_traverse_kernel(
         cell_range(a.x, b.x, org.x, cs.x, grid8[3], &x0, &x1);
         cell_range(a.y, b.y, org.y, cs.y, grid8[4], &y0, &y1);
         cell_range(a.z, b.z, org.z, cs.z, grid8[5], &z0, &z1);
-        for (int cx = x1; cx >= x0; --cx) {
-            for (int cy = y1; cy >= y0; --cy) {
-                for (int cz = z1; cz >= z0; --cz) {
-                    const int i = cx * kGridRes * kGridRes + cy * kGridRes + cz;
-                    const int leaf = i + kNumCells - 1;
-                    const float4 lmn = nmin4[leaf];
-                    if (__float_as_int(lmn.w) <= 0) continue;
-                    if (!overlap(a, b, mk(lmn), mk(nmax4[leaf]))) continue;
-                    const int rl = i == 0 ? 0 : prefix[i - 1];
-                    const int re = prefix[i];
-                    for (int j = rl; j < re; ++j) {
-                        const float4 fa = frec[2 * j], fb = frec[2 * j + 1];
-                        if (overlap(a, b, mk(fa), mk(fb))) {
-                            if (count < cap) out[count] = __float_as_int(fa.w);
-                            ++count;
+        if (z0 <= z1) {
+            const unsigned zmask = (z1 == 31 ? 0xffffffffu : ((1u << (z1 + 1)) - 1u)) & ~((1u << z0) - 1u);
+            for (int cx = x1; cx >= x0; --cx) {
+                for (int cy = y1; cy >= y0; --cy) {
+                    unsigned m = occ[cx * kGridRes + cy] & zmask;
+                    while (m) {  // non-empty cells of the column, descending z
+                        const int cz = 31 - __clz(m);
+                        m &= ~(1u << cz);
+                        const int i = cx * kGridRes * kGridRes + cy * kGridRes + cz;
+                        const int leaf = i + kNumCells - 1;
+                        if (!overlap(a, b, mk(nmin4[leaf]), mk(nmax4[leaf]))) continue;
+                        const int rl = i == 0 ? 0 : prefix[i - 1];
+                        const int re = prefix[i];
+                        for (int j = rl; j < re; ++j) {
+                            const float4 fa = frec[2 * j], fb = frec[2 * j + 1];
+                            if (overlap(a, b, mk(fa), mk(fb))) {
+                                if (count < cap) out[count] = __float_as_int(fa.w);
+                                ++count;
+                            }
                         }
                     }
                 }
@@ -656,6 +674,7 @@ extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_f
     int* flags = (int*)p;
     SX_CUDA(cudaMemsetAsync(prefix, 0, sizeof(int) * kNumCells, s));
     SX_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * kNumCells, s));
+    SX_CUDA(cudaMemsetAsync(grid8 + kGridHeader, 0, sizeof(unsigned) * kGridRes * kGridRes, s));
     launch(face_cell_kernel, grid_for(n_faces, 256), 256, 0, s, n_faces, (const float4*)fmin4, (const float4*)fmax4,
            box6, keys, sorted_face_ids, (unsigned*)prefix, grid8);
     int rc = check_launch("face_cell_kernel");

@@ -53,8 +53,9 @@ class LBVH_CELL:
         self.node_min4 = torch.zeros((2 * n - 1, 4), dtype=torch.float32, device=dev)
         self.node_max4 = torch.zeros((2 * n - 1, 4), dtype=torch.float32, device=dev)
         self.face_rec8 = torch.zeros((max(self.num_leafs, 1), 8), dtype=torch.float32, device=dev)
-        # grid8 = cell size xyz, largest leaf overhang beyond its cell xyz, 0, 0
-        self.grid8 = torch.zeros(8, dtype=torch.float32, device=dev)
+        # grid8 = cell size xyz, largest leaf overhang beyond its cell xyz, 0, 0,
+        # then 1024 occupancy words (one bit per cell, a word per z-column)
+        self.grid8 = torch.zeros(8 + 1024, dtype=torch.float32, device=dev)
         self.box6 = torch.zeros(6, dtype=torch.float32, device=dev)
         ws = int(sx.sx_cell_bvh_workspace_bytes(self.num_leafs))
         self.workspace = torch.empty(ws, dtype=torch.uint8, device=dev)

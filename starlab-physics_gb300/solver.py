@@ -63,6 +63,9 @@ class Solver:
         self.rebuild = rebuild
         self.compliance_collision = 1e8
         self.bending_on = bending_on
+        # vertex-vs-own-triangle contacts (__vt_dy); the reference always runs them
+        # when collisions are on
+        self.self_collision = True
 
         self.max_num_verts_dy = mesh_dy.num_verts
         self.max_num_edges_dy = mesh_dy.num_edges
@@ -91,7 +94,8 @@ class Solver:
         self._y_other = torch.zeros_like(mesh_dy.y4)
         # dense contact-pair list (int4 per pair, worst case every candidate slot)
         self._pairs = torch.empty(((2 * Vd + Vs) * cap, 4), **i32)
-        self._pairs_ws = torch.zeros(int(sx.sx_contact_pairs_workspace_bytes(Vd, Vs)), dtype=torch.uint8,
+        self._pairs_ws = torch.zeros(int(sx.sx_contact_pairs_workspace_bytes(Vd, Vs, mesh_dy.num_faces, cap)),
+                                     dtype=torch.uint8,
                                      device=dev)
         self._static_built_for = None
         self.use_graph = False
@@ -175,16 +179,20 @@ class Solver:
                                   self.status)
             self.lbvh_dy.traverse(self.mesh_st.x4, self.padding, cap, self.tv_st_candidates,
                                   self.tv_st_candidates_num, self.status)
-        self.lbvh_dy.traverse(m.y4, self.padding, cap, self.vt_dy_candidates, self.vt_dy_candidates_num,
-                              self.status)
+        if self.self_collision:
+            self.lbvh_dy.traverse(m.y4, self.padding, cap, self.vt_dy_candidates, self.vt_dy_candidates_num,
+                                  self.status)
+        else:
+            self.vt_dy_candidates_num.zero_()
 
     def build_contact_pairs(self):
         """Flatten this substep's candidate lists into the dense pair list used by
         every iteration's contact sweep (not needed when pair records are kept)."""
         m = self.mesh_dy
         s = self.mesh_st
-        sx.sx_contact_pairs_build(m.num_verts, s.num_verts if s is not None else 0, ptr(m.face_indices),
-                                  ptr(s.face_indices) if s is not None else None, self.cache_size,
+        sx.sx_contact_pairs_build(m.num_verts, s.num_verts if s is not None else 0, m.num_faces,
+                                  ptr(m.face_indices), ptr(s.face_indices) if s is not None else None,
+                                  self.cache_size,
                                   ptr(self.vt_st_candidates), ptr(self.vt_st_candidates_num),
                                   ptr(self.vt_dy_candidates), ptr(self.vt_dy_candidates_num),
                                   ptr(self.tv_st_candidates), ptr(self.tv_st_candidates_num), ptr(self._pairs),
@@ -197,7 +205,8 @@ class Solver:
         s = self.mesh_st
         c = self.compliance_collision if compliance_col is None else compliance_col
         if not self.record_pairs:
-            sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
+            sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, m.num_faces,
+                                      ptr(m.face_indices), self.cache_size, ptr(self._pairs),
                                       ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
                                       ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c), ptr(self._dx_fix),
                                       ptr(self._nc), ptr(self.status), stream_handle())
@@ -266,7 +275,7 @@ class Solver:
     def _graph_key(self, n_substeps):
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
-                self.compliance_collision, self.mesh_dy.y4.data_ptr())
+                self.compliance_collision, self.self_collision, self.mesh_dy.y4.data_ptr())
 
     def _capture(self, n_substeps):
         m = self.mesh_dy
