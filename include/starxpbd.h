@@ -188,21 +188,18 @@ int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const int* faces
  * once per substep), so sx_contact_pairs_build flattens them once -- in query
  * order, dropping the incident faces __vt_dy skips (XPBD.py:258) -- into
  * pairs[max_pairs] (int4: query vertex, triangle vertices;
- * max_pairs >= (2*n_dy + n_st) * cap) and, for self contact, also groups the
- * pairs by triangle in the workspace.  sx_contact_pairs_sweep then evaluates
- * per iteration each dynamic triangle's classifier terms once (a 192-byte
- * record per triangle) and runs one thread per pair, followed by update_dx.
- * Same values, decisions and order-independent accumulation as
- * sx_collision_sweep, hence the same result; pair records are only available
- * from sx_collision_sweep.  n_faces_dy = number of dynamic-mesh faces. */
-size_t sx_contact_pairs_workspace_bytes(int n_dy, int n_st, int n_faces_dy, int cap);
-int sx_contact_pairs_build(int n_dy, int n_st, int n_faces_dy, const int* faces_dy, const int* faces_st, int cap,
+ * max_pairs >= (2*n_dy + n_st) * cap), and sx_contact_pairs_sweep then runs
+ * one thread per pair followed by update_dx.  Same arithmetic and the same
+ * order-independent accumulation as sx_collision_sweep, hence the same result;
+ * pair records are only available from sx_collision_sweep. */
+size_t sx_contact_pairs_workspace_bytes(int n_dy, int n_st);
+int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* faces_st, int cap,
                            const int* vt_st_cand, const int* vt_st_num, const int* vt_dy_cand, const int* vt_dy_num,
                            const int* tv_st_cand, const int* tv_st_num, int* pairs, long long max_pairs, void* ws,
                            size_t ws_bytes, void* stream);
-int sx_contact_pairs_sweep(int n_dy, int n_st, int n_faces_dy, const int* faces_dy, int cap, const int* pairs,
-                           void* ws, float* y4, const float* xs4, const float* fixed, const float* m_inv, float dHat,
-                           float compliance, long long* dx_fix, int* nc, int* status, void* stream);
+int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4, const float* xs4,
+                           const float* fixed, const float* m_inv, float dHat, float compliance, long long* dx_fix,
+                           int* nc, int* status, void* stream);
 
 /* ---- batched independent cloths with obstacles ---------------------------- */
 

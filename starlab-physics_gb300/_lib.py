@@ -51,9 +51,9 @@ SIGNATURES = {
     "sx_face_bvh_refit": ([I, P, P, P, P, P, P, P, P, P, P, P], I),
     "sx_face_bvh_traverse": ([I, P, I, F, P, P, P, P, P, I, P, P, P, P], I),
     "sx_collision_sweep": ([I, I, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P], I),
-    "sx_contact_pairs_workspace_bytes": ([I, I, I, I], Z),
-    "sx_contact_pairs_build": ([I, I, I, P, P, I, P, P, P, P, P, P, P, C.c_longlong, P, Z, P], I),
-    "sx_contact_pairs_sweep": ([I, I, I, P, I, P, P, P, P, P, P, F, F, P, P, P, P], I),
+    "sx_contact_pairs_workspace_bytes": ([I, I], Z),
+    "sx_contact_pairs_build": ([I, I, P, P, I, P, P, P, P, P, P, P, C.c_longlong, P, Z, P], I),
+    "sx_contact_pairs_sweep": ([I, I, P, P, P, P, P, P, F, F, P, P, P, P], I),
     "sx_segment_aabbs": ([P, P, I, F, P, P], I),
     "sx_batched_obstacle_broadphase": ([I, P, P, P, P, P, P, F, P, I, P, P, P, P, P, P, I, P, P, P, P], I),
     "sx_batched_obstacle_contacts": ([I, P, P, P, P, P, P, P, P, I, P, P, I, P, F, F, P, P, P, P], I),

@@ -92,39 +92,57 @@ __global__ void __launch_bounds__(128) jacobi_sweep_kernel(int V, const float4* 
     for (int o = 4; o < 32; o <<= 1) rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
     const int qbase = lane & ~3;
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
-    for (int r = 0; r < rmax; ++r) {
-        const int k = b + 4 * r + j;
-        float tx = 0.0f, ty = 0.0f, tz = 0.0f;
-        if (k < e) {
-            const int2 a = __ldg(adj + k);
-            const bool bend = a.x < 0;
-            const int nb = a.x & 0x7fffffff;
-            const float rest = __int_as_float(a.y);
-            const bool use_x = bend && !bend_y;
-            const float4 self = use_x ? xs : ps;
-            const float4 other = __ldg((use_x ? x4 : yin) + nb);
-            const float kk = bend ? kb : ks;
-            const float ex = self.x - other.x, ey = self.y - other.y, ez = self.z - other.z;
-            const float lij = sqrtf((ex * ex + ey * ey) + ez * ez);
-            const float C = lij - rest;
-            const float inv = 1.0f / lij;
-            const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
-            const float schur = (self.w + other.w) * ((nx * nx + ny * ny) + nz * nz);
-            const float ld = (kk * C) / (kk * schur + 1.0f);
-            const float a0 = self.w * ld;
-            tx = a0 * nx;
-            ty = a0 * ny;
-            tz = a0 * nz;
+    // Up to R rounds per pass: every load of the pass is issued before any
+    // arithmetic, so the adjacency -> neighbour latency is paid once per pass.
+    constexpr int R = 4;
+    for (int r0 = 0; r0 < rmax; r0 += R) {
+        int2 a[R];
+        float4 other[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            const int k = b + 4 * (r0 + r) + j;
+            a[r] = k < e ? __ldg(adj + k) : make_int2(0, 0);
         }
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const float sx_ = __shfl_sync(0xffffffffu, tx, qbase + u);
-            const float sy_ = __shfl_sync(0xffffffffu, ty, qbase + u);
-            const float sz_ = __shfl_sync(0xffffffffu, tz, qbase + u);
-            if (b + 4 * r + u < e) {
-                dx = dx - sx_;
-                dy = dy - sy_;
-                dz = dz - sz_;
+        for (int r = 0; r < R; ++r) {
+            const int k = b + 4 * (r0 + r) + j;
+            const bool use_x = a[r].x < 0 && !bend_y;
+            other[r] = k < e ? __ldg((use_x ? x4 : yin) + (a[r].x & 0x7fffffff)) : ps;
+        }
+#pragma unroll
+        for (int r = 0; r < R; ++r) {
+            if (r0 + r >= rmax) break;
+            const int k = b + 4 * (r0 + r) + j;
+            float tx = 0.0f, ty = 0.0f, tz = 0.0f;
+            if (k < e) {
+                const bool bend = a[r].x < 0;
+                const float rest = __int_as_float(a[r].y);
+                const bool use_x = bend && !bend_y;
+                const float4 self = use_x ? xs : ps;
+                const float4 o = other[r];
+                const float kk = bend ? kb : ks;
+                const float ex = self.x - o.x, ey = self.y - o.y, ez = self.z - o.z;
+                const float lij = sqrtf((ex * ex + ey * ey) + ez * ez);
+                const float C = lij - rest;
+                const float inv = 1.0f / lij;
+                const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
+                const float schur = (self.w + o.w) * ((nx * nx + ny * ny) + nz * nz);
+                const float ld = (kk * C) / (kk * schur + 1.0f);
+                const float a0 = self.w * ld;
+                tx = a0 * nx;
+                ty = a0 * ny;
+                tz = a0 * nz;
+            }
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const float sx_ = __shfl_sync(0xffffffffu, tx, qbase + u);
+                const float sy_ = __shfl_sync(0xffffffffu, ty, qbase + u);
+                const float sz_ = __shfl_sync(0xffffffffu, tz, qbase + u);
+                if (b + 4 * (r0 + r) + u < e) {
+                    dx = dx - sx_;
+                    dy = dy - sy_;
+                    dz = dz - sz_;
+                }
             }
         }
     }

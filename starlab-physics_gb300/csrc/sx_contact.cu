@@ -439,13 +439,10 @@ __global__ void __launch_bounds__(256) pairs_project_kernel(const int* __restric
                                                              const float* __restrict__ fixed,
                                                              const float* __restrict__ m_inv, float dHat,
                                                              float compliance, long long* dx, int* nc,
-                                                             int* status, int skip_dy) {
+                                                             int* status) {
     const int st_end = meta[0], dy_end = meta[1], P = meta[2];
-    // with skip_dy the self-contact segment is left to the triangle-grouped kernel
-    const int ndy = skip_dy ? dy_end - st_end : 0;
     int bad = 0;
-    for (int u = blockIdx.x * blockDim.x + threadIdx.x; u < P - ndy; u += gridDim.x * blockDim.x) {
-        const int t = u < st_end ? u : u + ndy;
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
         const int4 pr = pairs[t];
         V3 g[4] = SX_ZERO_G;
         int dt;
@@ -485,171 +482,6 @@ __global__ void collision_apply_kernel(int V, float4* __restrict__ y4, const flo
         dx[3 * v + 2] = 0;
         nc[v] = 0;
     }
-}
-
-// ---------------------------------------------------------------------------
-// Self contact grouped by triangle.
-//
-// In a cloth each triangle is a candidate of ~10-30 nearby vertices, and the
-// region classifier of distance.py:5-47 spends most of its work (three edge
-// frames, three 2x2 inverses, three divisions) on quantities of the triangle
-// alone.  The self-contact pairs of the substep are grouped by triangle; in
-// every iteration, each tile of pairs evaluates those quantities once per
-// triangle it contains, with exactly the operations of d_type_PT, into a
-// 12-float4 record in shared memory, and each pair then only forms its two dot
-// products per edge.  Same values, same decisions, same distances: the result
-// is identical to project_vt_dy.
-//
-// record (float4 r[12]):
-//   r0 = x1, bits(a)   r1 = x2, bits(b)   r2 = x3, bits(c)
-//   r3 = v12, v12.v12  r4 = v13n, n.x     r5 = M1 (2x2 inverse, row major)
-//   r6 = v32, v32.v32  r7 = v32n, n.y     r8 = M2
-//   r9 = v31, v31.v31  r10 = v31n, n.z    r11 = M3
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ float4 inv2(float a00, float a01, float a10, float a11) {
-    const float det = a00 * a11 - a01 * a10;
-    const float id = 1.0f / det;
-    return make_float4(id * a11, id * (-a01), id * (-a10), id * a00);
-}
-
-__device__ __forceinline__ void build_record(int f, const int* __restrict__ faces, const float4* __restrict__ y4,
-                                             float4* r) {
-    const int a = faces[3 * f], b = faces[3 * f + 1], c = faces[3 * f + 2];
-    const V3 x1 = mk(y4[a]), x2 = mk(y4[b]), x3 = mk(y4[c]);
-    const V3 v12 = sub(x2, x1), v13 = sub(x3, x1);
-    const V3 n = cross(v12, v13);
-    const V3 v13n = cross(v12, n);
-    const V3 v32 = sub(x3, x2), v32n = cross(v32, n);
-    const V3 v31 = sub(x1, x3), v31n = cross(v31, n);
-    const float a1 = dot(v12, v12), a2 = dot(v32, v32), a3 = dot(v31, v31);
-    r[0] = make_float4(x1.x, x1.y, x1.z, __int_as_float(a));
-    r[1] = make_float4(x2.x, x2.y, x2.z, __int_as_float(b));
-    r[2] = make_float4(x3.x, x3.y, x3.z, __int_as_float(c));
-    r[3] = make_float4(v12.x, v12.y, v12.z, a1);
-    r[4] = make_float4(v13n.x, v13n.y, v13n.z, n.x);
-    r[5] = inv2(a1, dot(v12, v13n), dot(v13n, v12), dot(v13n, v13n));
-    r[6] = make_float4(v32.x, v32.y, v32.z, a2);
-    r[7] = make_float4(v32n.x, v32n.y, v32n.z, n.y);
-    r[8] = inv2(a2, dot(v32, v32n), dot(v32n, v32), dot(v32n, v32n));
-    r[9] = make_float4(v31.x, v31.y, v31.z, a3);
-    r[10] = make_float4(v31n.x, v31n.y, v31n.z, n.z);
-    r[11] = inv2(a3, dot(v31, v31n), dot(v31n, v31), dot(v31n, v31n));
-}
-
-// per query vertex: count its non-incident candidates per triangle
-__global__ void fpairs_count_kernel(int Vd, int cap, const int* __restrict__ faces_dy,
-                                    const int* __restrict__ vt_dy_c, const int* __restrict__ vt_dy_n, int* fcount) {
-    const int vid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vid >= Vd) return;
-    const int n = min(vt_dy_n[vid], cap);
-    for (int j = 0; j < n; ++j) {
-        const int fd = vt_dy_c[(size_t)vid * cap + j];
-        if (faces_dy[3 * fd] == vid || faces_dy[3 * fd + 1] == vid || faces_dy[3 * fd + 2] == vid) continue;
-        atomicAdd(fcount + fd, 1);
-    }
-}
-
-// the order of pairs within a triangle's group is arbitrary (atomic slots): the
-// contact sums are order independent
-__global__ void fpairs_fill_kernel(int Vd, int cap, const int* __restrict__ faces_dy,
-                                   const int* __restrict__ vt_dy_c, const int* __restrict__ vt_dy_n,
-                                   const int* __restrict__ foff, int* fcursor, int2* fpairs) {
-    const int vid = blockIdx.x * blockDim.x + threadIdx.x;
-    if (vid >= Vd) return;
-    const int n = min(vt_dy_n[vid], cap);
-    for (int j = 0; j < n; ++j) {
-        const int fd = vt_dy_c[(size_t)vid * cap + j];
-        if (faces_dy[3 * fd] == vid || faces_dy[3 * fd + 1] == vid || faces_dy[3 * fd + 2] == vid) continue;
-        fpairs[foff[fd] + atomicAdd(fcursor + fd, 1)] = make_int2(fd, vid);
-    }
-}
-
-// Tiles of FP_TILE pairs (sorted by triangle): the first pair of each
-// triangle in the tile builds that triangle's record in shared memory, then
-// every pair classifies against its record.
-constexpr int FP_TILE = 128;
-
-__global__ void __launch_bounds__(FP_TILE) fpairs_project_kernel(int F, const int* __restrict__ foff,
-                                                                  const int2* __restrict__ fpairs,
-                                                                  const int* __restrict__ faces,
-                                                                  const float4* __restrict__ y4,
-                                                                  const float* __restrict__ fixed,
-                                                                  const float* __restrict__ m_inv, float dHat,
-                                                                  long long* dx, int* nc, int* status) {
-    __shared__ float4 srec[FP_TILE * 12];
-    __shared__ int wsum[FP_TILE / 32];
-    const int P = foff[F];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int bad = 0;
-    for (int base = blockIdx.x * FP_TILE; base < P; base += gridDim.x * FP_TILE) {
-        const int t = base + threadIdx.x;
-        const bool valid = t < P;
-        int2 pr = make_int2(0, 0);
-        bool lead = false;
-        if (valid) {
-            pr = fpairs[t];
-            lead = t == base || fpairs[t - 1].x != pr.x;
-        }
-        // slot = (number of leaders at or before this pair in the tile) - 1
-        const unsigned ball = __ballot_sync(0xffffffffu, lead);
-        if (lane == 0) wsum[w] = __popc(ball);
-        __syncthreads();
-        int before = 0;
-        for (int k = 0; k < w; ++k) before += wsum[k];
-        const int slot = before + __popc(ball & (0xffffffffu >> (31 - lane))) - 1;
-        if (lead) build_record(pr.x, faces, y4, srec + 12 * slot);
-        __syncthreads();
-        if (valid) {
-            const float4* r = srec + 12 * slot;
-            const V3 x0 = mk(y4[pr.y]);
-            const float4 r0 = r[0], r1 = r[1], r2 = r[2];
-            const V3 x1 = mk(r0), x2 = mk(r1), x3 = mk(r2);
-            // d_type_PT (distance.py:5-47) from the record
-            const float4 r3 = r[3], r4 = r[4], r5 = r[5];
-            const V3 v10 = sub(x0, x1);
-            const float b00 = dot(mk(r3), v10), b01 = dot(mk(r4), v10);
-            const float p00 = r5.x * b00 + r5.y * b01, p01 = r5.z * b00 + r5.w * b01;
-            const float4 r6 = r[6], r7 = r[7], r8 = r[8];
-            const V3 v20 = sub(x0, x2);
-            const float b10 = dot(mk(r6), v20), b11 = dot(mk(r7), v20);
-            const float p10 = r8.x * b10 + r8.y * b11, p11 = r8.z * b10 + r8.w * b11;
-            const float4 r9 = r[9], r10 = r[10], r11 = r[11];
-            const V3 v30 = sub(x0, x3);
-            const float b20 = dot(mk(r9), v30), b21 = dot(mk(r10), v30);
-            const float p20 = r11.x * b20 + r11.y * b21, p21 = r11.z * b20 + r11.w * b21;
-            int dt;
-            if (p00 > 0.0f && p00 < 1.0f && p01 >= 0.0f) dt = 3;
-            else if (p10 > 0.0f && p10 < 1.0f && p11 >= 0.0f) dt = 4;
-            else if (p20 > 0.0f && p20 < 1.0f && p21 >= 0.0f) dt = 5;
-            else if (p00 <= 0.0f && p20 >= 1.0f) dt = 0;
-            else if (p10 <= 0.0f && p00 >= 1.0f) dt = 1;
-            else if (p20 <= 0.0f && p10 >= 1.0f) dt = 2;
-            else dt = 6;
-            // squared distance of the region (distance.py:102-116)
-            float d;
-            if (dt <= 2) {
-                const V3 u = dt == 0 ? v10 : dt == 1 ? v20 : v30;
-                d = dot(u, u);
-            } else if (dt <= 5) {
-                const V3 e0 = dt == 4 ? x2 : x1, e1 = dt == 3 ? x2 : x3;
-                const float ee = dt == 3 ? r3.w : dt == 4 ? r6.w : r9.w;
-                const V3 cc = cross(sub(e0, x0), sub(e1, x0));
-                d = dot(cc, cc) / ee;
-            } else {
-                const V3 n{r4.w, r7.w, r10.w};
-                const float s = dot(v10, n);
-                d = s * s / dot(n, n);
-            }
-            if (d < dHat) {
-                const int vv[4] = {pr.y, __float_as_int(r0.w), __float_as_int(r1.w), __float_as_int(r2.w)};
-                const V3 x[4] = {x0, x1, x2, x3};
-                V3 g[4] = SX_ZERO_G;
-                vt_dy_contact(dt, d, vv, x, fixed, m_inv, dHat, dx, nc, &bad, g);
-            }
-        }
-        __syncthreads();
-    }
-    if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
 }
 
 // ---------------------------------------------------------------------------
@@ -842,67 +674,45 @@ extern "C" int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const
 static inline size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 static inline int pairs_blocks(int n_dy, int n_st) { return (2 * n_dy + n_st + 1 + PB - 1) / PB; }
 
-// workspace: [block totals][meta 64 ints][foff F+1][fcursor F][fpairs int2 n_dy*cap][records 12 float4 * F]
+// workspace: [block totals][meta 64 ints]
 struct PairsWs {
     int* block_tot;
     int* meta;
-    int* foff;
-    int* fcursor;
-    int2* fpairs;
     size_t bytes;
 };
-static PairsWs pairs_ws(void* ws, int n_dy, int n_st, int n_faces, int cap) {
+static PairsWs pairs_ws(void* ws, int n_dy, int n_st) {
     PairsWs w;
-    const size_t F = (size_t)(n_faces > 0 ? n_faces : 1);
     char* p = (char*)ws;
     char* p0 = p;
     w.block_tot = (int*)p; p += a256((size_t)pairs_blocks(n_dy, n_st) * 4);
     w.meta = (int*)p; p += 256;
-    w.foff = (int*)p; p += a256((F + 1) * 4);
-    w.fcursor = (int*)p; p += a256(F * 4);
-    w.fpairs = (int2*)p; p += a256((size_t)(n_dy > 0 ? n_dy : 1) * (size_t)cap * 8);
     w.bytes = (size_t)(p - p0);
     return w;
 }
 
-extern "C" size_t sx_contact_pairs_workspace_bytes(int n_dy, int n_st, int n_faces_dy, int cap) {
-    return pairs_ws(nullptr, n_dy, n_st, n_faces_dy, cap < 1 ? 1 : cap).bytes;
-}
+extern "C" size_t sx_contact_pairs_workspace_bytes(int n_dy, int n_st) { return pairs_ws(nullptr, n_dy, n_st).bytes; }
 
-extern "C" int sx_contact_pairs_build(int n_dy, int n_st, int n_faces_dy, const int* faces_dy, const int* faces_st,
-                                      int cap, const int* vt_st_cand, const int* vt_st_num, const int* vt_dy_cand,
+extern "C" int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* faces_st, int cap,
+                                      const int* vt_st_cand, const int* vt_st_num, const int* vt_dy_cand,
                                       const int* vt_dy_num, const int* tv_st_cand, const int* tv_st_num, int* pairs,
                                       long long max_pairs, void* ws, size_t ws_bytes, void* stream) {
-    SX_REQUIRE(n_dy >= 0 && n_st >= 0 && n_faces_dy >= 0 && cap >= 1, "sx_contact_pairs_build: bad sizes");
+    SX_REQUIRE(n_dy >= 0 && n_st >= 0 && cap >= 1, "sx_contact_pairs_build: bad sizes");
     SX_REQUIRE(max_pairs >= (long long)(2 * n_dy + n_st) * cap,
                "sx_contact_pairs_build: pair buffer must hold (2*n_dy + n_st) * cap entries");
-    SX_REQUIRE(ws && ws_bytes >= sx_contact_pairs_workspace_bytes(n_dy, n_st, n_faces_dy, cap),
+    SX_REQUIRE(ws && ws_bytes >= sx_contact_pairs_workspace_bytes(n_dy, n_st),
                "sx_contact_pairs_build: workspace too small");
     SX_REQUIRE(faces_dy && vt_st_cand && vt_st_num && vt_dy_cand && vt_dy_num && pairs,
                "sx_contact_pairs_build: null pointer");
     SX_REQUIRE(n_st == 0 || (faces_st && tv_st_cand && tv_st_num), "sx_contact_pairs_build: null static pointer");
     cudaStream_t s = as_stream(stream);
     const int nb = pairs_blocks(n_dy, n_st);
-    PairsWs w = pairs_ws(ws, n_dy, n_st, n_faces_dy, cap);
+    PairsWs w = pairs_ws(ws, n_dy, n_st);
     launch(pairs_count_kernel, nb, PB, 0, s, n_dy, n_st, cap, faces_dy, vt_st_num, vt_dy_cand, vt_dy_num, tv_st_num,
            w.block_tot);
     launch(pairs_scan_kernel, 1, 1024, 0, s, nb, w.block_tot);
     launch(pairs_fill_kernel, nb, PB, 0, s, n_dy, n_st, cap, faces_dy, faces_st, vt_st_cand, vt_st_num, vt_dy_cand,
            vt_dy_num, tv_st_cand, tv_st_num, (const int*)w.block_tot, (int4*)pairs, w.meta);
-    int rc = check_launch("sx_contact_pairs_build");
-    if (rc) return rc;
-    // self-contact pairs grouped by triangle
-    SX_CUDA(cudaMemsetAsync(w.foff, 0, ((size_t)n_faces_dy + 1) * 4, s));
-    SX_CUDA(cudaMemsetAsync(w.fcursor, 0, (size_t)(n_faces_dy > 0 ? n_faces_dy : 1) * 4, s));
-    if (n_dy > 0) {
-        launch(fpairs_count_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, cap, faces_dy, vt_dy_cand, vt_dy_num,
-               w.foff);
-        rc = scan_u32((unsigned*)w.foff, n_faces_dy + 1, 0, s);
-        if (rc) return rc;
-        launch(fpairs_fill_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, cap, faces_dy, vt_dy_cand, vt_dy_num,
-               (const int*)w.foff, w.fcursor, w.fpairs);
-    }
-    return check_launch("sx_contact_pairs_build(triangle groups)");
+    return check_launch("sx_contact_pairs_build");
 }
 
 static int sm_count() {
@@ -915,23 +725,17 @@ static int sm_count() {
     return n;
 }
 
-extern "C" int sx_contact_pairs_sweep(int n_dy, int n_st, int n_faces_dy, const int* faces_dy, int cap,
-                                      const int* pairs, void* ws, float* y4, const float* xs4, const float* fixed,
-                                      const float* m_inv, float dHat, float compliance, long long* dx_fix, int* nc,
-                                      int* status, void* stream) {
-    SX_REQUIRE(n_dy >= 0 && n_st >= 0 && n_faces_dy >= 0 && cap >= 1, "sx_contact_pairs_sweep: bad sizes");
+extern "C" int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4,
+                                      const float* xs4, const float* fixed, const float* m_inv, float dHat,
+                                      float compliance, long long* dx_fix, int* nc, int* status, void* stream) {
+    SX_REQUIRE(n_dy >= 0 && n_st >= 0, "sx_contact_pairs_sweep: bad sizes");
     if (n_dy == 0) return SX_OK;
-    SX_REQUIRE(pairs && ws && y4 && fixed && m_inv && dx_fix && nc && status && (n_faces_dy == 0 || faces_dy),
-               "sx_contact_pairs_sweep: null pointer");
+    SX_REQUIRE(pairs && ws && y4 && fixed && m_inv && dx_fix && nc && status, "sx_contact_pairs_sweep: null pointer");
     SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_sweep: null static positions");
     cudaStream_t s = as_stream(stream);
-    PairsWs w = pairs_ws(ws, n_dy, n_st, n_faces_dy, cap);
-    if (n_faces_dy > 0)
-        launch(fpairs_project_kernel, sm_count() * 16, FP_TILE, 0, s, n_faces_dy, (const int*)w.foff,
-               (const int2*)w.fpairs, faces_dy, (const float4*)y4, fixed, m_inv, dHat, dx_fix, nc, status);
-    // the obstacle pairs are few in cloth scenes: one block per SM, grid-stride
-    launch(pairs_project_kernel, sm_count(), 256, 0, s, (const int*)w.meta, (const int4*)pairs, (const float4*)y4,
-           (const float4*)xs4, fixed, m_inv, dHat, compliance, dx_fix, nc, status, 1);
+    PairsWs w = pairs_ws(const_cast<void*>(ws), n_dy, n_st);
+    launch(pairs_project_kernel, sm_count() * 8, 256, 0, s, (const int*)w.meta, (const int4*)pairs,
+           (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, dx_fix, nc, status);
     int rc = check_launch("pairs_project_kernel");
     if (rc) return rc;
     launch(collision_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)y4, fixed, dx_fix, nc);

@@ -402,7 +402,24 @@ __device__ __forceinline__ void cell_range(float qa, float qb, float o, float c,
     *i1 = (int)fminf(f1, (float)(kGridRes - 1));
 }
 
-__global__ void __launch_bounds__(128) cell_traverse_kernel(
+// One warp per query.  The warp walks the (x, y) columns of the query's cell
+// range in descending order; in each column, lane k takes the k-th highest
+// occupied cell (descending z), tests its leaf box and counts the leaf's
+// overlapping faces; an exclusive scan over the lanes gives every lane the
+// place of its faces in the query's list, so candidates come out in
+// descending cell order and, within a cell, in sorted face order -- the
+// reference's visiting order.
+__device__ __forceinline__ int select_bit(unsigned m, int j) {
+    // position of the j-th lowest set bit of m (0-based), m having > j set bits
+    int pos = 0;
+    for (int s = 16; s > 0; s >>= 1)
+        if (__popc((unsigned)(m & ((1ull << (pos + s)) - 1ull))) <= j) pos += s;
+    return pos;
+}
+
+constexpr int CT_BLOCK = 256;
+
+__global__ void __launch_bounds__(CT_BLOCK) cell_traverse_kernel(
     int Q, const float4* __restrict__ p4, float pad, const float* __restrict__ grid8, const float* __restrict__ box6,
     const float4* __restrict__ nmin4, const float4* __restrict__ nmax4, const int* __restrict__ prefix,
     const float4* __restrict__ frec, int cap, int* __restrict__ cand, int* __restrict__ num, int* status) {
@@ -411,16 +428,18 @@ __global__ void __launch_bounds__(128) cell_traverse_kernel(
     const unsigned* gocc = reinterpret_cast<const unsigned*>(grid8) + kGridHeader;
     for (int k = threadIdx.x; k < kGridRes * kGridRes; k += blockDim.x) occ[k] = gocc[k];
     __syncthreads();
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= Q) return;
-    V3 p = mk(p4[q]);
-    V3 a{p.x - pad, p.y - pad, p.z - pad}, b{p.x + pad, p.y + pad, p.z + pad};
-    V3 pos = scale(0.5f, add(a, b));
-    V3 cs{grid8[0], grid8[1], grid8[2]}, org{box6[0], box6[1], box6[2]};
-    int ix = f2i_sat((pos.x - org.x) / cs.x), iy = f2i_sat((pos.y - org.y) / cs.y),
-        iz = f2i_sat((pos.z - org.z) / cs.z);
-    int cid = (int)((unsigned)ix * (unsigned)(kGridRes * kGridRes) + (unsigned)iy * (unsigned)kGridRes + (unsigned)iz);
-    int count = 0;
+    const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int lane = threadIdx.x & 31;
+    if (q >= Q) return;  // warp-uniform
+    const V3 p = mk(p4[q]);
+    const V3 a{p.x - pad, p.y - pad, p.z - pad}, b{p.x + pad, p.y + pad, p.z + pad};
+    const V3 pos = scale(0.5f, add(a, b));
+    const V3 cs{grid8[0], grid8[1], grid8[2]}, org{box6[0], box6[1], box6[2]};
+    const int ix = f2i_sat((pos.x - org.x) / cs.x), iy = f2i_sat((pos.y - org.y) / cs.y),
+              iz = f2i_sat((pos.z - org.z) / cs.z);
+    const int cid =
+        (int)((unsigned)ix * (unsigned)(kGridRes * kGridRes) + (unsigned)iy * (unsigned)kGridRes + (unsigned)iz);
+    int count = 0;  // warp-uniform
     int* out = cand + (size_t)q * cap;
     if (cid <= kNumCells - 1) {  // the reference's skip rule (lbvh_cell.py:665)
         int x0, x1, y0, y1, z0, z1;
@@ -431,29 +450,46 @@ __global__ void __launch_bounds__(128) cell_traverse_kernel(
             const unsigned zmask = (z1 == 31 ? 0xffffffffu : ((1u << (z1 + 1)) - 1u)) & ~((1u << z0) - 1u);
             for (int cx = x1; cx >= x0; --cx) {
                 for (int cy = y1; cy >= y0; --cy) {
-                    unsigned m = occ[cx * kGridRes + cy] & zmask;
-                    while (m) {  // non-empty cells of the column, descending z
-                        const int cz = 31 - __clz(m);
-                        m &= ~(1u << cz);
+                    const unsigned m = occ[cx * kGridRes + cy] & zmask;
+                    const int ncell = __popc(m);
+                    if (ncell == 0) continue;
+                    int rl = 0, re = 0;
+                    if (lane < ncell) {
+                        const int cz = select_bit(m, ncell - 1 - lane);
                         const int i = cx * kGridRes * kGridRes + cy * kGridRes + cz;
                         const int leaf = i + kNumCells - 1;
-                        if (!overlap(a, b, mk(nmin4[leaf]), mk(nmax4[leaf]))) continue;
-                        const int rl = i == 0 ? 0 : prefix[i - 1];
-                        const int re = prefix[i];
+                        if (overlap(a, b, mk(nmin4[leaf]), mk(nmax4[leaf]))) {
+                            rl = i == 0 ? 0 : prefix[i - 1];
+                            re = prefix[i];
+                        }
+                    }
+                    int mine = 0;
+                    for (int j = rl; j < re; ++j)
+                        mine += overlap(a, b, mk(frec[2 * j]), mk(frec[2 * j + 1])) ? 1 : 0;
+                    int incl = mine;
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += t;
+                    }
+                    int slot = count + incl - mine;
+                    if (mine) {
                         for (int j = rl; j < re; ++j) {
-                            const float4 fa = frec[2 * j], fb = frec[2 * j + 1];
-                            if (overlap(a, b, mk(fa), mk(fb))) {
-                                if (count < cap) out[count] = __float_as_int(fa.w);
-                                ++count;
+                            const float4 fa = frec[2 * j];
+                            if (overlap(a, b, mk(fa), mk(frec[2 * j + 1]))) {
+                                if (slot < cap) out[slot] = __float_as_int(fa.w);
+                                ++slot;
                             }
                         }
                     }
+                    count += __shfl_sync(0xffffffffu, incl, 31);
                 }
             }
         }
     }
-    num[q] = count;
-    if (count > cap) atomicOr(status, SX_STATUS_CAND_OVERFLOW);
+    if (lane == 0) {
+        num[q] = count;
+        if (count > cap) atomicOr(status, SX_STATUS_CAND_OVERFLOW);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -702,7 +738,8 @@ extern "C" int sx_cell_bvh_traverse(const float* p4, int n_queries, float paddin
     SX_REQUIRE(p4 && grid8 && origin_box6 && nmin4 && nmax4 && prefix && face_rec8 &&
                    cand && num && status,
                "sx_cell_bvh_traverse: null pointer");
-    launch(cell_traverse_kernel, grid_for(n_queries, 128), 128, 0, as_stream(stream), n_queries, (const float4*)p4,
+    launch(cell_traverse_kernel, grid_for(32LL * n_queries, CT_BLOCK), CT_BLOCK, 0, as_stream(stream), n_queries,
+           (const float4*)p4,
            padding, grid8, origin_box6, (const float4*)nmin4, (const float4*)nmax4, prefix,
            (const float4*)face_rec8, cap, cand, num, status);
     return check_launch("cell_traverse_kernel");

@@ -94,8 +94,7 @@ class Solver:
         self._y_other = torch.zeros_like(mesh_dy.y4)
         # dense contact-pair list (int4 per pair, worst case every candidate slot)
         self._pairs = torch.empty(((2 * Vd + Vs) * cap, 4), **i32)
-        self._pairs_ws = torch.zeros(int(sx.sx_contact_pairs_workspace_bytes(Vd, Vs, mesh_dy.num_faces, cap)),
-                                     dtype=torch.uint8,
+        self._pairs_ws = torch.zeros(int(sx.sx_contact_pairs_workspace_bytes(Vd, Vs)), dtype=torch.uint8,
                                      device=dev)
         self._static_built_for = None
         self.use_graph = False
@@ -190,9 +189,8 @@ class Solver:
         every iteration's contact sweep (not needed when pair records are kept)."""
         m = self.mesh_dy
         s = self.mesh_st
-        sx.sx_contact_pairs_build(m.num_verts, s.num_verts if s is not None else 0, m.num_faces,
-                                  ptr(m.face_indices), ptr(s.face_indices) if s is not None else None,
-                                  self.cache_size,
+        sx.sx_contact_pairs_build(m.num_verts, s.num_verts if s is not None else 0, ptr(m.face_indices),
+                                  ptr(s.face_indices) if s is not None else None, self.cache_size,
                                   ptr(self.vt_st_candidates), ptr(self.vt_st_candidates_num),
                                   ptr(self.vt_dy_candidates), ptr(self.vt_dy_candidates_num),
                                   ptr(self.tv_st_candidates), ptr(self.tv_st_candidates_num), ptr(self._pairs),
@@ -205,8 +203,7 @@ class Solver:
         s = self.mesh_st
         c = self.compliance_collision if compliance_col is None else compliance_col
         if not self.record_pairs:
-            sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, m.num_faces,
-                                      ptr(m.face_indices), self.cache_size, ptr(self._pairs),
+            sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
                                       ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
                                       ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c), ptr(self._dx_fix),
                                       ptr(self._nc), ptr(self.status), stream_handle())
