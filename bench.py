@@ -52,6 +52,7 @@ def parse_args():
     ap.add_argument("--eager", action="store_true", help="launch kernels one by one instead of replaying a graph")
     ap.add_argument("--no-lbvh", action="store_true", help="skip the standalone 2^20-triangle LBVH measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-cloth batched measurement")
+    ap.add_argument("--only-batched", action="store_true", help="run only the 512-cloth batched measurement")
     return ap.parse_args()
 
 
@@ -416,6 +417,9 @@ def main():
     from starlab_physics_gb300 import _lib
 
     _lib.load()
+    if args.only_batched:
+        print(json.dumps({"batched512": batched512(pkg, steps=args.steps, warmup=args.warmup)}))
+        return
     sim = pkg.scenes.make_solver(scene, device="cuda")
     sim.bending_on = "y"
     V = sim.mesh_dy.num_verts

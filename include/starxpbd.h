@@ -70,6 +70,15 @@ int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out4, const fl
 int sx_velocity_update(float* x4, const float* y4, float* v4, const float* fixed, int n_verts, float damping,
                        float dt, void* stream);
 
+/* Constraint residual (the reference defines none; it runs a fixed number of
+ * sweeps, XPBD.py:350-369): out3 (device) = {sum of C^2, number of
+ * constraints, sqrt(mean C^2)} with C = |p0 - p1| - l0 over springs and
+ * bending pairs, in FP64 from the float positions p4, combined in a fixed
+ * order (deterministic).  Workspace: sx_residual_workspace_bytes(n_verts). */
+size_t sx_residual_workspace_bytes(int n_verts);
+int sx_constraint_residual(const float* p4, const int* adj_ptr, const int* adj, int n_verts, double* out3, void* ws,
+                           size_t ws_bytes, void* stream);
+
 /* computeAABB_faces, meshTaichiWrapper.py:351-365 (positions p4) */
 int sx_face_aabbs(const float* p4, const int* faces, int n_faces, float padding, float* aabb_min4,
                   float* aabb_max4, void* stream);
@@ -191,15 +200,20 @@ int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const int* faces
  * max_pairs >= (2*n_dy + n_st) * cap), and sx_contact_pairs_sweep then runs
  * one thread per pair followed by update_dx.  Same arithmetic and the same
  * order-independent accumulation as sx_collision_sweep, hence the same result;
- * pair records are only available from sx_collision_sweep. */
+ * pair records are only available from sx_collision_sweep.
+ * cull_d2 > 0 skips a pair before its region classification when the squared
+ * distance from the point to the triangle's bounding box exceeds cull_d2; the
+ * point-triangle distance of every region is at least that distance, so with
+ * cull_d2 a margin above dHat (the solver passes dHat * 1.0625) a culled pair
+ * is one whose projection adds nothing.  cull_d2 <= 0 evaluates every pair. */
 size_t sx_contact_pairs_workspace_bytes(int n_dy, int n_st);
 int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* faces_st, int cap,
                            const int* vt_st_cand, const int* vt_st_num, const int* vt_dy_cand, const int* vt_dy_num,
                            const int* tv_st_cand, const int* tv_st_num, int* pairs, long long max_pairs, void* ws,
                            size_t ws_bytes, void* stream);
 int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4, const float* xs4,
-                           const float* fixed, const float* m_inv, float dHat, float compliance, long long* dx_fix,
-                           int* nc, int* status, void* stream);
+                           const float* fixed, const float* m_inv, float dHat, float compliance, float cull_d2,
+                           long long* dx_fix, int* nc, int* status, void* stream);
 
 /* ---- batched independent cloths with obstacles ---------------------------- */
 

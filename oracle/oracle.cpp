@@ -762,9 +762,20 @@ struct Pairs {  // optional pair records: pair[(q*cap+j)*2 + {0,1}] = (face, dty
 //   static mesh:  xs4 (positions), faces_st
 //   candidates:   vt_st (Vd x cap), vt_dy (Vd x cap), tv_st (Vs x cap), counts
 // Optional pair records (pass NULL to skip): three blocks, same layout.
+// cull_d2 > 0: a pair whose point-to-triangle-box squared distance exceeds
+// cull_d2 is skipped before classification (the CUDA pair-list sweep's cull;
+// every region's distance is at least the box distance, so with cull_d2 above
+// dHat the skipped pair would add nothing).  0 classifies every pair.
+static float box_d2(V3 p, V3 t0, V3 t1, V3 t2) {
+    float ex = std::fmax(std::fmax(std::fmin(std::fmin(t0.x, t1.x), t2.x) - p.x, p.x - std::fmax(std::fmax(t0.x, t1.x), t2.x)), 0.0f);
+    float ey = std::fmax(std::fmax(std::fmin(std::fmin(t0.y, t1.y), t2.y) - p.y, p.y - std::fmax(std::fmax(t0.y, t1.y), t2.y)), 0.0f);
+    float ez = std::fmax(std::fmax(std::fmin(std::fmin(t0.z, t1.z), t2.z) - p.z, p.z - std::fmax(std::fmax(t0.z, t1.z), t2.z)), 0.0f);
+    return (ex * ex + ey * ey) + ez * ez;
+}
+
 API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_t* faces_st, float* y4,
                            const float* xs4, const float* fixed, const float* m_inv, float dHat, float compliance,
-                           int cap, const int32_t* vt_st_c, const int32_t* vt_st_n, const int32_t* vt_dy_c,
+                           float cull_d2, int cap, const int32_t* vt_st_c, const int32_t* vt_st_n, const int32_t* vt_dy_c,
                            const int32_t* vt_dy_n, const int32_t* tv_st_c, const int32_t* tv_st_n,
                            int64_t* dx_fix, int32_t* nc, int32_t* pair, float* pair_g, float* pair_schur,
                            int32_t* pair_num, int32_t* status, int nthreads) {
@@ -793,6 +804,7 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
                 int fs = vt_st_c[(size_t)vid * cap + j];
                 V3 x0 = v3(y4 + 4 * vid);
                 V3 x1 = v3(xs4 + 4 * faces_st[3 * fs]), x2 = v3(xs4 + 4 * faces_st[3 * fs + 1]), x3 = v3(xs4 + 4 * faces_st[3 * fs + 2]);
+                if (cull_d2 > 0.0f && box_d2(x0, x1, x2, x3) > cull_d2) continue;
                 V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
                 int dt = d_type_PT(x0, x1, x2, x3);
                 float d = pt_distance(dt, x0, x1, x2, x3, g, true, dHat);
@@ -812,6 +824,7 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
                 if (a == vid || b == vid || c == vid) continue;
                 int vv[4] = {vid, a, b, c};
                 V3 x[4] = {v3(y4 + 4 * vid), v3(y4 + 4 * a), v3(y4 + 4 * b), v3(y4 + 4 * c)};
+                if (cull_d2 > 0.0f && box_d2(x[0], x[1], x[2], x[3]) > cull_d2) continue;
                 V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
                 int dt = d_type_PT(x[0], x[1], x[2], x[3]);
                 float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);
@@ -845,6 +858,7 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
                 int fd = tv_st_c[(size_t)vis * cap + j];
                 int vv[4] = {-1, faces_dy[3 * fd], faces_dy[3 * fd + 1], faces_dy[3 * fd + 2]};
                 V3 x[4] = {v3(xs4 + 4 * vis), v3(y4 + 4 * vv[1]), v3(y4 + 4 * vv[2]), v3(y4 + 4 * vv[3])};
+                if (cull_d2 > 0.0f && box_d2(x[0], x[1], x[2], x[3]) > cull_d2) continue;
                 V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
                 int dt = d_type_PT(x[0], x[1], x[2], x[3]);
                 float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);

@@ -40,7 +40,7 @@ _SIGS = {
     "or_cell_bvh_traverse": [I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, P, P, P],
     "or_face_bvh_refit": [I, P, P, P, P, P, P, P, P],
     "or_face_bvh_traverse": [I, I, P, P, P, P, P, P, P, I, P, P, P],
-    "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I],
+    "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I],
     "or_point_triangle": [P, P, P],
     "or_color_edges": [I, I, P, I, P, P, P],
     "or_version": [],
@@ -241,8 +241,10 @@ def point_triangle(p, t0, t1, t2):
 
 
 def collision_sweep(faces_dy, faces_st, y4, xs4, fixed, m_inv, dHat, compliance, cap, vt_st, vt_dy, tv_st,
-                    want_pairs=False, nthreads=1):
-    """Narrow phase + update_dx; updates y4 in place.  vt_st etc. = (cand, num)."""
+                    want_pairs=False, nthreads=1, cull_d2=0.0):
+    """Narrow phase + update_dx; updates y4 in place.  vt_st etc. = (cand, num).
+    cull_d2 > 0 skips pairs whose point-to-triangle-box squared distance
+    exceeds it (the CUDA pair-list sweep's cull)."""
     Vd = y4.shape[0]
     Vs = xs4.shape[0] if xs4 is not None else 0
     dx = np.zeros(3 * Vd, np.int64)
@@ -258,13 +260,23 @@ def collision_sweep(faces_dy, faces_st, y4, xs4, fixed, m_inv, dHat, compliance,
     fs = i32(faces_st) if faces_st is not None else np.zeros(3, np.int32)
     xs = xs4 if xs4 is not None else np.zeros((1, 4), np.float32)
     lib().or_collision_sweep(Vd, Vs, _p(i32(faces_dy)), _p(fs), _p(y4), _p(xs), _p(fixed), _p(m_inv), dHat,
-                             compliance, cap, _p(vt_st[0]), _p(vt_st[1]), _p(vt_dy[0]), _p(vt_dy[1]),
+                             compliance, cull_d2, cap, _p(vt_st[0]), _p(vt_st[1]), _p(vt_dy[0]), _p(vt_dy[1]),
                              _p(tv_st[0]), _p(tv_st[1]), _p(dx), _p(nc), _p(pair), _p(pair_g), _p(pair_schur),
                              _p(pair_num), _p(status), nthreads)
     out = {"status": int(status[0])}
     if want_pairs:
         out.update(pair=pair, pair_g=pair_g, pair_schur=pair_schur, pair_num=pair_num)
     return out
+
+
+def constraint_residual(p4, edges, l0, bend, bl0):
+    """RMS of C = |p0 - p1| - l0 over springs and bending pairs, in float64
+    (the definition the CUDA library uses; the reference defines none)."""
+    p = np.asarray(p4, np.float64)[:, :3]
+    pairs = np.concatenate([np.asarray(edges).reshape(-1, 2), np.asarray(bend).reshape(-1, 2)])
+    rest = np.concatenate([np.asarray(l0, np.float32), np.asarray(bl0, np.float32)]).astype(np.float64)
+    C = np.linalg.norm(p[pairs[:, 0]] - p[pairs[:, 1]], axis=1) - rest
+    return float(np.sum(C * C)), int(C.shape[0]), float(np.sqrt(np.mean(C * C))) if C.size else 0.0
 
 
 # ---- colouring --------------------------------------------------------------
@@ -292,8 +304,12 @@ class OracleSolver:
 
     def __init__(self, mesh_dy, mesh_st=None, *, dt, g, k_stretch_stiffness, k_bend_stiffness, dHat=4e-3,
                  damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
-                 compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True):
+                 compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True,
+                 contact_cull=False):
         self.d = mesh_dy
+        # the CUDA solver's contact_cull threshold, rounded to float32 from the
+        # same double product
+        self.cull_d2 = float(dHat) * 1.0625 if contact_cull else 0.0
         self.self_collision = self_collision
         self.s = mesh_st
         self.dt = float(dt)
@@ -375,7 +391,7 @@ class OracleSolver:
                 r = collision_sweep(self.faces, self.faces_st if self.s is not None else None, y4,
                                     self.xs4 if self.s is not None else None, self.fixed, self.m_inv, self.dHat,
                                     self.compliance, self.cap, vt_st[:2], vt_dy[:2], tv_st[:2],
-                                    nthreads=self.nthreads)
+                                    nthreads=self.nthreads, cull_d2=self.cull_d2)
                 self.last_status |= r["status"]
         velocity_update(self.x4, y4, self.v4, self.fixed, self.damping, dt_sub, self.nthreads)
         self.y4 = y4

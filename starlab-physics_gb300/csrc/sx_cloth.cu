@@ -92,57 +92,39 @@ __global__ void __launch_bounds__(128) jacobi_sweep_kernel(int V, const float4* 
     for (int o = 4; o < 32; o <<= 1) rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
     const int qbase = lane & ~3;
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
-    // Up to R rounds per pass: every load of the pass is issued before any
-    // arithmetic, so the adjacency -> neighbour latency is paid once per pass.
-    constexpr int R = 4;
-    for (int r0 = 0; r0 < rmax; r0 += R) {
-        int2 a[R];
-        float4 other[R];
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int k = b + 4 * (r0 + r) + j;
-            a[r] = k < e ? __ldg(adj + k) : make_int2(0, 0);
+    for (int r = 0; r < rmax; ++r) {
+        const int k = b + 4 * r + j;
+        float tx = 0.0f, ty = 0.0f, tz = 0.0f;
+        if (k < e) {
+            const int2 a = __ldg(adj + k);
+            const bool bend = a.x < 0;
+            const int nb = a.x & 0x7fffffff;
+            const float rest = __int_as_float(a.y);
+            const bool use_x = bend && !bend_y;
+            const float4 self = use_x ? xs : ps;
+            const float4 other = __ldg((use_x ? x4 : yin) + nb);
+            const float kk = bend ? kb : ks;
+            const float ex = self.x - other.x, ey = self.y - other.y, ez = self.z - other.z;
+            const float lij = sqrtf((ex * ex + ey * ey) + ez * ez);
+            const float C = lij - rest;
+            const float inv = 1.0f / lij;
+            const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
+            const float schur = (self.w + other.w) * ((nx * nx + ny * ny) + nz * nz);
+            const float ld = (kk * C) / (kk * schur + 1.0f);
+            const float a0 = self.w * ld;
+            tx = a0 * nx;
+            ty = a0 * ny;
+            tz = a0 * nz;
         }
 #pragma unroll
-        for (int r = 0; r < R; ++r) {
-            const int k = b + 4 * (r0 + r) + j;
-            const bool use_x = a[r].x < 0 && !bend_y;
-            other[r] = k < e ? __ldg((use_x ? x4 : yin) + (a[r].x & 0x7fffffff)) : ps;
-        }
-#pragma unroll
-        for (int r = 0; r < R; ++r) {
-            if (r0 + r >= rmax) break;
-            const int k = b + 4 * (r0 + r) + j;
-            float tx = 0.0f, ty = 0.0f, tz = 0.0f;
-            if (k < e) {
-                const bool bend = a[r].x < 0;
-                const float rest = __int_as_float(a[r].y);
-                const bool use_x = bend && !bend_y;
-                const float4 self = use_x ? xs : ps;
-                const float4 o = other[r];
-                const float kk = bend ? kb : ks;
-                const float ex = self.x - o.x, ey = self.y - o.y, ez = self.z - o.z;
-                const float lij = sqrtf((ex * ex + ey * ey) + ez * ez);
-                const float C = lij - rest;
-                const float inv = 1.0f / lij;
-                const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
-                const float schur = (self.w + o.w) * ((nx * nx + ny * ny) + nz * nz);
-                const float ld = (kk * C) / (kk * schur + 1.0f);
-                const float a0 = self.w * ld;
-                tx = a0 * nx;
-                ty = a0 * ny;
-                tz = a0 * nz;
-            }
-#pragma unroll
-            for (int u = 0; u < 4; ++u) {
-                const float sx_ = __shfl_sync(0xffffffffu, tx, qbase + u);
-                const float sy_ = __shfl_sync(0xffffffffu, ty, qbase + u);
-                const float sz_ = __shfl_sync(0xffffffffu, tz, qbase + u);
-                if (b + 4 * (r0 + r) + u < e) {
-                    dx = dx - sx_;
-                    dy = dy - sy_;
-                    dz = dz - sz_;
-                }
+        for (int u = 0; u < 4; ++u) {
+            const float sx_ = __shfl_sync(0xffffffffu, tx, qbase + u);
+            const float sy_ = __shfl_sync(0xffffffffu, ty, qbase + u);
+            const float sz_ = __shfl_sync(0xffffffffu, tz, qbase + u);
+            if (b + 4 * r + u < e) {
+                dx = dx - sx_;
+                dy = dy - sy_;
+                dz = dz - sz_;
             }
         }
     }
@@ -304,4 +286,82 @@ extern "C" int sx_scene_aabb(const float* p4, int n_verts, float padding, float*
     }
     launch(scene_aabb_finish, 1, 32, 0, s, box, padding);
     return check_launch("scene_aabb");
+}
+
+// ---------------------------------------------------------------------------
+// Constraint residual.  The reference defines none (XPBD.py:350-369 runs a
+// fixed number of sweeps); here it is the RMS of C = |p0 - p1| - l0 over the
+// springs and bending pairs, evaluated in FP64 from the float positions.  Each
+// constraint is counted at its lower-numbered endpoint; block sums are combined
+// in a fixed order, so the value is deterministic.
+// ---------------------------------------------------------------------------
+namespace sx {
+constexpr int RES_BLOCK = 256;
+
+__global__ void __launch_bounds__(RES_BLOCK) residual_partial_kernel(int V, const float4* __restrict__ p4,
+                                                                     const int* __restrict__ ptr,
+                                                                     const int2* __restrict__ adj,
+                                                                     double* __restrict__ partial) {
+    __shared__ double red[RES_BLOCK];
+    __shared__ double cnt[RES_BLOCK];
+    const int v = blockIdx.x * RES_BLOCK + threadIdx.x;
+    double s = 0.0, c = 0.0;
+    if (v < V) {
+        const float4 pv = p4[v];
+        for (int k = ptr[v]; k < ptr[v + 1]; ++k) {
+            const int2 a = adj[k];
+            const int nb = a.x & 0x7fffffff;
+            if (nb <= v) continue;
+            const float4 pn = p4[nb];
+            const double dx = (double)pv.x - (double)pn.x, dy = (double)pv.y - (double)pn.y,
+                         dz = (double)pv.z - (double)pn.z;
+            const double C = sqrt(dx * dx + dy * dy + dz * dz) - (double)__int_as_float(a.y);
+            s += C * C;
+            c += 1.0;
+        }
+    }
+    red[threadIdx.x] = s;
+    cnt[threadIdx.x] = c;
+    __syncthreads();
+    for (int o = RES_BLOCK / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+            red[threadIdx.x] += red[threadIdx.x + o];
+            cnt[threadIdx.x] += cnt[threadIdx.x + o];
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        partial[2 * blockIdx.x] = red[0];
+        partial[2 * blockIdx.x + 1] = cnt[0];
+    }
+}
+
+__global__ void residual_final_kernel(int nb, const double* __restrict__ partial, double* out) {
+    if (threadIdx.x != 0) return;
+    double s = 0.0, c = 0.0;
+    for (int i = 0; i < nb; ++i) {
+        s += partial[2 * i];
+        c += partial[2 * i + 1];
+    }
+    out[0] = s;
+    out[1] = c;
+    out[2] = c > 0.0 ? sqrt(s / c) : 0.0;
+}
+}  // namespace sx
+
+extern "C" size_t sx_residual_workspace_bytes(int n_verts) {
+    return (size_t)2 * sizeof(double) * (size_t)grid_for(n_verts > 0 ? n_verts : 1, RES_BLOCK);
+}
+
+extern "C" int sx_constraint_residual(const float* p4, const int* adj_ptr, const int* adj, int n_verts, double* out3,
+                                      void* ws, size_t ws_bytes, void* stream) {
+    SX_REQUIRE(n_verts >= 0, "sx_constraint_residual: n_verts < 0");
+    SX_REQUIRE(out3 && ws && (n_verts == 0 || (p4 && adj_ptr && adj)), "sx_constraint_residual: null pointer");
+    SX_REQUIRE(ws_bytes >= sx_residual_workspace_bytes(n_verts), "sx_constraint_residual: workspace too small");
+    cudaStream_t s = as_stream(stream);
+    const int nb = grid_for(n_verts > 0 ? n_verts : 1, RES_BLOCK);
+    launch(residual_partial_kernel, nb, RES_BLOCK, 0, s, n_verts, (const float4*)p4, adj_ptr, (const int2*)adj,
+           (double*)ws);
+    launch(residual_final_kernel, 1, 32, 0, s, nb, (const double*)ws, out3);
+    return check_launch("constraint_residual");
 }

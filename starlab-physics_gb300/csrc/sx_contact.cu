@@ -432,15 +432,28 @@ __global__ void __launch_bounds__(PB) pairs_fill_kernel(int Vd, int Vs, int cap,
     }
 }
 
+// Squared distance from p to the axis-aligned box of triangle (t0, t1, t2).
+// The point-triangle distance of every region d_type_PT can return is at
+// least this (its feature lies in the triangle), so a pair whose box distance
+// exceeds dHat by a margin cannot be in contact; the pair-list sweep culls
+// such pairs before the region classification when asked to.
+__device__ __forceinline__ float box_d2(V3 p, V3 t0, V3 t1, V3 t2) {
+    const float ex = fmaxf(fmaxf(fminf(fminf(t0.x, t1.x), t2.x) - p.x, p.x - fmaxf(fmaxf(t0.x, t1.x), t2.x)), 0.0f);
+    const float ey = fmaxf(fmaxf(fminf(fminf(t0.y, t1.y), t2.y) - p.y, p.y - fmaxf(fmaxf(t0.y, t1.y), t2.y)), 0.0f);
+    const float ez = fmaxf(fmaxf(fminf(fminf(t0.z, t1.z), t2.z) - p.z, p.z - fmaxf(fmaxf(t0.z, t1.z), t2.z)), 0.0f);
+    return (ex * ex + ey * ey) + ez * ez;
+}
+
 __global__ void __launch_bounds__(256) pairs_project_kernel(const int* __restrict__ meta,
-                                                             const int4* __restrict__ pairs,
-                                                             const float4* __restrict__ y4,
-                                                             const float4* __restrict__ xs4,
-                                                             const float* __restrict__ fixed,
-                                                             const float* __restrict__ m_inv, float dHat,
-                                                             float compliance, long long* dx, int* nc,
-                                                             int* status) {
+                                                            const int4* __restrict__ pairs,
+                                                            const float4* __restrict__ y4,
+                                                            const float4* __restrict__ xs4,
+                                                            const float* __restrict__ fixed,
+                                                            const float* __restrict__ m_inv, float dHat,
+                                                            float compliance, float cull_d2, long long* dx,
+                                                            int* nc, int* status) {
     const int st_end = meta[0], dy_end = meta[1], P = meta[2];
+    const bool cull = cull_d2 > 0.0f;
     int bad = 0;
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
         const int4 pr = pairs[t];
@@ -448,15 +461,18 @@ __global__ void __launch_bounds__(256) pairs_project_kernel(const int* __restric
         int dt;
         float schur;
         if (t < st_end) {
-            project_vt_st(pr.x, mk(y4[pr.x]), mk(xs4[pr.y]), mk(xs4[pr.z]), mk(xs4[pr.w]), m_inv[pr.x], dHat,
-                          compliance, dx, nc, &bad, g, &dt, &schur);
+            const V3 x0 = mk(y4[pr.x]), x1 = mk(xs4[pr.y]), x2 = mk(xs4[pr.z]), x3 = mk(xs4[pr.w]);
+            if (cull && box_d2(x0, x1, x2, x3) > cull_d2) continue;
+            project_vt_st(pr.x, x0, x1, x2, x3, m_inv[pr.x], dHat, compliance, dx, nc, &bad, g, &dt, &schur);
         } else if (t < dy_end) {
             const int vv[4] = {pr.x, pr.y, pr.z, pr.w};
             const V3 x[4] = {mk(y4[pr.x]), mk(y4[pr.y]), mk(y4[pr.z]), mk(y4[pr.w])};
+            if (cull && box_d2(x[0], x[1], x[2], x[3]) > cull_d2) continue;
             project_vt_dy(vv, x, fixed, m_inv, dHat, dx, nc, &bad, g, &dt, &schur);
         } else {
             const int vv[4] = {-1, pr.y, pr.z, pr.w};
             const V3 x[4] = {mk(xs4[pr.x]), mk(y4[pr.y]), mk(y4[pr.z]), mk(y4[pr.w])};
+            if (cull && box_d2(x[0], x[1], x[2], x[3]) > cull_d2) continue;
             project_tv_st(vv, x, fixed, m_inv, dHat, compliance, dx, nc, &bad, g, &dt, &schur);
         }
     }
@@ -727,7 +743,8 @@ static int sm_count() {
 
 extern "C" int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4,
                                       const float* xs4, const float* fixed, const float* m_inv, float dHat,
-                                      float compliance, long long* dx_fix, int* nc, int* status, void* stream) {
+                                      float compliance, float cull_d2, long long* dx_fix, int* nc, int* status,
+                                      void* stream) {
     SX_REQUIRE(n_dy >= 0 && n_st >= 0, "sx_contact_pairs_sweep: bad sizes");
     if (n_dy == 0) return SX_OK;
     SX_REQUIRE(pairs && ws && y4 && fixed && m_inv && dx_fix && nc && status, "sx_contact_pairs_sweep: null pointer");
@@ -735,7 +752,7 @@ extern "C" int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, cons
     cudaStream_t s = as_stream(stream);
     PairsWs w = pairs_ws(const_cast<void*>(ws), n_dy, n_st);
     launch(pairs_project_kernel, sm_count() * 8, 256, 0, s, (const int*)w.meta, (const int4*)pairs,
-           (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, dx_fix, nc, status);
+           (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, cull_d2, dx_fix, nc, status);
     int rc = check_launch("pairs_project_kernel");
     if (rc) return rc;
     launch(collision_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)y4, fixed, dx_fix, nc);

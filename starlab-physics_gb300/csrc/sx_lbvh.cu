@@ -403,20 +403,12 @@ __device__ __forceinline__ void cell_range(float qa, float qb, float o, float c,
 }
 
 // One warp per query.  The warp walks the (x, y) columns of the query's cell
-// range in descending order; in each column, lane k takes the k-th highest
-// occupied cell (descending z), tests its leaf box and counts the leaf's
-// overlapping faces; an exclusive scan over the lanes gives every lane the
-// place of its faces in the query's list, so candidates come out in
+// range in descending order and, in each column, the occupied cells in
+// descending z.  A cell's leaf box is tested once (a broadcast load); then the
+// lanes test the cell's faces 32 at a time in sorted order and a ballot places
+// each overlapping face after those of lower lanes, so candidates come out in
 // descending cell order and, within a cell, in sorted face order -- the
-// reference's visiting order.
-__device__ __forceinline__ int select_bit(unsigned m, int j) {
-    // position of the j-th lowest set bit of m (0-based), m having > j set bits
-    int pos = 0;
-    for (int s = 16; s > 0; s >>= 1)
-        if (__popc((unsigned)(m & ((1ull << (pos + s)) - 1ull))) <= j) pos += s;
-    return pos;
-}
-
+// reference's visiting order -- with every lane busy on the face records.
 constexpr int CT_BLOCK = 256;
 
 __global__ void __launch_bounds__(CT_BLOCK) cell_traverse_kernel(
@@ -450,38 +442,30 @@ __global__ void __launch_bounds__(CT_BLOCK) cell_traverse_kernel(
             const unsigned zmask = (z1 == 31 ? 0xffffffffu : ((1u << (z1 + 1)) - 1u)) & ~((1u << z0) - 1u);
             for (int cx = x1; cx >= x0; --cx) {
                 for (int cy = y1; cy >= y0; --cy) {
-                    const unsigned m = occ[cx * kGridRes + cy] & zmask;
-                    const int ncell = __popc(m);
-                    if (ncell == 0) continue;
-                    int rl = 0, re = 0;
-                    if (lane < ncell) {
-                        const int cz = select_bit(m, ncell - 1 - lane);
+                    unsigned m = occ[cx * kGridRes + cy] & zmask;
+                    while (m) {  // warp-uniform
+                        const int cz = 31 - __clz(m);
+                        m &= ~(1u << cz);
                         const int i = cx * kGridRes * kGridRes + cy * kGridRes + cz;
                         const int leaf = i + kNumCells - 1;
-                        if (overlap(a, b, mk(nmin4[leaf]), mk(nmax4[leaf]))) {
-                            rl = i == 0 ? 0 : prefix[i - 1];
-                            re = prefix[i];
-                        }
-                    }
-                    int mine = 0;
-                    for (int j = rl; j < re; ++j)
-                        mine += overlap(a, b, mk(frec[2 * j]), mk(frec[2 * j + 1])) ? 1 : 0;
-                    int incl = mine;
-                    for (int o = 1; o < 32; o <<= 1) {
-                        const int t = __shfl_up_sync(0xffffffffu, incl, o);
-                        if (lane >= o) incl += t;
-                    }
-                    int slot = count + incl - mine;
-                    if (mine) {
-                        for (int j = rl; j < re; ++j) {
-                            const float4 fa = frec[2 * j];
-                            if (overlap(a, b, mk(fa), mk(frec[2 * j + 1]))) {
-                                if (slot < cap) out[slot] = __float_as_int(fa.w);
-                                ++slot;
+                        if (!overlap(a, b, mk(nmin4[leaf]), mk(nmax4[leaf]))) continue;
+                        const int rl = i == 0 ? 0 : prefix[i - 1], re = prefix[i];
+                        for (int j0 = rl; j0 < re; j0 += 32) {
+                            const int j = j0 + lane;
+                            bool hit = false;
+                            float4 fa = make_float4(0.f, 0.f, 0.f, 0.f);
+                            if (j < re) {
+                                fa = frec[2 * j];
+                                hit = overlap(a, b, mk(fa), mk(frec[2 * j + 1]));
                             }
+                            const unsigned hits = __ballot_sync(0xffffffffu, hit);
+                            if (hit) {
+                                const int slot = count + __popc(hits & ((1u << lane) - 1u));
+                                if (slot < cap) out[slot] = __float_as_int(fa.w);
+                            }
+                            count += __popc(hits);
                         }
                     }
-                    count += __shfl_sync(0xffffffffu, incl, 31);
                 }
             }
         }

@@ -23,6 +23,11 @@ Options beyond the reference (keyword-only, defaults reproduce the reference):
   solves use ``"y"``.
 * ``cap`` -- candidate / pair list capacity per query (the reference's 40,
   ``XPBD.py:51``).  Longer lists are truncated and flagged in :attr:`status`.
+* ``contact_cull`` (attribute, default on) -- the pair-list contact sweep skips
+  a pair whose point-to-triangle-box squared distance exceeds ``dHat * 1.0625``
+  before classifying its region.  The distance of every region is at least the
+  box distance, so such a pair adds no correction; the skip only saves the
+  classification.  Off, every pair is classified as the reference does.
 
 Reference quirks kept on purpose: the stretch springs use
 ``stiffness_bending * dt^2`` and the bending pairs ``stiffness_stretch * dt^2``
@@ -66,6 +71,7 @@ class Solver:
         # vertex-vs-own-triangle contacts (__vt_dy); the reference always runs them
         # when collisions are on
         self.self_collision = True
+        self.contact_cull = True
 
         self.max_num_verts_dy = mesh_dy.num_verts
         self.max_num_edges_dy = mesh_dy.num_edges
@@ -205,8 +211,8 @@ class Solver:
         if not self.record_pairs:
             sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
                                       ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
-                                      ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c), ptr(self._dx_fix),
-                                      ptr(self._nc), ptr(self.status), stream_handle())
+                                      ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c), self.contact_cull_d2(),
+                                      ptr(self._dx_fix), ptr(self._nc), ptr(self.status), stream_handle())
             return
         sx.sx_collision_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(m.face_indices),
                               ptr(s.face_indices) if s is not None else None, ptr(m.y4),
@@ -262,6 +268,12 @@ class Solver:
             self._graphs[key] = g
         g.replay()
 
+    CULL_MARGIN = 1.0625
+
+    def contact_cull_d2(self) -> float:
+        """Box-distance threshold of the pair-list sweep (0 = classify every pair)."""
+        return self.dHat * self.CULL_MARGIN if self.contact_cull else 0.0
+
     def _forward_eager(self, n_substeps: int):
         dt_sub = self.dt / n_substeps
         if self.enable_collision_handling and self.rebuild == "frame":
@@ -272,7 +284,7 @@ class Solver:
     def _graph_key(self, n_substeps):
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
-                self.compliance_collision, self.self_collision, self.mesh_dy.y4.data_ptr())
+                self.compliance_collision, self.self_collision, self.contact_cull, self.mesh_dy.y4.data_ptr())
 
     def _capture(self, n_substeps):
         m = self.mesh_dy
@@ -296,6 +308,23 @@ class Solver:
         return g
 
     # -- diagnostics ---------------------------------------------------------------
+    def constraint_residual(self, positions: str = "x", out=None):
+        """RMS stretch/bending violation in FP64 on the GPU (``sx_constraint_residual``).
+
+        ``positions`` is ``"x"`` or ``"y"``.  Returns a device tensor
+        ``[sum C^2, count, rms]`` (float64); no host synchronisation unless the
+        caller reads it."""
+        m = self.mesh_dy
+        p = m.x4 if positions == "x" else m.y4
+        if out is None:
+            out = torch.empty(3, dtype=torch.float64, device=self.device)
+        if getattr(self, "_res_ws", None) is None:
+            self._res_ws = torch.empty(int(sx.sx_residual_workspace_bytes(m.num_verts)), dtype=torch.uint8,
+                                       device=self.device)
+        sx.sx_constraint_residual(ptr(p), ptr(m.adj_ptr), ptr(m.adj), m.num_verts, ptr(out), ptr(self._res_ws),
+                                  self._res_ws.numel(), stream_handle())
+        return out
+
     def status_flags(self) -> int:
         """Accumulated device status bits (host sync)."""
         return int(self.status.item())

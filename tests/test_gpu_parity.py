@@ -275,7 +275,8 @@ def _run_pair(pkg, po, scene, frames, **solver_kw):
                           dt=scene.dt, g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
                           k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
                           padding=scene.padding, n_iter=scene.n_iter, collisions=scene.collisions,
-                          rebuild=scene.rebuild, cap=scene.cap, bending_on=sim.bending_on)
+                          rebuild=scene.rebuild, cap=scene.cap, bending_on=sim.bending_on,
+                          contact_cull=sim.contact_cull)
     for _ in range(frames):
         sim.forward(scene.n_substeps)
         orc.forward(scene.n_substeps)
@@ -312,8 +313,10 @@ def test_coloring(pkg, po):
         assert np.array_equal(_np(gc.color_prefix_sum), prefix)
 
 
-def test_pair_list_sweep_equals_per_query_sweep(pkg):
-    """The compacted pair list gives the same positions as the per-query walk."""
+@pytest.mark.parametrize("cull", [False, True])
+def test_pair_list_sweep_equals_per_query_sweep(pkg, cull):
+    """The compacted pair list, with or without the box-distance cull, gives the
+    same positions as the per-query walk (which classifies every pair)."""
     outs = []
     for record in (True, False):
         sc, cl, sp = _drape(pkg, n=40)
@@ -327,6 +330,7 @@ def test_pair_list_sweep_equals_per_query_sweep(pkg):
         sim.build_bvhs()
         sim.compute_y(1 / 600)
         sim.broadphase_lbvh()
+        sim.contact_cull = cull
         if not record:
             sim.build_contact_pairs()
         for _ in range(3):
@@ -350,3 +354,18 @@ def test_graph_replay_equals_eager(pkg, n_iter):
         res.append((_np(sim.mesh_dy.x4), _np(sim.mesh_dy.v4), _np(sim.mesh_dy.y4)))
     for a, b in zip(*res):
         assert np.array_equal(a, b)
+
+
+def test_constraint_residual(pkg, po):
+    scene = pkg.scenes.plain64(n=24, seed=2)
+    scene.n_iter = 3
+    sim = pkg.scenes.make_solver(scene, device=DEV)
+    sim.bending_on = "y"
+    for _ in range(2):
+        sim.forward(scene.n_substeps)
+    r = sim.constraint_residual("x").cpu().numpy()
+    m = sim.mesh_dy
+    s, n, rms = po.constraint_residual(_np(m.x4), m.eid_np, m.l0_np, m.bending_np, m.bending_l0_np)
+    assert int(r[1]) == n == m.num_edges + m.bending_constraint_count
+    assert abs(r[0] - s) <= 1e-12 * max(s, 1e-30) * n
+    assert abs(r[2] - rms) <= 1e-9 * rms

@@ -417,6 +417,55 @@ def test_collision_parallel_matches_serial(pkg, po):
     assert not np.array_equal(ys, y4)
 
 
+def _box_d2_np(p, t):
+    """Point-to-triangle-box squared distance, float32, the kernels' order."""
+    lo = np.minimum(np.minimum(t[:, 0], t[:, 1]), t[:, 2])
+    hi = np.maximum(np.maximum(t[:, 0], t[:, 1]), t[:, 2])
+    e = np.maximum(np.maximum(lo - p, p - hi), np.float32(0))
+    return (e[:, 0] * e[:, 0] + e[:, 1] * e[:, 1]) + e[:, 2] * e[:, 2]
+
+
+def test_contact_cull_never_drops_a_contact(po):
+    """Every region's squared distance is at least the box distance: over random
+    point-triangle pairs placed around the contact threshold, no pair the cull
+    removes (box distance > 1.0625 dHat) has d < dHat."""
+    rng = np.random.default_rng(11)
+    dHat = np.float32(2e-3) ** 2
+    n, culled = 20000, 0
+    tri = rng.uniform(-1, 1, (n, 3, 3)).astype(np.float32) * np.float32(4e-3) + np.float32(0.7)
+    p = (tri.mean(axis=1) + rng.normal(0, 5e-3, (n, 3))).astype(np.float32)
+    bd = _box_d2_np(p, tri)
+    for i in range(n):
+        dt, d, _ = po.point_triangle(p[i], tri[i, 0], tri[i, 1], tri[i, 2])
+        if bd[i] > dHat * np.float32(1.0625):
+            culled += 1
+            assert not d < dHat, (i, dt, d, bd[i])
+    assert culled > n // 10
+
+
+def test_contact_cull_keeps_solver_result(pkg, po):
+    """The oracle solver gives bit-identical trajectories with and without the
+    cull on a colliding scene (plain64, 24x24, with iterations)."""
+    scene = pkg.scenes.plain64(n=24, seed=2)
+    scene.n_iter = 4
+    from starlab_physics_gb300 import mesh as M
+
+    cl = M.TriMesh(scene.cloth_x, scene.cloth_faces, device="cpu")
+    ob = M.TriMesh(scene.obstacle_x, scene.obstacle_faces, device="cpu")
+    runs = []
+    for cull in (False, True):
+        orc = po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob), dt=scene.dt,
+                              g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
+                              k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
+                              padding=scene.padding, n_iter=scene.n_iter, collisions=True, rebuild=scene.rebuild,
+                              cap=scene.cap, bending_on="y", contact_cull=cull)
+        for _ in range(8):
+            orc.forward(scene.n_substeps)
+        runs.append(orc.x4.copy())
+    assert np.array_equal(runs[0], runs[1])
+    assert np.abs(runs[0][:, 2] - cl.x0_np[:, 2]).max() > 0.01
+
+
 # ---------------------------------------------------------------------------
 # graph colouring (graph_coloring.py:112-201)
 # ---------------------------------------------------------------------------
