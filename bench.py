@@ -487,11 +487,11 @@ def main():
     sweeps = []
     orig = sim.spring_sweep
 
-    def timed_sweep(dt):
+    def timed_sweep(dt, iteration=0):
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        orig(dt)
+        orig(dt, iteration)
         b.record(stream)
         sweeps.append((a, b))
 

@@ -71,13 +71,37 @@ int sx_velocity_update(float* x4, const float* y4, float* v4, const float* fixed
                        float dt, void* stream);
 
 /* Constraint residual (the reference defines none; it runs a fixed number of
- * sweeps, XPBD.py:350-369): out3 (device) = {sum of C^2, number of
- * constraints, sqrt(mean C^2)} with C = |p0 - p1| - l0 over springs and
- * bending pairs, in FP64 from the float positions p4, combined in a fixed
- * order (deterministic).  Workspace: sx_residual_workspace_bytes(n_verts). */
+ * sweeps, XPBD.py:350-369): out3 (device) = {S, n, sqrt(S/n)} where n is the
+ * number of adjacency entries (each spring and bending pair counted from both
+ * endpoints) and S the sum of C^2 over them, C = |p_self - p_other| - l0
+ * evaluated in float as the sweep evaluates it.  Per-vertex and per-block
+ * sums are float in a fixed order, the sum over blocks is FP64 in a fixed
+ * order, so the value is deterministic.  Workspace:
+ * sx_residual_workspace_bytes(n_verts), zero-filled before its first use (its
+ * block counter is left zero after every call). */
 size_t sx_residual_workspace_bytes(int n_verts);
 int sx_constraint_residual(const float* p4, const int* adj_ptr, const int* adj, int n_verts, double* out3, void* ws,
                            size_t ws_bytes, void* stream);
+
+/* Iterating to a residual (no counterpart in the reference, which runs one
+ * sweep per substep).  conv is a device int[8]:
+ *   conv[0] stop iteration of the current substep (-1: not converged),
+ *   conv[2] checks made this substep, conv[3] sum of stop iterations and
+ *   conv[4] converged substeps since the last reset_totals.
+ * sx_convergence_begin starts a substep (conv[0] = -1, conv[2] = 0).
+ * sx_jacobi_sweep_checked is sx_jacobi_sweep with bending on y, launched for
+ * Jacobi iteration `iter` of the substep.  With check != 0 (iter even) it also
+ * computes the residual of its input y_in4 (the state after iteration iter-1)
+ * into res3, as sx_constraint_residual would, and if that is <= tol sets
+ * conv[0] = iter.  Every kernel of iteration iter' >= conv[0] + 2 -- this
+ * sweep, and the contact sweeps given the same conv and iter' -- returns at
+ * once, so iterations stop in pairs and y ends in the buffer it would have
+ * ended in after an even number of sweeps.  The checks run inside CUDA graphs
+ * without host synchronisation. */
+int sx_convergence_begin(int* conv, int reset_totals, void* stream);
+int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
+                            const int* adj, int n_verts, float k_spring, float k_bend, int iter, int check, double tol,
+                            int* conv, double* res3, void* ws, size_t ws_bytes, void* stream);
 
 /* computeAABB_faces, meshTaichiWrapper.py:351-365 (positions p4) */
 int sx_face_aabbs(const float* p4, const int* faces, int n_faces, float padding, float* aabb_min4,
@@ -205,7 +229,9 @@ int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const int* faces
  * distance from the point to the triangle's bounding box exceeds cull_d2; the
  * point-triangle distance of every region is at least that distance, so with
  * cull_d2 a margin above dHat (the solver passes dHat * 1.0625) a culled pair
- * is one whose projection adds nothing.  cull_d2 <= 0 evaluates every pair. */
+ * is one whose projection adds nothing.  cull_d2 <= 0 evaluates every pair.
+ * conv/iter: convergence gate of sx_jacobi_sweep_checked (conv NULL: always
+ * runs). */
 size_t sx_contact_pairs_workspace_bytes(int n_dy, int n_st);
 int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* faces_st, int cap,
                            const int* vt_st_cand, const int* vt_st_num, const int* vt_dy_cand, const int* vt_dy_num,
@@ -213,7 +239,7 @@ int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* f
                            size_t ws_bytes, void* stream);
 int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4, const float* xs4,
                            const float* fixed, const float* m_inv, float dHat, float compliance, float cull_d2,
-                           long long* dx_fix, int* nc, int* status, void* stream);
+                           long long* dx_fix, int* nc, int* status, const int* conv, int iter, void* stream);
 
 /* ---- batched independent cloths with obstacles ---------------------------- */
 
@@ -242,7 +268,8 @@ int sx_batched_obstacle_broadphase(int n_verts, const float* y4, const int* vins
 int sx_batched_obstacle_contacts(int n_verts, float* y4, const float* fixed, const float* m_inv, const int* vinst,
                                  const int* ob_fptr, const int* ob_faces, const float* xs4, const unsigned* vmask,
                                  int n_ob_verts, const int* tv_cand, const int* tv_num, int cap, const int* cl_faces,
-                                 float dHat, float compliance, long long* dx_fix, int* nc, int* status, void* stream);
+                                 float dHat, float compliance, long long* dx_fix, int* nc, int* status, const int* conv,
+                                 int iter, void* stream);
 
 /* ---- constraint-graph colouring (framework/utilities/graph_coloring.py) --- */
 

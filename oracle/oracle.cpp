@@ -897,6 +897,76 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
     return 0;
 }
 
+// Constraint residual of the CUDA library (sx_constraint_residual and the
+// checked sweep), in its exact summation order: C = |p_self - p_other| - l0 in
+// float per adjacency entry (vertex-centric CSR: entry word = neighbour with
+// bit 31 set for bending pairs, rest length bits), per-vertex float sums in
+// entry order, 32-vertex warp xor trees, 256-vertex block values
+// ((w0+w1)+(w2+w3))+((w4+w5)+(w6+w7)) converted to double, then the FP64
+// finish: 16384 strided thread sums, 32-lane xor trees, 8-warp pair trees and
+// 64 block values in index order.  out3 = {S, n, sqrt(S/n)}.
+API int or_residual(int V, const float* p4, const int32_t* ptr, const int32_t* adj, double* out3) {
+    const int nb = V > 0 ? (V + 255) / 256 : 1;
+    std::vector<double> partial(nb, 0.0);
+    for (int blk = 0; blk < nb; ++blk) {
+        float w[8];
+        for (int wi = 0; wi < 8; ++wi) {
+            float a[32];
+            for (int l = 0; l < 32; ++l) {
+                const int v = blk * 256 + wi * 32 + l;
+                float c2 = 0.0f;
+                if (v < V) {
+                    const float* ps = p4 + 4 * (size_t)v;
+                    for (int k = ptr[v]; k < ptr[v + 1]; ++k) {
+                        const int nbv = adj[2 * k] & 0x7fffffff;
+                        float rest;
+                        std::memcpy(&rest, adj + 2 * k + 1, 4);
+                        const float* o = p4 + 4 * (size_t)nbv;
+                        const float ex = ps[0] - o[0], ey = ps[1] - o[1], ez = ps[2] - o[2];
+                        const float C = std::sqrt((ex * ex + ey * ey) + ez * ez) - rest;
+                        c2 = c2 + C * C;
+                    }
+                }
+                a[l] = c2;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                float t[32];
+                for (int l = 0; l < 32; ++l) t[l] = a[l] + a[l ^ o];
+                std::memcpy(a, t, sizeof(a));
+            }
+            w[wi] = a[0];
+        }
+        partial[blk] = (double)(((w[0] + w[1]) + (w[2] + w[3])) + ((w[4] + w[5]) + (w[6] + w[7])));
+    }
+    const int RB = 64, RT = 256;
+    std::vector<double> part2(RB);
+    for (int b = 0; b < RB; ++b) {
+        double ws[8];
+        for (int wi = 0; wi < 8; ++wi) {
+            double a[32];
+            for (int l = 0; l < 32; ++l) {
+                double acc = 0.0;
+                for (int i = b * RT + wi * 32 + l; i < nb; i += RB * RT) acc += partial[i];
+                a[l] = acc;
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                double t[32];
+                for (int l = 0; l < 32; ++l) t[l] = a[l] + a[l ^ o];
+                std::memcpy(a, t, sizeof(a));
+            }
+            ws[wi] = a[0];
+        }
+        part2[b] = ((ws[0] + ws[1]) + (ws[2] + ws[3])) + ((ws[4] + ws[5]) + (ws[6] + ws[7]));
+    }
+    double S = 0.0;
+    for (int b = 0; b < RB; ++b) S += part2[b];
+    const double n = V > 0 ? (double)ptr[V] : 0.0;
+    out3[0] = S;
+    out3[1] = n;
+    out3[2] = n > 0.0 ? std::sqrt(S / n) : 0.0;
+    return 0;
+}
+
 // The region classifier, distance and gradient for one point-triangle query
 // (used by tests: known-answer and finite-difference checks).
 API int or_point_triangle(const float* p12, float* d_out, float* g12) {

@@ -40,6 +40,7 @@ _SIGS = {
     "or_cell_bvh_traverse": [I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, P, P, P],
     "or_face_bvh_refit": [I, P, P, P, P, P, P, P, P],
     "or_face_bvh_traverse": [I, I, P, P, P, P, P, P, P, I, P, P, P],
+    "or_residual": [I, P, P, P, P],
     "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I],
     "or_point_triangle": [P, P, P],
     "or_color_edges": [I, I, P, I, P, P, P],
@@ -269,14 +270,41 @@ def collision_sweep(faces_dy, faces_st, y4, xs4, fixed, m_inv, dHat, compliance,
     return out
 
 
+def adjacency(n_verts, edges, l0, bend, bl0):
+    """Vertex-centric CSR of the constraints in ascending constraint index
+    (springs 0..E-1, then bending pairs): entry = (neighbour | bit 31 for a
+    bending pair, bits of the rest length).  The order in which a serial run of
+    solve_spring_constraints_x (XPBD.py:141-184) meets a vertex's constraints."""
+    edges = i32(edges).reshape(-1, 2)
+    bend = i32(bend).reshape(-1, 2)
+    E, B = edges.shape[0], bend.shape[0]
+    a = np.concatenate([edges[:, 0], bend[:, 0], edges[:, 1], bend[:, 1]]).astype(np.int64)
+    nb = np.concatenate([edges[:, 1], bend[:, 1], edges[:, 0], bend[:, 0]]).astype(np.int64)
+    cid = np.concatenate([np.arange(E + B), np.arange(E + B)])
+    rest = np.concatenate([f32(l0), f32(bl0)])
+    order = np.lexsort((cid, a))
+    a, nb, cid = a[order], nb[order], cid[order]
+    ptr = np.zeros(n_verts + 1, np.int32)
+    ptr[1:] = np.cumsum(np.bincount(a, minlength=n_verts))
+    adj = np.empty((a.shape[0], 2), np.int32)
+    adj[:, 0] = np.where(cid >= E, nb | 0x80000000, nb).astype(np.int64).astype(np.uint32).view(np.int32)
+    adj[:, 1] = rest[cid].view(np.int32)
+    return ptr, adj
+
+
+def residual(p4, ptr, adj):
+    """The CUDA library's constraint residual {S, n, sqrt(S/n)} in its exact
+    summation order (float per vertex and block, FP64 across blocks); the
+    reference defines no residual."""
+    out = np.zeros(3, np.float64)
+    lib().or_residual(int(ptr.shape[0] - 1), _p(f32(p4)), _p(i32(ptr)), _p(i32(adj)), _p(out))
+    return out
+
+
 def constraint_residual(p4, edges, l0, bend, bl0):
-    """RMS of C = |p0 - p1| - l0 over springs and bending pairs, in float64
-    (the definition the CUDA library uses; the reference defines none)."""
-    p = np.asarray(p4, np.float64)[:, :3]
-    pairs = np.concatenate([np.asarray(edges).reshape(-1, 2), np.asarray(bend).reshape(-1, 2)])
-    rest = np.concatenate([np.asarray(l0, np.float32), np.asarray(bl0, np.float32)]).astype(np.float64)
-    C = np.linalg.norm(p[pairs[:, 0]] - p[pairs[:, 1]], axis=1) - rest
-    return float(np.sum(C * C)), int(C.shape[0]), float(np.sqrt(np.mean(C * C))) if C.size else 0.0
+    """residual() of positions p4 over the springs and bending pairs."""
+    ptr, adj = adjacency(p4.shape[0], edges, l0, bend, bl0)
+    return residual(p4, ptr, adj)
 
 
 # ---- colouring --------------------------------------------------------------
@@ -305,8 +333,17 @@ class OracleSolver:
     def __init__(self, mesh_dy, mesh_st=None, *, dt, g, k_stretch_stiffness, k_bend_stiffness, dHat=4e-3,
                  damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
                  compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True,
-                 contact_cull=False):
+                 contact_cull=False, tol=None, check_every=4):
         self.d = mesh_dy
+        # iterate to a residual (the CUDA solver's tol mode): every
+        # check_every-th iteration measures the residual of the current y; once
+        # it is <= tol, that iteration and the next run and the rest are skipped
+        self.tol = tol
+        self.check_every = check_every
+        self.checks = 0
+        self.stop_sum = 0
+        self.converged = 0
+        self.last_residual = None
         # the CUDA solver's contact_cull threshold, rounded to float32 from the
         # same double product
         self.cull_d2 = float(dHat) * 1.0625 if contact_cull else 0.0
@@ -338,6 +375,7 @@ class OracleSolver:
         self.bend = i32(mesh_dy["bend"]).reshape(-1, 2)
         self.bl0 = f32(mesh_dy["bend_l0"])
         self.faces = i32(mesh_dy["faces"])
+        self.adj_ptr, self.adj = adjacency(V, self.edges, self.l0, self.bend, self.bl0)
         if collisions:
             self.bvh_dy = CellBVH()
             if mesh_st is not None:
@@ -381,7 +419,19 @@ class OracleSolver:
         k_spring = float(self.kbs) * dt_sub * dt_sub   # XPBD.py:354 (names swapped)
         k_bend = float(self.kss) * dt_sub * dt_sub     # XPBD.py:355
         cands = None
+        stop = -1
         for it in range(self.n_iter):
+            if self.tol is not None:
+                if stop >= 0 and it >= stop + 2:
+                    break
+                if it > 0 and it % self.check_every == 0:
+                    r = residual(y4, self.adj_ptr, self.adj)
+                    self.last_residual = r
+                    self.checks += 1
+                    if stop < 0 and r[0] <= (self.tol * self.tol) * r[1]:
+                        stop = it
+                        self.stop_sum += it
+                        self.converged += 1
             spring_sweep(self.x4, y4, self.fixed, self.m_inv, self.edges, self.l0, self.bend, self.bl0, k_spring,
                          k_bend, self.nthreads, self.bend_on_y)
             if self.collisions:

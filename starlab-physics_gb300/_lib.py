@@ -39,6 +39,8 @@ SIGNATURES = {
     "sx_velocity_update": ([P, P, P, P, I, F, F, P], I),
     "sx_residual_workspace_bytes": ([I], Z),
     "sx_constraint_residual": ([P, P, P, I, P, P, Z, P], I),
+    "sx_convergence_begin": ([P, I, P], I),
+    "sx_jacobi_sweep_checked": ([P, P, P, P, P, P, I, F, F, I, I, C.c_double, P, P, P, Z, P], I),
     "sx_face_aabbs": ([P, P, I, F, P, P, P], I),
     "sx_scene_aabb": ([P, I, F, P, P], I),
     "sx_cell_bvh_workspace_bytes": ([I], Z),
@@ -55,10 +57,10 @@ SIGNATURES = {
     "sx_collision_sweep": ([I, I, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P], I),
     "sx_contact_pairs_workspace_bytes": ([I, I], Z),
     "sx_contact_pairs_build": ([I, I, P, P, I, P, P, P, P, P, P, P, C.c_longlong, P, Z, P], I),
-    "sx_contact_pairs_sweep": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P], I),
+    "sx_contact_pairs_sweep": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, P], I),
     "sx_segment_aabbs": ([P, P, I, F, P, P], I),
     "sx_batched_obstacle_broadphase": ([I, P, P, P, P, P, P, F, P, I, P, P, P, P, P, P, I, P, P, P, P], I),
-    "sx_batched_obstacle_contacts": ([I, P, P, P, P, P, P, P, P, I, P, P, I, P, F, F, P, P, P, P], I),
+    "sx_batched_obstacle_contacts": ([I, P, P, P, P, P, P, P, P, I, P, P, I, P, F, F, P, P, P, P, I, P], I),
     "sx_color_workspace_bytes": ([I, I], Z),
     "sx_color_edges_greedy": ([P, I, I, I, P, P, P, P, Z, P], I),
 }

@@ -160,6 +160,12 @@ class BatchedSolver:
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self._dx_fix = torch.zeros(3 * V, dtype=torch.int64, device=dev)
         self._nc = torch.zeros(V, dtype=torch.int32, device=dev)
+        # iterate to a residual (Solver.tol): n_iter is then the cap
+        self.tol = None
+        self.check_every = 4
+        self._conv = torch.zeros(8, dtype=torch.int32, device=dev)
+        self._res3 = torch.zeros(4, dtype=torch.float64, device=dev)
+        self._res_ws = torch.zeros(int(sx.sx_residual_workspace_bytes(V)), dtype=torch.uint8, device=dev)
 
     # -- pieces ------------------------------------------------------------------
     def _static_obstacles(self):
@@ -183,9 +189,23 @@ class BatchedSolver:
                       g[2], s)
         k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
         k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
+        tol_mode = self.tol is not None
+        if tol_mode:
+            if self.bending_on != "y" or self.n_iter % 2 or self.check_every < 2 or self.check_every % 2:
+                raise ValueError("iterating to a tolerance needs bending_on='y' and even n_iter and check_every")
+            sx.sx_convergence_begin(ptr(self._conv), 0, s)
+        conv = ptr(self._conv) if tol_mode else None
         for it in range(self.n_iter):
-            sx.sx_jacobi_sweep(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed), ptr(self.adj_ptr),
-                               ptr(self.adj), self.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0, s)
+            if tol_mode:
+                check = 1 if it > 0 and it % self.check_every == 0 else 0
+                sx.sx_jacobi_sweep_checked(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
+                                           ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend, it,
+                                           check, float(self.tol), conv, ptr(self._res3), ptr(self._res_ws),
+                                           self._res_ws.numel(), s)
+            else:
+                sx.sx_jacobi_sweep(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
+                                   ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend,
+                                   1 if self.bending_on == "y" else 0, s)
             self._swap_y()
             if it == 0:
                 sx.sx_batched_obstacle_broadphase(
@@ -197,7 +217,7 @@ class BatchedSolver:
                 self.num_verts, ptr(self.y4), ptr(self.fixed), ptr(self.m_inv), ptr(self.vinst), ptr(self.ob_fptr),
                 ptr(self.ob_faces), ptr(self.xs4), ptr(self.vmask), self.n_ob_verts, ptr(self.tv_cand),
                 ptr(self.tv_num), self.cap, ptr(self.faces), self.dHat, self.compliance_collision, ptr(self._dx_fix),
-                ptr(self._nc), ptr(self.status), s)
+                ptr(self._nc), ptr(self.status), conv, it, s)
         sx.sx_velocity_update(ptr(self.x4), ptr(self.y4), ptr(self.v4), ptr(self.fixed), self.num_verts, self.damping,
                               float(dt), s)
 
@@ -215,7 +235,7 @@ class BatchedSolver:
             self._forward_eager(n_substeps)
             return
         key = (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
-               self.stiffness_bending, self.n_iter, self.bending_on, self.y4.data_ptr())
+               self.stiffness_bending, self.n_iter, self.bending_on, self.tol, self.check_every, self.y4.data_ptr())
         gr = self._graphs.get(key)
         if gr is None:
             if self._ob_built_for != self.padding:
@@ -235,6 +255,25 @@ class BatchedSolver:
             self.graph_kernel_launches = lib.sx_kernel_launches() - n0
             self._graphs[key] = gr
         gr.replay()
+
+    def constraint_residual(self, positions: str = "x", out=None):
+        """Solver.constraint_residual over every instance's constraints."""
+        p = self.x4 if positions == "x" else self.y4
+        if out is None:
+            out = torch.empty(3, dtype=torch.float64, device=self.device)
+        sx.sx_constraint_residual(ptr(p), ptr(self.adj_ptr), ptr(self.adj), self.num_verts, ptr(out),
+                                  ptr(self._res_ws), self._res_ws.numel(), stream_handle())
+        return out
+
+    def convergence_stats(self, reset: bool = False) -> dict:
+        """Solver.convergence_stats."""
+        c = self._conv.cpu().tolist()
+        r = self._res3.cpu().tolist()
+        out = {"converged_substeps": c[4], "mean_stop_iteration": c[3] / c[4] if c[4] else None,
+               "last_residual": r[2]}
+        if reset:
+            sx.sx_convergence_begin(ptr(self._conv), 1, stream_handle())
+        return out
 
     def instance_positions(self, i):
         return self.x4[self.vptr_np[i]:self.vptr_np[i + 1], :3]

@@ -63,81 +63,92 @@ __global__ void predict_kernel(int V, const float4* __restrict__ x4, const float
 // dx -= (w_self*ld) * normalize(p_self - p_other) over its incident constraints
 // in ascending constraint index, which equals a serial run of the reference.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(128) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
-                                                           const float4* __restrict__ yin,
-                                                           float4* __restrict__ yout,
-                                                           const float* __restrict__ fixed,
-                                                           const int* __restrict__ ptr,
-                                                           const int2* __restrict__ adj, float ks, float kb,
-                                                           int bend_y) {
-    // Four lanes per vertex: in round r lane j evaluates entry b + 4r + j, then
-    // every lane of the quad adds the four terms in ascending entry order
-    // (shuffles), so the sum is the serial one while the loads, square roots and
-    // divisions run four-wide.
-    const int gt = blockIdx.x * blockDim.x + threadIdx.x;
-    const int lane = threadIdx.x & 31;
-    const int j = gt & 3;
-    const int v = gt >> 2;
-    const bool valid = v < V;
-    float4 ps = make_float4(0.f, 0.f, 0.f, 0.f), xs = ps;
-    int b = 0, e = 0;
-    if (valid) {
-        ps = __ldg(yin + v);
-        xs = __ldg(x4 + v);
-        b = __ldg(ptr + v);
-        e = __ldg(ptr + v + 1);
-    }
-    const int rounds = (e - b + 3) >> 2;
-    int rmax = rounds;
-    for (int o = 4; o < 32; o <<= 1) rmax = max(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-    const int qbase = lane & ~3;
-    float dx = 0.0f, dy = 0.0f, dz = 0.0f;
-    for (int r = 0; r < rmax; ++r) {
-        const int k = b + 4 * r + j;
-        float tx = 0.0f, ty = 0.0f, tz = 0.0f;
-        if (k < e) {
-            const int2 a = __ldg(adj + k);
-            const bool bend = a.x < 0;
-            const int nb = a.x & 0x7fffffff;
-            const float rest = __int_as_float(a.y);
-            const bool use_x = bend && !bend_y;
-            const float4 self = use_x ? xs : ps;
-            const float4 other = __ldg((use_x ? x4 : yin) + nb);
-            const float kk = bend ? kb : ks;
-            const float ex = self.x - other.x, ey = self.y - other.y, ez = self.z - other.z;
-            const float lij = sqrtf((ex * ex + ey * ey) + ez * ez);
-            const float C = lij - rest;
-            const float inv = 1.0f / lij;
-            const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
-            const float schur = (self.w + other.w) * ((nx * nx + ny * ny) + nz * nz);
-            const float ld = (kk * C) / (kk * schur + 1.0f);
-            const float a0 = self.w * ld;
-            tx = a0 * nx;
-            ty = a0 * ny;
-            tz = a0 * nz;
-        }
+constexpr int SW_BLOCK = 256;  // one vertex per thread
+inline int sweep_blocks(int n_verts) { return grid_for(n_verts, SW_BLOCK); }
+
+// ---------------------------------------------------------------------------
+// Residual reduction shared by the checked sweep and sx_constraint_residual.
+// Each thread holds its vertex's float sum of C^2 over its entries in
+// ascending order; the warp value is the xor tree over its 32 vertices (IEEE
+// addition is commutative, so every lane ends with the same value), the block
+// value ((w0 + w1) + (w2 + w3)) + ((w4 + w5) + (w6 + w7)) over the 8 warps,
+// all in float; the block values are then summed in FP64 by
+// residual_finish_kernel.  The CPU oracle reproduces this order exactly.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void block_residual_partial(float c2, double* __restrict__ partial) {
+    __shared__ float wsum[SW_BLOCK / 32];
+    float w = c2;
+    for (int o = 16; o > 0; o >>= 1) w = w + __shfl_xor_sync(0xffffffffu, w, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = w;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        partial[blockIdx.x] =
+            (double)(((wsum[0] + wsum[1]) + (wsum[2] + wsum[3])) + ((wsum[4] + wsum[5]) + (wsum[6] + wsum[7])));
+}
+
+// One vertex per thread.  Entries are taken two at a time with both adjacency
+// loads and then both neighbour loads issued before the arithmetic, which keeps
+// several independent gathers in flight per thread.
+template <bool CHECK>
+__global__ void __launch_bounds__(SW_BLOCK) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
+                                                                const float4* __restrict__ yin,
+                                                                float4* __restrict__ yout,
+                                                                const float* __restrict__ fixed,
+                                                                const int* __restrict__ ptr,
+                                                                const int2* __restrict__ adj, float ks, float kb,
+                                                                int bend_y, const int* conv, int iter,
+                                                                double* __restrict__ partial) {
+    if (iteration_skipped(conv, iter)) return;  // grid-uniform
+    constexpr int G = 2;
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    float c2 = 0.0f;  // sum of C^2 over this vertex's entries (CHECK)
+    if (v < V) {
+        const float4 ps = __ldg(yin + v), xs = __ldg(x4 + v);
+        const int b = __ldg(ptr + v), e = __ldg(ptr + v + 1);
+        float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+        for (int k0 = b; k0 < e; k0 += G) {
+            int2 a[G];
+            float4 o[G];
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-            const float sx_ = __shfl_sync(0xffffffffu, tx, qbase + u);
-            const float sy_ = __shfl_sync(0xffffffffu, ty, qbase + u);
-            const float sz_ = __shfl_sync(0xffffffffu, tz, qbase + u);
-            if (b + 4 * r + u < e) {
-                dx = dx - sx_;
-                dy = dy - sy_;
-                dz = dz - sz_;
+            for (int g = 0; g < G; ++g) a[g] = k0 + g < e ? __ldg(adj + k0 + g) : make_int2(0, 0);
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                const bool use_x = a[g].x < 0 && !bend_y;
+                o[g] = k0 + g < e ? __ldg((use_x ? x4 : yin) + (a[g].x & 0x7fffffff)) : ps;
+            }
+#pragma unroll
+            for (int g = 0; g < G; ++g) {
+                if (k0 + g >= e) break;
+                const bool bend = a[g].x < 0;
+                const float rest = __int_as_float(a[g].y);
+                const bool use_x = bend && !bend_y;
+                const float4 self = use_x ? xs : ps;
+                const float kk = bend ? kb : ks;
+                const float ex = self.x - o[g].x, ey = self.y - o[g].y, ez = self.z - o[g].z;
+                const float lij = sqrtf((ex * ex + ey * ey) + ez * ez);
+                const float C = lij - rest;
+                if (CHECK) c2 = c2 + C * C;
+                const float inv = 1.0f / lij;
+                const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
+                const float schur = (self.w + o[g].w) * ((nx * nx + ny * ny) + nz * nz);
+                const float ld = (kk * C) / (kk * schur + 1.0f);
+                const float a0 = self.w * ld;
+                dx = dx - a0 * nx;
+                dy = dy - a0 * ny;
+                dz = dz - a0 * nz;
             }
         }
+        float4 out = ps;
+        const float nc = (float)(e - b);
+        if (nc > 0.0f) {
+            const float f = fixed[v];
+            out.x = ps.x + f * (dx / nc);
+            out.y = ps.y + f * (dy / nc);
+            out.z = ps.z + f * (dz / nc);
+        }
+        yout[v] = out;
     }
-    if (!valid || j != 0) return;
-    float4 out = ps;
-    const float nc = (float)(e - b);
-    if (nc > 0.0f) {
-        const float f = fixed[v];
-        out.x = ps.x + f * (dx / nc);
-        out.y = ps.y + f * (dy / nc);
-        out.z = ps.z + f * (dz / nc);
-    }
-    yout[v] = out;
+    if (CHECK) block_residual_partial(c2, partial);
 }
 
 // ---------------------------------------------------------------------------
@@ -247,9 +258,9 @@ extern "C" int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out
     if (n_verts == 0) return SX_OK;
     SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj, "sx_jacobi_sweep: null pointer");
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep: y_in4 and y_out4 must not alias");
-    launch(jacobi_sweep_kernel, grid_for(4LL * n_verts, 128), 128, 0, as_stream(stream), 
-        n_verts, (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj,
-        k_spring, k_bend, bend_on_y ? 1 : 0);
+    launch(jacobi_sweep_kernel<false>, sweep_blocks(n_verts), SW_BLOCK, 0, as_stream(stream), n_verts,
+           (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
+           k_bend, bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr);
     return check_launch("jacobi_sweep_kernel");
 }
 
@@ -290,67 +301,106 @@ extern "C" int sx_scene_aabb(const float* p4, int n_verts, float padding, float*
 
 // ---------------------------------------------------------------------------
 // Constraint residual.  The reference defines none (XPBD.py:350-369 runs a
-// fixed number of sweeps); here it is the RMS of C = |p0 - p1| - l0 over the
-// springs and bending pairs, evaluated in FP64 from the float positions.  Each
-// constraint is counted at its lower-numbered endpoint; block sums are combined
-// in a fixed order, so the value is deterministic.
+// fixed number of sweeps).  Here it is sqrt(sum C^2 / n) over all adjacency
+// entries -- every spring and bending pair counted from both endpoints, so the
+// mean equals the per-constraint mean -- with C = |p_self - p_other| - l0 in
+// float exactly as the sweep evaluates it, per-vertex and per-block sums in
+// float (block_residual_partial) and the sum over blocks in FP64.  The checked
+// sweep produces the same value for its input positions.
 // ---------------------------------------------------------------------------
 namespace sx {
-constexpr int RES_BLOCK = 256;
+constexpr int RF_BLOCKS = 64, RF_THREADS = 256;
 
-__global__ void __launch_bounds__(RES_BLOCK) residual_partial_kernel(int V, const float4* __restrict__ p4,
-                                                                     const int* __restrict__ ptr,
-                                                                     const int2* __restrict__ adj,
-                                                                     double* __restrict__ partial) {
-    __shared__ double red[RES_BLOCK];
-    __shared__ double cnt[RES_BLOCK];
-    const int v = blockIdx.x * RES_BLOCK + threadIdx.x;
-    double s = 0.0, c = 0.0;
+__global__ void __launch_bounds__(SW_BLOCK) residual_partial_kernel(int V, const float4* __restrict__ p4,
+                                                                 const int* __restrict__ ptr,
+                                                                 const int2* __restrict__ adj,
+                                                                 double* __restrict__ partial) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    float c2 = 0.0f;
     if (v < V) {
-        const float4 pv = p4[v];
-        for (int k = ptr[v]; k < ptr[v + 1]; ++k) {
-            const int2 a = adj[k];
-            const int nb = a.x & 0x7fffffff;
-            if (nb <= v) continue;
-            const float4 pn = p4[nb];
-            const double dx = (double)pv.x - (double)pn.x, dy = (double)pv.y - (double)pn.y,
-                         dz = (double)pv.z - (double)pn.z;
-            const double C = sqrt(dx * dx + dy * dy + dz * dz) - (double)__int_as_float(a.y);
-            s += C * C;
-            c += 1.0;
+        const float4 ps = __ldg(p4 + v);
+        const int e = __ldg(ptr + v + 1);
+        for (int k = __ldg(ptr + v); k < e; ++k) {
+            const int2 a = __ldg(adj + k);
+            const float4 o = __ldg(p4 + (a.x & 0x7fffffff));
+            const float ex = ps.x - o.x, ey = ps.y - o.y, ez = ps.z - o.z;
+            const float C = sqrtf((ex * ex + ey * ey) + ez * ez) - __int_as_float(a.y);
+            c2 = c2 + C * C;
         }
     }
-    red[threadIdx.x] = s;
-    cnt[threadIdx.x] = c;
+    block_residual_partial(c2, partial);
+}
+
+// Sums the block values in FP64 (fixed order: strided per thread, xor tree per
+// warp, warps in pairs, then the RF_BLOCKS block values in index order by the
+// last block to finish).  With conv != nullptr it also records a check:
+// conv[2] += 1 and, if the residual is at or below tol and no stop iteration
+// is set, conv[0] = iter, conv[3] += iter, conv[4] += 1.
+__global__ void __launch_bounds__(RF_THREADS) residual_finish_kernel(int nb, const double* __restrict__ partial,
+                                                                     double* part2, int* counter,
+                                                                     const int* __restrict__ ptr, int V,
+                                                                     double* out3, int* conv, int iter,
+                                                                     double tol2) {
+    if (iteration_skipped(conv, iter)) return;
+    __shared__ double wsum[RF_THREADS / 32];
+    __shared__ bool last;
+    double acc = 0.0;
+    for (int i = blockIdx.x * RF_THREADS + threadIdx.x; i < nb; i += RF_BLOCKS * RF_THREADS) acc += partial[i];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = acc;
     __syncthreads();
-    for (int o = RES_BLOCK / 2; o > 0; o >>= 1) {
-        if (threadIdx.x < o) {
-            red[threadIdx.x] += red[threadIdx.x + o];
-            cnt[threadIdx.x] += cnt[threadIdx.x + o];
-        }
-        __syncthreads();
-    }
     if (threadIdx.x == 0) {
-        partial[2 * blockIdx.x] = red[0];
-        partial[2 * blockIdx.x + 1] = cnt[0];
+        part2[blockIdx.x] = ((wsum[0] + wsum[1]) + (wsum[2] + wsum[3])) + ((wsum[4] + wsum[5]) + (wsum[6] + wsum[7]));
+        __threadfence();
+        last = atomicAdd(counter, 1) == RF_BLOCKS - 1;
+    }
+    __syncthreads();
+    if (!last || threadIdx.x != 0) return;
+    __threadfence();
+    const volatile double* p2 = part2;
+    double S = 0.0;
+    for (int i = 0; i < RF_BLOCKS; ++i) S += p2[i];
+    const double n = V > 0 ? (double)ptr[V] : 0.0;
+    out3[0] = S;
+    out3[1] = n;
+    out3[2] = n > 0.0 ? sqrt(S / n) : 0.0;
+    *counter = 0;
+    if (conv != nullptr) {
+        conv[2] += 1;
+        if (conv[0] < 0 && S <= tol2 * n) {
+            conv[0] = iter;
+            conv[3] += iter;
+            conv[4] += 1;
+        }
     }
 }
 
-__global__ void residual_final_kernel(int nb, const double* __restrict__ partial, double* out) {
+__global__ void convergence_begin_kernel(int* conv, int reset_totals) {
     if (threadIdx.x != 0) return;
-    double s = 0.0, c = 0.0;
-    for (int i = 0; i < nb; ++i) {
-        s += partial[2 * i];
-        c += partial[2 * i + 1];
+    conv[0] = -1;
+    conv[2] = 0;
+    if (reset_totals) {
+        conv[3] = 0;
+        conv[4] = 0;
     }
-    out[0] = s;
-    out[1] = c;
-    out[2] = c > 0.0 ? sqrt(s / c) : 0.0;
 }
+
 }  // namespace sx
 
+// partial[sweep_blocks] + part2[RF_BLOCKS] (doubles), then the block counter
 extern "C" size_t sx_residual_workspace_bytes(int n_verts) {
-    return (size_t)2 * sizeof(double) * (size_t)grid_for(n_verts > 0 ? n_verts : 1, RES_BLOCK);
+    return sizeof(double) * ((size_t)sweep_blocks(n_verts > 0 ? n_verts : 1) + RF_BLOCKS) + 16;
+}
+
+static int residual_finish(int n_verts, const int* adj_ptr, void* ws, double* out3, int* conv, int iter, double tol,
+                           cudaStream_t s) {
+    const int nb = sweep_blocks(n_verts > 0 ? n_verts : 1);
+    double* partial = (double*)ws;
+    double* part2 = partial + nb;
+    int* counter = (int*)(part2 + RF_BLOCKS);
+    launch(residual_finish_kernel, RF_BLOCKS, RF_THREADS, 0, s, nb, (const double*)partial, part2, counter, adj_ptr,
+           n_verts, out3, conv, iter, tol * tol);
+    return check_launch("residual_finish_kernel");
 }
 
 extern "C" int sx_constraint_residual(const float* p4, const int* adj_ptr, const int* adj, int n_verts, double* out3,
@@ -359,9 +409,46 @@ extern "C" int sx_constraint_residual(const float* p4, const int* adj_ptr, const
     SX_REQUIRE(out3 && ws && (n_verts == 0 || (p4 && adj_ptr && adj)), "sx_constraint_residual: null pointer");
     SX_REQUIRE(ws_bytes >= sx_residual_workspace_bytes(n_verts), "sx_constraint_residual: workspace too small");
     cudaStream_t s = as_stream(stream);
-    const int nb = grid_for(n_verts > 0 ? n_verts : 1, RES_BLOCK);
-    launch(residual_partial_kernel, nb, RES_BLOCK, 0, s, n_verts, (const float4*)p4, adj_ptr, (const int2*)adj,
-           (double*)ws);
-    launch(residual_final_kernel, 1, 32, 0, s, nb, (const double*)ws, out3);
-    return check_launch("constraint_residual");
+    const int nb = sweep_blocks(n_verts > 0 ? n_verts : 1);
+    if (n_verts == 0) {
+        SX_CUDA(cudaMemsetAsync(ws, 0, sizeof(double) * nb, s));
+    } else {
+        launch(residual_partial_kernel, nb, SW_BLOCK, 0, s, n_verts, (const float4*)p4, adj_ptr, (const int2*)adj,
+               (double*)ws);
+        int rc = check_launch("residual_partial_kernel");
+        if (rc) return rc;
+    }
+    return residual_finish(n_verts, adj_ptr, ws, out3, nullptr, 0, 0.0, s);
+}
+
+extern "C" int sx_convergence_begin(int* conv, int reset_totals, void* stream) {
+    SX_REQUIRE(conv, "sx_convergence_begin: null pointer");
+    launch(convergence_begin_kernel, 1, 32, 0, as_stream(stream), conv, reset_totals);
+    return check_launch("convergence_begin_kernel");
+}
+
+extern "C" int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                                       const int* adj_ptr, const int* adj, int n_verts, float k_spring,
+                                       float k_bend, int iter, int check, double tol, int* conv, double* res3,
+                                       void* ws, size_t ws_bytes, void* stream) {
+    SX_REQUIRE(n_verts > 0, "sx_jacobi_sweep_checked: n_verts must be positive");
+    SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj && conv, "sx_jacobi_sweep_checked: null pointer");
+    SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_checked: y_in4 and y_out4 must not alias");
+    SX_REQUIRE(iter >= 0, "sx_jacobi_sweep_checked: iter < 0");
+    SX_REQUIRE(!check || (iter % 2 == 0 && res3 && ws && ws_bytes >= sx_residual_workspace_bytes(n_verts) && tol >= 0.0),
+               "sx_jacobi_sweep_checked: a check needs an even iter, res3, a residual workspace and tol >= 0");
+    cudaStream_t s = as_stream(stream);
+    const int nb = sweep_blocks(n_verts);
+    if (check) {
+        launch(jacobi_sweep_kernel<true>, nb, SW_BLOCK, 0, s, n_verts, (const float4*)x4, (const float4*)y_in4,
+               (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring, k_bend, 1, (const int*)conv, iter,
+               (double*)ws);
+        int rc = check_launch("jacobi_sweep_kernel");
+        if (rc) return rc;
+        return residual_finish(n_verts, adj_ptr, ws, res3, conv, iter, tol, s);
+    }
+    launch(jacobi_sweep_kernel<false>, nb, SW_BLOCK, 0, s, n_verts, (const float4*)x4, (const float4*)y_in4,
+           (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring, k_bend, 1, (const int*)conv, iter,
+           (double*)nullptr);
+    return check_launch("jacobi_sweep_kernel");
 }

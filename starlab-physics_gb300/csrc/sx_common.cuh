@@ -95,4 +95,16 @@ constexpr int kNumCells = kGridRes * kGridRes * kGridRes;
 constexpr int kGridHeader = 8;
 constexpr int kGridWords = kGridHeader + kGridRes * kGridRes;
 
+// ---- convergence control -------------------------------------------------------
+// conv[0] = stop iteration of the current substep: -1 while it has not
+// converged, else the even iteration j whose checked sweep found the residual
+// of its input at or below the tolerance.  Iterations j and j+1 still run (the
+// pair keeps the y ping-pong in step); every kernel of an iteration from j+2 on
+// returns at once.  conv == nullptr: nothing is skipped.
+__device__ __forceinline__ bool iteration_skipped(const int* conv, int iter) {
+    if (conv == nullptr) return false;
+    const int stop = *reinterpret_cast<const volatile int*>(conv);
+    return stop >= 0 && iter >= stop + 2;
+}
+
 }  // namespace sx

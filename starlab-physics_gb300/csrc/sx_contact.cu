@@ -444,44 +444,104 @@ __device__ __forceinline__ float box_d2(V3 p, V3 t0, V3 t1, V3 t2) {
     return (ex * ex + ey * ey) + ez * ez;
 }
 
-__global__ void __launch_bounds__(256) pairs_project_kernel(const int* __restrict__ meta,
-                                                            const int4* __restrict__ pairs,
-                                                            const float4* __restrict__ y4,
-                                                            const float4* __restrict__ xs4,
-                                                            const float* __restrict__ fixed,
-                                                            const float* __restrict__ m_inv, float dHat,
-                                                            float compliance, float cull_d2, long long* dx,
-                                                            int* nc, int* status) {
-    const int st_end = meta[0], dy_end = meta[1], P = meta[2];
-    const bool cull = cull_d2 > 0.0f;
+// One pair of the list: positions of its four vertices and the projection of
+// its kind (vt_st, vt_dy or tv_st by list position).
+struct PairCtx {
+    const int4* __restrict__ pairs;
+    const float4* __restrict__ y4;
+    const float4* __restrict__ xs4;
+    const float* __restrict__ fixed;
+    const float* __restrict__ m_inv;
+    float dHat, compliance;
+    long long* dx;
+    int* nc;
+    int st_end, dy_end;
+};
+
+__device__ __forceinline__ void pair_points(const PairCtx& c, int t, int4 pr, V3 x[4]) {
+    const bool st = t < c.st_end, tv = t >= c.dy_end;
+    x[0] = mk((tv ? c.xs4 : c.y4)[pr.x]);
+    const float4* tri = st ? c.xs4 : c.y4;
+    x[1] = mk(tri[pr.y]);
+    x[2] = mk(tri[pr.z]);
+    x[3] = mk(tri[pr.w]);
+}
+
+__device__ __forceinline__ void project_pair(const PairCtx& c, int t, int* bad) {
+    const int4 pr = c.pairs[t];
+    V3 x[4];
+    pair_points(c, t, pr, x);
+    V3 g[4] = SX_ZERO_G;
+    int dt;
+    float schur;
+    if (t < c.st_end) {
+        project_vt_st(pr.x, x[0], x[1], x[2], x[3], c.m_inv[pr.x], c.dHat, c.compliance, c.dx, c.nc, bad, g, &dt,
+                      &schur);
+    } else if (t < c.dy_end) {
+        const int vv[4] = {pr.x, pr.y, pr.z, pr.w};
+        project_vt_dy(vv, x, c.fixed, c.m_inv, c.dHat, c.dx, c.nc, bad, g, &dt, &schur);
+    } else {
+        const int vv[4] = {-1, pr.y, pr.z, pr.w};
+        project_tv_st(vv, x, c.fixed, c.m_inv, c.dHat, c.compliance, c.dx, c.nc, bad, g, &dt, &schur);
+    }
+}
+
+constexpr int PP_BLOCK = 256;
+
+// With the cull on, most pairs end at the box test and the few that remain
+// would leave a warp mostly idle through the region classification.  Each warp
+// therefore tests 32 pairs at a time, appends the survivors to its queue in
+// shared memory (ballot), and projects them 32 at a time with every lane busy.
+__global__ void __launch_bounds__(PP_BLOCK) pairs_project_kernel(const int* __restrict__ meta,
+                                                                 const int4* __restrict__ pairs,
+                                                                 const float4* __restrict__ y4,
+                                                                 const float4* __restrict__ xs4,
+                                                                 const float* __restrict__ fixed,
+                                                                 const float* __restrict__ m_inv, float dHat,
+                                                                 float compliance, float cull_d2, long long* dx,
+                                                                 int* nc, int* status, const int* conv, int iter) {
+    if (iteration_skipped(conv, iter)) return;
+    const PairCtx c{pairs, y4, xs4, fixed, m_inv, dHat, compliance, dx, nc, meta[0], meta[1]};
+    const int P = meta[2];
     int bad = 0;
-    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
-        const int4 pr = pairs[t];
-        V3 g[4] = SX_ZERO_G;
-        int dt;
-        float schur;
-        if (t < st_end) {
-            const V3 x0 = mk(y4[pr.x]), x1 = mk(xs4[pr.y]), x2 = mk(xs4[pr.z]), x3 = mk(xs4[pr.w]);
-            if (cull && box_d2(x0, x1, x2, x3) > cull_d2) continue;
-            project_vt_st(pr.x, x0, x1, x2, x3, m_inv[pr.x], dHat, compliance, dx, nc, &bad, g, &dt, &schur);
-        } else if (t < dy_end) {
-            const int vv[4] = {pr.x, pr.y, pr.z, pr.w};
-            const V3 x[4] = {mk(y4[pr.x]), mk(y4[pr.y]), mk(y4[pr.z]), mk(y4[pr.w])};
-            if (cull && box_d2(x[0], x[1], x[2], x[3]) > cull_d2) continue;
-            project_vt_dy(vv, x, fixed, m_inv, dHat, dx, nc, &bad, g, &dt, &schur);
-        } else {
-            const int vv[4] = {-1, pr.y, pr.z, pr.w};
-            const V3 x[4] = {mk(xs4[pr.x]), mk(y4[pr.y]), mk(y4[pr.z]), mk(y4[pr.w])};
-            if (cull && box_d2(x[0], x[1], x[2], x[3]) > cull_d2) continue;
-            project_tv_st(vv, x, fixed, m_inv, dHat, compliance, dx, nc, &bad, g, &dt, &schur);
+    if (!(cull_d2 > 0.0f)) {
+        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x)
+            project_pair(c, t, &bad);
+    } else {
+        __shared__ int queue[PP_BLOCK / 32][64];
+        const int lane = threadIdx.x & 31;
+        int* wq = queue[threadIdx.x >> 5];
+        int qn = 0;  // warp-uniform
+        const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+        for (int base = gw * 32; base < P; base += nw * 32) {
+            const int t = base + lane;
+            bool keep = false;
+            if (t < P) {
+                V3 x[4];
+                pair_points(c, t, pairs[t], x);
+                keep = !(box_d2(x[0], x[1], x[2], x[3]) > cull_d2);
+            }
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep) wq[qn + __popc(m & ((1u << lane) - 1u))] = t;
+            qn += __popc(m);
+            __syncwarp();
+            if (qn >= 32) {
+                project_pair(c, wq[lane], &bad);
+                __syncwarp();
+                if (lane < qn - 32) wq[lane] = wq[32 + lane];
+                __syncwarp();
+                qn -= 32;
+            }
         }
+        if (lane < qn) project_pair(c, wq[lane], &bad);
     }
     if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
 }
 
 // update_dx (XPBD.py:384-387) from the fixed-point accumulators; clears them.
 __global__ void collision_apply_kernel(int V, float4* __restrict__ y4, const float* __restrict__ fixed,
-                                       long long* __restrict__ dx, int* __restrict__ nc) {
+                                       long long* __restrict__ dx, int* __restrict__ nc, const int* conv, int iter) {
+    if (iteration_skipped(conv, iter)) return;
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     const int c = nc[v];
@@ -615,7 +675,8 @@ __global__ void __launch_bounds__(256) batched_contacts_kernel(
     const int* __restrict__ vinst, const int* __restrict__ ob_fptr, const int* __restrict__ ob_faces,
     const float4* __restrict__ xs4, const unsigned* __restrict__ vmask, const int* __restrict__ tv_cand,
     const int* __restrict__ tv_num, int cap, const int* __restrict__ cl_faces, float dHat, float compliance,
-    long long* dx, int* nc, int* status) {
+    long long* dx, int* nc, int* status, const int* conv, int iter) {
+    if (iteration_skipped(conv, iter)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     int bad = 0;
     if (i < V) {  // __vt_st: cloth vertex vs its obstacle's faces
@@ -683,7 +744,8 @@ extern "C" int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const
         vsc, vsn, vt_dy_cand, vt_dy_num, tv_st_cand, tv_st_num, dx_fix, nc, po, status);
     int rc = check_launch("collision_project_kernel");
     if (rc) return rc;
-    launch(collision_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)y4, fixed, dx_fix, nc);
+    launch(collision_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)y4, fixed, dx_fix, nc,
+           (const int*)nullptr, 0);
     return check_launch("collision_apply_kernel");
 }
 
@@ -744,18 +806,19 @@ static int sm_count() {
 extern "C" int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4,
                                       const float* xs4, const float* fixed, const float* m_inv, float dHat,
                                       float compliance, float cull_d2, long long* dx_fix, int* nc, int* status,
-                                      void* stream) {
+                                      const int* conv, int iter, void* stream) {
     SX_REQUIRE(n_dy >= 0 && n_st >= 0, "sx_contact_pairs_sweep: bad sizes");
     if (n_dy == 0) return SX_OK;
     SX_REQUIRE(pairs && ws && y4 && fixed && m_inv && dx_fix && nc && status, "sx_contact_pairs_sweep: null pointer");
     SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_sweep: null static positions");
     cudaStream_t s = as_stream(stream);
     PairsWs w = pairs_ws(const_cast<void*>(ws), n_dy, n_st);
-    launch(pairs_project_kernel, sm_count() * 8, 256, 0, s, (const int*)w.meta, (const int4*)pairs,
-           (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, cull_d2, dx_fix, nc, status);
+    launch(pairs_project_kernel, sm_count() * 8, PP_BLOCK, 0, s, (const int*)w.meta, (const int4*)pairs,
+           (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, cull_d2, dx_fix, nc, status, conv,
+           iter);
     int rc = check_launch("pairs_project_kernel");
     if (rc) return rc;
-    launch(collision_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)y4, fixed, dx_fix, nc);
+    launch(collision_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)y4, fixed, dx_fix, nc, conv, iter);
     return check_launch("collision_apply_kernel");
 }
 
@@ -795,7 +858,7 @@ extern "C" int sx_batched_obstacle_contacts(int n_verts, float* y4, const float*
                                             const float* xs4, const unsigned* vmask, int n_ob_verts,
                                             const int* tv_cand, const int* tv_num, int cap, const int* cl_faces,
                                             float dHat, float compliance, long long* dx_fix, int* nc, int* status,
-                                            void* stream) {
+                                            const int* conv, int iter, void* stream) {
     SX_REQUIRE(n_verts >= 0 && n_ob_verts >= 0 && cap >= 1, "sx_batched_obstacle_contacts: bad sizes");
     if (n_verts == 0) return SX_OK;
     SX_REQUIRE(y4 && fixed && m_inv && vinst && ob_fptr && ob_faces && xs4 && vmask && dx_fix && nc && status,
@@ -804,9 +867,10 @@ extern "C" int sx_batched_obstacle_contacts(int n_verts, float* y4, const float*
     cudaStream_t s = as_stream(stream);
     launch(batched_contacts_kernel, grid_for((long long)n_verts + n_ob_verts, 256), 256, 0, s, n_verts, n_ob_verts,
            (const float4*)y4, fixed, m_inv, vinst, ob_fptr, ob_faces, (const float4*)xs4, vmask, tv_cand, tv_num,
-           cap, cl_faces, dHat, compliance, dx_fix, nc, status);
+           cap, cl_faces, dHat, compliance, dx_fix, nc, status, conv, iter);
     int rc = check_launch("batched_contacts_kernel");
     if (rc) return rc;
-    launch(collision_apply_kernel, grid_for(n_verts, 256), 256, 0, s, n_verts, (float4*)y4, fixed, dx_fix, nc);
+    launch(collision_apply_kernel, grid_for(n_verts, 256), 256, 0, s, n_verts, (float4*)y4, fixed, dx_fix, nc, conv,
+           iter);
     return check_launch("collision_apply_kernel");
 }

@@ -23,6 +23,15 @@ Options beyond the reference (keyword-only, defaults reproduce the reference):
   solves use ``"y"``.
 * ``cap`` -- candidate / pair list capacity per query (the reference's 40,
   ``XPBD.py:51``).  Longer lists are truncated and flagged in :attr:`status`.
+* ``tol`` / ``check_every`` (attributes; ``tol=None`` = fixed iteration
+  count) -- iterate each substep until the constraint residual (RMS of
+  C = |p0 - p1| - l0 over springs and bending pairs, :meth:`constraint_residual`)
+  is at most ``tol``, with ``n_iter`` (even) as the cap.  Every
+  ``check_every``-th sweep (even) measures the residual of its input on the GPU;
+  once it is below ``tol`` the current pair of iterations completes and the
+  remaining ones are skipped on the device, inside the captured graph, with no
+  host synchronisation.  Needs ``bending_on="y"`` and the pair-list contacts.
+  :meth:`convergence_stats` reads the counters.
 * ``contact_cull`` (attribute, default on) -- the pair-list contact sweep skips
   a pair whose point-to-triangle-box squared distance exceeds ``dHat * 1.0625``
   before classifying its region.  The distance of every region is at least the
@@ -104,6 +113,11 @@ class Solver:
                                      device=dev)
         self._static_built_for = None
         self.use_graph = False
+        self.tol = None
+        self.check_every = 4
+        self._conv = torch.zeros(8, dtype=torch.int32, device=dev)
+        self._res3 = torch.zeros(4, dtype=torch.float64, device=dev)
+        self._res_ws = torch.zeros(int(sx.sx_residual_workspace_bytes(Vd)), dtype=torch.uint8, device=dev)
         self._graphs = {}
         self.graph_kernel_launches = 0  # library kernels in the last captured frame
         self.record_pairs = record_pairs
@@ -137,14 +151,21 @@ class Solver:
         sx.sx_predict(ptr(m.x4), ptr(m.v4), ptr(m.fixed), ptr(m.y4), m.num_verts, float(dt), g[0], g[1], g[2],
                       stream_handle())
 
-    def spring_sweep(self, dt):
+    def spring_sweep(self, dt, iteration: int = 0):
         """init_variables + solve_spring_constraints_x + update_dx
         (XPBD.py:345-348, :141-184, :384-387); ping-pongs ``y``."""
         m = self.mesh_dy
         k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
         k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
-        sx.sx_jacobi_sweep(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj),
-                           m.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0, stream_handle())
+        if self.tol is None:
+            sx.sx_jacobi_sweep(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj),
+                               m.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0, stream_handle())
+        else:
+            check = 1 if iteration > 0 and iteration % self.check_every == 0 else 0
+            sx.sx_jacobi_sweep_checked(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
+                                       ptr(m.adj), m.num_verts, k_spring, k_bend, iteration, check, float(self.tol),
+                                       ptr(self._conv), ptr(self._res3), ptr(self._res_ws), self._res_ws.numel(),
+                                       stream_handle())
         self._swap_y()
 
     def _swap_y(self):
@@ -203,7 +224,7 @@ class Solver:
                                   self._pairs.shape[0], ptr(self._pairs_ws), self._pairs_ws.numel(),
                                   stream_handle())
 
-    def solve_collision_constraints_x(self, compliance_col=None):
+    def solve_collision_constraints_x(self, compliance_col=None, iteration: int = 0):
         """XPBD.py:237-264 followed by update_dx (XPBD.py:384-387)."""
         m = self.mesh_dy
         s = self.mesh_st
@@ -212,7 +233,9 @@ class Solver:
             sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
                                       ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
                                       ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c), self.contact_cull_d2(),
-                                      ptr(self._dx_fix), ptr(self._nc), ptr(self.status), stream_handle())
+                                      ptr(self._dx_fix), ptr(self._nc), ptr(self.status),
+                                      ptr(self._conv) if self.tol is not None else None, iteration,
+                                      stream_handle())
             return
         sx.sx_collision_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(m.face_indices),
                               ptr(s.face_indices) if s is not None else None, ptr(m.y4),
@@ -223,9 +246,9 @@ class Solver:
                               ptr(self._nc), ptr(self.pair), ptr(self.pair_g), ptr(self.pair_schur),
                               ptr(self.pair_num), ptr(self.status), stream_handle())
 
-    def solve_constraints_jacobi_x(self, dt, first_iteration: bool = True):
+    def solve_constraints_jacobi_x(self, dt, first_iteration: bool = True, iteration: int = 0):
         """XPBD.py:350-369 (broad phase only in the first iteration of a substep)."""
-        self.spring_sweep(dt)
+        self.spring_sweep(dt, iteration)
         if self.enable_collision_handling:
             if self.mesh_st is None:
                 # the reference always has a static mesh when collisions are on
@@ -234,7 +257,7 @@ class Solver:
                 self.broadphase_lbvh()
                 if not self.record_pairs:
                     self.build_contact_pairs()
-            self.solve_collision_constraints_x()
+            self.solve_collision_constraints_x(iteration=iteration)
 
     def compute_velocity_update_x(self, dt):
         """compute_velocity (XPBD.py:341-343) then update_x (XPBD.py:333-337)."""
@@ -246,8 +269,11 @@ class Solver:
         if self.enable_collision_handling and self.rebuild == "substep":
             self.build_bvhs()
         self.compute_y(dt_sub)
+        if self.tol is not None:
+            self._check_tol_mode()
+            sx.sx_convergence_begin(ptr(self._conv), 0, stream_handle())
         for it in range(self.n_iter):
-            self.solve_constraints_jacobi_x(dt_sub, first_iteration=(it == 0))
+            self.solve_constraints_jacobi_x(dt_sub, first_iteration=(it == 0), iteration=it)
         if self.enable_velocity_update:
             raise NotImplementedError("the velocity-level contact pass is not part of this build")
         self.compute_velocity_update_x(dt_sub)
@@ -270,6 +296,27 @@ class Solver:
 
     CULL_MARGIN = 1.0625
 
+    def _check_tol_mode(self):
+        if self.bending_on != "y":
+            raise ValueError("iterating to a tolerance needs bending_on='y'")
+        if self.record_pairs:
+            raise ValueError("iterating to a tolerance needs the pair-list contacts (record_pairs=False)")
+        if self.n_iter % 2 or self.check_every < 2 or self.check_every % 2:
+            raise ValueError("n_iter and check_every must be even when iterating to a tolerance")
+
+    def convergence_stats(self, reset: bool = False) -> dict:
+        """Counters of the tolerance mode since the last reset (host sync):
+        converged substeps, their mean stop iteration (the sweep whose input met
+        the tolerance; two more iterations run after it) and the last residual
+        checked."""
+        c = self._conv.cpu().tolist()
+        r = self._res3.cpu().tolist()
+        out = {"converged_substeps": c[4], "mean_stop_iteration": c[3] / c[4] if c[4] else None,
+               "last_residual": r[2]}
+        if reset:
+            sx.sx_convergence_begin(ptr(self._conv), 1, stream_handle())
+        return out
+
     def contact_cull_d2(self) -> float:
         """Box-distance threshold of the pair-list sweep (0 = classify every pair)."""
         return self.dHat * self.CULL_MARGIN if self.contact_cull else 0.0
@@ -284,7 +331,8 @@ class Solver:
     def _graph_key(self, n_substeps):
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
-                self.compliance_collision, self.self_collision, self.contact_cull, self.mesh_dy.y4.data_ptr())
+                self.compliance_collision, self.self_collision, self.contact_cull, self.tol, self.check_every,
+                self.mesh_dy.y4.data_ptr())
 
     def _capture(self, n_substeps):
         m = self.mesh_dy
@@ -309,18 +357,18 @@ class Solver:
 
     # -- diagnostics ---------------------------------------------------------------
     def constraint_residual(self, positions: str = "x", out=None):
-        """RMS stretch/bending violation in FP64 on the GPU (``sx_constraint_residual``).
+        """RMS stretch/bending violation on the GPU (``sx_constraint_residual``):
+        C = |p0 - p1| - l0 in float as the sweep evaluates it, summed in float
+        per vertex and per block and in FP64 across blocks.
 
         ``positions`` is ``"x"`` or ``"y"``.  Returns a device tensor
-        ``[sum C^2, count, rms]`` (float64); no host synchronisation unless the
-        caller reads it."""
+        ``[sum C^2, count, rms]`` (float64) over the adjacency entries (each
+        constraint counted from both endpoints); no host synchronisation unless
+        the caller reads it."""
         m = self.mesh_dy
         p = m.x4 if positions == "x" else m.y4
         if out is None:
             out = torch.empty(3, dtype=torch.float64, device=self.device)
-        if getattr(self, "_res_ws", None) is None:
-            self._res_ws = torch.empty(int(sx.sx_residual_workspace_bytes(m.num_verts)), dtype=torch.uint8,
-                                       device=self.device)
         sx.sx_constraint_residual(ptr(p), ptr(m.adj_ptr), ptr(m.adj), m.num_verts, ptr(out), ptr(self._res_ws),
                                   self._res_ws.numel(), stream_handle())
         return out

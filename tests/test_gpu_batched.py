@@ -56,3 +56,34 @@ def test_batched_equals_single_instances(pkg, po, use_graph):
         contacts += int((orc.x4[:, 2] > 0.99).sum())
     assert contacts > 0
     assert int(sim.status.item()) & 4 == 0
+
+
+def test_batched_tolerance_mode(pkg):
+    """The batched solver's tolerance mode: tol large stops every substep after
+    iteration 5 (a fixed 6-iteration run), tol 0 never stops (a full run), and
+    an intermediate tolerance stops some substeps; graph replay equals eager."""
+    insts = _instances(pkg, seed=5)
+
+    def run(tol, n_iter=12, use_graph=False, frames=2):
+        sim = pkg.BatchedSolver(insts, dHat=(4e-3) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8,
+                                g=(0.0, 0.0, -9.81), dt=1 / 60, n_iter=n_iter, padding=8e-3)
+        sim.tol = tol
+        sim.use_graph = use_graph
+        for _ in range(frames):
+            sim.forward(10)
+        torch.cuda.synchronize()
+        return sim
+
+    big, six = run(1.0), run(None, n_iter=6)
+    assert big.convergence_stats()["converged_substeps"] == 20
+    assert torch.equal(big.x4, six.x4)
+    zero, full = run(0.0), run(None)
+    assert zero.convergence_stats()["converged_substeps"] == 0
+    assert torch.equal(zero.x4, full.x4)
+    probe = run(0.0, frames=1)
+    tol = probe.convergence_stats()["last_residual"]
+    mid, mid_g = run(tol), run(tol, use_graph=True)
+    n = mid.convergence_stats()["converged_substeps"]
+    assert 0 < n < 20
+    assert torch.equal(mid.x4, mid_g.x4)
+    assert mid_g.convergence_stats()["converged_substeps"] == n

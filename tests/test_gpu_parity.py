@@ -357,15 +357,72 @@ def test_graph_replay_equals_eager(pkg, n_iter):
 
 
 def test_constraint_residual(pkg, po):
+    """sx_constraint_residual equals the oracle's restatement of its summation
+    order bit for bit, and the FP64 value agrees with a float64 evaluation."""
     scene = pkg.scenes.plain64(n=24, seed=2)
     scene.n_iter = 3
     sim = pkg.scenes.make_solver(scene, device=DEV)
     sim.bending_on = "y"
     for _ in range(2):
         sim.forward(scene.n_substeps)
-    r = sim.constraint_residual("x").cpu().numpy()
     m = sim.mesh_dy
-    s, n, rms = po.constraint_residual(_np(m.x4), m.eid_np, m.l0_np, m.bending_np, m.bending_l0_np)
-    assert int(r[1]) == n == m.num_edges + m.bending_constraint_count
-    assert abs(r[0] - s) <= 1e-12 * max(s, 1e-30) * n
-    assert abs(r[2] - rms) <= 1e-9 * rms
+    for which in ("x", "y"):
+        r = sim.constraint_residual(which).cpu().numpy()
+        p = _np(m.x4 if which == "x" else m.y4)
+        ref = po.constraint_residual(p, m.eid_np, m.l0_np, m.bending_np, m.bending_l0_np)
+        assert int(r[1]) == 2 * (m.num_edges + m.bending_constraint_count)
+        assert np.array_equal(r[:3], ref), (r, ref)
+        # float64 evaluation of the same quantity
+        pp = p[:, :3].astype(np.float64)
+        prs = np.concatenate([m.eid_np.reshape(-1, 2), m.bending_np.reshape(-1, 2)])
+        rest = np.concatenate([m.l0_np, m.bending_l0_np]).astype(np.float64)
+        C = np.linalg.norm(pp[prs[:, 0]] - pp[prs[:, 1]], axis=1) - rest
+        assert abs(r[2] - np.sqrt(np.mean(C * C))) <= 1e-4 * r[2]
+
+
+def _tol_run(pkg, po, tol, frames=3, n_iter=16, use_graph=False):
+    scene = pkg.scenes.plain64(n=24, seed=4)
+    scene.n_iter = n_iter
+    sim = pkg.scenes.make_solver(scene, device=DEV)
+    sim.bending_on = "y"
+    sim.tol = tol
+    sim.use_graph = use_graph
+    orc = po.OracleSolver(pkg.scenes.oracle_inputs(sim.mesh_dy), pkg.scenes.oracle_inputs(sim.mesh_st),
+                          dt=scene.dt, g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
+                          k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
+                          padding=scene.padding, n_iter=n_iter, collisions=scene.collisions, rebuild=scene.rebuild,
+                          cap=scene.cap, bending_on="y", contact_cull=sim.contact_cull, tol=tol)
+    for _ in range(frames):
+        sim.forward(scene.n_substeps)
+        orc.forward(scene.n_substeps)
+    torch.cuda.synchronize()
+    return sim, orc
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_tolerance_mode_matches_oracle(pkg, po, use_graph):
+    """Iterating to a residual: the device-side stop decisions and the positions
+    equal the oracle's, for a tolerance that is met at some checks and missed
+    at others."""
+    # the residual after the first check of a free run sets the tolerance
+    probe_sim, probe = _tol_run(pkg, po, tol=0.0, frames=1)
+    tol = float(probe.last_residual[2]) * 1.0000001
+    sim, orc = _tol_run(pkg, po, tol=tol, use_graph=use_graph)
+    st = sim.convergence_stats()
+    assert st["converged_substeps"] == orc.converged
+    assert 0 < orc.converged < 30, orc.converged
+    assert st["mean_stop_iteration"] == orc.stop_sum / orc.converged
+    assert np.array_equal(_np(sim.mesh_dy.x4)[:, :3], orc.x4[:, :3])
+
+
+def test_tolerance_mode_extremes(pkg, po):
+    """tol large: every substep stops at the first check (iterations 0..5 run);
+    tol 0: none stops.  Both equal fixed-count runs."""
+    sim, orc = _tol_run(pkg, po, tol=1.0, frames=2)
+    assert sim.convergence_stats()["converged_substeps"] == 20 == orc.converged
+    fixed_sim, fixed_orc = _tol_run(pkg, po, tol=None, frames=2, n_iter=6)
+    assert np.array_equal(_np(sim.mesh_dy.x4), _np(fixed_sim.mesh_dy.x4))
+    sim0, _ = _tol_run(pkg, po, tol=0.0, frames=2)
+    full, _ = _tol_run(pkg, po, tol=None, frames=2)
+    assert sim0.convergence_stats()["converged_substeps"] == 0
+    assert np.array_equal(_np(sim0.mesh_dy.x4), _np(full.mesh_dy.x4))
