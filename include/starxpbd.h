@@ -283,6 +283,54 @@ size_t sx_color_workspace_bytes(int n_verts, int n_edges);
 int sx_color_edges_greedy(const int* edges, int n_edges, int n_verts, int max_colors, int* color, int* sorted_edges,
                           int* prefix, void* ws, size_t ws_bytes, void* stream);
 
+/* ---- learned warm start (no counterpart in the reference) -----------------
+ * The reference starts every Jacobi solve from the predicted positions
+ * (XPBD.py:116-118).  Here a per-vertex MLP 24 -> 64 -> 64 -> 3 (SiLU, BF16
+ * weights and activations, FP32 accumulation on tensor cores) predicts a
+ * position correction in units of L (the vertex's mean spring rest length);
+ * the solve starts from y_pred + fixed * L * correction, or from y_pred when
+ * that raises the constraint residual.
+ *
+ * Parameters: FP32 master blob of sx_mlp_param_count() floats
+ * (W1[64][32] | b1[64] | W2[64][64] | b2[64] | W3[8][64] | b3[8]) and its BF16
+ * copy of the three matrices (sx_mlp_bf16_count() values, 2 bytes each).
+ * Feature rows: BF16[n][32] (24 features, 8 zeros). */
+int sx_mlp_param_count(void);
+int sx_mlp_bf16_count(void);
+/* features of every vertex from y4 (predicted), x4, c4 (previous solve
+ * correction), fixed, the constraint CSR and Lref; also copies y4 to y_pred4
+ * when that is not NULL */
+int sx_warm_features(const float* x4, const float* y4, const float* c4, const float* fixed, const int* adj_ptr,
+                     const int* adj, const float* Lref, int n_verts, float gx, float gy, float gz, float dt,
+                     void* feat, float* y_pred4, void* stream);
+/* out4[n][4] (columns 0..2 used) = MLP(feat) */
+int sx_mlp_forward(const void* feat, int n_rows, const void* w16, const float* p32, float* out4, void* stream);
+/* y4 = y_pred4 + fixed * (Lref * out4[:, :3]) */
+int sx_warm_apply(const float* y_pred4, const float* out4, const float* fixed, const float* Lref, int n_verts,
+                  float* y4, void* stream);
+/* if res_warm3[2] > res_cold3[2] (residuals from sx_constraint_residual),
+ * y4 = y_pred4; flags2[0] counts such fallbacks, flags2[1] kept warm starts */
+int sx_warm_select(const double* res_warm3, const double* res_cold3, const float* y_pred4, float* y4, int n_verts,
+                   int* flags2, void* stream);
+/* after the solve: c4 = y4 - y_pred4, and (when target4 is not NULL) the
+ * training target target4 = ((y4 - y_pred4) / Lref, fixed) */
+int sx_warm_record(const float* y4, const float* y_pred4, const float* fixed, const float* Lref, int n_verts,
+                   float* c4, float* target4, void* stream);
+/* Training over the rows idx[n_rows] of (feat, target4): loss = sum of
+ * target4.w * |out[:3] - target4.xyz|^2 / n_valid.  sx_mlp_gradients writes
+ * the gradient (sx_mlp_param_count() floats) and stats[0] = n_valid * loss;
+ * sx_mlp_train_step also applies one Adam step (bias corrections for `step`,
+ * 1-based) to p32 and refreshes w16.  Partial sums are combined in a fixed
+ * order.  Workspace: sx_mlp_train_workspace_bytes(n_rows). */
+size_t sx_mlp_train_workspace_bytes(int max_rows);
+int sx_mlp_gradients(const void* feat, const float* target4, const int* idx, int n_rows, int n_valid, const void* w16,
+                     const float* p32, float* grad, float* stats, void* ws, size_t ws_bytes, void* stream);
+int sx_mlp_train_step(const void* feat, const float* target4, const int* idx, int n_rows, int n_valid, void* w16,
+                      float* p32, float* adam_m, float* adam_v, float lr, float beta1, float beta2, float eps, int step,
+                      float* stats, void* ws, size_t ws_bytes, void* stream);
+/* w16 = BF16(p32) for the three weight matrices */
+int sx_mlp_sync_bf16(const float* p32, void* w16, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

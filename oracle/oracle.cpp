@@ -967,6 +967,88 @@ API int or_residual(int V, const float* p4, const int32_t* ptr, const int32_t* a
     return 0;
 }
 
+// Features of the learned warm start (the CUDA library's warm_features_kernel;
+// no counterpart in the reference): per vertex, from the predicted positions
+// y4, start-of-substep positions x4, previous solve correction c4, fixed flags,
+// the vertex-centric constraint CSR and L = mean spring rest length, 24 FP32
+// values clamped to [-16, 16], rounded to BF16 (round to nearest even) and
+// padded with 8 zeros.  Same expressions, same order.
+static uint16_t bf16_rne(float f) {
+    uint32_t u;
+    std::memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u) return (uint16_t)((u >> 16) | 0x40u);
+    u += 0x7fffu + ((u >> 16) & 1u);
+    return (uint16_t)(u >> 16);
+}
+
+API int or_warm_features(int V, const float* x4, const float* y4, const float* c4, const float* fixed,
+                         const int32_t* ptr, const int32_t* adj, const float* Lref, float gx, float gy, float gz,
+                         float dt, uint16_t* feat) {
+    for (int v = 0; v < V; ++v) {
+        const float* ps = y4 + 4 * (size_t)v;
+        const float* xs = x4 + 4 * (size_t)v;
+        const float* cp = c4 + 4 * (size_t)v;
+        const float inv = 1.0f / Lref[v];
+        float sx = 0.0f, sy = 0.0f, sz = 0.0f, bx = 0.0f, by = 0.0f, bz = 0.0f;
+        float sa = 0.0f, ba = 0.0f, smax = 0.0f, smin = 0.0f;
+        int ns = 0, nb = 0;
+        for (int k = ptr[v]; k < ptr[v + 1]; ++k) {
+            const int32_t w = adj[2 * k];
+            float rest;
+            std::memcpy(&rest, adj + 2 * k + 1, 4);
+            const float* o = y4 + 4 * (size_t)(w & 0x7fffffff);
+            const float ex = ps[0] - o[0], ey = ps[1] - o[1], ez = ps[2] - o[2];
+            const float l = std::sqrt((ex * ex + ey * ey) + ez * ez);
+            const float C = l - rest;
+            const float il = l > 0.0f ? 1.0f / l : 0.0f;
+            const float cx = C * (il * ex), cy = C * (il * ey), cz = C * (il * ez);
+            const float r = rest > 0.0f ? C / rest : 0.0f;
+            if (w < 0) {
+                bx = bx + cx; by = by + cy; bz = bz + cz;
+                ba = ba + std::fabs(r);
+                ++nb;
+            } else {
+                sx = sx + cx; sy = sy + cy; sz = sz + cz;
+                sa = sa + std::fabs(r);
+                smax = ns ? std::fmax(smax, r) : r;
+                smin = ns ? std::fmin(smin, r) : r;
+                ++ns;
+            }
+        }
+        const float fs = (float)ns, fb = (float)nb;
+        float f[24];
+        f[0] = ns ? -((sx / fs) * inv) : 0.0f;
+        f[1] = ns ? -((sy / fs) * inv) : 0.0f;
+        f[2] = ns ? -((sz / fs) * inv) : 0.0f;
+        f[3] = nb ? -((bx / fb) * inv) : 0.0f;
+        f[4] = nb ? -((by / fb) * inv) : 0.0f;
+        f[5] = nb ? -((bz / fb) * inv) : 0.0f;
+        f[6] = ns ? sa / fs : 0.0f;
+        f[7] = smax;
+        f[8] = smin;
+        f[9] = nb ? ba / fb : 0.0f;
+        const float dx = ps[0] - xs[0], dy = ps[1] - xs[1], dz = ps[2] - xs[2];
+        f[10] = dx * inv;
+        f[11] = dy * inv;
+        f[12] = dz * inv;
+        f[13] = cp[0] * inv;
+        f[14] = cp[1] * inv;
+        f[15] = cp[2] * inv;
+        f[16] = fixed[v];
+        f[17] = fs / 6.0f;
+        f[18] = fb / 6.0f;
+        f[19] = std::sqrt((cp[0] * cp[0] + cp[1] * cp[1]) + cp[2] * cp[2]) * inv;
+        f[20] = std::sqrt((dx * dx + dy * dy) + dz * dz) * inv;
+        f[21] = ((gx * dt) * dt) * inv;
+        f[22] = ((gy * dt) * dt) * inv;
+        f[23] = ((gz * dt) * dt) * inv;
+        uint16_t* out = feat + 32 * (size_t)v;
+        for (int i = 0; i < 24; ++i) out[i] = bf16_rne(std::fmin(std::fmax(f[i], -16.0f), 16.0f));
+        for (int i = 24; i < 32; ++i) out[i] = 0;
+    }
+    return 0;
+}
+
 // The region classifier, distance and gradient for one point-triangle query
 // (used by tests: known-answer and finite-difference checks).
 API int or_point_triangle(const float* p12, float* d_out, float* g12) {

@@ -41,6 +41,7 @@ _SIGS = {
     "or_face_bvh_refit": [I, P, P, P, P, P, P, P, P],
     "or_face_bvh_traverse": [I, I, P, P, P, P, P, P, P, I, P, P, P],
     "or_residual": [I, P, P, P, P],
+    "or_warm_features": [I, P, P, P, P, P, P, P, F, F, F, F, P],
     "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I],
     "or_point_triangle": [P, P, P],
     "or_color_edges": [I, I, P, I, P, P, P],
@@ -305,6 +306,124 @@ def constraint_residual(p4, edges, l0, bend, bl0):
     """residual() of positions p4 over the springs and bending pairs."""
     ptr, adj = adjacency(p4.shape[0], edges, l0, bend, bl0)
     return residual(p4, ptr, adj)
+
+
+# ---- learned warm start (no counterpart in the reference) --------------------
+# Parameter blob (FP32, 6792): W1[64][32] | b1[64] | W2[64][64] | b2[64] |
+# W3[8][64] | b3[8]; the BF16 copy holds the three weight matrices.
+MLP_SHAPES = [("W1", (64, 32)), ("b1", (64,)), ("W2", (64, 64)), ("b2", (64,)), ("W3", (8, 64)), ("b3", (8,))]
+MLP_PARAMS = sum(int(np.prod(s)) for _, s in MLP_SHAPES)
+
+
+def mlp_unpack(p, dtype=np.float32):
+    out, o = {}, 0
+    for name, shape in MLP_SHAPES:
+        n = int(np.prod(shape))
+        out[name] = np.asarray(p[o:o + n], dtype).reshape(shape)
+        o += n
+    return out
+
+
+def bf16_round(a):
+    """float32 -> nearest BF16 (ties to even), returned as float32."""
+    u = np.ascontiguousarray(a, np.float32).view(np.uint32).astype(np.uint64)
+    r = ((u + 0x7FFF + ((u >> 16) & 1)) >> 16) << 16
+    return r.astype(np.uint32).view(np.float32)
+
+
+def bf16_to_f32(u16):
+    return (np.asarray(u16, np.uint16).astype(np.uint32) << 16).view(np.float32)
+
+
+def warm_features(x4, y4, c4, fixed, ptr, adj, Lref, g, dt):
+    """BF16 feature rows [V, 32] (uint16) of the CUDA warm_features_kernel."""
+    V = y4.shape[0]
+    feat = np.zeros((V, 32), np.uint16)
+    lib().or_warm_features(V, _p(f32(x4)), _p(f32(y4)), _p(f32(c4)), _p(f32(fixed)), _p(i32(ptr)), _p(i32(adj)),
+                           _p(f32(Lref)), float(g[0]), float(g[1]), float(g[2]), float(dt), _p(feat))
+    return feat
+
+
+def _silu(z):
+    return z / (np.float32(1) + np.exp(-z))
+
+
+def _silu_grad(z):
+    s = np.float32(1) / (np.float32(1) + np.exp(-z))
+    return s + z * (s * (np.float32(1) - s))
+
+
+def mlp_forward(feat_u16, params, keep=False):
+    """BF16 operands, FP32 accumulation, BF16 hidden activations."""
+    P = mlp_unpack(params)
+    X = bf16_to_f32(feat_u16)
+    W1, W2, W3 = (bf16_round(P[k]) for k in ("W1", "W2", "W3"))
+    Z1 = (X @ W1.T + P["b1"]).astype(np.float32)
+    H1 = bf16_round(_silu(Z1))
+    Z2 = (H1 @ W2.T + P["b2"]).astype(np.float32)
+    H2 = bf16_round(_silu(Z2))
+    O = (H2 @ W3.T + P["b3"]).astype(np.float32)
+    if keep:
+        return O, (X, Z1, H1, Z2, H2, W1, W2, W3)
+    return O
+
+
+def mlp_gradients(feat_u16, target4, params):
+    """Loss = sum over rows of mask * |O[:3] - t|^2 / n_valid and its gradient,
+    with the CUDA kernels' rounding points (BF16 dO, dZ2, dZ1 operands)."""
+    O, (X, Z1, H1, Z2, H2, W1, W2, W3) = mlp_forward(feat_u16, params, keep=True)
+    T = np.asarray(target4, np.float32)
+    mask = T[:, 3:4]
+    n_valid = max(int(np.count_nonzero(mask)), 1)
+    E = np.zeros_like(O)
+    E[:, :3] = mask * (O[:, :3] - T[:, :3])
+    loss = float(np.sum(E[:, :3] * (O[:, :3] - T[:, :3]), dtype=np.float64))
+    dO = (np.float32(2.0) * np.float32(1.0 / n_valid)) * E
+    dOb = bf16_round(dO)
+    dZ2 = (dOb @ W3).astype(np.float32) * _silu_grad(Z2)
+    dZ2b = bf16_round(dZ2)
+    dZ1 = (dZ2b @ W2).astype(np.float32) * _silu_grad(Z1)
+    dZ1b = bf16_round(dZ1)
+    g = {"W1": dZ1b.T @ X, "b1": dZ1.sum(0), "W2": dZ2b.T @ H1, "b2": dZ2.sum(0), "W3": dOb.T @ H2,
+         "b3": dO.sum(0)}
+    g["W1"][:, 24:] = 0
+    g["W3"][3:] = 0
+    g["b3"][3:] = 0
+    flat = np.concatenate([np.asarray(g[name], np.float32).ravel() for name, _ in MLP_SHAPES])
+    return flat, loss, n_valid
+
+
+def mlp_loss64(feat_u16, target4, params):
+    """Float64 loss of the same network without any rounding (for finite
+    differences of the gradient formulas)."""
+    P = mlp_unpack(params, np.float64)
+    X = bf16_to_f32(feat_u16).astype(np.float64)
+    s = lambda z: z / (1.0 + np.exp(-z))  # noqa: E731
+    O = s(s(X @ P["W1"].T + P["b1"]) @ P["W2"].T + P["b2"]) @ P["W3"].T + P["b3"]
+    T = np.asarray(target4, np.float64)
+    n_valid = max(int(np.count_nonzero(T[:, 3])), 1)
+    return float(np.sum(T[:, 3:4] * (O[:, :3] - T[:, :3]) ** 2) / n_valid)
+
+
+def mlp_gradients64(feat_u16, target4, params):
+    """The backward formulas in float64 without rounding."""
+    P = mlp_unpack(params, np.float64)
+    X = bf16_to_f32(feat_u16).astype(np.float64)
+    sig = lambda z: 1.0 / (1.0 + np.exp(-z))  # noqa: E731
+    Z1 = X @ P["W1"].T + P["b1"]
+    H1 = Z1 * sig(Z1)
+    Z2 = H1 @ P["W2"].T + P["b2"]
+    H2 = Z2 * sig(Z2)
+    O = H2 @ P["W3"].T + P["b3"]
+    T = np.asarray(target4, np.float64)
+    n_valid = max(int(np.count_nonzero(T[:, 3])), 1)
+    dO = np.zeros_like(O)
+    dO[:, :3] = 2.0 * T[:, 3:4] * (O[:, :3] - T[:, :3]) / n_valid
+    sg = lambda z: sig(z) + z * sig(z) * (1 - sig(z))  # noqa: E731
+    dZ2 = (dO @ P["W3"]) * sg(Z2)
+    dZ1 = (dZ2 @ P["W2"]) * sg(Z1)
+    g = {"W1": dZ1.T @ X, "b1": dZ1.sum(0), "W2": dZ2.T @ H1, "b2": dZ2.sum(0), "W3": dO.T @ H2, "b3": dO.sum(0)}
+    return np.concatenate([np.asarray(g[name]).ravel() for name, _ in MLP_SHAPES])
 
 
 # ---- colouring --------------------------------------------------------------

@@ -14,6 +14,9 @@ from .mesh import TriMesh, box_mesh, grid_cloth, icosphere
 from .solver import Solver
 from .batched import BatchedSolver, Instance, batched_scene
 from . import scenes
+from . import learned
+from .learned import WarmStart, WarmStartMLP
 
 __all__ = ["Solver", "BatchedSolver", "Instance", "batched_scene", "LBVH_CELL", "LBVH", "GraphColoring", "TriMesh",
-           "grid_cloth", "box_mesh", "icosphere", "scenes", "SxError", "load_library", "library_path"]
+           "grid_cloth", "box_mesh", "icosphere", "scenes", "learned", "WarmStart", "WarmStartMLP", "SxError",
+           "load_library", "library_path"]

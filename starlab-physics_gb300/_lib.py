@@ -61,6 +61,17 @@ SIGNATURES = {
     "sx_segment_aabbs": ([P, P, I, F, P, P], I),
     "sx_batched_obstacle_broadphase": ([I, P, P, P, P, P, P, F, P, I, P, P, P, P, P, P, I, P, P, P, P], I),
     "sx_batched_obstacle_contacts": ([I, P, P, P, P, P, P, P, P, I, P, P, I, P, F, F, P, P, P, P, I, P], I),
+    "sx_mlp_param_count": ([], I),
+    "sx_mlp_bf16_count": ([], I),
+    "sx_warm_features": ([P, P, P, P, P, P, P, I, F, F, F, F, P, P, P], I),
+    "sx_mlp_forward": ([P, I, P, P, P, P], I),
+    "sx_warm_apply": ([P, P, P, P, I, P, P], I),
+    "sx_warm_select": ([P, P, P, P, I, P, P], I),
+    "sx_warm_record": ([P, P, P, P, I, P, P, P], I),
+    "sx_mlp_train_workspace_bytes": ([I], Z),
+    "sx_mlp_gradients": ([P, P, P, I, I, P, P, P, P, P, Z, P], I),
+    "sx_mlp_train_step": ([P, P, P, I, I, P, P, P, P, F, F, F, F, I, P, P, Z, P], I),
+    "sx_mlp_sync_bf16": ([P, P, P], I),
     "sx_color_workspace_bytes": ([I, I], Z),
     "sx_color_edges_greedy": ([P, I, I, I, P, P, P, P, Z, P], I),
 }
@@ -126,7 +137,7 @@ class _Calls:
     def __getattr__(self, name):
         if name not in SIGNATURES:
             raise AttributeError(name)
-        if SIGNATURES[name][1] is I and name != "sx_version":
+        if SIGNATURES[name][1] is I and name not in ("sx_version", "sx_mlp_param_count", "sx_mlp_bf16_count"):
             return lambda *a: _call(name, *a)
         return getattr(load(), name)
 

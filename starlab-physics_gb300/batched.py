@@ -160,6 +160,8 @@ class BatchedSolver:
         self.status = torch.zeros(1, dtype=torch.int32, device=dev)
         self._dx_fix = torch.zeros(3 * V, dtype=torch.int64, device=dev)
         self._nc = torch.zeros(V, dtype=torch.int32, device=dev)
+        # learned warm start (learned.WarmStart) run after each prediction
+        self.warm = None
         # iterate to a residual (Solver.tol): n_iter is then the cap
         self.tol = None
         self.check_every = 4
@@ -187,6 +189,8 @@ class BatchedSolver:
         g = self.g
         sx.sx_predict(ptr(self.x4), ptr(self.v4), ptr(self.fixed), ptr(self.y4), self.num_verts, float(dt), g[0], g[1],
                       g[2], s)
+        if self.warm is not None:
+            self.warm.begin(self, dt)
         k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
         k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
         tol_mode = self.tol is not None
@@ -218,6 +222,8 @@ class BatchedSolver:
                 ptr(self.ob_faces), ptr(self.xs4), ptr(self.vmask), self.n_ob_verts, ptr(self.tv_cand),
                 ptr(self.tv_num), self.cap, ptr(self.faces), self.dHat, self.compliance_collision, ptr(self._dx_fix),
                 ptr(self._nc), ptr(self.status), conv, it, s)
+        if self.warm is not None:
+            self.warm.end(self)
         sx.sx_velocity_update(ptr(self.x4), ptr(self.y4), ptr(self.v4), ptr(self.fixed), self.num_verts, self.damping,
                               float(dt), s)
 
@@ -235,7 +241,9 @@ class BatchedSolver:
             self._forward_eager(n_substeps)
             return
         key = (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
-               self.stiffness_bending, self.n_iter, self.bending_on, self.tol, self.check_every, self.y4.data_ptr())
+               self.stiffness_bending, self.n_iter, self.bending_on, self.tol, self.check_every,
+               id(self.warm) if self.warm is not None else None,
+               self.warm.mode if self.warm is not None else None, self.y4.data_ptr())
         gr = self._graphs.get(key)
         if gr is None:
             if self._ob_built_for != self.padding:

@@ -77,10 +77,12 @@ __global__ void __launch_bounds__(256) warm_features_kernel(int V, const float4*
                                                             const int* __restrict__ ptr,
                                                             const int2* __restrict__ adj,
                                                             const float* __restrict__ Lref, float gx, float gy,
-                                                            float gz, float dt, unsigned short* __restrict__ feat) {
+                                                            float gz, float dt, unsigned short* __restrict__ feat,
+                                                            float4* __restrict__ ypred) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     const float4 ps = y4[v], xs = x4[v], cp = c4[v];
+    if (ypred) ypred[v] = ps;
     const float inv = 1.0f / Lref[v];
     float sx = 0.0f, sy = 0.0f, sz = 0.0f, bx = 0.0f, by = 0.0f, bz = 0.0f;
     float sa = 0.0f, ba = 0.0f, smax = 0.0f, smin = 0.0f;
@@ -660,13 +662,13 @@ extern "C" int sx_mlp_bf16_count(void) { return kW16; }
 
 extern "C" int sx_warm_features(const float* x4, const float* y4, const float* c4, const float* fixed,
                                 const int* adj_ptr, const int* adj, const float* Lref, int n_verts, float gx, float gy,
-                                float gz, float dt, void* feat, void* stream) {
+                                float gz, float dt, void* feat, float* y_pred4, void* stream) {
     SX_REQUIRE(n_verts >= 0, "sx_warm_features: n_verts < 0");
     if (n_verts == 0) return SX_OK;
     SX_REQUIRE(x4 && y4 && c4 && fixed && adj_ptr && adj && Lref && feat, "sx_warm_features: null pointer");
     launch(warm_features_kernel, grid_for(n_verts, 256), 256, 0, as_stream(stream), n_verts, (const float4*)x4,
            (const float4*)y4, (const float4*)c4, fixed, adj_ptr, (const int2*)adj, Lref, gx, gy, gz, dt,
-           (unsigned short*)feat);
+           (unsigned short*)feat, (float4*)y_pred4);
     return check_launch("warm_features_kernel");
 }
 
