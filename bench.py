@@ -53,6 +53,8 @@ def parse_args():
     ap.add_argument("--no-lbvh", action="store_true", help="skip the standalone 2^20-triangle LBVH measurement")
     ap.add_argument("--no-batched", action="store_true", help="skip the 512-cloth batched measurement")
     ap.add_argument("--only-batched", action="store_true", help="run only the 512-cloth batched measurement")
+    ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start measurement")
+    ap.add_argument("--only-learned", action="store_true", help="run only the learned warm-start measurement")
     return ap.parse_args()
 
 
@@ -358,6 +360,109 @@ def batched512(pkg, steps=5, warmup=2):
             "status_flags": int(sim.status.item())}
 
 
+def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2):
+    """Learned warm start against the plain cold start on the 512-cloth batched
+    workload, at a fixed residual.
+
+    Training: the plain solver (``target_iters`` Jacobi iterations per substep)
+    runs 6 frames of the seed-0 scene (61 440 cloth-substeps); 262 144 random
+    free vertices per substep give (features, correction) samples, and the MLP
+    trains on them for 3000 Adam steps of 65 536 rows with the library's
+    kernels.  Evaluation on the held-out seed-1 scene: from one snapshot, the
+    plain solver runs a frame with ``cal_iters`` iterations per substep and the
+    largest end-of-substep residual of that frame becomes the tolerance.  Both
+    solvers then run frames from the same snapshot, iterating every substep
+    until the residual is at most that tolerance (cap 4 x cal_iters, checks
+    every 4 iterations); the learned one starts from the network's prediction
+    unless that raises the residual."""
+    import torch
+
+    L = pkg.learned
+    kw = dict(dHat=(4e-3) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8, g=(0.0, 0.0, -9.81), dt=1.0 / 60.0,
+              n_iter=20, padding=8e-3)
+    A = pkg.BatchedSolver(pkg.batched_scene(512, seed=0), **kw)
+    for _ in range(2):
+        A.forward(10)
+    A.n_iter = target_iters
+    t0 = time.time()
+    feat, tgt = L.collect_samples(A, frames=6, rows_per_substep=262144)
+    torch.cuda.synchronize()
+    collect_s = time.time() - t0
+    del A
+    B = pkg.BatchedSolver(pkg.batched_scene(512, seed=1), **kw)
+    rec = L.WarmStart(B, mode="record")
+    B.warm = rec
+    for _ in range(2):
+        B.forward(10)
+    B.warm = None
+    vf, vt = L.collect_samples(B, frames=1, rows_per_substep=65536, seed=5)
+    snap = (B.x4.clone(), B.v4.clone(), rec.c4.clone())
+    mlp = pkg.WarmStartMLP(seed=0)
+    loss0 = L.evaluate_loss(mlp, vf, vt)
+    t0 = time.time()
+    h1 = L.train(mlp, feat, tgt, 1500, batch=65536, lr=2e-3)
+    h2 = L.train(mlp, feat, tgt, 1500, batch=65536, lr=5e-4)
+    torch.cuda.synchronize()
+    train_s = time.time() - t0
+    val = L.evaluate_loss(mlp, vf, vt)
+    zero_val = float(vt[:, :3].pow(2).sum(1).mean().item())
+    del feat, tgt
+
+    def restore(warm=None):
+        B.x4.copy_(snap[0])
+        B.v4.copy_(snap[1])
+        if warm is not None:
+            warm.c4.copy_(snap[2])
+
+    # calibration: residual after cal_iters iterations, every substep of a frame
+    restore()
+    B.tol, B.tol_relative, B.check_every, B.n_iter, B.use_graph = 0.0, False, 4, cal_iters + 4, False
+    res = []
+    for _ in range(10):
+        B.substep(B.dt / 10)
+        res.append(float(B._res3[2].item()))
+    tol = max(res)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    out = {"workload": f"512 cloths ({B.num_verts} vertices), held-out seed, frames from one snapshot, "
+                       f"10 substeps, iterate to residual <= {tol:.4e} (cap {4 * cal_iters})",
+           "training": {"samples": 6 * 10 * 262144, "cloth_substeps": 6 * 10 * 512,
+                        "target_iterations": target_iters, "adam_steps": 3000, "batch": 65536,
+                        "collect_s": round(collect_s, 2), "train_s": round(train_s, 2),
+                        "train_loss_first": float(h1[:10].mean()), "train_loss_last": float(h2[-100:].mean()),
+                        "val_loss_untrained": loss0, "val_loss": val, "val_loss_zero_prediction": zero_val},
+           "tolerance": tol, "calibration_residuals": [round(r, 9) for r in res]}
+    for mode in ("plain", "learned"):
+        restore()
+        B.tol, B.n_iter, B.use_graph = tol, 4 * cal_iters, True
+        B.warm = L.WarmStart(B, mlp) if mode == "learned" else None
+        restore(B.warm)
+        B.forward(10)  # capture
+        times = []
+        B.convergence_stats(reset=True)
+        if B.warm is not None:
+            B.warm.flags.zero_()
+        for _ in range(eval_frames):
+            restore(B.warm)
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            B.forward(10)
+            b.record()
+            torch.cuda.synchronize()
+            times.append(a.elapsed_time(b))
+        st = B.convergence_stats()
+        ms = sum(times) / len(times)
+        out[mode] = {"ms_per_frame": round(ms, 3), "value": B.num_verts * 10 / (ms / 1e3), "unit": UNIT,
+                     "converged_substeps": st["converged_substeps"], "substeps": 10 * eval_frames,
+                     "mean_stop_iteration": st["mean_stop_iteration"],
+                     "final_residual": float(B.constraint_residual("x")[2].item())}
+        if B.warm is not None:
+            out[mode].update(B.warm.fallback_counts())
+    B.warm = None
+    out["speedup"] = out["learned"]["value"] / out["plain"]["value"]
+    return out
+
+
 def run_reference(args):
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -419,6 +524,9 @@ def main():
     _lib.load()
     if args.only_batched:
         print(json.dumps({"batched512": batched512(pkg, steps=args.steps, warmup=args.warmup)}))
+        return
+    if args.only_learned:
+        print(json.dumps({"learned_batched512": learned_batched(pkg)}))
         return
     sim = pkg.scenes.make_solver(scene, device="cuda")
     sim.bending_on = "y"
@@ -487,11 +595,11 @@ def main():
     sweeps = []
     orig = sim.spring_sweep
 
-    def timed_sweep(dt, iteration=0):
+    def timed_sweep(dt, iteration=0, loop=0):
         a = torch.cuda.Event(enable_timing=True)
         b = torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        orig(dt, iteration)
+        orig(dt, iteration, loop)
         b.record(stream)
         sweeps.append((a, b))
 
@@ -535,6 +643,8 @@ def main():
         line["lbvh_soup"] = lbvh_soup(pkg, with_cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_batched:
         line["batched512"] = batched512(pkg)
+    if rank == 0 and not args.no_learned:
+        line["learned_batched512"] = learned_batched(pkg)
     if rank == 0 and world >= 1 and not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(scene, rank)
     if rank == 0:

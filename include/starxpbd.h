@@ -87,21 +87,36 @@ int sx_constraint_residual(const float* p4, const int* adj_ptr, const int* adj, 
  * sweep per substep).  conv is a device int[8]:
  *   conv[0] stop iteration of the current substep (-1: not converged),
  *   conv[2] checks made this substep, conv[3] sum of stop iterations and
- *   conv[4] converged substeps since the last reset_totals.
- * sx_convergence_begin starts a substep (conv[0] = -1, conv[2] = 0).
- * sx_jacobi_sweep_checked is sx_jacobi_sweep with bending on y, launched for
- * Jacobi iteration `iter` of the substep.  With check != 0 (iter even) it also
- * computes the residual of its input y_in4 (the state after iteration iter-1)
- * into res3, as sx_constraint_residual would, and if that is <= tol sets
- * conv[0] = iter.  Every kernel of iteration iter' >= conv[0] + 2 -- this
- * sweep, and the contact sweeps given the same conv and iter' -- returns at
- * once, so iterations stop in pairs and y ends in the buffer it would have
- * ended in after an even number of sweeps.  The checks run inside CUDA graphs
- * without host synchronisation. */
-int sx_convergence_begin(int* conv, int reset_totals, void* stream);
+ *   conv[4] converged substeps since the last reset_totals, conv[5] the next
+ *   check's iteration and conv[6] the check interval (device-side loops).
+ * sx_convergence_begin starts a substep with checks every check_every (even)
+ * iterations.  sx_jacobi_sweep_checked is sx_jacobi_sweep with bending on y,
+ * launched for Jacobi iteration `iter` of the substep.  With check != 0 (iter
+ * a multiple of check_every) it also computes the residual of its input y_in4
+ * (the state after iteration iter-1) into res3, as sx_constraint_residual
+ * would, and if that is <= tol (ref3 NULL) or <= tol * ref3[2] (ref3 = a
+ * residual from sx_constraint_residual, e.g. of the substep's cold start) sets
+ * conv[0] = iter.  The rest of that block of check_every iterations runs;
+ * every kernel of a later iteration iter' (this sweep, and the contact sweeps
+ * given the same conv and iter') returns at once, so y ends in the buffer it
+ * would have ended in after an even number of sweeps.  No host
+ * synchronisation is involved.
+ *
+ * Inside a CUDA graph the remaining iterations can run as a device-side loop
+ * instead (nothing is launched after convergence): sx_loop_begin, while
+ * `stream` is being captured, appends a conditional WHILE node and captures
+ * its body on body_stream; the caller issues one block of check_every
+ * iterations there -- the first a checked sweep given loop = *handle_out and
+ * the cap n_iter, the contact sweeps with conv NULL -- and sx_loop_end closes
+ * the body.  The checked sweep ends the loop once converged or when the next
+ * block would start at n_iter.  Same iterations as the gated form. */
+int sx_convergence_begin(int* conv, int check_every, int reset_totals, void* stream);
 int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
                             const int* adj, int n_verts, float k_spring, float k_bend, int iter, int check, double tol,
-                            int* conv, double* res3, void* ws, size_t ws_bytes, void* stream);
+                            const double* ref3, int* conv, double* res3, void* ws, size_t ws_bytes,
+                            unsigned long long loop, int n_iter, void* stream);
+int sx_loop_begin(void* stream, void* body_stream, unsigned long long* handle_out, void** ctx_out);
+int sx_loop_end(void* ctx);
 
 /* computeAABB_faces, meshTaichiWrapper.py:351-365 (positions p4) */
 int sx_face_aabbs(const float* p4, const int* faces, int n_faces, float padding, float* aabb_min4,

@@ -452,12 +452,14 @@ class OracleSolver:
     def __init__(self, mesh_dy, mesh_st=None, *, dt, g, k_stretch_stiffness, k_bend_stiffness, dHat=4e-3,
                  damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
                  compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True,
-                 contact_cull=False, tol=None, check_every=4):
+                 contact_cull=False, tol=None, check_every=4, tol_relative=False):
         self.d = mesh_dy
         # iterate to a residual (the CUDA solver's tol mode): every
         # check_every-th iteration measures the residual of the current y; once
-        # it is <= tol, that iteration and the next run and the rest are skipped
+        # it is <= tol, that block of check_every iterations completes and the
+        # rest are skipped
         self.tol = tol
+        self.tol_relative = tol_relative
         self.check_every = check_every
         self.checks = 0
         self.stop_sum = 0
@@ -539,15 +541,16 @@ class OracleSolver:
         k_bend = float(self.kss) * dt_sub * dt_sub     # XPBD.py:355
         cands = None
         stop = -1
+        ref = residual(y4, self.adj_ptr, self.adj) if self.tol is not None and self.tol_relative else None
         for it in range(self.n_iter):
             if self.tol is not None:
-                if stop >= 0 and it >= stop + 2:
+                if stop >= 0 and it >= stop + self.check_every:
                     break
                 if it > 0 and it % self.check_every == 0:
                     r = residual(y4, self.adj_ptr, self.adj)
                     self.last_residual = r
                     self.checks += 1
-                    if stop < 0 and r[0] <= (self.tol * self.tol) * r[1]:
+                    if stop < 0 and r[0] <= (self.tol * self.tol) * (ref[0] if ref is not None else r[1]):
                         stop = it
                         self.stop_sum += it
                         self.converged += 1

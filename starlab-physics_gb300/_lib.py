@@ -39,8 +39,10 @@ SIGNATURES = {
     "sx_velocity_update": ([P, P, P, P, I, F, F, P], I),
     "sx_residual_workspace_bytes": ([I], Z),
     "sx_constraint_residual": ([P, P, P, I, P, P, Z, P], I),
-    "sx_convergence_begin": ([P, I, P], I),
-    "sx_jacobi_sweep_checked": ([P, P, P, P, P, P, I, F, F, I, I, C.c_double, P, P, P, Z, P], I),
+    "sx_convergence_begin": ([P, I, I, P], I),
+    "sx_jacobi_sweep_checked": ([P, P, P, P, P, P, I, F, F, I, I, C.c_double, P, P, P, P, Z, C.c_ulonglong, I, P], I),
+    "sx_loop_begin": ([P, P, P, P], I),
+    "sx_loop_end": ([P], I),
     "sx_face_aabbs": ([P, P, I, F, P, P, P], I),
     "sx_scene_aabb": ([P, I, F, P, P], I),
     "sx_cell_bvh_workspace_bytes": ([I], Z),

@@ -19,6 +19,7 @@ Each instance's result equals that instance alone in :class:`Solver` with
 """
 from __future__ import annotations
 
+import ctypes as C
 from dataclasses import dataclass
 
 import numpy as np
@@ -164,7 +165,9 @@ class BatchedSolver:
         self.warm = None
         # iterate to a residual (Solver.tol): n_iter is then the cap
         self.tol = None
+        self.tol_relative = False
         self.check_every = 4
+        self._res_ref = torch.zeros(4, dtype=torch.float64, device=dev)
         self._conv = torch.zeros(8, dtype=torch.int32, device=dev)
         self._res3 = torch.zeros(4, dtype=torch.float64, device=dev)
         self._res_ws = torch.zeros(int(sx.sx_residual_workspace_bytes(V)), dtype=torch.uint8, device=dev)
@@ -191,41 +194,77 @@ class BatchedSolver:
                       g[2], s)
         if self.warm is not None:
             self.warm.begin(self, dt)
+        ref = None
+        if self.tol is not None and self.tol_relative:
+            # threshold relative to the residual of the predicted (cold) start
+            if self.warm is not None and self.warm.mode == "apply":
+                ref = ptr(self.warm.res_cold)
+            else:
+                self.constraint_residual("y", out=self._res_ref)
+                ref = ptr(self._res_ref)
         k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
         k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
         tol_mode = self.tol is not None
+        ce = self.check_every
         if tol_mode:
-            if self.bending_on != "y" or self.n_iter % 2 or self.check_every < 2 or self.check_every % 2:
-                raise ValueError("iterating to a tolerance needs bending_on='y' and even n_iter and check_every")
-            sx.sx_convergence_begin(ptr(self._conv), 0, s)
+            if self.bending_on != "y" or self.n_iter % ce or ce < 2 or ce % 2:
+                raise ValueError("iterating to a tolerance needs bending_on='y', an even check_every and n_iter a "
+                                 "multiple of it")
+            sx.sx_convergence_begin(ptr(self._conv), ce, 0, s)
         conv = ptr(self._conv) if tol_mode else None
-        for it in range(self.n_iter):
-            if tol_mode:
-                check = 1 if it > 0 and it % self.check_every == 0 else 0
-                sx.sx_jacobi_sweep_checked(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
-                                           ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend, it,
-                                           check, float(self.tol), conv, ptr(self._res3), ptr(self._res_ws),
-                                           self._res_ws.numel(), s)
-            else:
-                sx.sx_jacobi_sweep(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
-                                   ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend,
-                                   1 if self.bending_on == "y" else 0, s)
-            self._swap_y()
-            if it == 0:
-                sx.sx_batched_obstacle_broadphase(
-                    self.num_verts, ptr(self.y4), ptr(self.vinst), ptr(self.ob_box6), ptr(self.ob_fptr),
-                    ptr(self.ob_fmin4), ptr(self.ob_fmax4), self.padding, ptr(self.vmask), self.n_ob_verts,
-                    ptr(self.xs4), ptr(self.svinst), ptr(self.cl_box6), ptr(self.fptr), ptr(self.fmin4),
-                    ptr(self.fmax4), self.cap, ptr(self.tv_cand), ptr(self.tv_num), ptr(self.status), s)
-            sx.sx_batched_obstacle_contacts(
-                self.num_verts, ptr(self.y4), ptr(self.fixed), ptr(self.m_inv), ptr(self.vinst), ptr(self.ob_fptr),
-                ptr(self.ob_faces), ptr(self.xs4), ptr(self.vmask), self.n_ob_verts, ptr(self.tv_cand),
-                ptr(self.tv_num), self.cap, ptr(self.faces), self.dHat, self.compliance_collision, ptr(self._dx_fix),
-                ptr(self._nc), ptr(self.status), conv, it, s)
+        if tol_mode and self.n_iter > ce and torch.cuda.is_current_stream_capturing():
+            # inside a graph: the first block of iterations, then the rest as a
+            # device-side loop that stops once converged
+            for it in range(ce):
+                self._iteration(it, s, k_spring, k_bend, conv, ref, False)
+            body = self._loop_stream()
+            h, ctx = C.c_ulonglong(0), C.c_void_p(None)
+            sx.sx_loop_begin(s, body.cuda_stream, C.addressof(h), C.addressof(ctx))
+            try:
+                for k in range(ce):
+                    self._iteration(ce + k, body.cuda_stream, k_spring, k_bend, conv, ref, k == 0,
+                                    loop=h.value if k == 0 else 0, in_loop=True)
+            finally:
+                sx.sx_loop_end(ctx)
+        else:
+            for it in range(self.n_iter):
+                check = tol_mode and it > 0 and it % ce == 0
+                self._iteration(it, s, k_spring, k_bend, conv, ref, check)
         if self.warm is not None:
             self.warm.end(self)
         sx.sx_velocity_update(ptr(self.x4), ptr(self.y4), ptr(self.v4), ptr(self.fixed), self.num_verts, self.damping,
                               float(dt), s)
+
+    def _loop_stream(self):
+        if getattr(self, "_body_stream", None) is None:
+            self._body_stream = torch.cuda.Stream(device=self.device)
+        return self._body_stream
+
+    def _iteration(self, it, s, k_spring, k_bend, conv, ref, check, loop=0, in_loop=False):
+        """One Jacobi iteration: sweep (checked in tolerance mode), broad phase
+        in the first iteration, obstacle contacts.  Inside a device-side loop
+        (in_loop) the contact kernels are not gated; ``loop`` is the loop
+        handle, given with the body's checked sweep."""
+        if conv is not None:
+            sx.sx_jacobi_sweep_checked(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
+                                       ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend, it,
+                                       1 if check else 0, float(self.tol), ref, conv, ptr(self._res3),
+                                       ptr(self._res_ws), self._res_ws.numel(), loop, self.n_iter, s)
+        else:
+            sx.sx_jacobi_sweep(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed), ptr(self.adj_ptr),
+                               ptr(self.adj), self.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0, s)
+        self._swap_y()
+        if it == 0:
+            sx.sx_batched_obstacle_broadphase(
+                self.num_verts, ptr(self.y4), ptr(self.vinst), ptr(self.ob_box6), ptr(self.ob_fptr),
+                ptr(self.ob_fmin4), ptr(self.ob_fmax4), self.padding, ptr(self.vmask), self.n_ob_verts,
+                ptr(self.xs4), ptr(self.svinst), ptr(self.cl_box6), ptr(self.fptr), ptr(self.fmin4),
+                ptr(self.fmax4), self.cap, ptr(self.tv_cand), ptr(self.tv_num), ptr(self.status), s)
+        sx.sx_batched_obstacle_contacts(
+            self.num_verts, ptr(self.y4), ptr(self.fixed), ptr(self.m_inv), ptr(self.vinst), ptr(self.ob_fptr),
+            ptr(self.ob_faces), ptr(self.xs4), ptr(self.vmask), self.n_ob_verts, ptr(self.tv_cand),
+            ptr(self.tv_num), self.cap, ptr(self.faces), self.dHat, self.compliance_collision, ptr(self._dx_fix),
+            ptr(self._nc), ptr(self.status), None if in_loop else conv, it, s)
 
     def _forward_eager(self, n_substeps):
         if self._ob_built_for != self.padding:
@@ -241,7 +280,7 @@ class BatchedSolver:
             self._forward_eager(n_substeps)
             return
         key = (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
-               self.stiffness_bending, self.n_iter, self.bending_on, self.tol, self.check_every,
+               self.stiffness_bending, self.n_iter, self.bending_on, self.tol, self.tol_relative, self.check_every,
                id(self.warm) if self.warm is not None else None,
                self.warm.mode if self.warm is not None else None, self.y4.data_ptr())
         gr = self._graphs.get(key)
@@ -280,7 +319,7 @@ class BatchedSolver:
         out = {"converged_substeps": c[4], "mean_stop_iteration": c[3] / c[4] if c[4] else None,
                "last_residual": r[2]}
         if reset:
-            sx.sx_convergence_begin(ptr(self._conv), 1, stream_handle())
+            sx.sx_convergence_begin(ptr(self._conv), self.check_every, 1, stream_handle())
         return out
 
     def instance_positions(self, i):

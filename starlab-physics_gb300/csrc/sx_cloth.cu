@@ -4,6 +4,7 @@
 #include <atomic>
 #include <cstdarg>
 #include <cstdio>
+#include <mutex>
 
 #include "sx_common.cuh"
 
@@ -13,6 +14,27 @@ static thread_local std::string g_last_error;
 static std::atomic<long long> g_launches{0};
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
+
+int resident_blocks_of(const void* kernel, int block) {
+    static std::mutex mu;
+    static const void* keys[64];
+    static int vals[64];
+    static int n = 0;
+    std::lock_guard<std::mutex> lock(mu);
+    for (int i = 0; i < n; ++i)
+        if (keys[i] == kernel) return vals[i];
+    int dev = 0, sms = 0, per_sm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, 0) != cudaSuccess || per_sm < 1)
+        return 1024;
+    if (n < 64) {
+        keys[n] = kernel;
+        vals[n] = sms * per_sm;
+        ++n;
+    }
+    return sms * per_sm;
+}
 
 void set_error(const char* fmt, ...) {
     char buf[512];
@@ -75,15 +97,28 @@ inline int sweep_blocks(int n_verts) { return grid_for(n_verts, SW_BLOCK); }
 // all in float; the block values are then summed in FP64 by
 // residual_finish_kernel.  The CPU oracle reproduces this order exactly.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void block_residual_partial(float c2, double* __restrict__ partial) {
+__device__ __forceinline__ void block_residual_partial(float c2, double* __restrict__ partial, int tile) {
     __shared__ float wsum[SW_BLOCK / 32];
     float w = c2;
     for (int o = 16; o > 0; o >>= 1) w = w + __shfl_xor_sync(0xffffffffu, w, o);
     if ((threadIdx.x & 31) == 0) wsum[threadIdx.x >> 5] = w;
     __syncthreads();
     if (threadIdx.x == 0)
-        partial[blockIdx.x] =
+        partial[tile] =
             (double)(((wsum[0] + wsum[1]) + (wsum[2] + wsum[3])) + ((wsum[4] + wsum[5]) + (wsum[6] + wsum[7])));
+    __syncthreads();  // wsum is reused by the block's next tile
+}
+
+// Kernels over vertex tiles of SW_BLOCK: a block walks tiles blockIdx.x,
+// blockIdx.x + gridDim.x, ...  Per-tile results (residual partials) do not
+// depend on the grid size.  Gated launches (whose iteration may be skipped by
+// the convergence control) cap the grid at one resident wave (tile_grid), so a
+// skipped launch costs one short wave; other launches give every tile a block.
+template <typename K>
+inline int tile_grid(K kernel, int n_verts) {
+    const int tiles = sweep_blocks(n_verts);
+    const int cap = resident_blocks(kernel, SW_BLOCK);
+    return tiles < cap ? tiles : cap;
 }
 
 // One vertex per thread.  Entries are taken two at a time with both adjacency
@@ -100,7 +135,9 @@ __global__ void __launch_bounds__(SW_BLOCK) jacobi_sweep_kernel(int V, const flo
                                                                 double* __restrict__ partial) {
     if (iteration_skipped(conv, iter)) return;  // grid-uniform
     constexpr int G = 2;
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    const int ntiles = (V + SW_BLOCK - 1) / SW_BLOCK;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    const int v = tile * SW_BLOCK + threadIdx.x;
     float c2 = 0.0f;  // sum of C^2 over this vertex's entries (CHECK)
     if (v < V) {
         const float4 ps = __ldg(yin + v), xs = __ldg(x4 + v);
@@ -148,7 +185,8 @@ __global__ void __launch_bounds__(SW_BLOCK) jacobi_sweep_kernel(int V, const flo
         }
         yout[v] = out;
     }
-    if (CHECK) block_residual_partial(c2, partial);
+    if (CHECK) block_residual_partial(c2, partial, tile);
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -315,32 +353,37 @@ __global__ void __launch_bounds__(SW_BLOCK) residual_partial_kernel(int V, const
                                                                  const int* __restrict__ ptr,
                                                                  const int2* __restrict__ adj,
                                                                  double* __restrict__ partial) {
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    float c2 = 0.0f;
-    if (v < V) {
-        const float4 ps = __ldg(p4 + v);
-        const int e = __ldg(ptr + v + 1);
-        for (int k = __ldg(ptr + v); k < e; ++k) {
-            const int2 a = __ldg(adj + k);
-            const float4 o = __ldg(p4 + (a.x & 0x7fffffff));
-            const float ex = ps.x - o.x, ey = ps.y - o.y, ez = ps.z - o.z;
-            const float C = sqrtf((ex * ex + ey * ey) + ez * ez) - __int_as_float(a.y);
-            c2 = c2 + C * C;
+    const int ntiles = (V + SW_BLOCK - 1) / SW_BLOCK;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int v = tile * SW_BLOCK + threadIdx.x;
+        float c2 = 0.0f;
+        if (v < V) {
+            const float4 ps = __ldg(p4 + v);
+            const int e = __ldg(ptr + v + 1);
+            for (int k = __ldg(ptr + v); k < e; ++k) {
+                const int2 a = __ldg(adj + k);
+                const float4 o = __ldg(p4 + (a.x & 0x7fffffff));
+                const float ex = ps.x - o.x, ey = ps.y - o.y, ez = ps.z - o.z;
+                const float C = sqrtf((ex * ex + ey * ey) + ez * ez) - __int_as_float(a.y);
+                c2 = c2 + C * C;
+            }
         }
+        block_residual_partial(c2, partial, tile);
     }
-    block_residual_partial(c2, partial);
 }
 
 // Sums the block values in FP64 (fixed order: strided per thread, xor tree per
 // warp, warps in pairs, then the RF_BLOCKS block values in index order by the
 // last block to finish).  With conv != nullptr it also records a check:
-// conv[2] += 1 and, if the residual is at or below tol and no stop iteration
-// is set, conv[0] = iter, conv[3] += iter, conv[4] += 1.
+// conv[2] += 1 and, if the residual is at or below the threshold (tol, or
+// tol times the residual ref3 over the same constraints) and no stop
+// iteration is set, conv[0] = iter, conv[3] += iter, conv[4] += 1.
 __global__ void __launch_bounds__(RF_THREADS) residual_finish_kernel(int nb, const double* __restrict__ partial,
                                                                      double* part2, int* counter,
                                                                      const int* __restrict__ ptr, int V,
                                                                      double* out3, int* conv, int iter,
-                                                                     double tol2) {
+                                                                     double tol2, const double* ref3,
+                                                                     unsigned long long loop, int n_iter) {
     if (iteration_skipped(conv, iter)) return;
     __shared__ double wsum[RF_THREADS / 32];
     __shared__ bool last;
@@ -366,19 +409,31 @@ __global__ void __launch_bounds__(RF_THREADS) residual_finish_kernel(int nb, con
     out3[2] = n > 0.0 ? sqrt(S / n) : 0.0;
     *counter = 0;
     if (conv != nullptr) {
+        // inside a device-side loop the iteration of this check is conv[5]
+        const int j = loop ? conv[5] : iter;
         conv[2] += 1;
-        if (conv[0] < 0 && S <= tol2 * n) {
-            conv[0] = iter;
-            conv[3] += iter;
+        bool done = false;
+        // absolute: rms <= tol; relative to a reference residual ref3: rms <= tol * rms(ref)
+        if (conv[0] < 0 && S <= tol2 * (ref3 != nullptr ? ref3[0] : n)) {
+            conv[0] = j;
+            conv[3] += j;
             conv[4] += 1;
+            done = true;
+        }
+        if (loop) {
+            const int next = j + conv[6];
+            conv[5] = next;
+            cudaGraphSetConditional((cudaGraphConditionalHandle)loop, (done || next >= n_iter) ? 0u : 1u);
         }
     }
 }
 
-__global__ void convergence_begin_kernel(int* conv, int reset_totals) {
+__global__ void convergence_begin_kernel(int* conv, int check_every, int reset_totals) {
     if (threadIdx.x != 0) return;
     conv[0] = -1;
     conv[2] = 0;
+    conv[5] = check_every;  // the first check
+    conv[6] = check_every;
     if (reset_totals) {
         conv[3] = 0;
         conv[4] = 0;
@@ -393,13 +448,13 @@ extern "C" size_t sx_residual_workspace_bytes(int n_verts) {
 }
 
 static int residual_finish(int n_verts, const int* adj_ptr, void* ws, double* out3, int* conv, int iter, double tol,
-                           cudaStream_t s) {
+                           const double* ref3, unsigned long long loop, int n_iter, cudaStream_t s) {
     const int nb = sweep_blocks(n_verts > 0 ? n_verts : 1);
     double* partial = (double*)ws;
     double* part2 = partial + nb;
     int* counter = (int*)(part2 + RF_BLOCKS);
     launch(residual_finish_kernel, RF_BLOCKS, RF_THREADS, 0, s, nb, (const double*)partial, part2, counter, adj_ptr,
-           n_verts, out3, conv, iter, tol * tol);
+           n_verts, out3, conv, iter, tol * tol, ref3, loop, n_iter);
     return check_launch("residual_finish_kernel");
 }
 
@@ -413,42 +468,104 @@ extern "C" int sx_constraint_residual(const float* p4, const int* adj_ptr, const
     if (n_verts == 0) {
         SX_CUDA(cudaMemsetAsync(ws, 0, sizeof(double) * nb, s));
     } else {
-        launch(residual_partial_kernel, nb, SW_BLOCK, 0, s, n_verts, (const float4*)p4, adj_ptr, (const int2*)adj,
-               (double*)ws);
+        launch(residual_partial_kernel, tile_grid(residual_partial_kernel, n_verts), SW_BLOCK, 0, s, n_verts,
+               (const float4*)p4, adj_ptr,
+               (const int2*)adj, (double*)ws);
         int rc = check_launch("residual_partial_kernel");
         if (rc) return rc;
     }
-    return residual_finish(n_verts, adj_ptr, ws, out3, nullptr, 0, 0.0, s);
+    return residual_finish(n_verts, adj_ptr, ws, out3, nullptr, 0, 0.0, nullptr, 0ull, 0, s);
 }
 
-extern "C" int sx_convergence_begin(int* conv, int reset_totals, void* stream) {
+extern "C" int sx_convergence_begin(int* conv, int check_every, int reset_totals, void* stream) {
     SX_REQUIRE(conv, "sx_convergence_begin: null pointer");
-    launch(convergence_begin_kernel, 1, 32, 0, as_stream(stream), conv, reset_totals);
+    SX_REQUIRE(check_every >= 2 && check_every % 2 == 0, "sx_convergence_begin: check_every must be even and >= 2");
+    launch(convergence_begin_kernel, 1, 32, 0, as_stream(stream), conv, check_every, reset_totals);
     return check_launch("convergence_begin_kernel");
 }
 
 extern "C" int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
                                        const int* adj_ptr, const int* adj, int n_verts, float k_spring,
-                                       float k_bend, int iter, int check, double tol, int* conv, double* res3,
-                                       void* ws, size_t ws_bytes, void* stream) {
+                                       float k_bend, int iter, int check, double tol, const double* ref3,
+                                       int* conv, double* res3, void* ws, size_t ws_bytes,
+                                       unsigned long long loop, int n_iter, void* stream) {
     SX_REQUIRE(n_verts > 0, "sx_jacobi_sweep_checked: n_verts must be positive");
     SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj && conv, "sx_jacobi_sweep_checked: null pointer");
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_checked: y_in4 and y_out4 must not alias");
     SX_REQUIRE(iter >= 0, "sx_jacobi_sweep_checked: iter < 0");
     SX_REQUIRE(!check || (iter % 2 == 0 && res3 && ws && ws_bytes >= sx_residual_workspace_bytes(n_verts) && tol >= 0.0),
                "sx_jacobi_sweep_checked: a check needs an even iter, res3, a residual workspace and tol >= 0");
+    SX_REQUIRE(!loop || check, "sx_jacobi_sweep_checked: a loop handle goes with the check of the loop body");
     cudaStream_t s = as_stream(stream);
+    // inside a device-side loop the kernels are not gated (the loop stops instead)
+    const int* gate = loop ? nullptr : (const int*)conv;
     const int nb = sweep_blocks(n_verts);
     if (check) {
-        launch(jacobi_sweep_kernel<true>, nb, SW_BLOCK, 0, s, n_verts, (const float4*)x4, (const float4*)y_in4,
-               (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring, k_bend, 1, (const int*)conv, iter,
-               (double*)ws);
+        launch(jacobi_sweep_kernel<true>, gate ? tile_grid(jacobi_sweep_kernel<true>, n_verts) : sweep_blocks(n_verts),
+               SW_BLOCK, 0, s, n_verts,
+               (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
+               k_bend, 1, gate, iter, (double*)ws);
         int rc = check_launch("jacobi_sweep_kernel");
         if (rc) return rc;
-        return residual_finish(n_verts, adj_ptr, ws, res3, conv, iter, tol, s);
+        return residual_finish(n_verts, adj_ptr, ws, res3, conv, iter, tol, ref3, loop, n_iter, s);
     }
-    launch(jacobi_sweep_kernel<false>, nb, SW_BLOCK, 0, s, n_verts, (const float4*)x4, (const float4*)y_in4,
-           (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring, k_bend, 1, (const int*)conv, iter,
-           (double*)nullptr);
+    launch(jacobi_sweep_kernel<false>, gate ? tile_grid(jacobi_sweep_kernel<false>, n_verts) : sweep_blocks(n_verts),
+           SW_BLOCK, 0, s, n_verts,
+           (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
+           k_bend, 1, gate, iter, (double*)nullptr);
     return check_launch("jacobi_sweep_kernel");
+}
+
+// ---------------------------------------------------------------------------
+// Device-side iteration loop for CUDA graphs.  While `stream` is being
+// captured, sx_loop_begin adds a conditional WHILE node after the work
+// captured so far and starts capturing its body on `body_stream`; the caller
+// then issues one block of iterations on body_stream, whose checked sweep
+// passes *handle_out (it sets the loop condition: 0 once converged or at the
+// iteration cap), and sx_loop_end closes the body and makes the rest of the
+// capture on `stream` follow the loop.  The condition starts at 1 on every
+// launch of the graph.
+// ---------------------------------------------------------------------------
+namespace sx {
+struct LoopCtx {
+    cudaStream_t main, body;
+    cudaGraphNode_t node;
+};
+}  // namespace sx
+
+extern "C" int sx_loop_begin(void* stream, void* body_stream, unsigned long long* handle_out, void** ctx_out) {
+    SX_REQUIRE(handle_out && ctx_out && body_stream, "sx_loop_begin: null pointer");
+    cudaStream_t s = as_stream(stream), bs = as_stream(body_stream);
+    SX_REQUIRE(s != bs, "sx_loop_begin: the body needs its own stream");
+    cudaStreamCaptureStatus st;
+    cudaGraph_t g = nullptr;
+    const cudaGraphNode_t* deps = nullptr;
+    size_t nd = 0;
+    SX_CUDA(cudaStreamGetCaptureInfo(s, &st, nullptr, &g, &deps, nullptr, &nd));
+    SX_REQUIRE(st == cudaStreamCaptureStatusActive, "sx_loop_begin: the stream is not being captured");
+    cudaGraphConditionalHandle h;
+    SX_CUDA(cudaGraphConditionalHandleCreate(&h, g, 1, cudaGraphCondAssignDefault));
+    cudaGraphNodeParams p = {};
+    p.type = cudaGraphNodeTypeConditional;
+    p.conditional.handle = h;
+    p.conditional.type = cudaGraphCondTypeWhile;
+    p.conditional.size = 1;
+    cudaGraphNode_t node;
+    SX_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, nd, &p));
+    SX_CUDA(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+    SX_CUDA(cudaStreamBeginCaptureToGraph(bs, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed));
+    *handle_out = (unsigned long long)h;
+    *ctx_out = new LoopCtx{s, bs, node};
+    return SX_OK;
+}
+
+extern "C" int sx_loop_end(void* ctx) {
+    SX_REQUIRE(ctx, "sx_loop_end: null context");
+    LoopCtx* c = (LoopCtx*)ctx;
+    cudaGraph_t body = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(c->body, &body);
+    delete c;
+    if (e != cudaSuccess) return cuda_status(e, "sx_loop_end");
+    return SX_OK;
 }

@@ -39,6 +39,15 @@ inline int grid_for(long long n, int block) {
     return (int)(g < 1 ? 1 : g);
 }
 
+// Blocks of `kernel` (block threads, no dynamic shared memory) that the
+// current device keeps resident at once: SMs x active blocks per SM.  Queried
+// once per kernel (keyed by its address) and cached.
+int resident_blocks_of(const void* kernel, int block);
+template <typename K>
+inline int resident_blocks(K kernel, int block) {
+    return resident_blocks_of(reinterpret_cast<const void*>(kernel), block);
+}
+
 // Every kernel launch of the library goes through launch(), which counts it
 // (sx_kernel_launches() reports the running total for benchmarks).
 void note_launch();
@@ -97,14 +106,17 @@ constexpr int kGridWords = kGridHeader + kGridRes * kGridRes;
 
 // ---- convergence control -------------------------------------------------------
 // conv[0] = stop iteration of the current substep: -1 while it has not
-// converged, else the even iteration j whose checked sweep found the residual
-// of its input at or below the tolerance.  Iterations j and j+1 still run (the
-// pair keeps the y ping-pong in step); every kernel of an iteration from j+2 on
-// returns at once.  conv == nullptr: nothing is skipped.
+// converged, else the iteration j (a multiple of the check interval
+// conv[6], which is even) whose checked sweep found the residual of its input
+// at or below the tolerance.  Iterations j .. j + conv[6] - 1 still run (the
+// block of an even number of sweeps keeps the y ping-pong in step); every
+// kernel of a later iteration returns at once.  conv == nullptr: nothing is
+// skipped.
 __device__ __forceinline__ bool iteration_skipped(const int* conv, int iter) {
     if (conv == nullptr) return false;
-    const int stop = *reinterpret_cast<const volatile int*>(conv);
-    return stop >= 0 && iter >= stop + 2;
+    const volatile int* c = conv;
+    const int stop = c[0];
+    return stop >= 0 && iter >= stop + c[6];
 }
 
 }  // namespace sx

@@ -542,22 +542,29 @@ __global__ void __launch_bounds__(PP_BLOCK) pairs_project_kernel(const int* __re
 __global__ void collision_apply_kernel(int V, float4* __restrict__ y4, const float* __restrict__ fixed,
                                        long long* __restrict__ dx, int* __restrict__ nc, const int* conv, int iter) {
     if (iteration_skipped(conv, iter)) return;
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= V) return;
-    const int c = nc[v];
-    if (c > 0) {
-        const float cf = (float)c;
-        const float f = fixed[v];
-        float4 y = y4[v];
-        y.x = y.x + f * (from_fix(dx[3 * v]) / cf);
-        y.y = y.y + f * (from_fix(dx[3 * v + 1]) / cf);
-        y.z = y.z + f * (from_fix(dx[3 * v + 2]) / cf);
-        y4[v] = y;
-        dx[3 * v] = 0;
-        dx[3 * v + 1] = 0;
-        dx[3 * v + 2] = 0;
-        nc[v] = 0;
+    for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
+        const int c = nc[v];
+        if (c > 0) {
+            const float cf = (float)c;
+            const float f = fixed[v];
+            float4 y = y4[v];
+            y.x = y.x + f * (from_fix(dx[3 * v]) / cf);
+            y.y = y.y + f * (from_fix(dx[3 * v + 1]) / cf);
+            y.z = y.z + f * (from_fix(dx[3 * v + 2]) / cf);
+            y4[v] = y;
+            dx[3 * v] = 0;
+            dx[3 * v + 1] = 0;
+            dx[3 * v + 2] = 0;
+            nc[v] = 0;
+        }
     }
+}
+
+// one resident wave at most (the kernels above walk their range)
+template <typename K>
+inline int capped_grid(K kernel, long long n, int block) {
+    const int g = grid_for(n, block), cap = resident_blocks(kernel, block);
+    return g < cap ? g : cap;
 }
 
 // ---------------------------------------------------------------------------
@@ -677,8 +684,8 @@ __global__ void __launch_bounds__(256) batched_contacts_kernel(
     const int* __restrict__ tv_num, int cap, const int* __restrict__ cl_faces, float dHat, float compliance,
     long long* dx, int* nc, int* status, const int* conv, int iter) {
     if (iteration_skipped(conv, iter)) return;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
     int bad = 0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < V + S; i += gridDim.x * blockDim.x) {
     if (i < V) {  // __vt_st: cloth vertex vs its obstacle's faces
         unsigned m = vmask[i];
         if (m) {
@@ -708,6 +715,7 @@ __global__ void __launch_bounds__(256) batched_contacts_kernel(
             float schur;
             project_tv_st(vv, x, fixed, m_inv, dHat, compliance, dx, nc, &bad, g, &dt, &schur);
         }
+    }
     }
     if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
 }
@@ -818,7 +826,8 @@ extern "C" int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, cons
            iter);
     int rc = check_launch("pairs_project_kernel");
     if (rc) return rc;
-    launch(collision_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)y4, fixed, dx_fix, nc, conv, iter);
+    launch(collision_apply_kernel, conv ? capped_grid(collision_apply_kernel, n_dy, 256) : grid_for(n_dy, 256), 256, 0,
+           s, n_dy, (float4*)y4, fixed, dx_fix, nc, conv, iter);
     return check_launch("collision_apply_kernel");
 }
 
@@ -865,12 +874,16 @@ extern "C" int sx_batched_obstacle_contacts(int n_verts, float* y4, const float*
                "sx_batched_obstacle_contacts: null pointer");
     SX_REQUIRE(n_ob_verts == 0 || (tv_cand && tv_num && cl_faces), "sx_batched_obstacle_contacts: null pointer");
     cudaStream_t s = as_stream(stream);
-    launch(batched_contacts_kernel, grid_for((long long)n_verts + n_ob_verts, 256), 256, 0, s, n_verts, n_ob_verts,
+    launch(batched_contacts_kernel,
+           conv ? capped_grid(batched_contacts_kernel, (long long)n_verts + n_ob_verts, 256)
+                : grid_for((long long)n_verts + n_ob_verts, 256),
+           256, 0, s, n_verts, n_ob_verts,
            (const float4*)y4, fixed, m_inv, vinst, ob_fptr, ob_faces, (const float4*)xs4, vmask, tv_cand, tv_num,
            cap, cl_faces, dHat, compliance, dx_fix, nc, status, conv, iter);
     int rc = check_launch("batched_contacts_kernel");
     if (rc) return rc;
-    launch(collision_apply_kernel, grid_for(n_verts, 256), 256, 0, s, n_verts, (float4*)y4, fixed, dx_fix, nc, conv,
+    launch(collision_apply_kernel, conv ? capped_grid(collision_apply_kernel, n_verts, 256) : grid_for(n_verts, 256),
+           256, 0, s, n_verts, (float4*)y4, fixed, dx_fix, nc, conv,
            iter);
     return check_launch("collision_apply_kernel");
 }

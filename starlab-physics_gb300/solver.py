@@ -23,10 +23,12 @@ Options beyond the reference (keyword-only, defaults reproduce the reference):
   solves use ``"y"``.
 * ``cap`` -- candidate / pair list capacity per query (the reference's 40,
   ``XPBD.py:51``).  Longer lists are truncated and flagged in :attr:`status`.
-* ``tol`` / ``check_every`` (attributes; ``tol=None`` = fixed iteration
-  count) -- iterate each substep until the constraint residual (RMS of
-  C = |p0 - p1| - l0 over springs and bending pairs, :meth:`constraint_residual`)
-  is at most ``tol``, with ``n_iter`` (even) as the cap.  Every
+* ``tol`` / ``tol_relative`` / ``check_every`` (attributes; ``tol=None`` =
+  fixed iteration count) -- iterate each substep until the constraint
+  residual (RMS of C = |p0 - p1| - l0 over springs and bending pairs,
+  :meth:`constraint_residual`) is at most ``tol`` (or, with ``tol_relative``,
+  at most ``tol`` times the residual of the substep's predicted positions),
+  with ``n_iter`` (even) as the cap.  Every
   ``check_every``-th sweep (even) measures the residual of its input on the GPU;
   once it is below ``tol`` the current pair of iterations completes and the
   remaining ones are skipped on the device, inside the captured graph, with no
@@ -45,6 +47,8 @@ is compared with squared distances; the collision compliance is the constant
 ``1e8`` (``XPBD.py:367``).
 """
 from __future__ import annotations
+
+import ctypes as C
 
 import torch
 
@@ -114,7 +118,9 @@ class Solver:
         self._static_built_for = None
         self.use_graph = False
         self.tol = None
+        self.tol_relative = False
         self.check_every = 4
+        self._res_ref = torch.zeros(4, dtype=torch.float64, device=dev)
         self._conv = torch.zeros(8, dtype=torch.int32, device=dev)
         self._res3 = torch.zeros(4, dtype=torch.float64, device=dev)
         self._res_ws = torch.zeros(int(sx.sx_residual_workspace_bytes(Vd)), dtype=torch.uint8, device=dev)
@@ -151,9 +157,11 @@ class Solver:
         sx.sx_predict(ptr(m.x4), ptr(m.v4), ptr(m.fixed), ptr(m.y4), m.num_verts, float(dt), g[0], g[1], g[2],
                       stream_handle())
 
-    def spring_sweep(self, dt, iteration: int = 0):
+    def spring_sweep(self, dt, iteration: int = 0, loop: int = 0):
         """init_variables + solve_spring_constraints_x + update_dx
-        (XPBD.py:345-348, :141-184, :384-387); ping-pongs ``y``."""
+        (XPBD.py:345-348, :141-184, :384-387); ping-pongs ``y``.  In tolerance
+        mode the sweep of every check_every-th iteration measures the residual;
+        ``loop`` is the handle of a device-side loop whose body this is."""
         m = self.mesh_dy
         k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
         k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
@@ -164,7 +172,8 @@ class Solver:
             check = 1 if iteration > 0 and iteration % self.check_every == 0 else 0
             sx.sx_jacobi_sweep_checked(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
                                        ptr(m.adj), m.num_verts, k_spring, k_bend, iteration, check, float(self.tol),
-                                       ptr(self._conv), ptr(self._res3), ptr(self._res_ws), self._res_ws.numel(),
+                                       ptr(self._res_ref) if self.tol_relative else None, ptr(self._conv),
+                                       ptr(self._res3), ptr(self._res_ws), self._res_ws.numel(), loop, self.n_iter,
                                        stream_handle())
         self._swap_y()
 
@@ -224,7 +233,7 @@ class Solver:
                                   self._pairs.shape[0], ptr(self._pairs_ws), self._pairs_ws.numel(),
                                   stream_handle())
 
-    def solve_collision_constraints_x(self, compliance_col=None, iteration: int = 0):
+    def solve_collision_constraints_x(self, compliance_col=None, iteration: int = 0, gated: bool = True):
         """XPBD.py:237-264 followed by update_dx (XPBD.py:384-387)."""
         m = self.mesh_dy
         s = self.mesh_st
@@ -234,7 +243,7 @@ class Solver:
                                       ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
                                       ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c), self.contact_cull_d2(),
                                       ptr(self._dx_fix), ptr(self._nc), ptr(self.status),
-                                      ptr(self._conv) if self.tol is not None else None, iteration,
+                                      ptr(self._conv) if self.tol is not None and gated else None, iteration,
                                       stream_handle())
             return
         sx.sx_collision_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(m.face_indices),
@@ -246,9 +255,11 @@ class Solver:
                               ptr(self._nc), ptr(self.pair), ptr(self.pair_g), ptr(self.pair_schur),
                               ptr(self.pair_num), ptr(self.status), stream_handle())
 
-    def solve_constraints_jacobi_x(self, dt, first_iteration: bool = True, iteration: int = 0):
-        """XPBD.py:350-369 (broad phase only in the first iteration of a substep)."""
-        self.spring_sweep(dt, iteration)
+    def solve_constraints_jacobi_x(self, dt, first_iteration: bool = True, iteration: int = 0, loop: int = 0,
+                                   in_loop: bool = False):
+        """XPBD.py:350-369 (broad phase only in the first iteration of a substep).
+        ``in_loop``: part of the body of a device-side loop (kernels not gated)."""
+        self.spring_sweep(dt, iteration, loop)
         if self.enable_collision_handling:
             if self.mesh_st is None:
                 # the reference always has a static mesh when collisions are on
@@ -257,7 +268,7 @@ class Solver:
                 self.broadphase_lbvh()
                 if not self.record_pairs:
                     self.build_contact_pairs()
-            self.solve_collision_constraints_x(iteration=iteration)
+            self.solve_collision_constraints_x(iteration=iteration, gated=not in_loop)
 
     def compute_velocity_update_x(self, dt):
         """compute_velocity (XPBD.py:341-343) then update_x (XPBD.py:333-337)."""
@@ -269,11 +280,31 @@ class Solver:
         if self.enable_collision_handling and self.rebuild == "substep":
             self.build_bvhs()
         self.compute_y(dt_sub)
+        ce = self.check_every
         if self.tol is not None:
             self._check_tol_mode()
-            sx.sx_convergence_begin(ptr(self._conv), 0, stream_handle())
-        for it in range(self.n_iter):
-            self.solve_constraints_jacobi_x(dt_sub, first_iteration=(it == 0), iteration=it)
+            sx.sx_convergence_begin(ptr(self._conv), ce, 0, stream_handle())
+            if self.tol_relative:
+                self.constraint_residual("y", out=self._res_ref)
+        if self.tol is not None and self.n_iter > ce and torch.cuda.is_current_stream_capturing():
+            # inside a graph: the first block of iterations, then the rest as a
+            # device-side loop that stops once converged
+            for it in range(ce):
+                self.solve_constraints_jacobi_x(dt_sub, first_iteration=(it == 0), iteration=it)
+            if getattr(self, "_body_stream", None) is None:
+                self._body_stream = torch.cuda.Stream(device=self.device)
+            h, ctx = C.c_ulonglong(0), C.c_void_p(None)
+            sx.sx_loop_begin(stream_handle(), self._body_stream.cuda_stream, C.addressof(h), C.addressof(ctx))
+            try:
+                with torch.cuda.stream(self._body_stream):
+                    for k in range(ce):
+                        self.solve_constraints_jacobi_x(dt_sub, first_iteration=False, iteration=ce + k,
+                                                        loop=h.value if k == 0 else 0, in_loop=True)
+            finally:
+                sx.sx_loop_end(ctx)
+        else:
+            for it in range(self.n_iter):
+                self.solve_constraints_jacobi_x(dt_sub, first_iteration=(it == 0), iteration=it)
         if self.enable_velocity_update:
             raise NotImplementedError("the velocity-level contact pass is not part of this build")
         self.compute_velocity_update_x(dt_sub)
@@ -301,8 +332,8 @@ class Solver:
             raise ValueError("iterating to a tolerance needs bending_on='y'")
         if self.record_pairs:
             raise ValueError("iterating to a tolerance needs the pair-list contacts (record_pairs=False)")
-        if self.n_iter % 2 or self.check_every < 2 or self.check_every % 2:
-            raise ValueError("n_iter and check_every must be even when iterating to a tolerance")
+        if self.check_every < 2 or self.check_every % 2 or self.n_iter % self.check_every:
+            raise ValueError("iterating to a tolerance needs an even check_every and n_iter a multiple of it")
 
     def convergence_stats(self, reset: bool = False) -> dict:
         """Counters of the tolerance mode since the last reset (host sync):
@@ -314,7 +345,7 @@ class Solver:
         out = {"converged_substeps": c[4], "mean_stop_iteration": c[3] / c[4] if c[4] else None,
                "last_residual": r[2]}
         if reset:
-            sx.sx_convergence_begin(ptr(self._conv), 1, stream_handle())
+            sx.sx_convergence_begin(ptr(self._conv), self.check_every, 1, stream_handle())
         return out
 
     def contact_cull_d2(self) -> float:
@@ -331,7 +362,8 @@ class Solver:
     def _graph_key(self, n_substeps):
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
-                self.compliance_collision, self.self_collision, self.contact_cull, self.tol, self.check_every,
+                self.compliance_collision, self.self_collision, self.contact_cull, self.tol, self.tol_relative,
+                self.check_every,
                 self.mesh_dy.y4.data_ptr())
 
     def _capture(self, n_substeps):

@@ -59,9 +59,11 @@ def test_batched_equals_single_instances(pkg, po, use_graph):
 
 
 def test_batched_tolerance_mode(pkg):
-    """The batched solver's tolerance mode: tol large stops every substep after
-    iteration 5 (a fixed 6-iteration run), tol 0 never stops (a full run), and
-    an intermediate tolerance stops some substeps; graph replay equals eager."""
+    """The batched solver's tolerance mode: tol large stops every substep at the
+    first check (iteration 4; its block runs to iteration 7, a fixed
+    8-iteration run), tol 0 never stops (a full run), and an intermediate
+    tolerance stops some substeps; graph replay (a device-side loop) equals
+    eager (gated launches)."""
     insts = _instances(pkg, seed=5)
 
     def run(tol, n_iter=12, use_graph=False, frames=2):
@@ -74,12 +76,14 @@ def test_batched_tolerance_mode(pkg):
         torch.cuda.synchronize()
         return sim
 
-    big, six = run(1.0), run(None, n_iter=6)
+    big, eight = run(1.0), run(None, n_iter=8)
     assert big.convergence_stats()["converged_substeps"] == 20
-    assert torch.equal(big.x4, six.x4)
+    assert torch.equal(big.x4, eight.x4)
+    assert torch.equal(run(1.0, use_graph=True).x4, eight.x4)
     zero, full = run(0.0), run(None)
     assert zero.convergence_stats()["converged_substeps"] == 0
     assert torch.equal(zero.x4, full.x4)
+    assert torch.equal(run(0.0, use_graph=True).x4, full.x4)
     probe = run(0.0, frames=1)
     tol = probe.convergence_stats()["last_residual"]
     mid, mid_g = run(tol), run(tol, use_graph=True)

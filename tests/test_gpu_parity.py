@@ -380,18 +380,20 @@ def test_constraint_residual(pkg, po):
         assert abs(r[2] - np.sqrt(np.mean(C * C))) <= 1e-4 * r[2]
 
 
-def _tol_run(pkg, po, tol, frames=3, n_iter=16, use_graph=False):
+def _tol_run(pkg, po, tol, frames=3, n_iter=16, use_graph=False, relative=False):
     scene = pkg.scenes.plain64(n=24, seed=4)
     scene.n_iter = n_iter
     sim = pkg.scenes.make_solver(scene, device=DEV)
     sim.bending_on = "y"
     sim.tol = tol
+    sim.tol_relative = relative
     sim.use_graph = use_graph
     orc = po.OracleSolver(pkg.scenes.oracle_inputs(sim.mesh_dy), pkg.scenes.oracle_inputs(sim.mesh_st),
                           dt=scene.dt, g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
                           k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
                           padding=scene.padding, n_iter=n_iter, collisions=scene.collisions, rebuild=scene.rebuild,
-                          cap=scene.cap, bending_on="y", contact_cull=sim.contact_cull, tol=tol)
+                          cap=scene.cap, bending_on="y", contact_cull=sim.contact_cull, tol=tol,
+                          tol_relative=relative)
     for _ in range(frames):
         sim.forward(scene.n_substeps)
         orc.forward(scene.n_substeps)
@@ -415,14 +417,30 @@ def test_tolerance_mode_matches_oracle(pkg, po, use_graph):
     assert np.array_equal(_np(sim.mesh_dy.x4)[:, :3], orc.x4[:, :3])
 
 
+@pytest.mark.parametrize("rho", [0.999, 0.99])
+def test_relative_tolerance_matches_oracle(pkg, po, rho):
+    """Tolerance relative to each substep's cold-start residual."""
+    sim, orc = _tol_run(pkg, po, tol=rho, relative=True)
+    st = sim.convergence_stats()
+    assert st["converged_substeps"] == orc.converged > 0
+    assert st["mean_stop_iteration"] == orc.stop_sum / orc.converged
+    assert np.array_equal(_np(sim.mesh_dy.x4)[:, :3], orc.x4[:, :3])
+
+
 def test_tolerance_mode_extremes(pkg, po):
-    """tol large: every substep stops at the first check (iterations 0..5 run);
-    tol 0: none stops.  Both equal fixed-count runs."""
+    """tol large: every substep stops at the first check, iteration 4, and its
+    block (iterations 4..7) completes; tol 0: none stops.  Both equal
+    fixed-count runs."""
     sim, orc = _tol_run(pkg, po, tol=1.0, frames=2)
     assert sim.convergence_stats()["converged_substeps"] == 20 == orc.converged
-    fixed_sim, fixed_orc = _tol_run(pkg, po, tol=None, frames=2, n_iter=6)
+    fixed_sim, fixed_orc = _tol_run(pkg, po, tol=None, frames=2, n_iter=8)
     assert np.array_equal(_np(sim.mesh_dy.x4), _np(fixed_sim.mesh_dy.x4))
     sim0, _ = _tol_run(pkg, po, tol=0.0, frames=2)
     full, _ = _tol_run(pkg, po, tol=None, frames=2)
     assert sim0.convergence_stats()["converged_substeps"] == 0
     assert np.array_equal(_np(sim0.mesh_dy.x4), _np(full.mesh_dy.x4))
+    # the device-side loop of a captured frame gives the same iterations
+    g_big, _ = _tol_run(pkg, po, tol=1.0, frames=2, use_graph=True)
+    assert np.array_equal(_np(g_big.mesh_dy.x4), _np(fixed_sim.mesh_dy.x4))
+    g0, _ = _tol_run(pkg, po, tol=0.0, frames=2, use_graph=True)
+    assert np.array_equal(_np(g0.mesh_dy.x4), _np(full.mesh_dy.x4))
