@@ -318,7 +318,9 @@ def batched512(pkg, steps=5, warmup=2):
     V, S = sim.num_verts, 10
     stream = torch.cuda.current_stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    for _ in range(warmup):
+    sim.forward(S)
+    variant, _ = sim.autotune()
+    for _ in range(warmup - 1):
         sim.forward(S)
     torch.cuda.synchronize()
     x0, v0 = sim.x4.clone(), sim.v4.clone()
@@ -341,8 +343,8 @@ def batched512(pkg, steps=5, warmup=2):
         flush.zero_()
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        sx.sx_jacobi_sweep(ptr(sim.x4), ptr(sim.y4), ptr(sim._y_other), ptr(sim.fixed), ptr(sim.adj_ptr),
-                           ptr(sim.adj), V, ks, kb, 1, stream_handle())
+        sx.sx_jacobi_sweep_v(ptr(sim.x4), ptr(sim.y4), ptr(sim._y_other), ptr(sim.fixed), ptr(sim.adj_ptr),
+                             ptr(sim.adj), V, ks, kb, 1, sim.sweep_variant, stream_handle())
         b.record(stream)
         ev.append((a, b))
     torch.cuda.synchronize()
@@ -353,6 +355,7 @@ def batched512(pkg, steps=5, warmup=2):
     return {"workload": f"512 cloths, {V} vertices, {sim.num_faces} faces, 10 substeps x 20 iterations, "
                         "obstacle contacts", "value": V * S * steps / (tot / 1e3), "unit": UNIT,
             "ms_per_step": tot / steps, "steps": steps, "warmup": warmup,
+            "sweep_variant": sim.sweep_variant,
             "sweep_roofline": {"bound": "hbm", "achieved": round(alg / (sweep_ms / 1e3) / 1e9, 1), "peak": peak,
                                "unit": "GB/s", "frac": round(alg / (sweep_ms / 1e3) / 1e9 / peak, 4),
                                "algorithmic_bytes_per_launch": alg, "avg_launch_us": round(sweep_ms * 1e3, 2),
@@ -360,15 +363,16 @@ def batched512(pkg, steps=5, warmup=2):
             "status_flags": int(sim.status.item())}
 
 
-def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2):
+def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2, check_every=4, train_frames=10,
+                    train_steps=6000):
     """Learned warm start against the plain cold start on the 512-cloth batched
     workload, at a fixed residual.
 
     Training: the plain solver (``target_iters`` Jacobi iterations per substep)
-    runs 6 frames of the seed-0 scene (61 440 cloth-substeps); 262 144 random
-    free vertices per substep give (features, correction) samples, and the MLP
-    trains on them for 3000 Adam steps of 65 536 rows with the library's
-    kernels.  Evaluation on the held-out seed-1 scene: from one snapshot, the
+    runs ``train_frames`` frames of the seed-0 scene (10 frames: 51 200
+    cloth-substeps); 262 144 random free vertices per substep give (features,
+    correction) samples, and the MLP trains on them for ``train_steps`` Adam
+    steps of 65 536 rows with the library's kernels.  Evaluation on the held-out seed-1 scene: from one snapshot, the
     plain solver runs a frame with ``cal_iters`` iterations per substep and the
     largest end-of-substep residual of that frame becomes the tolerance.  Both
     solvers then run frames from the same snapshot, iterating every substep
@@ -385,7 +389,7 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2):
         A.forward(10)
     A.n_iter = target_iters
     t0 = time.time()
-    feat, tgt = L.collect_samples(A, frames=6, rows_per_substep=262144)
+    feat, tgt = L.collect_samples(A, frames=train_frames, rows_per_substep=262144)
     torch.cuda.synchronize()
     collect_s = time.time() - t0
     del A
@@ -400,8 +404,8 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2):
     mlp = pkg.WarmStartMLP(seed=0)
     loss0 = L.evaluate_loss(mlp, vf, vt)
     t0 = time.time()
-    h1 = L.train(mlp, feat, tgt, 1500, batch=65536, lr=2e-3)
-    h2 = L.train(mlp, feat, tgt, 1500, batch=65536, lr=5e-4)
+    h1 = L.train(mlp, feat, tgt, train_steps // 2, batch=65536, lr=2e-3)
+    h2 = L.train(mlp, feat, tgt, train_steps - train_steps // 2, batch=65536, lr=5e-4)
     torch.cuda.synchronize()
     train_s = time.time() - t0
     val = L.evaluate_loss(mlp, vf, vt)
@@ -416,7 +420,7 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2):
 
     # calibration: residual after cal_iters iterations, every substep of a frame
     restore()
-    B.tol, B.tol_relative, B.check_every, B.n_iter, B.use_graph = 0.0, False, 4, cal_iters + 4, False
+    B.tol, B.tol_relative, B.check_every, B.n_iter, B.use_graph = 0.0, False, check_every, cal_iters + check_every, False
     res = []
     for _ in range(10):
         B.substep(B.dt / 10)
@@ -424,9 +428,10 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2):
     tol = max(res)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
     out = {"workload": f"512 cloths ({B.num_verts} vertices), held-out seed, frames from one snapshot, "
-                       f"10 substeps, iterate to residual <= {tol:.4e} (cap {4 * cal_iters})",
-           "training": {"samples": 6 * 10 * 262144, "cloth_substeps": 6 * 10 * 512,
-                        "target_iterations": target_iters, "adam_steps": 3000, "batch": 65536,
+                       f"10 substeps, iterate to residual <= {tol:.4e} (cap {4 * cal_iters}, checks every "
+                       f"{check_every} iterations)",
+           "training": {"samples": train_frames * 10 * 262144, "cloth_substeps": train_frames * 10 * 512,
+                        "target_iterations": target_iters, "adam_steps": train_steps, "batch": 65536,
                         "collect_s": round(collect_s, 2), "train_s": round(train_s, 2),
                         "train_loss_first": float(h1[:10].mean()), "train_loss_last": float(h2[-100:].mean()),
                         "val_loss_untrained": loss0, "val_loss": val, "val_loss_zero_prediction": zero_val},
@@ -537,7 +542,13 @@ def main():
 
     # the frame runs as one captured CUDA graph (captured on the first call)
     sim.use_graph = not args.eager
-    for _ in range(args.warmup):
+    sim.forward(S)
+    # the sweep's launch configuration is picked by the autotuner on this mesh
+    variant, vtimes = sim.autotune()
+    from starlab_physics_gb300.autotune import variants as sweep_variants
+
+    sweep_cfg = sweep_variants()[variant]
+    for _ in range(args.warmup - 1):
         sim.forward(S)
     torch.cuda.synchronize()
     # every timed step simulates the same frame: the one after the warm-up frames
@@ -592,6 +603,8 @@ def main():
     bytes_io = 2 * V * 16
 
     # ---- dominant kernel: Jacobi sweep, instrumented pass ----
+    from starlab_physics_gb300._lib import ptr, stream_handle, sx
+
     sweeps = []
     orig = sim.spring_sweep
 
@@ -610,8 +623,38 @@ def main():
         sim.forward(S)
     torch.cuda.synchronize()
     sim.spring_sweep = orig
-    sweep_ms = sum(a.elapsed_time(b) for a, b in sweeps) / len(sweeps)
+    eager_ms = sum(a.elapsed_time(b) for a, b in sweeps) / len(sweeps)
+    # the same sweeps back to back as they run inside the frame's graph: a graph
+    # of 30 sweeps (alternating buffers) on the frame's state, replayed and timed
     m = sim.mesh_dy
+    dt_sub = scene.dt / S
+    ks_, kb_ = sim.stiffness_bending * dt_sub * dt_sub, sim.stiffness_stretch * dt_sub * dt_sub
+    ya, yb = m.y4.clone(), torch.empty_like(m.y4)
+
+    def burst():
+        for k in range(30):
+            src, dst = (ya, yb) if k % 2 == 0 else (yb, ya)
+            sx.sx_jacobi_sweep_v(ptr(m.x4), ptr(src), ptr(dst), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj), V, ks_,
+                                 kb_, 1, sim.sweep_variant, stream_handle())
+
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        burst()
+    stream.wait_stream(side)
+    gb = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(gb):
+        burst()
+    reps = []
+    for _ in range(5):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        gb.replay()
+        b.record(stream)
+        torch.cuda.synchronize()
+        reps.append(a.elapsed_time(b) / 30)
+    sweep_ms = sorted(reps)[len(reps) // 2]
     E, B = m.num_edges, m.bending_constraint_count
     alg_bytes = 12 * (E + B) + 28 * V
     achieved = alg_bytes / (sweep_ms / 1e3) / 1e9
@@ -621,6 +664,9 @@ def main():
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": ncu_traffic("jacobi_sweep_kernel_drape256.md"),
                 "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": round(sweep_ms * 1e3, 3),
+                "timing": "CUDA events around a graph of 30 back-to-back sweeps on the frame's state (L2 flushed "
+                          "before each replay), median of 5; one eager launch between events: "
+                          f"{eager_ms * 1e3:.2f} us",
                 "launches_per_step": len(sweeps) // n_inst,
                 "share_of_step": round(sweep_ms * (len(sweeps) / n_inst) / frame_ms, 4),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"}
@@ -631,6 +677,8 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generators)",
         "config": workload_config(scene, args.workload) | {
             "execution": "eager launches" if args.eager else "one CUDA graph per frame",
+            "sweep_config": {"entries_per_load_batch": sweep_cfg[0], "threads_per_block": sweep_cfg[1],
+                             "picked_by": "autotuner (fastest of %d bit-identical variants)" % len(vtimes)},
             "step": f"frame {args.warmup + 1} of the scene, restored from a snapshot before each step"},
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},

@@ -65,6 +65,24 @@ int sx_predict(const float* x4, const float* v4, const float* fixed, float* y4, 
 int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
                     const int* adj, int n_verts, float k_spring, float k_bend, int bend_on_y, void* stream);
 
+/* Launch configurations of the sweep (entries whose loads are issued together,
+ * threads per block) for an autotuner; no counterpart in the reference.  All
+ * variants give bit-identical results; variant 0 is the one sx_jacobi_sweep
+ * uses. */
+int sx_jacobi_sweep_variants(void);
+int sx_jacobi_sweep_variant_info(int variant, int* g, int* block);
+int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
+                      const int* adj, int n_verts, float k_spring, float k_bend, int bend_on_y, int variant,
+                      void* stream);
+
+/* solve_sewing_constraints_x (XPBD.py:425-441) + update_dx over sewn vertex
+ * pairs (zero rest length, k = compliance argument of the reference):
+ * sewn[n_sewn] the vertices with partners, partner[sptr[i] .. sptr[i+1]) the
+ * partners of sewn[i] in ascending pair index; scratch4 holds n_sewn float4.
+ * Coincident pairs add nothing. */
+int sx_sewing_sweep(float* y4, const float* fixed, int n_sewn, const int* sewn, const int* sptr, const int* partner,
+                    float k, float* scratch4, void* stream);
+
 /* compute_velocity + update_x, XPBD.py:341-343 and :333-337:
  * v = (1-damping)*fixed*(y-x)/dt ; x += dt*v */
 int sx_velocity_update(float* x4, const float* y4, float* v4, const float* fixed, int n_verts, float damping,
@@ -117,6 +135,13 @@ int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, float* y_out4, 
                             unsigned long long loop, int n_iter, void* stream);
 int sx_loop_begin(void* stream, void* body_stream, unsigned long long* handle_out, void** ctx_out);
 int sx_loop_end(void* ctx);
+
+/* the two halves of sx_velocity_update, for substeps with the velocity-level
+ * contact pass between them: compute_velocity (XPBD.py:341-343) and update_x
+ * (XPBD.py:333-337) */
+int sx_compute_velocity(const float* x4, const float* y4, float* v4, const float* fixed, int n_verts, float damping,
+                        float dt, void* stream);
+int sx_update_x(float* x4, const float* v4, int n_verts, float dt, void* stream);
 
 /* computeAABB_faces, meshTaichiWrapper.py:351-365 (positions p4) */
 int sx_face_aabbs(const float* p4, const int* faces, int n_faces, float padding, float* aabb_min4,
@@ -255,6 +280,19 @@ int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* f
 int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4, const float* xs4,
                            const float* fixed, const float* m_inv, float dHat, float compliance, float cull_d2,
                            long long* dx_fix, int* nc, int* status, const int* conv, int iter, void* stream);
+
+/* solve_constraints_v (XPBD.py:374-381, :398-404; collision_constraints_v.py
+ * __vt_st :6-133, __tv_st :137-330, __vt_dy :334-570): velocity-level contact
+ * and friction over the pair records of the last sx_collision_sweep (pair,
+ * pair_g, pair_schur, pair_num as written there), velocities v4 of the dynamic
+ * mesh and vs4 of the static one, friction coefficient mu; then update_dv
+ * (v += fixed * dv / nc where m_inv > 0).  dv_fix/nc: zero on entry, left
+ * zero.  m_inv_st: the static mesh's inverse masses (read by __vt_st region
+ * 3, as the reference does). */
+int sx_velocity_contacts(int n_dy, int n_st, const int* faces_dy, const int* faces_st, int cap, const int* pair,
+                         const float* pair_g, const float* pair_schur, const int* pair_num, float* v4, const float* vs4,
+                         const float* fixed, const float* m_inv, const float* m_inv_st, float mu, long long* dv_fix,
+                         int* nc, int* status, void* stream);
 
 /* ---- batched independent cloths with obstacles ---------------------------- */
 

@@ -1049,6 +1049,43 @@ API int or_warm_features(int V, const float* x4, const float* y4, const float* c
     return 0;
 }
 
+// solve_sewing_constraints_x (XPBD.py:425-441) + update_dx, gathered per sewn
+// vertex over its partners in ascending pair index (the CUDA sewing sweep's
+// order); coincident pairs add nothing.  Updates y4 in place.
+API int or_sewing_step(int n_sewn, const int32_t* sewn, const int32_t* sptr, const int32_t* partner, float* y4,
+                       const float* fixed, float k) {
+    std::vector<float> out(4 * (size_t)n_sewn);
+    for (int i = 0; i < n_sewn; ++i) {
+        const float* ps = y4 + 4 * (size_t)sewn[i];
+        float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+        for (int j = sptr[i]; j < sptr[i + 1]; ++j) {
+            const float* o = y4 + 4 * (size_t)partner[j];
+            const float ex = ps[0] - o[0], ey = ps[1] - o[1], ez = ps[2] - o[2];
+            const float C = std::sqrt((ex * ex + ey * ey) + ez * ez);
+            if (C > 0.0f) {
+                const float inv = 1.0f / C;
+                const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
+                const float ld = (k * C) / (k * (ps[3] + o[3]) + 1.0f);
+                const float a0 = ps[3] * ld;
+                dx = dx - a0 * nx;
+                dy = dy - a0 * ny;
+                dz = dz - a0 * nz;
+            }
+        }
+        float* r = out.data() + 4 * (size_t)i;
+        r[0] = ps[0]; r[1] = ps[1]; r[2] = ps[2]; r[3] = ps[3];
+        const float nc = (float)(sptr[i + 1] - sptr[i]);
+        if (nc > 0.0f) {
+            const float f = fixed[sewn[i]];
+            r[0] = ps[0] + f * (dx / nc);
+            r[1] = ps[1] + f * (dy / nc);
+            r[2] = ps[2] + f * (dz / nc);
+        }
+    }
+    for (int i = 0; i < n_sewn; ++i) std::memcpy(y4 + 4 * (size_t)sewn[i], out.data() + 4 * (size_t)i, 16);
+    return 0;
+}
+
 // The region classifier, distance and gradient for one point-triangle query
 // (used by tests: known-answer and finite-difference checks).
 API int or_point_triangle(const float* p12, float* d_out, float* g12) {

@@ -41,6 +41,7 @@ _SIGS = {
     "or_face_bvh_refit": [I, P, P, P, P, P, P, P, P],
     "or_face_bvh_traverse": [I, I, P, P, P, P, P, P, P, I, P, P, P],
     "or_residual": [I, P, P, P, P],
+    "or_sewing_step": [I, P, P, P, P, P, F],
     "or_warm_features": [I, P, P, P, P, P, P, P, F, F, F, F, P],
     "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I],
     "or_point_triangle": [P, P, P],
@@ -293,6 +294,13 @@ def adjacency(n_verts, edges, l0, bend, bl0):
     return ptr, adj
 
 
+def sewing_step(y4, fixed, sewn, sptr, partner, k):
+    """Sewing constraints + update_dx on y4 (in place)."""
+    lib().or_sewing_step(int(len(sewn)), _p(i32(sewn)), _p(i32(sptr)), _p(i32(partner)), _p(y4), _p(f32(fixed)),
+                         float(k))
+    return y4
+
+
 def residual(p4, ptr, adj):
     """The CUDA library's constraint residual {S, n, sqrt(S/n)} in its exact
     summation order (float per vertex and block, FP64 across blocks); the
@@ -452,7 +460,7 @@ class OracleSolver:
     def __init__(self, mesh_dy, mesh_st=None, *, dt, g, k_stretch_stiffness, k_bend_stiffness, dHat=4e-3,
                  damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
                  compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True,
-                 contact_cull=False, tol=None, check_every=4, tol_relative=False):
+                 contact_cull=False, tol=None, check_every=4, tol_relative=False, sewing=None):
         self.d = mesh_dy
         # iterate to a residual (the CUDA solver's tol mode): every
         # check_every-th iteration measures the residual of the current y; once
@@ -460,6 +468,8 @@ class OracleSolver:
         # rest are skipped
         self.tol = tol
         self.tol_relative = tol_relative
+        # sewing: (sewn, sptr, partner, stiffness) -- k = stiffness * dt^2 per iteration
+        self.sewing = sewing
         self.check_every = check_every
         self.checks = 0
         self.stop_sum = 0
@@ -565,6 +575,9 @@ class OracleSolver:
                                     self.compliance, self.cap, vt_st[:2], vt_dy[:2], tv_st[:2],
                                     nthreads=self.nthreads, cull_d2=self.cull_d2)
                 self.last_status |= r["status"]
+            if self.sewing is not None:
+                sewn, sptr, partner, stiff = self.sewing
+                sewing_step(y4, self.fixed, sewn, sptr, partner, float(stiff) * dt_sub * dt_sub)
         velocity_update(self.x4, y4, self.v4, self.fixed, self.damping, dt_sub, self.nthreads)
         self.y4 = y4
 

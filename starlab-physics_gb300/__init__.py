@@ -15,8 +15,9 @@ from .solver import Solver
 from .batched import BatchedSolver, Instance, batched_scene
 from . import scenes
 from . import learned
+from . import meshio
 from .learned import WarmStart, WarmStartMLP
 
 __all__ = ["Solver", "BatchedSolver", "Instance", "batched_scene", "LBVH_CELL", "LBVH", "GraphColoring", "TriMesh",
-           "grid_cloth", "box_mesh", "icosphere", "scenes", "learned", "WarmStart", "WarmStartMLP", "SxError",
+           "grid_cloth", "box_mesh", "icosphere", "scenes", "learned", "meshio", "WarmStart", "WarmStartMLP", "SxError",
            "load_library", "library_path"]

@@ -36,7 +36,14 @@ SIGNATURES = {
     "sx_kernel_launches": ([], C.c_longlong),
     "sx_predict": ([P, P, P, P, I, F, F, F, F, P], I),
     "sx_jacobi_sweep": ([P, P, P, P, P, P, I, F, F, I, P], I),
+    "sx_jacobi_sweep_variants": ([], I),
+    "sx_jacobi_sweep_variant_info": ([I, P, P], I),
+    "sx_jacobi_sweep_v": ([P, P, P, P, P, P, I, F, F, I, I, P], I),
     "sx_velocity_update": ([P, P, P, P, I, F, F, P], I),
+    "sx_compute_velocity": ([P, P, P, P, I, F, F, P], I),
+    "sx_update_x": ([P, P, I, F, P], I),
+    "sx_velocity_contacts": ([I, I, P, P, I, P, P, P, P, P, P, P, P, P, F, P, P, P, P], I),
+    "sx_sewing_sweep": ([P, P, I, P, P, P, F, P, P], I),
     "sx_residual_workspace_bytes": ([I], Z),
     "sx_constraint_residual": ([P, P, P, I, P, P, Z, P], I),
     "sx_convergence_begin": ([P, I, I, P], I),
@@ -139,7 +146,8 @@ class _Calls:
     def __getattr__(self, name):
         if name not in SIGNATURES:
             raise AttributeError(name)
-        if SIGNATURES[name][1] is I and name not in ("sx_version", "sx_mlp_param_count", "sx_mlp_bf16_count"):
+        if SIGNATURES[name][1] is I and name not in ("sx_version", "sx_mlp_param_count", "sx_mlp_bf16_count",
+                                                     "sx_jacobi_sweep_variants"):
             return lambda *a: _call(name, *a)
         return getattr(load(), name)
 

@@ -1,0 +1,75 @@
+"""Autotuner for the Jacobi sweep's launch configuration.
+
+The sweep kernel is compiled in several configurations -- how many adjacency
+entries a thread loads before it computes, and how many threads (= vertices) a
+block holds (``sx_jacobi_sweep_variant_info``); all give bit-identical
+results.  The best one depends on the mesh: a 65 536-vertex cloth whose sweep
+is L2-resident and latency-bound wants more loads in flight per thread, a
+3.2 M-vertex batch that streams from HBM wants more resident threads.
+:func:`tune_sweep` times every configuration on the caller's own arrays (a
+CUDA graph of back-to-back sweeps, CUDA events, median of rounds) and returns
+the fastest; results are cached per (device, vertex count, adjacency size).
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from ._lib import load, ptr, stream_handle, sx
+
+_cache: dict = {}
+
+
+def variants() -> list[tuple[int, int]]:
+    """(entries per load batch, threads per block) of every compiled variant."""
+    L = load()
+    out = []
+    for k in range(int(L.sx_jacobi_sweep_variants())):
+        g, b = C.c_int(0), C.c_int(0)
+        sx.sx_jacobi_sweep_variant_info(k, C.addressof(g), C.addressof(b))
+        out.append((g.value, b.value))
+    return out
+
+
+def _time_variant(v, args, reps, rounds):
+    x4, y4, out, fixed, adj_ptr, adj, n, ks, kb, bend_y = args
+
+    def run():
+        sx.sx_jacobi_sweep_v(ptr(x4), ptr(y4), ptr(out), ptr(fixed), ptr(adj_ptr), ptr(adj), n, ks, kb, bend_y, v,
+                             stream_handle())
+
+    side = torch.cuda.Stream(device=x4.device)
+    side.wait_stream(torch.cuda.current_stream(x4.device))
+    with torch.cuda.stream(side):
+        run()
+    torch.cuda.current_stream(x4.device).wait_stream(side)
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        for _ in range(reps):
+            run()
+    g.replay()
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(rounds):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record()
+        g.replay()
+        b.record()
+        torch.cuda.synchronize()
+        ts.append(a.elapsed_time(b) / reps)
+    return float(np.median(ts))
+
+
+def tune_sweep(x4, y4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y=1, reps=20, rounds=5):
+    """Fastest sweep variant for these arrays, and the per-variant times (ms)."""
+    key = (torch.cuda.get_device_name(x4.device), int(n_verts), int(adj.shape[0]))
+    if key in _cache:
+        return _cache[key]
+    out = torch.empty_like(y4)
+    args = (x4, y4, out, fixed, adj_ptr, adj, int(n_verts), float(k_spring), float(k_bend), int(bend_on_y))
+    times = [_time_variant(v, args, reps, rounds) for v in range(len(variants()))]
+    best = int(np.argmin(times))
+    _cache[key] = (best, times)
+    return best, times

@@ -163,6 +163,8 @@ class BatchedSolver:
         self._nc = torch.zeros(V, dtype=torch.int32, device=dev)
         # learned warm start (learned.WarmStart) run after each prediction
         self.warm = None
+        # launch configuration of the fixed-count sweep (autotune() picks one)
+        self.sweep_variant = 0
         # iterate to a residual (Solver.tol): n_iter is then the cap
         self.tol = None
         self.tol_relative = False
@@ -251,8 +253,9 @@ class BatchedSolver:
                                        1 if check else 0, float(self.tol), ref, conv, ptr(self._res3),
                                        ptr(self._res_ws), self._res_ws.numel(), loop, self.n_iter, s)
         else:
-            sx.sx_jacobi_sweep(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed), ptr(self.adj_ptr),
-                               ptr(self.adj), self.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0, s)
+            sx.sx_jacobi_sweep_v(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed), ptr(self.adj_ptr),
+                                 ptr(self.adj), self.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0,
+                                 self.sweep_variant, s)
         self._swap_y()
         if it == 0:
             sx.sx_batched_obstacle_broadphase(
@@ -280,7 +283,8 @@ class BatchedSolver:
             self._forward_eager(n_substeps)
             return
         key = (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
-               self.stiffness_bending, self.n_iter, self.bending_on, self.tol, self.tol_relative, self.check_every,
+               self.stiffness_bending, self.n_iter, self.bending_on, self.sweep_variant, self.tol, self.tol_relative,
+               self.check_every,
                id(self.warm) if self.warm is not None else None,
                self.warm.mode if self.warm is not None else None, self.y4.data_ptr())
         gr = self._graphs.get(key)
@@ -302,6 +306,17 @@ class BatchedSolver:
             self.graph_kernel_launches = lib.sx_kernel_launches() - n0
             self._graphs[key] = gr
         gr.replay()
+
+    def autotune(self):
+        """Solver.autotune for the concatenated instances."""
+        from .autotune import tune_sweep
+
+        dt = self.dt / 10
+        best, times = tune_sweep(self.x4, self.y4, self.fixed, self.adj_ptr, self.adj, self.num_verts,
+                                 self.stiffness_bending * dt * dt, self.stiffness_stretch * dt * dt,
+                                 1 if self.bending_on == "y" else 0)
+        self.sweep_variant = best
+        return best, times
 
     def constraint_residual(self, positions: str = "x", out=None):
         """Solver.constraint_residual over every instance's constraints."""

@@ -124,8 +124,11 @@ inline int tile_grid(K kernel, int n_verts) {
 // One vertex per thread.  Entries are taken two at a time with both adjacency
 // loads and then both neighbour loads issued before the arithmetic, which keeps
 // several independent gathers in flight per thread.
-template <bool CHECK>
-__global__ void __launch_bounds__(SW_BLOCK) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
+// G: entries whose loads are issued together; BLOCK: threads (= vertices) per
+// tile.  Every (G, BLOCK) gives the same result; the residual partials of
+// CHECK assume BLOCK == SW_BLOCK.
+template <bool CHECK, int G = 2, int BLOCK = SW_BLOCK>
+__global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
                                                                 const float4* __restrict__ yin,
                                                                 float4* __restrict__ yout,
                                                                 const float* __restrict__ fixed,
@@ -134,10 +137,10 @@ __global__ void __launch_bounds__(SW_BLOCK) jacobi_sweep_kernel(int V, const flo
                                                                 int bend_y, const int* conv, int iter,
                                                                 double* __restrict__ partial) {
     if (iteration_skipped(conv, iter)) return;  // grid-uniform
-    constexpr int G = 2;
-    const int ntiles = (V + SW_BLOCK - 1) / SW_BLOCK;
+    static_assert(!CHECK || BLOCK == SW_BLOCK, "residual partials are per SW_BLOCK tile");
+    const int ntiles = (V + BLOCK - 1) / BLOCK;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    const int v = tile * SW_BLOCK + threadIdx.x;
+    const int v = tile * BLOCK + threadIdx.x;
     float c2 = 0.0f;  // sum of C^2 over this vertex's entries (CHECK)
     if (v < V) {
         const float4 ps = __ldg(yin + v), xs = __ldg(x4 + v);
@@ -190,6 +193,57 @@ __global__ void __launch_bounds__(SW_BLOCK) jacobi_sweep_kernel(int V, const flo
 }
 
 // ---------------------------------------------------------------------------
+// Sewing (solve_sewing_constraints_x, XPBD.py:425-441, + update_dx): zero-rest
+// distance constraints between vertex pairs, C = |y_b - y_a|,
+// n = normalize(y_a - y_b), schur = f_a w_a + f_b w_b, ld = k C / (k schur + 1),
+// dx_a -= f_a w_a ld n, dx_b += f_b w_b ld n.  Gathered per sewn vertex over its
+// partners in ascending pair index (from b's side n flips sign exactly), then
+// y += fixed dx / nc.  Coincident vertices (C = 0) contribute nothing, where
+// the reference's normalize would give NaN.  The reference's call is
+// commented out (XPBD.py:371-372); here it runs after the contact update of
+// every Jacobi iteration, where that comment places it.
+// ---------------------------------------------------------------------------
+__global__ void sewing_gather_kernel(int n_sewn, const int* __restrict__ sewn, const int* __restrict__ sptr,
+                                     const int* __restrict__ partner, const float4* __restrict__ y4,
+                                     const float* __restrict__ fixed, float k, float4* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n_sewn) return;
+    const int v = sewn[i];
+    const float4 ps = y4[v];
+    float dx = 0.0f, dy = 0.0f, dz = 0.0f;
+    const int b = sptr[i], e = sptr[i + 1];
+    for (int j = b; j < e; ++j) {
+        const float4 o = y4[partner[j]];
+        const float ex = ps.x - o.x, ey = ps.y - o.y, ez = ps.z - o.z;
+        const float C = sqrtf((ex * ex + ey * ey) + ez * ez);
+        if (C > 0.0f) {
+            const float inv = 1.0f / C;
+            const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
+            const float ld = (k * C) / (k * (ps.w + o.w) + 1.0f);
+            const float a0 = ps.w * ld;
+            dx = dx - a0 * nx;
+            dy = dy - a0 * ny;
+            dz = dz - a0 * nz;
+        }
+    }
+    float4 r = ps;
+    const float nc = (float)(e - b);
+    if (nc > 0.0f) {
+        const float f = fixed[v];
+        r.x = ps.x + f * (dx / nc);
+        r.y = ps.y + f * (dy / nc);
+        r.z = ps.z + f * (dz / nc);
+    }
+    out[i] = r;
+}
+
+__global__ void sewing_scatter_kernel(int n_sewn, const int* __restrict__ sewn, const float4* __restrict__ out,
+                                      float4* __restrict__ y4) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n_sewn) y4[sewn[i]] = out[i];
+}
+
+// ---------------------------------------------------------------------------
 // compute_velocity + update_x (XPBD.py:341-343, :333-337)
 // ---------------------------------------------------------------------------
 __global__ void velocity_update_kernel(int V, float4* __restrict__ x4, const float4* __restrict__ y4,
@@ -205,6 +259,29 @@ __global__ void velocity_update_kernel(int V, float4* __restrict__ x4, const flo
     v.z = (s * (y.z - x.z)) / dt;
     v.w = 0.0f;
     v4[i] = v;
+    x.x = x.x + dt * v.x;
+    x.y = x.y + dt * v.y;
+    x.z = x.z + dt * v.z;
+    x4[i] = x;
+}
+
+// compute_velocity alone (XPBD.py:341-343) and update_x alone (:333-337), for
+// substeps with the velocity-level contact pass between them; the same
+// arithmetic as velocity_update_kernel.
+__global__ void compute_velocity_kernel(int V, const float4* __restrict__ x4, const float4* __restrict__ y4,
+                                        float4* __restrict__ v4, const float* __restrict__ fixed, float damping,
+                                        float dt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    float4 x = x4[i], y = y4[i];
+    float s = (1.0f - damping) * fixed[i];
+    v4[i] = make_float4((s * (y.x - x.x)) / dt, (s * (y.y - x.y)) / dt, (s * (y.z - x.z)) / dt, 0.0f);
+}
+
+__global__ void update_x_kernel(int V, float4* __restrict__ x4, const float4* __restrict__ v4, float dt) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= V) return;
+    float4 x = x4[i], v = v4[i];
     x.x = x.x + dt * v.x;
     x.y = x.y + dt * v.y;
     x.z = x.z + dt * v.z;
@@ -302,6 +379,62 @@ extern "C" int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out
     return check_launch("jacobi_sweep_kernel");
 }
 
+// Launch configurations of the sweep for the autotuner: (entries per load
+// batch, threads per block).  All give bit-identical results.
+namespace sx {
+struct SweepVariant {
+    int g, block;
+    void (*kern)(int, const float4*, const float4*, float4*, const float*, const int*, const int2*, float, float,
+                 int, const int*, int, double*);
+};
+static const SweepVariant kSweepVariants[] = {
+    {2, 256, jacobi_sweep_kernel<false, 2, 256>}, {1, 256, jacobi_sweep_kernel<false, 1, 256>},
+    {4, 256, jacobi_sweep_kernel<false, 4, 256>}, {2, 128, jacobi_sweep_kernel<false, 2, 128>},
+    {2, 512, jacobi_sweep_kernel<false, 2, 512>}, {4, 128, jacobi_sweep_kernel<false, 4, 128>},
+    {1, 128, jacobi_sweep_kernel<false, 1, 128>}, {3, 256, jacobi_sweep_kernel<false, 3, 256>},
+};
+constexpr int kNumSweepVariants = sizeof(kSweepVariants) / sizeof(kSweepVariants[0]);
+}  // namespace sx
+
+extern "C" int sx_jacobi_sweep_variants(void) { return kNumSweepVariants; }
+
+extern "C" int sx_jacobi_sweep_variant_info(int variant, int* g, int* block) {
+    SX_REQUIRE(variant >= 0 && variant < kNumSweepVariants && g && block, "sx_jacobi_sweep_variant_info: bad variant");
+    *g = kSweepVariants[variant].g;
+    *block = kSweepVariants[variant].block;
+    return SX_OK;
+}
+
+extern "C" int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                                 const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
+                                 int bend_on_y, int variant, void* stream) {
+    SX_REQUIRE(n_verts >= 0, "sx_jacobi_sweep_v: n_verts < 0");
+    SX_REQUIRE(variant >= 0 && variant < kNumSweepVariants, "sx_jacobi_sweep_v: bad variant");
+    if (n_verts == 0) return SX_OK;
+    SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj, "sx_jacobi_sweep_v: null pointer");
+    SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_v: y_in4 and y_out4 must not alias");
+    const SweepVariant& sv = kSweepVariants[variant];
+    launch(sv.kern, grid_for(n_verts, sv.block), sv.block, 0, as_stream(stream), n_verts, (const float4*)x4,
+           (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring, k_bend,
+           bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr);
+    return check_launch("jacobi_sweep_kernel");
+}
+
+extern "C" int sx_sewing_sweep(float* y4, const float* fixed, int n_sewn, const int* sewn, const int* sptr,
+                               const int* partner, float k, float* scratch4, void* stream) {
+    SX_REQUIRE(n_sewn >= 0, "sx_sewing_sweep: n_sewn < 0");
+    if (n_sewn == 0) return SX_OK;
+    SX_REQUIRE(y4 && fixed && sewn && sptr && partner && scratch4, "sx_sewing_sweep: null pointer");
+    cudaStream_t s = as_stream(stream);
+    launch(sewing_gather_kernel, grid_for(n_sewn, 256), 256, 0, s, n_sewn, sewn, sptr, partner, (const float4*)y4,
+           fixed, k, (float4*)scratch4);
+    int rc = check_launch("sewing_gather_kernel");
+    if (rc) return rc;
+    launch(sewing_scatter_kernel, grid_for(n_sewn, 256), 256, 0, s, n_sewn, sewn, (const float4*)scratch4,
+           (float4*)y4);
+    return check_launch("sewing_scatter_kernel");
+}
+
 extern "C" int sx_velocity_update(float* x4, const float* y4, float* v4, const float* fixed, int n_verts,
                                   float damping, float dt, void* stream) {
     SX_REQUIRE(n_verts >= 0, "sx_velocity_update: n_verts < 0");
@@ -310,6 +443,25 @@ extern "C" int sx_velocity_update(float* x4, const float* y4, float* v4, const f
     launch(velocity_update_kernel, grid_for(n_verts, 256), 256, 0, as_stream(stream), 
         n_verts, (float4*)x4, (const float4*)y4, (float4*)v4, fixed, damping, dt);
     return check_launch("velocity_update_kernel");
+}
+
+extern "C" int sx_compute_velocity(const float* x4, const float* y4, float* v4, const float* fixed, int n_verts,
+                                   float damping, float dt, void* stream) {
+    SX_REQUIRE(n_verts >= 0, "sx_compute_velocity: n_verts < 0");
+    if (n_verts == 0) return SX_OK;
+    SX_REQUIRE(x4 && y4 && v4 && fixed, "sx_compute_velocity: null pointer");
+    launch(compute_velocity_kernel, grid_for(n_verts, 256), 256, 0, as_stream(stream), n_verts, (const float4*)x4,
+           (const float4*)y4, (float4*)v4, fixed, damping, dt);
+    return check_launch("compute_velocity_kernel");
+}
+
+extern "C" int sx_update_x(float* x4, const float* v4, int n_verts, float dt, void* stream) {
+    SX_REQUIRE(n_verts >= 0, "sx_update_x: n_verts < 0");
+    if (n_verts == 0) return SX_OK;
+    SX_REQUIRE(x4 && v4, "sx_update_x: null pointer");
+    launch(update_x_kernel, grid_for(n_verts, 256), 256, 0, as_stream(stream), n_verts, (float4*)x4,
+           (const float4*)v4, dt);
+    return check_launch("update_x_kernel");
 }
 
 extern "C" int sx_face_aabbs(const float* p4, const int* faces, int n_faces, float padding, float* aabb_min4,

@@ -720,6 +720,258 @@ __global__ void __launch_bounds__(256) batched_contacts_kernel(
     if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
 }
 
+// ---------------------------------------------------------------------------
+// Velocity-level contact and friction (solve_constraints_v, XPBD.py:374-381
+// and :398-404; collision_constraints_v.py __vt_st :6-133, __tv_st :137-330,
+// __vt_dy :334-570), over the pair records of the last position-level contact
+// sweep (pair, g, schur).  For a record with Cv = sum g_k . v_k < 0: a normal
+// velocity impulse, then a tangential one towards the feature's (weighted)
+// velocity, scaled by mu unless mu |Cv| > cTan.  Each `dv += ...` pairs with
+// `nc += 1`; dv is accumulated in fixed point (order independent) and applied
+// as v += fixed * dv / nc where m_inv > 0 (update_dv).  Written in the
+// reference's evaluation order, including its quirks: __vt_st region 3 scales
+// the normal impulse by the static mesh's m_inv indexed by the dynamic vertex
+// id (0 where that id is past the static mesh), region 5 reverses the
+// tangential direction; __tv_st's Cv weights v2 with g3; __vt_dy region 1
+// scales the second vertex's tangential impulse by m_inv of v1.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ V3 vmul(V3 a, float s) { return V3{a.x * s, a.y * s, a.z * s}; }  // (v * s)
+__device__ __forceinline__ float vnorm(V3 a) { return sqrtf(dot(a, a)); }
+
+struct VelCtx {
+    const float4* v4;
+    const float4* vs4;
+    const float* fixed;
+    const float* m_inv;
+    const float* m_inv_st;
+    int Vs;
+    long long* dv;
+    int* nc;
+    int* bad;
+};
+__device__ __forceinline__ V3 vel(const VelCtx& c, int v) { return mk(c.v4[v]); }
+__device__ __forceinline__ V3 vel_st(const VelCtx& c, int v) { return mk(c.vs4[v]); }
+__device__ __forceinline__ void dv_add(const VelCtx& c, int v, V3 d) {
+    acc_add(c.dv, c.nc, v, 1.0f, d, c.bad);  // 1.0f * d is exact
+}
+
+// static triangle (v1..v3) vs dynamic vertex v0 (collision_constraints_v.py:6-133)
+__device__ void vel_vt_st(const VelCtx& c, int v0, int v1, int v2, int v3, int dtype, const V3 g[4], float schur,
+                          float mu) {
+    const V3 u0 = vel(c, v0), u1 = vel_st(c, v1), u2 = vel_st(c, v2), u3 = vel_st(c, v3);
+    const float Cv = ((dot(g[0], u0) + dot(g[1], u1)) + dot(g[2], u2)) + dot(g[3], u3);
+    if (!(Cv < 0.0f) || dtype < 0 || dtype > 6) return;
+    const float ld_v = -Cv / schur;
+    const float m0 = c.m_inv[v0];
+    const float mn = dtype == 3 ? (v0 < c.Vs ? c.m_inv_st[v0] : 0.0f) : m0;
+    dv_add(c, v0, scale(mn * ld_v, g[0]));
+    const V3 vTan0 = add(u0, scale(m0 * ld_v, g[0]));
+    V3 p;
+    if (dtype <= 2) {
+        p = dtype == 0 ? u1 : dtype == 1 ? u2 : u3;
+    } else if (dtype == 6) {
+        const float a = vnorm(g[1]), b = vnorm(g[2]), d = vnorm(g[3]);
+        const float s = (a + b) + d;
+        p = V3{((a * u1.x + b * u2.x) + d * u3.x) / s, ((a * u1.y + b * u2.y) + d * u3.y) / s,
+               ((a * u1.z + b * u2.z) + d * u3.z) / s};
+    } else {
+        const V3 ua = dtype == 4 ? u2 : u1, ub = dtype == 3 ? u2 : u3;
+        const float a = vnorm(dtype == 4 ? g[2] : g[1]), b = vnorm(dtype == 3 ? g[2] : g[3]);
+        const float s = a + b;
+        p = V3{(a * ua.x + b * ub.x) / s, (a * ua.y + b * ub.y) / s, (a * ua.z + b * ub.z) / s};
+    }
+    const V3 g0Tan = dtype == 5 ? sub(vTan0, p) : sub(p, vTan0);
+    const float cTan = 0.5f * dot(g0Tan, g0Tan);
+    const float sT = m0 * dot(g0Tan, g0Tan) + 1e-4f;
+    const float ldTan = cTan / sT;
+    const V3 dvTan = scale(m0 * ldTan, g0Tan);
+    const float mu_e = mu * fabsf(Cv) > cTan ? 1.0f : mu;
+    dv_add(c, v0, scale(mu_e, dvTan));
+}
+
+// static vertex v0 vs dynamic triangle (v1..v3) (collision_constraints_v.py:137-330)
+__device__ void vel_tv_st(const VelCtx& c, int v0, const int vt[3], int dtype, const V3 g[4], float schur,
+                          float mu) {
+    const V3 w0 = vel_st(c, v0);
+    const V3 u[3] = {vel(c, vt[0]), vel(c, vt[1]), vel(c, vt[2])};
+    const float Cv = ((dot(g[0], w0) + dot(g[1], u[0])) + dot(g[3], u[1])) + dot(g[3], u[2]);
+    if (!(Cv < 0.0f) || dtype < 0 || dtype > 6) return;
+    const float ld_v = -Cv / schur;
+    // participating triangle corners (index into vt/u, gradient index = k + 1)
+    int ks[3], n;
+    if (dtype <= 2) { ks[0] = dtype; n = 1; }
+    else if (dtype == 3) { ks[0] = 0; ks[1] = 1; n = 2; }
+    else if (dtype == 4) { ks[0] = 1; ks[1] = 2; n = 2; }
+    else if (dtype == 5) { ks[0] = 0; ks[1] = 2; n = 2; }
+    else { ks[0] = 0; ks[1] = 1; ks[2] = 2; n = 3; }
+    V3 vTan[3];
+    float m[3];
+    for (int i = 0; i < n; ++i) {
+        const int k = ks[i], vid = vt[k];
+        const float fm = c.fixed[vid] * c.m_inv[vid];
+        m[i] = c.m_inv[vid];
+        dv_add(c, vid, scale(fm * ld_v, g[k + 1]));
+        vTan[i] = add(u[k], vmul(scale(fm, g[k + 1]), ld_v));
+    }
+    if (n == 1) {
+        const V3 gT = sub(w0, vTan[0]);
+        const float cTan = 0.5f * dot(gT, gT);
+        const float sT = m[0] * dot(gT, gT) + 1e-4f;
+        const float ldTan = cTan / sT;
+        const float mu_e = mu * fabsf(Cv) > cTan ? 1.0f : mu;
+        dv_add(c, vt[ks[0]], scale(mu_e, scale(m[0] * ldTan, gT)));
+        return;
+    }
+    float w[3], s;
+    V3 p;
+    if (n == 2) {
+        w[0] = vnorm(g[ks[0] + 1]);
+        w[1] = vnorm(g[ks[1] + 1]);
+        s = w[0] + w[1];
+        p = V3{(w[0] * vTan[0].x + w[1] * vTan[1].x) / s, (w[0] * vTan[0].y + w[1] * vTan[1].y) / s,
+               (w[0] * vTan[0].z + w[1] * vTan[1].z) / s};
+    } else {
+        w[0] = vnorm(g[1]);
+        w[1] = vnorm(g[2]);
+        w[2] = vnorm(g[3]);
+        s = (w[0] + w[1]) + w[2];
+        p = V3{((w[0] * vTan[0].x + w[1] * vTan[1].x) + w[2] * vTan[2].x) / s,
+               ((w[0] * vTan[0].y + w[1] * vTan[1].y) + w[2] * vTan[2].y) / s,
+               ((w[0] * vTan[0].z + w[1] * vTan[1].z) + w[2] * vTan[2].z) / s};
+    }
+    const V3 d = sub(w0, p);
+    V3 gT[3];
+    float sT = 0.0f;
+    for (int i = 0; i < n; ++i) {
+        gT[i] = scale(w[i] / s, d);
+        const float t = m[i] * dot(gT[i], gT[i]);
+        sT = i == 0 ? t : sT + t;
+    }
+    const float cTan = 0.5f * dot(d, d);
+    sT = sT + 1e-4f;
+    const float ldTan = cTan / sT;
+    const float mu_e = mu * fabsf(Cv) > cTan ? 1.0f : mu;
+    for (int i = 0; i < n; ++i) dv_add(c, vt[ks[i]], scale(mu_e, scale(m[i] * ldTan, gT[i])));
+}
+
+// self contact, all dynamic (collision_constraints_v.py:334-570)
+__device__ void vel_vt_dy(const VelCtx& c, const int vv[4], int dtype, const V3 g[4], float schur, float mu) {
+    const V3 u[4] = {vel(c, vv[0]), vel(c, vv[1]), vel(c, vv[2]), vel(c, vv[3])};
+    const float Cv = ((dot(g[0], u[0]) + dot(g[1], u[1])) + dot(g[2], u[2])) + dot(g[3], u[3]);
+    if (!(Cv < 0.0f) || dtype < 0 || dtype > 6) return;
+    const float ld_v = -Cv / schur;
+    // participants: the query vertex and the feature's corners (gradient index)
+    int ks[4], n;
+    ks[0] = 0;
+    if (dtype <= 2) { ks[1] = dtype + 1; n = 2; }
+    else if (dtype == 3) { ks[1] = 1; ks[2] = 2; n = 3; }
+    else if (dtype == 4) { ks[1] = 2; ks[2] = 3; n = 3; }
+    else if (dtype == 5) { ks[1] = 1; ks[2] = 3; n = 3; }
+    else { ks[1] = 1; ks[2] = 2; ks[3] = 3; n = 4; }
+    V3 vTan[4];
+    for (int i = 0; i < n; ++i) {
+        const int k = ks[i], vid = vv[k];
+        const float fm = c.fixed[vid] * c.m_inv[vid];
+        dv_add(c, vid, vmul(scale(fm, g[k]), ld_v));
+        vTan[i] = add(u[k], vmul(scale(fm, g[k]), ld_v));
+    }
+    V3 gT[4];
+    float cTan, sT;
+    if (n == 2) {
+        gT[0] = neg(sub(vTan[0], vTan[1]));
+        gT[1] = sub(vTan[0], vTan[1]);
+        cTan = 0.5f * (dot(gT[1], gT[1]) + dot(gT[0], gT[0]));
+        sT = (c.m_inv[vv[0]] * dot(gT[0], gT[0]) + c.m_inv[vv[ks[1]]] * dot(gT[1], gT[1])) + 1e-4f;
+    } else {
+        float w[3], s;
+        V3 p;
+        if (n == 3) {
+            w[0] = vnorm(g[ks[1]]);
+            w[1] = vnorm(g[ks[2]]);
+            s = w[0] + w[1];
+            p = V3{(w[0] * vTan[1].x + w[1] * vTan[2].x) / s, (w[0] * vTan[1].y + w[1] * vTan[2].y) / s,
+                   (w[0] * vTan[1].z + w[1] * vTan[2].z) / s};
+        } else {
+            w[0] = vnorm(g[1]);
+            w[1] = vnorm(g[2]);
+            w[2] = vnorm(g[3]);
+            s = (w[0] + w[1]) + w[2];
+            p = V3{((w[0] * vTan[1].x + w[1] * vTan[2].x) + w[2] * vTan[3].x) / s,
+                   ((w[0] * vTan[1].y + w[1] * vTan[2].y) + w[2] * vTan[3].y) / s,
+                   ((w[0] * vTan[1].z + w[1] * vTan[2].z) + w[2] * vTan[3].z) / s};
+        }
+        gT[0] = sub(p, vTan[0]);
+        for (int i = 1; i < n; ++i) gT[i] = scale(-(w[i - 1] / s), gT[0]);
+        cTan = dot(gT[0], gT[0]);
+        sT = c.m_inv[vv[0]] * dot(gT[0], gT[0]);
+        for (int i = 1; i < n; ++i) {
+            cTan = cTan + dot(gT[i], gT[i]);
+            sT = sT + c.m_inv[vv[ks[i]]] * dot(gT[i], gT[i]);
+        }
+        cTan = 0.5f * cTan;
+        sT = sT + 1e-4f;
+    }
+    const float ldTan = cTan / sT;
+    const float mu_e = mu * fabsf(Cv) > cTan ? 1.0f : mu;
+    for (int i = 0; i < n; ++i) {
+        // region 1 scales the second vertex's impulse by m_inv of v1 (collision_constraints_v.py:410)
+        const int mv = (dtype == 1 && i == 1) ? vv[1] : vv[ks[i]];
+        dv_add(c, vv[ks[i]], scale(mu_e, scale(c.m_inv[mv] * ldTan, gT[i])));
+    }
+}
+
+__global__ void __launch_bounds__(128) velocity_contact_kernel(
+    int Vd, int Vs, const int* __restrict__ faces_dy, const int* __restrict__ faces_st, int cap,
+    const int* __restrict__ pair, const float4* __restrict__ pair_g, const float* __restrict__ pair_schur,
+    const int* __restrict__ pair_num, const float4* __restrict__ v4, const float4* __restrict__ vs4,
+    const float* __restrict__ fixed, const float* __restrict__ m_inv, const float* __restrict__ m_inv_st, float mu,
+    long long* dv, int* nc, int* status) {
+    const int q = blockIdx.x * blockDim.x + threadIdx.x;
+    if (q >= 2 * Vd + Vs) return;
+    int bad = 0;
+    const VelCtx c{v4, vs4, fixed, m_inv, m_inv_st, Vs, dv, nc, &bad};
+    const int n = min(pair_num[q], cap);
+    for (int j = 0; j < n; ++j) {
+        const size_t o = (size_t)q * cap + j;
+        const int face = pair[2 * o], dtype = pair[2 * o + 1];
+        const V3 g[4] = {mk(pair_g[4 * o]), mk(pair_g[4 * o + 1]), mk(pair_g[4 * o + 2]), mk(pair_g[4 * o + 3])};
+        const float sc = pair_schur[o];
+        if (q < Vd) {
+            vel_vt_st(c, q, faces_st[3 * face], faces_st[3 * face + 1], faces_st[3 * face + 2], dtype, g, sc, mu);
+        } else if (q < 2 * Vd) {
+            const int vv[4] = {q - Vd, faces_dy[3 * face], faces_dy[3 * face + 1], faces_dy[3 * face + 2]};
+            vel_vt_dy(c, vv, dtype, g, sc, mu);
+        } else {
+            const int vt[3] = {faces_dy[3 * face], faces_dy[3 * face + 1], faces_dy[3 * face + 2]};
+            vel_tv_st(c, q - 2 * Vd, vt, dtype, g, sc, mu);
+        }
+    }
+    if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
+}
+
+// update_dv (XPBD.py:398-404): v += fixed * dv / nc where m_inv > 0; clears dv, nc
+__global__ void velocity_apply_kernel(int V, float4* __restrict__ v4, const float* __restrict__ fixed,
+                                      const float* __restrict__ m_inv, long long* __restrict__ dv,
+                                      int* __restrict__ nc) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V) return;
+    const int cnt = nc[v];
+    if (cnt > 0) {
+        if (m_inv[v] > 0.0f) {
+            const float cf = (float)cnt, f = fixed[v];
+            float4 u = v4[v];
+            u.x = u.x + f * (from_fix(dv[3 * v]) / cf);
+            u.y = u.y + f * (from_fix(dv[3 * v + 1]) / cf);
+            u.z = u.z + f * (from_fix(dv[3 * v + 2]) / cf);
+            v4[v] = u;
+        }
+        dv[3 * v] = 0;
+        dv[3 * v + 1] = 0;
+        dv[3 * v + 2] = 0;
+        nc[v] = 0;
+    }
+}
+
 }  // namespace sx
 
 using namespace sx;
@@ -886,4 +1138,24 @@ extern "C" int sx_batched_obstacle_contacts(int n_verts, float* y4, const float*
            256, 0, s, n_verts, (float4*)y4, fixed, dx_fix, nc, conv,
            iter);
     return check_launch("collision_apply_kernel");
+}
+
+extern "C" int sx_velocity_contacts(int n_dy, int n_st, const int* faces_dy, const int* faces_st, int cap,
+                                    const int* pair, const float* pair_g, const float* pair_schur,
+                                    const int* pair_num, float* v4, const float* vs4, const float* fixed,
+                                    const float* m_inv, const float* m_inv_st, float mu, long long* dv_fix, int* nc,
+                                    int* status, void* stream) {
+    SX_REQUIRE(n_dy >= 0 && n_st >= 0 && cap >= 1, "sx_velocity_contacts: bad sizes");
+    if (n_dy == 0) return SX_OK;
+    SX_REQUIRE(faces_dy && pair && pair_g && pair_schur && pair_num && v4 && fixed && m_inv && dv_fix && nc && status,
+               "sx_velocity_contacts: null pointer");
+    SX_REQUIRE(n_st == 0 || (faces_st && vs4 && m_inv_st), "sx_velocity_contacts: null static pointer");
+    cudaStream_t s = as_stream(stream);
+    launch(velocity_contact_kernel, grid_for(2LL * n_dy + n_st, 128), 128, 0, s, n_dy, n_st, faces_dy, faces_st, cap,
+           pair, (const float4*)pair_g, pair_schur, pair_num, (const float4*)v4, (const float4*)vs4, fixed, m_inv,
+           m_inv_st, mu, dv_fix, nc, status);
+    int rc = check_launch("velocity_contact_kernel");
+    if (rc) return rc;
+    launch(velocity_apply_kernel, grid_for(n_dy, 256), 256, 0, s, n_dy, (float4*)v4, fixed, m_inv, dv_fix, nc);
+    return check_launch("velocity_apply_kernel");
 }

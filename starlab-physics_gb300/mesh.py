@@ -354,3 +354,22 @@ class TriMesh:
     def bbox_diagonal(self) -> float:
         p = self.x0_np.astype(np.float64)
         return float(np.linalg.norm(p.max(0) - p.min(0)))
+
+
+def sewing_adjacency(n_verts: int, pairs: np.ndarray):
+    """Sewn vertices and their partners for sx_sewing_sweep: sewn[i] has
+    partners partner[sptr[i]:sptr[i+1]] in ascending pair index (a pair (a, b)
+    lists b at a and a at b)."""
+    pairs = np.asarray(pairs, dtype=np.int64).reshape(-1, 2)
+    if pairs.size and (pairs.min() < 0 or pairs.max() >= n_verts):
+        raise ValueError("sewing pair vertex out of range")
+    P = pairs.shape[0]
+    owner = np.concatenate([pairs[:, 0], pairs[:, 1]])
+    other = np.concatenate([pairs[:, 1], pairs[:, 0]])
+    pid = np.concatenate([np.arange(P), np.arange(P)])
+    order = np.lexsort((pid, owner))
+    owner, other = owner[order], other[order]
+    sewn, counts = np.unique(owner, return_counts=True)
+    sptr = np.zeros(sewn.shape[0] + 1, dtype=np.int32)
+    sptr[1:] = np.cumsum(counts)
+    return sewn.astype(np.int32), sptr, other.astype(np.int32)

@@ -34,6 +34,10 @@ Options beyond the reference (keyword-only, defaults reproduce the reference):
   remaining ones are skipped on the device, inside the captured graph, with no
   host synchronisation.  Needs ``bending_on="y"`` and the pair-list contacts.
   :meth:`convergence_stats` reads the counters.
+* ``set_sewing_pairs(pairs, stiffness)`` -- zero-rest distance constraints
+  between vertex pairs (``solve_sewing_constraints_x``, XPBD.py:425-441,
+  commented out at XPBD.py:371-372 in the reference), solved after the contact
+  update of every Jacobi iteration with k = stiffness * dt^2.
 * ``contact_cull`` (attribute, default on) -- the pair-list contact sweep skips
   a pair whose point-to-triangle-box squared distance exceeds ``dHat * 1.0625``
   before classifying its region.  The distance of every region is at least the
@@ -50,6 +54,7 @@ from __future__ import annotations
 
 import ctypes as C
 
+import numpy as np
 import torch
 
 from ._lib import load, ptr, stream_handle, sx
@@ -85,6 +90,9 @@ class Solver:
         # when collisions are on
         self.self_collision = True
         self.contact_cull = True
+        self._sewing = None  # (sewn, sptr, partner, scratch, stiffness)
+        # launch configuration of the fixed-count sweep (autotune() picks one)
+        self.sweep_variant = 0
 
         self.max_num_verts_dy = mesh_dy.num_verts
         self.max_num_edges_dy = mesh_dy.num_edges
@@ -166,8 +174,9 @@ class Solver:
         k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
         k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
         if self.tol is None:
-            sx.sx_jacobi_sweep(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj),
-                               m.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0, stream_handle())
+            sx.sx_jacobi_sweep_v(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj),
+                                 m.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0, self.sweep_variant,
+                                 stream_handle())
         else:
             check = 1 if iteration > 0 and iteration % self.check_every == 0 else 0
             sx.sx_jacobi_sweep_checked(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
@@ -269,6 +278,31 @@ class Solver:
                 if not self.record_pairs:
                     self.build_contact_pairs()
             self.solve_collision_constraints_x(iteration=iteration, gated=not in_loop)
+        self.solve_sewing_constraints_x(dt)
+
+    def set_sewing_pairs(self, pairs, stiffness: float):
+        """Sew vertex pairs (an int array [P, 2]); None or an empty array removes
+        the sewing."""
+        from .mesh import sewing_adjacency
+
+        if pairs is None or len(pairs) == 0:
+            self._sewing = None
+            self._graphs.clear()
+            return
+        sewn, sptr, partner = sewing_adjacency(self.mesh_dy.num_verts, np.asarray(pairs))
+        t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(self.device)  # noqa: E731
+        self._sewing = (t(sewn), t(sptr), t(partner),
+                        torch.zeros((sewn.shape[0], 4), dtype=torch.float32, device=self.device), float(stiffness))
+        self._graphs.clear()
+
+    def solve_sewing_constraints_x(self, dt):
+        """XPBD.py:425-441 followed by update_dx (no-op without sewing pairs)."""
+        if self._sewing is None:
+            return
+        sewn, sptr, partner, scratch, stiff = self._sewing
+        m = self.mesh_dy
+        sx.sx_sewing_sweep(ptr(m.y4), ptr(m.fixed), sewn.shape[0], ptr(sewn), ptr(sptr), ptr(partner),
+                           stiff * dt * dt, ptr(scratch), stream_handle())
 
     def compute_velocity_update_x(self, dt):
         """compute_velocity (XPBD.py:341-343) then update_x (XPBD.py:333-337)."""
@@ -327,7 +361,21 @@ class Solver:
 
     CULL_MARGIN = 1.0625
 
+    def autotune(self):
+        """Time every launch configuration of the sweep on this mesh and keep
+        the fastest (identical results).  Returns (variant, times in ms)."""
+        from .autotune import tune_sweep
+
+        m = self.mesh_dy
+        dt = self.dt / 10
+        best, times = tune_sweep(m.x4, m.y4, m.fixed, m.adj_ptr, m.adj, m.num_verts, self.stiffness_bending * dt * dt,
+                                 self.stiffness_stretch * dt * dt, 1 if self.bending_on == "y" else 0)
+        self.sweep_variant = best
+        return best, times
+
     def _check_tol_mode(self):
+        if self._sewing is not None:
+            raise ValueError("iterating to a tolerance does not support sewing pairs")
         if self.bending_on != "y":
             raise ValueError("iterating to a tolerance needs bending_on='y'")
         if self.record_pairs:
@@ -362,7 +410,8 @@ class Solver:
     def _graph_key(self, n_substeps):
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
-                self.compliance_collision, self.self_collision, self.contact_cull, self.tol, self.tol_relative,
+                self.compliance_collision, self.self_collision, self.contact_cull, self.sweep_variant, self.tol,
+                self.tol_relative,
                 self.check_every,
                 self.mesh_dy.y4.data_ptr())
 

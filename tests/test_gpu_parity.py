@@ -81,6 +81,33 @@ def test_predict_sweep_velocity_bit_exact(pkg, po, sxm):
     assert np.array_equal(_np(Vv)[:, :3], vo[:, :3])
 
 
+def test_sweep_variants_and_autotune(pkg, po, sxm):
+    """Every launch configuration of the sweep gives the oracle's result bit for
+    bit, and the autotuner picks one of them."""
+    sc, m = _cloth(pkg)
+    rng = np.random.default_rng(5)
+    x4, v4 = _state(m, rng)
+    fixed, m_inv = _np(m.fixed), _np(m.m_inv)
+    dt = 1.0 / 600.0
+    ks, kb = 1e8 * dt * dt, 1e5 * dt * dt
+    y = po.predict(x4, v4, fixed, dt, (0.0, 0.0, -9.81))
+    yo = y.copy()
+    po.spring_sweep(x4, yo, fixed, m_inv, m.eid_np, m.l0_np, m.bending_np, m.bending_l0_np, ks, kb, bend_on_y=1)
+    X, Yin, Yout = _t(x4), _t(y), torch.empty_like(m.x4)
+    s = torch.cuda.current_stream().cuda_stream
+    n_var = int(sxm.load().sx_jacobi_sweep_variants())
+    assert n_var >= 4
+    for v in range(n_var):
+        Yout.fill_(float("nan"))
+        sxm.sx.sx_jacobi_sweep_v(X.data_ptr(), Yin.data_ptr(), Yout.data_ptr(), m.fixed.data_ptr(),
+                                 m.adj_ptr.data_ptr(), m.adj.data_ptr(), m.num_verts, ks, kb, 1, v, s)
+        assert np.array_equal(_np(Yout)[:, :3], yo[:, :3]), v
+    from starlab_physics_gb300 import autotune
+
+    best, times = autotune.tune_sweep(X, Yin, m.fixed, m.adj_ptr, m.adj, m.num_verts, ks, kb, 1, reps=5, rounds=3)
+    assert 0 <= best < n_var and len(times) == n_var and min(times) > 0
+
+
 def test_aabbs(pkg, po, sxm):
     sc, m = _cloth(pkg, n=20)
     x4 = _np(m.x4)
@@ -444,3 +471,31 @@ def test_tolerance_mode_extremes(pkg, po):
     assert np.array_equal(_np(g_big.mesh_dy.x4), _np(fixed_sim.mesh_dy.x4))
     g0, _ = _tol_run(pkg, po, tol=0.0, frames=2, use_graph=True)
     assert np.array_equal(_np(g0.mesh_dy.x4), _np(full.mesh_dy.x4))
+
+
+def test_sewing_matches_oracle(pkg, po):
+    """Sewing constraints (two edges of a cloth sewn together) through the
+    solver, against the oracle, bit for bit; the sewn vertices approach."""
+    scene = pkg.scenes.plain64(n=16, seed=5, collisions=False)
+    scene.n_iter = 4
+    sim = pkg.scenes.make_solver(scene, device=DEV)
+    sim.bending_on = "y"
+    n = 16
+    pairs = np.array([[i, (n - 1) * n + i] for i in range(2, n - 2)], np.int32)  # first row to last row
+    sim.set_sewing_pairs(pairs, 1e5)
+    sewn, sptr, partner = pkg.mesh.sewing_adjacency(sim.mesh_dy.num_verts, pairs)
+    orc = po.OracleSolver(pkg.scenes.oracle_inputs(sim.mesh_dy), None, dt=scene.dt, g=scene.gravity,
+                          k_stretch_stiffness=scene.stiffness_stretch, k_bend_stiffness=scene.stiffness_bending,
+                          dHat=scene.dHat, damping=scene.damping, padding=scene.padding, n_iter=scene.n_iter,
+                          collisions=False, rebuild=scene.rebuild, cap=scene.cap, bending_on="y",
+                          sewing=(sewn, sptr, partner, 1e5))
+    x0 = _np(sim.mesh_dy.x4).copy()
+    for _ in range(3):
+        sim.forward(scene.n_substeps)
+        orc.forward(scene.n_substeps)
+    torch.cuda.synchronize()
+    gx = _np(sim.mesh_dy.x4)
+    assert np.array_equal(gx[:, :3], orc.x4[:, :3])
+    d0 = np.linalg.norm(x0[pairs[:, 0], :3] - x0[pairs[:, 1], :3], axis=1)
+    d1 = np.linalg.norm(gx[pairs[:, 0], :3] - gx[pairs[:, 1], :3], axis=1)
+    assert np.all(d1 < d0)

@@ -217,3 +217,84 @@ def test_adam_step_matches_reference(pkg, po):
     P["b3"][3:] = 0
     ref = np.concatenate([P[k].ravel() for k, _ in po.MLP_SHAPES])
     assert np.allclose(got, ref, rtol=1e-5, atol=1e-7)
+
+
+def _small_batch(pkg, seed, n_inst=96):
+    insts = pkg.batched_scene(n_inst, seed=seed, n_min=16, n_max=64)
+    return pkg.BatchedSolver(insts, dHat=(4e-3) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8,
+                             g=(0.0, 0.0, -9.81), dt=1.0 / 60.0, n_iter=20, padding=8e-3)
+
+
+@pytest.fixture(scope="module")
+def trained(pkg):
+    """A network trained on samples of the plain solver (seed-0 scene, 80
+    iterations per substep), with its loss history and held-out samples of
+    another scene."""
+    if not torch.cuda.is_available():
+        pytest.skip("needs a GPU")
+    L = pkg.learned
+    A = _small_batch(pkg, 0)
+    A.forward(10)
+    A.n_iter = 80
+    feat, tgt = L.collect_samples(A, frames=3, rows_per_substep=32768)
+    B = _small_batch(pkg, 1)
+    B.forward(10)
+    B.n_iter = 80
+    vf, vt = L.collect_samples(B, frames=1, rows_per_substep=16384, seed=3)
+    mlp = pkg.WarmStartMLP(seed=0)
+    before = L.evaluate_loss(mlp, vf, vt)
+    h1 = L.train(mlp, feat, tgt, 1500, batch=16384, lr=2e-3)
+    h2 = L.train(mlp, feat, tgt, 500, batch=16384, lr=5e-4)
+    return mlp, np.concatenate([h1, h2]), before, vf, vt
+
+
+@pytest.mark.gpu
+def test_training_reduces_loss(pkg, trained):
+    """Training on solver-generated samples lowers the loss on the training
+    samples and on held-out samples from another scene, below the loss of
+    predicting no correction."""
+    L = pkg.learned
+    mlp, hist, before, vf, vt = trained
+    after = L.evaluate_loss(mlp, vf, vt)
+    zero = float(vt[:, :3].pow(2).sum(1).mean().item())
+    assert np.all(np.isfinite(hist))
+    assert hist[-50:].mean() < 0.1 * hist[:10].mean()
+    assert after < 0.1 * before
+    assert after < 0.8 * zero, (after, zero)
+
+
+@pytest.mark.gpu
+def test_warm_start_gain(pkg, trained):
+    """What the trained network gains: on a held-out scene, from the same
+    state, the learned warm start reaches the plain solver's tolerance in fewer
+    Jacobi iterations (device-side loop in a captured frame)."""
+    L = pkg.learned
+    mlp = trained[0]
+    B = _small_batch(pkg, 1)
+    rec = L.WarmStart(B, mode="record")
+    B.warm = rec
+    B.forward(10)
+    B.warm = None
+    snap = (B.x4.clone(), B.v4.clone(), rec.c4.clone())
+    # tolerance: the largest residual the plain solver reaches after 40 iterations per substep
+    B.tol, B.n_iter, B.check_every = 0.0, 44, 4
+    res = []
+    for _ in range(10):
+        B.substep(B.dt / 10)
+        res.append(float(B._res3[2].item()))
+    tol = max(res)
+    stops = {}
+    for mode in ("plain", "learned"):
+        B.x4.copy_(snap[0])
+        B.v4.copy_(snap[1])
+        B.tol, B.n_iter, B.use_graph = tol, 200, True
+        B.warm = L.WarmStart(B, mlp) if mode == "learned" else None
+        if B.warm is not None:
+            B.warm.c4.copy_(snap[2])
+        B.convergence_stats(reset=True)
+        B.forward(10)
+        st = B.convergence_stats()
+        assert st["converged_substeps"] == 10, (mode, st)
+        stops[mode] = st["mean_stop_iteration"]
+    B.warm = None
+    assert stops["learned"] < 0.8 * stops["plain"], stops
