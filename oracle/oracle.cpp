@@ -1086,6 +1086,217 @@ API int or_sewing_step(int n_sewn, const int32_t* sewn, const int32_t* sptr, con
     return 0;
 }
 
+// solve_constraints_v (XPBD.py:374-381, :398-404) over the pair records:
+// collision_constraints_v.py __vt_st (:6-133), __tv_st (:137-330) and __vt_dy
+// (:334-570), branch by branch in the reference's own expression order
+// (scalar products evaluated left to right: f*m*ld*g = ((f*m)*ld)*g,
+// f*m*g*ld = ((f*m)*g)*ld), each `dv += ...` with its `nc += 1`, fixed-point
+// accumulation, then update_dv.  Quirks kept: __vt_st region 3 scales the
+// normal impulse by the static mesh's m_inv at the dynamic vertex's id (0 past
+// the static mesh), region 5 reverses the tangent; __tv_st's Cv uses g3 for v2;
+// __vt_dy region 1 scales v2's tangential impulse by m_inv of v1.
+namespace {
+struct VelAcc {
+    int64_t* dv;
+    int32_t* nc;
+    int* bad;
+    void add(int v, V3 d) {
+        dv[3 * v] += to_fix(d.x, bad);
+        dv[3 * v + 1] += to_fix(d.y, bad);
+        dv[3 * v + 2] += to_fix(d.z, bad);
+        nc[v] += 1;
+    }
+};
+inline V3 load3(const float* p) { return V3{p[0], p[1], p[2]}; }
+inline V3 mulv(V3 a, float s) { return V3{a.x * s, a.y * s, a.z * s}; }
+inline float norm3(V3 a) { return std::sqrt(dot(a, a)); }
+inline V3 divs(V3 a, float s) { return V3{a.x / s, a.y / s, a.z / s}; }
+inline V3 wsum2(float a, V3 p, float b, V3 q) { return V3{a * p.x + b * q.x, a * p.y + b * q.y, a * p.z + b * q.z}; }
+inline V3 wsum3(float a, V3 p, float b, V3 q, float c, V3 r) {
+    return V3{(a * p.x + b * q.x) + c * r.x, (a * p.y + b * q.y) + c * r.y, (a * p.z + b * q.z) + c * r.z};
+}
+inline float mu_eff(float mu, float Cv, float cTan) { return mu * std::fabs(Cv) > cTan ? 1.0f : mu; }
+
+void or_vt_st_v(VelAcc& A, int v0, int v1, int v2, int v3, int dtype, const V3* g, float schur, float mu,
+                const float* v4, const float* vs4, const float* m_inv, const float* m_inv_st, int Vs) {
+    V3 u0 = load3(v4 + 4 * v0), s1 = load3(vs4 + 4 * v1), s2 = load3(vs4 + 4 * v2), s3 = load3(vs4 + 4 * v3);
+    float Cv = ((dot(g[0], u0) + dot(g[1], s1)) + dot(g[2], s2)) + dot(g[3], s3);
+    if (!(Cv < 0.0f) || dtype < 0 || dtype > 6) return;
+    float ld_v = -Cv / schur;
+    float m0 = m_inv[v0];
+    float mn = dtype == 3 ? (v0 < Vs ? m_inv_st[v0] : 0.0f) : m0;
+    A.add(v0, scale(mn * ld_v, g[0]));
+    V3 vTan0 = add(u0, scale(m0 * ld_v, g[0]));
+    V3 g0Tan;
+    if (dtype == 0) g0Tan = sub(s1, vTan0);
+    else if (dtype == 1) g0Tan = sub(s2, vTan0);
+    else if (dtype == 2) g0Tan = sub(s3, vTan0);
+    else if (dtype == 3) { float a = norm3(g[1]), b = norm3(g[2]); g0Tan = sub(divs(wsum2(a, s1, b, s2), a + b), vTan0); }
+    else if (dtype == 4) { float a = norm3(g[2]), b = norm3(g[3]); g0Tan = sub(divs(wsum2(a, s2, b, s3), a + b), vTan0); }
+    else if (dtype == 5) { float a = norm3(g[1]), b = norm3(g[3]); g0Tan = sub(vTan0, divs(wsum2(a, s1, b, s3), a + b)); }
+    else {
+        float a = norm3(g[1]), b = norm3(g[2]), c = norm3(g[3]);
+        g0Tan = sub(divs(wsum3(a, s1, b, s2, c, s3), (a + b) + c), vTan0);
+    }
+    float cTan = 0.5f * dot(g0Tan, g0Tan);
+    float sT = m0 * dot(g0Tan, g0Tan) + 1e-4f;
+    float ldTan = cTan / sT;
+    V3 dvTan = scale(m0 * ldTan, g0Tan);
+    A.add(v0, scale(mu_eff(mu, Cv, cTan), dvTan));
+}
+
+void or_tv_st_v(VelAcc& A, int v0, int v1, int v2, int v3, int dtype, const V3* g, float schur, float mu,
+                const float* v4, const float* vs4, const float* fixed, const float* m_inv) {
+    V3 w0 = load3(vs4 + 4 * v0), u1 = load3(v4 + 4 * v1), u2 = load3(v4 + 4 * v2), u3 = load3(v4 + 4 * v3);
+    float Cv = ((dot(g[0], w0) + dot(g[1], u1)) + dot(g[3], u2)) + dot(g[3], u3);
+    if (!(Cv < 0.0f) || dtype < 0 || dtype > 6) return;
+    float ld_v = -Cv / schur;
+    int vid[3] = {v1, v2, v3};
+    V3 uu[3] = {u1, u2, u3};
+    auto impulse = [&](int k) {  // dv[vk] += f m ld g_k ; returns vTan_k = v_k + f m g_k ld
+        float fm = fixed[vid[k]] * m_inv[vid[k]];
+        A.add(vid[k], scale(fm * ld_v, g[k + 1]));
+        return add(uu[k], mulv(scale(fm, g[k + 1]), ld_v));
+    };
+    if (dtype <= 2) {
+        int k = dtype;
+        V3 vT = impulse(k);
+        V3 gT = sub(w0, vT);
+        float cTan = 0.5f * dot(gT, gT);
+        float sT = m_inv[vid[k]] * dot(gT, gT) + 1e-4f;
+        float ldTan = cTan / sT;
+        V3 dvT = scale(m_inv[vid[k]] * ldTan, gT);
+        A.add(vid[k], scale(mu_eff(mu, Cv, cTan), dvT));
+    } else if (dtype <= 5) {
+        int i = dtype == 4 ? 1 : 0, j = dtype == 3 ? 1 : 2;
+        V3 vTi = impulse(i), vTj = impulse(j);
+        float a = norm3(g[i + 1]), b = norm3(g[j + 1]);
+        float ab = a + b;
+        V3 p = divs(wsum2(a, vTi, b, vTj), dtype == 3 ? (a + b) : ab);
+        V3 d = sub(w0, p);
+        V3 giT = scale(a / ab, d), gjT = scale(b / ab, d);
+        float cTan = 0.5f * dot(d, d);
+        float sT = (m_inv[vid[i]] * dot(giT, giT) + m_inv[vid[j]] * dot(gjT, gjT)) + 1e-4f;
+        float ldTan = cTan / sT;
+        V3 dvi = scale(m_inv[vid[i]] * ldTan, giT), dvj = scale(m_inv[vid[j]] * ldTan, gjT);
+        float me = mu_eff(mu, Cv, cTan);
+        A.add(vid[i], scale(me, dvi));
+        A.add(vid[j], scale(me, dvj));
+    } else {
+        V3 vT1 = impulse(0), vT2 = impulse(1), vT3 = impulse(2);
+        float a = norm3(g[1]), b = norm3(g[2]), c = norm3(g[3]);
+        float abc = (a + b) + c;
+        V3 p = divs(wsum3(a, vT1, b, vT2, c, vT3), abc);
+        V3 d = sub(w0, p);
+        V3 g1T = scale(a / abc, d), g2T = scale(b / abc, d), g3T = scale(c / abc, d);
+        float cTan = 0.5f * dot(d, d);
+        float sT = ((m_inv[v1] * dot(g1T, g1T) + m_inv[v2] * dot(g2T, g2T)) + m_inv[v3] * dot(g3T, g3T)) + 1e-4f;
+        float ldTan = cTan / sT;
+        float me = mu_eff(mu, Cv, cTan);
+        A.add(v1, scale(me, scale(m_inv[v1] * ldTan, g1T)));
+        A.add(v2, scale(me, scale(m_inv[v2] * ldTan, g2T)));
+        A.add(v3, scale(me, scale(m_inv[v3] * ldTan, g3T)));
+    }
+}
+
+void or_vt_dy_v(VelAcc& A, const int* vv, int dtype, const V3* g, float schur, float mu, const float* v4,
+                const float* fixed, const float* m_inv) {
+    V3 u[4];
+    for (int k = 0; k < 4; ++k) u[k] = load3(v4 + 4 * vv[k]);
+    float Cv = ((dot(g[0], u[0]) + dot(g[1], u[1])) + dot(g[2], u[2])) + dot(g[3], u[3]);
+    if (!(Cv < 0.0f) || dtype < 0 || dtype > 6) return;
+    float ld_v = -Cv / schur;
+    auto impulse = [&](int k) {  // dv[vk] += f m g_k ld ; returns vTan_k = v_k + f m g_k ld
+        float fm = fixed[vv[k]] * m_inv[vv[k]];
+        A.add(vv[k], mulv(scale(fm, g[k]), ld_v));
+        return add(u[k], mulv(scale(fm, g[k]), ld_v));
+    };
+    if (dtype <= 2) {
+        int k = dtype + 1;
+        V3 vT0 = impulse(0), vTk = impulse(k);
+        V3 g0T = neg(sub(vT0, vTk)), gkT = sub(vT0, vTk);
+        float cTan = 0.5f * (dot(gkT, gkT) + dot(g0T, g0T));
+        float sT = (m_inv[vv[0]] * dot(g0T, g0T) + m_inv[vv[k]] * dot(gkT, gkT)) + 1e-4f;
+        float ldTan = cTan / sT;
+        V3 dv0 = scale(m_inv[vv[0]] * ldTan, g0T);
+        V3 dvk = scale(m_inv[dtype == 1 ? vv[1] : vv[k]] * ldTan, gkT);
+        float me = mu_eff(mu, Cv, cTan);
+        A.add(vv[0], scale(me, dv0));
+        A.add(vv[k], scale(me, dvk));
+    } else if (dtype <= 5) {
+        int i = dtype == 4 ? 2 : 1, j = dtype == 3 ? 2 : 3;
+        V3 vT0 = impulse(0), vTi = impulse(i), vTj = impulse(j);
+        float a = norm3(g[i]), b = norm3(g[j]);
+        float ab = a + b;
+        V3 p = divs(wsum2(a, vTi, b, vTj), ab);
+        V3 g0T = sub(p, vT0);
+        V3 giT = scale(-(a / ab), g0T), gjT = scale(-(b / ab), g0T);
+        float cTan = 0.5f * ((dot(g0T, g0T) + dot(giT, giT)) + dot(gjT, gjT));
+        float sT = ((m_inv[vv[0]] * dot(g0T, g0T) + m_inv[vv[i]] * dot(giT, giT)) + m_inv[vv[j]] * dot(gjT, gjT)) +
+                   1e-4f;
+        float ldTan = cTan / sT;
+        float me = mu_eff(mu, Cv, cTan);
+        A.add(vv[0], scale(me, scale(m_inv[vv[0]] * ldTan, g0T)));
+        A.add(vv[i], scale(me, scale(m_inv[vv[i]] * ldTan, giT)));
+        A.add(vv[j], scale(me, scale(m_inv[vv[j]] * ldTan, gjT)));
+    } else {
+        V3 vT0 = impulse(0), vT1 = impulse(1), vT2 = impulse(2), vT3 = impulse(3);
+        float a = norm3(g[1]), b = norm3(g[2]), c = norm3(g[3]);
+        float abc = (a + b) + c;
+        V3 p = divs(wsum3(a, vT1, b, vT2, c, vT3), abc);
+        V3 g0T = sub(p, vT0);
+        V3 g1T = scale(-(a / abc), g0T), g2T = scale(-(b / abc), g0T), g3T = scale(-(c / abc), g0T);
+        float cTan = 0.5f * (((dot(g0T, g0T) + dot(g1T, g1T)) + dot(g2T, g2T)) + dot(g3T, g3T));
+        float sT = (((m_inv[vv[0]] * dot(g0T, g0T) + m_inv[vv[1]] * dot(g1T, g1T)) + m_inv[vv[2]] * dot(g2T, g2T)) +
+                    m_inv[vv[3]] * dot(g3T, g3T)) + 1e-4f;
+        float ldTan = cTan / sT;
+        float me = mu_eff(mu, Cv, cTan);
+        A.add(vv[0], scale(me, scale(m_inv[vv[0]] * ldTan, g0T)));
+        A.add(vv[1], scale(me, scale(m_inv[vv[1]] * ldTan, g1T)));
+        A.add(vv[2], scale(me, scale(m_inv[vv[2]] * ldTan, g2T)));
+        A.add(vv[3], scale(me, scale(m_inv[vv[3]] * ldTan, g3T)));
+    }
+}
+}  // namespace
+
+API int or_velocity_contacts(int Vd, int Vs, const int32_t* faces_dy, const int32_t* faces_st, int cap,
+                             const int32_t* pair, const float* pair_g, const float* pair_schur,
+                             const int32_t* pair_num, float* v4, const float* vs4, const float* fixed,
+                             const float* m_inv, const float* m_inv_st, float mu, int32_t* status) {
+    std::vector<int64_t> dv(3 * (size_t)Vd, 0);
+    std::vector<int32_t> nc((size_t)Vd, 0);
+    int bad = 0;
+    VelAcc A{dv.data(), nc.data(), &bad};
+    for (int q = 0; q < 2 * Vd + Vs; ++q) {
+        int n = std::min(pair_num[q], cap);
+        for (int j = 0; j < n; ++j) {
+            size_t o = (size_t)q * cap + j;
+            int face = pair[2 * o], dtype = pair[2 * o + 1];
+            V3 g[4];
+            for (int k = 0; k < 4; ++k) g[k] = v3(pair_g + 16 * o + 4 * k);
+            float sc = pair_schur[o];
+            if (q < Vd) {
+                or_vt_st_v(A, q, faces_st[3 * face], faces_st[3 * face + 1], faces_st[3 * face + 2], dtype, g, sc, mu,
+                           v4, vs4, m_inv, m_inv_st, Vs);
+            } else if (q < 2 * Vd) {
+                int vv[4] = {q - Vd, faces_dy[3 * face], faces_dy[3 * face + 1], faces_dy[3 * face + 2]};
+                or_vt_dy_v(A, vv, dtype, g, sc, mu, v4, fixed, m_inv);
+            } else {
+                or_tv_st_v(A, q - 2 * Vd, faces_dy[3 * face], faces_dy[3 * face + 1], faces_dy[3 * face + 2], dtype, g,
+                           sc, mu, v4, vs4, fixed, m_inv);
+            }
+        }
+    }
+    for (int v = 0; v < Vd; ++v) {  // update_dv (XPBD.py:398-404)
+        if (nc[v] > 0 && m_inv[v] > 0.0f) {
+            float c = (float)nc[v];
+            for (int k = 0; k < 3; ++k) v4[4 * v + k] = v4[4 * v + k] + fixed[v] * (from_fix(dv[3 * v + k]) / c);
+        }
+    }
+    if (bad && status) *status |= 4;
+    return 0;
+}
+
 // The region classifier, distance and gradient for one point-triangle query
 // (used by tests: known-answer and finite-difference checks).
 API int or_point_triangle(const float* p12, float* d_out, float* g12) {

@@ -42,6 +42,7 @@ _SIGS = {
     "or_face_bvh_traverse": [I, I, P, P, P, P, P, P, P, I, P, P, P],
     "or_residual": [I, P, P, P, P],
     "or_sewing_step": [I, P, P, P, P, P, F],
+    "or_velocity_contacts": [I, I, P, P, I, P, P, P, P, P, P, P, P, P, F, P],
     "or_warm_features": [I, P, P, P, P, P, P, P, F, F, F, F, P],
     "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I],
     "or_point_triangle": [P, P, P],
@@ -294,6 +295,21 @@ def adjacency(n_verts, edges, l0, bend, bl0):
     return ptr, adj
 
 
+def velocity_contacts(faces_dy, faces_st, cap, rec, v4, vs4, fixed, m_inv, m_inv_st, mu):
+    """solve_constraints_v over pair records rec (the dict collision_sweep
+    returns with want_pairs); updates v4 in place."""
+    Vd = v4.shape[0]
+    Vs = vs4.shape[0] if vs4 is not None else 0
+    fs = i32(faces_st) if faces_st is not None else np.zeros(3, np.int32)
+    vs = vs4 if vs4 is not None else np.zeros((1, 4), np.float32)
+    ms = f32(m_inv_st) if m_inv_st is not None else np.zeros(1, np.float32)
+    status = np.zeros(1, np.int32)
+    lib().or_velocity_contacts(Vd, Vs, _p(i32(faces_dy)), _p(fs), cap, _p(rec["pair"]), _p(rec["pair_g"]),
+                               _p(rec["pair_schur"]), _p(rec["pair_num"]), _p(v4), _p(vs), _p(f32(fixed)),
+                               _p(f32(m_inv)), _p(ms), float(mu), _p(status))
+    return int(status[0])
+
+
 def sewing_step(y4, fixed, sewn, sptr, partner, k):
     """Sewing constraints + update_dx on y4 (in place)."""
     lib().or_sewing_step(int(len(sewn)), _p(i32(sewn)), _p(i32(sptr)), _p(i32(partner)), _p(y4), _p(f32(fixed)),
@@ -460,7 +476,8 @@ class OracleSolver:
     def __init__(self, mesh_dy, mesh_st=None, *, dt, g, k_stretch_stiffness, k_bend_stiffness, dHat=4e-3,
                  damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
                  compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True,
-                 contact_cull=False, tol=None, check_every=4, tol_relative=False, sewing=None):
+                 contact_cull=False, tol=None, check_every=4, tol_relative=False, sewing=None,
+                 velocity_update=False, mu=0.8):
         self.d = mesh_dy
         # iterate to a residual (the CUDA solver's tol mode): every
         # check_every-th iteration measures the residual of the current y; once
@@ -470,6 +487,10 @@ class OracleSolver:
         self.tol_relative = tol_relative
         # sewing: (sewn, sptr, partner, stiffness) -- k = stiffness * dt^2 per iteration
         self.sewing = sewing
+        # velocity-level contact + friction pass after compute_velocity (XPBD.py:467-468)
+        self.velocity_update = velocity_update
+        self.mu = mu
+        self._records = None
         self.check_every = check_every
         self.checks = 0
         self.stop_sum = 0
@@ -573,12 +594,27 @@ class OracleSolver:
                 r = collision_sweep(self.faces, self.faces_st if self.s is not None else None, y4,
                                     self.xs4 if self.s is not None else None, self.fixed, self.m_inv, self.dHat,
                                     self.compliance, self.cap, vt_st[:2], vt_dy[:2], tv_st[:2],
-                                    nthreads=self.nthreads, cull_d2=self.cull_d2)
+                                    nthreads=self.nthreads, cull_d2=self.cull_d2,
+                                    want_pairs=self.velocity_update)
                 self.last_status |= r["status"]
+                if self.velocity_update:
+                    self._records = r
             if self.sewing is not None:
                 sewn, sptr, partner, stiff = self.sewing
                 sewing_step(y4, self.fixed, sewn, sptr, partner, float(stiff) * dt_sub * dt_sub)
-        velocity_update(self.x4, y4, self.v4, self.fixed, self.damping, dt_sub, self.nthreads)
+        if self.velocity_update and self._records is not None:
+            # compute_velocity, solve_constraints_v, update_x (XPBD.py:465-469), float32 as the kernels
+            dtf = np.float32(dt_sub)
+            s_ = (np.float32(1.0) - np.float32(self.damping)) * self.fixed
+            self.v4[:, :3] = (s_[:, None] * (y4[:, :3] - self.x4[:, :3])) / dtf
+            self.v4[:, 3] = 0
+            vs4 = np.zeros_like(self.xs4) if self.s is not None else None
+            self.last_status |= velocity_contacts(self.faces, self.faces_st if self.s is not None else None,
+                                                  self.cap, self._records, self.v4, vs4, self.fixed, self.m_inv,
+                                                  f32(self.s["m_inv"]) if self.s is not None else None, self.mu)
+            self.x4[:, :3] = self.x4[:, :3] + dtf * self.v4[:, :3]
+        else:
+            velocity_update(self.x4, y4, self.v4, self.fixed, self.damping, dt_sub, self.nthreads)
         self.y4 = y4
 
     def forward(self, n_substeps):

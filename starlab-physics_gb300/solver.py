@@ -310,6 +310,20 @@ class Solver:
         sx.sx_velocity_update(ptr(m.x4), ptr(m.y4), ptr(m.v4), ptr(m.fixed), m.num_verts, self.damping, float(dt),
                               stream_handle())
 
+    def solve_constraints_v(self):
+        """solve_constraints_v (XPBD.py:374-381): velocity-level contact and
+        friction (mu) over the pair records of the last contact sweep, then
+        update_dv.  Needs the records: ``record_pairs=True``."""
+        if not self.record_pairs:
+            raise ValueError("the velocity-level contact pass reads pair records: construct with record_pairs=True")
+        m, s = self.mesh_dy, self.mesh_st
+        sx.sx_velocity_contacts(m.num_verts, s.num_verts if s is not None else 0, ptr(m.face_indices),
+                                ptr(s.face_indices) if s is not None else None, self.cache_size, ptr(self.pair),
+                                ptr(self.pair_g), ptr(self.pair_schur), ptr(self.pair_num), ptr(m.v4),
+                                ptr(s.v4) if s is not None else None, ptr(m.fixed), ptr(m.m_inv),
+                                ptr(s.m_inv) if s is not None else None, float(self.mu), ptr(self._dx_fix),
+                                ptr(self._nc), ptr(self.status), stream_handle())
+
     def substep(self, dt_sub):
         if self.enable_collision_handling and self.rebuild == "substep":
             self.build_bvhs()
@@ -339,9 +353,15 @@ class Solver:
         else:
             for it in range(self.n_iter):
                 self.solve_constraints_jacobi_x(dt_sub, first_iteration=(it == 0), iteration=it)
-        if self.enable_velocity_update:
-            raise NotImplementedError("the velocity-level contact pass is not part of this build")
-        self.compute_velocity_update_x(dt_sub)
+        if self.enable_velocity_update and self.enable_collision_handling:
+            # compute_velocity, solve_constraints_v, update_x (XPBD.py:465-469)
+            m = self.mesh_dy
+            sx.sx_compute_velocity(ptr(m.x4), ptr(m.y4), ptr(m.v4), ptr(m.fixed), m.num_verts, self.damping,
+                                   float(dt_sub), stream_handle())
+            self.solve_constraints_v()
+            sx.sx_update_x(ptr(m.x4), ptr(m.v4), m.num_verts, float(dt_sub), stream_handle())
+        else:
+            self.compute_velocity_update_x(dt_sub)
 
     def forward(self, n_substeps: int):
         """``Solver.forward`` (XPBD.py:443-469).
@@ -410,7 +430,8 @@ class Solver:
     def _graph_key(self, n_substeps):
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
-                self.compliance_collision, self.self_collision, self.contact_cull, self.sweep_variant, self.tol,
+                self.compliance_collision, self.self_collision, self.contact_cull, self.sweep_variant,
+                self.enable_velocity_update, self.mu, self.tol,
                 self.tol_relative,
                 self.check_every,
                 self.mesh_dy.y4.data_ptr())

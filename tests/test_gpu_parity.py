@@ -499,3 +499,88 @@ def test_sewing_matches_oracle(pkg, po):
     d0 = np.linalg.norm(x0[pairs[:, 0], :3] - x0[pairs[:, 1], :3], axis=1)
     d1 = np.linalg.norm(gx[pairs[:, 0], :3] - gx[pairs[:, 1], :3], axis=1)
     assert np.all(d1 < d0)
+
+
+def test_velocity_contacts_all_branches(pkg, po, sxm):
+    """solve_constraints_v over synthetic pair records that exercise every
+    region of every kind (random g, schur, velocities; half the records with
+    Cv < 0): the kernel equals the oracle's branch-by-branch restatement."""
+    rng = np.random.default_rng(21)
+    Vd, Vs, cap = 300, 120, 6
+    faces_dy = rng.integers(0, Vd, (200, 3)).astype(np.int32)
+    faces_st = rng.integers(0, Vs, (80, 3)).astype(np.int32)
+    Q = 2 * Vd + Vs
+    num = rng.integers(0, cap + 1, Q).astype(np.int32)
+    pair = np.zeros((Q, cap, 2), np.int32)
+    pair[:Vd, :, 0] = rng.integers(0, 80, (Vd, cap))
+    pair[Vd:, :, 0] = rng.integers(0, 200, (Vd + Vs, cap))
+    pair[:, :, 1] = rng.integers(0, 7, (Q, cap))
+    g = np.zeros((Q, cap, 4, 4), np.float32)
+    g[..., :3] = rng.normal(0, 1, (Q, cap, 4, 3))
+    schur = rng.uniform(0.5, 3.0, (Q, cap)).astype(np.float32)
+    v4 = np.zeros((Vd, 4), np.float32)
+    v4[:, :3] = rng.normal(0, 1, (Vd, 3))
+    vs4 = np.zeros((Vs, 4), np.float32)
+    vs4[:, :3] = rng.normal(0, 0.3, (Vs, 3))
+    fixed = (rng.uniform(size=Vd) > 0.1).astype(np.float32)
+    m_inv = rng.uniform(0.5, 2.0, Vd).astype(np.float32)
+    m_inv[:5] = 0.0
+    m_inv_st = rng.uniform(0.5, 2.0, Vs).astype(np.float32)
+    rec = {"pair": pair, "pair_g": g, "pair_schur": schur, "pair_num": num}
+    ref = v4.copy()
+    po.velocity_contacts(faces_dy, faces_st, cap, rec, ref, vs4, fixed, m_inv, m_inv_st, 0.3)
+    t = {k: _t(np.ascontiguousarray(a)) for k, a in
+         dict(fd=faces_dy, fs=faces_st, pair=pair, g=g, schur=schur, num=num, v=v4, vs=vs4, fixed=fixed,
+              m=m_inv, ms=m_inv_st).items()}
+    dv = torch.zeros(3 * Vd, dtype=torch.int64, device=DEV)
+    nc = torch.zeros(Vd, dtype=torch.int32, device=DEV)
+    status = torch.zeros(1, dtype=torch.int32, device=DEV)
+    sxm.sx.sx_velocity_contacts(Vd, Vs, t["fd"].data_ptr(), t["fs"].data_ptr(), cap, t["pair"].data_ptr(),
+                                t["g"].data_ptr(), t["schur"].data_ptr(), t["num"].data_ptr(), t["v"].data_ptr(),
+                                t["vs"].data_ptr(), t["fixed"].data_ptr(), t["m"].data_ptr(), t["ms"].data_ptr(), 0.3,
+                                dv.data_ptr(), nc.data_ptr(), status.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    got = _np(t["v"])
+    assert not np.array_equal(ref, v4)
+    assert np.array_equal(got[:, :3], ref[:, :3]), np.abs(got - ref).max()
+    assert not _np(dv).any() and not _np(nc).any()
+
+
+def test_velocity_pass_solver_matches_oracle(pkg, po):
+    """enable_velocity_update through the solver (contacts on a box, pair
+    records kept), against the oracle, bit for bit."""
+    scene = pkg.scenes.plain64(n=24, seed=7)
+    scene.n_iter = 3
+    from starlab_physics_gb300 import mesh as M
+
+    cl = M.TriMesh(scene.cloth_x, scene.cloth_faces, device=DEV)
+    ob = M.TriMesh(scene.obstacle_x, scene.obstacle_faces, device=DEV, is_static=True)
+    sim = pkg.Solver(cl, ob, dHat=scene.dHat, stiffness_stretch=scene.stiffness_stretch,
+                     stiffness_bending=scene.stiffness_bending, g=scene.gravity, dt=scene.dt, n_iter=scene.n_iter,
+                     rebuild=scene.rebuild, record_pairs=True, bending_on="y")
+    mask = np.zeros(cl.num_verts, np.int32)
+    mask[scene.pinned] = 1
+    sim.set_fixed_vertices(torch.from_numpy(mask))
+    sim.damping = scene.damping
+    sim.padding = scene.padding
+    sim.enable_collision_handling = True
+    sim.enable_velocity_update = True
+    sim.mu = 0.4
+    orc = po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob), dt=scene.dt, g=scene.gravity,
+                          k_stretch_stiffness=scene.stiffness_stretch, k_bend_stiffness=scene.stiffness_bending,
+                          dHat=scene.dHat, damping=scene.damping, padding=scene.padding, n_iter=scene.n_iter,
+                          collisions=True, rebuild=scene.rebuild, cap=scene.cap, bending_on="y", contact_cull=False,
+                          velocity_update=True, mu=0.4)
+    plain = po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob), dt=scene.dt,
+                            g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
+                            k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
+                            padding=scene.padding, n_iter=scene.n_iter, collisions=True, rebuild=scene.rebuild,
+                            cap=scene.cap, bending_on="y", contact_cull=False)
+    for _ in range(30):
+        sim.forward(scene.n_substeps)
+        orc.forward(scene.n_substeps)
+        plain.forward(scene.n_substeps)
+    torch.cuda.synchronize()
+    assert int(_np(sim.pair_num).sum()) > 0, "no contact records"
+    assert not np.array_equal(orc.x4, plain.x4), "the velocity pass changed nothing"
+    assert np.array_equal(_np(cl.x4)[:, :3], orc.x4[:, :3])
+    assert np.array_equal(_np(cl.v4)[:, :3], orc.v4[:, :3])
