@@ -396,22 +396,47 @@ __global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int
 // same leaf and face tests produces the same candidate list in the same order,
 // with independent loads instead of a chain of dependent node fetches.
 __device__ __forceinline__ void cell_range(float qa, float qb, float o, float c, float e, int* i0, int* i1) {
-    // one extra cell on each side absorbs rounding in the divisions
-    const float f0 = floorf((qa - e - o) / c) - 1.0f, f1 = floorf((qb + e - o) / c) + 1.0f;
+    // A leaf box lies within [o + c i - e, o + c (i + 1) + e] up to the
+    // rounding of those bounds (relative 2^-24 of |o| + 64 c and of e); the
+    // divisions below carry relative 2^-22 of (|q| + e + |o|) / c.  delta covers
+    // both 64 times over, so a cell is left out only when no leaf box in it
+    // can reach the query box.  A zero or non-finite cell size gives the full
+    // range.
+    const float delta = 1.5e-5f * ((fabsf(qa) + fabsf(qb) + 2.0f * e + 2.0f * fabsf(o) + 64.0f * c) / c);
+    const float f0 = ceilf((qa - e - o) / c - 1.0f - delta), f1 = floorf((qb + e - o) / c + delta);
     *i0 = (int)fmaxf(f0, 0.0f);
     *i1 = (int)fminf(f1, (float)(kGridRes - 1));
 }
 
 // One warp per query.  The warp walks the (x, y) columns of the query's cell
-// range in descending order and, in each column, the occupied cells in
-// descending z.  A cell's leaf box is tested once (a broadcast load); then the
-// lanes test the cell's faces 32 at a time in sorted order and a ballot places
-// each overlapping face after those of lower lanes, so candidates come out in
-// descending cell order and, within a cell, in sorted face order -- the
-// reference's visiting order -- with every lane busy on the face records.
+// range in descending order.  In each column, lane l takes cell z = 31 - l, so
+// that ascending lanes are the reference's descending-z visiting order: the
+// occupied cells' leaf boxes are tested at once, a warp scan lays the faces of
+// the cells that pass end to end in that order, and the lanes test those faces
+// 32 at a time (each lane finds its cell by a binary search over the scan).  A
+// ballot places each overlapping face after those of lower lanes, so
+// candidates come out in descending cell order and, within a cell, in sorted
+// face order -- the reference's visiting order -- with every lane busy.
 constexpr int CT_BLOCK = 256;
 
-__global__ void __launch_bounds__(CT_BLOCK) cell_traverse_kernel(
+__device__ __forceinline__ int warp_incl_scan(int v, int lane) {
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int o = __shfl_up_sync(0xffffffffu, v, d);
+        if (lane >= d) v += o;
+    }
+    return v;
+}
+// lowest lane whose inclusive count exceeds k (31 when none does)
+__device__ __forceinline__ int warp_owner(int incl, int k) {
+    int lo = 0;
+#pragma unroll
+    for (int step = 16; step >= 1; step >>= 1)
+        if (__shfl_sync(0xffffffffu, incl, lo + step - 1) <= k) lo += step;
+    return lo;
+}
+
+__global__ void __launch_bounds__(CT_BLOCK, 4) cell_traverse_kernel(
     int Q, const float4* __restrict__ p4, float pad, const float* __restrict__ grid8, const float* __restrict__ box6,
     const float4* __restrict__ nmin4, const float4* __restrict__ nmax4, const int* __restrict__ prefix,
     const float4* __restrict__ frec, int cap, int* __restrict__ cand, int* __restrict__ num, int* status) {
@@ -438,33 +463,62 @@ __global__ void __launch_bounds__(CT_BLOCK) cell_traverse_kernel(
         cell_range(a.x, b.x, org.x, cs.x, grid8[3], &x0, &x1);
         cell_range(a.y, b.y, org.y, cs.y, grid8[4], &y0, &y1);
         cell_range(a.z, b.z, org.z, cs.z, grid8[5], &z0, &z1);
-        if (z0 <= z1) {
+        if (z0 <= z1 && x0 <= x1 && y0 <= y1) {
             const unsigned zmask = (z1 == 31 ? 0xffffffffu : ((1u << (z1 + 1)) - 1u)) & ~((1u << z0) - 1u);
-            for (int cx = x1; cx >= x0; --cx) {
-                for (int cy = y1; cy >= y0; --cy) {
-                    unsigned m = occ[cx * kGridRes + cy] & zmask;
-                    while (m) {  // warp-uniform
-                        const int cz = 31 - __clz(m);
-                        m &= ~(1u << cz);
-                        const int i = cx * kGridRes * kGridRes + cy * kGridRes + cz;
+            const int ny = y1 - y0 + 1, ncol = (x1 - x0 + 1) * ny;
+            // columns in visiting order (x descending, then y descending), 32 at a time
+            for (int c0 = 0; c0 < ncol; c0 += 32) {
+                unsigned cm = 0u;  // this lane's column: occupied cells within the z range
+                if (c0 + lane < ncol) {
+                    const int cc = c0 + lane;
+                    cm = occ[(x1 - cc / ny) * kGridRes + (y1 - cc % ny)] & zmask;
+                }
+                const int cn = __popc(cm);
+                const int cincl = warp_incl_scan(cn, lane);
+                const int ctotal = __shfl_sync(0xffffffffu, cincl, 31);
+                // the occupied cells of these columns end to end (z descending
+                // within a column), 32 at a time: lane k takes the k-th
+                for (int k0 = 0; k0 < ctotal; k0 += 32) {
+                    const int k = k0 + lane;
+                    const int oc = warp_owner(cincl, k);
+                    const unsigned m = __shfl_sync(0xffffffffu, cm, oc);
+                    const int rank = k - (__shfl_sync(0xffffffffu, cincl, oc) - __shfl_sync(0xffffffffu, cn, oc));
+                    int start = 0, n = 0;
+                    if (k < ctotal) {
+                        // position of the rank-th highest set bit of m
+                        int cz = 0;
+#pragma unroll
+                        for (int step = 16; step >= 1; step >>= 1)
+                            if (__popc(m >> (cz + step)) >= rank + 1) cz += step;
+                        const int cc = c0 + oc;
+                        const int i = (x1 - cc / ny) * kGridRes * kGridRes + (y1 - cc % ny) * kGridRes + cz;
                         const int leaf = i + kNumCells - 1;
-                        if (!overlap(a, b, mk(nmin4[leaf]), mk(nmax4[leaf]))) continue;
-                        const int rl = i == 0 ? 0 : prefix[i - 1], re = prefix[i];
-                        for (int j0 = rl; j0 < re; j0 += 32) {
-                            const int j = j0 + lane;
-                            bool hit = false;
-                            float4 fa = make_float4(0.f, 0.f, 0.f, 0.f);
-                            if (j < re) {
-                                fa = frec[2 * j];
-                                hit = overlap(a, b, mk(fa), mk(frec[2 * j + 1]));
-                            }
-                            const unsigned hits = __ballot_sync(0xffffffffu, hit);
-                            if (hit) {
-                                const int slot = count + __popc(hits & ((1u << lane) - 1u));
-                                if (slot < cap) out[slot] = __float_as_int(fa.w);
-                            }
-                            count += __popc(hits);
+                        if (overlap(a, b, mk(nmin4[leaf]), mk(nmax4[leaf]))) {
+                            start = i == 0 ? 0 : prefix[i - 1];
+                            n = prefix[i] - start;
                         }
+                    }
+                    const int incl = warp_incl_scan(n, lane);  // faces of the passing cells, in order
+                    const int total = __shfl_sync(0xffffffffu, incl, 31);
+                    for (int f0 = 0; f0 < total; f0 += 32) {
+                        const int f = f0 + lane;
+                        const int lo = warp_owner(incl, f);
+                        const int o_incl = __shfl_sync(0xffffffffu, incl, lo);
+                        const int o_n = __shfl_sync(0xffffffffu, n, lo);
+                        const int o_start = __shfl_sync(0xffffffffu, start, lo);
+                        bool hit = false;
+                        float4 fa = make_float4(0.f, 0.f, 0.f, 0.f);
+                        if (f < total) {
+                            const int j = o_start + (f - (o_incl - o_n));
+                            fa = frec[2 * j];
+                            hit = overlap(a, b, mk(fa), mk(frec[2 * j + 1]));
+                        }
+                        const unsigned hits = __ballot_sync(0xffffffffu, hit);
+                        if (hit) {
+                            const int slot = count + __popc(hits & ((1u << lane) - 1u));
+                            if (slot < cap) out[slot] = __float_as_int(fa.w);
+                        }
+                        count += __popc(hits);
                     }
                 }
             }

@@ -475,6 +475,12 @@ class Solver:
                                   self._res_ws.numel(), stream_handle())
         return out
 
+    def contact_pair_count(self) -> int:
+        """Pairs in the current contact pair list (host sync): the counts sit in
+        the last 256 bytes of the pair-list workspace, {end of vertex-vs-static
+        pairs, end of vertex-vs-cloth pairs, total}."""
+        return int(self._pairs_ws[-256:].view(torch.int32)[2].item())
+
     def status_flags(self) -> int:
         """Accumulated device status bits (host sync)."""
         return int(self.status.item())
