@@ -306,22 +306,62 @@ __device__ __forceinline__ V3 load_cg(const float4* p) {
 // an internal node computes it from both (finished) children.  Each leaf also
 // writes its faces' records (min.xyz + face id, max.xyz) in sorted order, the
 // contiguous array the traversal scans.
-__global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int* __restrict__ prefix,
-                                       const int* __restrict__ sorted_face_ids, const float4* __restrict__ fmn4,
-                                       const float4* __restrict__ fmx4, const int* __restrict__ child_a,
-                                       const int* __restrict__ child_b, const int* __restrict__ parent,
-                                       int* num_faces, float4* nmin4, float4* nmax4, float4* frec, int* flags,
-                                       int* status, float* grid8) {
-    int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= kNumCells) return;
-    V3 lo{box6[0], box6[1], box6[2]};
-    V3 cs = cell_size_of(box6);
-    const int leaf = i + kNumCells - 1;
+// The cell tree is the perfect tree over the 32768 row-major cells (leaf slot
+// i = cell i, child_a = lower half).  The Karras build numbers an internal
+// node covering the aligned slot range [l, r] of size s >= 2 as 0 for the
+// root, r when it is a left child (l / s even) and l when it is a right child;
+// a leaf is slot + 32767.  The refit therefore needs no climbing: one block
+// per z-column (32 leaves, an aligned subtree) fits its leaves and the
+// subtree's 31 nodes in shared memory, and a second kernel fits the 1023
+// nodes above the columns level by level.
+__device__ __forceinline__ int cell_node_index(int l, int size) {
+    if (size == kNumCells) return 0;
+    if (size == 1) return l + kNumCells - 1;
+    return ((l / size) & 1) == 0 ? l + size - 1 : l;
+}
+
+struct NodeBox {
+    V3 a, b;
+    int n;
+};
+// compute_cell_node_aabbs (lbvh_cell.py:491-522): union of the non-empty
+// children; two empty children give the point at the mean of their corners
+__device__ __forceinline__ NodeBox join_nodes(const NodeBox& l, const NodeBox& r) {
+    NodeBox o;
+    if (l.n > 0 && r.n > 0) {
+        o.a = vmin(l.a, r.a);
+        o.b = vmax(l.b, r.b);
+    } else if (l.n > 0) {
+        o.a = l.a;
+        o.b = l.b;
+    } else if (r.n > 0) {
+        o.a = r.a;
+        o.b = r.b;
+    } else {
+        o.a = scale(0.25f, add(add(add(l.a, l.b), r.a), r.b));
+        o.b = o.a;
+    }
+    o.n = l.n + r.n;
+    return o;
+}
+
+// Block = one z-column (cells col*32 .. col*32+31), warp w = cell col*32 + w.
+__global__ void __launch_bounds__(1024) cell_column_refit_kernel(
+    const float* __restrict__ box6, const int* __restrict__ prefix, const int* __restrict__ sorted_face_ids,
+    const float4* __restrict__ fmn4, const float4* __restrict__ fmx4, int* __restrict__ num_faces,
+    float4* __restrict__ nmin4, float4* __restrict__ nmax4, float4* __restrict__ frec, float* grid8) {
+    __shared__ NodeBox tree[64];  // [32 + k]: leaf k; [16 + k], [8 + k], ...: levels above
+    __shared__ unsigned ext_bits[3];
+    const int col = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int i = col * kGridRes + w;
+    if (threadIdx.x < 3) ext_bits[threadIdx.x] = 0u;
+    const V3 lo{box6[0], box6[1], box6[2]};
+    const V3 cs = cell_size_of(box6);
     const int rl = i == 0 ? 0 : prefix[i - 1];
     const int size = prefix[i] - rl;
-    V3 c = cell_center(i, cs, lo);
+    const V3 c = cell_center(i, cs, lo);
     V3 a = c, b = c;
-    for (int j = 0; j < size; ++j) {
+    for (int j = lane; j < size; j += 32) {
         const int fid = sorted_face_ids[rl + j];
         const float4 fa = fmn4[fid], fb = fmx4[fid];
         a = vmin(a, mk(fa));
@@ -329,55 +369,79 @@ __global__ void cell_leaf_refit_kernel(const float* __restrict__ box6, const int
         frec[2 * (rl + j)] = make_float4(fa.x, fa.y, fa.z, __int_as_float(fid));
         frec[2 * (rl + j) + 1] = make_float4(fb.x, fb.y, fb.z, 0.0f);
     }
-    num_faces[leaf] = size;
-    store_box(nmin4, nmax4, leaf, a, b, size);
-    // How far this leaf's box reaches beyond its cell (>= 0), maximised over the
-    // grid: the traversal scans the cells within that reach of a query box.
-    {
-        const int x0 = i / (kGridRes * kGridRes), y0 = (i % (kGridRes * kGridRes)) / kGridRes, z0 = i % kGridRes;
-        const float clo[3] = {lo.x + cs.x * (float)x0, lo.y + cs.y * (float)y0, lo.z + cs.z * (float)z0};
-        const float chi[3] = {lo.x + cs.x * (float)(x0 + 1), lo.y + cs.y * (float)(y0 + 1),
-                              lo.z + cs.z * (float)(z0 + 1)};
-        const float am[3] = {a.x, a.y, a.z}, bm[3] = {b.x, b.y, b.z};
-        for (int k = 0; k < 3; ++k) {
-            float ext = size > 0 ? fmaxf(fmaxf(clo[k] - am[k], bm[k] - chi[k]), 0.0f) : 0.0f;
-            for (int o = 16; o > 0; o >>= 1) ext = fmaxf(ext, __shfl_xor_sync(0xffffffffu, ext, o));
-            if ((threadIdx.x & 31) == 0 && ext > 0.0f)
-                atomicMax(reinterpret_cast<unsigned*>(grid8) + 3 + k, __float_as_uint(ext));
-        }
-        // occupancy: the 32 cells of a warp are one z-column (x, y fixed, z = 0..31)
-        const unsigned occ = __ballot_sync(0xffffffffu, size > 0);
-        if ((threadIdx.x & 31) == 0) reinterpret_cast<unsigned*>(grid8)[kGridHeader + (i >> 5)] = occ;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a = vmin(a, V3{__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o),
+                       __shfl_xor_sync(0xffffffffu, a.z, o)});
+        b = vmax(b, V3{__shfl_xor_sync(0xffffffffu, b.x, o), __shfl_xor_sync(0xffffffffu, b.y, o),
+                       __shfl_xor_sync(0xffffffffu, b.z, o)});
     }
-    int node = parent[leaf];
-    for (int steps = 0; node >= 0; ++steps) {
-        if (steps > kNumCells) {
-            atomicOr(status, SX_STATUS_CLIMB_LIMIT);
-            return;
+    __syncthreads();  // ext_bits initialised
+    if (lane == 0) {
+        const int leaf = i + kNumCells - 1;
+        num_faces[leaf] = size;
+        store_box(nmin4, nmax4, leaf, a, b, size);
+        tree[32 + w] = NodeBox{a, b, size};
+        // how far this leaf's box reaches beyond its cell (>= 0), maximised
+        // over the grid: the traversal scans the cells within that reach
+        if (size > 0) {
+            const int x0 = i / (kGridRes * kGridRes), y0 = (i % (kGridRes * kGridRes)) / kGridRes, z0 = w;
+            const float clo[3] = {lo.x + cs.x * (float)x0, lo.y + cs.y * (float)y0, lo.z + cs.z * (float)z0};
+            const float chi[3] = {lo.x + cs.x * (float)(x0 + 1), lo.y + cs.y * (float)(y0 + 1),
+                                  lo.z + cs.z * (float)(z0 + 1)};
+            const float am[3] = {a.x, a.y, a.z}, bm[3] = {b.x, b.y, b.z};
+            for (int k = 0; k < 3; ++k) {
+                const float ext = fmaxf(fmaxf(clo[k] - am[k], bm[k] - chi[k]), 0.0f);
+                if (ext > 0.0f) atomicMax(ext_bits + k, __float_as_uint(ext));
+            }
         }
-        __threadfence();
-        if (atomicAdd(flags + node, 1) == 0) return;
-        flags[node] = 0;
-        const int l = child_a[node], r = child_b[node];
-        const int nl = __ldcg(num_faces + l), nr = __ldcg(num_faces + r);
-        V3 min0 = load_cg(nmin4 + l), max0 = load_cg(nmax4 + l), min1 = load_cg(nmin4 + r), max1 = load_cg(nmax4 + r);
-        V3 na, nb;
-        if (nl > 0 && nr > 0) {
-            na = vmin(min0, min1);
-            nb = vmax(max0, max1);
-        } else if (nl > 0) {
-            na = min0;
-            nb = max0;
-        } else if (nr > 0) {
-            na = min1;
-            nb = max1;
-        } else {
-            na = scale(0.25f, add(add(add(min0, max0), min1), max1));
-            nb = na;
+    }
+    __syncthreads();
+    if (w == 0) {
+        // occupancy word of the column, and the column's subtree, level by level
+        const unsigned occ = __ballot_sync(0xffffffffu, tree[32 + lane].n > 0);
+        if (lane == 0) reinterpret_cast<unsigned*>(grid8)[kGridHeader + col] = occ;
+        if (lane < 3 && ext_bits[lane] != 0u) atomicMax(reinterpret_cast<unsigned*>(grid8) + 3 + lane, ext_bits[lane]);
+        for (int half = 16, sz = 2; half >= 1; half >>= 1, sz <<= 1) {
+            if (lane < half) {
+                const NodeBox nb = join_nodes(tree[2 * half + 2 * lane], tree[2 * half + 2 * lane + 1]);
+                tree[half + lane] = nb;
+                const int node = cell_node_index(col * kGridRes + lane * sz, sz);
+                num_faces[node] = nb.n;
+                store_box(nmin4, nmax4, node, nb.a, nb.b, nb.n);
+            }
+            __syncwarp();
         }
-        num_faces[node] = nl + nr;
-        store_box(nmin4, nmax4, node, na, nb, nl + nr);
-        node = parent[node];
+    }
+}
+
+// The 1023 nodes above the columns (sizes 64 .. 32768), one block.
+__global__ void __launch_bounds__(1024) cell_top_refit_kernel(int* __restrict__ num_faces,
+                                                              float4* __restrict__ nmin4,
+                                                              float4* __restrict__ nmax4) {
+    __shared__ float4 sa[kGridRes * kGridRes], sb[kGridRes * kGridRes];
+    const int t = threadIdx.x;
+    {
+        const int node = cell_node_index(t * kGridRes, kGridRes);
+        sa[t] = nmin4[node];
+        sb[t] = nmax4[node];
+    }
+    __syncthreads();
+    for (int half = kGridRes * kGridRes / 2, sz = 2 * kGridRes; half >= 1; half >>= 1, sz <<= 1) {
+        NodeBox nb;
+        if (t < half) {
+            const float4 la = sa[2 * t], lb = sb[2 * t], ra = sa[2 * t + 1], rb = sb[2 * t + 1];
+            nb = join_nodes(NodeBox{mk(la), mk(lb), __float_as_int(la.w)}, NodeBox{mk(ra), mk(rb), __float_as_int(ra.w)});
+            const int node = cell_node_index(t * sz, sz);
+            num_faces[node] = nb.n;
+            store_box(nmin4, nmax4, node, nb.a, nb.b, nb.n);
+        }
+        __syncthreads();
+        if (t < half) {
+            sa[t] = make_float4(nb.a.x, nb.a.y, nb.a.z, __int_as_float(nb.n));
+            sb[t] = make_float4(nb.b.x, nb.b.y, nb.b.z, 0.0f);
+        }
+        __syncthreads();
     }
 }
 
@@ -745,10 +809,7 @@ extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_f
     p += align256((size_t)(n_faces > 0 ? n_faces : 1) * 4);
     void* rws = p;
     p += rs_ws_bytes(n_faces);
-    int* flags = (int*)p;
     SX_CUDA(cudaMemsetAsync(prefix, 0, sizeof(int) * kNumCells, s));
-    SX_CUDA(cudaMemsetAsync(flags, 0, sizeof(int) * kNumCells, s));
-    SX_CUDA(cudaMemsetAsync(grid8 + kGridHeader, 0, sizeof(unsigned) * kGridRes * kGridRes, s));
     launch(face_cell_kernel, grid_for(n_faces, 256), 256, 0, s, n_faces, (const float4*)fmin4, (const float4*)fmax4,
            box6, keys, sorted_face_ids, (unsigned*)prefix, grid8);
     int rc = check_launch("face_cell_kernel");
@@ -758,12 +819,13 @@ extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_f
         rc = radix_sort(keys, sorted_face_ids, n_faces, 15, rws, rs_ws_bytes(n_faces), s);
         if (rc) return rc;
     }
-    // the status word lives in the flags scratch tail (flags[NC-1] is never a node)
-    int* status = flags + (kNumCells - 1);
-    launch(cell_leaf_refit_kernel, grid_for(kNumCells, 256), 256, 0, s, box6, (const int*)prefix,
-           (const int*)sorted_face_ids, (const float4*)fmin4, (const float4*)fmax4, child_a, child_b, parent,
-           num_faces, (float4*)nmin4, (float4*)nmax4, (float4*)face_rec8, flags, status, grid8);
-    return check_launch("cell_leaf_refit_kernel");
+    launch(cell_column_refit_kernel, kGridRes * kGridRes, 1024, 0, s, box6, (const int*)prefix,
+           (const int*)sorted_face_ids, (const float4*)fmin4, (const float4*)fmax4, num_faces, (float4*)nmin4,
+           (float4*)nmax4, (float4*)face_rec8, grid8);
+    rc = check_launch("cell_column_refit_kernel");
+    if (rc) return rc;
+    launch(cell_top_refit_kernel, 1, 1024, 0, s, num_faces, (float4*)nmin4, (float4*)nmax4);
+    return check_launch("cell_top_refit_kernel");
 }
 
 extern "C" int sx_cell_bvh_traverse(const float* p4, int n_queries, float padding, const float* grid8,
