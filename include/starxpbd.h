@@ -191,6 +191,13 @@ int sx_cell_bvh_traverse(const float* p4, int n_queries, float padding, const fl
                          const float* nmin4, const float* nmax4, const int* prefix, const float* face_rec8, int cap,
                          int* cand, int* num, int* status, void* stream);
 
+/* The same walk for edge boxes (the reference's commented-out edge broad
+ * phase, XPBD.py:217-232): query q is the box of edge (edges[2q], edges[2q+1])
+ * of the points p4, min - padding .. max + padding per axis. */
+int sx_cell_bvh_traverse_edges(const int* edges, int n_edges, const float* p4, float padding, const float* grid8,
+                               const float* origin_box6, const float* nmin4, const float* nmax4, const int* prefix,
+                               const float* face_rec8, int cap, int* cand, int* num, int* status, void* stream);
+
 /* ---- face-level LBVH (standalone broad phase) ------------------------------ */
 
 /* Morton codes of face-AABB centres normalised by box6 (intended form of
@@ -280,6 +287,32 @@ int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* f
 int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4, const float* xs4,
                            const float* fixed, const float* m_inv, float dHat, float compliance, float cull_d2,
                            long long* dx_fix, int* nc, int* status, const int* conv, int iter, void* stream);
+
+/* Edge-edge contacts: __ee_st / __ee_dy (collision_constraints_x.py:313-588;
+ * d_type_EE distance.py:50-99, d_EE :119-124; the gradient in closed form)
+ * as the reference's commented-out solver code would call them
+ * (XPBD.py:266-281): for every cloth edge e and candidate face f (ee_st:
+ * static faces, ee_dy: cloth faces; n_edges_dy x cap each), the three edges
+ * face_edges[3f + k] of f; ee_dy skips edges sharing a vertex with e.  Only
+ * d_type_EE == 8 with |x01 x x23| > 1e-3 and d_EE < dHat projects:
+ * ld = compliance (dHat - d) / (compliance schur + 1), dx += fixed m_inv ld g
+ * on the cloth's vertices (ee_st: e's two; ee_dy: all four).  Terms are
+ * ADDED to dx_fix / nc; no update_dx -- run before sx_collision_sweep or
+ * sx_contact_pairs_sweep of the same iteration, which apply both.  ee_st_cand
+ * NULL: no static mesh.  Records (optional): blocks ee_st | ee_dy of
+ * n_edges_dy queries x cap, (partner edge, dtype), gradients, schur; records
+ * past cap are dropped (the reference writes past its cache).  conv/iter: the
+ * convergence gate of sx_jacobi_sweep_checked. */
+int sx_edge_edge_sweep(int n_edges_dy, const int* edges_dy, const int* edges_st, const int* face_edges_dy,
+                       const int* face_edges_st, const float* y4, const float* xs4, const float* fixed,
+                       const float* m_inv, float dHat, float compliance, int cap, const int* ee_st_cand,
+                       const int* ee_st_num, const int* ee_dy_cand, const int* ee_dy_num, long long* dx_fix, int* nc,
+                       int* pair, float* pair_g, float* pair_schur, int* pair_num, int* status, const int* conv,
+                       int iter, void* stream);
+/* d_type_EE, the projected distance (dHat unless dtype 8 with
+ * |x01 x x23| > 1e-3) and its gradient for n quadruples p12[12 i ..] = x0, x1
+ * (edge 0), x2, x3 (edge 1): dtype[n], d[n], g12[12 n]. */
+int sx_edge_edge_classify(int n, const float* p12, float dHat, int* dtype, float* d, float* g12, void* stream);
 
 /* solve_constraints_v (XPBD.py:374-381, :398-404; collision_constraints_v.py
  * __vt_st :6-133, __tv_st :137-330, __vt_dy :334-570): velocity-level contact

@@ -773,15 +773,19 @@ static float box_d2(V3 p, V3 t0, V3 t1, V3 t2) {
     return (ex * ex + ey * ey) + ez * ez;
 }
 
+// accumulate != 0: dx_fix / nc already hold this iteration's edge-edge terms
+// (or_edge_edge_sweep) and are added to instead of cleared.
 API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_t* faces_st, float* y4,
                            const float* xs4, const float* fixed, const float* m_inv, float dHat, float compliance,
                            float cull_d2, int cap, const int32_t* vt_st_c, const int32_t* vt_st_n, const int32_t* vt_dy_c,
                            const int32_t* vt_dy_n, const int32_t* tv_st_c, const int32_t* tv_st_n,
                            int64_t* dx_fix, int32_t* nc, int32_t* pair, float* pair_g, float* pair_schur,
-                           int32_t* pair_num, int32_t* status, int nthreads) {
+                           int32_t* pair_num, int32_t* status, int nthreads, int accumulate) {
     int par = set_threads(nthreads);
-    std::memset(dx_fix, 0, sizeof(int64_t) * 3 * (size_t)Vd);
-    std::memset(nc, 0, sizeof(int32_t) * (size_t)Vd);
+    if (!accumulate) {
+        std::memset(dx_fix, 0, sizeof(int64_t) * 3 * (size_t)Vd);
+        std::memset(nc, 0, sizeof(int32_t) * (size_t)Vd);
+    }
     int bad = 0;
     Acc acc{dx_fix, nc, &bad, par != 0};
     Pairs P[3];
@@ -891,6 +895,184 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
         if (nc[v] > 0) {
             float c = (float)nc[v];
             for (int k = 0; k < 3; ++k) y4[4 * v + k] = y4[4 * v + k] + fixed[v] * (from_fix(dx_fix[3 * v + k]) / c);
+        }
+    }
+    if (bad && status) *status |= 4;
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Edge-edge narrow phase: __ee_st / __ee_dy (collision_constraints_x.py:313-588)
+// as the commented-out callers would run them (XPBD.py:217-232 broad phase on
+// edge boxes, :266-281 narrow phase over the three edges of every candidate
+// face, vertex-sharing pairs skipped for ee_dy).  Only the interior-interior
+// case (dtype 8) with |x01 x x23| > 1e-3 projects; the other cases are
+// commented out in the reference.
+// ---------------------------------------------------------------------------
+// d_type_EE (distance.py:50-99)
+int d_type_EE(V3 v0, V3 v1, V3 v2, V3 v3) {
+    const V3 u = sub(v1, v0), v = sub(v3, v2), w = sub(v0, v2);
+    const float a = dot(u, u), b = dot(u, v), c = dot(v, v), d = dot(u, w), e = dot(v, w);
+    const float D = a * c - b * b;
+    float tD = D, tN = 0.0f;
+    int dc = 8;
+    const float sN = b * e - c * d;
+    if (sN <= 0.0f) {
+        tN = e;
+        tD = c;
+        dc = 2;
+    } else if (sN >= D) {
+        tN = e + b;
+        tD = c;
+        dc = 5;
+    } else {
+        tN = a * e - b * d;
+        const V3 uv = cross(u, v);
+        if (tN > 0.0f && tN < tD && (dot(uv, w) < 1e-4f || dot(uv, uv) < 1.0e-20f * a * c)) {
+            if (sN < D / 2.0f) {
+                tN = e;
+                tD = c;
+                dc = 2;
+            } else {
+                tN = e + b;
+                tD = c;
+                dc = 5;
+            }
+        }
+    }
+    if (tN <= 0.0f) {
+        if (-d <= 0.0f) dc = 0;
+        else if (-d >= a) dc = 3;
+        else dc = 6;
+    } else if (tN >= tD) {
+        if (-d + b <= 0.0f) dc = 1;
+        else if (-d + b >= a) dc = 4;
+        else dc = 7;
+    }
+    return dc;
+}
+// d_EE (distance.py:119-124): squared distance between the two lines
+inline float d_EE(V3 x0, V3 x1, V3 x2, V3 x3) {
+    const V3 b = cross(sub(x1, x0), sub(x3, x2));
+    const float aTb = dot(sub(x2, x0), b);
+    return aTb * aTb / dot(b, b);
+}
+// Closed-form gradient of d_EE: u = x1-x0, v = x3-x2, r = x2-x0, n = u x v,
+// s = r.n, N = n.n, d = s^2/N;
+//   g0 = (-2s (n + v x r) + 2d v x n)/N,  g1 = (2s v x r - 2d v x n)/N,
+//   g2 = (2s (n - r x u) + 2d n x u)/N,   g3 = (2s r x u - 2d n x u)/N.
+inline void g_EE(V3 x0, V3 x1, V3 x2, V3 x3, V3 g[4]) {
+    const V3 u = sub(x1, x0), v = sub(x3, x2), r = sub(x2, x0);
+    const V3 n = cross(u, v);
+    const float s = dot(r, n);
+    const float N = dot(n, n);
+    const float iN = 1.0f / N;
+    const float d = (s * s) * iN;
+    const float ts = 2.0f * s, td = 2.0f * d;
+    const V3 vr = cross(v, r), ru = cross(r, u), vn = cross(v, n), nu = cross(n, u);
+    g[0] = scale(iN, add(scale(-ts, add(n, vr)), scale(td, vn)));
+    g[1] = scale(iN, sub(scale(ts, vr), scale(td, vn)));
+    g[2] = scale(iN, add(scale(ts, sub(n, ru)), scale(td, nu)));
+    g[3] = scale(iN, sub(scale(ts, ru), scale(td, nu)));
+}
+// One edge pair: dtype, and for dtype 8 with |x01 x x23| > 1e-3 the squared
+// distance and (when it is below dHat) its gradient; d = dHat otherwise.
+inline float ee_pair(V3 x0, V3 x1, V3 x2, V3 x3, float dHat, int* dtype, V3 g[4]) {
+    const int dt = d_type_EE(x0, x1, x2, x3);
+    *dtype = dt;
+    float d = dHat;
+    if (dt == 8) {
+        const V3 c = cross(sub(x0, x1), sub(x2, x3));
+        if (std::sqrt(dot(c, c)) > 1e-3f) {
+            d = d_EE(x0, x1, x2, x3);
+            if (d < dHat) g_EE(x0, x1, x2, x3, g);
+        }
+    }
+    return d;
+}
+
+// Classification and distance of n point quadruples (12 floats each): the
+// kernel-level check of every branch.
+API int or_edge_edge_classify(int n, const float* p12, float dHat, int32_t* dtype, float* d, float* g12) {
+    for (int i = 0; i < n; ++i) {
+        const float* p = p12 + 12 * (size_t)i;
+        V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+        d[i] = ee_pair(v3(p), v3(p + 3), v3(p + 6), v3(p + 9), dHat, dtype + i, g);
+        for (int k = 0; k < 4; ++k) {
+            g12[12 * (size_t)i + 3 * k] = g[k].x;
+            g12[12 * (size_t)i + 3 * k + 1] = g[k].y;
+            g12[12 * (size_t)i + 3 * k + 2] = g[k].z;
+        }
+    }
+    return 0;
+}
+
+// Edge-edge terms of one iteration, added to dx_fix / nc (no update_dx: the
+// vertex-triangle sweep follows with accumulate = 1 and applies both).
+//   dynamic edges (Ed): edges_dy, face_edges_dy[3 F_dy], positions y4
+//   static mesh: edges_st, face_edges_st, xs4 (NULL: no ee_st)
+//   candidates (faces): ee_st (Ed x cap) on the static BVH, ee_dy on the
+//   dynamic one.  Records (optional): ee_st block then ee_dy block of Ed
+//   queries, (partner edge, dtype), 4 gradients, schur; records past cap are
+//   dropped.
+API int or_edge_edge_sweep(int Ed, const int32_t* edges_dy, const int32_t* edges_st, const int32_t* face_edges_dy,
+                           const int32_t* face_edges_st, const float* y4, const float* xs4, const float* fixed,
+                           const float* m_inv, float dHat, float compliance, int cap, const int32_t* ee_st_c,
+                           const int32_t* ee_st_n, const int32_t* ee_dy_c, const int32_t* ee_dy_n, int64_t* dx_fix,
+                           int32_t* nc, int32_t* pair, float* pair_g, float* pair_schur, int32_t* pair_num,
+                           int32_t* status, int nthreads) {
+    int par = set_threads(nthreads);
+    int bad = 0;
+    Acc acc{dx_fix, nc, &bad, par != 0};
+    Pairs P[2];
+    for (int s = 0; s < 2; ++s) {
+        size_t qoff = s * (size_t)Ed;
+        P[s].cap = cap;
+        P[s].num = pair_num ? pair_num + qoff : nullptr;
+        P[s].pair = pair ? pair + 2 * qoff * cap : nullptr;
+        P[s].g = pair_g ? pair_g + 16 * qoff * cap : nullptr;
+        P[s].schur = pair_schur ? pair_schur + qoff * cap : nullptr;
+    }
+    if (pair_num) std::memset(pair_num, 0, sizeof(int32_t) * 2 * (size_t)Ed);
+#pragma omp parallel for if (par) schedule(dynamic, 64)
+    for (int i = 0; i < 2 * Ed; ++i) {
+        const bool st = i < Ed;
+        const int e = st ? i : i - Ed;
+        if (st && !ee_st_c) continue;
+        const int v0 = edges_dy[2 * e], v1 = edges_dy[2 * e + 1];
+        const int n = std::min(st ? ee_st_n[e] : ee_dy_n[e], cap);
+        for (int j = 0; j < n; ++j) {
+            const int f = st ? ee_st_c[(size_t)e * cap + j] : ee_dy_c[(size_t)e * cap + j];
+            for (int k = 0; k < 3; ++k) {
+                const int e2 = st ? face_edges_st[3 * f + k] : face_edges_dy[3 * f + k];
+                const int v2 = st ? edges_st[2 * e2] : edges_dy[2 * e2];
+                const int v3i = st ? edges_st[2 * e2 + 1] : edges_dy[2 * e2 + 1];
+                if (!st && (v0 == v2 || v0 == v3i || v1 == v2 || v1 == v3i)) continue;  // share_vertex (XPBD.py:130-136)
+                const V3 x0 = v3(y4 + 4 * v0), x1 = v3(y4 + 4 * v1);
+                const V3 x2 = st ? v3(xs4 + 4 * v2) : v3(y4 + 4 * v2), x3 = st ? v3(xs4 + 4 * v3i) : v3(y4 + 4 * v3i);
+                V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+                int dt;
+                const float d = ee_pair(x0, x1, x2, x3, dHat, &dt, g);
+                float schur = 0.0f;
+                if (d < dHat) {
+                    const float w0 = fixed[v0] * m_inv[v0], w1 = fixed[v1] * m_inv[v1];
+                    if (st) {
+                        schur = w0 * dot(g[0], g[0]) + w1 * dot(g[1], g[1]);
+                    } else {
+                        const float w2 = fixed[v2] * m_inv[v2], w3 = fixed[v3i] * m_inv[v3i];
+                        schur = ((w0 * dot(g[0], g[0]) + w1 * dot(g[1], g[1])) + w2 * dot(g[2], g[2])) +
+                                w3 * dot(g[3], g[3]);
+                    }
+                    const float ld = (compliance * (dHat - d)) / (compliance * schur + 1.0f);
+                    acc.add(v0, w0 * ld, g[0]);
+                    acc.add(v1, w1 * ld, g[1]);
+                    if (!st) {
+                        acc.add(v2, (fixed[v2] * m_inv[v2]) * ld, g[2]);
+                        acc.add(v3i, (fixed[v3i] * m_inv[v3i]) * ld, g[3]);
+                    }
+                    P[st ? 0 : 1].rec(e, e2, dt, g, schur);
+                }
+            }
         }
     }
     if (bad && status) *status |= 4;

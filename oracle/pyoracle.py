@@ -44,7 +44,9 @@ _SIGS = {
     "or_sewing_step": [I, P, P, P, P, P, F],
     "or_velocity_contacts": [I, I, P, P, I, P, P, P, P, P, P, P, P, P, F, P],
     "or_warm_features": [I, P, P, P, P, P, P, P, F, F, F, F, P],
-    "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I],
+    "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, I],
+    "or_edge_edge_classify": [I, P, F, P, P, P],
+    "or_edge_edge_sweep": [I, P, P, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, I],
     "or_point_triangle": [P, P, P],
     "or_color_edges": [I, I, P, I, P, P, P],
     "or_version": [],
@@ -245,14 +247,18 @@ def point_triangle(p, t0, t1, t2):
 
 
 def collision_sweep(faces_dy, faces_st, y4, xs4, fixed, m_inv, dHat, compliance, cap, vt_st, vt_dy, tv_st,
-                    want_pairs=False, nthreads=1, cull_d2=0.0):
+                    want_pairs=False, nthreads=1, cull_d2=0.0, acc=None):
     """Narrow phase + update_dx; updates y4 in place.  vt_st etc. = (cand, num).
     cull_d2 > 0 skips pairs whose point-to-triangle-box squared distance
-    exceeds it (the CUDA pair-list sweep's cull)."""
+    exceeds it (the CUDA pair-list sweep's cull).  acc = (dx, nc) from
+    :func:`edge_edge_sweep` of the same iteration, added to before update_dx."""
     Vd = y4.shape[0]
     Vs = xs4.shape[0] if xs4 is not None else 0
-    dx = np.zeros(3 * Vd, np.int64)
-    nc = np.zeros(Vd, np.int32)
+    if acc is None:
+        dx = np.zeros(3 * Vd, np.int64)
+        nc = np.zeros(Vd, np.int32)
+    else:
+        dx, nc = acc
     status = np.zeros(1, np.int32)
     pair = pair_g = pair_schur = pair_num = None
     if want_pairs:
@@ -266,7 +272,60 @@ def collision_sweep(faces_dy, faces_st, y4, xs4, fixed, m_inv, dHat, compliance,
     lib().or_collision_sweep(Vd, Vs, _p(i32(faces_dy)), _p(fs), _p(y4), _p(xs), _p(fixed), _p(m_inv), dHat,
                              compliance, cull_d2, cap, _p(vt_st[0]), _p(vt_st[1]), _p(vt_dy[0]), _p(vt_dy[1]),
                              _p(tv_st[0]), _p(tv_st[1]), _p(dx), _p(nc), _p(pair), _p(pair_g), _p(pair_schur),
-                             _p(pair_num), _p(status), nthreads)
+                             _p(pair_num), _p(status), nthreads, 0 if acc is None else 1)
+    out = {"status": int(status[0])}
+    if want_pairs:
+        out.update(pair=pair, pair_g=pair_g, pair_schur=pair_schur, pair_num=pair_num)
+    return out
+
+
+def edge_query_boxes(p4, edges, padding):
+    """Edge boxes of the edge broad phase (XPBD.py:221-232): min / max of the two
+    endpoints, minus / plus padding."""
+    p = f32(p4)[:, :3]
+    e = i32(edges).reshape(-1, 2)
+    pad = np.float32(padding)
+    mn = np.zeros((e.shape[0], 4), np.float32)
+    mx = np.zeros((e.shape[0], 4), np.float32)
+    mn[:, :3] = np.minimum(p[e[:, 0]], p[e[:, 1]]) - pad
+    mx[:, :3] = np.maximum(p[e[:, 0]], p[e[:, 1]]) + pad
+    return mn, mx
+
+
+def edge_edge_classify(p12, dHat):
+    """d_type_EE, squared distance and gradient of n quadruples (x0, x1 = edge 0,
+    x2, x3 = edge 1): d = dHat unless dtype 8 with |x01 x x23| > 1e-3."""
+    p12 = f32(p12).reshape(-1, 12)
+    n = p12.shape[0]
+    dt = np.zeros(n, np.int32)
+    d = np.zeros(n, np.float32)
+    g = np.zeros((n, 12), np.float32)
+    lib().or_edge_edge_classify(n, _p(np.ascontiguousarray(p12)), np.float32(dHat), _p(dt), _p(d), _p(g))
+    return dt, d, g.reshape(n, 4, 3)
+
+
+def edge_edge_sweep(edges_dy, edges_st, face_edges_dy, face_edges_st, y4, xs4, fixed, m_inv, dHat, compliance, cap,
+                    ee_st, ee_dy, dx, nc, want_pairs=False, nthreads=1):
+    """Edge-edge terms of one iteration added to (dx, nc); ee_st / ee_dy =
+    (cand, num) of the edge broad phase (ee_st None: no static mesh)."""
+    e_dy = i32(edges_dy).reshape(-1, 2)
+    Ed = e_dy.shape[0]
+    status = np.zeros(1, np.int32)
+    pair = pair_g = pair_schur = pair_num = None
+    if want_pairs:
+        pair = np.zeros((2 * Ed, cap, 2), np.int32)
+        pair_g = np.zeros((2 * Ed, cap, 4, 4), np.float32)
+        pair_schur = np.zeros((2 * Ed, cap), np.float32)
+        pair_num = np.zeros(2 * Ed, np.int32)
+    has_st = ee_st is not None
+    e_st = i32(edges_st) if has_st else np.zeros(2, np.int32)
+    fe_st = i32(face_edges_st) if has_st else np.zeros(3, np.int32)
+    xs = xs4 if has_st else np.zeros((1, 4), np.float32)
+    lib().or_edge_edge_sweep(Ed, _p(e_dy), _p(e_st), _p(i32(face_edges_dy)), _p(fe_st), _p(y4), _p(xs), _p(fixed),
+                             _p(m_inv), np.float32(dHat), np.float32(compliance), cap,
+                             _p(ee_st[0]) if has_st else None, _p(ee_st[1]) if has_st else None, _p(ee_dy[0]),
+                             _p(ee_dy[1]), _p(dx), _p(nc), _p(pair), _p(pair_g), _p(pair_schur), _p(pair_num),
+                             _p(status), nthreads)
     out = {"status": int(status[0])}
     if want_pairs:
         out.update(pair=pair, pair_g=pair_g, pair_schur=pair_schur, pair_num=pair_num)
@@ -477,8 +536,10 @@ class OracleSolver:
                  damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
                  compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True,
                  contact_cull=False, tol=None, check_every=4, tol_relative=False, sewing=None,
-                 velocity_update=False, mu=0.8):
+                 velocity_update=False, mu=0.8, edge_edge=False):
         self.d = mesh_dy
+        # edge-edge contacts (the reference's commented-out ee_st / ee_dy path)
+        self.edge_edge = edge_edge
         # iterate to a residual (the CUDA solver's tol mode): every
         # check_every-th iteration measures the residual of the current y; once
         # it is <= tol, that block of check_every iterations completes and the
@@ -528,6 +589,11 @@ class OracleSolver:
         self.bl0 = f32(mesh_dy["bend_l0"])
         self.faces = i32(mesh_dy["faces"])
         self.adj_ptr, self.adj = adjacency(V, self.edges, self.l0, self.bend, self.bl0)
+        if edge_edge:
+            self.face_edges = i32(mesh_dy["face_edges"])
+            if mesh_st is not None:
+                self.edges_st = i32(mesh_st["edges"])
+                self.face_edges_st = i32(mesh_st["face_edges"])
         if collisions:
             self.bvh_dy = CellBVH()
             if mesh_st is not None:
@@ -559,6 +625,13 @@ class OracleSolver:
         else:
             vt_dy = (np.zeros((Vd, self.cap), np.int32), np.zeros(Vd, np.int32), 0)
         self.last_status |= vt_st[2] | vt_dy[2] | tv_st[2]
+        self._ee = None
+        if self.edge_edge:
+            emn, emx = edge_query_boxes(y4, self.edges, self.padding)
+            ee_st = self.bvh_st.traverse(emn, emx, self.cap) if self.s is not None else None
+            ee_dy = self.bvh_dy.traverse(emn, emx, self.cap)
+            self.last_status |= ee_dy[2] | (ee_st[2] if ee_st is not None else 0)
+            self._ee = (ee_st, ee_dy)
         return vt_st, vt_dy, tv_st
 
     def substep(self, dt_sub):
@@ -591,11 +664,23 @@ class OracleSolver:
                 if it == 0:
                     cands = self._broad(y4)
                 vt_st, vt_dy, tv_st = cands
+                acc = None
+                if self.edge_edge:
+                    Vd = y4.shape[0]
+                    acc = (np.zeros(3 * Vd, np.int64), np.zeros(Vd, np.int32))
+                    ee_st, ee_dy = self._ee
+                    has_st = self.s is not None
+                    re = edge_edge_sweep(self.edges, self.edges_st if has_st else None, self.face_edges,
+                                         self.face_edges_st if has_st else None, y4, self.xs4 if has_st else None,
+                                         self.fixed, self.m_inv, self.dHat, self.compliance, self.cap,
+                                         ee_st[:2] if ee_st is not None else None, ee_dy[:2], acc[0], acc[1],
+                                         nthreads=self.nthreads)
+                    self.last_status |= re["status"]
                 r = collision_sweep(self.faces, self.faces_st if self.s is not None else None, y4,
                                     self.xs4 if self.s is not None else None, self.fixed, self.m_inv, self.dHat,
                                     self.compliance, self.cap, vt_st[:2], vt_dy[:2], tv_st[:2],
                                     nthreads=self.nthreads, cull_d2=self.cull_d2,
-                                    want_pairs=self.velocity_update)
+                                    want_pairs=self.velocity_update, acc=acc)
                 self.last_status |= r["status"]
                 if self.velocity_update:
                     self._records = r

@@ -245,6 +245,167 @@ __device__ __forceinline__ void project_tv_st(const int vv[4], const V3 x[4], co
 
 // Candidate lists walked per query, in list order, as the reference does; the
 // only variant that can write pair records (their slot order is list order).
+// ---------------------------------------------------------------------------
+// Edge-edge contacts: __ee_st / __ee_dy (collision_constraints_x.py:313-588)
+// as the reference's commented-out callers would run them (XPBD.py:217-232,
+// :266-281).  Only dtype 8 (both closest points interior) with
+// |x01 x x23| > 1e-3 projects; the reference comments out the other cases.
+// ---------------------------------------------------------------------------
+// d_type_EE (distance.py:50-99); the triple-product test is signed, as there
+__device__ int d_type_EE(V3 v0, V3 v1, V3 v2, V3 v3) {
+    const V3 u = sub(v1, v0), v = sub(v3, v2), w = sub(v0, v2);
+    const float a = dot(u, u), b = dot(u, v), c = dot(v, v), d = dot(u, w), e = dot(v, w);
+    const float D = a * c - b * b;
+    float tD = D, tN = 0.0f;
+    int dc = 8;
+    const float sN = b * e - c * d;
+    if (sN <= 0.0f) {
+        tN = e;
+        tD = c;
+        dc = 2;
+    } else if (sN >= D) {
+        tN = e + b;
+        tD = c;
+        dc = 5;
+    } else {
+        tN = a * e - b * d;
+        const V3 uv = cross(u, v);
+        if (tN > 0.0f && tN < tD && (dot(uv, w) < 1e-4f || dot(uv, uv) < 1.0e-20f * a * c)) {
+            if (sN < D / 2.0f) {
+                tN = e;
+                tD = c;
+                dc = 2;
+            } else {
+                tN = e + b;
+                tD = c;
+                dc = 5;
+            }
+        }
+    }
+    if (tN <= 0.0f) {
+        if (-d <= 0.0f) dc = 0;
+        else if (-d >= a) dc = 3;
+        else dc = 6;
+    } else if (tN >= tD) {
+        if (-d + b <= 0.0f) dc = 1;
+        else if (-d + b >= a) dc = 4;
+        else dc = 7;
+    }
+    return dc;
+}
+// d_EE (distance.py:119-124): squared distance between the two lines
+__device__ __forceinline__ float d_EE(V3 x0, V3 x1, V3 x2, V3 x3) {
+    const V3 b = cross(sub(x1, x0), sub(x3, x2));
+    const float aTb = dot(sub(x2, x0), b);
+    return aTb * aTb / dot(b, b);
+}
+// Closed-form gradient of d_EE: u = x1-x0, v = x3-x2, r = x2-x0, n = u x v,
+// s = r.n, N = n.n, d = s^2/N;
+//   g0 = (-2s (n + v x r) + 2d v x n)/N,  g1 = (2s v x r - 2d v x n)/N,
+//   g2 = (2s (n - r x u) + 2d n x u)/N,   g3 = (2s r x u - 2d n x u)/N.
+__device__ __forceinline__ void g_EE(V3 x0, V3 x1, V3 x2, V3 x3, V3 g[4]) {
+    const V3 u = sub(x1, x0), v = sub(x3, x2), r = sub(x2, x0);
+    const V3 n = cross(u, v);
+    const float s = dot(r, n);
+    const float N = dot(n, n);
+    const float iN = 1.0f / N;
+    const float d = (s * s) * iN;
+    const float ts = 2.0f * s, td = 2.0f * d;
+    const V3 vr = cross(v, r), ru = cross(r, u), vn = cross(v, n), nu = cross(n, u);
+    g[0] = scale(iN, add(scale(-ts, add(n, vr)), scale(td, vn)));
+    g[1] = scale(iN, sub(scale(ts, vr), scale(td, vn)));
+    g[2] = scale(iN, add(scale(ts, sub(n, ru)), scale(td, nu)));
+    g[3] = scale(iN, sub(scale(ts, ru), scale(td, nu)));
+}
+// dtype; for dtype 8 with |x01 x x23| > 1e-3 the squared distance and, below
+// dHat, its gradient; d = dHat otherwise
+__device__ __forceinline__ float ee_pair(V3 x0, V3 x1, V3 x2, V3 x3, float dHat, int* dtype, V3 g[4]) {
+    const int dt = d_type_EE(x0, x1, x2, x3);
+    *dtype = dt;
+    float d = dHat;
+    if (dt == 8) {
+        const V3 c = cross(sub(x0, x1), sub(x2, x3));
+        if (sqrtf(dot(c, c)) > 1e-3f) {
+            d = d_EE(x0, x1, x2, x3);
+            if (d < dHat) g_EE(x0, x1, x2, x3, g);
+        }
+    }
+    return d;
+}
+
+__global__ void edge_edge_classify_kernel(int n, const float* __restrict__ p12, float dHat, int* dtype, float* d,
+                                          float* g12) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float* p = p12 + 12 * (size_t)i;
+    V3 g[4] = SX_ZERO_G;
+    int dt;
+    d[i] = ee_pair(V3{p[0], p[1], p[2]}, V3{p[3], p[4], p[5]}, V3{p[6], p[7], p[8]}, V3{p[9], p[10], p[11]}, dHat,
+                   &dt, g);
+    dtype[i] = dt;
+    for (int k = 0; k < 4; ++k) {
+        g12[12 * (size_t)i + 3 * k] = g[k].x;
+        g12[12 * (size_t)i + 3 * k + 1] = g[k].y;
+        g12[12 * (size_t)i + 3 * k + 2] = g[k].z;
+    }
+}
+
+// Thread per query edge: ee_st block [0, Ed) against the static mesh's edges,
+// ee_dy block [Ed, 2 Ed) against the cloth's own; for each candidate face, its
+// three edges in order (vertex-sharing pairs skipped for ee_dy, XPBD.py:130-136).
+__global__ void __launch_bounds__(128) edge_edge_kernel(
+    int Ed, const int* __restrict__ edges_dy, const int* __restrict__ edges_st, const int* __restrict__ fe_dy,
+    const int* __restrict__ fe_st, const float4* __restrict__ y4, const float4* __restrict__ xs4,
+    const float* __restrict__ fixed, const float* __restrict__ m_inv, float dHat, float compliance, int cap,
+    const int* __restrict__ st_c, const int* __restrict__ st_n, const int* __restrict__ dy_c,
+    const int* __restrict__ dy_n, long long* dx, int* nc, PairOut po, int* status, const int* conv, int iter) {
+    if (iteration_skipped(conv, iter)) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= 2 * Ed) return;
+    const bool st = i < Ed;
+    const int e = st ? i : i - Ed;
+    int bad = 0, cnt = 0;
+    if (!st || st_c != nullptr) {
+        const int v0 = edges_dy[2 * e], v1 = edges_dy[2 * e + 1];
+        const V3 x0 = mk(y4[v0]), x1 = mk(y4[v1]);
+        const float w0 = fixed[v0] * m_inv[v0], w1 = fixed[v1] * m_inv[v1];
+        const int n = min(st ? st_n[e] : dy_n[e], cap);
+        for (int j = 0; j < n; ++j) {
+            const int f = st ? st_c[(size_t)e * cap + j] : dy_c[(size_t)e * cap + j];
+            for (int k = 0; k < 3; ++k) {
+                const int e2 = st ? fe_st[3 * f + k] : fe_dy[3 * f + k];
+                const int v2 = st ? edges_st[2 * e2] : edges_dy[2 * e2];
+                const int v3 = st ? edges_st[2 * e2 + 1] : edges_dy[2 * e2 + 1];
+                if (!st && (v0 == v2 || v0 == v3 || v1 == v2 || v1 == v3)) continue;
+                const V3 x2 = mk((st ? xs4 : y4)[v2]), x3 = mk((st ? xs4 : y4)[v3]);
+                V3 g[4] = SX_ZERO_G;
+                int dt;
+                const float d = ee_pair(x0, x1, x2, x3, dHat, &dt, g);
+                if (d < dHat) {
+                    float schur;
+                    if (st) {
+                        schur = w0 * dot(g[0], g[0]) + w1 * dot(g[1], g[1]);
+                    } else {
+                        const float w2 = fixed[v2] * m_inv[v2], w3 = fixed[v3] * m_inv[v3];
+                        schur = ((w0 * dot(g[0], g[0]) + w1 * dot(g[1], g[1])) + w2 * dot(g[2], g[2])) +
+                                w3 * dot(g[3], g[3]);
+                    }
+                    const float ld = (compliance * (dHat - d)) / (compliance * schur + 1.0f);
+                    acc_add(dx, nc, v0, w0 * ld, g[0], &bad);
+                    acc_add(dx, nc, v1, w1 * ld, g[1], &bad);
+                    if (!st) {
+                        acc_add(dx, nc, v2, (fixed[v2] * m_inv[v2]) * ld, g[2], &bad);
+                        acc_add(dx, nc, v3, (fixed[v3] * m_inv[v3]) * ld, g[3], &bad);
+                    }
+                    po.rec((size_t)i, cnt, e2, dt, g, schur);
+                }
+            }
+        }
+    }
+    if (po.num) po.num[i] = cnt;
+    if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
+}
+
 __global__ void __launch_bounds__(128) collision_project_kernel(
     int Vd, int Vs, const int* __restrict__ faces_dy, const int* __restrict__ faces_st,
     const float4* __restrict__ y4, const float4* __restrict__ xs4, const float* __restrict__ fixed,
@@ -975,6 +1136,36 @@ __global__ void velocity_apply_kernel(int V, float4* __restrict__ v4, const floa
 }  // namespace sx
 
 using namespace sx;
+
+extern "C" int sx_edge_edge_classify(int n, const float* p12, float dHat, int* dtype, float* d, float* g12,
+                                     void* stream) {
+    SX_REQUIRE(n >= 0, "sx_edge_edge_classify: n < 0");
+    if (n == 0) return SX_OK;
+    SX_REQUIRE(p12 && dtype && d && g12, "sx_edge_edge_classify: null pointer");
+    launch(edge_edge_classify_kernel, grid_for(n, 128), 128, 0, as_stream(stream), n, p12, dHat, dtype, d, g12);
+    return check_launch("edge_edge_classify_kernel");
+}
+
+extern "C" int sx_edge_edge_sweep(int n_edges_dy, const int* edges_dy, const int* edges_st, const int* face_edges_dy,
+                                  const int* face_edges_st, const float* y4, const float* xs4, const float* fixed,
+                                  const float* m_inv, float dHat, float compliance, int cap, const int* ee_st_cand,
+                                  const int* ee_st_num, const int* ee_dy_cand, const int* ee_dy_num,
+                                  long long* dx_fix, int* nc, int* pair, float* pair_g, float* pair_schur,
+                                  int* pair_num, int* status, const int* conv, int iter, void* stream) {
+    SX_REQUIRE(n_edges_dy >= 0 && cap >= 1, "sx_edge_edge_sweep: bad sizes");
+    if (n_edges_dy == 0) return SX_OK;
+    SX_REQUIRE(edges_dy && face_edges_dy && y4 && fixed && m_inv && ee_dy_cand && ee_dy_num && dx_fix && nc &&
+                   status,
+               "sx_edge_edge_sweep: null pointer");
+    SX_REQUIRE(!ee_st_cand || (ee_st_num && edges_st && face_edges_st && xs4),
+               "sx_edge_edge_sweep: null static-mesh pointer");
+    SX_REQUIRE(!pair_num || (pair && pair_g && pair_schur), "sx_edge_edge_sweep: partial pair outputs");
+    PairOut po{pair, pair_g, pair_schur, pair_num, cap};
+    launch(edge_edge_kernel, grid_for(2LL * n_edges_dy, 128), 128, 0, as_stream(stream), n_edges_dy, edges_dy, edges_st, face_edges_dy, face_edges_st,
+           (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, cap, ee_st_cand, ee_st_num,
+           ee_dy_cand, ee_dy_num, dx_fix, nc, po, status, conv, iter);
+    return check_launch("edge_edge_kernel");
+}
 
 extern "C" int sx_collision_sweep(int n_dy, int n_st, const int* faces_dy, const int* faces_st, float* y4,
                                   const float* xs4, const float* fixed, const float* m_inv, float dHat,

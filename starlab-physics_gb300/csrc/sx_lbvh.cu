@@ -500,10 +500,14 @@ __device__ __forceinline__ int warp_owner(int incl, int k) {
     return lo;
 }
 
+// EDGE: query q is the box of edge q (endpoints edges[2q], edges[2q+1] in p4)
+// grown by pad (XPBD.py:221-232), else the box p4[q] +- pad.
+template <bool EDGE>
 __global__ void __launch_bounds__(CT_BLOCK, 4) cell_traverse_kernel(
     int Q, const float4* __restrict__ p4, float pad, const float* __restrict__ grid8, const float* __restrict__ box6,
     const float4* __restrict__ nmin4, const float4* __restrict__ nmax4, const int* __restrict__ prefix,
-    const float4* __restrict__ frec, int cap, int* __restrict__ cand, int* __restrict__ num, int* status) {
+    const float4* __restrict__ frec, int cap, int* __restrict__ cand, int* __restrict__ num, int* status,
+    const int* __restrict__ edges) {
     // occupancy words: bit z of word x*32 + y = cell (x, y, z) holds faces
     __shared__ unsigned occ[kGridRes * kGridRes];
     const unsigned* gocc = reinterpret_cast<const unsigned*>(grid8) + kGridHeader;
@@ -512,8 +516,17 @@ __global__ void __launch_bounds__(CT_BLOCK, 4) cell_traverse_kernel(
     const int q = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (q >= Q) return;  // warp-uniform
-    const V3 p = mk(p4[q]);
-    const V3 a{p.x - pad, p.y - pad, p.z - pad}, b{p.x + pad, p.y + pad, p.z + pad};
+    V3 a, b;
+    if (EDGE) {
+        const V3 p0 = mk(p4[edges[2 * q]]), p1 = mk(p4[edges[2 * q + 1]]);
+        const V3 lo = vmin(p0, p1), hi = vmax(p0, p1);
+        a = V3{lo.x - pad, lo.y - pad, lo.z - pad};
+        b = V3{hi.x + pad, hi.y + pad, hi.z + pad};
+    } else {
+        const V3 p = mk(p4[q]);
+        a = V3{p.x - pad, p.y - pad, p.z - pad};
+        b = V3{p.x + pad, p.y + pad, p.z + pad};
+    }
     const V3 pos = scale(0.5f, add(a, b));
     const V3 cs{grid8[0], grid8[1], grid8[2]}, org{box6[0], box6[1], box6[2]};
     const int ix = f2i_sat((pos.x - org.x) / cs.x), iy = f2i_sat((pos.y - org.y) / cs.y),
@@ -838,10 +851,24 @@ extern "C" int sx_cell_bvh_traverse(const float* p4, int n_queries, float paddin
     SX_REQUIRE(p4 && grid8 && origin_box6 && nmin4 && nmax4 && prefix && face_rec8 &&
                    cand && num && status,
                "sx_cell_bvh_traverse: null pointer");
-    launch(cell_traverse_kernel, grid_for(32LL * n_queries, CT_BLOCK), CT_BLOCK, 0, as_stream(stream), n_queries,
-           (const float4*)p4,
-           padding, grid8, origin_box6, (const float4*)nmin4, (const float4*)nmax4, prefix,
-           (const float4*)face_rec8, cap, cand, num, status);
+    launch(cell_traverse_kernel<false>, grid_for(32LL * n_queries, CT_BLOCK), CT_BLOCK, 0, as_stream(stream),
+           n_queries, (const float4*)p4, padding, grid8, origin_box6, (const float4*)nmin4, (const float4*)nmax4,
+           prefix, (const float4*)face_rec8, cap, cand, num, status, (const int*)nullptr);
+    return check_launch("cell_traverse_kernel");
+}
+
+extern "C" int sx_cell_bvh_traverse_edges(const int* edges, int n_edges, const float* p4, float padding,
+                                          const float* grid8, const float* origin_box6, const float* nmin4,
+                                          const float* nmax4, const int* prefix, const float* face_rec8, int cap,
+                                          int* cand, int* num, int* status, void* stream) {
+    SX_REQUIRE(n_edges >= 0 && cap >= 1, "sx_cell_bvh_traverse_edges: bad sizes");
+    if (n_edges == 0) return SX_OK;
+    SX_REQUIRE(edges && p4 && grid8 && origin_box6 && nmin4 && nmax4 && prefix && face_rec8 && cand && num &&
+                   status,
+               "sx_cell_bvh_traverse_edges: null pointer");
+    launch(cell_traverse_kernel<true>, grid_for(32LL * n_edges, CT_BLOCK), CT_BLOCK, 0, as_stream(stream), n_edges,
+           (const float4*)p4, padding, grid8, origin_box6, (const float4*)nmin4, (const float4*)nmax4, prefix,
+           (const float4*)face_rec8, cap, cand, num, status, edges);
     return check_launch("cell_traverse_kernel");
 }
 

@@ -102,6 +102,14 @@ class LBVH_CELL:
                                 ptr(self.node_min4), ptr(self.node_max4), ptr(self.prefix_sum_cell),
                                 ptr(self.face_rec8), int(cap), ptr(cand), ptr(num), ptr(status), stream_handle())
 
+    def traverse_edges(self, edge_indices, n_edges: int, points4, padding: float, cap: int, cand, num, status):
+        """``traverse_cell_bvh_single`` for edge boxes: min / max of each edge's
+        endpoints in ``points4`` -/+ padding (XPBD.py:217-232)."""
+        sx.sx_cell_bvh_traverse_edges(ptr(edge_indices), int(n_edges), ptr(points4), float(padding), ptr(self.grid8),
+                                      ptr(self.box6), ptr(self.node_min4), ptr(self.node_max4),
+                                      ptr(self.prefix_sum_cell), ptr(self.face_rec8), int(cap), ptr(cand), ptr(num),
+                                      ptr(status), stream_handle())
+
 
 class LBVH:
     """Face-level LBVH over ``n`` faces (one face per leaf).

@@ -25,7 +25,9 @@ Device layout (torch CUDA tensors, SoA, float4-padded):
   and its effective inverse mass; ``v4.w`` is 0.
 * ``fixed, m_inv: float32[V]``.
 * ``face_indices: int32[F*3]``, ``edge_indices: int32[E*2]``, ``l0: float32[E]``,
-  ``bending_indices: int32[B*2]``, ``bending_l0: float32[B]``.
+  ``bending_indices: int32[B*2]``, ``bending_l0: float32[B]``,
+  ``face_edge_indices: int32[F*3]`` (edge ids of each face's sides, for the
+  edge-edge contacts).
 * ``adj_ptr: int32[V+1]`` and ``adj: int32[2*(E+B), 2]`` -- the vertex-centric
   list of incident constraints in ascending constraint index (springs
   ``0..E-1`` then bending pairs ``E..E+B-1``); each entry is
@@ -134,6 +136,27 @@ def edges_from_faces(faces: np.ndarray) -> np.ndarray:
     e.sort(axis=1)
     e = np.unique(e, axis=0)
     return e.astype(np.int32)
+
+
+def face_edges(faces: np.ndarray, edges: np.ndarray) -> np.ndarray:
+    """Edge ids of each face's sides ``(f0, f1), (f1, f2), (f2, f0)``
+    (``face_edge_indices``, ``meshTaichiWrapper.py:115-119``), against the
+    canonical edge table of :func:`edges_from_faces`."""
+    f = np.asarray(faces, dtype=np.int64).reshape(-1, 3)
+    e = np.asarray(edges, dtype=np.int64).reshape(-1, 2)
+    if f.shape[0] == 0:
+        return np.zeros((0, 3), np.int32)
+    n = int(max(f.max(), e.max() if e.size else 0)) + 1
+    keys = e[:, 0] * n + e[:, 1]
+    out = np.empty(f.shape, dtype=np.int64)
+    for k in range(3):
+        a, b = f[:, k], f[:, (k + 1) % 3]
+        q = np.minimum(a, b) * n + np.maximum(a, b)
+        idx = np.searchsorted(keys, q)
+        if (idx >= keys.shape[0]).any() or (keys[np.minimum(idx, keys.shape[0] - 1)] != q).any():
+            raise ValueError("a face side is missing from the edge table")
+        out[:, k] = idx
+    return out.astype(np.int32)
 
 
 def bending_pairs(faces: np.ndarray) -> np.ndarray:
@@ -274,6 +297,7 @@ class TriMesh:
         self.x0_np = x
         self.fid_np = faces
         self.eid_np = edges
+        self.face_edge_np = face_edges(faces, edges)
         self.l0_np = l0
         self.m_inv_np = m_inv
         self.bending_np = bend
@@ -285,6 +309,7 @@ class TriMesh:
         t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
         self.face_indices = t(faces.reshape(-1))
         self.edge_indices = t(edges.reshape(-1))
+        self.face_edge_indices = t(self.face_edge_np.reshape(-1))
         self.l0 = t(l0)
         self.bending_indices = t(bend.reshape(-1))
         self.bending_l0 = t(bend_l0)

@@ -14,6 +14,11 @@ with the shapes, sizes and parameters of the benchmark configurations:
   offsets; contact thickness 2e-3 (dHat = thickness^2, since the reference
   compares squared distances); 10 substeps, 30 iterations; BVHs rebuilt every
   substep.
+* ``crossed_layers`` -- two coarse 6 x 6 cloth layers (side 0.7, edges 0.14),
+  the lower one turned by 35 degrees, falling onto a box (side 0.5): long
+  edges crossing at close range, the case in which the reference's
+  edge-edge classifier (whose interior case needs a triple product >= 1e-4)
+  reports edge-edge contacts; 5 substeps, 4 iterations, thickness 0.02.
 * ``soup``      -- 2^20 random triangles for the standalone broad phase:
   centroids U[0,1]^3, edge lengths U[1e-3, 1e-2], random orientation; queries
   are the first vertex of every triangle with padding 2e-3.
@@ -82,6 +87,23 @@ def drape256(n: int = 256, seed: int = 0, sphere_subdiv: int = 5, gap: float = 0
                  meta={"grid": n, "thickness": thickness, "sphere_faces": int(sf.shape[0])})
 
 
+def crossed_layers() -> Scene:
+    a_x, a_f = grid_cloth(6, origin=(0.15, 0.15), size=0.7, height=0.56)
+    b_x, b_f = grid_cloth(6, origin=(0.0, 0.0), size=0.7, height=0.53)
+    th = np.deg2rad(35.0)
+    R = np.array([[np.cos(th), -np.sin(th)], [np.sin(th), np.cos(th)]], np.float32)
+    b_x = b_x.copy()
+    b_x[:, :2] = ((b_x[:, :2] - np.float32(0.35)) @ R.T + np.float32(0.5)).astype(np.float32)
+    x = np.concatenate([a_x, b_x]).astype(np.float32)
+    f = np.concatenate([a_f, b_f + a_x.shape[0]]).astype(np.int32)
+    bx, bf = box_mesh(0.5, center=(0.5, 0.5, 0.25))
+    thickness = 0.02
+    return Scene("crossed_layers", x, f, bx, bf, np.zeros(0, np.int64), dt=1.0 / 60.0, n_substeps=5, n_iter=4,
+                 gravity=(0.0, 0.0, -9.81), stiffness_stretch=1e5, stiffness_bending=1e8,
+                 dHat=thickness * thickness, padding=2 * thickness, collisions=True, rebuild="substep",
+                 meta={"thickness": thickness})
+
+
 def triangle_soup(n_tris: int = 1 << 20, seed: int = 0):
     """Returns (verts float32[3n,3], faces int32[n,3], queries float32[n,3])."""
     rng = np.random.default_rng(seed)
@@ -132,7 +154,8 @@ def make_solver(scene: Scene, device="cuda"):
 def oracle_inputs(mesh):
     """Host arrays of a TriMesh in the form the CPU oracle takes."""
     return {
-        "x": mesh.x0_np, "faces": mesh.fid_np, "edges": mesh.eid_np, "l0": mesh.l0_np,
+        "x": mesh.x0_np, "faces": mesh.fid_np, "edges": mesh.eid_np, "face_edges": mesh.face_edge_np,
+        "l0": mesh.l0_np,
         "bend": mesh.bending_np, "bend_l0": mesh.bending_l0_np, "m_inv": mesh.m_inv_np,
         "fixed": mesh.fixed.detach().cpu().numpy(),
     }

@@ -38,6 +38,11 @@ Options beyond the reference (keyword-only, defaults reproduce the reference):
   between vertex pairs (``solve_sewing_constraints_x``, XPBD.py:425-441,
   commented out at XPBD.py:371-372 in the reference), solved after the contact
   update of every Jacobi iteration with k = stiffness * dt^2.
+* ``enable_edge_edge`` (attribute, default off as in the reference, whose
+  edge-edge calls are commented out) -- per substep an edge broad phase (each
+  cloth edge's box against both cell BVHs, XPBD.py:217-232) and per iteration
+  the edge-edge contacts __ee_st / __ee_dy (collision_constraints_x.py:313-588)
+  over the three edges of every candidate face, added to the contact update.
 * ``contact_cull`` (attribute, default on) -- the pair-list contact sweep skips
   a pair whose point-to-triangle-box squared distance exceeds ``dHat * 1.0625``
   before classifying its region.  The distance of every region is at least the
@@ -90,6 +95,10 @@ class Solver:
         # when collisions are on
         self.self_collision = True
         self.contact_cull = True
+        # edge-edge contacts (__ee_st / __ee_dy; commented out in the
+        # reference's solver, so off by default)
+        self.enable_edge_edge = False
+        self._ee = None
         self._sewing = None  # (sewn, sptr, partner, scratch, stiffness)
         # launch configuration of the fixed-count sweep (autotune() picks one)
         self.sweep_variant = 0
@@ -228,6 +237,49 @@ class Solver:
                                   self.status)
         else:
             self.vt_dy_candidates_num.zero_()
+        if self.enable_edge_edge:
+            ee = self._ensure_ee()
+            cap = self.cache_size
+            if self.mesh_st is not None:
+                self.lbvh_st.traverse_edges(m.edge_indices, m.num_edges, m.y4, self.padding, cap, ee["st_c"],
+                                            ee["st_n"], self.status)
+            self.lbvh_dy.traverse_edges(m.edge_indices, m.num_edges, m.y4, self.padding, cap, ee["dy_c"], ee["dy_n"],
+                                        self.status)
+
+    def _ensure_ee(self):
+        """Edge-edge candidate lists (and records with record_pairs): blocks of
+        num_edges x cap, allocated on first use."""
+        if self._ee is None:
+            E, cap, dev = self.mesh_dy.num_edges, self.cache_size, self.device
+            i32 = dict(dtype=torch.int32, device=dev)
+            ee = {"st_c": torch.zeros((E, cap), **i32), "st_n": torch.zeros(E, **i32),
+                  "dy_c": torch.zeros((E, cap), **i32), "dy_n": torch.zeros(E, **i32)}
+            if self.record_pairs:
+                ee["pair"] = torch.zeros((2 * E, cap, 2), **i32)
+                ee["pair_g"] = torch.zeros((2 * E, cap, 4, 4), dtype=torch.float32, device=dev)
+                ee["pair_schur"] = torch.zeros((2 * E, cap), dtype=torch.float32, device=dev)
+                ee["pair_num"] = torch.zeros(2 * E, **i32)
+            self._ee = ee
+        return self._ee
+
+    def solve_edge_edge_constraints_x(self, compliance_col=None, iteration: int = 0, gated: bool = True):
+        """The edge-edge half of solve_collision_constraints_x (the reference's
+        commented-out loop, XPBD.py:266-281): terms added to the contact
+        accumulators, applied by the vertex-triangle sweep that follows."""
+        m, s = self.mesh_dy, self.mesh_st
+        ee = self._ensure_ee()
+        c = self.compliance_collision if compliance_col is None else compliance_col
+        rec = self.record_pairs
+        sx.sx_edge_edge_sweep(m.num_edges, ptr(m.edge_indices), ptr(s.edge_indices) if s is not None else None,
+                              ptr(m.face_edge_indices), ptr(s.face_edge_indices) if s is not None else None, ptr(m.y4),
+                              ptr(s.x4) if s is not None else None, ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c),
+                              self.cache_size, ptr(ee["st_c"]) if s is not None else None,
+                              ptr(ee["st_n"]) if s is not None else None, ptr(ee["dy_c"]), ptr(ee["dy_n"]),
+                              ptr(self._dx_fix), ptr(self._nc), ptr(ee["pair"]) if rec else None,
+                              ptr(ee["pair_g"]) if rec else None, ptr(ee["pair_schur"]) if rec else None,
+                              ptr(ee["pair_num"]) if rec else None, ptr(self.status),
+                              ptr(self._conv) if self.tol is not None and gated else None, iteration,
+                              stream_handle())
 
     def build_contact_pairs(self):
         """Flatten this substep's candidate lists into the dense pair list used by
@@ -247,6 +299,8 @@ class Solver:
         m = self.mesh_dy
         s = self.mesh_st
         c = self.compliance_collision if compliance_col is None else compliance_col
+        if self.enable_edge_edge:
+            self.solve_edge_edge_constraints_x(c, iteration, gated)
         if not self.record_pairs:
             sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
                                       ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
@@ -369,6 +423,8 @@ class Solver:
         With ``use_graph = True`` the whole frame is captured once into a CUDA
         graph (per set of parameters that the kernels receive by value) and
         replayed on later calls; results are identical to the eager path."""
+        if self.enable_edge_edge and self.enable_collision_handling:
+            self._ensure_ee()  # allocated outside any capture
         if not self.use_graph:
             self._forward_eager(n_substeps)
             return
@@ -431,6 +487,7 @@ class Solver:
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
                 self.compliance_collision, self.self_collision, self.contact_cull, self.sweep_variant,
+                self.enable_edge_edge,
                 self.enable_velocity_update, self.mu, self.tol,
                 self.tol_relative,
                 self.check_every,

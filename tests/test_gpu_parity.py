@@ -4,7 +4,7 @@ Integer outputs (Morton codes, sort order, BVH topology, candidate lists,
 colourings) must match bit for bit.  Float outputs are compared bit for bit as
 well: kernels and oracle evaluate the same expressions in the same order with
 no FMA contraction, so any difference is a bug.  End-to-end solver runs are
-additionally held to the benchmark spec's tolerance 1e-4 x bounding-box diagonal.
+additionally held to a tolerance of 1e-4 x the bounding-box diagonal.
 """
 import numpy as np
 import pytest
