@@ -13,8 +13,9 @@ Timing: W untimed warm-up frames, then K timed frames; before each timed frame a
 is smaller than L2); each frame is bracketed by CUDA events on the solver's
 stream.  ``e2e`` repeats the measurement through the public API with the
 state uploaded from pinned host memory and downloaded again inside the timed
-region.  ``roofline`` reports the dominant kernel (the Jacobi sweep) timed with
-CUDA events over a separate instrumented pass.  ``cpu_baseline`` times the CPU
+region.  ``roofline`` reports the dominant kernel (the contact-pair projection,
+about half of a frame) timed with CUDA events over a graph of back-to-back
+launches; ``roofline_sweep`` the same for the Jacobi sweep.  ``cpu_baseline`` times the CPU
 oracle (a port of the reference algorithm, OpenMP on all host cores) on one
 substep of the same scene.
 
@@ -660,7 +661,7 @@ def main():
     achieved = alg_bytes / (sweep_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     frame_ms = ms / args.steps
-    roofline = {"kernel": "jacobi_sweep_kernel", "bound": "hbm", "achieved": round(achieved, 1),
+    roofline_sweep = {"kernel": "jacobi_sweep_kernel", "bound": "hbm", "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": ncu_traffic("jacobi_sweep_kernel_drape256.md"),
                 "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": round(sweep_ms * 1e3, 3),
@@ -670,6 +671,60 @@ def main():
                 "launches_per_step": len(sweeps) // n_inst,
                 "share_of_step": round(sweep_ms * (len(sweeps) / n_inst) / frame_ms, 4),
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback"}
+
+    # ---- dominant kernel: the contact-pair projection (about half of a frame) ----
+    # the pair list of one substep (its first iteration), then a graph of 30
+    # projections back to back on that state; the projections only add to the
+    # fixed-point accumulators, which are cleared afterwards
+    sim.mesh_dy.x4.copy_(x0)
+    sim.mesh_dy.v4.copy_(v0)
+    sim.build_bvhs()
+    sim.compute_y(dt_sub)
+    sim.solve_constraints_jacobi_x(dt_sub, first_iteration=True, iteration=0)
+    torch.cuda.synchronize()
+    n_pairs = sim.contact_pair_count()
+    st_mesh = sim.mesh_st
+    Vs = st_mesh.num_verts if st_mesh is not None else 0
+
+    def project():
+        sx.sx_contact_pairs_project(V, Vs, ptr(sim._pairs), ptr(sim._pairs_ws), ptr(m.y4),
+                                    ptr(st_mesh.x4) if st_mesh is not None else None, ptr(m.fixed), ptr(m.m_inv),
+                                    sim.dHat, float(sim.compliance_collision), sim.contact_cull_d2(),
+                                    ptr(sim._dx_fix), ptr(sim._nc), ptr(sim.status), None, 0, stream_handle())
+
+    side = torch.cuda.Stream()
+    side.wait_stream(stream)
+    with torch.cuda.stream(side):
+        project()
+    stream.wait_stream(side)
+    gp = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(gp):
+        for _ in range(30):
+            project()
+    preps = []
+    for _ in range(5):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        gp.replay()
+        b.record(stream)
+        torch.cuda.synchronize()
+        preps.append(a.elapsed_time(b) / 30)
+    sim._dx_fix.zero_()
+    sim._nc.zero_()
+    proj_ms = sorted(preps)[len(preps) // 2]
+    proj_bytes = 16 * n_pairs + 16 * V + 16 * Vs
+    proj_gbs = proj_bytes / (proj_ms / 1e3) / 1e9
+    roofline = {"kernel": "pairs_project_kernel", "bound": "hbm", "achieved": round(proj_gbs, 1), "peak": peak,
+                "unit": "GB/s", "frac": round(proj_gbs / peak, 4),
+                "traffic": ncu_traffic("pairs_project_kernel_drape256.md"),
+                "algorithmic_bytes_per_launch": proj_bytes, "pairs_per_launch": n_pairs,
+                "avg_launch_us": round(proj_ms * 1e3, 3),
+                "timing": "CUDA events around a graph of 30 back-to-back projections of one substep's pair list "
+                          "(L2 flushed before each replay), median of 5",
+                "launches_per_step": roofline_sweep["launches_per_step"],
+                "share_of_step": round(proj_ms * roofline_sweep["launches_per_step"] / frame_ms, 4),
+                "peak_source": roofline_sweep["peak_source"]}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
@@ -683,6 +738,7 @@ def main():
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},
         "roofline": roofline,
+        "roofline_sweep": roofline_sweep,
         "clocks": clk.summary(),
         "status_flags": status,
     }

@@ -287,6 +287,14 @@ int sx_contact_pairs_build(int n_dy, int n_st, const int* faces_dy, const int* f
 int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4, const float* xs4,
                            const float* fixed, const float* m_inv, float dHat, float compliance, float cull_d2,
                            long long* dx_fix, int* nc, int* status, const int* conv, int iter, void* stream);
+/* The two halves of sx_contact_pairs_sweep: the projection, which only adds
+ * to dx_fix / nc, and update_dx (XPBD.py:384-387), which applies and clears
+ * them. */
+int sx_contact_pairs_project(int n_dy, int n_st, const int* pairs, const void* ws, const float* y4, const float* xs4,
+                             const float* fixed, const float* m_inv, float dHat, float compliance, float cull_d2,
+                             long long* dx_fix, int* nc, int* status, const int* conv, int iter, void* stream);
+int sx_contact_apply(int n_dy, float* y4, const float* fixed, long long* dx_fix, int* nc, const int* conv, int iter,
+                     void* stream);
 
 /* Edge-edge contacts: __ee_st / __ee_dy (collision_constraints_x.py:313-588;
  * d_type_EE distance.py:50-99, d_EE :119-124; the gradient in closed form)

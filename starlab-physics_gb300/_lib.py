@@ -67,6 +67,8 @@ SIGNATURES = {
     "sx_contact_pairs_workspace_bytes": ([I, I], Z),
     "sx_contact_pairs_build": ([I, I, P, P, I, P, P, P, P, P, P, P, C.c_longlong, P, Z, P], I),
     "sx_contact_pairs_sweep": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, P], I),
+    "sx_contact_pairs_project": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, P], I),
+    "sx_contact_apply": ([I, P, P, P, P, P, I, P], I),
     "sx_edge_edge_sweep": ([I, P, P, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, I, P], I),
     "sx_edge_edge_classify": ([I, P, F, P, P, P, P], I),
     "sx_cell_bvh_traverse_edges": ([P, I, P, F, P, P, P, P, P, P, I, P, P, P, P], I),

@@ -1254,24 +1254,40 @@ static int sm_count() {
     return n;
 }
 
+extern "C" int sx_contact_pairs_project(int n_dy, int n_st, const int* pairs, const void* ws, const float* y4,
+                                        const float* xs4, const float* fixed, const float* m_inv, float dHat,
+                                        float compliance, float cull_d2, long long* dx_fix, int* nc, int* status,
+                                        const int* conv, int iter, void* stream) {
+    SX_REQUIRE(n_dy >= 0 && n_st >= 0, "sx_contact_pairs_project: bad sizes");
+    if (n_dy == 0) return SX_OK;
+    SX_REQUIRE(pairs && ws && y4 && fixed && m_inv && dx_fix && nc && status,
+               "sx_contact_pairs_project: null pointer");
+    SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_project: null static positions");
+    PairsWs w = pairs_ws(const_cast<void*>(ws), n_dy, n_st);
+    launch(pairs_project_kernel, sm_count() * 8, PP_BLOCK, 0, as_stream(stream), (const int*)w.meta,
+           (const int4*)pairs, (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, cull_d2, dx_fix,
+           nc, status, conv, iter);
+    return check_launch("pairs_project_kernel");
+}
+
+extern "C" int sx_contact_apply(int n_dy, float* y4, const float* fixed, long long* dx_fix, int* nc, const int* conv,
+                                int iter, void* stream) {
+    SX_REQUIRE(n_dy >= 0, "sx_contact_apply: bad size");
+    if (n_dy == 0) return SX_OK;
+    SX_REQUIRE(y4 && fixed && dx_fix && nc, "sx_contact_apply: null pointer");
+    launch(collision_apply_kernel, conv ? capped_grid(collision_apply_kernel, n_dy, 256) : grid_for(n_dy, 256), 256, 0,
+           as_stream(stream), n_dy, (float4*)y4, fixed, dx_fix, nc, conv, iter);
+    return check_launch("collision_apply_kernel");
+}
+
 extern "C" int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4,
                                       const float* xs4, const float* fixed, const float* m_inv, float dHat,
                                       float compliance, float cull_d2, long long* dx_fix, int* nc, int* status,
                                       const int* conv, int iter, void* stream) {
-    SX_REQUIRE(n_dy >= 0 && n_st >= 0, "sx_contact_pairs_sweep: bad sizes");
-    if (n_dy == 0) return SX_OK;
-    SX_REQUIRE(pairs && ws && y4 && fixed && m_inv && dx_fix && nc && status, "sx_contact_pairs_sweep: null pointer");
-    SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_sweep: null static positions");
-    cudaStream_t s = as_stream(stream);
-    PairsWs w = pairs_ws(const_cast<void*>(ws), n_dy, n_st);
-    launch(pairs_project_kernel, sm_count() * 8, PP_BLOCK, 0, s, (const int*)w.meta, (const int4*)pairs,
-           (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, cull_d2, dx_fix, nc, status, conv,
-           iter);
-    int rc = check_launch("pairs_project_kernel");
+    const int rc = sx_contact_pairs_project(n_dy, n_st, pairs, ws, y4, xs4, fixed, m_inv, dHat, compliance, cull_d2,
+                                            dx_fix, nc, status, conv, iter, stream);
     if (rc) return rc;
-    launch(collision_apply_kernel, conv ? capped_grid(collision_apply_kernel, n_dy, 256) : grid_for(n_dy, 256), 256, 0,
-           s, n_dy, (float4*)y4, fixed, dx_fix, nc, conv, iter);
-    return check_launch("collision_apply_kernel");
+    return sx_contact_apply(n_dy, y4, fixed, dx_fix, nc, conv, iter, stream);
 }
 
 extern "C" int sx_segment_aabbs(const float* p4, const int* seg_ptr, int n_seg, float padding, float* box6,
