@@ -42,6 +42,7 @@ extern "C" {
 #define SX_STATUS_STACK_OVERFLOW 2 /* a traversal stack (64 entries) overflowed     */
 #define SX_STATUS_FIXED_RANGE 4    /* a contact term was NaN or out of fixed range  */
 #define SX_STATUS_CLIMB_LIMIT 8    /* a bottom-up refit walk exceeded n steps        */
+#define SX_STATUS_WAIT_TIMEOUT 16  /* a bounded device-side wait gave up             */
 
 int sx_version(void);
 const char* sx_last_error(void);
@@ -399,6 +400,12 @@ int sx_warm_features(const float* x4, const float* y4, const float* c4, const fl
                      void* feat, float* y_pred4, void* stream);
 /* out4[n][4] (columns 0..2 used) = MLP(feat) */
 int sx_mlp_forward(const void* feat, int n_rows, const void* w16, const float* p32, float* out4, void* stream);
+/* The same network on tcgen05 tensor cores (128-row tiles, accumulators in
+ * tensor memory); same outputs up to the order of FP32 accumulation and the
+ * bias being added after the products.  A device-side wait that gives up
+ * (1 s) sets SX_STATUS_WAIT_TIMEOUT in status. */
+int sx_mlp_forward_tc(const void* feat, int n_rows, const void* w16, const float* p32, float* out4, int* status,
+                      void* stream);
 /* y4 = y_pred4 + fixed * (Lref * out4[:, :3]) */
 int sx_warm_apply(const float* y_pred4, const float* out4, const float* fixed, const float* Lref, int n_verts,
                   float* y4, void* stream);

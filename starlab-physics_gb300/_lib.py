@@ -79,6 +79,7 @@ SIGNATURES = {
     "sx_mlp_bf16_count": ([], I),
     "sx_warm_features": ([P, P, P, P, P, P, P, I, F, F, F, F, P, P, P], I),
     "sx_mlp_forward": ([P, I, P, P, P, P], I),
+    "sx_mlp_forward_tc": ([P, I, P, P, P, P, P], I),
     "sx_warm_apply": ([P, P, P, P, I, P, P], I),
     "sx_warm_select": ([P, P, P, P, I, P, P], I),
     "sx_warm_record": ([P, P, P, P, I, P, P, P], I),

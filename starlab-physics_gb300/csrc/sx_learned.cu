@@ -327,6 +327,243 @@ __global__ void __launch_bounds__(MLP_BLOCK) mlp_forward_kernel(int V, const uns
 }
 
 // ---------------------------------------------------------------------------
+// Inference on the 5th-generation tensor cores (tcgen05).  One CTA of 256
+// threads takes 128 rows at a time (M = 128; two threads per row, one per
+// half of the 64 hidden columns): the rows' features, the hidden
+// activations and the three weight matrices sit in shared memory in the
+// canonical no-swizzle K-major layout (8 x 16-byte core matrices; LBO = 128 B
+// between core matrices along K, SBO = (K / 8) x 128 B between 8-row groups);
+// thread 0 issues tcgen05.mma (kind::f16, BF16 x BF16 -> FP32) into tensor
+// memory, whose completion tcgen05.commit signals on an mbarrier; each warp
+// then reads its 32 rows of the accumulator with tcgen05.ld, adds the bias,
+// applies SiLU, and writes the next layer's BF16 operand.  Layer 3 is N = 16
+// (W3's 8 rows and 8 zero rows); 128 tensor-memory columns per CTA (D1 at 0,
+// D2 at 64, D3 at 0 once D1 is read).  Every wait is bounded (1 s of global time);
+// a wait that gives up sets SX_STATUS_WAIT_TIMEOUT, waits once more (bounded)
+// for the MMAs in flight, frees the tensor memory and ends the kernel.
+// ---------------------------------------------------------------------------
+constexpr int TC_ROWS = 128;
+constexpr int TC_THREADS = 256;  // warp w reads tensor-memory lanes 32 (w % 4).., columns half w / 4
+constexpr int TC_TMEM_COLS = 128;  // D1 at column 0, D2 at 64, D3 at 0 (D1 is read by then)
+constexpr int TC_PAD_SMEM = 12 * 1024;  // with the 39.5 KB static: 4 CTAs per SM fit, 5 do not
+
+struct TcSmem {
+    alignas(128) unsigned short A1[TC_ROWS * kFeat];
+    alignas(128) unsigned short A2[TC_ROWS * kHid];
+    alignas(128) unsigned short B1[kHid * kFeat];
+    alignas(128) unsigned short B2[kHid * kHid];
+    alignas(128) unsigned short B3[16 * kHid];
+    float b1[kHid], b2[kHid], b3[16];
+    alignas(8) unsigned long long bar;
+    unsigned tmem_base;
+};
+
+// element (r, k) of a K-major operand with K columns, canonical layout
+__device__ __forceinline__ int canon(int r, int k, int K) {
+    return ((r >> 3) * (K >> 3) + (k >> 3)) * 64 + (r & 7) * 8 + (k & 7);
+}
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+// shared-memory matrix descriptor: start, LBO, SBO (16-byte units), version 1, no swizzle
+__device__ __forceinline__ unsigned long long umma_sdesc(unsigned saddr, unsigned lbo, unsigned sbo) {
+    return (unsigned long long)((saddr >> 4) & 0x3FFFu) | ((unsigned long long)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((unsigned long long)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// instruction descriptor, kind::f16: D F32, A and B BF16, both K-major
+__host__ __device__ constexpr unsigned umma_idesc_bf16(int M, int N) {
+    return (1u << 4) | (1u << 7) | (1u << 10) | ((unsigned)(N >> 3) << 17) | ((unsigned)(M >> 4) << 24);
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void umma_bf16(unsigned d_tmem, unsigned long long a, unsigned long long b, unsigned idesc,
+                                          unsigned accum) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+        "l"(a), "l"(b), "r"(idesc), "r"(accum)
+        : "memory");
+}
+__device__ __forceinline__ void umma_commit(unsigned bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_test(unsigned bar, unsigned parity) {
+    unsigned done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return done != 0u;
+}
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ bool mbar_wait_bounded(unsigned bar, unsigned parity) {
+    const unsigned long long t0 = global_ns();
+    while (!mbar_test(bar, parity))
+        if (global_ns() - t0 > 1000000000ull) return false;
+    return true;
+}
+__device__ __forceinline__ void tmem_ld32(unsigned taddr, unsigned (&r)[32]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+                 : "r"(taddr)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&r)[16]) {
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+                 : "r"(taddr)
+                 : "memory");
+}
+__device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
+
+// SiLU with the fast exponential and division: the tensor-core path's hidden
+// activations are rounded to BF16, far coarser than these approximations
+__device__ __forceinline__ float silu_fast(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
+
+// 32 accumulator columns of this thread's row (at taddr) + bias -> SiLU ->
+// BF16 columns [c0, c0 + 32) of row `row` of A2
+__device__ __forceinline__ void tc_hidden_half(unsigned taddr, const float* bias, unsigned short* A2, int row, int c0) {
+    unsigned r[32];
+    tmem_ld32(taddr, r);
+    tmem_wait_ld();
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        uint4 v;
+        unsigned* pv = reinterpret_cast<unsigned*>(&v);
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const int c = 8 * q + 2 * e;
+            pv[e] = pack_bf2(silu_fast(__uint_as_float(r[c]) + bias[c0 + c]),
+                             silu_fast(__uint_as_float(r[c + 1]) + bias[c0 + c + 1]));
+        }
+        *reinterpret_cast<uint4*>(A2 + canon(row, c0 + 8 * q, kHid)) = v;
+    }
+}
+
+__global__ void __launch_bounds__(TC_THREADS, 1) mlp_forward_tc_kernel(int V, const unsigned short* __restrict__ feat,
+                                                                    const unsigned short* __restrict__ w16,
+                                                                    const float* __restrict__ p32,
+                                                                    float* __restrict__ out4, int* status) {
+    __shared__ TcSmem s;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    const int quad = warp & 3, half = warp >> 2;
+    const int trow = 32 * quad + lane;  // this thread's row within a tile
+    for (int i = tid; i < kHid * kFeat; i += TC_THREADS) s.B1[canon(i / kFeat, i % kFeat, kFeat)] = w16[qW1 + i];
+    for (int i = tid; i < kHid * kHid; i += TC_THREADS) s.B2[canon(i / kHid, i % kHid, kHid)] = w16[qW2 + i];
+    for (int i = tid; i < 16 * kHid; i += TC_THREADS) {
+        const int n = i / kHid, k = i % kHid;
+        s.B3[canon(n, k, kHid)] = n < kOut ? w16[qW3 + n * kHid + k] : (unsigned short)0;
+    }
+    for (int i = tid; i < kHid; i += TC_THREADS) {
+        s.b1[i] = p32[ob1 + i];
+        s.b2[i] = p32[ob2 + i];
+    }
+    if (tid < 16) s.b3[tid] = tid < kOut ? p32[ob3 + tid] : 0.0f;
+    const unsigned bar = smem_u32(&s.bar);
+    if (tid == 0) asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s.tmem_base)),
+                     "r"(TC_TMEM_COLS)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const unsigned tbase = s.tmem_base;
+    const unsigned lane_row = (unsigned)(32 * quad) << 16;  // this warp's 32 tensor-memory lanes
+    const unsigned long long dB1 = umma_sdesc(smem_u32(s.B1), 128, 512);
+    const unsigned long long dB2 = umma_sdesc(smem_u32(s.B2), 128, 1024);
+    const unsigned long long dB3 = umma_sdesc(smem_u32(s.B3), 128, 1024);
+    const unsigned long long dA1 = umma_sdesc(smem_u32(s.A1), 128, 512);
+    const unsigned long long dA2 = umma_sdesc(smem_u32(s.A2), 128, 1024);
+    constexpr unsigned id64 = umma_idesc_bf16(TC_ROWS, kHid), id16 = umma_idesc_bf16(TC_ROWS, 16);
+    unsigned phase = 0;
+    bool ok = true;
+    const int ntiles = (V + TC_ROWS - 1) / TC_ROWS;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int row = tile * TC_ROWS + trow;
+        // layer 1: features (BF16, 32 columns; half a row per thread) -> A1
+        uint4 f[2];
+#pragma unroll
+        for (int j = 0; j < 2; ++j)
+            f[j] = row < V ? __ldg(reinterpret_cast<const uint4*>(feat + (size_t)row * kFeat) + 2 * half + j)
+                           : make_uint4(0, 0, 0, 0);
+#pragma unroll
+        for (int j = 0; j < 2; ++j) *reinterpret_cast<uint4*>(s.A1 + canon(trow, 16 * half + 8 * j, kFeat)) = f[j];
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int ks = 0; ks < kFeat / 16; ++ks) umma_bf16(tbase, dA1 + 16 * ks, dB1 + 16 * ks, id64, ks);
+            umma_commit(bar);
+        }
+        ok = __syncthreads_and(mbar_wait_bounded(bar, phase));
+        if (!ok) break;
+        phase ^= 1u;
+        tc_fence_after();
+        tc_hidden_half(tbase + lane_row + 32 * half, s.b1, s.A2, trow, 32 * half);
+        // layer 2
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int ks = 0; ks < kHid / 16; ++ks) umma_bf16(tbase + 64, dA2 + 16 * ks, dB2 + 16 * ks, id64, ks);
+            umma_commit(bar);
+        }
+        ok = __syncthreads_and(mbar_wait_bounded(bar, phase));
+        if (!ok) break;
+        phase ^= 1u;
+        tc_fence_after();
+        tc_hidden_half(tbase + lane_row + 64 + 32 * half, s.b2, s.A2, trow, 32 * half);  // layer 2 is done with A2
+        // layer 3 (N = 16)
+        fence_async_smem();
+        tc_fence_before();
+        __syncthreads();
+        if (tid == 0) {
+            tc_fence_after();
+#pragma unroll
+            for (int ks = 0; ks < kHid / 16; ++ks) umma_bf16(tbase, dA2 + 16 * ks, dB3 + 16 * ks, id16, ks);
+            umma_commit(bar);
+        }
+        ok = __syncthreads_and(mbar_wait_bounded(bar, phase));
+        if (!ok) break;
+        phase ^= 1u;
+        tc_fence_after();
+        unsigned r[16];
+        tmem_ld16(tbase + lane_row, r);
+        tmem_wait_ld();
+        if (half == 0 && row < V)
+            *reinterpret_cast<float4*>(out4 + 4 * (size_t)row) =
+                make_float4(__uint_as_float(r[0]) + s.b3[0], __uint_as_float(r[1]) + s.b3[1],
+                            __uint_as_float(r[2]) + s.b3[2], __uint_as_float(r[3]) + s.b3[3]);
+        tc_fence_before();
+        __syncthreads();  // every row read before the next tile's MMAs reuse the accumulators
+    }
+    if (!ok) {
+        if (tid == 0) atomicOr(status, SX_STATUS_WAIT_TIMEOUT);
+        mbar_wait_bounded(bar, phase);  // the MMAs in flight, once more within the bound
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tbase), "r"(TC_TMEM_COLS)
+                     : "memory");
+}
+
+// ---------------------------------------------------------------------------
 // Training, part 1: forward + backward data path of a minibatch.  Rows are
 // idx[i] into the sample arrays (feat, target4 = (t, mask)).  Loss =
 // sum over rows and the 3 outputs of mask * (o - t)^2 / n_valid.  Writes per
@@ -699,6 +936,29 @@ extern "C" int sx_warm_select(const double* res_warm3, const double* res_cold3, 
     launch(warm_select_kernel, grid_for(n_verts, 256), 256, 0, as_stream(stream), n_verts, res_warm3, res_cold3,
            (const float4*)y_pred4, (float4*)y4, flags2);
     return check_launch("warm_select_kernel");
+}
+
+extern "C" int sx_mlp_forward_tc(const void* feat, int n_rows, const void* w16, const float* p32, float* out4,
+                                 int* status, void* stream) {
+    SX_REQUIRE(n_rows >= 0, "sx_mlp_forward_tc: n_rows < 0");
+    if (n_rows == 0) return SX_OK;
+    SX_REQUIRE(feat && w16 && p32 && out4 && status, "sx_mlp_forward_tc: null pointer");
+    const int tiles = (n_rows + TC_ROWS - 1) / TC_ROWS;
+    int dev = 0, sms = 0;
+    SX_CUDA(cudaGetDevice(&dev));
+    SX_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+    // four CTAs per SM share the SM's 512 tensor-memory columns; unused dynamic
+    // shared memory keeps a fifth from becoming resident and waiting in
+    // tcgen05.alloc for a column range
+    static bool attr = false;
+    if (!attr) {
+        SX_CUDA(cudaFuncSetAttribute(mlp_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_PAD_SMEM));
+        attr = true;
+    }
+    const int blocks = tiles < 4 * sms ? tiles : 4 * sms;
+    launch(mlp_forward_tc_kernel, blocks, TC_THREADS, TC_PAD_SMEM, as_stream(stream), n_rows,
+           (const unsigned short*)feat, (const unsigned short*)w16, p32, out4, status);
+    return check_launch("mlp_forward_tc_kernel");
 }
 
 extern "C" int sx_mlp_forward(const void* feat, int n_rows, const void* w16, const float* p32, float* out4,

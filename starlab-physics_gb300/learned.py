@@ -67,9 +67,15 @@ def mean_spring_rest(adj_ptr: np.ndarray, adj: np.ndarray) -> np.ndarray:
 
 
 class WarmStartMLP:
-    """Parameters, Adam state and the library calls of the warm-start MLP."""
+    """Parameters, Adam state and the library calls of the warm-start MLP.
 
-    def __init__(self, device="cuda", seed: int = 0, params: np.ndarray | None = None):
+    Inference runs on the tcgen05 tensor cores (``sx_mlp_forward_tc``: 128-row
+    tiles, accumulators in tensor memory) unless ``tcgen05`` is False, which
+    selects the mma.sync kernel (``sx_mlp_forward``) that training's forward
+    pass shares; the two agree to the BF16 rounding of the hidden activations.
+    """
+
+    def __init__(self, device="cuda", seed: int = 0, params: np.ndarray | None = None, tcgen05: bool = True):
         if int(sx.sx_mlp_param_count()) != N_PARAMS or int(sx.sx_mlp_bf16_count()) != N_BF16:
             raise RuntimeError("MLP layout of the library does not match")
         self.device = torch.device(device)
@@ -83,6 +89,8 @@ class WarmStartMLP:
         self.step = 0
         self._ws = None
         self._ws_rows = 0
+        self.tcgen05 = tcgen05
+        self.status = torch.zeros(1, dtype=torch.int32, device=self.device)  # SX_STATUS_* of the tcgen05 path
         self.sync()
 
     def sync(self):
@@ -90,7 +98,11 @@ class WarmStartMLP:
 
     def forward(self, feat: torch.Tensor, out4: torch.Tensor, n_rows: int | None = None):
         n = feat.shape[0] if n_rows is None else n_rows
-        sx.sx_mlp_forward(ptr(feat), n, ptr(self.w16), ptr(self.p32), ptr(out4), stream_handle())
+        if self.tcgen05:
+            sx.sx_mlp_forward_tc(ptr(feat), n, ptr(self.w16), ptr(self.p32), ptr(out4), ptr(self.status),
+                                 stream_handle())
+        else:
+            sx.sx_mlp_forward(ptr(feat), n, ptr(self.w16), ptr(self.p32), ptr(out4), stream_handle())
         return out4
 
     def _workspace(self, rows: int):

@@ -161,10 +161,11 @@ def _gpu_batch(po, rng, n):
 @pytest.mark.gpu
 @pytest.mark.parametrize("n", [16, 1000, 70001])
 def test_mlp_forward_matches_oracle(pkg, po, n):
+    """The mma.sync forward (shared with training) against the oracle."""
     rng = np.random.default_rng(n)
     u16, _, feat, _ = _gpu_batch(po, rng, n)
     p = _params(pkg, seed=n % 7)
-    mlp = pkg.WarmStartMLP(params=p)
+    mlp = pkg.WarmStartMLP(params=p, tcgen05=False)
     out = torch.full((n, 4), np.nan, dtype=torch.float32, device="cuda")
     mlp.forward(feat, out)
     got = out.cpu().numpy()
@@ -173,6 +174,37 @@ def test_mlp_forward_matches_oracle(pkg, po, n):
     assert np.abs(got[:, :3] - ref[:, :3]).max() <= 1e-2 * scale
     assert np.abs(got[:, :3] - ref[:, :3]).mean() <= 1e-3 * scale
     assert not got[:, 3].any()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [16, 129, 1000, 70001])
+def test_mlp_forward_tcgen05_matches(pkg, po, n):
+    """The tcgen05 forward (128-row tiles, accumulators in tensor memory)
+    against the oracle (same tolerance as the mma.sync forward) and against the
+    mma.sync forward (FP32 accumulation order and the bias step differ; the
+    BF16 hidden activations may round differently by one unit)."""
+    from starlab_physics_gb300._lib import ptr, stream_handle, sx
+
+    rng = np.random.default_rng(n + 1)
+    u16, _, feat, _ = _gpu_batch(po, rng, n)
+    p = _params(pkg, seed=n % 5)
+    mlp = pkg.WarmStartMLP(params=p, tcgen05=False)
+    ref_gpu = torch.full((n, 4), np.nan, dtype=torch.float32, device="cuda")
+    mlp.forward(feat, ref_gpu)
+    out = torch.full((n, 4), np.nan, dtype=torch.float32, device="cuda")
+    status = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert sx.sx_mlp_forward_tc(ptr(feat), n, ptr(mlp.w16), ptr(mlp.p32), ptr(out), ptr(status), stream_handle()) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    got = out.cpu().numpy()
+    ref = po.mlp_forward(u16, p)
+    scale = np.abs(ref[:, :3]).max()
+    assert np.isfinite(got).all()
+    assert np.abs(got[:, :3] - ref[:, :3]).max() <= 1e-2 * scale
+    assert np.abs(got[:, :3] - ref[:, :3]).mean() <= 1e-3 * scale
+    assert not got[:, 3].any()
+    g2 = ref_gpu.cpu().numpy()
+    assert np.abs(got[:, :3] - g2[:, :3]).max() <= 1e-2 * scale
 
 
 @pytest.mark.gpu
