@@ -412,6 +412,32 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2, check_e
     val = L.evaluate_loss(mlp, vf, vt)
     zero_val = float(vt[:, :3].pow(2).sum(1).mean().item())
     del feat, tgt
+    # inference alone, eager launches: the validation rows repeated to a batch
+    # larger than L2, on the tcgen05 kernel and on the mma.sync kernel
+    big = torch.cat([vf] * 5)
+    n_big = big.shape[0]
+    out_big = torch.empty((n_big, 4), dtype=torch.float32, device="cuda")
+    flush_inf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    inf = {"rows": n_big, "flop_per_row": 2 * (24 * 64 + 64 * 64 + 64 * 3), "bytes_per_row": 64 + 16}
+    for name, tc in (("tcgen05", True), ("mma_sync", False)):
+        mlp.tcgen05 = tc
+        mlp.forward(big, out_big)
+        ts = []
+        for _ in range(5):
+            flush_inf.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            mlp.forward(big, out_big)
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        ms_inf = sorted(ts)[2]
+        inf[name] = {"us": round(ms_inf * 1e3, 1),
+                     "tflops": round(inf["flop_per_row"] * n_big / (ms_inf / 1e3) / 1e12, 1),
+                     "gbs": round(inf["bytes_per_row"] * n_big / (ms_inf / 1e3) / 1e9, 1)}
+    mlp.tcgen05 = True
+    inf["tcgen05_status"] = int(mlp.status.item())
+    del big, out_big, flush_inf
 
     def restore(warm=None):
         B.x4.copy_(snap[0])
@@ -436,7 +462,7 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2, check_e
                         "collect_s": round(collect_s, 2), "train_s": round(train_s, 2),
                         "train_loss_first": float(h1[:10].mean()), "train_loss_last": float(h2[-100:].mean()),
                         "val_loss_untrained": loss0, "val_loss": val, "val_loss_zero_prediction": zero_val},
-           "tolerance": tol, "calibration_residuals": [round(r, 9) for r in res]}
+           "inference": inf, "tolerance": tol, "calibration_residuals": [round(r, 9) for r in res]}
     for mode in ("plain", "learned"):
         restore()
         B.tol, B.n_iter, B.use_graph = tol, 4 * cal_iters, True
