@@ -70,6 +70,13 @@ int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out4, const fl
  * threads per block) for an autotuner; no counterpart in the reference.  All
  * variants give bit-identical results; variant 0 is the one sx_jacobi_sweep
  * uses. */
+/* Programmatic dependent launch for the library's kernels: each may be
+ * scheduled while its predecessor on the stream finishes, and waits on the
+ * device for the predecessor's results (griddepcontrol) before it touches
+ * memory.  Kernels recorded into a device-side loop body (sx_loop_begin ..
+ * sx_loop_end) are plain launches.  On by default; returns the previous
+ * setting.  Results do not depend on it. */
+int sx_set_programmatic_launch(int enable);
 int sx_jacobi_sweep_variants(void);
 int sx_jacobi_sweep_variant_info(int variant, int* g, int* block);
 int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,

@@ -38,6 +38,7 @@ SIGNATURES = {
     "sx_jacobi_sweep": ([P, P, P, P, P, P, I, F, F, I, P], I),
     "sx_jacobi_sweep_variants": ([], I),
     "sx_jacobi_sweep_variant_info": ([I, P, P], I),
+    "sx_set_programmatic_launch": ([I], I),
     "sx_jacobi_sweep_v": ([P, P, P, P, P, P, I, F, F, I, I, P], I),
     "sx_velocity_update": ([P, P, P, P, I, F, F, P], I),
     "sx_compute_velocity": ([P, P, P, P, I, F, F, P], I),

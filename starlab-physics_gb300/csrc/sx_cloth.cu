@@ -15,6 +15,17 @@ static std::atomic<long long> g_launches{0};
 
 void note_launch() { g_launches.fetch_add(1, std::memory_order_relaxed); }
 
+static int g_pdl = 1;
+static thread_local int g_pdl_suspend = 0;  // > 0 while a device-side loop body is recorded
+bool pdl_enabled() { return g_pdl != 0 && g_pdl_suspend == 0; }
+}  // namespace sx
+extern "C" int sx_set_programmatic_launch(int enable) {
+    const int prev = sx::g_pdl;
+    sx::g_pdl = enable ? 1 : 0;
+    return prev;
+}
+namespace sx {
+
 int resident_blocks_of(const void* kernel, int block) {
     static std::mutex mu;
     static const void* keys[64];
@@ -62,6 +73,7 @@ int check_launch(const char* what) {
 __global__ void predict_kernel(int V, const float4* __restrict__ x4, const float4* __restrict__ v4,
                                const float* __restrict__ fixed, float4* __restrict__ y4, float dt, float gx,
                                float gy, float gz) {
+    pdl_entry();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     float4 x = x4[i], v = v4[i];
@@ -136,6 +148,7 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
                                                                 const int2* __restrict__ adj, float ks, float kb,
                                                                 int bend_y, const int* conv, int iter,
                                                                 double* __restrict__ partial) {
+    pdl_entry();
     if (iteration_skipped(conv, iter)) return;  // grid-uniform
     static_assert(!CHECK || BLOCK == SW_BLOCK, "residual partials are per SW_BLOCK tile");
     const int ntiles = (V + BLOCK - 1) / BLOCK;
@@ -206,6 +219,7 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
 __global__ void sewing_gather_kernel(int n_sewn, const int* __restrict__ sewn, const int* __restrict__ sptr,
                                      const int* __restrict__ partner, const float4* __restrict__ y4,
                                      const float* __restrict__ fixed, float k, float4* __restrict__ out) {
+    pdl_entry();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n_sewn) return;
     const int v = sewn[i];
@@ -239,6 +253,7 @@ __global__ void sewing_gather_kernel(int n_sewn, const int* __restrict__ sewn, c
 
 __global__ void sewing_scatter_kernel(int n_sewn, const int* __restrict__ sewn, const float4* __restrict__ out,
                                       float4* __restrict__ y4) {
+    pdl_entry();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n_sewn) y4[sewn[i]] = out[i];
 }
@@ -249,6 +264,7 @@ __global__ void sewing_scatter_kernel(int n_sewn, const int* __restrict__ sewn, 
 __global__ void velocity_update_kernel(int V, float4* __restrict__ x4, const float4* __restrict__ y4,
                                        float4* __restrict__ v4, const float* __restrict__ fixed, float damping,
                                        float dt) {
+    pdl_entry();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     float4 x = x4[i], y = y4[i];
@@ -271,6 +287,7 @@ __global__ void velocity_update_kernel(int V, float4* __restrict__ x4, const flo
 __global__ void compute_velocity_kernel(int V, const float4* __restrict__ x4, const float4* __restrict__ y4,
                                         float4* __restrict__ v4, const float* __restrict__ fixed, float damping,
                                         float dt) {
+    pdl_entry();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     float4 x = x4[i], y = y4[i];
@@ -279,6 +296,7 @@ __global__ void compute_velocity_kernel(int V, const float4* __restrict__ x4, co
 }
 
 __global__ void update_x_kernel(int V, float4* __restrict__ x4, const float4* __restrict__ v4, float dt) {
+    pdl_entry();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= V) return;
     float4 x = x4[i], v = v4[i];
@@ -293,6 +311,7 @@ __global__ void update_x_kernel(int V, float4* __restrict__ x4, const float4* __
 // ---------------------------------------------------------------------------
 __global__ void face_aabb_kernel(int F, const float4* __restrict__ p4, const int* __restrict__ faces, float pad,
                                  float4* __restrict__ mn4, float4* __restrict__ mx4) {
+    pdl_entry();
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
     V3 a = mk(p4[faces[3 * f]]), b = mk(p4[faces[3 * f + 1]]), c = mk(p4[faces[3 * f + 2]]);
@@ -314,12 +333,14 @@ __device__ __forceinline__ float ord2f(unsigned u) {
 }
 
 __global__ void scene_aabb_init(unsigned* box) {
+    pdl_entry();
     int t = threadIdx.x;
     if (t < 3) box[t] = f2ord(1e5f);
     else if (t < 6) box[t] = f2ord(-1e5f);
 }
 
 __global__ void scene_aabb_reduce(int V, const float4* __restrict__ p4, unsigned* box) {
+    pdl_entry();
     float lo[3] = {1e5f, 1e5f, 1e5f}, hi[3] = {-1e5f, -1e5f, -1e5f};
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x) {
         float4 p = p4[i];
@@ -341,6 +362,7 @@ __global__ void scene_aabb_reduce(int V, const float4* __restrict__ p4, unsigned
 }
 
 __global__ void scene_aabb_finish(unsigned* box, float pad) {
+    pdl_entry();
     int t = threadIdx.x;
     if (t < 6) {
         float v = ord2f(box[t]);
@@ -505,6 +527,7 @@ __global__ void __launch_bounds__(SW_BLOCK) residual_partial_kernel(int V, const
                                                                  const int* __restrict__ ptr,
                                                                  const int2* __restrict__ adj,
                                                                  double* __restrict__ partial) {
+    pdl_entry();
     const int ntiles = (V + SW_BLOCK - 1) / SW_BLOCK;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int v = tile * SW_BLOCK + threadIdx.x;
@@ -536,6 +559,7 @@ __global__ void __launch_bounds__(RF_THREADS) residual_finish_kernel(int nb, con
                                                                      double* out3, int* conv, int iter,
                                                                      double tol2, const double* ref3,
                                                                      unsigned long long loop, int n_iter) {
+    pdl_entry();
     if (iteration_skipped(conv, iter)) return;
     __shared__ double wsum[RF_THREADS / 32];
     __shared__ bool last;
@@ -581,6 +605,7 @@ __global__ void __launch_bounds__(RF_THREADS) residual_finish_kernel(int nb, con
 }
 
 __global__ void convergence_begin_kernel(int* conv, int check_every, int reset_totals) {
+    pdl_entry();
     if (threadIdx.x != 0) return;
     conv[0] = -1;
     conv[2] = 0;
@@ -709,6 +734,7 @@ extern "C" int sx_loop_begin(void* stream, void* body_stream, unsigned long long
                                           cudaStreamCaptureModeRelaxed));
     *handle_out = (unsigned long long)h;
     *ctx_out = new LoopCtx{s, bs, node};
+    ++g_pdl_suspend;  // the body's kernels are plain launches
     return SX_OK;
 }
 
@@ -718,6 +744,7 @@ extern "C" int sx_loop_end(void* ctx) {
     cudaGraph_t body = nullptr;
     const cudaError_t e = cudaStreamEndCapture(c->body, &body);
     delete c;
+    if (g_pdl_suspend > 0) --g_pdl_suspend;
     if (e != cudaSuccess) return cuda_status(e, "sx_loop_end");
     return SX_OK;
 }

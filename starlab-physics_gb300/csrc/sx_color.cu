@@ -22,6 +22,7 @@ constexpr int kRoundsPerPoll = 16;
 static inline size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 
 __global__ void inc_count_kernel(int E, const int* __restrict__ edges, int* cnt) {
+    pdl_entry();
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     atomicAdd(cnt + edges[2 * e], 1);
@@ -30,6 +31,7 @@ __global__ void inc_count_kernel(int E, const int* __restrict__ edges, int* cnt)
 
 __global__ void inc_fill_kernel(int E, const int* __restrict__ edges, const int* __restrict__ ptr, int* cursor,
                                 int* inc) {
+    pdl_entry();
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     int a = edges[2 * e], b = edges[2 * e + 1];
@@ -38,6 +40,7 @@ __global__ void inc_fill_kernel(int E, const int* __restrict__ edges, const int*
 }
 
 __global__ void color_init_kernel(int E, int* color, unsigned* keys, int* ids) {
+    pdl_entry();
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     color[e] = -1;
@@ -46,6 +49,7 @@ __global__ void color_init_kernel(int E, int* color, unsigned* keys, int* ids) {
 
 __global__ void color_round_kernel(int E, const int* __restrict__ edges, const int* __restrict__ ptr,
                                    const int* __restrict__ inc, int max_colors, int* color, int* remaining) {
+    pdl_entry();
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     volatile int* vc = color;
@@ -75,6 +79,7 @@ __global__ void color_round_kernel(int E, const int* __restrict__ edges, const i
 }
 
 __global__ void color_hist_kernel(int E, const int* __restrict__ color, unsigned* keys, unsigned* hist) {
+    pdl_entry();
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
     keys[e] = (unsigned)color[e];
@@ -83,6 +88,7 @@ __global__ void color_hist_kernel(int E, const int* __restrict__ color, unsigned
 
 // exclusive scan of the colour histogram (max_colors <= 128) -> start offsets
 __global__ void color_prefix_kernel(int max_colors, const unsigned* hist, int* prefix) {
+    pdl_entry();
     if (threadIdx.x != 0) return;
     unsigned run = 0;
     for (int c = 0; c < max_colors; ++c) {
@@ -91,7 +97,8 @@ __global__ void color_prefix_kernel(int max_colors, const unsigned* hist, int* p
     }
 }
 
-__global__ void scan_excl_small(int n, int* data) {  // single thread; n = V+1 only for small V
+__global__ void scan_excl_small(int n, int* data) {
+    pdl_entry();  // single thread; n = V+1 only for small V
     if (threadIdx.x != 0) return;
     int run = 0;
     for (int i = 0; i < n; ++i) {
@@ -115,6 +122,7 @@ extern "C" size_t sx_color_workspace_bytes(int n_verts, int n_edges) {
 // exclusive scan of V+1 ints, reusing the radix-sort scan would need unsigned
 // layout; a block-wide scan keeps it simple.
 __global__ void scan_excl_block(int n, int* data) {
+    pdl_entry();
     __shared__ int s[1024];
     const int tid = threadIdx.x;
     const int per = (n + 1023) / 1024;

@@ -49,12 +49,39 @@ inline int resident_blocks(K kernel, int block) {
 }
 
 // Every kernel launch of the library goes through launch(), which counts it
-// (sx_kernel_launches() reports the running total for benchmarks).
+// (sx_kernel_launches() reports the running total for benchmarks) and, unless
+// switched off, makes it a programmatic dependent launch: the kernel may be
+// scheduled while the previous kernel on the stream is still finishing.
+// Every kernel of the library therefore starts with pdl_entry(), whose
+// griddepcontrol.wait returns once the previous grid has completed and its
+// writes are visible (before the kernel touches any memory), and whose
+// launch_dependents lets the kernel's own successor be scheduled early.
+// Launches recorded into the body of a device-side loop (sx_loop_begin ..
+// sx_loop_end) are plain launches.
 void note_launch();
-template <typename K, typename... A>
-inline void launch(K kernel, dim3 grid, dim3 block, size_t smem, cudaStream_t s, A... args) {
-    kernel<<<grid, block, smem, s>>>(args...);
+bool pdl_enabled();
+template <typename... KArgs, typename... A>
+inline void launch(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A... args) {
+    if (!pdl_enabled()) {
+        kernel<<<grid, block, smem, s>>>(args...);
+    } else {
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = grid;
+        cfg.blockDim = block;
+        cfg.dynamicSmemBytes = smem;
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        cudaLaunchKernelEx(&cfg, kernel, static_cast<KArgs>(args)...);
+    }
     note_launch();
+}
+__device__ __forceinline__ void pdl_entry() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
 // ---- float3 arithmetic with fixed evaluation order ----------------------------

@@ -335,6 +335,7 @@ __device__ __forceinline__ float ee_pair(V3 x0, V3 x1, V3 x2, V3 x3, float dHat,
 
 __global__ void edge_edge_classify_kernel(int n, const float* __restrict__ p12, float dHat, int* dtype, float* d,
                                           float* g12) {
+    pdl_entry();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const float* p = p12 + 12 * (size_t)i;
@@ -359,6 +360,7 @@ __global__ void __launch_bounds__(128) edge_edge_kernel(
     const float* __restrict__ fixed, const float* __restrict__ m_inv, float dHat, float compliance, int cap,
     const int* __restrict__ st_c, const int* __restrict__ st_n, const int* __restrict__ dy_c,
     const int* __restrict__ dy_n, long long* dx, int* nc, PairOut po, int* status, const int* conv, int iter) {
+    pdl_entry();
     if (iteration_skipped(conv, iter)) return;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 2 * Ed) return;
@@ -413,6 +415,7 @@ __global__ void __launch_bounds__(128) collision_project_kernel(
     const int* __restrict__ vt_st_n, const int* __restrict__ vt_dy_c, const int* __restrict__ vt_dy_n,
     const int* __restrict__ tv_st_c, const int* __restrict__ tv_st_n, long long* dx, int* nc, PairOut po,
     int* status) {
+    pdl_entry();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= 2 * Vd + Vs) return;
     int bad = 0;
@@ -521,6 +524,7 @@ __global__ void __launch_bounds__(PB) pairs_count_kernel(int Vd, int Vs, int cap
                                                           const int* __restrict__ vt_dy_c,
                                                           const int* __restrict__ vt_dy_n,
                                                           const int* __restrict__ tv_st_n, int* block_tot) {
+    pdl_entry();
     const int q = blockIdx.x * PB + threadIdx.x;
     const int c = q < 2 * Vd + Vs ? query_pairs(q, Vd, cap, faces_dy, vt_st_n, vt_dy_c, vt_dy_n, tv_st_n) : 0;
     int tot;
@@ -529,6 +533,7 @@ __global__ void __launch_bounds__(PB) pairs_count_kernel(int Vd, int Vs, int cap
 }
 
 __global__ void __launch_bounds__(1024) pairs_scan_kernel(int nb, int* block_tot) {
+    pdl_entry();
     __shared__ int s[1024];
     const int tid = threadIdx.x;
     const int per = (nb + 1023) / 1024;
@@ -560,6 +565,7 @@ __global__ void __launch_bounds__(PB) pairs_fill_kernel(int Vd, int Vs, int cap,
                                                          const int* __restrict__ tv_st_c,
                                                          const int* __restrict__ tv_st_n,
                                                          const int* __restrict__ block_off, int4* pairs, int* meta) {
+    pdl_entry();
     const int Q = 2 * Vd + Vs;
     const int q = blockIdx.x * PB + threadIdx.x;
     const int c = q < Q ? query_pairs(q, Vd, cap, faces_dy, vt_st_n, vt_dy_c, vt_dy_n, tv_st_n) : 0;
@@ -661,6 +667,7 @@ __global__ void __launch_bounds__(PP_BLOCK) pairs_project_kernel(const int* __re
                                                                  const float* __restrict__ m_inv, float dHat,
                                                                  float compliance, float cull_d2, long long* dx,
                                                                  int* nc, int* status, const int* conv, int iter) {
+    pdl_entry();
     if (iteration_skipped(conv, iter)) return;
     const PairCtx c{pairs, y4, xs4, fixed, m_inv, dHat, compliance, dx, nc, meta[0], meta[1]};
     const int P = meta[2];
@@ -702,6 +709,7 @@ __global__ void __launch_bounds__(PP_BLOCK) pairs_project_kernel(const int* __re
 // update_dx (XPBD.py:384-387) from the fixed-point accumulators; clears them.
 __global__ void collision_apply_kernel(int V, float4* __restrict__ y4, const float* __restrict__ fixed,
                                        long long* __restrict__ dx, int* __restrict__ nc, const int* conv, int iter) {
+    pdl_entry();
     if (iteration_skipped(conv, iter)) return;
     for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < V; v += gridDim.x * blockDim.x) {
         const int c = nc[v];
@@ -756,6 +764,7 @@ __device__ __forceinline__ float ord2f_c(unsigned u) {
 // with the reference's 1e5 initial bounds (meshTaichiWrapper.py:335-347).
 __global__ void __launch_bounds__(256) segment_aabb_kernel(const float4* __restrict__ p4, const int* __restrict__ seg,
                                                            float pad, float* __restrict__ box6) {
+    pdl_entry();
     const int s = blockIdx.x;
     float lo[3] = {1e5f, 1e5f, 1e5f}, hi[3] = {-1e5f, -1e5f, -1e5f};
     for (int i = seg[s] + threadIdx.x; i < seg[s + 1]; i += blockDim.x) {
@@ -794,6 +803,7 @@ __global__ void batched_vt_st_broad_kernel(int V, const float4* __restrict__ y4,
                                            const float* __restrict__ ob_box6, const int* __restrict__ ob_fptr,
                                            const float4* __restrict__ ob_fmin4, const float4* __restrict__ ob_fmax4,
                                            float pad, unsigned* __restrict__ vmask) {
+    pdl_entry();
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     const int inst = vinst[v];
@@ -814,6 +824,7 @@ __global__ void batched_tv_st_broad_kernel(int S, const float4* __restrict__ xs4
                                            const float4* __restrict__ cl_fmin4, const float4* __restrict__ cl_fmax4,
                                            float pad, int cap, int* __restrict__ cand, int* __restrict__ num,
                                            int* status) {
+    pdl_entry();
     const int w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (w >= S) return;
@@ -844,6 +855,7 @@ __global__ void __launch_bounds__(256) batched_contacts_kernel(
     const float4* __restrict__ xs4, const unsigned* __restrict__ vmask, const int* __restrict__ tv_cand,
     const int* __restrict__ tv_num, int cap, const int* __restrict__ cl_faces, float dHat, float compliance,
     long long* dx, int* nc, int* status, const int* conv, int iter) {
+    pdl_entry();
     if (iteration_skipped(conv, iter)) return;
     int bad = 0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < V + S; i += gridDim.x * blockDim.x) {
@@ -1087,6 +1099,7 @@ __global__ void __launch_bounds__(128) velocity_contact_kernel(
     const int* __restrict__ pair_num, const float4* __restrict__ v4, const float4* __restrict__ vs4,
     const float* __restrict__ fixed, const float* __restrict__ m_inv, const float* __restrict__ m_inv_st, float mu,
     long long* dv, int* nc, int* status) {
+    pdl_entry();
     const int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= 2 * Vd + Vs) return;
     int bad = 0;
@@ -1114,6 +1127,7 @@ __global__ void __launch_bounds__(128) velocity_contact_kernel(
 __global__ void velocity_apply_kernel(int V, float4* __restrict__ v4, const float* __restrict__ fixed,
                                       const float* __restrict__ m_inv, long long* __restrict__ dv,
                                       int* __restrict__ nc) {
+    pdl_entry();
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     const int cnt = nc[v];

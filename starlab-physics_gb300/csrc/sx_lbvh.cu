@@ -46,6 +46,7 @@ __device__ __forceinline__ V3 cell_center(int i, V3 cs, V3 lo) {
 }
 
 __global__ void cell_morton_kernel(unsigned* codes, int* ids) {
+    pdl_entry();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kNumCells) return;
     const float box[6] = {0.f, 0.f, 0.f, 1e3f, 1e3f, 1e3f};
@@ -57,6 +58,7 @@ __global__ void cell_morton_kernel(unsigned* codes, int* ids) {
 
 __global__ void face_morton_kernel(int F, const float4* __restrict__ mn4, const float4* __restrict__ mx4,
                                    const float* __restrict__ box6, unsigned* codes, int* ids) {
+    pdl_entry();
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     if (f >= F) return;
     V3 lo{box6[0], box6[1], box6[2]}, hi{box6[3], box6[4], box6[5]};
@@ -79,6 +81,7 @@ constexpr int RS_WARPS = RS_BLOCK / 32;
 
 __global__ void __launch_bounds__(RS_BLOCK) rs_upsweep(const unsigned* __restrict__ keys, int n, int shift,
                                                        unsigned* __restrict__ hist, int nblocks) {
+    pdl_entry();
     __shared__ unsigned cnt[256];
     const int tid = threadIdx.x;
     cnt[tid] = 0;
@@ -98,6 +101,7 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_upsweep(const unsigned* __restric
 // elements at a time (coalesced); a shuffle scan combines each group of 32 and
 // the warp chunk totals are scanned across warps in shared memory.
 __global__ void __launch_bounds__(1024) scan_single_block(unsigned* data, int n, int inclusive) {
+    pdl_entry();
     __shared__ unsigned wsum[32];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
     const int chunk = ((n + 31) / 32 + 31) / 32 * 32;
@@ -126,6 +130,7 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_scatter(const unsigned* __restric
                                                        const int* __restrict__ vin, unsigned* __restrict__ kout,
                                                        int* __restrict__ vout, int n, int shift,
                                                        const unsigned* __restrict__ hist, int nblocks) {
+    pdl_entry();
     __shared__ unsigned s_base[256];
     __shared__ unsigned s_wcnt[RS_WARPS][256];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -221,6 +226,7 @@ __device__ __forceinline__ int kdelta(int i, long long j, int n, const unsigned*
 
 __global__ void karras_kernel(int n, const unsigned* __restrict__ c, int tie, int* child_a, int* child_b,
                               int* range_l, int* range_r, int* parent) {
+    pdl_entry();
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) parent[0] = -1;
     if (i >= n - 1) return;
@@ -269,6 +275,7 @@ __global__ void karras_kernel(int n, const unsigned* __restrict__ c, int tie, in
 __global__ void face_cell_kernel(int F, const float4* __restrict__ mn4, const float4* __restrict__ mx4,
                                  const float* __restrict__ box6, unsigned* keys, int* ids, unsigned* counts,
                                  float* grid8) {
+    pdl_entry();
     int f = blockIdx.x * blockDim.x + threadIdx.x;
     V3 lo{box6[0], box6[1], box6[2]};
     V3 cs = cell_size_of(box6);
@@ -350,6 +357,7 @@ __global__ void __launch_bounds__(1024) cell_column_refit_kernel(
     const float* __restrict__ box6, const int* __restrict__ prefix, const int* __restrict__ sorted_face_ids,
     const float4* __restrict__ fmn4, const float4* __restrict__ fmx4, int* __restrict__ num_faces,
     float4* __restrict__ nmin4, float4* __restrict__ nmax4, float4* __restrict__ frec, float* grid8) {
+    pdl_entry();
     __shared__ NodeBox tree[64];  // [32 + k]: leaf k; [16 + k], [8 + k], ...: levels above
     __shared__ unsigned ext_bits[3];
     const int col = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -419,6 +427,7 @@ __global__ void __launch_bounds__(1024) cell_column_refit_kernel(
 __global__ void __launch_bounds__(1024) cell_top_refit_kernel(int* __restrict__ num_faces,
                                                               float4* __restrict__ nmin4,
                                                               float4* __restrict__ nmax4) {
+    pdl_entry();
     __shared__ float4 sa[kGridRes * kGridRes], sb[kGridRes * kGridRes];
     const int t = threadIdx.x;
     {
@@ -508,6 +517,7 @@ __global__ void __launch_bounds__(CT_BLOCK, 4) cell_traverse_kernel(
     const float4* __restrict__ nmin4, const float4* __restrict__ nmax4, const int* __restrict__ prefix,
     const float4* __restrict__ frec, int cap, int* __restrict__ cand, int* __restrict__ num, int* status,
     const int* __restrict__ edges) {
+    pdl_entry();
     // occupancy words: bit z of word x*32 + y = cell (x, y, z) holds faces
     __shared__ unsigned occ[kGridRes * kGridRes];
     const unsigned* gocc = reinterpret_cast<const unsigned*>(grid8) + kGridHeader;
@@ -614,6 +624,7 @@ __global__ void face_refit_kernel(int n, const int* __restrict__ sorted_ids, con
                                   const float4* __restrict__ fmx4, const int* __restrict__ child_a,
                                   const int* __restrict__ child_b, const int* __restrict__ parent, float4* nmin4,
                                   float4* nmax4, int* flags, int* status) {
+    pdl_entry();
     int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
     const int leaf = n - 1 + j, f = sorted_ids[j];
@@ -645,6 +656,7 @@ __global__ void __launch_bounds__(128) face_traverse_kernel(int n, int Q, const 
                                                             const float4* __restrict__ nmax4, int cap,
                                                             int* __restrict__ cand, int* __restrict__ num,
                                                             int* status) {
+    pdl_entry();
     int q = blockIdx.x * blockDim.x + threadIdx.x;
     if (q >= Q) return;
     V3 p = mk(p4[q]);

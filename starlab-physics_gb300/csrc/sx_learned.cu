@@ -79,6 +79,7 @@ __global__ void __launch_bounds__(256) warm_features_kernel(int V, const float4*
                                                             const float* __restrict__ Lref, float gx, float gy,
                                                             float gz, float dt, unsigned short* __restrict__ feat,
                                                             float4* __restrict__ ypred) {
+    pdl_entry();
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     const float4 ps = y4[v], xs = x4[v], cp = c4[v];
@@ -149,6 +150,7 @@ __global__ void __launch_bounds__(256) warm_features_kernel(int V, const float4*
 __global__ void warm_apply_kernel(int V, const float4* __restrict__ ypred, const float* __restrict__ out4,
                                   const float* __restrict__ fixed, const float* __restrict__ Lref,
                                   float4* __restrict__ y4) {
+    pdl_entry();
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     const float4 p = ypred[v];
@@ -165,6 +167,7 @@ __global__ void warm_apply_kernel(int V, const float4* __restrict__ ypred, const
 __global__ void warm_record_kernel(int V, const float4* __restrict__ y4, const float4* __restrict__ ypred,
                                    const float* __restrict__ fixed, const float* __restrict__ Lref,
                                    float4* __restrict__ c4, float4* __restrict__ target4) {
+    pdl_entry();
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= V) return;
     const float4 y = y4[v], p = ypred[v];
@@ -180,6 +183,7 @@ __global__ void warm_record_kernel(int V, const float4* __restrict__ y4, const f
 // the cold start y = y_pred; flag[0] counts fallbacks, flag[1] warm starts.
 __global__ void warm_select_kernel(int V, const double* __restrict__ res_warm, const double* __restrict__ res_cold,
                                    const float4* __restrict__ ypred, float4* __restrict__ y4, int* flag) {
+    pdl_entry();
     const bool cold = res_warm[2] > res_cold[2];
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v == 0) {
@@ -307,6 +311,7 @@ __global__ void __launch_bounds__(MLP_BLOCK) mlp_forward_kernel(int V, const uns
                                                                 const unsigned short* __restrict__ w16,
                                                                 const float* __restrict__ p32,
                                                                 float* __restrict__ out4) {
+    pdl_entry();
     __shared__ MlpSmem s;
     stage_weights(s, w16, p32);
     __syncthreads();
@@ -450,6 +455,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1) mlp_forward_tc_kernel(int V, co
                                                                     const unsigned short* __restrict__ w16,
                                                                     const float* __restrict__ p32,
                                                                     float* __restrict__ out4, int* status) {
+    pdl_entry();
     __shared__ TcSmem s;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     const int quad = warp & 3, half = warp >> 2;
@@ -601,6 +607,7 @@ __global__ void __launch_bounds__(MLP_BLOCK) mlp_train_fwd_bwd_kernel(int M, con
                                                                       float inv_valid,
                                                                       const unsigned short* __restrict__ w16,
                                                                       const float* __restrict__ p32, TrainBuf tb) {
+    pdl_entry();
     __shared__ MlpSmem s;
     __shared__ MlpSmemT st;
     stage_weights(s, w16, p32);
@@ -728,6 +735,7 @@ __global__ void __launch_bounds__(MLP_BLOCK) mlp_wgrad_kernel(int M, int rows_pe
                                                               const int* __restrict__ idx,
                                                               const unsigned short* __restrict__ feat,
                                                               TrainBuf tb, float* __restrict__ bpart) {
+    pdl_entry();
     __shared__ __align__(16) unsigned short X[WG_ROWS * SL], H1[WG_ROWS * SL], H2[WG_ROWS * SL],
         D1[WG_ROWS * SL], D2[WG_ROWS * SL], DO[WG_ROWS * SL];
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, g = lane >> 2, tig = lane & 3;
@@ -830,6 +838,7 @@ __global__ void __launch_bounds__(MLP_BLOCK) mlp_wgrad_kernel(int M, int rows_pe
 __global__ void mlp_reduce_kernel(int nblocks, const float* __restrict__ bpart, int nwarps,
                                   const float* __restrict__ wpart, float* __restrict__ grad,
                                   float* __restrict__ stats) {
+    pdl_entry();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i == 0) {
         float l = 0.0f;
@@ -861,6 +870,7 @@ __device__ __forceinline__ bool structural_zero(int i) {
 __global__ void mlp_adam_kernel(const float* __restrict__ grad, float* __restrict__ p32, float* __restrict__ m1,
                                 float* __restrict__ m2, unsigned short* __restrict__ w16, float lr, float beta1,
                                 float beta2, float eps, float bc1, float bc2) {
+    pdl_entry();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     float p = p32[i];
@@ -883,6 +893,7 @@ __global__ void mlp_adam_kernel(const float* __restrict__ grad, float* __restric
 }
 
 __global__ void mlp_sync_bf16_kernel(const float* __restrict__ p32, unsigned short* __restrict__ w16) {
+    pdl_entry();
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= kParams) return;
     if (i < ob1) w16[qW1 + (i - oW1)] = f2bf(p32[i]);
