@@ -154,6 +154,11 @@ int sx_update_x(float* x4, const float* v4, int n_verts, float dt, void* stream)
 /* computeAABB_faces, meshTaichiWrapper.py:351-365 (positions p4) */
 int sx_face_aabbs(const float* p4, const int* faces, int n_faces, float padding, float* aabb_min4,
                   float* aabb_max4, void* stream);
+/* The same, plus chunk boxes: chunk_min4/max4[c] (float4, ceil(n_faces / 32)
+ * of each) = the union of the padded boxes of faces 32c .. 32c+31, for broad
+ * phases that test chunks before faces (no counterpart in the reference). */
+int sx_face_aabbs_chunked(const float* p4, const int* faces, int n_faces, float padding, float* aabb_min4,
+                          float* aabb_max4, float* chunk_min4, float* chunk_max4, void* stream);
 
 /* computeAABB, meshTaichiWrapper.py:335-347: box6 (device) = vertex AABB +- padding.
  * The reference returns the box to the host; here it stays on the device. */
@@ -357,13 +362,15 @@ int sx_segment_aabbs(const float* p4, const int* seg_ptr, int n_seg, float paddi
  * s of instance svinst[s], tv_cand[s*cap..] lists its cloth faces in
  * [cl_fptr[inst], cl_fptr[inst+1]) (ascending, grid cl_box6[inst]).  These are
  * the candidate sets the reference's cell-BVH traversal returns.  At most 32
- * obstacle faces per instance. */
+ * obstacle faces per instance.  cl_cmin4/cl_cmax4: the cloth faces' chunk
+ * boxes (sx_face_aabbs_chunked); a chunk that misses the query is skipped
+ * whole, which leaves the candidate lists unchanged. */
 int sx_batched_obstacle_broadphase(int n_verts, const float* y4, const int* vinst, const float* ob_box6,
                                    const int* ob_fptr, const float* ob_fmin4, const float* ob_fmax4, float padding,
                                    unsigned* vmask, int n_ob_verts, const float* xs4, const int* svinst,
                                    const float* cl_box6, const int* cl_fptr, const float* cl_fmin4,
-                                   const float* cl_fmax4, int cap, int* tv_cand, int* tv_num, int* status,
-                                   void* stream);
+                                   const float* cl_fmax4, const float* cl_cmin4, const float* cl_cmax4, int cap,
+                                   int* tv_cand, int* tv_num, int* status, void* stream);
 
 /* __vt_st / __tv_st (collision_constraints_x.py:6-173) over those candidates,
  * fixed-point accumulation, then update_dx (XPBD.py:384-387). */

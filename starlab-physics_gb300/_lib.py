@@ -52,6 +52,7 @@ SIGNATURES = {
     "sx_loop_begin": ([P, P, P, P], I),
     "sx_loop_end": ([P], I),
     "sx_face_aabbs": ([P, P, I, F, P, P, P], I),
+    "sx_face_aabbs_chunked": ([P, P, I, F, P, P, P, P, P], I),
     "sx_scene_aabb": ([P, I, F, P, P], I),
     "sx_cell_bvh_workspace_bytes": ([I], Z),
     "sx_cell_bvh_init": ([P, P, P, P, P, P, P, P, Z, P], I),
@@ -74,7 +75,7 @@ SIGNATURES = {
     "sx_edge_edge_classify": ([I, P, F, P, P, P, P], I),
     "sx_cell_bvh_traverse_edges": ([P, I, P, F, P, P, P, P, P, P, I, P, P, P, P], I),
     "sx_segment_aabbs": ([P, P, I, F, P, P], I),
-    "sx_batched_obstacle_broadphase": ([I, P, P, P, P, P, P, F, P, I, P, P, P, P, P, P, I, P, P, P, P], I),
+    "sx_batched_obstacle_broadphase": ([I, P, P, P, P, P, P, F, P, I, P, P, P, P, P, P, P, P, I, P, P, P, P], I),
     "sx_batched_obstacle_contacts": ([I, P, P, P, P, P, P, P, P, I, P, P, I, P, F, F, P, P, P, P, I, P], I),
     "sx_mlp_param_count": ([], I),
     "sx_mlp_bf16_count": ([], I),

@@ -140,6 +140,9 @@ class BatchedSolver:
         self._y_other = torch.zeros_like(self.x4)
         self.v4 = torch.zeros_like(self.x4)
         self.fmin4 = torch.zeros((self.num_faces, 4), dtype=torch.float32, device=dev)
+        # boxes of 32-face chunks, for the obstacle broad phase
+        self.cmin4 = torch.zeros(((self.num_faces + 31) // 32, 4), dtype=torch.float32, device=dev)
+        self.cmax4 = torch.zeros_like(self.cmin4)
         self.fmax4 = torch.zeros_like(self.fmin4)
         self.cl_box6 = torch.zeros((self.n_instances, 6), dtype=torch.float32, device=dev)
         # obstacles: static; their face boxes and grids are computed once
@@ -188,8 +191,8 @@ class BatchedSolver:
     def substep(self, dt):
         s = stream_handle()
         # per-instance cloth grids and face boxes on x (the substep's BVH build)
-        sx.sx_face_aabbs(ptr(self.x4), ptr(self.faces), self.num_faces, self.padding, ptr(self.fmin4),
-                         ptr(self.fmax4), s)
+        sx.sx_face_aabbs_chunked(ptr(self.x4), ptr(self.faces), self.num_faces, self.padding, ptr(self.fmin4),
+                                 ptr(self.fmax4), ptr(self.cmin4), ptr(self.cmax4), s)
         sx.sx_segment_aabbs(ptr(self.x4), ptr(self.vptr), self.n_instances, self.padding, ptr(self.cl_box6), s)
         g = self.g
         sx.sx_predict(ptr(self.x4), ptr(self.v4), ptr(self.fixed), ptr(self.y4), self.num_verts, float(dt), g[0], g[1],
@@ -262,7 +265,8 @@ class BatchedSolver:
                 self.num_verts, ptr(self.y4), ptr(self.vinst), ptr(self.ob_box6), ptr(self.ob_fptr),
                 ptr(self.ob_fmin4), ptr(self.ob_fmax4), self.padding, ptr(self.vmask), self.n_ob_verts,
                 ptr(self.xs4), ptr(self.svinst), ptr(self.cl_box6), ptr(self.fptr), ptr(self.fmin4),
-                ptr(self.fmax4), self.cap, ptr(self.tv_cand), ptr(self.tv_num), ptr(self.status), s)
+                ptr(self.fmax4), ptr(self.cmin4), ptr(self.cmax4), self.cap, ptr(self.tv_cand), ptr(self.tv_num),
+                ptr(self.status), s)
         sx.sx_batched_obstacle_contacts(
             self.num_verts, ptr(self.y4), ptr(self.fixed), ptr(self.m_inv), ptr(self.vinst), ptr(self.ob_fptr),
             ptr(self.ob_faces), ptr(self.xs4), ptr(self.vmask), self.n_ob_verts, ptr(self.tv_cand),

@@ -309,15 +309,36 @@ __global__ void update_x_kernel(int V, float4* __restrict__ x4, const float4* __
 // ---------------------------------------------------------------------------
 // computeAABB_faces (meshTaichiWrapper.py:351-365)
 // ---------------------------------------------------------------------------
+// cmn4/cmx4 (optional): the union of the padded boxes of faces 32c .. 32c+31
+// (chunk c), for broad phases that test chunks before faces
 __global__ void face_aabb_kernel(int F, const float4* __restrict__ p4, const int* __restrict__ faces, float pad,
-                                 float4* __restrict__ mn4, float4* __restrict__ mx4) {
+                                 float4* __restrict__ mn4, float4* __restrict__ mx4, float4* __restrict__ cmn4,
+                                 float4* __restrict__ cmx4) {
     pdl_entry();
-    int f = blockIdx.x * blockDim.x + threadIdx.x;
-    if (f >= F) return;
-    V3 a = mk(p4[faces[3 * f]]), b = mk(p4[faces[3 * f + 1]]), c = mk(p4[faces[3 * f + 2]]);
-    V3 lo = vmin(vmin(a, b), c), hi = vmax(vmax(a, b), c);
-    mn4[f] = make_float4(lo.x - pad, lo.y - pad, lo.z - pad, 0.0f);
-    mx4[f] = make_float4(hi.x + pad, hi.y + pad, hi.z + pad, 0.0f);
+    const int f = blockIdx.x * blockDim.x + threadIdx.x;
+    V3 lo{INFINITY, INFINITY, INFINITY}, hi{-INFINITY, -INFINITY, -INFINITY};
+    if (f < F) {
+        const V3 a = mk(p4[faces[3 * f]]), b = mk(p4[faces[3 * f + 1]]), c = mk(p4[faces[3 * f + 2]]);
+        const V3 l = vmin(vmin(a, b), c), h = vmax(vmax(a, b), c);
+        lo = V3{l.x - pad, l.y - pad, l.z - pad};
+        hi = V3{h.x + pad, h.y + pad, h.z + pad};
+        mn4[f] = make_float4(lo.x, lo.y, lo.z, 0.0f);
+        mx4[f] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+    }
+    if (cmn4 != nullptr) {  // block size is a multiple of 32: warp w of the grid is chunk w
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            lo = vmin(lo, V3{__shfl_xor_sync(0xffffffffu, lo.x, o), __shfl_xor_sync(0xffffffffu, lo.y, o),
+                             __shfl_xor_sync(0xffffffffu, lo.z, o)});
+            hi = vmax(hi, V3{__shfl_xor_sync(0xffffffffu, hi.x, o), __shfl_xor_sync(0xffffffffu, hi.y, o),
+                             __shfl_xor_sync(0xffffffffu, hi.z, o)});
+        }
+        const int chunk = f >> 5;
+        if ((threadIdx.x & 31) == 0 && 32 * chunk < F) {
+            cmn4[chunk] = make_float4(lo.x, lo.y, lo.z, 0.0f);
+            cmx4[chunk] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+        }
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -491,8 +512,19 @@ extern "C" int sx_face_aabbs(const float* p4, const int* faces, int n_faces, flo
     SX_REQUIRE(n_faces >= 0, "sx_face_aabbs: n_faces < 0");
     if (n_faces == 0) return SX_OK;
     SX_REQUIRE(p4 && faces && aabb_min4 && aabb_max4, "sx_face_aabbs: null pointer");
-    launch(face_aabb_kernel, grid_for(n_faces, 256), 256, 0, as_stream(stream), 
-        n_faces, (const float4*)p4, faces, padding, (float4*)aabb_min4, (float4*)aabb_max4);
+    launch(face_aabb_kernel, grid_for(n_faces, 256), 256, 0, as_stream(stream), n_faces, (const float4*)p4, faces,
+           padding, (float4*)aabb_min4, (float4*)aabb_max4, (float4*)nullptr, (float4*)nullptr);
+    return check_launch("face_aabb_kernel");
+}
+
+extern "C" int sx_face_aabbs_chunked(const float* p4, const int* faces, int n_faces, float padding, float* aabb_min4,
+                                     float* aabb_max4, float* chunk_min4, float* chunk_max4, void* stream) {
+    SX_REQUIRE(n_faces >= 0, "sx_face_aabbs_chunked: n_faces < 0");
+    if (n_faces == 0) return SX_OK;
+    SX_REQUIRE(p4 && faces && aabb_min4 && aabb_max4 && chunk_min4 && chunk_max4,
+               "sx_face_aabbs_chunked: null pointer");
+    launch(face_aabb_kernel, grid_for(n_faces, 256), 256, 0, as_stream(stream), n_faces, (const float4*)p4, faces,
+           padding, (float4*)aabb_min4, (float4*)aabb_max4, (float4*)chunk_min4, (float4*)chunk_max4);
     return check_launch("face_aabb_kernel");
 }
 

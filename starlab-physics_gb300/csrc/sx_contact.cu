@@ -818,10 +818,14 @@ __global__ void batched_vt_st_broad_kernel(int V, const float4* __restrict__ y4,
     vmask[v] = m;
 }
 
-// one warp per obstacle vertex; candidates appended in ascending face order
+// one warp per obstacle vertex; candidates appended in ascending face order.
+// The lanes first test the boxes of 32 chunks of 32 faces (cl_cmin4/cmax4,
+// chunk c = faces 32c .. 32c+31, a superset of every face box in it), then
+// test the faces of the chunks that overlap, in order.
 __global__ void batched_tv_st_broad_kernel(int S, const float4* __restrict__ xs4, const int* __restrict__ svinst,
                                            const float* __restrict__ cl_box6, const int* __restrict__ cl_fptr,
                                            const float4* __restrict__ cl_fmin4, const float4* __restrict__ cl_fmax4,
+                                           const float4* __restrict__ cl_cmin4, const float4* __restrict__ cl_cmax4,
                                            float pad, int cap, int* __restrict__ cand, int* __restrict__ num,
                                            int* status) {
     pdl_entry();
@@ -834,13 +838,21 @@ __global__ void batched_tv_st_broad_kernel(int S, const float4* __restrict__ xs4
     int count = 0;
     if (!query_skipped(a, b, cl_box6 + 6 * inst)) {
         const int f0 = cl_fptr[inst], f1 = cl_fptr[inst + 1];
-        for (int base = f0; base < f1; base += 32) {
-            const int f = base + lane;
-            const bool hit = f < f1 && overlap(a, b, mk(cl_fmin4[f]), mk(cl_fmax4[f]));
-            const unsigned ball = __ballot_sync(0xffffffffu, hit);
-            const int slot = count + __popc(ball & ((1u << lane) - 1u));
-            if (hit && slot < cap) cand[(size_t)w * cap + slot] = f;
-            count += __popc(ball);
+        const int c0 = f0 >> 5, c1 = (f1 + 31) >> 5;  // chunks touching [f0, f1)
+        for (int cb = c0; cb < c1; cb += 32) {
+            const int c = cb + lane;
+            const bool near = c < c1 && overlap(a, b, mk(cl_cmin4[c]), mk(cl_cmax4[c]));
+            unsigned hits = __ballot_sync(0xffffffffu, near);
+            while (hits) {  // warp-uniform, ascending chunks
+                const int ch = cb + __ffs(hits) - 1;
+                hits &= hits - 1u;
+                const int f = 32 * ch + lane;
+                const bool hit = f >= f0 && f < f1 && overlap(a, b, mk(cl_fmin4[f]), mk(cl_fmax4[f]));
+                const unsigned ball = __ballot_sync(0xffffffffu, hit);
+                const int slot = count + __popc(ball & ((1u << lane) - 1u));
+                if (hit && slot < cap) cand[(size_t)w * cap + slot] = f;
+                count += __popc(ball);
+            }
         }
     }
     if (lane == 0) {
@@ -1317,12 +1329,14 @@ extern "C" int sx_batched_obstacle_broadphase(int n_verts, const float* y4, cons
                                               const int* ob_fptr, const float* ob_fmin4, const float* ob_fmax4,
                                               float padding, unsigned* vmask, int n_ob_verts, const float* xs4,
                                               const int* svinst, const float* cl_box6, const int* cl_fptr,
-                                              const float* cl_fmin4, const float* cl_fmax4, int cap, int* tv_cand,
-                                              int* tv_num, int* status, void* stream) {
+                                              const float* cl_fmin4, const float* cl_fmax4, const float* cl_cmin4,
+                                              const float* cl_cmax4, int cap, int* tv_cand, int* tv_num, int* status,
+                                              void* stream) {
     SX_REQUIRE(n_verts >= 0 && n_ob_verts >= 0 && cap >= 1, "sx_batched_obstacle_broadphase: bad sizes");
     SX_REQUIRE(y4 && vinst && ob_box6 && ob_fptr && ob_fmin4 && ob_fmax4 && vmask && status,
                "sx_batched_obstacle_broadphase: null pointer");
-    SX_REQUIRE(n_ob_verts == 0 || (xs4 && svinst && cl_box6 && cl_fptr && cl_fmin4 && cl_fmax4 && tv_cand && tv_num),
+    SX_REQUIRE(n_ob_verts == 0 || (xs4 && svinst && cl_box6 && cl_fptr && cl_fmin4 && cl_fmax4 && cl_cmin4 &&
+                                   cl_cmax4 && tv_cand && tv_num),
                "sx_batched_obstacle_broadphase: null obstacle-vertex pointer");
     cudaStream_t s = as_stream(stream);
     if (n_verts > 0)
@@ -1331,7 +1345,7 @@ extern "C" int sx_batched_obstacle_broadphase(int n_verts, const float* y4, cons
     if (n_ob_verts > 0)
         launch(batched_tv_st_broad_kernel, grid_for(32LL * n_ob_verts, 256), 256, 0, s, n_ob_verts,
                (const float4*)xs4, svinst, cl_box6, cl_fptr, (const float4*)cl_fmin4, (const float4*)cl_fmax4,
-               padding, cap, tv_cand, tv_num, status);
+               (const float4*)cl_cmin4, (const float4*)cl_cmax4, padding, cap, tv_cand, tv_num, status);
     return check_launch("sx_batched_obstacle_broadphase");
 }
 
