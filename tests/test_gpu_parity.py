@@ -584,3 +584,27 @@ def test_velocity_pass_solver_matches_oracle(pkg, po):
     assert not np.array_equal(orc.x4, plain.x4), "the velocity pass changed nothing"
     assert np.array_equal(_np(cl.x4)[:, :3], orc.x4[:, :3])
     assert np.array_equal(_np(cl.v4)[:, :3], orc.v4[:, :3])
+
+
+@pytest.mark.parametrize("use_graph", [False, True])
+def test_programmatic_launch_gives_the_same_frames(pkg, sxm, use_graph):
+    """Kernels launched as programmatic dependents (the default) give the same
+    frames as plain launches."""
+    lib = sxm.load()
+    res = []
+    prev = lib.sx_set_programmatic_launch(1)
+    try:
+        for pdl in (0, 1):
+            lib.sx_set_programmatic_launch(pdl)
+            scene = pkg.scenes.plain64(n=24, seed=9)
+            scene.n_iter = 6
+            sim = pkg.scenes.make_solver(scene, device=DEV)
+            sim.bending_on = "y"
+            sim.use_graph = use_graph
+            for _ in range(3):
+                sim.forward(scene.n_substeps)
+            torch.cuda.synchronize()
+            res.append((_np(sim.mesh_dy.x4), _np(sim.mesh_dy.v4)))
+    finally:
+        lib.sx_set_programmatic_launch(prev)
+    assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
