@@ -139,7 +139,9 @@ inline int tile_grid(K kernel, int n_verts) {
 // G: entries whose loads are issued together; BLOCK: threads (= vertices) per
 // tile.  Every (G, BLOCK) gives the same result; the residual partials of
 // CHECK assume BLOCK == SW_BLOCK.
-template <bool CHECK, int G = 2, int BLOCK = SW_BLOCK>
+// BY: bending pairs evaluated on y, fixed at compile time (the bend_y
+// argument is then ignored), which drops the per-entry x/y selection.
+template <bool CHECK, int G = 2, int BLOCK = SW_BLOCK, bool BY = false>
 __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
                                                                 const float4* __restrict__ yin,
                                                                 float4* __restrict__ yout,
@@ -166,7 +168,7 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
             for (int g = 0; g < G; ++g) a[g] = k0 + g < e ? __ldg(adj + k0 + g) : make_int2(0, 0);
 #pragma unroll
             for (int g = 0; g < G; ++g) {
-                const bool use_x = a[g].x < 0 && !bend_y;
+                const bool use_x = !BY && a[g].x < 0 && !bend_y;
                 o[g] = k0 + g < e ? __ldg((use_x ? x4 : yin) + (a[g].x & 0x7fffffff)) : ps;
             }
 #pragma unroll
@@ -174,7 +176,7 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
                 if (k0 + g >= e) break;
                 const bool bend = a[g].x < 0;
                 const float rest = __int_as_float(a[g].y);
-                const bool use_x = bend && !bend_y;
+                const bool use_x = !BY && bend && !bend_y;
                 const float4 self = use_x ? xs : ps;
                 const float kk = bend ? kb : ks;
                 const float ex = self.x - o[g].x, ey = self.y - o[g].y, ez = self.z - o[g].z;
@@ -416,26 +418,27 @@ extern "C" int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out
     if (n_verts == 0) return SX_OK;
     SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj, "sx_jacobi_sweep: null pointer");
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep: y_in4 and y_out4 must not alias");
-    launch(jacobi_sweep_kernel<false>, sweep_blocks(n_verts), SW_BLOCK, 0, as_stream(stream), n_verts,
-           (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
-           k_bend, bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr);
+    launch(bend_on_y ? jacobi_sweep_kernel<false, 2, SW_BLOCK, true> : jacobi_sweep_kernel<false>, sweep_blocks(n_verts),
+           SW_BLOCK, 0, as_stream(stream), n_verts, (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed,
+           adj_ptr, (const int2*)adj, k_spring, k_bend, bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr);
     return check_launch("jacobi_sweep_kernel");
 }
 
 // Launch configurations of the sweep for the autotuner: (entries per load
 // batch, threads per block).  All give bit-identical results.
 namespace sx {
+using SweepKernel = void (*)(int, const float4*, const float4*, float4*, const float*, const int*, const int2*, float,
+                            float, int, const int*, int, double*);
 struct SweepVariant {
     int g, block;
-    void (*kern)(int, const float4*, const float4*, float4*, const float*, const int*, const int2*, float, float,
-                 int, const int*, int, double*);
+    SweepKernel kern, kern_y;  // bending on x or y chosen at run time / bending on y
 };
+#define SX_SWEEP_VARIANT(G, B) {G, B, jacobi_sweep_kernel<false, G, B>, jacobi_sweep_kernel<false, G, B, true>}
 static const SweepVariant kSweepVariants[] = {
-    {2, 256, jacobi_sweep_kernel<false, 2, 256>}, {1, 256, jacobi_sweep_kernel<false, 1, 256>},
-    {4, 256, jacobi_sweep_kernel<false, 4, 256>}, {2, 128, jacobi_sweep_kernel<false, 2, 128>},
-    {2, 512, jacobi_sweep_kernel<false, 2, 512>}, {4, 128, jacobi_sweep_kernel<false, 4, 128>},
-    {1, 128, jacobi_sweep_kernel<false, 1, 128>}, {3, 256, jacobi_sweep_kernel<false, 3, 256>},
+    SX_SWEEP_VARIANT(2, 256), SX_SWEEP_VARIANT(1, 256), SX_SWEEP_VARIANT(4, 256), SX_SWEEP_VARIANT(2, 128),
+    SX_SWEEP_VARIANT(2, 512), SX_SWEEP_VARIANT(4, 128), SX_SWEEP_VARIANT(1, 128), SX_SWEEP_VARIANT(3, 256),
 };
+#undef SX_SWEEP_VARIANT
 constexpr int kNumSweepVariants = sizeof(kSweepVariants) / sizeof(kSweepVariants[0]);
 }  // namespace sx
 
@@ -457,7 +460,8 @@ extern "C" int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_o
     SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj, "sx_jacobi_sweep_v: null pointer");
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_v: y_in4 and y_out4 must not alias");
     const SweepVariant& sv = kSweepVariants[variant];
-    launch(sv.kern, grid_for(n_verts, sv.block), sv.block, 0, as_stream(stream), n_verts, (const float4*)x4,
+    launch(bend_on_y ? sv.kern_y : sv.kern, grid_for(n_verts, sv.block), sv.block, 0, as_stream(stream), n_verts,
+           (const float4*)x4,
            (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring, k_bend,
            bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr);
     return check_launch("jacobi_sweep_kernel");
@@ -710,16 +714,16 @@ extern "C" int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, floa
     const int* gate = loop ? nullptr : (const int*)conv;
     const int nb = sweep_blocks(n_verts);
     if (check) {
-        launch(jacobi_sweep_kernel<true>, gate ? tile_grid(jacobi_sweep_kernel<true>, n_verts) : sweep_blocks(n_verts),
-               SW_BLOCK, 0, s, n_verts,
+            constexpr auto kc = jacobi_sweep_kernel<true, 2, SW_BLOCK, true>;
+        launch(kc, gate ? tile_grid(kc, n_verts) : sweep_blocks(n_verts), SW_BLOCK, 0, s, n_verts,
                (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
                k_bend, 1, gate, iter, (double*)ws);
         int rc = check_launch("jacobi_sweep_kernel");
         if (rc) return rc;
         return residual_finish(n_verts, adj_ptr, ws, res3, conv, iter, tol, ref3, loop, n_iter, s);
     }
-    launch(jacobi_sweep_kernel<false>, gate ? tile_grid(jacobi_sweep_kernel<false>, n_verts) : sweep_blocks(n_verts),
-           SW_BLOCK, 0, s, n_verts,
+    constexpr auto kp = jacobi_sweep_kernel<false, 2, SW_BLOCK, true>;
+    launch(kp, gate ? tile_grid(kp, n_verts) : sweep_blocks(n_verts), SW_BLOCK, 0, s, n_verts,
            (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
            k_bend, 1, gate, iter, (double*)nullptr);
     return check_launch("jacobi_sweep_kernel");
