@@ -1490,6 +1490,12 @@ API int or_point_triangle(const float* p12, float* d_out, float* g12) {
     return dt;
 }
 
+// or_point_triangle over n quadruples (12 floats each): dtype[n], d[n], g12[12 n]
+API int or_point_triangles(int n, const float* p12, int32_t* dtype, float* d, float* g12) {
+    for (int i = 0; i < n; ++i) dtype[i] = or_point_triangle(p12 + 12 * (size_t)i, d + i, g12 + 12 * (size_t)i);
+    return 0;
+}
+
 // ---------------------------------------------------------------------------
 // Graph colouring (framework/utilities/graph_coloring.py)
 // ---------------------------------------------------------------------------

@@ -46,6 +46,7 @@ _SIGS = {
     "or_warm_features": [I, P, P, P, P, P, P, P, F, F, F, F, P],
     "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, I],
     "or_edge_edge_classify": [I, P, F, P, P, P],
+    "or_point_triangles": [I, P, P, P, P],
     "or_edge_edge_sweep": [I, P, P, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, I],
     "or_point_triangle": [P, P, P],
     "or_color_edges": [I, I, P, I, P, P, P],
@@ -244,6 +245,17 @@ def point_triangle(p, t0, t1, t2):
     g = np.zeros(12, np.float32)
     dt = lib().or_point_triangle(_p(buf), _p(d), _p(g))
     return dt, float(d[0]), g.reshape(4, 3)
+
+
+def point_triangles(p12):
+    """point_triangle over rows of 12 floats (p, t0, t1, t2): dtype, d, g[n, 4, 3]."""
+    p12 = np.ascontiguousarray(f32(p12).reshape(-1, 12))
+    n = p12.shape[0]
+    dt = np.zeros(n, np.int32)
+    d = np.zeros(n, np.float32)
+    g = np.zeros((n, 12), np.float32)
+    lib().or_point_triangles(n, _p(p12), _p(dt), _p(d), _p(g))
+    return dt, d, g.reshape(n, 4, 3)
 
 
 def collision_sweep(faces_dy, faces_st, y4, xs4, fixed, m_inv, dHat, compliance, cap, vt_st, vt_dy, tv_st,

@@ -1,0 +1,194 @@
+"""Golden vectors from the reference's own source -- TEST INFRASTRUCTURE ONLY.
+
+Runs functions of the reference (medialab-ku/starlab-physics, read from the
+directory given as the first argument) through ``taichi_standin`` (a numpy
+stand-in for the Taichi API: serial loops, IEEE float32 per operation) on
+seeded inputs and writes ``reference_vectors.npz`` beside this script:
+
+* ``pt_*``   distance.d_type_PT and the distance of the branch it selects
+             (d_PP / d_PE / d_PT, as collision_constraints_x.py calls them),
+             plus the reference's generated gradients (g_PP / g_PE / g_PT);
+* ``ee_*``   distance.d_type_EE and d_EE;
+* ``morton_*`` LBVH_CELL.morton_3d on points in and around the unit cube;
+* ``sub_*``  XPBD.Solver.compute_y, init_variables +
+             solve_spring_constraints_x + update_dx (one sweep per substep,
+             bending on x, the reference's substep) and compute_velocity +
+             update_x, for three substeps of a small pinned cloth.
+
+Usage: python tests/golden/make_reference_vectors.py <reference checkout>
+The npz is committed; the tests read it without the reference.
+"""
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+
+
+def point_triangle_vectors(ti, di, rng):
+    pts = []
+    for scale in (0.05, 2.0):
+        pts.append((rng.normal(size=(800, 12)) * scale).astype(np.float32))
+    # points near the triangle's plane and edges: region boundaries
+    tri = rng.normal(size=(1200, 9)).astype(np.float32)
+    w = rng.uniform(-0.2, 1.2, size=(1200, 3)).astype(np.float32)
+    w /= w.sum(1, keepdims=True)
+    p = (w[:, :1] * tri[:, 0:3] + w[:, 1:2] * tri[:, 3:6] + w[:, 2:3] * tri[:, 6:9]).astype(np.float32)
+    p += rng.normal(size=p.shape).astype(np.float32) * np.float32(1e-3)
+    pts.append(np.concatenate([p, tri], axis=1).astype(np.float32))
+    P = np.concatenate(pts)
+    n = P.shape[0]
+    dtype = np.zeros(n, np.int32)
+    d = np.zeros(n, np.float32)
+    g = np.zeros((n, 4, 3), np.float32)
+    for i in range(n):
+        x = [ti.math.vec3(P[i, 3 * k: 3 * k + 3]) for k in range(4)]
+        t = di.d_type_PT(*x)
+        dtype[i] = t
+        pair = {0: (0, 1), 1: (0, 2), 2: (0, 3)}
+        edge = {3: (0, 1, 2), 4: (0, 2, 3), 5: (0, 1, 3)}
+        if t in pair:
+            a, b = pair[t]
+            d[i] = di.d_PP(x[a], x[b])
+            ga, gb = di.g_PP(x[a], x[b])
+            g[i, a], g[i, b] = ga.to_numpy(), gb.to_numpy()
+        elif t in edge:
+            a, b, c = edge[t]
+            d[i] = di.d_PE(x[a], x[b], x[c])
+            ga, gb, gc = di.g_PE(x[a], x[b], x[c])
+            g[i, a], g[i, b], g[i, c] = ga.to_numpy(), gb.to_numpy(), gc.to_numpy()
+        else:
+            d[i] = di.d_PT(*x)
+            gg = di.g_PT(*x)
+            for k in range(4):
+                g[i, k] = gg[k].to_numpy()
+    return {"pt_points": P, "pt_dtype": dtype, "pt_d": d, "pt_g": g}
+
+
+def edge_edge_vectors(ti, di, rng):
+    P = np.concatenate([(rng.normal(size=(1000, 12)) * s).astype(np.float32) for s in (0.01, 0.1, 1.0)])
+    n = P.shape[0]
+    dtype = np.zeros(n, np.int32)
+    d = np.zeros(n, np.float32)
+    for i in range(n):
+        x = [ti.math.vec3(P[i, 3 * k: 3 * k + 3]) for k in range(4)]
+        dtype[i] = di.d_type_EE(*x)
+        d[i] = di.d_EE(*x) if dtype[i] == 8 else np.float32(0.0)
+    return {"ee_points": P, "ee_dtype": dtype, "ee_d": d}
+
+
+def morton_vectors(ti, lbvh_mod, rng):
+    L = object.__new__(lbvh_mod.LBVH_CELL)
+    pts = rng.uniform(-0.1, 1.1, size=(2000, 3)).astype(np.float32)
+    pts[:20] = np.array([[0, 0, 0], [1, 1, 1], [0.5, 0, 0], [0, 0.5, 0], [0, 0, 0.5], [0.999, 0.001, 0.5],
+                         [1023 / 1024, 0, 0], [1 / 1024, 1 / 1024, 1 / 1024]] + [[0.25, 0.5, 0.75]] * 12,
+                        np.float32)
+    codes = np.array([int(L.morton_3d(np.float32(x), np.float32(y), np.float32(z))) for x, y, z in pts], np.int64)
+    return {"morton_points": pts, "morton_codes": codes.astype(np.int32)}
+
+
+class _Verts:
+    """mesh.verts: named per-vertex fields, struct-for over vertices."""
+
+    def __init__(self, ti, n, **arrays):
+        self._n = n
+        for k, a in arrays.items():
+            a = np.ascontiguousarray(a)
+            object.__setattr__(self, k, ti.Field(a.copy(), a.shape[1] if a.ndim == 2 else None))
+
+    def __iter__(self):
+        for i in range(self._n):
+            yield _VRef(self, i)
+
+
+class _VRef:
+    def __init__(self, verts, i):
+        object.__setattr__(self, "_v", verts)
+        object.__setattr__(self, "id", i)
+
+    def __getattr__(self, k):
+        return getattr(self._v, k)[self.id]
+
+    def __setattr__(self, k, val):
+        getattr(self._v, k)[self.id] = val
+
+
+def substep_vectors(ti, xpbd_mod, repo_pkg):
+    mesh = repo_pkg.mesh
+    x, f = mesh.grid_cloth(7, height=1.0)
+    rng = np.random.default_rng(3)
+    x = (x + rng.uniform(-1e-3, 1e-3, size=x.shape)).astype(np.float32)
+    edges = mesh.edges_from_faces(f)
+    bend = mesh.bending_pairs(f)
+    l0 = mesh.rest_lengths(x, edges)
+    bl0 = mesh.rest_lengths(x, bend)
+    m_inv = mesh.inverse_masses(x.shape[0], edges, l0)
+    V = x.shape[0]
+    fixed = np.ones(V, np.float32)
+    fixed[[V - 7, V - 1]] = 0.0
+    v0 = (rng.normal(size=(V, 3)) * 0.05).astype(np.float32)
+    m = types.SimpleNamespace()
+    m.verts = _Verts(ti, V, x=x, y=x, v=v0, dx=np.zeros((V, 3), np.float32), nc=np.zeros(V, np.float32),
+                     fixed=fixed, m_inv=m_inv)
+    m.edges = types.SimpleNamespace(l0=ti.Field(l0.astype(np.float32).copy()))
+    m.edge_indices = ti.Field(edges.reshape(-1).astype(np.int32).copy())
+    m.bending_indices = ti.Field(bend.reshape(-1).astype(np.int32).copy())
+    m.bending_l0 = ti.Field(bl0.astype(np.float32).copy())
+    m.bending_constraint_count = bend.shape[0]
+    S = xpbd_mod.Solver
+    s = object.__new__(S)
+    s.mesh_dy = m
+    s.max_num_edges_dy = edges.shape[0]
+    s.g = ti.math.vec3(0.0, 0.0, -9.81)
+    stiff_stretch, stiff_bending = 1e5, 1e8   # reference arguments (springs use stiffness_bending)
+    s.stiffness_stretch, s.stiffness_bending = stiff_stretch, stiff_bending
+    dt_frame, n_sub, damping = 1.0 / 60.0, 3, 0.001
+    dt = dt_frame / n_sub
+    ys, xs, vs = [], [], []
+    for _ in range(n_sub):
+        S.compute_y(s, dt)
+        S.init_variables(s)
+        S.solve_spring_constraints_x(s, stiff_bending * dt * dt, stiff_stretch * dt * dt)
+        S.update_dx(s)
+        ys.append(m.verts.y.to_numpy())
+        S.compute_velocity(s, damping, dt)
+        S.update_x(s, dt)
+        xs.append(m.verts.x.to_numpy())
+        vs.append(m.verts.v.to_numpy())
+    return {"sub_x0": x, "sub_v0": v0, "sub_faces": f.astype(np.int32), "sub_fixed": fixed,
+            "sub_params": np.array([dt_frame, n_sub, damping, stiff_stretch, stiff_bending], np.float64),
+            "sub_y": np.stack(ys), "sub_x": np.stack(xs), "sub_v": np.stack(vs)}
+
+
+def main(ref_dir):
+    sys.path.insert(0, HERE)
+    import taichi_standin
+
+    ti = taichi_standin.install()
+    sys.path.insert(0, ref_dir)
+    import framework.collision.distance as di
+    import framework.collision.lbvh_cell as lbvh_mod
+    import framework.physics.XPBD as xpbd_mod
+
+    sys.path.insert(0, ROOT)
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    rng = np.random.default_rng(20240611)
+    out = {}
+    out.update(point_triangle_vectors(ti, di, rng))
+    out.update(edge_edge_vectors(ti, di, rng))
+    out.update(morton_vectors(ti, lbvh_mod, rng))
+    out.update(substep_vectors(ti, xpbd_mod, pkg))
+    path = os.path.join(HERE, "reference_vectors.npz")
+    np.savez_compressed(path, **out)
+    print("wrote", path, {k: v.shape for k, v in out.items()})
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("STARLAB_REFERENCE", "."))
