@@ -13,7 +13,9 @@ seeded inputs and writes ``reference_vectors.npz`` beside this script:
 * ``sub_*``  XPBD.Solver.compute_y, init_variables +
              solve_spring_constraints_x + update_dx (one sweep per substep,
              bending on x, the reference's substep) and compute_velocity +
-             update_x, for three substeps of a small pinned cloth.
+             update_x, for three substeps of a small pinned cloth;
+* ``lbvh_*`` LBVH_CELL.__init__ / build / traverse_cell_bvh_single on a
+             small drape (digests of the 32768-cell arrays, candidate lists).
 
 Usage: python tests/golden/make_reference_vectors.py <reference checkout>
 The npz is committed; the tests read it without the reference.
@@ -90,6 +92,62 @@ def morton_vectors(ti, lbvh_mod, rng):
                         np.float32)
     codes = np.array([int(L.morton_3d(np.float32(x), np.float32(y), np.float32(z))) for x, y, z in pts], np.int64)
     return {"morton_points": pts, "morton_codes": codes.astype(np.int32)}
+
+
+def _digest(a):
+    import hashlib
+
+    a = np.ascontiguousarray(a)
+    return np.frombuffer(hashlib.sha256(a.tobytes()).digest(), dtype=np.uint8).copy()
+
+
+class _Faces:
+    """mesh.faces: per-face AABB fields, struct-for over faces."""
+
+    def __init__(self, ti, mn, mx):
+        self.n = mn.shape[0]
+        self.aabb_min = ti.Field(np.ascontiguousarray(mn[:, :3]).copy(), 3)
+        self.aabb_max = ti.Field(np.ascontiguousarray(mx[:, :3]).copy(), 3)
+
+    def __iter__(self):
+        for i in range(self.n):
+            yield types.SimpleNamespace(id=i, aabb_min=self.aabb_min[i], aabb_max=self.aabb_max[i])
+
+
+def lbvh_vectors(ti, lbvh_mod, repo_pkg, po):
+    """LBVH_CELL.__init__ (cell codes, radix sort, Karras), build (face cells,
+    counting sort, leaves, refit) and traverse_cell_bvh_single for the vertex
+    boxes of a small drape.  The 32768-cell arrays are stored as SHA-256
+    digests of their bytes."""
+    sc = repo_pkg.scenes.drape256(n=12, sphere_subdiv=1)
+    x = sc.cloth_x.astype(np.float32)
+    f = sc.cloth_faces.astype(np.int32)
+    x4 = np.zeros((x.shape[0], 4), np.float32)
+    x4[:, :3] = x
+    pad = np.float32(0.01)
+    mn, mx = po.face_aabbs(x4, f, pad)
+    box6 = po.scene_aabb(x4, pad)
+    ref = lbvh_mod.LBVH_CELL(f.shape[0])
+    n = ref.cell_nodes
+    out = {"lbvh_init_digest": np.stack([_digest(ref.cell_morton_codes.a), _digest(ref.cell_ids.a),
+                                         _digest(n.child_a.a[:32767]), _digest(n.child_b.a[:32767]),
+                                         _digest(n.parent.a[1:]), _digest(n.range_l.a[:32767]),
+                                         _digest(n.range_r.a[:32767])])}
+    mesh = types.SimpleNamespace(faces=_Faces(ti, mn, mx))
+    ref.build(mesh, ti.math.vec3(box6[:3]), ti.math.vec3(box6[3:]))
+    out["lbvh_build_digest"] = np.stack([_digest(ref.prefix_sum_cell.a), _digest(ref.sorted_face_ids.a),
+                                         _digest(n.num_faces.a), _digest(n.aabb_min.a),
+                                         _digest(n.aabb_max.a)])
+    Q, cap = x.shape[0], 40
+    cache = ti.Field(np.full((Q, cap), -1, np.int32))
+    nums = ti.Field(np.zeros(Q, np.int32))
+    qmn, qmx = po.query_boxes(x4, pad)
+    for i in range(Q):
+        ref.traverse_cell_bvh_single(ref.cell_size, ref.origin, ti.math.vec3(qmn[i, :3]), ti.math.vec3(qmx[i, :3]),
+                                     i, cache, nums)
+    out.update(lbvh_x4=x4, lbvh_faces=f, lbvh_pad=np.array([pad], np.float32), lbvh_cand=cache.a.copy(),
+               lbvh_num=nums.a.copy(), lbvh_cell_size=np.array(ref.cell_size.c, np.float32))
+    return out
 
 
 class _Verts:
@@ -185,6 +243,9 @@ def main(ref_dir):
     out.update(edge_edge_vectors(ti, di, rng))
     out.update(morton_vectors(ti, lbvh_mod, rng))
     out.update(substep_vectors(ti, xpbd_mod, pkg))
+    from oracle import pyoracle as po
+
+    out.update(lbvh_vectors(ti, lbvh_mod, pkg, po))
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, {k: v.shape for k, v in out.items()})

@@ -25,8 +25,10 @@ arithmetic, not the last bits of a Taichi build.
 """
 from __future__ import annotations
 
+import ast
 import inspect
 import sys
+import textwrap
 import types as _pytypes
 
 import numpy as np
@@ -59,7 +61,77 @@ def _cast_scalar(v, t):
     return v
 
 
+def _atomic_field(op, f, idx, v):
+    """Atomic read-modify-write of a field element; returns the old value."""
+    old = f[idx]
+    if op == "add":
+        f[idx] = old + v
+    elif op == "sub":
+        f[idx] = old - v
+    elif op == "max":
+        f[idx] = old if old > v else v
+    else:
+        f[idx] = old if old < v else v
+    return old
+
+
+class _AtomicRewrite(ast.NodeTransformer):
+    """ti.atomic_op(name, v) on a local becomes an augmented assignment;
+    ti.atomic_op(field[i], v) becomes _atomic_field(op, field, i, v)."""
+
+    OPS = {"atomic_add": "add", "atomic_sub": "sub", "atomic_max": "max", "atomic_min": "min"}
+
+    @classmethod
+    def _is_atomic(cls, node):
+        return (isinstance(node, ast.Call) and isinstance(node.func, ast.Attribute)
+                and isinstance(node.func.value, ast.Name) and node.func.value.id == "ti"
+                and node.func.attr in cls.OPS)
+
+    def visit_Expr(self, node):
+        if self._is_atomic(node.value) and isinstance(node.value.args[0], ast.Name):
+            call = node.value
+            name = call.args[0].id
+            op = self.OPS[call.func.attr]
+            if op in ("add", "sub"):
+                return ast.copy_location(ast.AugAssign(target=ast.Name(name, ast.Store()),
+                                                       op=ast.Add() if op == "add" else ast.Sub(),
+                                                       value=call.args[1]), node)
+            fn = "max" if op == "max" else "min"
+            return ast.copy_location(ast.Assign(targets=[ast.Name(name, ast.Store())],
+                                                value=ast.Call(ast.Name(fn, ast.Load()),
+                                                               [ast.Name(name, ast.Load()), call.args[1]], [])),
+                                     node)
+        return self.generic_visit(node)
+
+    def visit_Call(self, node):
+        self.generic_visit(node)
+        if self._is_atomic(node) and isinstance(node.args[0], ast.Subscript):
+            sub = node.args[0]
+            return ast.copy_location(
+                ast.Call(ast.Attribute(ast.Name("ti", ast.Load()), "_atomic_field", ast.Load()),
+                         [ast.Constant(self.OPS[node.func.attr]), sub.value, sub.slice, node.args[1]], []), node)
+        return node
+
+
+def _rewrite(fn):
+    """The function recompiled with the atomics rewritten (see _AtomicRewrite)."""
+    try:
+        src = textwrap.dedent(inspect.getsource(fn))
+    except (OSError, TypeError):
+        return fn
+    if "atomic_" not in src:
+        return fn
+    tree = ast.parse(src)
+    fdef = tree.body[0]
+    fdef.decorator_list = []
+    tree = ast.fix_missing_locations(_AtomicRewrite().visit(tree))
+    ns = {}
+    exec(compile(tree, inspect.getsourcefile(fn) or "<reference>", "exec"), fn.__globals__, ns)
+    return ns[fdef.name]
+
+
 def kernel(fn):
+    fn = _rewrite(fn)
     sig = inspect.signature(fn)
 
     def run(*args, **kwargs):
@@ -75,14 +147,52 @@ def kernel(fn):
 
 
 def func(fn):
-    return fn
+    return _rewrite(fn)
 
 
 def data_oriented(cls):
     return cls
 
 
+def loop_config(*a, **k):
+    pass
+
+
+class StructField:
+    """Field of a ti.dataclass: one numpy array per member."""
+
+    def __init__(self, members, shape):
+        shape = (shape,) if np.isscalar(shape) else tuple(shape)
+        object.__setattr__(self, "_m", {})
+        for name, ann in members.items():
+            if ann is math.vec3:
+                self._m[name] = Field(np.zeros(shape + (3,), np.float32), 3)
+            else:
+                t = ann.np if isinstance(ann, _Type) and ann.np is not None else np.int32
+                self._m[name] = Field(np.zeros(shape, t))
+
+    def __getattr__(self, k):
+        return self._m[k]
+
+    def __getitem__(self, i):
+        return _StructRef(self, int(i))
+
+
+class _StructRef:
+    def __init__(self, sf, i):
+        object.__setattr__(self, "_sf", sf)
+        object.__setattr__(self, "_i", i)
+
+    def __getattr__(self, k):
+        return self._sf._m[k][self._i]
+
+    def __setattr__(self, k, v):
+        self._sf._m[k][self._i] = v
+
+
 def dataclass(cls):
+    members = dict(getattr(cls, "__annotations__", {}))
+    cls.field = staticmethod(lambda shape=(), **k: StructField(members, shape))
     return cls
 
 
@@ -108,10 +218,14 @@ def abs(x):  # noqa: A001
 
 
 def min(a, b):  # noqa: A001
+    if isinstance(a, Vec):
+        return Vec([x if x < y else y for x, y in zip(a.c, b.c)])
     return a if a < b else b
 
 
 def max(a, b):  # noqa: A001
+    if isinstance(a, Vec):
+        return Vec([x if x > y else y for x, y in zip(a.c, b.c)])
     return a if a > b else b
 
 
@@ -214,6 +328,11 @@ class Vec:
     def to_numpy(self):
         return np.array(self.c)
 
+    def cast(self, t):
+        if t is int or (isinstance(t, _Type) and t.np is not None and np.issubdtype(t.np, np.integer)):
+            return Vec([int(np.trunc(np.float64(x))) for x in self.c])
+        return Vec([_F(x) for x in self.c])
+
 
 class Mat:
     def __init__(self, rows):
@@ -266,6 +385,8 @@ def _vec_ctor(n, dtype=np.float32):
             comps = [args[0]] * n
         else:
             comps = list(args)
+        if dtype is int:
+            return Vec([int(c) for c in comps])
         return Vec([dtype(c) for c in comps])
 
     return make
@@ -279,10 +400,10 @@ def _mat_ctor(n):
 
 
 math = _pytypes.SimpleNamespace(
-    vec2=_vec_ctor(2), vec3=_vec_ctor(3), vec4=_vec_ctor(4), ivec2=_vec_ctor(2, np.int32),
-    ivec3=_vec_ctor(3, np.int32), mat2=_mat_ctor(2), mat3=_mat_ctor(3),
+    vec2=_vec_ctor(2), vec3=_vec_ctor(3), vec4=_vec_ctor(4), ivec2=_vec_ctor(2, int),
+    ivec3=_vec_ctor(3, int), mat2=_mat_ctor(2), mat3=_mat_ctor(3),
     clamp=lambda x, lo, hi: (lo if x < lo else (hi if x > hi else x)),
-    sqrt=sqrt, min=min, max=max, dot=lambda a, b: a.dot(b), cross=lambda a, b: a.cross(b),
+    sqrt=sqrt, min=lambda a, b: min(a, b), max=lambda a, b: max(a, b), dot=lambda a, b: a.dot(b), cross=lambda a, b: a.cross(b),
     normalize=lambda a: a.normalized(), length=lambda a: a.norm(),
     clz=lambda v: 32 - int(np.uint32(v)).bit_length(),
 )
@@ -301,7 +422,8 @@ class Field:
         else:
             i = int(i)
         if self.n is None:
-            return self.a[i]
+            v = self.a[i]
+            return int(v) if np.issubdtype(self.a.dtype, np.integer) else v
         return Vec(list(self.a[i]))
 
     def __setitem__(self, i, v):
@@ -316,6 +438,9 @@ class Field:
 
     def fill(self, v):
         self.a[...] = v
+
+    def copy_from(self, other):
+        self.a[...] = other.a
 
     def to_numpy(self):
         return self.a.copy()
@@ -341,11 +466,27 @@ class _VectorNS:
         return Field(np.zeros(shape + (n,), dtype=t), n)
 
     def __call__(self, comps, dt=None):
+        comps = list(comps)
+        if all(isinstance(c, int) for c in comps):
+            return Vec(comps)
         return Vec([_F(c) for c in comps])
 
 
 Vector = _VectorNS()
 Matrix = Mat
+
+
+class _PrefixSumExecutor:
+    """ti.algorithms.PrefixSumExecutor: inclusive prefix sum in place."""
+
+    def __init__(self, n):
+        self.n = n
+
+    def run(self, f):
+        f.a[...] = np.cumsum(f.a, dtype=np.int64).astype(f.a.dtype)
+
+
+algorithms = _pytypes.SimpleNamespace(PrefixSumExecutor=_PrefixSumExecutor)
 types = _pytypes.SimpleNamespace(ndarray=template, template=template, vector=lambda *a, **k: None,
                                  matrix=lambda *a, **k: None)
 

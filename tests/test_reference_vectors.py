@@ -67,3 +67,33 @@ def test_substeps_match_reference(pkg, po, R):
         po.velocity_update(x4, y4, v4, fixed, float(damping), dt)
         assert np.array_equal(x4[:, :3], R["sub_x"][s]), s
         assert np.array_equal(v4[:, :3], R["sub_v"][s]), s
+
+
+def _digest(a):
+    import hashlib
+
+    return np.frombuffer(hashlib.sha256(np.ascontiguousarray(a).tobytes()).digest(), dtype=np.uint8)
+
+
+def test_cell_bvh_matches_reference(po, R):
+    """LBVH_CELL: the cell codes and Karras topology of __init__, the build's
+    prefix sums, sorted faces, leaf/node boxes and face counts, and the
+    candidate lists of traverse_cell_bvh_single (order included)."""
+    b = po.CellBVH()
+    init = [b.codes, b.ids, b.child_a, b.child_b, b.parent[1:], b.range_l, b.range_r]
+    for k, a in enumerate(init):
+        assert np.array_equal(_digest(a.astype(np.int32)), R["lbvh_init_digest"][k]), k
+    x4, f, pad = R["lbvh_x4"], R["lbvh_faces"], R["lbvh_pad"][0]
+    mn, mx = po.face_aabbs(x4, f, pad)
+    b.build(mn, mx, po.scene_aabb(x4, pad))
+    assert np.array_equal(b.cell_size, R["lbvh_cell_size"])
+    built = [b.prefix, b.sorted_face_ids, b.num_faces, np.ascontiguousarray(b.nmin4[:, :3]),
+             np.ascontiguousarray(b.nmax4[:, :3])]
+    for k, a in enumerate(built):
+        assert np.array_equal(_digest(a), R["lbvh_build_digest"][k]), k
+    qmn, qmx = po.query_boxes(x4, pad)
+    cand, num, _ = b.traverse(qmn, qmx, R["lbvh_cand"].shape[1])
+    assert np.array_equal(num, R["lbvh_num"]) and num.sum() > 100
+    for q in range(num.shape[0]):
+        k = min(num[q], cand.shape[1])
+        assert np.array_equal(cand[q, :k], R["lbvh_cand"][q, :k]), q
