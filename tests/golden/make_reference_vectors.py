@@ -15,7 +15,10 @@ seeded inputs and writes ``reference_vectors.npz`` beside this script:
              bending on x, the reference's substep) and compute_velocity +
              update_x, for three substeps of a small pinned cloth;
 * ``lbvh_*`` LBVH_CELL.__init__ / build / traverse_cell_bvh_single on a
-             small drape (digests of the 32768-cell arrays, candidate lists).
+             small drape (digests of the 32768-cell arrays, candidate lists);
+* ``ct_*``   XPBD.Solver.solve_collision_constraints_x + update_dx (the
+             three vertex-triangle contact kinds, with the reference's own
+             gradients) on two cloth layers over a box.
 
 Usage: python tests/golden/make_reference_vectors.py <reference checkout>
 The npz is committed; the tests read it without the reference.
@@ -223,6 +226,77 @@ def substep_vectors(ti, xpbd_mod, repo_pkg):
             "sub_y": np.stack(ys), "sub_x": np.stack(xs), "sub_v": np.stack(vs)}
 
 
+def contact_vectors(ti, xpbd_mod, repo_pkg, po):
+    """XPBD.Solver.solve_collision_constraints_x (+ update_dx) on two coarse
+    cloth layers 1 cm apart lying 5 mm above a box: vertex-vs-static,
+    vertex-vs-own-cloth and static-vertex contacts, with the reference's
+    generated gradients.  Candidates come from the oracle's cell BVHs (pinned
+    above)."""
+    sc = repo_pkg.scenes.crossed_layers()
+    x = sc.cloth_x.astype(np.float32).copy()
+    nA = x.shape[0] // 2
+    x[:nA, 2] = np.float32(0.515)
+    x[nA:, 2] = np.float32(0.505)
+    rng = np.random.default_rng(7)
+    x[:, 2] += (rng.normal(size=x.shape[0]) * 2e-3).astype(np.float32)
+    f = sc.cloth_faces.astype(np.int32)
+    xs, fs = sc.obstacle_x.astype(np.float32), sc.obstacle_faces.astype(np.int32)
+    mesh = repo_pkg.mesh
+    edges = mesh.edges_from_faces(f)
+    l0 = mesh.rest_lengths(x, edges)
+    m_inv = mesh.inverse_masses(x.shape[0], edges, l0)
+    fixed = np.ones(x.shape[0], np.float32)
+    fixed[[0, nA + 5]] = 0.0
+    Vd, Vs, cap = x.shape[0], xs.shape[0], 40
+    pad, dHat, comp = np.float32(sc.padding), np.float32(sc.dHat), np.float32(1e8)
+    x4 = np.zeros((Vd, 4), np.float32)
+    x4[:, :3] = x
+    xs4 = np.zeros((Vs, 4), np.float32)
+    xs4[:, :3] = xs
+    bd, bs = po.CellBVH(), po.CellBVH()
+    mn, mx = po.face_aabbs(x4, f, pad)
+    bd.build(mn, mx, po.scene_aabb(x4, pad))
+    mn, mx = po.face_aabbs(xs4, fs, pad)
+    bs.build(mn, mx, po.scene_aabb(xs4, pad))
+    qd = po.query_boxes(x4, pad)
+    qs = po.query_boxes(xs4, pad)
+    vt_st = bs.traverse(*qd, cap)
+    vt_dy = bd.traverse(*qd, cap)
+    tv_st = bd.traverse(*qs, cap)
+    s = object.__new__(xpbd_mod.Solver)
+    md = types.SimpleNamespace()
+    md.verts = _Verts(ti, Vd, x=x, y=x, dx=np.zeros((Vd, 3), np.float32), nc=np.zeros(Vd, np.float32), fixed=fixed,
+                      m_inv=m_inv)
+    md.face_indices = ti.Field(f.reshape(-1).copy())
+    ms = types.SimpleNamespace()
+    ms.verts = _Verts(ti, Vs, x=xs, m_inv=np.ones(Vs, np.float32))
+    ms.face_indices = ti.Field(fs.reshape(-1).copy())
+    s.mesh_dy, s.mesh_st = md, ms
+    s.max_num_verts_dy, s.max_num_verts_st = Vd, Vs
+    s.dHat = dHat
+    s.vt_st_pair_cache_size = s.tv_st_pair_cache_size = s.vt_dy_pair_cache_size = cap
+    for name, (c, nm), Q in (("vt_st", vt_st[:2], Vd), ("vt_dy", vt_dy[:2], Vd), ("tv_st", tv_st[:2], Vs)):
+        setattr(s, name + "_candidates", ti.Field(c.copy()))
+        setattr(s, name + "_candidates_num", ti.Field(np.minimum(nm, cap).astype(np.int32)))
+        setattr(s, name + "_pair", ti.Field(np.zeros((Q, cap, 2), np.int32)))
+        setattr(s, name + "_pair_num", ti.Field(np.zeros(Q, np.int32)))
+        setattr(s, name + "_pair_g", ti.Field(np.zeros((Q, cap, 4, 3), np.float32), 3))
+        setattr(s, name + "_pair_schur", ti.Field(np.zeros((Q, cap), np.float32)))
+    xpbd_mod.Solver.solve_collision_constraints_x(s, comp)
+    dx = md.verts.dx.to_numpy()
+    nc = md.verts.nc.to_numpy()
+    xpbd_mod.Solver.update_dx(s)
+    out = {"ct_x4": x4, "ct_faces": f, "ct_xs4": xs4, "ct_faces_st": fs, "ct_fixed": fixed, "ct_m_inv": m_inv,
+           "ct_params": np.array([pad, dHat, comp, cap], np.float32), "ct_dx": dx, "ct_nc": nc,
+           "ct_y": md.verts.y.to_numpy()}
+    for name in ("vt_st", "vt_dy", "tv_st"):
+        out["ct_%s_pair" % name] = getattr(s, name + "_pair").a.copy()
+        out["ct_%s_pair_num" % name] = getattr(s, name + "_pair_num").a.copy()
+        out["ct_%s_pair_g" % name] = getattr(s, name + "_pair_g").a.copy()
+        out["ct_%s_pair_schur" % name] = getattr(s, name + "_pair_schur").a.copy()
+    return out
+
+
 def main(ref_dir):
     sys.path.insert(0, HERE)
     import taichi_standin
@@ -246,6 +320,7 @@ def main(ref_dir):
     from oracle import pyoracle as po
 
     out.update(lbvh_vectors(ti, lbvh_mod, pkg, po))
+    out.update(contact_vectors(ti, xpbd_mod, pkg, po))
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, {k: v.shape for k, v in out.items()})

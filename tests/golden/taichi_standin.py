@@ -114,12 +114,14 @@ class _AtomicRewrite(ast.NodeTransformer):
 
 
 def _rewrite(fn):
-    """The function recompiled with the atomics rewritten (see _AtomicRewrite)."""
+    """The function recompiled from its source outside any class (so that, as
+    in Taichi's own front end, names such as ``module.__vt_st`` are not
+    mangled), with the atomics rewritten (see _AtomicRewrite)."""
     try:
         src = textwrap.dedent(inspect.getsource(fn))
     except (OSError, TypeError):
         return fn
-    if "atomic_" not in src:
+    if "atomic_" not in src and "__" not in src.split(":", 1)[-1]:
         return fn
     tree = ast.parse(src)
     fdef = tree.body[0]

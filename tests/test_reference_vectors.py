@@ -97,3 +97,40 @@ def test_cell_bvh_matches_reference(po, R):
     for q in range(num.shape[0]):
         k = min(num[q], cand.shape[1])
         assert np.array_equal(cand[q, :k], R["lbvh_cand"][q, :k]), q
+
+
+def test_contacts_match_reference(po, R):
+    """solve_collision_constraints_x + update_dx of the reference on two cloth
+    layers over a box: the pair records of all three contact kinds (face and
+    region) equal the oracle's; gradients, Schur complements and the updated
+    positions agree to float32 rounding (the reference's generated gradient
+    expressions and our closed forms round differently; the reference sums
+    corrections in float, the oracle in fixed point)."""
+    x4, f, xs4, fs = R["ct_x4"], R["ct_faces"], R["ct_xs4"], R["ct_faces_st"]
+    pad, dHat, comp, cap = R["ct_params"]
+    cap = int(cap)
+    Vd, Vs = x4.shape[0], xs4.shape[0]
+    bd, bs = po.CellBVH(), po.CellBVH()
+    mn, mx = po.face_aabbs(x4, f, pad)
+    bd.build(mn, mx, po.scene_aabb(x4, pad))
+    mn, mx = po.face_aabbs(xs4, fs, pad)
+    bs.build(mn, mx, po.scene_aabb(xs4, pad))
+    qd, qs = po.query_boxes(x4, pad), po.query_boxes(xs4, pad)
+    vt_st, vt_dy, tv_st = bs.traverse(*qd, cap), bd.traverse(*qd, cap), bd.traverse(*qs, cap)
+    y4 = x4.copy()
+    r = po.collision_sweep(f, fs, y4, xs4, R["ct_fixed"], R["ct_m_inv"], np.float32(dHat), np.float32(comp), cap,
+                           vt_st[:2], vt_dy[:2], tv_st[:2], want_pairs=True)
+    blocks = {"vt_st": (0, Vd), "vt_dy": (Vd, 2 * Vd), "tv_st": (2 * Vd, 2 * Vd + Vs)}
+    for name, (a, b) in blocks.items():
+        pn = r["pair_num"][a:b]
+        assert np.array_equal(pn, R["ct_%s_pair_num" % name]), name
+        assert pn.sum() > 20, name
+        mask = np.arange(cap)[None, :] < pn[:, None]
+        assert np.array_equal(r["pair"][a:b][mask], R["ct_%s_pair" % name][mask]), name
+        g, rg = r["pair_g"][a:b, :, :, :3][mask], R["ct_%s_pair_g" % name][mask]
+        assert np.abs(g - rg).max() <= 1e-5 * np.abs(rg).max(), name
+        s, rs = r["pair_schur"][a:b][mask], R["ct_%s_pair_schur" % name][mask]
+        assert np.abs(s - rs).max() <= 1e-5 * np.abs(rs).max(), name
+    moved = np.abs(R["ct_y"] - x4[:, :3]).max()
+    assert moved > 1e-3
+    assert np.abs(y4[:, :3] - R["ct_y"]).max() <= 1e-5 * moved
