@@ -4,11 +4,14 @@
 // loaded only by tests/, by __graft_entry__.smoke() and by bench.py's CPU
 // baseline leg; the product path (the CUDA library) never calls it.
 //
-// Parity status: the reference (Python + Taichi 1.7.1) cannot run in this
-// environment, so nothing here is checked against reference outputs.  Each
-// function below restates the reference file:line it follows, and is pinned
-// against known-answer tests and brute-force checks in tests/ (parity against
-// the reference itself is "unpinned").
+// Parity status: the reference (Python + Taichi 1.7.1) runs here only through
+// a numpy stand-in for the Taichi API (serial loops, IEEE float32); its outputs
+// are committed as golden vectors (tests/golden/reference_vectors.npz) and this
+// library matches them bit for bit on classification, distances, Morton codes,
+// the cell BVH and the substep kernels, and to float32 rounding on contact
+// gradients, positions and velocities (contact records equal).  Each function
+// below restates the reference file:line it follows; known-answer tests and
+// brute-force checks in tests/ cover the rest.
 //
 // Numeric conventions shared with the CUDA kernels (documented, not taken from
 // the reference, whose Taichi build uses float atomics and fast math):

@@ -7,8 +7,13 @@ function follows) and provides :class:`OracleSolver`, which strings the pieces
 together exactly like ``Solver.forward`` (``framework/physics/XPBD.py:443-469``)
 with the iteration and rebuild options of the GPU solver.
 
-Parity status: unpinned against the reference itself (Taichi is not available);
-pinned by known-answer and brute-force checks in tests/.
+Parity status: pinned against the reference's own source, executed on the CPU
+through a numpy stand-in for the Taichi API (tests/golden/taichi_standin.py,
+tests/golden/make_reference_vectors.py -> tests/golden/reference_vectors.npz,
+checked by tests/test_reference_vectors.py): classification, distances, Morton
+codes, the cell BVH and the substep kernels bit for bit; contact records equal,
+contact gradients, positions and velocities to float32 rounding.  Known-answer
+and brute-force checks in tests/ cover the rest.
 """
 from __future__ import annotations
 

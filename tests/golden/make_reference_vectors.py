@@ -16,7 +16,8 @@ seeded inputs and writes ``reference_vectors.npz`` beside this script:
              update_x, for three substeps of a small pinned cloth;
 * ``lbvh_*`` LBVH_CELL.__init__ / build / traverse_cell_bvh_single on a
              small drape (digests of the 32768-cell arrays, candidate lists);
-* ``ct_*``   XPBD.Solver.solve_collision_constraints_x + update_dx (the
+* ``ct_*``   XPBD.Solver.solve_collision_constraints_x + update_dx, then
+             solve_constraints_v (friction + update_dv) (the
              three vertex-triangle contact kinds, with the reference's own
              gradients) on two cloth layers over a box.
 
@@ -265,11 +266,18 @@ def contact_vectors(ti, xpbd_mod, repo_pkg, po):
     tv_st = bd.traverse(*qs, cap)
     s = object.__new__(xpbd_mod.Solver)
     md = types.SimpleNamespace()
-    md.verts = _Verts(ti, Vd, x=x, y=x, dx=np.zeros((Vd, 3), np.float32), nc=np.zeros(Vd, np.float32), fixed=fixed,
-                      m_inv=m_inv)
+    v0 = (rng.normal(size=(Vd, 3)) * 0.3).astype(np.float32)
+    vs0 = (rng.normal(size=(Vs, 3)) * 0.05).astype(np.float32)
+    # the static mesh's inverse masses are read at a cloth vertex index in one
+    # branch of __vt_st (collision_constraints_v.py:68); padded with zeros past
+    # the static vertex count, the convention the oracle follows
+    ms_m_inv = np.zeros(max(Vd, Vs), np.float32)
+    ms_m_inv[:Vs] = 1.0
+    md.verts = _Verts(ti, Vd, x=x, y=x, v=v0, dx=np.zeros((Vd, 3), np.float32), dv=np.zeros((Vd, 3), np.float32),
+                      nc=np.zeros(Vd, np.float32), fixed=fixed, m_inv=m_inv)
     md.face_indices = ti.Field(f.reshape(-1).copy())
     ms = types.SimpleNamespace()
-    ms.verts = _Verts(ti, Vs, x=xs, m_inv=np.ones(Vs, np.float32))
+    ms.verts = _Verts(ti, Vs, x=xs, v=vs0, m_inv=ms_m_inv)
     ms.face_indices = ti.Field(fs.reshape(-1).copy())
     s.mesh_dy, s.mesh_st = md, ms
     s.max_num_verts_dy, s.max_num_verts_st = Vd, Vs
@@ -286,9 +294,15 @@ def contact_vectors(ti, xpbd_mod, repo_pkg, po):
     dx = md.verts.dx.to_numpy()
     nc = md.verts.nc.to_numpy()
     xpbd_mod.Solver.update_dx(s)
+    y = md.verts.y.to_numpy()
+    # the velocity pass (solve_constraints_v: reset dv/nc, friction over the
+    # pair records just made, update_dv)
+    s.mu = np.float32(0.8)
+    s.enable_collision_handling = True
+    xpbd_mod.Solver.solve_constraints_v(s)
     out = {"ct_x4": x4, "ct_faces": f, "ct_xs4": xs4, "ct_faces_st": fs, "ct_fixed": fixed, "ct_m_inv": m_inv,
-           "ct_params": np.array([pad, dHat, comp, cap], np.float32), "ct_dx": dx, "ct_nc": nc,
-           "ct_y": md.verts.y.to_numpy()}
+           "ct_params": np.array([pad, dHat, comp, cap], np.float32), "ct_dx": dx, "ct_nc": nc, "ct_y": y,
+           "ct_v0": v0, "ct_vs0": vs0, "ct_mu": np.array([s.mu], np.float32), "ct_v": md.verts.v.to_numpy()}
     for name in ("vt_st", "vt_dy", "tv_st"):
         out["ct_%s_pair" % name] = getattr(s, name + "_pair").a.copy()
         out["ct_%s_pair_num" % name] = getattr(s, name + "_pair_num").a.copy()

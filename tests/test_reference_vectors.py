@@ -134,3 +134,37 @@ def test_contacts_match_reference(po, R):
     moved = np.abs(R["ct_y"] - x4[:, :3]).max()
     assert moved > 1e-3
     assert np.abs(y4[:, :3] - R["ct_y"]).max() <= 1e-5 * moved
+
+
+def test_velocity_pass_matches_reference(po, R):
+    """solve_constraints_v of the reference (friction over the pair records of
+    the position pass, then update_dv) on the same scene: the oracle's
+    velocity pass over its own records gives the same velocities to float32
+    rounding (the gradients and Schur complements it reads differ from the
+    reference's in the last bits, see the test above)."""
+    x4, f, xs4, fs = R["ct_x4"], R["ct_faces"], R["ct_xs4"], R["ct_faces_st"]
+    pad, dHat, comp, cap = R["ct_params"]
+    cap = int(cap)
+    Vd, Vs = x4.shape[0], xs4.shape[0]
+    bd, bs = po.CellBVH(), po.CellBVH()
+    mn, mx = po.face_aabbs(x4, f, pad)
+    bd.build(mn, mx, po.scene_aabb(x4, pad))
+    mn, mx = po.face_aabbs(xs4, fs, pad)
+    bs.build(mn, mx, po.scene_aabb(xs4, pad))
+    qd, qs = po.query_boxes(x4, pad), po.query_boxes(xs4, pad)
+    vt_st, vt_dy, tv_st = bs.traverse(*qd, cap), bd.traverse(*qd, cap), bd.traverse(*qs, cap)
+    y4 = x4.copy()
+    r = po.collision_sweep(f, fs, y4, xs4, R["ct_fixed"], R["ct_m_inv"], np.float32(dHat), np.float32(comp), cap,
+                           vt_st[:2], vt_dy[:2], tv_st[:2], want_pairs=True)
+    v4 = np.zeros((Vd, 4), np.float32)
+    v4[:, :3] = R["ct_v0"]
+    vs4 = np.zeros((Vs, 4), np.float32)
+    vs4[:, :3] = R["ct_vs0"]
+    status = po.velocity_contacts(f, fs, cap, r, v4, vs4, R["ct_fixed"], R["ct_m_inv"], np.ones(Vs, np.float32),
+                                  float(R["ct_mu"][0]))
+    assert status == 0
+    changed = np.abs(R["ct_v"] - R["ct_v0"]).max(1) > 0
+    assert changed.sum() > 10
+    dv = np.abs(R["ct_v"] - R["ct_v0"]).max()
+    assert np.array_equal(np.abs(v4[:, :3] - R["ct_v0"]).max(1) > 0, changed)
+    assert np.abs(v4[:, :3] - R["ct_v"]).max() <= 1e-5 * max(dv, np.abs(R["ct_v"]).max())
