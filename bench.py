@@ -575,6 +575,10 @@ def main():
     from starlab_physics_gb300.autotune import variants as sweep_variants
 
     sweep_cfg = sweep_variants()[variant]
+    from starlab_physics_gb300.autotune import pairs_project_variants
+
+    pp_variants = pairs_project_variants()
+    pp_variant = sim.pairs_variant if sim.pairs_variant is not None else 0
     for _ in range(args.warmup - 1):
         sim.forward(S)
     torch.cuda.synchronize()
@@ -713,10 +717,11 @@ def main():
     Vs = st_mesh.num_verts if st_mesh is not None else 0
 
     def project():
-        sx.sx_contact_pairs_project(V, Vs, ptr(sim._pairs), ptr(sim._pairs_ws), ptr(m.y4),
-                                    ptr(st_mesh.x4) if st_mesh is not None else None, ptr(m.fixed), ptr(m.m_inv),
-                                    sim.dHat, float(sim.compliance_collision), sim.contact_cull_d2(),
-                                    ptr(sim._dx_fix), ptr(sim._nc), ptr(sim.status), None, 0, stream_handle())
+        sx.sx_contact_pairs_project_v(V, Vs, ptr(sim._pairs), ptr(sim._pairs_ws), ptr(m.y4),
+                                      ptr(st_mesh.x4) if st_mesh is not None else None, ptr(m.fixed), ptr(m.m_inv),
+                                      sim.dHat, float(sim.compliance_collision), sim.contact_cull_d2(),
+                                      ptr(sim._dx_fix), ptr(sim._nc), ptr(sim.status), None, 0, pp_variant,
+                                      stream_handle())
 
     side = torch.cuda.Stream()
     side.wait_stream(stream)
@@ -760,6 +765,10 @@ def main():
             "execution": "eager launches" if args.eager else "one CUDA graph per frame",
             "sweep_config": {"entries_per_load_batch": sweep_cfg[0], "threads_per_block": sweep_cfg[1],
                              "picked_by": "autotuner (fastest of %d bit-identical variants)" % len(vtimes)},
+            "pairs_project_config": {"pair_batches_per_warp_step": pp_variants[pp_variant][0],
+                                     "blocks_per_sm": pp_variants[pp_variant][1],
+                                     "picked_by": "library default (fastest of %d identical variants in "
+                                                  "frame timing)" % len(pp_variants)},
             "step": f"frame {args.warmup + 1} of the scene, restored from a snapshot before each step"},
         "gpu_launches": int(launches),
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},

@@ -306,6 +306,15 @@ int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws,
 int sx_contact_pairs_project(int n_dy, int n_st, const int* pairs, const void* ws, const float* y4, const float* xs4,
                              const float* fixed, const float* m_inv, float dHat, float compliance, float cull_d2,
                              long long* dx_fix, int* nc, int* status, const int* conv, int iter, void* stream);
+/* sx_contact_pairs_project in one of its compiled launch configurations
+ * (identical results): pair batches box-tested per warp step and resident
+ * blocks per SM, as sx_contact_pairs_project_variant_info reports. */
+int sx_contact_pairs_project_variants(void);
+int sx_contact_pairs_project_variant_info(int variant, int* unroll, int* blocks_per_sm);
+int sx_contact_pairs_project_v(int n_dy, int n_st, const int* pairs, const void* ws, const float* y4,
+                               const float* xs4, const float* fixed, const float* m_inv, float dHat, float compliance,
+                               float cull_d2, long long* dx_fix, int* nc, int* status, const int* conv, int iter,
+                               int variant, void* stream);
 int sx_contact_apply(int n_dy, float* y4, const float* fixed, long long* dx_fix, int* nc, const int* conv, int iter,
                      void* stream);
 

@@ -765,15 +765,71 @@ struct Pairs {  // optional pair records: pair[(q*cap+j)*2 + {0,1}] = (face, dty
 //   static mesh:  xs4 (positions), faces_st
 //   candidates:   vt_st (Vd x cap), vt_dy (Vd x cap), tv_st (Vs x cap), counts
 // Optional pair records (pass NULL to skip): three blocks, same layout.
-// cull_d2 > 0: a pair whose point-to-triangle-box squared distance exceeds
-// cull_d2 is skipped before classification (the CUDA pair-list sweep's cull;
-// every region's distance is at least the box distance, so with cull_d2 above
-// dHat the skipped pair would add nothing).  0 classifies every pair.
+// cull_d2 > 0: a pair whose point-to-triangle-box squared distance, or whose
+// separating-axis bound (sat_far below), exceeds cull_d2 is skipped before
+// classification (the CUDA pair-list sweep's cull; every region's distance is
+// at least both, so with cull_d2 above dHat the skipped pair would add
+// nothing).  0 classifies every pair.
 static float box_d2(V3 p, V3 t0, V3 t1, V3 t2) {
     float ex = std::fmax(std::fmax(std::fmin(std::fmin(t0.x, t1.x), t2.x) - p.x, p.x - std::fmax(std::fmax(t0.x, t1.x), t2.x)), 0.0f);
     float ey = std::fmax(std::fmax(std::fmin(std::fmin(t0.y, t1.y), t2.y) - p.y, p.y - std::fmax(std::fmax(t0.y, t1.y), t2.y)), 0.0f);
     float ez = std::fmax(std::fmax(std::fmin(std::fmin(t0.z, t1.z), t2.z) - p.z, p.z - std::fmax(std::fmax(t0.z, t1.z), t2.z)), 0.0f);
     return (ex * ex + ey * ey) + ez * ez;
+}
+
+// Both cull stages skip only pairs of triangles on which d_type_PT's 2x2
+// solves stay far inside float32's normal range (determinant about
+// |e|^4 |n|^2): |n|^2 min|e|^4 > 1e-30 and |n|^2 max|e|^4 < 1e30.  On tinier
+// or degenerate triangles the classification turns arbitrary (a far point can
+// get the plane region and a spurious contact, which the reference applies).
+static bool classifiable(V3 a, V3 b, V3 c) {
+    V3 e0 = sub(b, a), e1 = sub(c, b), e2 = sub(a, c);
+    V3 n = cross(e0, sub(c, a));
+    float nn = dot(n, n);
+    float l0 = dot(e0, e0), l1 = dot(e1, e1), l2 = dot(e2, e2);
+    float lo = std::fmin(std::fmin(l0, l1), l2), hi = std::fmax(std::fmax(l0, l1), l2);
+    return (nn * lo) * lo > 1e-30f && (nn * hi) * hi < 1e30f;
+}
+
+// Second cull stage of the CUDA pair-list sweep, mirrored so that the
+// oracle's cull mode skips the same pairs: a separating-axis lower bound on
+// dist(p, T) along the face normal n = (b-a) x (c-a) and the in-plane edge
+// normals e x n, made safe against rounding (each projection errs by less
+// than 2.4e-7 max|v - p|_1 |m|_1; 1e-6 of that is subtracted and a 1e-5
+// relative margin asked for; axes with |m|^2 <= 1e-30 are not used).  Every
+// region's distance is at least dist(p, T), so with cull_d2 above dHat a pair
+// it removes would add nothing.
+static float l1n(V3 a) { return (std::fabs(a.x) + std::fabs(a.y)) + std::fabs(a.z); }
+
+static bool far_along(V3 m, V3 da, V3 db, V3 dc, float l1, float cull_d2) {
+    float mm = dot(m, m);
+    float sa = dot(da, m), sb = dot(db, m), sc = dot(dc, m);
+    float gap = std::fmax(std::fmin(std::fmin(sa, sb), sc), -std::fmax(std::fmax(sa, sb), sc)) - 1e-6f * (l1 * l1n(m));
+    return mm > 1e-30f && gap > 0.0f && gap * gap > (cull_d2 * mm) * 1.00001f;
+}
+
+static bool sat_far(V3 p, V3 a, V3 b, V3 c, float cull_d2) {
+    V3 da = sub(a, p), db = sub(b, p), dc = sub(c, p);
+    float l1 = std::fmax(std::fmax(l1n(da), l1n(db)), l1n(dc));
+    V3 eab = sub(db, da), ebc = sub(dc, db), eca = sub(da, dc);
+    V3 n = cross(eab, sub(dc, da));
+    return far_along(n, da, db, dc, l1, cull_d2) || far_along(cross(eab, n), da, db, dc, l1, cull_d2) ||
+           far_along(cross(ebc, n), da, db, dc, l1, cull_d2) || far_along(cross(eca, n), da, db, dc, l1, cull_d2);
+}
+
+static bool culled(float cull_d2, V3 p, V3 a, V3 b, V3 c) {
+    return cull_d2 > 0.0f && classifiable(a, b, c) && (box_d2(p, a, b, c) > cull_d2 || sat_far(p, a, b, c, cull_d2));
+}
+
+// The two cull stages over n quadruples (12 floats each): out[i] = 1 box,
+// 2 separating axes, 0 kept.
+API int or_contact_cull(int n, const float* p12, float cull_d2, int32_t* out) {
+    for (int i = 0; i < n; ++i) {
+        const float* q = p12 + 12 * (size_t)i;
+        V3 p = v3(q), a = v3(q + 3), b = v3(q + 6), c = v3(q + 9);
+        out[i] = !classifiable(a, b, c) ? 0 : box_d2(p, a, b, c) > cull_d2 ? 1 : sat_far(p, a, b, c, cull_d2) ? 2 : 0;
+    }
+    return 0;
 }
 
 // accumulate != 0: dx_fix / nc already hold this iteration's edge-edge terms
@@ -811,7 +867,7 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
                 int fs = vt_st_c[(size_t)vid * cap + j];
                 V3 x0 = v3(y4 + 4 * vid);
                 V3 x1 = v3(xs4 + 4 * faces_st[3 * fs]), x2 = v3(xs4 + 4 * faces_st[3 * fs + 1]), x3 = v3(xs4 + 4 * faces_st[3 * fs + 2]);
-                if (cull_d2 > 0.0f && box_d2(x0, x1, x2, x3) > cull_d2) continue;
+                if (culled(cull_d2, x0, x1, x2, x3)) continue;
                 V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
                 int dt = d_type_PT(x0, x1, x2, x3);
                 float d = pt_distance(dt, x0, x1, x2, x3, g, true, dHat);
@@ -831,7 +887,7 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
                 if (a == vid || b == vid || c == vid) continue;
                 int vv[4] = {vid, a, b, c};
                 V3 x[4] = {v3(y4 + 4 * vid), v3(y4 + 4 * a), v3(y4 + 4 * b), v3(y4 + 4 * c)};
-                if (cull_d2 > 0.0f && box_d2(x[0], x[1], x[2], x[3]) > cull_d2) continue;
+                if (culled(cull_d2, x[0], x[1], x[2], x[3])) continue;
                 V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
                 int dt = d_type_PT(x[0], x[1], x[2], x[3]);
                 float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);
@@ -865,7 +921,7 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
                 int fd = tv_st_c[(size_t)vis * cap + j];
                 int vv[4] = {-1, faces_dy[3 * fd], faces_dy[3 * fd + 1], faces_dy[3 * fd + 2]};
                 V3 x[4] = {v3(xs4 + 4 * vis), v3(y4 + 4 * vv[1]), v3(y4 + 4 * vv[2]), v3(y4 + 4 * vv[3])};
-                if (cull_d2 > 0.0f && box_d2(x[0], x[1], x[2], x[3]) > cull_d2) continue;
+                if (culled(cull_d2, x[0], x[1], x[2], x[3])) continue;
                 V3 g[4] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
                 int dt = d_type_PT(x[0], x[1], x[2], x[3]);
                 float d = pt_distance(dt, x[0], x[1], x[2], x[3], g, false, dHat);

@@ -52,6 +52,7 @@ _SIGS = {
     "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, I],
     "or_edge_edge_classify": [I, P, F, P, P, P],
     "or_point_triangles": [I, P, P, P, P],
+    "or_contact_cull": [I, P, F, P],
     "or_edge_edge_sweep": [I, P, P, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, I],
     "or_point_triangle": [P, P, P],
     "or_color_edges": [I, I, P, I, P, P, P],
@@ -369,6 +370,16 @@ def adjacency(n_verts, edges, l0, bend, bl0):
     adj[:, 0] = np.where(cid >= E, nb | 0x80000000, nb).astype(np.int64).astype(np.uint32).view(np.int32)
     adj[:, 1] = rest[cid].view(np.int32)
     return ptr, adj
+
+
+def contact_cull(p12, cull_d2):
+    """The pair-list sweep's two cull stages on n point-triangle quadruples
+    (n x 12 floats: point, then the triangle): 1 = box distance, 2 =
+    separating axes, 0 = kept."""
+    p = f32(np.asarray(p12, np.float32).reshape(-1, 12))
+    out = np.zeros(p.shape[0], np.int32)
+    lib().or_contact_cull(p.shape[0], _p(p), float(cull_d2), _p(out))
+    return out
 
 
 def velocity_contacts(faces_dy, faces_st, cap, rec, v4, vs4, fixed, m_inv, m_inv_st, mu):

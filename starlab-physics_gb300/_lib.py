@@ -70,6 +70,9 @@ SIGNATURES = {
     "sx_contact_pairs_build": ([I, I, P, P, I, P, P, P, P, P, P, P, C.c_longlong, P, Z, P], I),
     "sx_contact_pairs_sweep": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, P], I),
     "sx_contact_pairs_project": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, P], I),
+    "sx_contact_pairs_project_variants": ([], I),
+    "sx_contact_pairs_project_variant_info": ([I, P, P], I),
+    "sx_contact_pairs_project_v": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, I, P], I),
     "sx_contact_apply": ([I, P, P, P, P, P, I, P], I),
     "sx_edge_edge_sweep": ([I, P, P, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, I, P], I),
     "sx_edge_edge_classify": ([I, P, F, P, P, P, P], I),
@@ -155,7 +158,8 @@ class _Calls:
         if name not in SIGNATURES:
             raise AttributeError(name)
         if SIGNATURES[name][1] is I and name not in ("sx_version", "sx_mlp_param_count", "sx_mlp_bf16_count",
-                                                     "sx_jacobi_sweep_variants"):
+                                                     "sx_jacobi_sweep_variants",
+                                                     "sx_contact_pairs_project_variants"):
             return lambda *a: _call(name, *a)
         return getattr(load(), name)
 

@@ -1,4 +1,5 @@
-"""Autotuner for the Jacobi sweep's launch configuration.
+"""Autotuner for the launch configuration of the Jacobi sweep (and the list
+of the contact-pair projection's configurations).
 
 The sweep kernel is compiled in several configurations -- how many adjacency
 entries a thread loads before it computes, and how many threads (= vertices) a
@@ -73,3 +74,15 @@ def tune_sweep(x4, y4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y
     best = int(np.argmin(times))
     _cache[key] = (best, times)
     return best, times
+
+
+def pairs_project_variants() -> list[tuple[int, int]]:
+    """(pair batches box-tested per warp step, resident blocks per SM) of every
+    compiled configuration of the contact-pair projection."""
+    L = load()
+    out = []
+    for k in range(int(L.sx_contact_pairs_project_variants())):
+        u, b = C.c_int(0), C.c_int(0)
+        sx.sx_contact_pairs_project_variant_info(k, C.addressof(u), C.addressof(b))
+        out.append((u.value, b.value))
+    return out

@@ -611,6 +611,69 @@ __device__ __forceinline__ float box_d2(V3 p, V3 t0, V3 t1, V3 t2) {
     return (ex * ex + ey * ey) + ez * ez;
 }
 
+// Both cull stages below rely on d_type_PT picking the region of the nearest
+// feature.  It solves one 2x2 system per edge whose float32 determinant is
+// about |e|^4 |n|^2 (n the face normal); for tiny or degenerate triangles that
+// leaves the normal range and the classification turns arbitrary (a far point
+// can get the plane region and a spurious contact, which the reference then
+// applies).  The culls therefore skip only pairs of triangles whose
+// determinants stay far inside the range: |n|^2 min|e|^4 > 1e-30 and
+// |n|^2 max|e|^4 < 1e30.  NaN positions fail the test as well.
+// The thresholds sit eight orders of magnitude inside the range, so the test
+// is evaluated with fused multiply-adds: it decides only whether a pair may be
+// skipped, and on classifiable triangles both decisions give the same sums.
+__device__ __forceinline__ float fdot(V3 a, V3 b) { return __fmaf_rn(a.x, b.x, __fmaf_rn(a.y, b.y, a.z * b.z)); }
+
+__device__ __forceinline__ bool classifiable(V3 a, V3 b, V3 c) {
+    const V3 e0 = sub(b, a), e1 = sub(c, b), e2 = sub(a, c);
+    const V3 n = {__fmaf_rn(e0.y, -e2.z, e0.z * e2.y), __fmaf_rn(e0.z, -e2.x, e0.x * e2.z),
+                  __fmaf_rn(e0.x, -e2.y, e0.y * e2.x)};  // e0 x (c - a)
+    const float nn = fdot(n, n);
+    const float l0 = fdot(e0, e0), l1 = fdot(e1, e1), l2 = fdot(e2, e2);
+    const float lo = fminf(fminf(l0, l1), l2), hi = fmaxf(fmaxf(l0, l1), l2);
+    return (nn * lo) * lo > 1e-30f && (nn * hi) * hi < 1e30f;
+}
+
+// First stage: the point's squared distance to the triangle's box exceeds
+// cull_d2 (a margin above dHat) on a classifiable triangle.
+__device__ __forceinline__ bool box_far(V3 p, V3 a, V3 b, V3 c, float cull_d2) {
+    return box_d2(p, a, b, c) > cull_d2 && classifiable(a, b, c);
+}
+
+// Separating-axis cull, the second stage after box_d2.  For any axis m the
+// projection onto m/|m| is 1-Lipschitz, so dist(p, T) >= gap / |m| where gap
+// is the distance from p's projection to the interval of T's vertices.  The
+// axes are the face normal n = (b-a) x (c-a) and the in-plane edge normals
+// e x n: together they give the distance to the edge line for a point beside
+// an edge, which is what separates a flat cloth's vertex from the nearby
+// triangles of its own sheet (their boxes contain it, so box_d2 is 0).  Every
+// region's distance d_type_PT picks is at least dist(p, T) (a vertex, the
+// edge segment its projection falls on, or the plane over the triangle), so a
+// pair whose bound exceeds cull_d2 (a margin above dHat) adds nothing.  The
+// bound is made safe against rounding: each projection s_k = (v_k - p) . m
+// errs by less than 2.4e-7 |v_k - p|_1 |m|_1 (three products and two sums,
+// plus the rounding of v_k - p), the test subtracts 1e-6 max_k |v_k - p|_1
+// |m|_1 from the gap and asks for a further 1e-5 relative margin; axes with
+// |m|^2 <= 1e-30 (degenerate triangles) are not used.
+__device__ __forceinline__ float l1n(V3 a) { return (fabsf(a.x) + fabsf(a.y)) + fabsf(a.z); }
+
+__device__ __forceinline__ bool far_along(V3 m, V3 da, V3 db, V3 dc, float l1, float cull_d2) {
+    const float mm = dot(m, m);
+    const float sa = dot(da, m), sb = dot(db, m), sc = dot(dc, m);
+    const float gap = fmaxf(fminf(fminf(sa, sb), sc), -fmaxf(fmaxf(sa, sb), sc)) - 1e-6f * (l1 * l1n(m));
+    return mm > 1e-30f && gap > 0.0f && gap * gap > (cull_d2 * mm) * 1.00001f;
+}
+
+__device__ __forceinline__ bool sat_far(V3 p, V3 a, V3 b, V3 c, float cull_d2) {
+    const V3 da = sub(a, p), db = sub(b, p), dc = sub(c, p);
+    const float l1 = fmaxf(fmaxf(l1n(da), l1n(db)), l1n(dc));
+    const V3 eab = sub(db, da), ebc = sub(dc, db), eca = sub(da, dc);
+    const V3 n = cross(eab, sub(dc, da));
+    return classifiable(a, b, c) &&
+           (far_along(n, da, db, dc, l1, cull_d2) || far_along(cross(eab, n), da, db, dc, l1, cull_d2) ||
+            far_along(cross(ebc, n), da, db, dc, l1, cull_d2) || far_along(cross(eca, n), da, db, dc, l1, cull_d2));
+}
+
 // One pair of the list: positions of its four vertices and the projection of
 // its kind (vt_st, vt_dy or tv_st by list position).
 struct PairCtx {
@@ -655,18 +718,25 @@ __device__ __forceinline__ void project_pair(const PairCtx& c, int t, int* bad) 
 
 constexpr int PP_BLOCK = 256;
 
-// With the cull on, most pairs end at the box test and the few that remain
-// would leave a warp mostly idle through the region classification.  Each warp
-// therefore tests 32 pairs at a time, appends the survivors to its queue in
-// shared memory (ballot), and projects them 32 at a time with every lane busy.
-__global__ void __launch_bounds__(PP_BLOCK) pairs_project_kernel(const int* __restrict__ meta,
-                                                                 const int4* __restrict__ pairs,
-                                                                 const float4* __restrict__ y4,
-                                                                 const float4* __restrict__ xs4,
-                                                                 const float* __restrict__ fixed,
-                                                                 const float* __restrict__ m_inv, float dHat,
-                                                                 float compliance, float cull_d2, long long* dx,
-                                                                 int* nc, int* status, const int* conv, int iter) {
+// With the cull on, most pairs end at the box test, most of the rest at the
+// separating-axis test, and the few that remain would leave a warp mostly idle
+// through the region classification.  Each warp therefore box-tests U x 32
+// pairs at a time (all their records first, then all their vertex gathers, so
+// U batches of loads are in flight) and appends the survivors to a stack in
+// shared memory (ballot); 32 at a time they go through the separating-axis
+// test onto a second stack, and 32 at a time from there through the
+// projection, every stage with all lanes busy.  The contact sums are order
+// independent, so U and the stacking change the speed only.
+template <int U, int MINB>
+__global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_kernel(const int* __restrict__ meta,
+                                                                       const int4* __restrict__ pairs,
+                                                                       const float4* __restrict__ y4,
+                                                                       const float4* __restrict__ xs4,
+                                                                       const float* __restrict__ fixed,
+                                                                       const float* __restrict__ m_inv, float dHat,
+                                                                       float compliance, float cull_d2, long long* dx,
+                                                                       int* nc, int* status, const int* conv,
+                                                                       int iter) {
     pdl_entry();
     if (iteration_skipped(conv, iter)) return;
     const PairCtx c{pairs, y4, xs4, fixed, m_inv, dHat, compliance, dx, nc, meta[0], meta[1]};
@@ -676,32 +746,61 @@ __global__ void __launch_bounds__(PP_BLOCK) pairs_project_kernel(const int* __re
         for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x)
             project_pair(c, t, &bad);
     } else {
-        __shared__ int queue[PP_BLOCK / 32][64];
+        __shared__ int box_stack[PP_BLOCK / 32][32 * U + 32];
+        __shared__ int sat_stack[PP_BLOCK / 32][64];
         const int lane = threadIdx.x & 31;
-        int* wq = queue[threadIdx.x >> 5];
-        int qn = 0;  // warp-uniform
-        const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-        for (int base = gw * 32; base < P; base += nw * 32) {
-            const int t = base + lane;
+        const unsigned below = (1u << lane) - 1u;
+        int* s1 = box_stack[threadIdx.x >> 5];
+        int* s2 = sat_stack[threadIdx.x >> 5];
+        int n1 = 0, n2 = 0;  // warp-uniform
+        // the top cnt (<= 32) entries of s1 through the separating-axis test
+        // onto s2; projects the top 32 of s2 once it holds that many
+        auto sat_stage = [&](int cnt) {
+            const int t = lane < cnt ? s1[n1 - cnt + lane] : -1;
             bool keep = false;
-            if (t < P) {
+            if (t >= 0) {
                 V3 x[4];
                 pair_points(c, t, pairs[t], x);
-                keep = !(box_d2(x[0], x[1], x[2], x[3]) > cull_d2);
+                keep = !sat_far(x[0], x[1], x[2], x[3], cull_d2);
             }
+            n1 -= cnt;
             const unsigned m = __ballot_sync(0xffffffffu, keep);
-            if (keep) wq[qn + __popc(m & ((1u << lane) - 1u))] = t;
-            qn += __popc(m);
+            if (keep) s2[n2 + __popc(m & below)] = t;
+            n2 += __popc(m);
             __syncwarp();
-            if (qn >= 32) {
-                project_pair(c, wq[lane], &bad);
+            if (n2 >= 32) {
+                project_pair(c, s2[n2 - 32 + lane], &bad);
+                n2 -= 32;
                 __syncwarp();
-                if (lane < qn - 32) wq[lane] = wq[32 + lane];
-                __syncwarp();
-                qn -= 32;
             }
+        };
+        const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+        for (int base = gw * 32 * U; base < P; base += nw * 32 * U) {
+            int4 pr[U];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int t = base + 32 * u + lane;
+                pr[u] = t < P ? pairs[t] : make_int4(0, 0, 0, 0);
+            }
+            V3 x[U][4];
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int t = base + 32 * u + lane;
+                if (t < P) pair_points(c, t, pr[u], x[u]);
+            }
+#pragma unroll
+            for (int u = 0; u < U; ++u) {
+                const int t = base + 32 * u + lane;
+                const bool keep = t < P && !box_far(x[u][0], x[u][1], x[u][2], x[u][3], cull_d2);
+                const unsigned m = __ballot_sync(0xffffffffu, keep);
+                if (keep) s1[n1 + __popc(m & below)] = t;
+                n1 += __popc(m);
+            }
+            __syncwarp();
+            while (n1 >= 32) sat_stage(32);
         }
-        if (lane < qn) project_pair(c, wq[lane], &bad);
+        if (n1 > 0) sat_stage(n1);
+        if (lane < n2) project_pair(c, s2[lane], &bad);
     }
     if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
 }
@@ -1280,20 +1379,58 @@ static int sm_count() {
     return n;
 }
 
-extern "C" int sx_contact_pairs_project(int n_dy, int n_st, const int* pairs, const void* ws, const float* y4,
-                                        const float* xs4, const float* fixed, const float* m_inv, float dHat,
-                                        float compliance, float cull_d2, long long* dx_fix, int* nc, int* status,
-                                        const int* conv, int iter, void* stream) {
+// Launch configurations of the pair projection: pair batches box-tested per
+// warp step (U) and resident blocks per SM (the grid is that many blocks per
+// SM; registers are capped to keep them resident).  All give identical
+// results.  The default was the fastest inside the drape256 frame; timed
+// alone on a fixed state the ranking differs, so it is not autotuned.
+struct PairsProjectVariant {
+    int unroll, blocks_per_sm;
+    decltype(&pairs_project_kernel<1, 4>) kern;
+};
+static const PairsProjectVariant kPairsProjectVariants[] = {
+    {2, 3, pairs_project_kernel<2, 3>},
+    {1, 4, pairs_project_kernel<1, 4>},
+    {2, 6, pairs_project_kernel<2, 3>},
+    {4, 2, pairs_project_kernel<4, 2>},
+};
+constexpr int kNumPairsProjectVariants = sizeof(kPairsProjectVariants) / sizeof(kPairsProjectVariants[0]);
+constexpr int kPairsProjectDefault = 0;
+
+extern "C" int sx_contact_pairs_project_variants(void) { return kNumPairsProjectVariants; }
+
+extern "C" int sx_contact_pairs_project_variant_info(int variant, int* unroll, int* blocks_per_sm) {
+    SX_REQUIRE(variant >= 0 && variant < kNumPairsProjectVariants && unroll && blocks_per_sm,
+               "sx_contact_pairs_project_variant_info: bad variant");
+    *unroll = kPairsProjectVariants[variant].unroll;
+    *blocks_per_sm = kPairsProjectVariants[variant].blocks_per_sm;
+    return SX_OK;
+}
+
+extern "C" int sx_contact_pairs_project_v(int n_dy, int n_st, const int* pairs, const void* ws, const float* y4,
+                                          const float* xs4, const float* fixed, const float* m_inv, float dHat,
+                                          float compliance, float cull_d2, long long* dx_fix, int* nc, int* status,
+                                          const int* conv, int iter, int variant, void* stream) {
+    SX_REQUIRE(variant >= 0 && variant < kNumPairsProjectVariants, "sx_contact_pairs_project_v: bad variant");
     SX_REQUIRE(n_dy >= 0 && n_st >= 0, "sx_contact_pairs_project: bad sizes");
     if (n_dy == 0) return SX_OK;
     SX_REQUIRE(pairs && ws && y4 && fixed && m_inv && dx_fix && nc && status,
                "sx_contact_pairs_project: null pointer");
     SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_project: null static positions");
     PairsWs w = pairs_ws(const_cast<void*>(ws), n_dy, n_st);
-    launch(pairs_project_kernel, sm_count() * 8, PP_BLOCK, 0, as_stream(stream), (const int*)w.meta,
+    const PairsProjectVariant& pv = kPairsProjectVariants[variant];
+    launch(pv.kern, sm_count() * pv.blocks_per_sm, PP_BLOCK, 0, as_stream(stream), (const int*)w.meta,
            (const int4*)pairs, (const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, cull_d2, dx_fix,
            nc, status, conv, iter);
     return check_launch("pairs_project_kernel");
+}
+
+extern "C" int sx_contact_pairs_project(int n_dy, int n_st, const int* pairs, const void* ws, const float* y4,
+                                        const float* xs4, const float* fixed, const float* m_inv, float dHat,
+                                        float compliance, float cull_d2, long long* dx_fix, int* nc, int* status,
+                                        const int* conv, int iter, void* stream) {
+    return sx_contact_pairs_project_v(n_dy, n_st, pairs, ws, y4, xs4, fixed, m_inv, dHat, compliance, cull_d2, dx_fix,
+                                      nc, status, conv, iter, kPairsProjectDefault, stream);
 }
 
 extern "C" int sx_contact_apply(int n_dy, float* y4, const float* fixed, long long* dx_fix, int* nc, const int* conv,

@@ -102,6 +102,9 @@ class Solver:
         self._sewing = None  # (sewn, sptr, partner, scratch, stiffness)
         # launch configuration of the fixed-count sweep (autotune() picks one)
         self.sweep_variant = 0
+        # launch configuration of the contact-pair projection (None: the
+        # library's default, sx_contact_pairs_project_variant_info lists all)
+        self.pairs_variant = None
 
         self.max_num_verts_dy = mesh_dy.num_verts
         self.max_num_edges_dy = mesh_dy.num_edges
@@ -302,12 +305,22 @@ class Solver:
         if self.enable_edge_edge:
             self.solve_edge_edge_constraints_x(c, iteration, gated)
         if not self.record_pairs:
-            sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
-                                      ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
-                                      ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c), self.contact_cull_d2(),
-                                      ptr(self._dx_fix), ptr(self._nc), ptr(self.status),
-                                      ptr(self._conv) if self.tol is not None and gated else None, iteration,
-                                      stream_handle())
+            conv = ptr(self._conv) if self.tol is not None and gated else None
+            if self.pairs_variant is None:
+                sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
+                                          ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
+                                          ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c), self.contact_cull_d2(),
+                                          ptr(self._dx_fix), ptr(self._nc), ptr(self.status), conv, iteration,
+                                          stream_handle())
+            else:
+                sx.sx_contact_pairs_project_v(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
+                                              ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
+                                              ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c),
+                                              self.contact_cull_d2(), ptr(self._dx_fix), ptr(self._nc),
+                                              ptr(self.status), conv, iteration, int(self.pairs_variant),
+                                              stream_handle())
+                sx.sx_contact_apply(m.num_verts, ptr(m.y4), ptr(m.fixed), ptr(self._dx_fix), ptr(self._nc), conv,
+                                    iteration, stream_handle())
             return
         sx.sx_collision_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(m.face_indices),
                               ptr(s.face_indices) if s is not None else None, ptr(m.y4),
@@ -487,7 +500,7 @@ class Solver:
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
                 self.compliance_collision, self.self_collision, self.contact_cull, self.sweep_variant,
-                self.enable_edge_edge,
+                self.pairs_variant, self.enable_edge_edge,
                 self.enable_velocity_update, self.mu, self.tol,
                 self.tol_relative,
                 self.check_every,

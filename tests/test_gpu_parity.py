@@ -366,6 +366,51 @@ def test_pair_list_sweep_equals_per_query_sweep(pkg, cull):
     assert np.array_equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("cull", [False, True])
+def test_pair_projection_variants_agree(pkg, cull):
+    """Every compiled launch configuration of the pair projection adds the same
+    fixed-point corrections and counts as the default one."""
+    from starlab_physics_gb300._lib import ptr, sx, stream_handle
+
+    sc, cl, sp = _drape(pkg, n=40)
+    sim = pkg.Solver(cl, sp, dHat=(4e-2) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8, g=(0, 0, -9.81),
+                     dt=1 / 60, record_pairs=False)
+    sim.padding = 0.04
+    sim.enable_collision_handling = True
+    x = _np(cl.x4).copy()
+    x[:, 2] = 0.5 + 0.3 + 0.01 * np.sin(13 * x[:, 0]) * np.cos(7 * x[:, 1])
+    cl.x4.copy_(_t(x))
+    sim.build_bvhs()
+    sim.compute_y(1 / 600)
+    sim.broadphase_lbvh()
+    sim.contact_cull = cull
+    sim.build_contact_pairs()
+    torch.cuda.synchronize()
+    assert sim.contact_pair_count() > 1000
+    V, Vs = cl.num_verts, sp.num_verts
+    n_var = sx.sx_contact_pairs_project_variants()
+    assert n_var >= 2
+    outs = []
+    for v in [None, *range(n_var)]:
+        sim._dx_fix.zero_()
+        sim._nc.zero_()
+        args = (V, Vs, ptr(sim._pairs), ptr(sim._pairs_ws), ptr(cl.y4), ptr(sp.x4), ptr(cl.fixed), ptr(cl.m_inv),
+                sim.dHat, float(sim.compliance_collision), sim.contact_cull_d2(), ptr(sim._dx_fix), ptr(sim._nc),
+                ptr(sim.status), None, 0)
+        if v is None:
+            sx.sx_contact_pairs_project(*args, stream_handle())
+        else:
+            sx.sx_contact_pairs_project_v(*args, v, stream_handle())
+        torch.cuda.synchronize()
+        outs.append((_np(sim._dx_fix).copy(), _np(sim._nc).copy()))
+    assert outs[0][1].sum() > 0
+    for dxf, nc in outs[1:]:
+        assert np.array_equal(dxf, outs[0][0]) and np.array_equal(nc, outs[0][1])
+    assert int(sim.status.item()) & 4 == 0  # SX_STATUS_FIXED_RANGE
+    sim._dx_fix.zero_()
+    sim._nc.zero_()
+
+
 @pytest.mark.parametrize("n_iter", [3, 4])
 def test_graph_replay_equals_eager(pkg, n_iter):
     res = []

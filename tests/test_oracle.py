@@ -443,6 +443,74 @@ def test_contact_cull_never_drops_a_contact(po):
     assert culled > n // 10
 
 
+def test_separating_axis_cull_never_drops_a_contact(po):
+    """The second cull stage (separating axes: face normal and in-plane edge
+    normals) on adversarial pairs: flat and bent sheets whose vertices sit
+    beside the neighbouring triangles (box distance 0), slivers, tiny and
+    large triangles, points placed at 0.8-1.3 x the contact distance from
+    points of the triangle in random and in-plane directions.  No pair with
+    d < dHat is culled, and the stage removes most of the box survivors of
+    the sheets.  Triangles too small or too thin for the region classifier's
+    float32 solves (where it can return the plane region for a far point) are
+    not culled at all."""
+    rng = np.random.default_rng(5)
+    dHat = np.float32(2e-3) ** 2
+    cull = dHat * np.float32(1.0625)
+    r = np.sqrt(np.float64(dHat))
+    quads = []
+    # sheets: grid spacing 1.2-3 r, jittered, flat or bent; every vertex against
+    # the triangles of its 5 x 5 neighbourhood that do not contain it
+    for h_over_r, bend in ((1.2, 0.0), (1.45, 0.0), (2.0, 0.3), (3.0, 1.0), (1.3, 2.0)):
+        n = 9
+        h = h_over_r * r
+        u, v = np.meshgrid(np.arange(n) * h, np.arange(n) * h, indexing="ij")
+        z = bend * h * np.sin(u / (3 * h)) * np.cos(v / (2 * h))
+        X = np.stack([u, v, z], -1).reshape(-1, 3) + rng.normal(0, 0.05 * h, (n * n, 3))
+        X = (X + 0.5).astype(np.float32)
+        F = []
+        for i in range(n - 1):
+            for j in range(n - 1):
+                a, b, c, d = i * n + j, (i + 1) * n + j, (i + 1) * n + j + 1, i * n + j + 1
+                F += [(a, b, c), (a, c, d)] if (i + j) % 2 else [(a, b, d), (b, c, d)]
+        F = np.array(F)
+        for q in range(n * n):
+            for f in F:
+                if q in f or np.abs(X[f].mean(0) - X[q]).max() > 3 * h:
+                    continue
+                quads.append(np.concatenate([X[q], X[f[0]], X[f[1]], X[f[2]]]))
+    n_sheet = len(quads)
+    # random triangles, slivers among them, points near the threshold
+    for _ in range(12000):
+        size = 10 ** rng.uniform(-4, -1)
+        T = rng.normal(0, size, (3, 3))
+        if rng.random() < 0.3:  # sliver: the third vertex near the opposite edge
+            w = rng.random()
+            T[2] = w * T[0] + (1 - w) * T[1] + rng.normal(0, size * 1e-3, 3)
+        bary = rng.dirichlet((1, 1, 1)) if rng.random() < 0.5 else np.eye(3)[rng.integers(3)]
+        q = bary @ T
+        nrm = np.cross(T[1] - T[0], T[2] - T[0])
+        if rng.random() < 0.5 and np.linalg.norm(nrm) > 0:
+            dirn = np.cross(nrm, rng.normal(size=3))  # in the plane
+        else:
+            dirn = rng.normal(size=3)
+        dirn /= np.linalg.norm(dirn)
+        p = q + dirn * r * rng.uniform(0.8, 1.3)
+        off = rng.uniform(-2, 2, 3)
+        quads.append(np.concatenate([p + off, *(T + off)]).astype(np.float32))
+    Q = np.array(quads, np.float32)
+    dt, d, _ = po.point_triangles(Q)
+    out = po.contact_cull(Q, cull)
+    assert not ((out != 0) & (d < dHat)).any()
+    assert (d < dHat).sum() > 500
+    sheet = out[:n_sheet]
+    assert (sheet == 2).sum() > 0.8 * (sheet != 1).sum() - (d[:n_sheet] < dHat).sum()
+    assert (out[n_sheet:] == 2).sum() > 500
+    # tiny slivers whose classification is arbitrary are never culled, though
+    # their box distance exceeds the threshold
+    tiny = _box_d2_np(Q[:, :3], Q[:, 3:].reshape(-1, 3, 3)) > cull
+    assert ((out == 0) & tiny & (d < dHat)).sum() > 10
+
+
 def test_contact_cull_keeps_solver_result(pkg, po):
     """The oracle solver gives bit-identical trajectories with and without the
     cull on a colliding scene (plain64, 24x24, with iterations)."""
