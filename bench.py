@@ -228,9 +228,21 @@ def cpu_baseline(scene, rank):
         if el > 8.0 or n >= 10:
             break
     V = scene.cloth_x.shape[0]
+    # the same port on one core, one or two substeps
+    orc.nthreads = 1
+    n1 = 0
+    t0 = time.perf_counter()
+    while True:
+        orc.substep(dt_sub)
+        n1 += 1
+        el1 = time.perf_counter() - t0
+        if el1 > 4.0 or n1 >= 2:
+            break
     return {"value": V * n / el, "unit": UNIT, "cores": cores, "kind": "port",
             "sample": f"{n} substep(s) of the same scene on the CPU oracle (OpenMP, {cores} threads), "
-                      f"{el:.2f} s"}
+                      f"{el:.2f} s",
+            "one_core": {"value": V * n1 / el1, "unit": UNIT, "cores": 1,
+                         "sample": f"{n1} substep(s) of the same scene, 1 thread, {el1:.2f} s"}}
 
 
 def lbvh_soup(pkg, reps=10, with_cpu=True):

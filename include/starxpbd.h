@@ -254,6 +254,14 @@ int sx_face_bvh_refit(int n, const int* sorted_ids, const float* fmin4, const fl
                       const int* child_b, const int* parent, float* nmin4, float* nmax4, int* flags, int* status,
                       void* stream);
 
+/* sx_face_bvh_refit with the tree's lower levels in shared memory: nodes
+ * whose leaf range [range_l, range_r] (from sx_karras_build) lies in one tile
+ * of 256 sorted leaves are refit inside the tile's block; the rest as above.
+ * Same boxes, same scratch contract. */
+int sx_face_bvh_refit_tiled(int n, const int* sorted_ids, const float* fmin4, const float* fmax4,
+                            const int* child_a, const int* child_b, const int* parent, const int* range_l,
+                            const int* range_r, float* nmin4, float* nmax4, int* flags, int* status, void* stream);
+
 /* Stack traversal of a face-level LBVH for query boxes p4[i] +- padding, same
  * visiting order as traverse_cell_bvh_single (lbvh_cell.py:662-714). */
 int sx_face_bvh_traverse(int n, const float* p4, int n_queries, float padding, const int* child_a,

@@ -64,6 +64,7 @@ SIGNATURES = {
     "sx_radix_sort_pairs_noalloc": ([P, P, I, I, P], I),
     "sx_karras_build": ([P, I, I, P, P, P, P, P, P], I),
     "sx_face_bvh_refit": ([I, P, P, P, P, P, P, P, P, P, P, P], I),
+    "sx_face_bvh_refit_tiled": ([I, P, P, P, P, P, P, P, P, P, P, P, P, P], I),
     "sx_face_bvh_traverse": ([I, P, I, F, P, P, P, P, P, I, P, P, P, P], I),
     "sx_collision_sweep": ([I, I, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P], I),
     "sx_contact_pairs_workspace_bytes": ([I, I], Z),

@@ -362,25 +362,47 @@ __global__ void scene_aabb_init(unsigned* box) {
     else if (t < 6) box[t] = f2ord(-1e5f);
 }
 
-__global__ void scene_aabb_reduce(int V, const float4* __restrict__ p4, unsigned* box) {
+// Per block: four loads in flight per thread, warp shuffles, then the block's
+// warps combine in shared memory and one thread issues the six atomics (min
+// and max are exact, so the order does not matter).
+__global__ void __launch_bounds__(256) scene_aabb_reduce(int V, const float4* __restrict__ p4, unsigned* box) {
     pdl_entry();
     float lo[3] = {1e5f, 1e5f, 1e5f}, hi[3] = {-1e5f, -1e5f, -1e5f};
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < V; i += gridDim.x * blockDim.x) {
-        float4 p = p4[i];
+    const int stride = gridDim.x * blockDim.x;
+    auto take = [&](float4 p) {
         lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
         hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
+    };
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    for (; i + 3 * stride < V; i += 4 * stride) {
+        const float4 a = p4[i], b = p4[i + stride], c = p4[i + 2 * stride], d = p4[i + 3 * stride];
+        take(a);
+        take(b);
+        take(c);
+        take(d);
     }
+    for (; i < V; i += stride) take(p4[i]);
     for (int o = 16; o > 0; o >>= 1) {
         for (int k = 0; k < 3; ++k) {
             lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
             hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
         }
     }
+    __shared__ float red[8][6];
+    const int w = threadIdx.x >> 5;
     if ((threadIdx.x & 31) == 0) {
         for (int k = 0; k < 3; ++k) {
-            atomicMin(box + k, f2ord(lo[k]));
-            atomicMax(box + 3 + k, f2ord(hi[k]));
+            red[w][k] = lo[k];
+            red[w][3 + k] = hi[k];
         }
+    }
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        const int k = threadIdx.x;
+        float v = red[0][k];
+        for (int j = 1; j < (int)(blockDim.x >> 5); ++j) v = k < 3 ? fminf(v, red[j][k]) : fmaxf(v, red[j][k]);
+        if (k < 3) atomicMin(box + k, f2ord(v));
+        else atomicMax(box + k, f2ord(v));
     }
 }
 
@@ -540,7 +562,8 @@ extern "C" int sx_scene_aabb(const float* p4, int n_verts, float padding, float*
     launch(scene_aabb_init, 1, 32, 0, s, box);
     if (n_verts > 0) {
         int g = grid_for(n_verts, 256);
-        if (g > 1024) g = 1024;
+        const int cap = resident_blocks(scene_aabb_reduce, 256);
+        if (g > cap) g = cap;
         launch(scene_aabb_reduce, g, 256, 0, s, n_verts, (const float4*)p4, box);
     }
     launch(scene_aabb_finish, 1, 32, 0, s, box, padding);

@@ -2,6 +2,7 @@
 // single-launch bottom-up refit and stack traversal, for the reference's 32^3
 // cell-grid BVH (framework/collision/lbvh_cell.py, class LBVH_CELL) and for a
 // face-level LBVH over triangle soups.
+#include <cuda/atomic>
 #include <mutex>
 
 #include "sx_common.cuh"
@@ -70,9 +71,13 @@ __global__ void face_morton_kernel(int F, const float4* __restrict__ mn4, const 
 // ---------------------------------------------------------------------------
 // Stable LSD radix sort, 8-bit digits.
 //   upsweep : per-tile digit histogram -> hist[digit * nblocks + block]
-//   scan    : exclusive scan of hist (digit-major => stable across tiles)
-//   scatter : per tile, keys ranked within their digit in input order with
-//             __match_any_sync + per-warp counts, written to their final slots.
+//   scan    : one block per digit scans its column (exclusive over the tiles,
+//             in tile order) and writes the digit's total
+//   scatter : each tile takes its digit bases (exclusive scan of the 256
+//             totals + its column offset); each warp owns a contiguous 256-key
+//             slice of the tile and ranks its keys within their digit in input
+//             order (__match_any_sync, warp-private counters), so the order is
+//             stable with three block barriers per tile.
 // ---------------------------------------------------------------------------
 constexpr int RS_BLOCK = 256;
 constexpr int RS_ITEMS = 8;
@@ -94,6 +99,48 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_upsweep(const unsigned* __restric
     }
     __syncthreads();
     hist[(size_t)tid * nblocks + blockIdx.x] = cnt[tid];
+}
+
+// Exclusive scan of one value per thread over a 256-thread block; returns the
+// block total through *total.
+__device__ __forceinline__ unsigned block256_excl_scan(unsigned v, unsigned* total) {
+    __shared__ unsigned wsum[RS_WARPS];
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    unsigned incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) wsum[w] = incl;
+    __syncthreads();
+    unsigned before = 0, all = 0;
+#pragma unroll
+    for (int k = 0; k < RS_WARPS; ++k) {
+        before += k < w ? wsum[k] : 0u;
+        all += wsum[k];
+    }
+    __syncthreads();
+    *total = all;
+    return before + incl - v;
+}
+
+// Block d: exclusive scan of hist[d * nblocks .. (d + 1) * nblocks) in place,
+// the column total to tot[d].
+__global__ void __launch_bounds__(RS_BLOCK) rs_digit_scan(unsigned* __restrict__ hist, int nblocks,
+                                                          unsigned* __restrict__ tot) {
+    pdl_entry();
+    unsigned* col = hist + (size_t)blockIdx.x * nblocks;
+    unsigned carry = 0;
+    for (int b0 = 0; b0 < nblocks; b0 += RS_BLOCK) {
+        const int b = b0 + threadIdx.x;
+        const unsigned v = b < nblocks ? col[b] : 0u;
+        unsigned sum;
+        const unsigned ex = block256_excl_scan(v, &sum);
+        if (b < nblocks) col[b] = carry + ex;
+        carry += sum;
+    }
+    if (threadIdx.x == 0) tot[blockIdx.x] = carry;
 }
 
 // Single-block scan over n entries (exclusive or inclusive), 1024 threads.
@@ -129,43 +176,79 @@ __global__ void __launch_bounds__(1024) scan_single_block(unsigned* data, int n,
 __global__ void __launch_bounds__(RS_BLOCK) rs_scatter(const unsigned* __restrict__ kin,
                                                        const int* __restrict__ vin, unsigned* __restrict__ kout,
                                                        int* __restrict__ vout, int n, int shift,
-                                                       const unsigned* __restrict__ hist, int nblocks) {
+                                                       const unsigned* __restrict__ hist,
+                                                       const unsigned* __restrict__ tot, int nblocks) {
     pdl_entry();
-    __shared__ unsigned s_base[256];
-    __shared__ unsigned s_wcnt[RS_WARPS][256];
+    __shared__ unsigned s_off[RS_WARPS][256];
+    __shared__ unsigned s_gbase[256], s_lbase[256];
+    __shared__ unsigned s_key[RS_TILE];
+    __shared__ int s_val[RS_TILE];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
-    s_base[tid] = hist[(size_t)tid * nblocks + blockIdx.x];
-    const long long base = (long long)blockIdx.x * RS_TILE;
+    unsigned all;
+    const unsigned digit_base = block256_excl_scan(tot[tid], &all) + hist[(size_t)tid * nblocks + blockIdx.x];
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; ++w) s_off[w][tid] = 0;
+    __syncthreads();
+    // warp `warp` owns keys [tile + warp * 256, tile + (warp + 1) * 256)
+    const long long tile = (long long)blockIdx.x * RS_TILE;
+    const long long base = tile + warp * (RS_ITEMS * 32);
+    unsigned key[RS_ITEMS], rank[RS_ITEMS];
+    int val[RS_ITEMS];
+#pragma unroll
     for (int r = 0; r < RS_ITEMS; ++r) {
-        const long long idx = base + r * RS_BLOCK + tid;
-        const bool valid = idx < n;
-        unsigned key = 0;
-        int val = 0;
-        if (valid) {
-            key = kin[idx];
-            val = vin[idx];
-        }
-        const unsigned digit = valid ? ((key >> shift) & 255u) : 256u;
+        const long long idx = base + r * 32 + lane;
+        key[r] = idx < n ? kin[idx] : 0u;
+        val[r] = idx < n ? vin[idx] : 0;
+    }
+    unsigned* cnt = s_off[warp];
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) s_wcnt[w][tid] = 0;
-        __syncthreads();
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        const bool valid = base + r * 32 + lane < n;
+        const unsigned digit = valid ? ((key[r] >> shift) & 255u) : 256u;
         const unsigned peers = __match_any_sync(0xffffffffu, digit);
-        const unsigned rank = __popc(peers & lt_mask);
-        if (valid && (__ffs(peers) - 1) == lane) s_wcnt[warp][digit] = __popc(peers);
-        __syncthreads();
-        if (valid) {
-            unsigned off = s_base[digit];
-            for (int w = 0; w < warp; ++w) off += s_wcnt[w][digit];
-            const unsigned pos = off + rank;
-            kout[pos] = key;
-            vout[pos] = val;
-        }
-        __syncthreads();
-        unsigned tot = 0;
+        const unsigned before = valid ? cnt[digit] : 0u;
+        rank[r] = before + __popc(peers & lt_mask);
+        __syncwarp();
+        if (valid && (__ffs(peers) - 1) == lane) cnt[digit] = before + __popc(peers);
+        __syncwarp();
+    }
+    __syncthreads();
+    // per digit: the tile's count, its offset in the tile's digit order, and
+    // each warp's offset within it
+    unsigned tsum = 0;
 #pragma unroll
-        for (int w = 0; w < RS_WARPS; ++w) tot += s_wcnt[w][tid];
-        s_base[tid] += tot;
+    for (int w = 0; w < RS_WARPS; ++w) tsum += s_off[w][tid];
+    const unsigned lbase = block256_excl_scan(tsum, &all);
+    s_lbase[tid] = lbase;
+    s_gbase[tid] = digit_base;
+    unsigned run = lbase;
+#pragma unroll
+    for (int w = 0; w < RS_WARPS; ++w) {
+        const unsigned c = s_off[w][tid];
+        s_off[w][tid] = run;
+        run += c;
+    }
+    __syncthreads();
+    // the tile in digit order (stable within a digit) in shared memory ...
+#pragma unroll
+    for (int r = 0; r < RS_ITEMS; ++r) {
+        if (base + r * 32 + lane < n) {
+            const unsigned lp = cnt[(key[r] >> shift) & 255u] + rank[r];
+            s_key[lp] = key[r];
+            s_val[lp] = val[r];
+        }
+    }
+    __syncthreads();
+    // ... written out so that consecutive threads fill consecutive slots of
+    // each digit's run
+    const int count = (int)min((long long)RS_TILE, (long long)n - tile);
+    for (int i = tid; i < count; i += RS_BLOCK) {
+        const unsigned k = s_key[i];
+        const unsigned d = (k >> shift) & 255u;
+        const unsigned g = s_gbase[d] + ((unsigned)i - s_lbase[d]);
+        kout[g] = k;
+        vout[g] = s_val[i];
     }
 }
 
@@ -179,7 +262,7 @@ static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
 static inline int rs_nblocks(int n) { return n <= 0 ? 1 : (n + RS_TILE - 1) / RS_TILE; }
 static size_t rs_ws_bytes(int n) {
     size_t nn = (size_t)(n > 0 ? n : 1);
-    return align256(nn * 4) * 2 + align256((size_t)256 * rs_nblocks(n) * 4);
+    return align256(nn * 4) * 2 + align256((size_t)256 * rs_nblocks(n) * 4) + align256(256 * 4);
 }
 
 static int radix_sort(unsigned* keys, int* vals, int n, int bits, void* ws, size_t ws_bytes, cudaStream_t s) {
@@ -194,6 +277,8 @@ static int radix_sort(unsigned* keys, int* vals, int n, int bits, void* ws, size
     p += align256((size_t)n * 4);
     unsigned* hist = (unsigned*)p;
     const int nb = rs_nblocks(n);
+    p += align256((size_t)256 * nb * 4);
+    unsigned* tot = (unsigned*)p;
     const int passes = (bits + 7) / 8;
     unsigned* ki = keys;
     int* vi = vals;
@@ -202,8 +287,9 @@ static int radix_sort(unsigned* keys, int* vals, int n, int bits, void* ws, size
     for (int pass = 0; pass < passes; ++pass) {
         const int shift = 8 * pass;
         launch(rs_upsweep, nb, RS_BLOCK, 0, s, ki, n, shift, hist, nb);
-        launch(scan_single_block, 1, 1024, 0, s, hist, 256 * nb, 0);
-        launch(rs_scatter, nb, RS_BLOCK, 0, s, ki, vi, ko, vo, n, shift, hist, nb);
+        launch(rs_digit_scan, 256, RS_BLOCK, 0, s, hist, nb, tot);
+        launch(rs_scatter, nb, RS_BLOCK, 0, s, ki, vi, ko, vo, n, shift, (const unsigned*)hist, (const unsigned*)tot,
+               nb);
         unsigned* tk = ki; ki = ko; ko = tk;
         int* tv = vi; vi = vo; vo = tv;
     }
@@ -648,6 +734,106 @@ __global__ void face_refit_kernel(int n, const int* __restrict__ sorted_ids, con
     }
 }
 
+// The same refit with its lower levels in shared memory.  A Karras node
+// covers a contiguous range of sorted leaves and carries the index of one of
+// its ends, so every node whose range lies inside a block's tile of 256 leaves
+// has its index in the tile as well: the block keeps those nodes' boxes and
+// arrival counters in shared memory (block-scope fences, no global atomics).
+// A thread that climbs out of the tile continues with the global protocol of
+// face_refit_kernel.  Each thread carries its current box in registers; every
+// internal box is also written to global memory.  Min and max are exact, so
+// the boxes are the same as the one-thread-per-leaf climb's.
+constexpr int FR_TILE = 256;
+
+// node c (internal 0..n-2 or leaf n-1+j) has its slot in the tile [B, tile_end]
+__device__ __forceinline__ bool in_tile(int c, int n, int B, int tile_end) {
+    const int k = c >= n - 1 ? c - (n - 1) : c;
+    return k >= B && k <= tile_end;
+}
+
+__global__ void __launch_bounds__(FR_TILE) face_refit_tiled_kernel(
+    int n, const int* __restrict__ sorted_ids, const float4* __restrict__ fmn4, const float4* __restrict__ fmx4,
+    const int* __restrict__ child_a, const int* __restrict__ child_b, const int* __restrict__ parent,
+    const int* __restrict__ range_l, const int* __restrict__ range_r, float4* nmin4, float4* nmax4, int* flags,
+    int* status) {
+    pdl_entry();
+    __shared__ float4 s_leaf[2][FR_TILE];
+    __shared__ float4 s_node[2][FR_TILE];
+    __shared__ int s_flag[FR_TILE];
+    const int B = blockIdx.x * FR_TILE, t = threadIdx.x, j = B + t;
+    s_flag[t] = 0;
+    float4 lo = make_float4(0.f, 0.f, 0.f, 0.f), hi = lo;
+    if (j < n) {
+        const int f = sorted_ids[j];
+        lo = fmn4[f];
+        hi = fmx4[f];
+        nmin4[n - 1 + j] = lo;
+        nmax4[n - 1 + j] = hi;
+        s_leaf[0][t] = lo;
+        s_leaf[1][t] = hi;
+    }
+    __syncthreads();
+    if (j >= n || n == 1) return;
+    const int tile_end = min(B + FR_TILE, n) - 1;  // last leaf of the tile
+    int me = n - 1 + j;
+    int node = parent[me];
+    bool local = true;
+    // topology of the current node; the next level's is loaded before this
+    // level's arrival counter, so that only the counter and the sibling's box
+    // are round trips on the climb's critical path
+    int ca = 0, cb = 0, up = -1, rl = 0, rr = 0;
+    if (node >= 0) {
+        ca = __ldg(child_a + node); cb = __ldg(child_b + node); up = __ldg(parent + node);
+        rl = __ldg(range_l + node); rr = __ldg(range_r + node);
+    }
+    for (int steps = 0; node >= 0; ++steps) {
+        if (steps > n) {
+            atomicOr(status, SX_STATUS_CLIMB_LIMIT);
+            return;
+        }
+        int nca = 0, ncb = 0, nup = -1, nrl = 0, nrr = 0;
+        if (up >= 0) {
+            nca = __ldg(child_a + up); ncb = __ldg(child_b + up); nup = __ldg(parent + up);
+            nrl = __ldg(range_l + up); nrr = __ldg(range_r + up);
+        }
+        const int sib = ca == me ? cb : ca;
+        float4 slo, shi;
+        // local: the node and both children lie in the tile (decided from the
+        // node alone, so both children agree; always true below a node whose
+        // range is in the tile when the hierarchy is well formed)
+        if (local && node >= B && node <= tile_end && rl >= B && rr <= tile_end && in_tile(ca, n, B, tile_end) &&
+            in_tile(cb, n, B, tile_end)) {
+            __threadfence_block();
+            if (atomicAdd(s_flag + (node - B), 1) == 0) return;
+            __threadfence_block();
+            const bool sib_leaf = sib >= n - 1;
+            const int k = sib_leaf ? sib - (n - 1) - B : sib - B;
+            slo = sib_leaf ? s_leaf[0][k] : s_node[0][k];
+            shi = sib_leaf ? s_leaf[1][k] : s_node[1][k];
+        } else {
+            local = false;
+            // release: this thread's box stores are visible before the count;
+            // acquire: the sibling's are visible to the loads below
+            cuda::atomic_ref<int, cuda::thread_scope_device> cnt(flags[node]);
+            if (cnt.fetch_add(1, cuda::memory_order_acq_rel) == 0) return;
+            flags[node] = 0;
+            slo = __ldcg(nmin4 + sib);
+            shi = __ldcg(nmax4 + sib);
+        }
+        const V3 a = vmin(mk(lo), mk(slo)), b = vmax(mk(hi), mk(shi));
+        store_box(nmin4, nmax4, node, a, b);
+        lo = make_float4(a.x, a.y, a.z, 0.f);
+        hi = make_float4(b.x, b.y, b.z, 0.f);
+        if (local) {
+            s_node[0][node - B] = lo;
+            s_node[1][node - B] = hi;
+        }
+        me = node;
+        node = up;
+        ca = nca; cb = ncb; up = nup; rl = nrl; rr = nrr;
+    }
+}
+
 __global__ void __launch_bounds__(128) face_traverse_kernel(int n, int Q, const float4* __restrict__ p4, float pad,
                                                             const int* __restrict__ child_a,
                                                             const int* __restrict__ child_b,
@@ -744,7 +930,7 @@ extern "C" int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, v
 constexpr int kNoAllocMaxKeys = 1 << 18;
 constexpr size_t kNoAllocScratchBytes =
     2 * (((size_t)kNoAllocMaxKeys * 4 + 255) & ~(size_t)255) +
-    (((size_t)256 * ((kNoAllocMaxKeys + RS_TILE - 1) / RS_TILE) * 4 + 255) & ~(size_t)255);
+    (((size_t)256 * ((kNoAllocMaxKeys + RS_TILE - 1) / RS_TILE) * 4 + 255) & ~(size_t)255) + 256 * 4;
 static __device__ __align__(256) unsigned char g_sort_scratch[kNoAllocScratchBytes];
 
 constexpr int kMaxDevices = 64;
@@ -895,6 +1081,20 @@ extern "C" int sx_face_bvh_refit(int n, const int* sorted_ids, const float* fmin
         n, sorted_ids, (const float4*)fmin4, (const float4*)fmax4, child_a, child_b, parent, (float4*)nmin4,
         (float4*)nmax4, flags, status);
     return check_launch("face_refit_kernel");
+}
+
+extern "C" int sx_face_bvh_refit_tiled(int n, const int* sorted_ids, const float* fmin4, const float* fmax4,
+                                       const int* child_a, const int* child_b, const int* parent, const int* range_l,
+                                       const int* range_r, float* nmin4, float* nmax4, int* flags, int* status,
+                                       void* stream) {
+    SX_REQUIRE(n >= 1, "sx_face_bvh_refit_tiled: n must be >= 1");
+    SX_REQUIRE(sorted_ids && fmin4 && fmax4 && parent && nmin4 && nmax4 && status &&
+                   (n == 1 || (child_a && child_b && flags && range_l && range_r)),
+               "sx_face_bvh_refit_tiled: null pointer");
+    launch(face_refit_tiled_kernel, grid_for(n, FR_TILE), FR_TILE, 0, as_stream(stream), n, sorted_ids,
+           (const float4*)fmin4, (const float4*)fmax4, child_a, child_b, parent, range_l, range_r, (float4*)nmin4,
+           (float4*)nmax4, flags, status);
+    return check_launch("face_refit_tiled_kernel");
 }
 
 extern "C" int sx_face_bvh_traverse(int n, const float* p4, int n_queries, float padding, const int* child_a,

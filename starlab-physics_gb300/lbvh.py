@@ -159,9 +159,17 @@ class LBVH:
                            ptr(self.range_l), ptr(self.range_r), ptr(self.parent), stream_handle())
 
     def refit(self, face_min4, face_max4):
-        sx.sx_face_bvh_refit(self.n, ptr(self.sorted_ids), ptr(face_min4), ptr(face_max4), ptr(self.child_a),
-                             ptr(self.child_b), ptr(self.parent), ptr(self.node_min4), ptr(self.node_max4),
-                             ptr(self.flags), ptr(self.status), stream_handle())
+        if self.tie != 1:
+            # the reference's tie rule can give a malformed hierarchy on repeated
+            # codes: the plain one-thread-per-leaf climb handles that case
+            sx.sx_face_bvh_refit(self.n, ptr(self.sorted_ids), ptr(face_min4), ptr(face_max4), ptr(self.child_a),
+                                 ptr(self.child_b), ptr(self.parent), ptr(self.node_min4), ptr(self.node_max4),
+                                 ptr(self.flags), ptr(self.status), stream_handle())
+            return
+        sx.sx_face_bvh_refit_tiled(self.n, ptr(self.sorted_ids), ptr(face_min4), ptr(face_max4), ptr(self.child_a),
+                                   ptr(self.child_b), ptr(self.parent), ptr(self.range_l), ptr(self.range_r),
+                                   ptr(self.node_min4), ptr(self.node_max4), ptr(self.flags), ptr(self.status),
+                                   stream_handle())
 
     def build(self, face_min4, face_max4, box6):
         self.morton(face_min4, face_max4, box6)

@@ -224,6 +224,23 @@ def test_cell_traverse_adversarial(pkg, po, size, seed):
             assert np.array_equal(gc[q, :k], rc[q, :k]), q
 
 
+@pytest.mark.parametrize("n", [1, 2, 3, 255, 257, 1000, 5000])
+def test_face_lbvh_tiled_refit_ragged(pkg, po, n):
+    """The shared-memory refit (tiles of 256 sorted leaves) at sizes that are
+    not multiples of the tile: node boxes equal the oracle's bit for bit."""
+    verts, faces, _ = pkg.scenes.triangle_soup(n, seed=n)
+    V4 = np.zeros((verts.shape[0], 4), np.float32)
+    V4[:, :3] = verts
+    mn, mx = po.face_aabbs(V4, faces, 0.0)
+    box = po.scene_aabb(V4, 0.0)
+    bvh = pkg.LBVH(n, DEV, tie=1)
+    bvh.build(_t(mn), _t(mx), _t(box))
+    ref = po.FaceBVH(mn, mx, box, tie=1)
+    assert np.array_equal(_np(bvh.node_min4), ref.nmin4)
+    assert np.array_equal(_np(bvh.node_max4), ref.nmax4)
+    assert int(bvh.status.item()) == 0
+
+
 def test_face_lbvh_small_soup(pkg, po):
     verts, faces, queries = pkg.scenes.triangle_soup(1 << 14, seed=5)
     V4 = np.zeros((verts.shape[0], 4), np.float32)
