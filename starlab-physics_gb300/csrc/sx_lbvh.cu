@@ -143,34 +143,77 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_digit_scan(unsigned* __restrict__
     if (threadIdx.x == 0) tot[blockIdx.x] = carry;
 }
 
-// Single-block scan over n entries (exclusive or inclusive), 1024 threads.
-// Each warp owns a contiguous chunk that its lanes read 32 consecutive
-// elements at a time (coalesced); a shuffle scan combines each group of 32 and
-// the warp chunk totals are scanned across warps in shared memory.
+// Single-block scan over n entries (exclusive or inclusive), 1024 threads, in
+// segments of 32768 staged in (dynamic) shared memory: one coalesced load of
+// the segment, each thread sums 32 consecutive entries (one padding word per
+// 32 keeps those reads on distinct banks), a block scan of the sums (warp
+// shuffles, then the 32 warp totals), each thread rewrites its 32, one
+// coalesced store; the running total carries into the next segment.
+constexpr int SCAN_SEG = 32768;
+constexpr int SCAN_PER = SCAN_SEG / 1024;
+constexpr size_t SCAN_SMEM = (size_t)(SCAN_SEG + SCAN_SEG / 32) * 4;
+
+__device__ __forceinline__ int scan_slot(int i) { return i + (i >> 5); }
+
 __global__ void __launch_bounds__(1024) scan_single_block(unsigned* data, int n, int inclusive) {
     pdl_entry();
+    extern __shared__ unsigned seg[];
     __shared__ unsigned wsum[32];
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    const int chunk = ((n + 31) / 32 + 31) / 32 * 32;
-    const int beg = min(w * chunk, n), end = min(beg + chunk, n);
-    unsigned tot = 0;
-    for (int i = beg + lane; i < end; i += 32) tot += data[i];
-    for (int o = 16; o > 0; o >>= 1) tot += __shfl_xor_sync(0xffffffffu, tot, o);
-    if (lane == 0) wsum[w] = tot;
-    __syncthreads();
-    unsigned run = 0;
-    for (int k = 0; k < w; ++k) run += wsum[k];
-    for (int i0 = beg; i0 < end; i0 += 32) {
-        const int i = i0 + lane;
-        const unsigned v = i < end ? data[i] : 0u;
-        unsigned incl = v;
+    const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+    unsigned carry = 0;
+    for (int s0 = 0; s0 < n; s0 += SCAN_SEG) {
+        const int m = min(SCAN_SEG, n - s0);
+#pragma unroll 8
+        for (int i = tid; i < SCAN_SEG; i += 1024) seg[scan_slot(i)] = i < m ? data[s0 + i] : 0u;
+        __syncthreads();
+        unsigned sum = 0;
+#pragma unroll
+        for (int k = 0; k < SCAN_PER; ++k) sum += seg[scan_slot(tid * SCAN_PER + k)];
+        unsigned incl = sum;
+#pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
-            unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
+            const unsigned t = __shfl_up_sync(0xffffffffu, incl, o);
             if (lane >= o) incl += t;
         }
-        if (i < end) data[i] = run + (inclusive ? incl : incl - v);
-        run += __shfl_sync(0xffffffffu, incl, 31);
+        if (lane == 31) wsum[w] = incl;
+        __syncthreads();
+        unsigned before = 0, total = 0;
+        for (int k = 0; k < 32; ++k) {
+            before += k < w ? wsum[k] : 0u;
+            total += wsum[k];
+        }
+        unsigned run = carry + before + incl - sum;
+#pragma unroll
+        for (int k = 0; k < SCAN_PER; ++k) {
+            const int j = scan_slot(tid * SCAN_PER + k);
+            const unsigned x = seg[j];
+            seg[j] = inclusive ? run + x : run;
+            run += x;
+        }
+        __syncthreads();
+#pragma unroll 8
+        for (int i = tid; i < m; i += 1024) data[s0 + i] = seg[scan_slot(i)];
+        carry += total;
+        __syncthreads();
     }
+}
+
+// The shared-memory limit is raised once per process; sx_cell_bvh_init does it
+// first, outside any stream capture.
+static cudaError_t scan_smem_attr() {
+    static std::once_flag once;
+    static cudaError_t attr = cudaSuccess;
+    std::call_once(once, [] {
+        attr = cudaFuncSetAttribute(scan_single_block, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)SCAN_SMEM);
+    });
+    return attr;
+}
+
+static int launch_scan_single_block(unsigned* data, int n, int inclusive, cudaStream_t s) {
+    const cudaError_t attr = scan_smem_attr();
+    if (attr != cudaSuccess) return cuda_status(attr, "cudaFuncSetAttribute(scan_single_block)");
+    launch(scan_single_block, 1, 1024, SCAN_SMEM, s, data, n, inclusive);
+    return check_launch("scan_single_block");
 }
 
 __global__ void __launch_bounds__(RS_BLOCK) rs_scatter(const unsigned* __restrict__ kin,
@@ -254,8 +297,7 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_scatter(const unsigned* __restric
 
 int scan_u32(unsigned* data, int n, int inclusive, cudaStream_t s) {
     if (n <= 0) return SX_OK;
-    launch(scan_single_block, 1, 1024, 0, s, data, n, inclusive);
-    return check_launch("scan_single_block");
+    return launch_scan_single_block(data, n, inclusive, s);
 }
 
 static inline size_t align256(size_t b) { return (b + 255) & ~(size_t)255; }
@@ -993,6 +1035,8 @@ extern "C" int sx_cell_bvh_init(int* sorted_codes, int* sorted_ids, int* child_a
     SX_REQUIRE(sorted_codes && sorted_ids && child_a && child_b && range_l && range_r && parent,
                "sx_cell_bvh_init: null pointer");
     SX_REQUIRE(ws && ws_bytes >= sx_cell_bvh_workspace_bytes(0), "sx_cell_bvh_init: workspace too small");
+    const cudaError_t attr = scan_smem_attr();  // for sx_cell_bvh_build's prefix scan
+    if (attr != cudaSuccess) return cuda_status(attr, "cudaFuncSetAttribute(scan_single_block)");
     cudaStream_t s = as_stream(stream);
     launch(cell_morton_kernel, grid_for(kNumCells, 256), 256, 0, s, (unsigned*)sorted_codes, sorted_ids);
     int rc = check_launch("cell_morton_kernel");
@@ -1025,7 +1069,8 @@ extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_f
            box6, keys, sorted_face_ids, (unsigned*)prefix, grid8);
     int rc = check_launch("face_cell_kernel");
     if (rc) return rc;
-    launch(scan_single_block, 1, 1024, 0, s, (unsigned*)prefix, kNumCells, 1);
+    rc = launch_scan_single_block((unsigned*)prefix, kNumCells, 1, s);
+    if (rc) return rc;
     if (n_faces > 1) {
         rc = radix_sort(keys, sorted_face_ids, n_faces, 15, rws, rs_ws_bytes(n_faces), s);
         if (rc) return rc;
