@@ -224,10 +224,11 @@ def test_cell_traverse_adversarial(pkg, po, size, seed):
             assert np.array_equal(gc[q, :k], rc[q, :k]), q
 
 
-@pytest.mark.parametrize("n", [1, 2, 3, 255, 257, 1000, 5000])
+@pytest.mark.parametrize("n", [1, 2, 3, 255, 257, 1000, 5000, 4800 * 256 + 7])
 def test_face_lbvh_tiled_refit_ragged(pkg, po, n):
-    """The shared-memory refit (tiles of 256 sorted leaves) at sizes that are
-    not multiples of the tile: node boxes equal the oracle's bit for bit."""
+    """The shared-memory refit (tiles of 256 sorted leaves, a climb above
+    them) at sizes that are not multiples of the tile: node boxes equal the
+    oracle's bit for bit."""
     verts, faces, _ = pkg.scenes.triangle_soup(n, seed=n)
     V4 = np.zeros((verts.shape[0], 4), np.float32)
     V4[:, :3] = verts
