@@ -56,6 +56,8 @@ def parse_args():
     ap.add_argument("--only-batched", action="store_true", help="run only the 512-cloth batched measurement")
     ap.add_argument("--no-learned", action="store_true", help="skip the learned warm-start measurement")
     ap.add_argument("--only-learned", action="store_true", help="run only the learned warm-start measurement")
+    ap.add_argument("--only-lbvh", action="store_true",
+                    help="run only the standalone 2^20-triangle LBVH measurement (no CPU baseline)")
     return ap.parse_args()
 
 
@@ -568,6 +570,9 @@ def main():
     _lib.load()
     if args.only_batched:
         print(json.dumps({"batched512": batched512(pkg, steps=args.steps, warmup=args.warmup)}))
+        return
+    if args.only_lbvh:
+        print(json.dumps({"lbvh_soup": lbvh_soup(pkg, with_cpu=False)}))
         return
     if args.only_learned:
         print(json.dumps({"learned_batched512": learned_batched(pkg)}))

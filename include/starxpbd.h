@@ -267,6 +267,12 @@ int sx_face_bvh_refit_tiled(int n, const int* sorted_ids, const float* fmin4, co
 int sx_face_bvh_traverse(int n, const float* p4, int n_queries, float padding, const int* child_a,
                          const int* child_b, const int* sorted_ids, const float* nmin4, const float* nmax4, int cap,
                          int* cand, int* num, int* status, void* stream);
+/* sx_face_bvh_traverse visiting the queries in the order order[0..n_queries)
+ * (a permutation, e.g. the queries sorted by Morton code: a warp then walks
+ * nearby parts of the tree).  Results are per query and do not depend on it. */
+int sx_face_bvh_traverse_ordered(int n, const float* p4, int n_queries, float padding, const int* child_a,
+                                 const int* child_b, const int* sorted_ids, const float* nmin4, const float* nmax4,
+                                 int cap, int* cand, int* num, int* status, const int* order, void* stream);
 
 /* ---- narrow phase + contact projection ------------------------------------ */
 

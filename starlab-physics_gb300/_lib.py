@@ -66,6 +66,7 @@ SIGNATURES = {
     "sx_face_bvh_refit": ([I, P, P, P, P, P, P, P, P, P, P, P], I),
     "sx_face_bvh_refit_tiled": ([I, P, P, P, P, P, P, P, P, P, P, P, P, P], I),
     "sx_face_bvh_traverse": ([I, P, I, F, P, P, P, P, P, I, P, P, P, P], I),
+    "sx_face_bvh_traverse_ordered": ([I, P, I, F, P, P, P, P, P, I, P, P, P, P, P], I),
     "sx_collision_sweep": ([I, I, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, P], I),
     "sx_contact_pairs_workspace_bytes": ([I, I], Z),
     "sx_contact_pairs_build": ([I, I, P, P, I, P, P, P, P, P, P, P, C.c_longlong, P, Z, P], I),

@@ -883,10 +883,13 @@ __global__ void __launch_bounds__(128) face_traverse_kernel(int n, int Q, const 
                                                             const float4* __restrict__ nmin4,
                                                             const float4* __restrict__ nmax4, int cap,
                                                             int* __restrict__ cand, int* __restrict__ num,
-                                                            int* status) {
+                                                            int* status, const int* __restrict__ order) {
     pdl_entry();
-    int q = blockIdx.x * blockDim.x + threadIdx.x;
-    if (q >= Q) return;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= Q) return;
+    // order (optional): the queries in a spatially coherent order, so that a
+    // warp's threads walk nearby parts of the tree
+    const int q = order ? order[i] : i;
     V3 p = mk(p4[q]);
     V3 a{p.x - pad, p.y - pad, p.z - pad}, b{p.x + pad, p.y + pad, p.z + pad};
     int count = 0, flags = 0;
@@ -1151,6 +1154,21 @@ extern "C" int sx_face_bvh_traverse(int n, const float* p4, int n_queries, float
                "sx_face_bvh_traverse: null pointer");
     launch(face_traverse_kernel, grid_for(n_queries, 128), 128, 0, as_stream(stream), 
         n, n_queries, (const float4*)p4, padding, child_a, child_b, sorted_ids, (const float4*)nmin4,
-        (const float4*)nmax4, cap, cand, num, status);
+        (const float4*)nmax4, cap, cand, num, status, (const int*)nullptr);
+    return check_launch("face_traverse_kernel");
+}
+
+extern "C" int sx_face_bvh_traverse_ordered(int n, const float* p4, int n_queries, float padding,
+                                            const int* child_a, const int* child_b, const int* sorted_ids,
+                                            const float* nmin4, const float* nmax4, int cap, int* cand, int* num,
+                                            int* status, const int* order, void* stream) {
+    SX_REQUIRE(n >= 1 && n_queries >= 0 && cap >= 1, "sx_face_bvh_traverse_ordered: bad sizes");
+    if (n_queries == 0) return SX_OK;
+    SX_REQUIRE(p4 && sorted_ids && nmin4 && nmax4 && cand && num && status && order &&
+                   (n == 1 || (child_a && child_b)),
+               "sx_face_bvh_traverse_ordered: null pointer");
+    launch(face_traverse_kernel, grid_for(n_queries, 128), 128, 0, as_stream(stream), n, n_queries,
+           (const float4*)p4, padding, child_a, child_b, sorted_ids, (const float4*)nmin4, (const float4*)nmax4, cap,
+           cand, num, status, order);
     return check_launch("face_traverse_kernel");
 }

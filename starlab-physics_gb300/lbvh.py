@@ -172,6 +172,7 @@ class LBVH:
                                    stream_handle())
 
     def build(self, face_min4, face_max4, box6):
+        self.box6 = box6
         self.morton(face_min4, face_max4, box6)
         self.sort()
         self.hierarchy()
@@ -185,7 +186,31 @@ class LBVH:
             num = torch.empty(q, dtype=torch.int32, device=self.device)
         if status is None:
             status = self.status
+        if q >= self.COHERENT_MIN_QUERIES and getattr(self, "box6", None) is not None:
+            # visit the queries in Morton order of the points (normalised by the
+            # build's box): a warp's threads then walk nearby parts of the tree
+            order = self._query_order(points4, q)
+            sx.sx_face_bvh_traverse_ordered(self.n, ptr(points4), q, float(padding), ptr(self.child_a),
+                                            ptr(self.child_b), ptr(self.sorted_ids), ptr(self.node_min4),
+                                            ptr(self.node_max4), int(cap), ptr(cand), ptr(num), ptr(status),
+                                            ptr(order), stream_handle())
+            return cand, num
         sx.sx_face_bvh_traverse(self.n, ptr(points4), q, float(padding), ptr(self.child_a), ptr(self.child_b),
                                 ptr(self.sorted_ids), ptr(self.node_min4), ptr(self.node_max4), int(cap), ptr(cand),
                                 ptr(num), ptr(status), stream_handle())
         return cand, num
+
+    COHERENT_MIN_QUERIES = 1 << 14
+
+    def _query_order(self, points4, q):
+        if getattr(self, "_q_n", None) != q:
+            i32 = dict(dtype=torch.int32, device=self.device)
+            self._q_codes = torch.empty(q, **i32)
+            self._q_order = torch.empty(q, **i32)
+            self._q_ws = torch.empty(int(sx.sx_radix_sort_workspace_bytes(q)), dtype=torch.uint8, device=self.device)
+            self._q_n = q
+        sx.sx_face_morton(ptr(points4), ptr(points4), q, ptr(self.box6), ptr(self._q_codes), ptr(self._q_order),
+                          stream_handle())
+        sx.sx_radix_sort_pairs(ptr(self._q_codes), ptr(self._q_order), q, 30, ptr(self._q_ws), self._q_ws.numel(),
+                               stream_handle())
+        return self._q_order
