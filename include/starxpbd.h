@@ -221,7 +221,8 @@ int sx_face_morton(const float* fmin4, const float* fmax4, int n_faces, const fl
 /* Stable LSD radix sort of (key, value) pairs on the low `bits` key bits
  * (radix_sort_cells, lbvh_cell.py:525-562: the reference uses 6-bit digits and
  * a serialised scatter; here 8-bit digits, per-block histograms and a
- * warp-ranked stable scatter give the same permutation). In place. */
+ * warp-ranked stable scatter give the same permutation). In place. Key bits
+ * at and above `bits` take no part in the order: they move with their key. */
 size_t sx_radix_sort_workspace_bytes(int n);
 int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, void* ws, size_t ws_bytes, void* stream);
 
@@ -233,9 +234,12 @@ int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, void* ws, si
  * held on every GPU that loads the library until the process exits).
  * n is limited to 262144 (2^18) keys; larger n returns SX_ERR_ARG.  The first
  * call on a device looks up the array's device address with that device
- * current; make that first call before any stream capture.  All calls share
- * the array, so calls that overlap on the GPU race and must be ordered by the
- * caller.  This entry point has no counterpart in the reference. */
+ * current; make that first call before any stream capture.  The address is
+ * kept for the life of the process: after cudaDeviceReset (or anything else
+ * that re-creates the device's primary context) this entry point must not be
+ * called again in that process.  All calls share the array, so calls that
+ * overlap on the GPU race and must be ordered by the caller.  This entry point
+ * has no counterpart in the reference. */
 int sx_radix_sort_pairs_noalloc(unsigned* keys, int* vals, int n, int bits, void* stream);
 
 /* Karras 2012 hierarchy over sorted codes (assign_internal_nodes_Karras12,

@@ -85,7 +85,7 @@ constexpr int RS_TILE = RS_BLOCK * RS_ITEMS;
 constexpr int RS_WARPS = RS_BLOCK / 32;
 
 __global__ void __launch_bounds__(RS_BLOCK) rs_upsweep(const unsigned* __restrict__ keys, int n, int shift,
-                                                       unsigned* __restrict__ hist, int nblocks) {
+                                                       unsigned dmask, unsigned* __restrict__ hist, int nblocks) {
     pdl_entry();
     __shared__ unsigned cnt[256];
     const int tid = threadIdx.x;
@@ -95,7 +95,7 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_upsweep(const unsigned* __restric
 #pragma unroll
     for (int r = 0; r < RS_ITEMS; ++r) {
         long long idx = base + r * RS_BLOCK + tid;
-        if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & 255u], 1u);
+        if (idx < n) atomicAdd(&cnt[(keys[idx] >> shift) & dmask], 1u);
     }
     __syncthreads();
     hist[(size_t)tid * nblocks + blockIdx.x] = cnt[tid];
@@ -218,7 +218,7 @@ static int launch_scan_single_block(unsigned* data, int n, int inclusive, cudaSt
 
 __global__ void __launch_bounds__(RS_BLOCK) rs_scatter(const unsigned* __restrict__ kin,
                                                        const int* __restrict__ vin, unsigned* __restrict__ kout,
-                                                       int* __restrict__ vout, int n, int shift,
+                                                       int* __restrict__ vout, int n, int shift, unsigned dmask,
                                                        const unsigned* __restrict__ hist,
                                                        const unsigned* __restrict__ tot, int nblocks) {
     pdl_entry();
@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_scatter(const unsigned* __restric
 #pragma unroll
     for (int r = 0; r < RS_ITEMS; ++r) {
         const bool valid = base + r * 32 + lane < n;
-        const unsigned digit = valid ? ((key[r] >> shift) & 255u) : 256u;
+        const unsigned digit = valid ? ((key[r] >> shift) & dmask) : 256u;
         const unsigned peers = __match_any_sync(0xffffffffu, digit);
         const unsigned before = valid ? cnt[digit] : 0u;
         rank[r] = before + __popc(peers & lt_mask);
@@ -277,7 +277,7 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_scatter(const unsigned* __restric
 #pragma unroll
     for (int r = 0; r < RS_ITEMS; ++r) {
         if (base + r * 32 + lane < n) {
-            const unsigned lp = cnt[(key[r] >> shift) & 255u] + rank[r];
+            const unsigned lp = cnt[(key[r] >> shift) & dmask] + rank[r];
             s_key[lp] = key[r];
             s_val[lp] = val[r];
         }
@@ -288,7 +288,7 @@ __global__ void __launch_bounds__(RS_BLOCK) rs_scatter(const unsigned* __restric
     const int count = (int)min((long long)RS_TILE, (long long)n - tile);
     for (int i = tid; i < count; i += RS_BLOCK) {
         const unsigned k = s_key[i];
-        const unsigned d = (k >> shift) & 255u;
+        const unsigned d = (k >> shift) & dmask;
         const unsigned g = s_gbase[d] + ((unsigned)i - s_lbase[d]);
         kout[g] = k;
         vout[g] = s_val[i];
@@ -328,10 +328,14 @@ static int radix_sort(unsigned* keys, int* vals, int n, int bits, void* ws, size
     int* vo = valt;
     for (int pass = 0; pass < passes; ++pass) {
         const int shift = 8 * pass;
-        launch(rs_upsweep, nb, RS_BLOCK, 0, s, ki, n, shift, hist, nb);
+        // the last digit keeps only the key bits below `bits`: keys are ordered
+        // by their low `bits` bits, higher bits ride along unsorted
+        const int width = bits - shift < 8 ? bits - shift : 8;
+        const unsigned dmask = (1u << width) - 1u;
+        launch(rs_upsweep, nb, RS_BLOCK, 0, s, ki, n, shift, dmask, hist, nb);
         launch(rs_digit_scan, 256, RS_BLOCK, 0, s, hist, nb, tot);
-        launch(rs_scatter, nb, RS_BLOCK, 0, s, ki, vi, ko, vo, n, shift, (const unsigned*)hist, (const unsigned*)tot,
-               nb);
+        launch(rs_scatter, nb, RS_BLOCK, 0, s, ki, vi, ko, vo, n, shift, dmask, (const unsigned*)hist,
+               (const unsigned*)tot, nb);
         unsigned* tk = ki; ki = ko; ko = tk;
         int* tv = vi; vi = vo; vo = tv;
     }
@@ -967,7 +971,9 @@ extern "C" int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, v
 // In host code the array's name is only a host-side stand-in for the symbol, so
 // its device address is looked up once per device, on the first call made with
 // that device current, with cudaGetSymbolAddress; that first call should come
-// before any stream capture.  All calls share the array: calls that overlap on
+// before any stream capture.  The cached address is never refreshed: a
+// cudaDeviceReset re-creates the context and may move the array, so callers
+// must not use this entry point after resetting the device.  All calls share the array: calls that overlap on
 // the GPU (different streams, or threads) race on it and must be ordered by the
 // caller.  Nothing in it needs clearing: every pass overwrites the histogram
 // and both ping-pong buffers before reading them.

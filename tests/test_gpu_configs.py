@@ -1,0 +1,163 @@
+"""Parity on the benchmark configurations themselves, at full size.
+
+Each test runs the CUDA solver and the CPU oracle on the same seeded inputs and
+checks the acceptance criteria of the substep: positions bit for bit equal,
+max |dx| <= 1e-4 x the cloth's bounding-box diagonal, and the constraint
+residual (RMS of C = |p0 - p1| - l0, ``sx_constraint_residual``) within 1 % of
+the oracle's.  Bit-equality implies the other two; they are asserted
+separately so that a failure says which criterion broke.
+
+* 64 x 64 cloth over a box, 10 substeps x 20 Jacobi iterations, 60 frames.
+* 256 x 256 cloth draped over a 20480-face sphere with self contact, BVHs
+  rebuilt every substep, 10 substeps x 30 iterations, 60 substeps (6 frames),
+  replayed as a captured CUDA graph as the benchmark runs it.
+* 512 batched cloths (grid side uniform in [16, 128]): the batch runs on the
+  GPU; the smallest, the largest, the one whose box is nearest the cloth and
+  five seeded picks are each run alone by the oracle.
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+NTHREADS = os.cpu_count() or 1
+POS_TOL = 1e-4   # x bounding-box diagonal
+RES_TOL = 0.01   # relative
+
+
+def _np(t):
+    return t.detach().cpu().numpy()
+
+
+def _oracle_for(pkg, po, scene, sim):
+    return po.OracleSolver(pkg.scenes.oracle_inputs(sim.mesh_dy),
+                           pkg.scenes.oracle_inputs(sim.mesh_st) if sim.mesh_st is not None else None,
+                           dt=scene.dt, g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
+                           k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
+                           padding=scene.padding, n_iter=scene.n_iter, collisions=scene.collisions,
+                           rebuild=scene.rebuild, cap=scene.cap, bending_on=sim.bending_on,
+                           contact_cull=sim.contact_cull, nthreads=NTHREADS)
+
+
+def _check(po, got4, orc_x4, adj_ptr, adj, diag, what):
+    got = got4[:, :3]
+    ref = orc_x4[:, :3]
+    assert np.isfinite(got).all(), what
+    dmax = float(np.abs(got.astype(np.float64) - ref).max())
+    assert dmax <= POS_TOL * diag, f"{what}: max |dx| {dmax:.3e} > {POS_TOL} x diagonal {diag:.4f}"
+    r_got = po.residual(np.ascontiguousarray(got4), adj_ptr, adj)
+    r_ref = po.residual(np.ascontiguousarray(orc_x4), adj_ptr, adj)
+    rms_got, rms_ref = np.sqrt(r_got[0] / r_got[1]), np.sqrt(r_ref[0] / r_ref[1])
+    assert abs(rms_got - rms_ref) <= RES_TOL * rms_ref, f"{what}: residual {rms_got:.6e} vs {rms_ref:.6e}"
+    assert np.array_equal(got, ref), f"{what}: not bit-exact (max |dx| {dmax:.3e})"
+    return dmax, rms_ref
+
+
+def test_plain64_box_60_frames(pkg, po):
+    """64 x 64 cloth (4096 vertices, 7938 faces, 12033 springs, 11781 bending
+    pairs), box obstacle, 10 substeps x 20 iterations, 60 frames."""
+    scene = pkg.scenes.plain64()
+    assert scene.n_substeps == 10 and scene.n_iter == 20
+    sim = pkg.scenes.make_solver(scene, device="cuda")
+    sim.bending_on = "y"
+    sim.use_graph = True
+    m = sim.mesh_dy
+    assert (m.num_verts, m.num_faces, m.num_edges, m.bending_constraint_count) == (4096, 7938, 12033, 11781)
+    orc = _oracle_for(pkg, po, scene, sim)
+    for _ in range(60):
+        sim.forward(scene.n_substeps)
+        orc.forward(scene.n_substeps)
+    torch.cuda.synchronize()
+    got = _np(m.x4)
+    _check(po, got, orc.x4, orc.adj_ptr, orc.adj, m.bbox_diagonal(), "plain64 after 60 frames")
+    # the cloth came down on the box: vertices rest on its top face (z = 0.55)
+    # instead of falling past it
+    on_top = (np.abs(got[:, 2] - 0.55) < 0.02) & (np.abs(got[:, 0] - 0.5) < 0.25) & (np.abs(got[:, 1] - 0.5) < 0.25)
+    assert on_top.sum() > 100
+    gpu_res = float(sim.constraint_residual("x")[2].item())
+    r = po.residual(orc.x4, orc.adj_ptr, orc.adj)
+    assert gpu_res == pytest.approx(np.sqrt(r[0] / r[1]), rel=RES_TOL)
+    # candidate lists longer than the reference's 40 slots are truncated and
+    # flagged by both (vertices on the box's top edges)
+    assert sim.status_flags() & 1 == orc.last_status & 1
+    assert sim.status_flags() & 4 == 0
+
+
+def test_drape256_60_substeps(pkg, po):
+    """256 x 256 cloth over the sphere with self contact, BVHs rebuilt every
+    substep, 10 substeps x 30 iterations, 6 frames, as a replayed graph."""
+    scene = pkg.scenes.drape256()
+    assert scene.n_iter == 30 and scene.rebuild == "substep"
+    sim = pkg.scenes.make_solver(scene, device="cuda")
+    sim.bending_on = "y"
+    sim.use_graph = True
+    m = sim.mesh_dy
+    assert (m.num_verts, m.num_faces) == (65536, 130050)
+    orc = _oracle_for(pkg, po, scene, sim)
+    for f in range(6):
+        sim.forward(scene.n_substeps)
+        orc.forward(scene.n_substeps)
+    torch.cuda.synchronize()
+    _check(po, _np(m.x4), orc.x4, orc.adj_ptr, orc.adj, m.bbox_diagonal(), "drape256 after 60 substeps")
+    assert np.array_equal(_np(m.v4)[:, :3], orc.v4[:, :3])
+    # contacts were active: the pair list of the last substep is not empty and
+    # the vertices over the sphere's cap are held above its top (z = 0.8)
+    assert sim.contact_pair_count() > 100_000
+    x = _np(m.x4)
+    cap_ = (x[:, 0] - 0.5) ** 2 + (x[:, 1] - 0.5) ** 2 < 0.05 ** 2
+    assert cap_.sum() > 100 and x[cap_, 2].min() > 0.8 - 2 * scene.meta["thickness"]
+    gpu_res = float(sim.constraint_residual("x")[2].item())
+    r = po.residual(orc.x4, orc.adj_ptr, orc.adj)
+    assert gpu_res == pytest.approx(np.sqrt(r[0] / r[1]), rel=RES_TOL)
+    assert sim.status_flags() & 1 == orc.last_status & 1
+    assert sim.status_flags() & 4 == 0
+
+
+def test_batched512_sampled_instances(pkg, po):
+    """512 cloths in one BatchedSolver (graph per frame), 10 substeps x 20
+    iterations, 10 frames; eight instances compared with the oracle run alone."""
+    from starlab_physics_gb300 import mesh as M
+
+    insts = pkg.batched_scene(512, seed=0)
+    kw = dict(dt=1 / 60, g=(0.0, 0.0, -9.81), k_stretch_stiffness=1e5, k_bend_stiffness=1e8, dHat=(4e-3) ** 2,
+              damping=0.001, padding=8e-3, n_iter=20, cap=40)
+    sim = pkg.BatchedSolver(insts, dHat=kw["dHat"], stiffness_stretch=1e5, stiffness_bending=1e8, g=kw["g"],
+                            dt=kw["dt"], n_iter=20, padding=8e-3)
+    assert 3.0e6 < sim.num_verts < 3.4e6
+    sim.use_graph = True
+    frames = 10
+    for _ in range(frames):
+        sim.forward(10)
+    torch.cuda.synchronize()
+    sides = np.array([int(round(np.sqrt(i.x.shape[0]))) for i in insts])
+    box_top = np.array([float(i.obstacle_x[:, 2].max()) for i in insts])
+    picks = [int(np.argmin(sides)), int(np.argmax(sides)), int(np.argmax(box_top))]
+    rng = np.random.default_rng(11)
+    for k in rng.permutation(len(insts)):
+        if len(picks) == 8:
+            break
+        if int(k) not in picks:
+            picks.append(int(k))
+    touched = 0
+    for i in picks:
+        inst = insts[i]
+        cl = M.TriMesh(inst.x, inst.faces, device="cpu")
+        cl.fixed[np.asarray(inst.pinned)] = 0.0
+        ob = M.TriMesh(inst.obstacle_x, inst.obstacle_faces, device="cpu")
+        orc = po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob), collisions=True,
+                              rebuild="substep", self_collision=False, bending_on="y", nthreads=NTHREADS, **kw)
+        for _ in range(frames):
+            orc.forward(10)
+        got = np.zeros_like(orc.x4)
+        got[:, :3] = _np(sim.instance_positions(i))
+        got[:, 3] = orc.x4[:, 3]
+        p = inst.x.astype(np.float64)
+        diag = float(np.linalg.norm(p.max(0) - p.min(0)))
+        _check(po, got, orc.x4, orc.adj_ptr, orc.adj, diag, f"instance {i} (side {sides[i]})")
+        # the box holds part of the cloth above the free-fall height
+        touched += int((orc.x4[:, 2] > 1.0 - 0.5 * 9.81 * (frames / 60) ** 2 + 0.01).sum() > 0)
+    assert touched >= 1
+    assert int(sim.status.item()) & 4 == 0
