@@ -176,6 +176,58 @@ API int or_spring_sweep(int V, int E, int B, const float* x4, float* y4, const f
     return 0;
 }
 
+// The same sweep as a per-vertex gather over the vertex-centric CSR (adjacency
+// entries in ascending constraint index: springs, then bending pairs), for
+// multithreaded runs that must equal the serial one bit for bit.  A vertex
+// meets its constraints in the order the serial loop above does, and from the
+// second endpoint the difference P[v] - P[u] is the exact negation of the
+// scatter's x10, so lij, C, schur (w0 + w1 commutes) and ld are the same bits
+// and -(w_self * ld * n_self) is the scattered term bit for bit.  ynew is
+// scratch of 4 V floats.
+API int or_spring_sweep_gather(int V, const float* x4, float* y4, const float* fixed, const float* m_inv,
+                               const int32_t* ptr, const int32_t* adj, float k_spring, float k_bend, int bend_on_y,
+                               float* ynew, int nthreads) {
+    int par = set_threads(nthreads);
+#pragma omp parallel for if (par) schedule(static, 256)
+    for (int v = 0; v < V; ++v) {
+        float d0 = 0.0f, d1 = 0.0f, d2 = 0.0f, cnt = 0.0f;
+        const float wv = fixed[v] * m_inv[v];
+        for (int e = ptr[v]; e < ptr[v + 1]; ++e) {
+            const uint32_t w = (uint32_t)adj[2 * e];
+            const int u = (int)(w & 0x7fffffffu);
+            const bool bending = (w >> 31) != 0;
+            float rest;
+            std::memcpy(&rest, &adj[2 * e + 1], 4);
+            const float k = bending ? k_bend : k_spring;
+            const float* P = (bending && !bend_on_y) ? x4 : y4;
+            V3 x = sub(v3(P + 4 * v), v3(P + 4 * u));
+            float lij = std::sqrt(dot(x, x));
+            float C = lij - rest;
+            float inv = 1.0f / lij;
+            V3 n = scale(inv, x);
+            float wu = fixed[u] * m_inv[u];
+            // the scatter evaluates (w0 + w1) with w0 of the constraint's first vertex
+            float schur = (wv + wu) * dot(n, n);
+            float ld = (k * C) / (k * schur + 1.0f);
+            float a = wv * ld;
+            d0 = d0 + -(a * n.x);
+            d1 = d1 + -(a * n.y);
+            d2 = d2 + -(a * n.z);
+            cnt = cnt + 1.0f;
+        }
+        float* o = ynew + 4 * (size_t)v;
+        const float* yi = y4 + 4 * (size_t)v;
+        o[0] = yi[0]; o[1] = yi[1]; o[2] = yi[2]; o[3] = yi[3];
+        if (cnt > 0.0f) {
+            o[0] = yi[0] + fixed[v] * (d0 / cnt);
+            o[1] = yi[1] + fixed[v] * (d1 / cnt);
+            o[2] = yi[2] + fixed[v] * (d2 / cnt);
+        }
+    }
+    std::memcpy(y4, ynew, sizeof(float) * 4 * (size_t)V);
+    return 0;
+}
+
 // XPBD.py:341-343 compute_velocity then XPBD.py:333-337 update_x
 API int or_velocity_update(int V, float* x4, const float* y4, float* v4, const float* fixed,
                            float damping, float dt, int nthreads) {

@@ -33,6 +33,7 @@ F = C.c_float
 _SIGS = {
     "or_predict": [I, P, P, P, P, F, F, F, F, I],
     "or_spring_sweep": [I, I, I, P, P, P, P, P, P, P, P, F, F, I, P, P, I],
+    "or_spring_sweep_gather": [I, P, P, P, P, P, P, F, F, I, P, I],
     "or_velocity_update": [I, P, P, P, P, F, F, I],
     "or_face_aabbs": [I, P, P, F, P, P],
     "or_scene_aabb": [I, P, F, P],
@@ -103,6 +104,16 @@ def spring_sweep(x4, y4, fixed, m_inv, edges, l0, bend, bl0, k_spring, k_bend, n
     nc = np.empty(V, np.float32)
     lib().or_spring_sweep(V, edges.shape[0], bend.shape[0], _p(x4), _p(y4), _p(fixed), _p(m_inv), _p(edges),
                           _p(l0), _p(bend), _p(bl0), k_spring, k_bend, int(bend_on_y), _p(dx), _p(nc), nthreads)
+    return y4
+
+
+def spring_sweep_gather(x4, y4, fixed, m_inv, ptr, adj, k_spring, k_bend, nthreads=1, bend_on_y=0):
+    """spring_sweep as a per-vertex gather over adjacency(): the serial sweep's
+    result bit for bit at any thread count.  Updates y4 in place."""
+    V = x4.shape[0]
+    scratch = np.empty((V, 4), np.float32)
+    lib().or_spring_sweep_gather(V, _p(x4), _p(y4), _p(fixed), _p(m_inv), _p(i32(ptr)), _p(i32(adj)), k_spring,
+                                 k_bend, int(bend_on_y), _p(scratch), nthreads)
     return y4
 
 
@@ -564,8 +575,13 @@ class OracleSolver:
                  damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
                  compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True,
                  contact_cull=False, tol=None, check_every=4, tol_relative=False, sewing=None,
-                 velocity_update=False, mu=0.8, edge_edge=False):
+                 velocity_update=False, mu=0.8, edge_edge=False, scatter_atomics=False):
         self.d = mesh_dy
+        # multithreaded spring sweeps: a deterministic per-vertex gather (equal
+        # to the serial sweep bit for bit) unless scatter_atomics, which runs
+        # the reference's scatter with float atomics (order dependent), the
+        # way a parallel Taichi CPU build executes it
+        self.scatter_atomics = scatter_atomics
         # edge-edge contacts (the reference's commented-out ee_st / ee_dy path)
         self.edge_edge = edge_edge
         # iterate to a residual (the CUDA solver's tol mode): every
@@ -686,8 +702,12 @@ class OracleSolver:
                         stop = it
                         self.stop_sum += it
                         self.converged += 1
-            spring_sweep(self.x4, y4, self.fixed, self.m_inv, self.edges, self.l0, self.bend, self.bl0, k_spring,
-                         k_bend, self.nthreads, self.bend_on_y)
+            if self.nthreads > 1 and not self.scatter_atomics:
+                spring_sweep_gather(self.x4, y4, self.fixed, self.m_inv, self.adj_ptr, self.adj, k_spring, k_bend,
+                                    self.nthreads, self.bend_on_y)
+            else:
+                spring_sweep(self.x4, y4, self.fixed, self.m_inv, self.edges, self.l0, self.bend, self.bl0, k_spring,
+                             k_bend, self.nthreads, self.bend_on_y)
             if self.collisions:
                 if it == 0:
                     cands = self._broad(y4)

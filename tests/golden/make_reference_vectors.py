@@ -19,7 +19,17 @@ seeded inputs and writes ``reference_vectors.npz`` beside this script:
 * ``ct_*``   XPBD.Solver.solve_collision_constraints_x + update_dx, then
              solve_constraints_v (friction + update_dv) (the
              three vertex-triangle contact kinds, with the reference's own
-             gradients) on two cloth layers over a box.
+             gradients) on two cloth layers over a box;
+* ``col_*``  GraphColoring.initEdgeIndicesForColor / initAdjEdges /
+             colorEdgesGreedy / colorCountingSort on the edges of two grid
+             cloths and an icosphere (edge ids in this repository's canonical
+             numbering: the reference's own ids come from meshtaichi_patcher);
+* ``mi_*``   MeshTaichiWrapper.findTriNeighbors / getBendingPair /
+             init_bengding_l0 and initEdgeIndices (rest lengths, inverse
+             masses) on a jittered grid cloth and an icosphere;
+* ``kd_*``   LBVH_CELL.assign_internal_nodes_Karras12 (delta / find_split /
+             determine_range) on sorted face codes with many repeated codes,
+             the reference's equal-code rule.
 
 Usage: python tests/golden/make_reference_vectors.py <reference checkout>
 The npz is committed; the tests read it without the reference.
@@ -311,6 +321,158 @@ def contact_vectors(ti, xpbd_mod, repo_pkg, po):
     return out
 
 
+class _ERef:
+    """One mesh edge in a struct-for: .id, .verts (two vertex refs), .l0."""
+
+    def __init__(self, l0_field, verts, i, a, b):
+        object.__setattr__(self, "_l0", l0_field)
+        object.__setattr__(self, "id", i)
+        object.__setattr__(self, "verts", [_VRef(verts, a), _VRef(verts, b)])
+
+    def __getattr__(self, k):
+        if k == "l0":
+            return self._l0[self.id]
+        raise AttributeError(k)
+
+    def __setattr__(self, k, val):
+        if k != "l0":
+            raise AttributeError(k)
+        self._l0[self.id] = val
+
+
+def coloring_vectors(ti, gc_mod, repo_pkg):
+    """GraphColoring's greedy colouring and counting sort (graph_coloring.py:
+    112-149, 172-201), run as the reference's constructor runs them when no
+    precomputed colouring exists (:55-92), minus the phantom insertion (prints
+    only) and the .npy export."""
+    mesh = repo_pkg.mesh
+    cases = [mesh.grid_cloth(9)[1], mesh.grid_cloth(14)[1], mesh.icosphere(2, 1.0)[1]]
+    out = {}
+    for k, f in enumerate(cases):
+        e = mesh.edges_from_faces(f).astype(np.int32)
+        E = e.shape[0]
+        g = object.__new__(gc_mod.GraphColoring)
+        g.num_edges = E
+        g.num_verts = int(f.max()) + 1
+        g.edges = [types.SimpleNamespace(id=i) for i in range(E)]
+        g.eid_np = e
+        g.eid_field = ti.Field(e.copy())
+        g.edge_indices_sequence = ti.Field(np.zeros(E, np.int32))
+        g.edges_color = ti.Field(np.full(E, -1, np.int32))
+        g.adj_edges_list = ti.Field(np.zeros((E, E), np.int32))
+        g.max_num_colors = 100
+        g.available_colors = ti.Field(np.zeros(g.max_num_colors, np.int32))
+        g.initEdgeIndicesForColor()
+        g.edge_indices_sequence_np = g.edge_indices_sequence.to_numpy()
+        g.initAdjEdges()
+        g.edges_color_np = g.edges_color.to_numpy()
+        g.adj_edges_list_np = g.adj_edges_list.to_numpy()
+        g.available_colors_np = g.available_colors.to_numpy()
+        g.colorEdgesGreedy()
+        g.sorted_edges_sequence_np = g.edge_indices_sequence.to_numpy()
+        g.sorted_edges_color_np = g.edges_color_np.copy()
+        g.color_prefix_sum_np = np.zeros(g.max_num_colors, np.int32)
+        g.colorCountingSort()
+        out["col%d_edges" % k] = e
+        out["col%d_color" % k] = g.edges_color_np.astype(np.int32)
+        out["col%d_sorted" % k] = g.sorted_edges_sequence_np.astype(np.int32)
+        out["col%d_prefix" % k] = g.color_prefix_sum_np.astype(np.int32)
+    return out
+
+
+class _Np126Array(np.ndarray):
+    """numpy 1.26 (the reference's pinned version) let a size-1 array be
+    assigned to a scalar element (getBendingPair's ``pairs[count, 0] =
+    v[~np.isin(v, w)]``); numpy 2.x raises.  This array restores that one rule."""
+
+    def __setitem__(self, key, value):
+        if isinstance(value, np.ndarray) and value.ndim > 0 and value.size == 1 and np.ndim(self[key]) == 0:
+            value = value.reshape(()).item()
+        super().__setitem__(key, value)
+
+
+class _Np126:
+    """The numpy namespace with zeros() returning _Np126Array."""
+
+    def __getattr__(self, name):
+        return getattr(np, name)
+
+    @staticmethod
+    def zeros(*a, **k):
+        return np.zeros(*a, **k).view(_Np126Array)
+
+
+def mesh_init_vectors(ti, mtw_mod, repo_pkg):
+    """findTriNeighbors / getBendingPair (meshTaichiWrapper.py:177-225) and the
+    bending rest lengths of init_bengding_l0 (:142-145); initEdgeIndices
+    (:244-256): rest lengths l0 and m_inv = 1 / sum of half the incident rest
+    lengths, accumulated in edge order."""
+    mesh = repo_pkg.mesh
+    rng = np.random.default_rng(17)
+    xg, fg = mesh.grid_cloth(11)
+    xg = (xg + rng.uniform(-1e-3, 1e-3, xg.shape)).astype(np.float32)
+    xi, fi = mesh.icosphere(2, 0.3, (0.5, 0.5, 0.5))
+    out = {}
+    for k, (x, f) in enumerate([(xg, fg), (xi.astype(np.float32), fi)]):
+        m = object.__new__(mtw_mod.MeshTaichiWrapper)
+        m.fid_np = np.asarray(f, np.int64)
+        saved = mtw_mod.np
+        mtw_mod.np = _Np126()
+        try:
+            count, nb = m.findTriNeighbors()
+            pairs = np.asarray(m.getBendingPair(count, nb))
+        finally:
+            mtw_mod.np = saved
+        V = x.shape[0]
+        verts = _Verts(ti, V, x=x, m_inv=np.zeros(V, np.float32))
+        e = mesh.edges_from_faces(f).astype(np.int32)
+        E = e.shape[0]
+        l0f = ti.Field(np.zeros(E, np.float32))
+        m.mesh = types.SimpleNamespace(edges=[_ERef(l0f, verts, i, int(e[i, 0]), int(e[i, 1])) for i in range(E)],
+                                       verts=verts)
+        m.bending_constraint_count = count
+        m.bending_indices = ti.Field(pairs.reshape(-1).astype(np.int32).copy())
+        m.bending_l0 = ti.Field(np.zeros(count, np.float32))
+        mtw_mod.MeshTaichiWrapper.init_bengding_l0(m)
+        bl0 = m.bending_l0.to_numpy().astype(np.float32)
+        m.edge_indices = ti.Field(np.zeros(2 * E, np.int32))
+        mtw_mod.MeshTaichiWrapper.initEdgeIndices(m)
+        out.update({"mi%d_x" % k: x, "mi%d_faces" % k: np.asarray(f, np.int32),
+                    "mi%d_bend" % k: pairs.astype(np.int32), "mi%d_bend_l0" % k: bl0,
+                    "mi%d_edges" % k: e, "mi%d_l0" % k: l0f.to_numpy().astype(np.float32),
+                    "mi%d_m_inv" % k: verts.m_inv.to_numpy().astype(np.float32),
+                    "mi%d_edge_indices" % k: m.edge_indices.to_numpy().astype(np.int32)})
+    return out
+
+
+def karras_dup_vectors(ti, lbvh_mod, rng):
+    """assign_internal_nodes_Karras12 (lbvh_cell.py:384-405) over sorted 30-bit
+    codes in which most codes repeat (runs of 1-40 equal codes, plus one long
+    run), the case where delta returns 32 for equal neighbours (:256-264)."""
+    out = {}
+    for k, n in enumerate((600, 2500)):
+        runs = []
+        total = 0
+        while total < n:
+            r = int(rng.integers(1, 41)) if rng.random() > 0.02 else 200
+            runs.append(min(r, n - total))
+            total += runs[-1]
+        vals = np.sort(rng.choice(1 << 30, size=len(runs), replace=False)).astype(np.int64)
+        codes = np.repeat(vals, runs).astype(np.int32)
+        L = object.__new__(lbvh_mod.LBVH_CELL)
+        L.num_leafs = n
+        L.leaf_offset = n - 1
+        L.morton_codes = ti.Field(codes.copy())
+        L.nodes = lbvh_mod.Node.field(shape=(2 * n - 1))
+        L.assign_internal_nodes_Karras12()
+        nd = L.nodes
+        out.update({"kd%d_codes" % k: codes, "kd%d_child_a" % k: nd.child_a.a[: n - 1].copy(),
+                    "kd%d_child_b" % k: nd.child_b.a[: n - 1].copy(),
+                    "kd%d_range_l" % k: nd.range_l.a[: n - 1].copy(),
+                    "kd%d_range_r" % k: nd.range_r.a[: n - 1].copy(), "kd%d_parent" % k: nd.parent.a.copy()})
+    return out
+
+
 def main(ref_dir):
     sys.path.insert(0, HERE)
     import taichi_standin
@@ -335,6 +497,17 @@ def main(ref_dir):
 
     out.update(lbvh_vectors(ti, lbvh_mod, pkg, po))
     out.update(contact_vectors(ti, xpbd_mod, pkg, po))
+    import framework.utilities.graph_coloring as gc_mod
+
+    # meshTaichiWrapper imports meshtaichi_patcher and igl at module level; the
+    # functions used here touch neither
+    for name in ("meshtaichi_patcher", "igl"):
+        sys.modules.setdefault(name, types.ModuleType(name))
+    import framework.meshio.meshTaichiWrapper as mtw_mod
+
+    out.update(coloring_vectors(ti, gc_mod, pkg))
+    out.update(mesh_init_vectors(ti, mtw_mod, pkg))
+    out.update(karras_dup_vectors(ti, lbvh_mod, rng))
     path = os.path.join(HERE, "reference_vectors.npz")
     np.savez_compressed(path, **out)
     print("wrote", path, {k: v.shape for k, v in out.items()})

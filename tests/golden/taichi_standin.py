@@ -489,6 +489,14 @@ class _PrefixSumExecutor:
 
 
 algorithms = _pytypes.SimpleNamespace(PrefixSumExecutor=_PrefixSumExecutor)
+
+
+def ndrange(*dims):
+    """ti.ndrange: ascending indices (tuples for more than one dimension)."""
+    import itertools
+
+    rs = [range(d) if np.isscalar(d) else range(d[0], d[1]) for d in dims]
+    return rs[0] if len(rs) == 1 else itertools.product(*rs)
 types = _pytypes.SimpleNamespace(ndarray=template, template=template, vector=lambda *a, **k: None,
                                  matrix=lambda *a, **k: None)
 

@@ -61,3 +61,27 @@ def test_full_size_properties(soup):
     own = (cand == np.arange(N)[:, None]).any(axis=1)
     assert np.all(own[ok])
     assert num.min() >= 1
+
+
+def test_full_size_reference_tie_rule(pkg, po, soup):
+    """The same 2^20 soup under the reference's equal-code rule (tie = 0:
+    delta = 32 for equal codes, lbvh_cell.py:256-264): codes, sort order and
+    the child and range arrays equal the oracle's bit for bit at full size.
+    The soup has repeated codes, so the tree is the reference's malformed one;
+    parents are compared where a node is claimed by exactly one internal node
+    (a node claimed twice gets the last serial writer in the oracle and a
+    racing writer on the GPU)."""
+    t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).cuda()  # noqa: E731
+    bvh = pkg.LBVH(N, "cuda", tie=0)
+    bvh.build(t(soup["mn"]), t(soup["mx"]), t(soup["box"]))
+    torch.cuda.synchronize()
+    ref = po.FaceBVH(soup["mn"], soup["mx"], soup["box"], tie=0)
+    codes = bvh.codes.cpu().numpy()
+    assert np.array_equal(codes, ref.sorted_codes)
+    assert len(np.unique(codes)) < N   # repeated codes: the tie rule matters
+    assert np.array_equal(bvh.sorted_ids.cpu().numpy(), ref.sorted_ids)
+    for name in ("child_a", "child_b", "range_l", "range_r"):
+        assert np.array_equal(getattr(bvh, name).cpu().numpy()[: N - 1], getattr(ref, name)[: N - 1]), name
+    kids = np.concatenate([ref.child_a[: N - 1], ref.child_b[: N - 1]])
+    once = np.bincount(kids, minlength=2 * N - 1) == 1
+    assert np.array_equal(bvh.parent.cpu().numpy()[once], ref.parent[once])

@@ -383,6 +383,37 @@ def test_jacobi_sweep_literal(pkg, po):
     assert np.allclose(yp, yo, atol=1e-6)
 
 
+@pytest.mark.parametrize("bend_on_y", [0, 1])
+def test_gather_sweep_equals_serial_scatter(pkg, po, bend_on_y):
+    """The oracle's per-vertex gather sweep (its multithreaded form for parity
+    runs) equals the serial scatter bit for bit at any thread count."""
+    from starlab_physics_gb300 import mesh as M
+
+    x, f = M.grid_cloth(40)
+    rng = np.random.default_rng(4)
+    x = (x + rng.uniform(-0.003, 0.003, x.shape)).astype(np.float32)
+    V = x.shape[0]
+    e = M.edges_from_faces(f)
+    l0 = M.rest_lengths(x, e)
+    bend = M.bending_pairs(f)
+    bl0 = M.rest_lengths(x, bend)
+    m_inv = M.inverse_masses(V, e, l0)
+    fixed = np.ones(V, np.float32)
+    fixed[[V - 40, V - 1]] = 0
+    x4 = np.zeros((V, 4), np.float32)
+    x4[:, :3] = x
+    y4 = x4.copy()
+    y4[:, :3] += rng.normal(0, 0.004, (V, 3)).astype(np.float32)
+    ks, kb = 1e8 / 3.6e5, 1e5 / 3.6e5
+    ys = y4.copy()
+    po.spring_sweep(x4, ys, fixed, m_inv, e, l0, bend, bl0, ks, kb, bend_on_y=bend_on_y)
+    ptr, adj = po.adjacency(V, e, l0, bend, bl0)
+    for nt in (1, 4):
+        yg = y4.copy()
+        po.spring_sweep_gather(x4, yg, fixed, m_inv, ptr, adj, ks, kb, nthreads=nt, bend_on_y=bend_on_y)
+        assert np.array_equal(yg, ys), nt
+
+
 def test_collision_parallel_matches_serial(pkg, po):
     """Fixed-point contact accumulation makes the parallel oracle equal the serial one."""
     sc = pkg.scenes.drape256(n=24, sphere_subdiv=2)

@@ -1,7 +1,9 @@
 """The CPU oracle against golden vectors produced by the reference's own source
-(tests/golden/make_reference_vectors.py runs distance.py, lbvh_cell.py and
-XPBD.py of the reference through a numpy stand-in for the Taichi API: serial
-loops, IEEE float32 per operation).  No GPU, no reference checkout needed."""
+(tests/golden/make_reference_vectors.py runs distance.py, lbvh_cell.py,
+XPBD.py, graph_coloring.py and meshTaichiWrapper.py of the reference through a
+numpy stand-in for the Taichi API: serial loops, IEEE float32 per operation).
+No reference checkout needed; the tests marked gpu hold the CUDA library to the
+same vectors."""
 import os
 
 import numpy as np
@@ -168,3 +170,77 @@ def test_velocity_pass_matches_reference(po, R):
     dv = np.abs(R["ct_v"] - R["ct_v0"]).max()
     assert np.array_equal(np.abs(v4[:, :3] - R["ct_v0"]).max(1) > 0, changed)
     assert np.abs(v4[:, :3] - R["ct_v"]).max() <= 1e-5 * max(dv, np.abs(R["ct_v"]).max())
+
+
+@pytest.mark.parametrize("k", [0, 1, 2])
+def test_coloring_matches_reference(po, R, k):
+    """GraphColoring.colorEdgesGreedy + colorCountingSort (graph_coloring.py:
+    131-149, 172-201) on two grid cloths and an icosphere: colours, colour-sorted
+    edge sequence and start offsets bit for bit."""
+    e = R["col%d_edges" % k]
+    color, sorted_e, prefix = po.color_edges(int(e.max()) + 1, e)
+    assert np.array_equal(color, R["col%d_color" % k])
+    assert np.array_equal(sorted_e, R["col%d_sorted" % k])
+    assert np.array_equal(prefix, R["col%d_prefix" % k])
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_mesh_init_matches_reference(pkg, R, k):
+    """findTriNeighbors / getBendingPair / init_bengding_l0 and initEdgeIndices
+    (meshTaichiWrapper.py:142-145, 177-225, 244-256): bending pairs in the
+    reference's order, their rest lengths, spring rest lengths and the inverse
+    masses 1 / sum(l0 / 2), bit for bit, through the product's mesh set-up."""
+    x, f = R["mi%d_x" % k], R["mi%d_faces" % k]
+    m = pkg.TriMesh(x, f, device="cpu")
+    assert np.array_equal(m.eid_np.reshape(-1), R["mi%d_edge_indices" % k])
+    assert np.array_equal(m.bending_np.reshape(-1, 2), R["mi%d_bend" % k])
+    assert np.array_equal(m.bending_l0_np, R["mi%d_bend_l0" % k])
+    assert np.array_equal(m.l0_np, R["mi%d_l0" % k])
+    assert np.array_equal(m.m_inv_np, R["mi%d_m_inv" % k])
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_karras_repeated_codes_match_reference(po, R, k):
+    """assign_internal_nodes_Karras12 with delta/find_split/determine_range
+    (lbvh_cell.py:256-336, 384-405) on sorted codes with long runs of equal
+    codes (the reference's equal-code rule, oracle tie = 0): children and ranges
+    bit for bit; parents equal wherever the reference writes one (nodes its
+    malformed tree never claims keep the field's initial 0 there and -1 here)."""
+    codes = R["kd%d_codes" % k]
+    ca, cb, rl, rr, par = po.karras(codes, tie=0)
+    assert np.array_equal(ca, R["kd%d_child_a" % k]) and np.array_equal(cb, R["kd%d_child_b" % k])
+    assert np.array_equal(rl, R["kd%d_range_l" % k]) and np.array_equal(rr, R["kd%d_range_r" % k])
+    written = par >= 0
+    assert np.array_equal(par[written], R["kd%d_parent" % k][written])
+    assert np.all(R["kd%d_parent" % k][~written] == 0)
+    assert (~written).sum() > 1   # duplicates leave nodes unclaimed besides the root
+
+
+@pytest.mark.gpu
+def test_gpu_coloring_and_karras_match_reference(pkg, R):
+    """The CUDA colouring (sx_color_edges_greedy) and Karras build
+    (sx_karras_build, tie = 0) against the same reference vectors."""
+    import torch
+    from starlab_physics_gb300._lib import ptr, stream_handle, sx
+
+    for k in range(3):
+        e = R["col%d_edges" % k]
+        gc = pkg.GraphColoring(int(e.max()) + 1, e, device="cuda")
+        E = e.shape[0]
+        assert np.array_equal(gc.edges_color.cpu().numpy()[:E], R["col%d_color" % k])
+        assert np.array_equal(gc.sorted_edges_sequence_for_color.cpu().numpy()[:E], R["col%d_sorted" % k])
+        assert np.array_equal(gc.color_prefix_sum.cpu().numpy(), R["col%d_prefix" % k])
+    for k in range(2):
+        codes = R["kd%d_codes" % k]
+        n = codes.shape[0]
+        c = torch.from_numpy(codes).cuda()
+        i32 = dict(dtype=torch.int32, device="cuda")
+        ca, cb, rl, rr = (torch.full((n - 1,), -7, **i32) for _ in range(4))
+        par = torch.full((2 * n - 1,), -7, **i32)
+        assert sx.sx_karras_build(ptr(c), n, 0, ptr(ca), ptr(cb), ptr(rl), ptr(rr), ptr(par), stream_handle()) == 0
+        torch.cuda.synchronize()
+        for got, name in ((ca, "child_a"), (cb, "child_b"), (rl, "range_l"), (rr, "range_r")):
+            assert np.array_equal(got.cpu().numpy(), R["kd%d_%s" % (k, name)]), name
+        kids = np.concatenate([R["kd%d_child_a" % k], R["kd%d_child_b" % k]])
+        once = np.bincount(kids, minlength=2 * n - 1) == 1
+        assert np.array_equal(par.cpu().numpy()[once], R["kd%d_parent" % k][once])
