@@ -82,6 +82,19 @@ int sx_jacobi_sweep_variant_info(int variant, int* g, int* block);
 int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
                       const int* adj, int n_verts, float k_spring, float k_bend, int bend_on_y, int variant,
                       void* stream);
+/* sx_jacobi_sweep_v that also tracks how far each vertex moves during a
+ * substep's Jacobi iterations, for the contact-pair split
+ * (sx_contact_pairs_split; no counterpart in the reference).  yref4 (float4
+ * per vertex) NULL: a plain sweep.  motion_flags NULL: the sweep's output is
+ * also written to yref4 (the reference positions; the first iteration of a
+ * substep).  Otherwise bit v of motion_flags (ceil(n_verts / 32) words, every
+ * word written) is set when the output's L1 distance from yref4[v] is at least
+ * motion_budget (or NaN); a clear bit guarantees a Euclidean displacement below
+ * motion_budget.  The positions computed are those of sx_jacobi_sweep_v. */
+int sx_jacobi_sweep_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                            const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
+                            int bend_on_y, int variant, float* yref4, unsigned* motion_flags, float motion_budget,
+                            void* stream);
 
 /* solve_sewing_constraints_x (XPBD.py:425-441) + update_dx over sewn vertex
  * pairs (zero rest length, k = compliance argument of the reference):
@@ -141,6 +154,12 @@ int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, float* y_out4, 
                             const int* adj, int n_verts, float k_spring, float k_bend, int iter, int check, double tol,
                             const double* ref3, int* conv, double* res3, void* ws, size_t ws_bytes,
                             unsigned long long loop, int n_iter, void* stream);
+/* sx_jacobi_sweep_checked with the motion tracking of sx_jacobi_sweep_tracked */
+int sx_jacobi_sweep_checked_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                                    const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
+                                    int iter, int check, double tol, const double* ref3, int* conv, double* res3,
+                                    void* ws, size_t ws_bytes, unsigned long long loop, int n_iter, float* yref4,
+                                    unsigned* motion_flags, float motion_budget, void* stream);
 int sx_loop_begin(void* stream, void* body_stream, unsigned long long* handle_out, void** ctx_out);
 int sx_loop_end(void* ctx);
 
@@ -335,6 +354,38 @@ int sx_contact_pairs_project_v(int n_dy, int n_st, const int* pairs, const void*
                                int variant, void* stream);
 int sx_contact_apply(int n_dy, float* y4, const float* fixed, long long* dx_fix, int* nc, const int* conv, int iter,
                      void* stream);
+
+/* The pair-list projection split by motion (no counterpart in the reference;
+ * same sums as sx_contact_pairs_project, hence the same positions).
+ *
+ * sx_contact_pairs_split runs a substep's first projection (as
+ * sx_contact_pairs_project with cull_d2 > 0) on positions y4 that are the
+ * reference positions of sx_jacobi_sweep_tracked, and writes every pair of
+ * `pairs` to split[max_split] (int4, kind vt_st / vt_dy / tv_st in bits 30-31
+ * of the query index): FAR pairs, whose distance provably exceeds
+ * sqrt(cull_d2) + 2 motion_budget on a triangle that stays classifiable
+ * while its vertices move less than motion_budget (box-distance and
+ * separating-axis bounds, rounding-safe), at the end; all others (NEAR) at the
+ * front.  sx_contact_pairs_project_moved projects a later iteration: every
+ * near pair as sx_contact_pairs_project does, and a far pair only when a
+ * dynamic vertex of it has its bit set in motion_flags (from
+ * sx_jacobi_sweep_tracked with the same motion_budget).  A far pair none of
+ * whose vertices moved that far is farther than sqrt(cull_d2) and adds
+ * nothing.  The pair counts stay in the workspace (sx_contact_pairs_counts).
+ * The order inside the split list varies from run to run; the fixed-point
+ * sums do not depend on it. */
+int sx_contact_pairs_split(int n_dy, int n_st, const int* pairs, void* ws, int* split, long long max_split,
+                           const float* y4, const float* xs4, const float* fixed, const float* m_inv, float dHat,
+                           float compliance, float cull_d2, float motion_budget, long long* dx_fix, int* nc,
+                           int* status, const int* conv, int iter, int variant, void* stream);
+int sx_contact_pairs_project_moved(int n_dy, int n_st, const int* split, const void* ws,
+                                   const unsigned* motion_flags, const float* y4, const float* xs4,
+                                   const float* fixed, const float* m_inv, float dHat, float compliance,
+                                   float cull_d2, long long* dx_fix, int* nc, int* status, const int* conv, int iter,
+                                   int variant, void* stream);
+/* host copy of {vt_st end, vt_dy end, total pairs, near pairs} from the
+ * workspace (synchronises the stream) */
+int sx_contact_pairs_counts(const void* ws, int n_dy, int n_st, int* counts4, void* stream);
 
 /* Edge-edge contacts: __ee_st / __ee_dy (collision_constraints_x.py:313-588;
  * d_type_EE distance.py:50-99, d_EE :119-124; the gradient in closed form)

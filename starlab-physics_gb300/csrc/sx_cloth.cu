@@ -141,6 +141,12 @@ inline int tile_grid(K kernel, int n_verts) {
 // CHECK assume BLOCK == SW_BLOCK.
 // BY: bending pairs evaluated on y, fixed at compile time (the bend_y
 // argument is then ignored), which drops the per-entry x/y selection.
+//
+// Motion tracking for the contact-pair split (optional, yref != nullptr):
+// with mflags == nullptr the sweep also writes its output to yref (the
+// reference positions of a substep's pair-list split); otherwise bit v of
+// mflags is set when |out - yref|_1 >= beta or is NaN (one 32-bit word per
+// warp, written whole).  The positions the sweep computes do not change.
 template <bool CHECK, int G = 2, int BLOCK = SW_BLOCK, bool BY = false>
 __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
                                                                 const float4* __restrict__ yin,
@@ -149,14 +155,17 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
                                                                 const int* __restrict__ ptr,
                                                                 const int2* __restrict__ adj, float ks, float kb,
                                                                 int bend_y, const int* conv, int iter,
-                                                                double* __restrict__ partial) {
+                                                                double* __restrict__ partial, float4* yref,
+                                                                unsigned* __restrict__ mflags, float beta) {
     pdl_entry();
     if (iteration_skipped(conv, iter)) return;  // grid-uniform
     static_assert(!CHECK || BLOCK == SW_BLOCK, "residual partials are per SW_BLOCK tile");
+    static_assert(BLOCK % 32 == 0, "motion flags are written one word per warp");
     const int ntiles = (V + BLOCK - 1) / BLOCK;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int v = tile * BLOCK + threadIdx.x;
     float c2 = 0.0f;  // sum of C^2 over this vertex's entries (CHECK)
+    bool moved = false;
     if (v < V) {
         const float4 ps = __ldg(yin + v), xs = __ldg(x4 + v);
         const int b = __ldg(ptr + v), e = __ldg(ptr + v + 1);
@@ -202,6 +211,20 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
             out.z = ps.z + f * (dz / nc);
         }
         yout[v] = out;
+        if (yref != nullptr) {
+            if (mflags == nullptr) {
+                yref[v] = out;
+            } else {
+                const float4 r = yref[v];
+                const float d = (fabsf(out.x - r.x) + fabsf(out.y - r.y)) + fabsf(out.z - r.z);
+                moved = !(d < beta);
+            }
+        }
+    }
+    if (mflags != nullptr) {  // block-uniform
+        const unsigned m = __ballot_sync(0xffffffffu, moved);
+        const int w0 = tile * BLOCK + (threadIdx.x & ~31);
+        if ((threadIdx.x & 31) == 0 && w0 < V) mflags[w0 >> 5] = m;
     }
     if (CHECK) block_residual_partial(c2, partial, tile);
     }
@@ -442,15 +465,23 @@ extern "C" int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep: y_in4 and y_out4 must not alias");
     launch(bend_on_y ? jacobi_sweep_kernel<false, 2, SW_BLOCK, true> : jacobi_sweep_kernel<false>, sweep_blocks(n_verts),
            SW_BLOCK, 0, as_stream(stream), n_verts, (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed,
-           adj_ptr, (const int2*)adj, k_spring, k_bend, bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr);
+           adj_ptr, (const int2*)adj, k_spring, k_bend, bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr,
+           (float4*)nullptr, (unsigned*)nullptr, 0.0f);
     return check_launch("jacobi_sweep_kernel");
 }
+
+namespace sx {
+// The motion test compares a float L1 displacement (three float differences
+// and two sums, relative error below 4 * 2^-24) with the budget shrunk by
+// 1e-5, so a clear bit means a true displacement below the budget.
+float motion_beta_check(float budget) { return (float)((double)budget * (1.0 - 1e-5)); }
+}  // namespace sx
 
 // Launch configurations of the sweep for the autotuner: (entries per load
 // batch, threads per block).  All give bit-identical results.
 namespace sx {
 using SweepKernel = void (*)(int, const float4*, const float4*, float4*, const float*, const int*, const int2*, float,
-                            float, int, const int*, int, double*);
+                            float, int, const int*, int, double*, float4*, unsigned*, float);
 struct SweepVariant {
     int g, block;
     SweepKernel kern, kern_y;  // bending on x or y chosen at run time / bending on y
@@ -476,16 +507,28 @@ extern "C" int sx_jacobi_sweep_variant_info(int variant, int* g, int* block) {
 extern "C" int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
                                  const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
                                  int bend_on_y, int variant, void* stream) {
+    return sx_jacobi_sweep_tracked(x4, y_in4, y_out4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y,
+                                   variant, nullptr, nullptr, 0.0f, stream);
+}
+
+extern "C" int sx_jacobi_sweep_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                                       const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
+                                       int bend_on_y, int variant, float* yref4, unsigned* motion_flags,
+                                       float motion_budget, void* stream) {
     SX_REQUIRE(n_verts >= 0, "sx_jacobi_sweep_v: n_verts < 0");
     SX_REQUIRE(variant >= 0 && variant < kNumSweepVariants, "sx_jacobi_sweep_v: bad variant");
     if (n_verts == 0) return SX_OK;
     SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj, "sx_jacobi_sweep_v: null pointer");
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_v: y_in4 and y_out4 must not alias");
+    SX_REQUIRE(!motion_flags || (yref4 && motion_budget > 0.0f),
+               "sx_jacobi_sweep_tracked: motion flags need reference positions and a positive budget");
+    SX_REQUIRE(!yref4 || (yref4 != y_in4 && yref4 != y_out4), "sx_jacobi_sweep_tracked: yref4 must not alias y");
     const SweepVariant& sv = kSweepVariants[variant];
     launch(bend_on_y ? sv.kern_y : sv.kern, grid_for(n_verts, sv.block), sv.block, 0, as_stream(stream), n_verts,
            (const float4*)x4,
            (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring, k_bend,
-           bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr);
+           bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr, (float4*)yref4, motion_flags,
+           motion_flags ? motion_beta_check(motion_budget) : 0.0f);
     return check_launch("jacobi_sweep_kernel");
 }
 
@@ -725,7 +768,23 @@ extern "C" int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, floa
                                        float k_bend, int iter, int check, double tol, const double* ref3,
                                        int* conv, double* res3, void* ws, size_t ws_bytes,
                                        unsigned long long loop, int n_iter, void* stream) {
+    return sx_jacobi_sweep_checked_tracked(x4, y_in4, y_out4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, iter,
+                                           check, tol, ref3, conv, res3, ws, ws_bytes, loop, n_iter, nullptr, nullptr,
+                                           0.0f, stream);
+}
+
+extern "C" int sx_jacobi_sweep_checked_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                                               const int* adj_ptr, const int* adj, int n_verts, float k_spring,
+                                               float k_bend, int iter, int check, double tol, const double* ref3,
+                                               int* conv, double* res3, void* ws, size_t ws_bytes,
+                                               unsigned long long loop, int n_iter, float* yref4,
+                                               unsigned* motion_flags, float motion_budget, void* stream) {
     SX_REQUIRE(n_verts > 0, "sx_jacobi_sweep_checked: n_verts must be positive");
+    SX_REQUIRE(!motion_flags || (yref4 && motion_budget > 0.0f),
+               "sx_jacobi_sweep_checked_tracked: motion flags need reference positions and a positive budget");
+    SX_REQUIRE(!yref4 || (yref4 != y_in4 && yref4 != y_out4),
+               "sx_jacobi_sweep_checked_tracked: yref4 must not alias y");
+    const float beta = motion_flags ? motion_beta_check(motion_budget) : 0.0f;
     SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj && conv, "sx_jacobi_sweep_checked: null pointer");
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_checked: y_in4 and y_out4 must not alias");
     SX_REQUIRE(iter >= 0, "sx_jacobi_sweep_checked: iter < 0");
@@ -740,7 +799,7 @@ extern "C" int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, floa
             constexpr auto kc = jacobi_sweep_kernel<true, 2, SW_BLOCK, true>;
         launch(kc, gate ? tile_grid(kc, n_verts) : sweep_blocks(n_verts), SW_BLOCK, 0, s, n_verts,
                (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
-               k_bend, 1, gate, iter, (double*)ws);
+               k_bend, 1, gate, iter, (double*)ws, (float4*)yref4, motion_flags, beta);
         int rc = check_launch("jacobi_sweep_kernel");
         if (rc) return rc;
         return residual_finish(n_verts, adj_ptr, ws, res3, conv, iter, tol, ref3, loop, n_iter, s);
@@ -748,7 +807,7 @@ extern "C" int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, floa
     constexpr auto kp = jacobi_sweep_kernel<false, 2, SW_BLOCK, true>;
     launch(kp, gate ? tile_grid(kp, n_verts) : sweep_blocks(n_verts), SW_BLOCK, 0, s, n_verts,
            (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
-           k_bend, 1, gate, iter, (double*)nullptr);
+           k_bend, 1, gate, iter, (double*)nullptr, (float4*)yref4, motion_flags, beta);
     return check_launch("jacobi_sweep_kernel");
 }
 
