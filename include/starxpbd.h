@@ -366,23 +366,28 @@ int sx_contact_apply(int n_dy, float* y4, const float* fixed, long long* dx_fix,
  * sqrt(cull_d2) + 2 motion_budget on a triangle that stays classifiable
  * while its vertices move less than motion_budget (box-distance and
  * separating-axis bounds, rounding-safe), at the end; all others (NEAR) at the
- * front.  sx_contact_pairs_project_moved projects a later iteration: every
- * near pair as sx_contact_pairs_project does, and a far pair only when a
- * dynamic vertex of it has its bit set in motion_flags (from
- * sx_jacobi_sweep_tracked with the same motion_budget).  A far pair none of
- * whose vertices moved that far is farther than sqrt(cull_d2) and adds
- * nothing.  The pair counts stay in the workspace (sx_contact_pairs_counts).
- * The order inside the split list varies from run to run; the fixed-point
- * sums do not depend on it. */
+ * front.  It then sorts the far pairs by vertex into split_ws
+ * (sx_contact_split_workspace_bytes(n_dy, max_split) bytes, zero-filled
+ * before its first use).  sx_contact_pairs_project_moved projects a later
+ * iteration: every near pair as sx_contact_pairs_project does, and the far
+ * pairs of the vertices flagged in motion_flags (sx_jacobi_sweep_tracked
+ * with the same motion_budget), each pair once.  A far pair none of whose
+ * vertices moved that far is farther than sqrt(cull_d2) and adds nothing.
+ * Call sx_contact_pairs_split once after each sx_contact_pairs_build.  The
+ * pair counts stay in the workspace (sx_contact_pairs_counts).  The order
+ * inside the split list varies from run to run; the fixed-point sums do not
+ * depend on it. */
+size_t sx_contact_split_workspace_bytes(int n_dy, long long max_split);
 int sx_contact_pairs_split(int n_dy, int n_st, const int* pairs, void* ws, int* split, long long max_split,
-                           const float* y4, const float* xs4, const float* fixed, const float* m_inv, float dHat,
-                           float compliance, float cull_d2, float motion_budget, long long* dx_fix, int* nc,
-                           int* status, const int* conv, int iter, int variant, void* stream);
-int sx_contact_pairs_project_moved(int n_dy, int n_st, const int* split, const void* ws,
-                                   const unsigned* motion_flags, const float* y4, const float* xs4,
-                                   const float* fixed, const float* m_inv, float dHat, float compliance,
-                                   float cull_d2, long long* dx_fix, int* nc, int* status, const int* conv, int iter,
-                                   int variant, void* stream);
+                           void* split_ws, size_t split_ws_bytes, const float* y4, const float* xs4,
+                           const float* fixed, const float* m_inv, float dHat, float compliance, float cull_d2,
+                           float motion_budget, long long* dx_fix, int* nc, int* status, const int* conv, int iter,
+                           int variant, void* stream);
+int sx_contact_pairs_project_moved(int n_dy, int n_st, const int* split, const void* ws, const void* split_ws,
+                                   long long max_split, const unsigned* motion_flags, const float* y4,
+                                   const float* xs4, const float* fixed, const float* m_inv, float dHat,
+                                   float compliance, float cull_d2, long long* dx_fix, int* nc, int* status,
+                                   const int* conv, int iter, int variant, void* stream);
 /* host copy of {vt_st end, vt_dy end, total pairs, near pairs} from the
  * workspace (synchronises the stream) */
 int sx_contact_pairs_counts(const void* ws, int n_dy, int n_st, int* counts4, void* stream);

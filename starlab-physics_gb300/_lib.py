@@ -79,8 +79,10 @@ SIGNATURES = {
     "sx_contact_pairs_project_variant_info": ([I, P, P], I),
     "sx_contact_pairs_project_v": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, I, P], I),
     "sx_contact_apply": ([I, P, P, P, P, P, I, P], I),
-    "sx_contact_pairs_split": ([I, I, P, P, P, C.c_longlong, P, P, P, P, F, F, F, F, P, P, P, P, I, I, P], I),
-    "sx_contact_pairs_project_moved": ([I, I, P, P, P, P, P, P, P, F, F, F, P, P, P, P, I, I, P], I),
+    "sx_contact_split_workspace_bytes": ([I, C.c_longlong], Z),
+    "sx_contact_pairs_split": ([I, I, P, P, P, C.c_longlong, P, Z, P, P, P, P, F, F, F, F, P, P, P, P, I, I, P], I),
+    "sx_contact_pairs_project_moved": ([I, I, P, P, P, C.c_longlong, P, P, P, P, P, F, F, F, P, P, P, P, I, I, P],
+                                       I),
     "sx_contact_pairs_counts": ([P, I, I, P, P], I),
     "sx_edge_edge_sweep": ([I, P, P, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, I, P], I),
     "sx_edge_edge_classify": ([I, P, F, P, P, P, P], I),

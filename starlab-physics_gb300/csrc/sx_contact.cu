@@ -1018,20 +1018,112 @@ __global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_split_kernel(int* meta, 
     if (bad & 2) atomicOr(status, SX_STATUS_CAND_OVERFLOW);
 }
 
+// Vertex -> far-pair incidence, built once per substep after the split
+// (counting sort by vertex): a later iteration visits only the far pairs of
+// the vertices flagged as moved instead of testing every far pair's flags.
+// Arrays (split workspace): cnt[V] (zero between substeps), cur[V], count[V],
+// start[V] (block-local exclusive prefix), btot[nb] (block offsets), then the
+// incidence list inc[] of far-pair indices into split.
+struct IncWs {
+    int *cnt, *cur, *count, *start, *btot, *inc;
+    long long inc_cap;
+    size_t bytes;
+};
+constexpr int INC_BLOCK = 256;
+
+__device__ __forceinline__ int rec_dyn(int4 r, int k, int* v) {  // dynamic vertex k (0..3) of record r, or -1
+    const int kind = rec_kind(r);
+    const int id = k == 0 ? (kind == 2 ? -1 : rec_query(r)) : (kind == 0 ? -1 : (k == 1 ? r.y : k == 2 ? r.z : r.w));
+    *v = id;
+    return id;
+}
+
+__global__ void inc_count_kernel(const int* __restrict__ meta, const int4* __restrict__ split, int max_split,
+                                 int* cnt) {
+    pdl_entry();
+    const int P = min(meta[2], max_split), NN = meta[M_NEAR];
+    for (int t = NN + blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
+        const int4 r = split[t];
+        for (int k = 0; k < 4; ++k) {
+            int v;
+            if (rec_dyn(r, k, &v) >= 0) atomicAdd(cnt + v, 1);
+        }
+    }
+}
+
+// count -> block-local exclusive prefix; clears cnt for the next substep and
+// the fill cursors
+__global__ void __launch_bounds__(INC_BLOCK) inc_block_scan_kernel(int V, int* cnt, int* cur, int* count, int* start,
+                                                                   int* btot) {
+    pdl_entry();
+    __shared__ int warp_tot[INC_BLOCK / 32];
+    const int v = blockIdx.x * INC_BLOCK + threadIdx.x;
+    const int c = v < V ? cnt[v] : 0;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int incl = c;
+    for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+    }
+    if (lane == 31) warp_tot[w] = incl;
+    __syncthreads();
+    int base = 0, tot = 0;
+    for (int k = 0; k < INC_BLOCK / 32; ++k) {
+        if (k < w) base += warp_tot[k];
+        tot += warp_tot[k];
+    }
+    if (v < V) {
+        count[v] = c;
+        start[v] = base + incl - c;
+        cnt[v] = 0;
+        cur[v] = 0;
+    }
+    if (threadIdx.x == 0) btot[blockIdx.x] = tot;
+}
+
+__global__ void inc_fill_kernel(const int* __restrict__ meta, const int4* __restrict__ split, int max_split,
+                                int* cur, const int* __restrict__ start, const int* __restrict__ btot, int* inc,
+                                long long inc_cap, int* status) {
+    pdl_entry();
+    const int P = min(meta[2], max_split), NN = meta[M_NEAR];
+    for (int t = NN + blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
+        const int4 r = split[t];
+        for (int k = 0; k < 4; ++k) {
+            int v;
+            if (rec_dyn(r, k, &v) < 0) continue;
+            const long long slot = (long long)start[v] + btot[v / INC_BLOCK] + atomicAdd(cur + v, 1);
+            if (slot < inc_cap) inc[slot] = t;
+            else atomicOr(status, SX_STATUS_CAND_OVERFLOW);
+        }
+    }
+}
+
+// the record's smallest flagged dynamic vertex (INT_MAX if none)
+__device__ __forceinline__ int lowest_flagged(const unsigned* __restrict__ f, int4 r) {
+    int lo = 0x7fffffff;
+    for (int k = 0; k < 4; ++k) {
+        int v;
+        if (rec_dyn(r, k, &v) >= 0 && flag_bit(f, v) && v < lo) lo = v;
+    }
+    return lo;
+}
+
 // A later projection of the substep over the split list: near pairs through
-// the regular two-stage cull, far pairs only when flagged as moved (then the
-// same cull).  Stacks per warp: s0 flagged far pairs awaiting the box test,
-// s1 box survivors awaiting the separating-axis test, s2 pairs to project.
+// the regular two-stage cull; far pairs only when a dynamic vertex of theirs
+// is flagged as moved, found through the flagged vertices' incidence lists
+// (a pair met from several flagged vertices is taken from the smallest), then
+// the same cull.  Stacks per warp: s0 flagged far pairs awaiting the box
+// test, s1 box survivors awaiting the separating-axis test, s2 pairs to
+// project.
 template <int U, int MINB>
-__global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_moved_kernel(const int* __restrict__ meta,
-                                                                             const int4* __restrict__ split,
-                                                                             const unsigned* __restrict__ mflags,
-                                                                             RecCtx rc, float cull_d2, int* status,
-                                                                             const int* conv, int iter) {
+__global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_moved_kernel(
+    const int* __restrict__ meta, const int4* __restrict__ split, const unsigned* __restrict__ mflags, int n_words,
+    const int* __restrict__ count, const int* __restrict__ start, const int* __restrict__ btot,
+    const int* __restrict__ inc, RecCtx rc, float cull_d2, int* status, const int* conv, int iter) {
     pdl_entry();
     if (iteration_skipped(conv, iter)) return;
-    const int P = meta[2], NN = meta[M_NEAR];
-    __shared__ int far_stack[PP_BLOCK / 32][32 * U + 32];
+    const int NN = min(meta[M_NEAR], meta[2]);
+    __shared__ int far_stack[PP_BLOCK / 32][64];
     __shared__ int box_stack[PP_BLOCK / 32][32 * U + 32];
     __shared__ int sat_stack[PP_BLOCK / 32][64];
     const int lane = threadIdx.x & 31;
@@ -1100,23 +1192,22 @@ __global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_moved_kernel(con
         __syncwarp();
         while (n1 >= 32) sat_stage(32);
     }
-    for (int base = NN + gw * 32 * U; base < P; base += nw * 32 * U) {
-        int4 r[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int t = base + 32 * u + lane;
-            r[u] = t < P ? split[t] : make_int4(0, 0, 0, 0);
+    for (int w = gw; w < n_words; w += nw) {
+        unsigned word = __ldg(mflags + w);  // warp-uniform
+        while (word) {
+            const int v = 32 * w + __ffs(word) - 1;
+            word &= word - 1u;
+            const int s = start[v] + btot[v / INC_BLOCK], n = count[v];
+            for (int b = 0; b < n; b += 32) {
+                const int t = b + lane < n ? inc[s + b + lane] : -1;
+                const bool take = t >= 0 && lowest_flagged(mflags, split[t]) == v;
+                const unsigned m = __ballot_sync(0xffffffffu, take);
+                if (take) s0[n0 + __popc(m & below)] = t;
+                n0 += __popc(m);
+                __syncwarp();
+                if (n0 >= 32) box_stage(32);
+            }
         }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int t = base + 32 * u + lane;
-            const bool moved = t < P && rec_moved(mflags, r[u]);
-            const unsigned m = __ballot_sync(0xffffffffu, moved);
-            if (moved) s0[n0 + __popc(m & below)] = t;
-            n0 += __popc(m);
-        }
-        __syncwarp();
-        while (n0 >= 32) box_stage(32);
     }
     if (n0 > 0) box_stage(n0);
     while (n1 >= 32) sat_stage(32);
@@ -1786,47 +1877,85 @@ static float far_radius_d2(float cull_d2, float beta) {
     return std::nextafter((float)(r * r), INFINITY);
 }
 
+static IncWs inc_ws(void* ws, int n_dy, long long max_split) {
+    IncWs w;
+    char* p = (char*)ws;
+    char* p0 = p;
+    const size_t vb = a256((size_t)(n_dy > 0 ? n_dy : 1) * 4);
+    w.cnt = (int*)p; p += vb;
+    w.cur = (int*)p; p += vb;
+    w.count = (int*)p; p += vb;
+    w.start = (int*)p; p += vb;
+    w.btot = (int*)p; p += a256((size_t)((n_dy + INC_BLOCK - 1) / INC_BLOCK + 1) * 4);
+    w.inc = (int*)p;
+    w.inc_cap = 4 * (max_split > 0 ? max_split : 1);
+    p += a256((size_t)w.inc_cap * 4);
+    w.bytes = (size_t)(p - p0);
+    return w;
+}
+
+extern "C" size_t sx_contact_split_workspace_bytes(int n_dy, long long max_split) {
+    return inc_ws(nullptr, n_dy, max_split).bytes;
+}
+
 extern "C" int sx_contact_pairs_split(int n_dy, int n_st, const int* pairs, void* ws, int* split,
-                                      long long max_split, const float* y4, const float* xs4, const float* fixed,
-                                      const float* m_inv, float dHat, float compliance, float cull_d2,
-                                      float motion_budget, long long* dx_fix, int* nc, int* status, const int* conv,
-                                      int iter, int variant, void* stream) {
+                                      long long max_split, void* split_ws, size_t split_ws_bytes, const float* y4,
+                                      const float* xs4, const float* fixed, const float* m_inv, float dHat,
+                                      float compliance, float cull_d2, float motion_budget, long long* dx_fix,
+                                      int* nc, int* status, const int* conv, int iter, int variant, void* stream) {
     SX_REQUIRE(variant >= 0 && variant < kNumPairsProjectVariants, "sx_contact_pairs_split: bad variant");
     SX_REQUIRE(n_dy >= 0 && n_st >= 0 && max_split >= 0, "sx_contact_pairs_split: bad sizes");
     SX_REQUIRE(cull_d2 > 0.0f && motion_budget > 0.0f, "sx_contact_pairs_split: needs cull_d2 > 0 and a positive "
                                                        "motion budget");
     if (n_dy == 0) return SX_OK;
-    SX_REQUIRE(pairs && ws && split && y4 && fixed && m_inv && dx_fix && nc && status,
+    SX_REQUIRE(pairs && ws && split && split_ws && y4 && fixed && m_inv && dx_fix && nc && status,
                "sx_contact_pairs_split: null pointer");
+    SX_REQUIRE(split_ws_bytes >= sx_contact_split_workspace_bytes(n_dy, max_split),
+               "sx_contact_pairs_split: split workspace too small");
     SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_split: null static positions");
     SX_REQUIRE((const void*)pairs != (const void*)split, "sx_contact_pairs_split: split must not alias pairs");
+    cudaStream_t st = as_stream(stream);
     PairsWs w = pairs_ws(ws, n_dy, n_st);
+    IncWs iw = inc_ws(split_ws, n_dy, max_split);
     const PairsProjectVariant& pv = kPairsProjectVariants[variant];
     const RecCtx rc{(const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, dx_fix, nc};
     const int ms = max_split > 0x7fffffffLL ? 0x7fffffff : (int)max_split;
-    launch(kPairsSplitVariants[variant].split, sm_count() * pv.blocks_per_sm, PP_BLOCK, 0, as_stream(stream), w.meta,
+    launch(kPairsSplitVariants[variant].split, sm_count() * pv.blocks_per_sm, PP_BLOCK, 0, st, w.meta,
            (const int4*)pairs, (int4*)split, ms, rc, cull_d2, far_radius_d2(cull_d2, motion_budget), motion_budget,
            status, conv, iter);
-    return check_launch("pairs_split_kernel");
+    int rc_ = check_launch("pairs_split_kernel");
+    if (rc_) return rc_;
+    // vertex -> far-pair incidence for the later iterations
+    const int nb = (n_dy + INC_BLOCK - 1) / INC_BLOCK;
+    const int gf = sm_count() * 8;
+    launch(inc_count_kernel, gf, 256, 0, st, (const int*)w.meta, (const int4*)split, ms, iw.cnt);
+    launch(inc_block_scan_kernel, nb, INC_BLOCK, 0, st, n_dy, iw.cnt, iw.cur, iw.count, iw.start, iw.btot);
+    launch(pairs_scan_kernel, 1, 1024, 0, st, nb, iw.btot);
+    launch(inc_fill_kernel, gf, 256, 0, st, (const int*)w.meta, (const int4*)split, ms, iw.cur, (const int*)iw.start,
+           (const int*)iw.btot, iw.inc, iw.inc_cap, status);
+    return check_launch("sx_contact_pairs_split incidence");
 }
 
 extern "C" int sx_contact_pairs_project_moved(int n_dy, int n_st, const int* split, const void* ws,
+                                              const void* split_ws, long long max_split,
                                               const unsigned* motion_flags, const float* y4, const float* xs4,
                                               const float* fixed, const float* m_inv, float dHat, float compliance,
                                               float cull_d2, long long* dx_fix, int* nc, int* status,
                                               const int* conv, int iter, int variant, void* stream) {
     SX_REQUIRE(variant >= 0 && variant < kNumPairsProjectVariants, "sx_contact_pairs_project_moved: bad variant");
-    SX_REQUIRE(n_dy >= 0 && n_st >= 0, "sx_contact_pairs_project_moved: bad sizes");
+    SX_REQUIRE(n_dy >= 0 && n_st >= 0 && max_split >= 0, "sx_contact_pairs_project_moved: bad sizes");
     SX_REQUIRE(cull_d2 > 0.0f, "sx_contact_pairs_project_moved: needs cull_d2 > 0");
     if (n_dy == 0) return SX_OK;
-    SX_REQUIRE(split && ws && motion_flags && y4 && fixed && m_inv && dx_fix && nc && status,
+    SX_REQUIRE(split && ws && split_ws && motion_flags && y4 && fixed && m_inv && dx_fix && nc && status,
                "sx_contact_pairs_project_moved: null pointer");
     SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_project_moved: null static positions");
     PairsWs w = pairs_ws(const_cast<void*>(ws), n_dy, n_st);
+    IncWs iw = inc_ws(const_cast<void*>(split_ws), n_dy, max_split);
     const PairsProjectVariant& pv = kPairsProjectVariants[variant];
     const RecCtx rc{(const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, dx_fix, nc};
     launch(kPairsSplitVariants[variant].moved, sm_count() * pv.blocks_per_sm, PP_BLOCK, 0, as_stream(stream),
-           (const int*)w.meta, (const int4*)split, motion_flags, rc, cull_d2, status, conv, iter);
+           (const int*)w.meta, (const int4*)split, motion_flags, (n_dy + 31) / 32, (const int*)iw.count,
+           (const int*)iw.start, (const int*)iw.btot, (const int*)iw.inc, rc, cull_d2, status, conv, iter);
     return check_launch("pairs_project_moved_kernel");
 }
 

@@ -232,6 +232,8 @@ class Solver:
         if self._split is None:
             Vd = self.mesh_dy.num_verts
             self._split = torch.empty_like(self._pairs)
+            self._split_ws = torch.zeros(int(sx.sx_contact_split_workspace_bytes(Vd, self._split.shape[0])),
+                                         dtype=torch.uint8, device=self.device)
             self._yref4 = torch.zeros_like(self.mesh_dy.y4)
             self._mflags = torch.zeros((Vd + 31) // 32, dtype=torch.int32, device=self.device)
 
@@ -349,14 +351,16 @@ class Solver:
                 variant = 0 if self.pairs_variant is None else int(self.pairs_variant)
                 if iteration == 0:
                     sx.sx_contact_pairs_split(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
-                                              ptr(self._pairs_ws), ptr(self._split), self._split.shape[0], ptr(m.y4),
+                                              ptr(self._pairs_ws), ptr(self._split), self._split.shape[0],
+                                              ptr(self._split_ws), self._split_ws.numel(), ptr(m.y4),
                                               xs, ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c),
                                               self.contact_cull_d2(), self.motion_budget(), ptr(self._dx_fix),
                                               ptr(self._nc), ptr(self.status), conv, iteration, variant,
                                               stream_handle())
                 else:
                     sx.sx_contact_pairs_project_moved(m.num_verts, s.num_verts if s is not None else 0,
-                                                      ptr(self._split), ptr(self._pairs_ws), ptr(self._mflags),
+                                                      ptr(self._split), ptr(self._pairs_ws), ptr(self._split_ws),
+                                                      self._split.shape[0], ptr(self._mflags),
                                                       ptr(m.y4), xs, ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c),
                                                       self.contact_cull_d2(), ptr(self._dx_fix), ptr(self._nc),
                                                       ptr(self.status), conv, iteration, variant, stream_handle())
