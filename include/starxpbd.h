@@ -84,17 +84,24 @@ int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_out4, const 
                       void* stream);
 /* sx_jacobi_sweep_v that also tracks how far each vertex moves during a
  * substep's Jacobi iterations, for the contact-pair split
- * (sx_contact_pairs_split; no counterpart in the reference).  yref4 (float4
- * per vertex) NULL: a plain sweep.  motion_flags NULL: the sweep's output is
- * also written to yref4 (the reference positions; the first iteration of a
- * substep).  Otherwise bit v of motion_flags (ceil(n_verts / 32) words, every
- * word written) is set when the output's L1 distance from yref4[v] is at least
- * motion_budget (or NaN); a clear bit guarantees a Euclidean displacement below
- * motion_budget.  The positions computed are those of sx_jacobi_sweep_v. */
+ * (sx_contact_pairs_split; no counterpart in the reference), and optionally
+ * uses the fast arithmetic (fast != 0: fused multiply-adds, the hardware
+ * reciprocal square root, a fast divide and n.n taken as 1 -- within float
+ * rounding of the exact sweep, not bit-identical; fast = 0 is the exact,
+ * reference-order arithmetic).  yref4 (float4 per vertex) NULL: no tracking.
+ * motion NULL: the sweep's output is also written to yref4 (the reference
+ * positions; the first iteration of a substep).  Otherwise, in the motion
+ * buffer (sx_motion_buffer_bytes(n_verts)), bit v of the flag words is set
+ * when the output's L1 distance from yref4[v] is at least motion_budget (or
+ * NaN), and v is appended to the list of vertices flagged in this iteration;
+ * a clear bit guarantees a Euclidean displacement below motion_budget.
+ * iteration: the Jacobi iteration within the substep (its parity selects the
+ * list counter).  The positions computed are those of sx_jacobi_sweep_v. */
+size_t sx_motion_buffer_bytes(int n_verts);
 int sx_jacobi_sweep_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
                             const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
-                            int bend_on_y, int variant, float* yref4, unsigned* motion_flags, float motion_budget,
-                            void* stream);
+                            int bend_on_y, int variant, int fast, float* yref4, unsigned* motion,
+                            float motion_budget, int iteration, void* stream);
 
 /* solve_sewing_constraints_x (XPBD.py:425-441) + update_dx over sewn vertex
  * pairs (zero rest length, k = compliance argument of the reference):
@@ -154,12 +161,13 @@ int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, float* y_out4, 
                             const int* adj, int n_verts, float k_spring, float k_bend, int iter, int check, double tol,
                             const double* ref3, int* conv, double* res3, void* ws, size_t ws_bytes,
                             unsigned long long loop, int n_iter, void* stream);
-/* sx_jacobi_sweep_checked with the motion tracking of sx_jacobi_sweep_tracked */
+/* sx_jacobi_sweep_checked with the arithmetic choice and motion tracking of
+ * sx_jacobi_sweep_tracked */
 int sx_jacobi_sweep_checked_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
                                     const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
                                     int iter, int check, double tol, const double* ref3, int* conv, double* res3,
-                                    void* ws, size_t ws_bytes, unsigned long long loop, int n_iter, float* yref4,
-                                    unsigned* motion_flags, float motion_budget, void* stream);
+                                    void* ws, size_t ws_bytes, unsigned long long loop, int n_iter, int fast,
+                                    float* yref4, unsigned* motion, float motion_budget, void* stream);
 int sx_loop_begin(void* stream, void* body_stream, unsigned long long* handle_out, void** ctx_out);
 int sx_loop_end(void* ctx);
 
@@ -368,10 +376,12 @@ int sx_contact_apply(int n_dy, float* y4, const float* fixed, long long* dx_fix,
  * separating-axis bounds, rounding-safe), at the end; all others (NEAR) at the
  * front.  It then sorts the far pairs by vertex into split_ws
  * (sx_contact_split_workspace_bytes(n_dy, max_split) bytes, zero-filled
- * before its first use).  sx_contact_pairs_project_moved projects a later
- * iteration: every near pair as sx_contact_pairs_project does, and the far
- * pairs of the vertices flagged in motion_flags (sx_jacobi_sweep_tracked
- * with the same motion_budget), each pair once.  A far pair none of whose
+ * before its first use) and clears the flagged-vertex lists of the motion
+ * buffer (sx_motion_buffer_bytes).  sx_contact_pairs_project_moved projects
+ * a later iteration `iter`: every near pair as sx_contact_pairs_project does,
+ * and the far pairs of the vertices that sx_jacobi_sweep_tracked (same
+ * motion_budget, same iteration) flagged and listed in `motion`, each pair
+ * once.  A far pair none of whose
  * vertices moved that far is farther than sqrt(cull_d2) and adds nothing.
  * Call sx_contact_pairs_split once after each sx_contact_pairs_build.  The
  * pair counts stay in the workspace (sx_contact_pairs_counts).  The order
@@ -379,12 +389,12 @@ int sx_contact_apply(int n_dy, float* y4, const float* fixed, long long* dx_fix,
  * depend on it. */
 size_t sx_contact_split_workspace_bytes(int n_dy, long long max_split);
 int sx_contact_pairs_split(int n_dy, int n_st, const int* pairs, void* ws, int* split, long long max_split,
-                           void* split_ws, size_t split_ws_bytes, const float* y4, const float* xs4,
+                           void* split_ws, size_t split_ws_bytes, unsigned* motion, const float* y4, const float* xs4,
                            const float* fixed, const float* m_inv, float dHat, float compliance, float cull_d2,
                            float motion_budget, long long* dx_fix, int* nc, int* status, const int* conv, int iter,
                            int variant, void* stream);
 int sx_contact_pairs_project_moved(int n_dy, int n_st, const int* split, const void* ws, const void* split_ws,
-                                   long long max_split, const unsigned* motion_flags, const float* y4,
+                                   long long max_split, const unsigned* motion, const float* y4,
                                    const float* xs4, const float* fixed, const float* m_inv, float dHat,
                                    float compliance, float cull_d2, long long* dx_fix, int* nc, int* status,
                                    const int* conv, int iter, int variant, void* stream);

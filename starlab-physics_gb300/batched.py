@@ -168,6 +168,8 @@ class BatchedSolver:
         self.warm = None
         # launch configuration of the fixed-count sweep (autotune() picks one)
         self.sweep_variant = 0
+        # the sweep's fast arithmetic (Solver.fast_math)
+        self.fast_math = False
         # iterate to a residual (Solver.tol): n_iter is then the cap
         self.tol = None
         self.tol_relative = False
@@ -250,15 +252,18 @@ class BatchedSolver:
         in the first iteration, obstacle contacts.  Inside a device-side loop
         (in_loop) the contact kernels are not gated; ``loop`` is the loop
         handle, given with the body's checked sweep."""
+        fast = 1 if self.fast_math else 0
         if conv is not None:
-            sx.sx_jacobi_sweep_checked(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
-                                       ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend, it,
-                                       1 if check else 0, float(self.tol), ref, conv, ptr(self._res3),
-                                       ptr(self._res_ws), self._res_ws.numel(), loop, self.n_iter, s)
+            sx.sx_jacobi_sweep_checked_tracked(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
+                                               ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend, it,
+                                               1 if check else 0, float(self.tol), ref, conv, ptr(self._res3),
+                                               ptr(self._res_ws), self._res_ws.numel(), loop, self.n_iter, fast, None,
+                                               None, 0.0, s)
         else:
-            sx.sx_jacobi_sweep_v(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed), ptr(self.adj_ptr),
-                                 ptr(self.adj), self.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0,
-                                 self.sweep_variant, s)
+            sx.sx_jacobi_sweep_tracked(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
+                                       ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend,
+                                       1 if self.bending_on == "y" else 0, self.sweep_variant, fast, None, None, 0.0, it,
+                                       s)
         self._swap_y()
         if it == 0:
             sx.sx_batched_obstacle_broadphase(
@@ -287,7 +292,8 @@ class BatchedSolver:
             self._forward_eager(n_substeps)
             return
         key = (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
-               self.stiffness_bending, self.n_iter, self.bending_on, self.sweep_variant, self.tol, self.tol_relative,
+               self.stiffness_bending, self.n_iter, self.bending_on, self.sweep_variant, self.fast_math, self.tol,
+               self.tol_relative,
                self.check_every,
                id(self.warm) if self.warm is not None else None,
                self.warm.mode if self.warm is not None else None, self.y4.data_ptr())

@@ -141,13 +141,20 @@ inline int tile_grid(K kernel, int n_verts) {
 // CHECK assume BLOCK == SW_BLOCK.
 // BY: bending pairs evaluated on y, fixed at compile time (the bend_y
 // argument is then ignored), which drops the per-entry x/y selection.
+// FAST: the same constraint projection with fused multiply-adds, the
+// hardware reciprocal square root for the length and normal, a fast divide
+// for the multiplier, and n.n taken as 1 (n is a unit vector up to rounding):
+// fewer instructions per entry, results within float rounding of the exact
+// form but not bit-identical to it; validated against the oracle at the
+// position and residual tolerance of the substep instead.
 //
 // Motion tracking for the contact-pair split (optional, yref != nullptr):
-// with mflags == nullptr the sweep also writes its output to yref (the
-// reference positions of a substep's pair-list split); otherwise bit v of
-// mflags is set when |out - yref|_1 >= beta or is NaN (one 32-bit word per
-// warp, written whole).  The positions the sweep computes do not change.
-template <bool CHECK, int G = 2, int BLOCK = SW_BLOCK, bool BY = false>
+// with motion == nullptr the sweep also writes its output to yref (the
+// reference positions of a substep's pair-list split); otherwise bit v of the
+// motion buffer's flags is set when |out - yref|_1 >= beta or is NaN (one
+// 32-bit word per warp, written whole) and v is appended to its list
+// (count[iter & 1]).  The positions the sweep computes do not change.
+template <bool CHECK, int G = 2, int BLOCK = SW_BLOCK, bool BY = false, bool FAST = false>
 __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
                                                                 const float4* __restrict__ yin,
                                                                 float4* __restrict__ yout,
@@ -156,7 +163,7 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
                                                                 const int2* __restrict__ adj, float ks, float kb,
                                                                 int bend_y, const int* conv, int iter,
                                                                 double* __restrict__ partial, float4* yref,
-                                                                unsigned* __restrict__ mflags, float beta) {
+                                                                unsigned* __restrict__ motion, float beta) {
     pdl_entry();
     if (iteration_skipped(conv, iter)) return;  // grid-uniform
     static_assert(!CHECK || BLOCK == SW_BLOCK, "residual partials are per SW_BLOCK tile");
@@ -189,6 +196,17 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
                 const float4 self = use_x ? xs : ps;
                 const float kk = bend ? kb : ks;
                 const float ex = self.x - o[g].x, ey = self.y - o[g].y, ez = self.z - o[g].z;
+                if (FAST) {
+                    const float d2 = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, ez * ez));
+                    const float inv = rsqrtf(d2);
+                    const float C = d2 * inv - rest;
+                    if (CHECK) c2 = __fmaf_rn(C, C, c2);
+                    const float ld = __fdividef(kk * C, __fmaf_rn(kk, self.w + o[g].w, 1.0f));
+                    const float a0 = (self.w * ld) * inv;  // times the unnormalised difference
+                    dx = __fmaf_rn(-a0, ex, dx);
+                    dy = __fmaf_rn(-a0, ey, dy);
+                    dz = __fmaf_rn(-a0, ez, dz);
+                } else {
                 const float lij = sqrtf((ex * ex + ey * ey) + ez * ez);
                 const float C = lij - rest;
                 if (CHECK) c2 = c2 + C * C;
@@ -200,19 +218,27 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
                 dx = dx - a0 * nx;
                 dy = dy - a0 * ny;
                 dz = dz - a0 * nz;
+                }
             }
         }
         float4 out = ps;
         const float nc = (float)(e - b);
         if (nc > 0.0f) {
             const float f = fixed[v];
+            if (FAST) {
+                const float fs = __fdividef(f, nc);
+                out.x = __fmaf_rn(fs, dx, ps.x);
+                out.y = __fmaf_rn(fs, dy, ps.y);
+                out.z = __fmaf_rn(fs, dz, ps.z);
+            } else {
             out.x = ps.x + f * (dx / nc);
             out.y = ps.y + f * (dy / nc);
             out.z = ps.z + f * (dz / nc);
+            }
         }
         yout[v] = out;
         if (yref != nullptr) {
-            if (mflags == nullptr) {
+            if (motion == nullptr) {
                 yref[v] = out;
             } else {
                 const float4 r = yref[v];
@@ -221,10 +247,19 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
             }
         }
     }
-    if (mflags != nullptr) {  // block-uniform
+    if (motion != nullptr) {  // block-uniform
+        const MotionBuf mb = motion_buf(motion, V);
         const unsigned m = __ballot_sync(0xffffffffu, moved);
         const int w0 = tile * BLOCK + (threadIdx.x & ~31);
-        if ((threadIdx.x & 31) == 0 && w0 < V) mflags[w0 >> 5] = m;
+        const int lane = threadIdx.x & 31;
+        if (lane == 0 && w0 < V) mb.flags[w0 >> 5] = m;
+        if (m) {
+            int base = 0;
+            if (lane == 0) base = atomicAdd(mb.count + (iter & 1), __popc(m));
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (moved) mb.list[base + __popc(m & ((1u << lane) - 1u))] = v;
+        }
+        if (tile == 0 && threadIdx.x == 0) mb.count[(iter + 1) & 1] = 0;
     }
     if (CHECK) block_residual_partial(c2, partial, tile);
     }
@@ -485,8 +520,11 @@ using SweepKernel = void (*)(int, const float4*, const float4*, float4*, const f
 struct SweepVariant {
     int g, block;
     SweepKernel kern, kern_y;  // bending on x or y chosen at run time / bending on y
+    SweepKernel fast, fast_y;  // the FAST arithmetic
 };
-#define SX_SWEEP_VARIANT(G, B) {G, B, jacobi_sweep_kernel<false, G, B>, jacobi_sweep_kernel<false, G, B, true>}
+#define SX_SWEEP_VARIANT(G, B)                                                                                  \
+    {G, B, jacobi_sweep_kernel<false, G, B>, jacobi_sweep_kernel<false, G, B, true>,                           \
+     jacobi_sweep_kernel<false, G, B, false, true>, jacobi_sweep_kernel<false, G, B, true, true>}
 static const SweepVariant kSweepVariants[] = {
     SX_SWEEP_VARIANT(2, 256), SX_SWEEP_VARIANT(1, 256), SX_SWEEP_VARIANT(4, 256), SX_SWEEP_VARIANT(2, 128),
     SX_SWEEP_VARIANT(2, 512), SX_SWEEP_VARIANT(4, 128), SX_SWEEP_VARIANT(1, 128), SX_SWEEP_VARIANT(3, 256),
@@ -508,13 +546,15 @@ extern "C" int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_o
                                  const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
                                  int bend_on_y, int variant, void* stream) {
     return sx_jacobi_sweep_tracked(x4, y_in4, y_out4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y,
-                                   variant, nullptr, nullptr, 0.0f, stream);
+                                   variant, 0, nullptr, nullptr, 0.0f, 0, stream);
 }
+
+extern "C" size_t sx_motion_buffer_bytes(int n_verts) { return motion_buf_bytes(n_verts > 0 ? n_verts : 1); }
 
 extern "C" int sx_jacobi_sweep_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
                                        const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
-                                       int bend_on_y, int variant, float* yref4, unsigned* motion_flags,
-                                       float motion_budget, void* stream) {
+                                       int bend_on_y, int variant, int fast, float* yref4, unsigned* motion_flags,
+                                       float motion_budget, int iteration, void* stream) {
     SX_REQUIRE(n_verts >= 0, "sx_jacobi_sweep_v: n_verts < 0");
     SX_REQUIRE(variant >= 0 && variant < kNumSweepVariants, "sx_jacobi_sweep_v: bad variant");
     if (n_verts == 0) return SX_OK;
@@ -524,10 +564,11 @@ extern "C" int sx_jacobi_sweep_tracked(const float* x4, const float* y_in4, floa
                "sx_jacobi_sweep_tracked: motion flags need reference positions and a positive budget");
     SX_REQUIRE(!yref4 || (yref4 != y_in4 && yref4 != y_out4), "sx_jacobi_sweep_tracked: yref4 must not alias y");
     const SweepVariant& sv = kSweepVariants[variant];
-    launch(bend_on_y ? sv.kern_y : sv.kern, grid_for(n_verts, sv.block), sv.block, 0, as_stream(stream), n_verts,
+    const SweepKernel k = fast ? (bend_on_y ? sv.fast_y : sv.fast) : (bend_on_y ? sv.kern_y : sv.kern);
+    launch(k, grid_for(n_verts, sv.block), sv.block, 0, as_stream(stream), n_verts,
            (const float4*)x4,
            (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring, k_bend,
-           bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr, (float4*)yref4, motion_flags,
+           bend_on_y ? 1 : 0, (const int*)nullptr, iteration, (double*)nullptr, (float4*)yref4, motion_flags,
            motion_flags ? motion_beta_check(motion_budget) : 0.0f);
     return check_launch("jacobi_sweep_kernel");
 }
@@ -769,15 +810,15 @@ extern "C" int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, floa
                                        int* conv, double* res3, void* ws, size_t ws_bytes,
                                        unsigned long long loop, int n_iter, void* stream) {
     return sx_jacobi_sweep_checked_tracked(x4, y_in4, y_out4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, iter,
-                                           check, tol, ref3, conv, res3, ws, ws_bytes, loop, n_iter, nullptr, nullptr,
-                                           0.0f, stream);
+                                           check, tol, ref3, conv, res3, ws, ws_bytes, loop, n_iter, 0, nullptr,
+                                           nullptr, 0.0f, stream);
 }
 
 extern "C" int sx_jacobi_sweep_checked_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
                                                const int* adj_ptr, const int* adj, int n_verts, float k_spring,
                                                float k_bend, int iter, int check, double tol, const double* ref3,
                                                int* conv, double* res3, void* ws, size_t ws_bytes,
-                                               unsigned long long loop, int n_iter, float* yref4,
+                                               unsigned long long loop, int n_iter, int fast, float* yref4,
                                                unsigned* motion_flags, float motion_budget, void* stream) {
     SX_REQUIRE(n_verts > 0, "sx_jacobi_sweep_checked: n_verts must be positive");
     SX_REQUIRE(!motion_flags || (yref4 && motion_budget > 0.0f),
@@ -796,7 +837,8 @@ extern "C" int sx_jacobi_sweep_checked_tracked(const float* x4, const float* y_i
     const int* gate = loop ? nullptr : (const int*)conv;
     const int nb = sweep_blocks(n_verts);
     if (check) {
-            constexpr auto kc = jacobi_sweep_kernel<true, 2, SW_BLOCK, true>;
+        const auto kc = fast ? jacobi_sweep_kernel<true, 2, SW_BLOCK, true, true>
+                             : jacobi_sweep_kernel<true, 2, SW_BLOCK, true>;
         launch(kc, gate ? tile_grid(kc, n_verts) : sweep_blocks(n_verts), SW_BLOCK, 0, s, n_verts,
                (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
                k_bend, 1, gate, iter, (double*)ws, (float4*)yref4, motion_flags, beta);
@@ -804,7 +846,8 @@ extern "C" int sx_jacobi_sweep_checked_tracked(const float* x4, const float* y_i
         if (rc) return rc;
         return residual_finish(n_verts, adj_ptr, ws, res3, conv, iter, tol, ref3, loop, n_iter, s);
     }
-    constexpr auto kp = jacobi_sweep_kernel<false, 2, SW_BLOCK, true>;
+    const auto kp = fast ? jacobi_sweep_kernel<false, 2, SW_BLOCK, true, true>
+                         : jacobi_sweep_kernel<false, 2, SW_BLOCK, true>;
     launch(kp, gate ? tile_grid(kp, n_verts) : sweep_blocks(n_verts), SW_BLOCK, 0, s, n_verts,
            (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
            k_bend, 1, gate, iter, (double*)nullptr, (float4*)yref4, motion_flags, beta);

@@ -1054,8 +1054,9 @@ __global__ void inc_count_kernel(const int* __restrict__ meta, const int4* __res
 // count -> block-local exclusive prefix; clears cnt for the next substep and
 // the fill cursors
 __global__ void __launch_bounds__(INC_BLOCK) inc_block_scan_kernel(int V, int* cnt, int* cur, int* count, int* start,
-                                                                   int* btot) {
+                                                                   int* btot, int* motion_count) {
     pdl_entry();
+    if (blockIdx.x == 0 && threadIdx.x < 2) motion_count[threadIdx.x] = 0;  // flagged lists of the iterations to come
     __shared__ int warp_tot[INC_BLOCK / 32];
     const int v = blockIdx.x * INC_BLOCK + threadIdx.x;
     const int c = v < V ? cnt[v] : 0;
@@ -1117,7 +1118,7 @@ __device__ __forceinline__ int lowest_flagged(const unsigned* __restrict__ f, in
 // project.
 template <int U, int MINB>
 __global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_moved_kernel(
-    const int* __restrict__ meta, const int4* __restrict__ split, const unsigned* __restrict__ mflags, int n_words,
+    const int* __restrict__ meta, const int4* __restrict__ split, const unsigned* __restrict__ motion, int n_dy,
     const int* __restrict__ count, const int* __restrict__ start, const int* __restrict__ btot,
     const int* __restrict__ inc, RecCtx rc, float cull_d2, int* status, const int* conv, int iter) {
     pdl_entry();
@@ -1192,21 +1193,21 @@ __global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_moved_kernel(
         __syncwarp();
         while (n1 >= 32) sat_stage(32);
     }
-    for (int w = gw; w < n_words; w += nw) {
-        unsigned word = __ldg(mflags + w);  // warp-uniform
-        while (word) {
-            const int v = 32 * w + __ffs(word) - 1;
-            word &= word - 1u;
-            const int s = start[v] + btot[v / INC_BLOCK], n = count[v];
-            for (int b = 0; b < n; b += 32) {
-                const int t = b + lane < n ? inc[s + b + lane] : -1;
-                const bool take = t >= 0 && lowest_flagged(mflags, split[t]) == v;
-                const unsigned m = __ballot_sync(0xffffffffu, take);
-                if (take) s0[n0 + __popc(m & below)] = t;
-                n0 += __popc(m);
-                __syncwarp();
-                if (n0 >= 32) box_stage(32);
-            }
+    // the vertices flagged in this iteration, one per warp
+    const MotionBuf mb = motion_buf(const_cast<unsigned*>(motion), n_dy);
+    const unsigned* mflags = mb.flags;
+    const int nflag = mb.count[iter & 1];
+    for (int h = gw; h < nflag; h += nw) {
+        const int v = mb.list[h];
+        const int s = start[v] + btot[v / INC_BLOCK], n = count[v];
+        for (int b = 0; b < n; b += 32) {
+            const int t = b + lane < n ? inc[s + b + lane] : -1;
+            const bool take = t >= 0 && lowest_flagged(mflags, split[t]) == v;
+            const unsigned m = __ballot_sync(0xffffffffu, take);
+            if (take) s0[n0 + __popc(m & below)] = t;
+            n0 += __popc(m);
+            __syncwarp();
+            if (n0 >= 32) box_stage(32);
         }
     }
     if (n0 > 0) box_stage(n0);
@@ -1899,7 +1900,8 @@ extern "C" size_t sx_contact_split_workspace_bytes(int n_dy, long long max_split
 }
 
 extern "C" int sx_contact_pairs_split(int n_dy, int n_st, const int* pairs, void* ws, int* split,
-                                      long long max_split, void* split_ws, size_t split_ws_bytes, const float* y4,
+                                      long long max_split, void* split_ws, size_t split_ws_bytes, unsigned* motion,
+                                      const float* y4,
                                       const float* xs4, const float* fixed, const float* m_inv, float dHat,
                                       float compliance, float cull_d2, float motion_budget, long long* dx_fix,
                                       int* nc, int* status, const int* conv, int iter, int variant, void* stream) {
@@ -1908,7 +1910,7 @@ extern "C" int sx_contact_pairs_split(int n_dy, int n_st, const int* pairs, void
     SX_REQUIRE(cull_d2 > 0.0f && motion_budget > 0.0f, "sx_contact_pairs_split: needs cull_d2 > 0 and a positive "
                                                        "motion budget");
     if (n_dy == 0) return SX_OK;
-    SX_REQUIRE(pairs && ws && split && split_ws && y4 && fixed && m_inv && dx_fix && nc && status,
+    SX_REQUIRE(pairs && ws && split && split_ws && motion && y4 && fixed && m_inv && dx_fix && nc && status,
                "sx_contact_pairs_split: null pointer");
     SX_REQUIRE(split_ws_bytes >= sx_contact_split_workspace_bytes(n_dy, max_split),
                "sx_contact_pairs_split: split workspace too small");
@@ -1929,7 +1931,8 @@ extern "C" int sx_contact_pairs_split(int n_dy, int n_st, const int* pairs, void
     const int nb = (n_dy + INC_BLOCK - 1) / INC_BLOCK;
     const int gf = sm_count() * 8;
     launch(inc_count_kernel, gf, 256, 0, st, (const int*)w.meta, (const int4*)split, ms, iw.cnt);
-    launch(inc_block_scan_kernel, nb, INC_BLOCK, 0, st, n_dy, iw.cnt, iw.cur, iw.count, iw.start, iw.btot);
+    launch(inc_block_scan_kernel, nb, INC_BLOCK, 0, st, n_dy, iw.cnt, iw.cur, iw.count, iw.start, iw.btot,
+           motion_buf(motion, n_dy).count);
     launch(pairs_scan_kernel, 1, 1024, 0, st, nb, iw.btot);
     launch(inc_fill_kernel, gf, 256, 0, st, (const int*)w.meta, (const int4*)split, ms, iw.cur, (const int*)iw.start,
            (const int*)iw.btot, iw.inc, iw.inc_cap, status);
@@ -1938,7 +1941,7 @@ extern "C" int sx_contact_pairs_split(int n_dy, int n_st, const int* pairs, void
 
 extern "C" int sx_contact_pairs_project_moved(int n_dy, int n_st, const int* split, const void* ws,
                                               const void* split_ws, long long max_split,
-                                              const unsigned* motion_flags, const float* y4, const float* xs4,
+                                              const unsigned* motion, const float* y4, const float* xs4,
                                               const float* fixed, const float* m_inv, float dHat, float compliance,
                                               float cull_d2, long long* dx_fix, int* nc, int* status,
                                               const int* conv, int iter, int variant, void* stream) {
@@ -1946,7 +1949,7 @@ extern "C" int sx_contact_pairs_project_moved(int n_dy, int n_st, const int* spl
     SX_REQUIRE(n_dy >= 0 && n_st >= 0 && max_split >= 0, "sx_contact_pairs_project_moved: bad sizes");
     SX_REQUIRE(cull_d2 > 0.0f, "sx_contact_pairs_project_moved: needs cull_d2 > 0");
     if (n_dy == 0) return SX_OK;
-    SX_REQUIRE(split && ws && split_ws && motion_flags && y4 && fixed && m_inv && dx_fix && nc && status,
+    SX_REQUIRE(split && ws && split_ws && motion && y4 && fixed && m_inv && dx_fix && nc && status,
                "sx_contact_pairs_project_moved: null pointer");
     SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_project_moved: null static positions");
     PairsWs w = pairs_ws(const_cast<void*>(ws), n_dy, n_st);
@@ -1954,7 +1957,7 @@ extern "C" int sx_contact_pairs_project_moved(int n_dy, int n_st, const int* spl
     const PairsProjectVariant& pv = kPairsProjectVariants[variant];
     const RecCtx rc{(const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, dx_fix, nc};
     launch(kPairsSplitVariants[variant].moved, sm_count() * pv.blocks_per_sm, PP_BLOCK, 0, as_stream(stream),
-           (const int*)w.meta, (const int4*)split, motion_flags, (n_dy + 31) / 32, (const int*)iw.count,
+           (const int*)w.meta, (const int4*)split, motion, n_dy, (const int*)iw.count,
            (const int*)iw.start, (const int*)iw.btot, (const int*)iw.inc, rc, cull_d2, status, conv, iter);
     return check_launch("pairs_project_moved_kernel");
 }

@@ -105,6 +105,10 @@ class Solver:
         self.contact_cull = True
         self.contact_motion_budget = 0.05
         self._split = self._yref4 = self._mflags = None
+        # the sweep's fast arithmetic (FMA, hardware reciprocal square root):
+        # within float rounding of the exact sweep, held to the substep's
+        # position and residual tolerance rather than bit-equality
+        self.fast_math = False
         # edge-edge contacts (__ee_st / __ee_dy; commented out in the
         # reference's solver, so off by default)
         self.enable_edge_edge = False
@@ -207,7 +211,8 @@ class Solver:
         if self.tol is None:
             sx.sx_jacobi_sweep_tracked(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
                                        ptr(m.adj), m.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0,
-                                       self.sweep_variant, yref, mfl, beta, stream_handle())
+                                       self.sweep_variant, 1 if self.fast_math else 0, yref, mfl, beta, iteration,
+                                       stream_handle())
         else:
             check = 1 if iteration > 0 and iteration % self.check_every == 0 else 0
             sx.sx_jacobi_sweep_checked_tracked(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed),
@@ -215,7 +220,8 @@ class Solver:
                                                check, float(self.tol),
                                                ptr(self._res_ref) if self.tol_relative else None, ptr(self._conv),
                                                ptr(self._res3), ptr(self._res_ws), self._res_ws.numel(), loop,
-                                               self.n_iter, yref, mfl, beta, stream_handle())
+                                               self.n_iter, 1 if self.fast_math else 0, yref, mfl, beta,
+                                               stream_handle())
         self._swap_y()
 
     def _split_active(self) -> bool:
@@ -235,7 +241,8 @@ class Solver:
             self._split_ws = torch.zeros(int(sx.sx_contact_split_workspace_bytes(Vd, self._split.shape[0])),
                                          dtype=torch.uint8, device=self.device)
             self._yref4 = torch.zeros_like(self.mesh_dy.y4)
-            self._mflags = torch.zeros((Vd + 31) // 32, dtype=torch.int32, device=self.device)
+            self._mflags = torch.zeros(int(sx.sx_motion_buffer_bytes(Vd)) // 4, dtype=torch.int32,
+                                       device=self.device)
 
     def _swap_y(self):
         m = self.mesh_dy
@@ -352,7 +359,8 @@ class Solver:
                 if iteration == 0:
                     sx.sx_contact_pairs_split(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
                                               ptr(self._pairs_ws), ptr(self._split), self._split.shape[0],
-                                              ptr(self._split_ws), self._split_ws.numel(), ptr(m.y4),
+                                              ptr(self._split_ws), self._split_ws.numel(), ptr(self._mflags),
+                                              ptr(m.y4),
                                               xs, ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c),
                                               self.contact_cull_d2(), self.motion_budget(), ptr(self._dx_fix),
                                               ptr(self._nc), ptr(self.status), conv, iteration, variant,
@@ -563,7 +571,7 @@ class Solver:
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
                 self.compliance_collision, self.self_collision, self.contact_cull, self.contact_motion_budget,
-                self.sweep_variant,
+                self.fast_math, self.sweep_variant,
                 self.pairs_variant, self.enable_edge_edge,
                 self.enable_velocity_update, self.mu, self.tol,
                 self.tol_relative,
