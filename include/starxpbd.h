@@ -82,26 +82,15 @@ int sx_jacobi_sweep_variant_info(int variant, int* g, int* block);
 int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
                       const int* adj, int n_verts, float k_spring, float k_bend, int bend_on_y, int variant,
                       void* stream);
-/* sx_jacobi_sweep_v that also tracks how far each vertex moves during a
- * substep's Jacobi iterations, for the contact-pair split
- * (sx_contact_pairs_split; no counterpart in the reference), and optionally
- * uses the fast arithmetic (fast != 0: fused multiply-adds, the hardware
- * reciprocal square root, a fast divide and n.n taken as 1 -- within float
- * rounding of the exact sweep, not bit-identical; fast = 0 is the exact,
- * reference-order arithmetic).  yref4 (float4 per vertex) NULL: no tracking.
- * motion NULL: the sweep's output is also written to yref4 (the reference
- * positions; the first iteration of a substep).  Otherwise, in the motion
- * buffer (sx_motion_buffer_bytes(n_verts)), bit v of the flag words is set
- * when the output's L1 distance from yref4[v] is at least motion_budget (or
- * NaN), and v is appended to the list of vertices flagged in this iteration;
- * a clear bit guarantees a Euclidean displacement below motion_budget.
- * iteration: the Jacobi iteration within the substep (its parity selects the
- * list counter).  The positions computed are those of sx_jacobi_sweep_v. */
-size_t sx_motion_buffer_bytes(int n_verts);
-int sx_jacobi_sweep_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
-                            const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
-                            int bend_on_y, int variant, int fast, float* yref4, unsigned* motion,
-                            float motion_budget, int iteration, void* stream);
+/* sx_jacobi_sweep_v with a choice of arithmetic (no counterpart in the
+ * reference): fast = 0 is the exact, reference-order float arithmetic of
+ * sx_jacobi_sweep_v (bit for bit); fast != 0 uses fused multiply-adds, the
+ * hardware reciprocal square root, a fast divide and n.n taken as 1 --
+ * within float rounding of the exact sweep, not bit-identical, and held to
+ * the substep's position and residual tolerance instead. */
+int sx_jacobi_sweep_mode(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
+                         const int* adj, int n_verts, float k_spring, float k_bend, int bend_on_y, int variant,
+                         int fast, void* stream);
 
 /* solve_sewing_constraints_x (XPBD.py:425-441) + update_dx over sewn vertex
  * pairs (zero rest length, k = compliance argument of the reference):
@@ -161,13 +150,12 @@ int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, float* y_out4, 
                             const int* adj, int n_verts, float k_spring, float k_bend, int iter, int check, double tol,
                             const double* ref3, int* conv, double* res3, void* ws, size_t ws_bytes,
                             unsigned long long loop, int n_iter, void* stream);
-/* sx_jacobi_sweep_checked with the arithmetic choice and motion tracking of
- * sx_jacobi_sweep_tracked */
-int sx_jacobi_sweep_checked_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
-                                    const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
-                                    int iter, int check, double tol, const double* ref3, int* conv, double* res3,
-                                    void* ws, size_t ws_bytes, unsigned long long loop, int n_iter, int fast,
-                                    float* yref4, unsigned* motion, float motion_budget, void* stream);
+/* sx_jacobi_sweep_checked with the arithmetic choice of sx_jacobi_sweep_mode */
+int sx_jacobi_sweep_checked_mode(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                                 const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
+                                 int iter, int check, double tol, const double* ref3, int* conv, double* res3,
+                                 void* ws, size_t ws_bytes, unsigned long long loop, int n_iter, int fast,
+                                 void* stream);
 int sx_loop_begin(void* stream, void* body_stream, unsigned long long* handle_out, void** ctx_out);
 int sx_loop_end(void* ctx);
 
@@ -363,44 +351,6 @@ int sx_contact_pairs_project_v(int n_dy, int n_st, const int* pairs, const void*
 int sx_contact_apply(int n_dy, float* y4, const float* fixed, long long* dx_fix, int* nc, const int* conv, int iter,
                      void* stream);
 
-/* The pair-list projection split by motion (no counterpart in the reference;
- * same sums as sx_contact_pairs_project, hence the same positions).
- *
- * sx_contact_pairs_split runs a substep's first projection (as
- * sx_contact_pairs_project with cull_d2 > 0) on positions y4 that are the
- * reference positions of sx_jacobi_sweep_tracked, and writes every pair of
- * `pairs` to split[max_split] (int4, kind vt_st / vt_dy / tv_st in bits 30-31
- * of the query index): FAR pairs, whose distance provably exceeds
- * sqrt(cull_d2) + 2 motion_budget on a triangle that stays classifiable
- * while its vertices move less than motion_budget (box-distance and
- * separating-axis bounds, rounding-safe), at the end; all others (NEAR) at the
- * front.  It then sorts the far pairs by vertex into split_ws
- * (sx_contact_split_workspace_bytes(n_dy, max_split) bytes, zero-filled
- * before its first use) and clears the flagged-vertex lists of the motion
- * buffer (sx_motion_buffer_bytes).  sx_contact_pairs_project_moved projects
- * a later iteration `iter`: every near pair as sx_contact_pairs_project does,
- * and the far pairs of the vertices that sx_jacobi_sweep_tracked (same
- * motion_budget, same iteration) flagged and listed in `motion`, each pair
- * once.  A far pair none of whose
- * vertices moved that far is farther than sqrt(cull_d2) and adds nothing.
- * Call sx_contact_pairs_split once after each sx_contact_pairs_build.  The
- * pair counts stay in the workspace (sx_contact_pairs_counts).  The order
- * inside the split list varies from run to run; the fixed-point sums do not
- * depend on it. */
-size_t sx_contact_split_workspace_bytes(int n_dy, long long max_split);
-int sx_contact_pairs_split(int n_dy, int n_st, const int* pairs, void* ws, int* split, long long max_split,
-                           void* split_ws, size_t split_ws_bytes, unsigned* motion, const float* y4, const float* xs4,
-                           const float* fixed, const float* m_inv, float dHat, float compliance, float cull_d2,
-                           float motion_budget, long long* dx_fix, int* nc, int* status, const int* conv, int iter,
-                           int variant, void* stream);
-int sx_contact_pairs_project_moved(int n_dy, int n_st, const int* split, const void* ws, const void* split_ws,
-                                   long long max_split, const unsigned* motion, const float* y4,
-                                   const float* xs4, const float* fixed, const float* m_inv, float dHat,
-                                   float compliance, float cull_d2, long long* dx_fix, int* nc, int* status,
-                                   const int* conv, int iter, int variant, void* stream);
-/* host copy of {vt_st end, vt_dy end, total pairs, near pairs} from the
- * workspace (synchronises the stream) */
-int sx_contact_pairs_counts(const void* ws, int n_dy, int n_st, int* counts4, void* stream);
 
 /* Edge-edge contacts: __ee_st / __ee_dy (collision_constraints_x.py:313-588;
  * d_type_EE distance.py:50-99, d_EE :119-124; the gradient in closed form)

@@ -884,105 +884,14 @@ API int or_contact_cull(int n, const float* p12, float cull_d2, int32_t* out) {
     return 0;
 }
 
-// ---------------------------------------------------------------------------
-// The CUDA pair-list split by motion (sx_contact_pairs_split /
-// sx_contact_pairs_project_moved), restated to check on the CPU that it never
-// changes a sum: or_split_far marks the far candidate slots at the reference
-// positions, or_split_skip the far slots none of whose dynamic vertices has
-// moved by the budget since; or_collision_sweep skips the slots so marked.
-// The formulas are the kernels' (robust_classifiable, far_radius_d2, the L1
-// motion test against budget * (1 - 1e-5)).
-// ---------------------------------------------------------------------------
-static bool robust_classifiable(V3 a, V3 b, V3 c, float beta) {
-    V3 e0 = sub(b, a), e1 = sub(c, b), e2 = sub(a, c);
-    V3 n = cross(e0, sub(c, a));
-    float nn = dot(n, n);
-    float l0 = dot(e0, e0), l1 = dot(e1, e1), l2 = dot(e2, e2);
-    float lo = std::fmin(std::fmin(l0, l1), l2), hi = std::fmax(std::fmax(l0, l1), l2);
-    float nmin = 8.0f * beta * std::sqrt(hi) + 8.0f * beta * beta;
-    return lo > 16.16f * beta * beta && nn > 1.01f * nmin * nmin && (nn * lo) * lo > 6.5e-29f &&
-           (nn * hi) * hi < 8.0e28f;
-}
-static float far_radius_d2(float cull_d2, float beta) {
-    double r = (std::sqrt((double)cull_d2) + 2.0 * (double)beta) * (1.0 + 1e-5);
-    return std::nextafter((float)(r * r), INFINITY);
-}
-namespace {
-// the four points and dynamic vertex ids (-1: static) of candidate slot j of
-// query i (vt_st | vt_dy | tv_st blocks); false for an empty or incident slot
-struct SlotView {
-    int Vd, Vs, cap;
-    const int32_t *faces_dy, *faces_st, *c[3], *n[3];
-    const float *y4, *xs4;
-    bool get(int i, int j, V3 x[4], int ids[4]) const {
-        int k = i < Vd ? 0 : i < 2 * Vd ? 1 : 2;
-        int q = k == 0 ? i : k == 1 ? i - Vd : i - 2 * Vd;
-        if (j >= std::min(n[k][q], cap)) return false;
-        int f = c[k][(size_t)q * cap + j];
-        const int32_t* F = k == 0 ? faces_st : faces_dy;
-        int a = F[3 * f], b = F[3 * f + 1], cc = F[3 * f + 2];
-        if (k == 1 && (a == q || b == q || cc == q)) return false;
-        const float* T = k == 0 ? xs4 : y4;
-        x[0] = v3((k == 2 ? xs4 : y4) + 4 * q);
-        x[1] = v3(T + 4 * a); x[2] = v3(T + 4 * b); x[3] = v3(T + 4 * cc);
-        ids[0] = k == 2 ? -1 : q;
-        ids[1] = k == 0 ? -1 : a; ids[2] = k == 0 ? -1 : b; ids[3] = k == 0 ? -1 : cc;
-        return true;
-    }
-};
-}  // namespace
-
-API int or_split_far(int Vd, int Vs, const int32_t* faces_dy, const int32_t* faces_st, const float* y4,
-                     const float* xs4, int cap, const int32_t* vt_st_c, const int32_t* vt_st_n, const int32_t* vt_dy_c,
-                     const int32_t* vt_dy_n, const int32_t* tv_st_c, const int32_t* tv_st_n, float cull_d2,
-                     float beta, uint8_t* far) {
-    SlotView sv{Vd, Vs, cap, faces_dy, faces_st, {vt_st_c, vt_dy_c, tv_st_c}, {vt_st_n, vt_dy_n, tv_st_n}, y4, xs4};
-    float fd2 = far_radius_d2(cull_d2, beta);
-    for (int i = 0; i < 2 * Vd + Vs; ++i)
-        for (int j = 0; j < cap; ++j) {
-            V3 x[4];
-            int ids[4];
-            far[(size_t)i * cap + j] = sv.get(i, j, x, ids) && robust_classifiable(x[1], x[2], x[3], beta) &&
-                                       (box_d2(x[0], x[1], x[2], x[3]) > fd2 || sat_far(x[0], x[1], x[2], x[3], fd2));
-        }
-    return 0;
-}
-
-API int or_split_skip(int Vd, int Vs, const int32_t* faces_dy, const int32_t* faces_st, const float* y4,
-                      const float* yref4, const float* xs4, int cap, const int32_t* vt_st_c, const int32_t* vt_st_n,
-                      const int32_t* vt_dy_c, const int32_t* vt_dy_n, const int32_t* tv_st_c,
-                      const int32_t* tv_st_n, float beta, const uint8_t* far, uint8_t* skip) {
-    SlotView sv{Vd, Vs, cap, faces_dy, faces_st, {vt_st_c, vt_dy_c, tv_st_c}, {vt_st_n, vt_dy_n, tv_st_n}, y4, xs4};
-    float bc = (float)((double)beta * (1.0 - 1e-5));
-    std::vector<uint8_t> moved(Vd);
-    for (int v = 0; v < Vd; ++v) {
-        const float *a = y4 + 4 * (size_t)v, *r = yref4 + 4 * (size_t)v;
-        float d = (std::fabs(a[0] - r[0]) + std::fabs(a[1] - r[1])) + std::fabs(a[2] - r[2]);
-        moved[v] = !(d < bc);
-    }
-    for (int i = 0; i < 2 * Vd + Vs; ++i)
-        for (int j = 0; j < cap; ++j) {
-            size_t o = (size_t)i * cap + j;
-            V3 x[4];
-            int ids[4];
-            bool m = false;
-            if (far[o] && sv.get(i, j, x, ids))
-                for (int k = 0; k < 4; ++k) m = m || (ids[k] >= 0 && moved[ids[k]]);
-            skip[o] = far[o] && !m;
-        }
-    return 0;
-}
-
 // accumulate != 0: dx_fix / nc already hold this iteration's edge-edge terms
 // (or_edge_edge_sweep) and are added to instead of cleared.
-// skip (optional, one byte per candidate slot, (2 Vd + Vs) x cap): slots to
-// leave out, as the CUDA split leaves out unmoved far pairs.
 API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_t* faces_st, float* y4,
                            const float* xs4, const float* fixed, const float* m_inv, float dHat, float compliance,
                            float cull_d2, int cap, const int32_t* vt_st_c, const int32_t* vt_st_n, const int32_t* vt_dy_c,
                            const int32_t* vt_dy_n, const int32_t* tv_st_c, const int32_t* tv_st_n,
                            int64_t* dx_fix, int32_t* nc, int32_t* pair, float* pair_g, float* pair_schur,
-                           int32_t* pair_num, int32_t* status, int nthreads, int accumulate, const uint8_t* skip) {
+                           int32_t* pair_num, int32_t* status, int nthreads, int accumulate) {
     int par = set_threads(nthreads);
     if (!accumulate) {
         std::memset(dx_fix, 0, sizeof(int64_t) * 3 * (size_t)Vd);
@@ -1008,7 +917,6 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
             int n = std::min(vt_st_n[vid], cap);
             for (int j = 0; j < n; ++j) {
                 int fs = vt_st_c[(size_t)vid * cap + j];
-                if (skip && skip[(size_t)i * cap + j]) continue;
                 V3 x0 = v3(y4 + 4 * vid);
                 V3 x1 = v3(xs4 + 4 * faces_st[3 * fs]), x2 = v3(xs4 + 4 * faces_st[3 * fs + 1]), x3 = v3(xs4 + 4 * faces_st[3 * fs + 2]);
                 if (culled(cull_d2, x0, x1, x2, x3)) continue;
@@ -1029,7 +937,6 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
                 int fd = vt_dy_c[(size_t)vid * cap + j];
                 int a = faces_dy[3 * fd], b = faces_dy[3 * fd + 1], c = faces_dy[3 * fd + 2];
                 if (a == vid || b == vid || c == vid) continue;
-                if (skip && skip[(size_t)i * cap + j]) continue;
                 int vv[4] = {vid, a, b, c};
                 V3 x[4] = {v3(y4 + 4 * vid), v3(y4 + 4 * a), v3(y4 + 4 * b), v3(y4 + 4 * c)};
                 if (culled(cull_d2, x[0], x[1], x[2], x[3])) continue;
@@ -1064,7 +971,6 @@ API int or_collision_sweep(int Vd, int Vs, const int32_t* faces_dy, const int32_
             int n = std::min(tv_st_n[vis], cap);
             for (int j = 0; j < n; ++j) {
                 int fd = tv_st_c[(size_t)vis * cap + j];
-                if (skip && skip[(size_t)i * cap + j]) continue;
                 int vv[4] = {-1, faces_dy[3 * fd], faces_dy[3 * fd + 1], faces_dy[3 * fd + 2]};
                 V3 x[4] = {v3(xs4 + 4 * vis), v3(y4 + 4 * vv[1]), v3(y4 + 4 * vv[2]), v3(y4 + 4 * vv[3])};
                 if (culled(cull_d2, x[0], x[1], x[2], x[3])) continue;

@@ -50,9 +50,7 @@ _SIGS = {
     "or_sewing_step": [I, P, P, P, P, P, F],
     "or_velocity_contacts": [I, I, P, P, I, P, P, P, P, P, P, P, P, P, F, P],
     "or_warm_features": [I, P, P, P, P, P, P, P, F, F, F, F, P],
-    "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, I, P],
-    "or_split_far": [I, I, P, P, P, P, I, P, P, P, P, P, P, F, F, P],
-    "or_split_skip": [I, I, P, P, P, P, P, I, P, P, P, P, P, P, F, P, P],
+    "or_collision_sweep": [I, I, P, P, P, P, P, P, F, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, P, I, I],
     "or_edge_edge_classify": [I, P, F, P, P, P],
     "or_point_triangles": [I, P, P, P, P],
     "or_contact_cull": [I, P, F, P],
@@ -278,13 +276,11 @@ def point_triangles(p12):
 
 
 def collision_sweep(faces_dy, faces_st, y4, xs4, fixed, m_inv, dHat, compliance, cap, vt_st, vt_dy, tv_st,
-                    want_pairs=False, nthreads=1, cull_d2=0.0, acc=None, skip=None):
+                    want_pairs=False, nthreads=1, cull_d2=0.0, acc=None):
     """Narrow phase + update_dx; updates y4 in place.  vt_st etc. = (cand, num).
     cull_d2 > 0 skips pairs whose point-to-triangle-box squared distance
     exceeds it (the CUDA pair-list sweep's cull).  acc = (dx, nc) from
-    :func:`edge_edge_sweep` of the same iteration, added to before update_dx.
-    skip: uint8 per candidate slot ((2 Vd + Vs) x cap, from :func:`split_skip`)
-    of slots to leave out."""
+    :func:`edge_edge_sweep` of the same iteration, added to before update_dx."""
     Vd = y4.shape[0]
     Vs = xs4.shape[0] if xs4 is not None else 0
     if acc is None:
@@ -305,42 +301,11 @@ def collision_sweep(faces_dy, faces_st, y4, xs4, fixed, m_inv, dHat, compliance,
     lib().or_collision_sweep(Vd, Vs, _p(i32(faces_dy)), _p(fs), _p(y4), _p(xs), _p(fixed), _p(m_inv), dHat,
                              compliance, cull_d2, cap, _p(vt_st[0]), _p(vt_st[1]), _p(vt_dy[0]), _p(vt_dy[1]),
                              _p(tv_st[0]), _p(tv_st[1]), _p(dx), _p(nc), _p(pair), _p(pair_g), _p(pair_schur),
-                             _p(pair_num), _p(status), nthreads, 0 if acc is None else 1,
-                             _p(skip) if skip is not None else None)
+                             _p(pair_num), _p(status), nthreads, 0 if acc is None else 1)
     out = {"status": int(status[0])}
     if want_pairs:
         out.update(pair=pair, pair_g=pair_g, pair_schur=pair_schur, pair_num=pair_num)
     return out
-
-
-def _slot_args(faces_dy, faces_st, xs4, vt_st, vt_dy, tv_st):
-    fs = i32(faces_st) if faces_st is not None else np.zeros(3, np.int32)
-    xs = xs4 if xs4 is not None else np.zeros((1, 4), np.float32)
-    return fs, xs, [_p(vt_st[0]), _p(vt_st[1]), _p(vt_dy[0]), _p(vt_dy[1]), _p(tv_st[0]), _p(tv_st[1])]
-
-
-def split_far(faces_dy, faces_st, y4, xs4, cap, vt_st, vt_dy, tv_st, cull_d2, beta):
-    """The CUDA contact-pair split's far test (sx_contact_pairs_split) on every
-    candidate slot at positions y4: uint8 [(2 Vd + Vs) x cap]."""
-    Vd = y4.shape[0]
-    Vs = xs4.shape[0] if xs4 is not None else 0
-    fs, xs, c = _slot_args(faces_dy, faces_st, xs4, vt_st, vt_dy, tv_st)
-    far = np.zeros((2 * Vd + Vs) * cap, np.uint8)
-    lib().or_split_far(Vd, Vs, _p(i32(faces_dy)), _p(fs), _p(y4), _p(xs), cap, *c, cull_d2, beta, _p(far))
-    return far
-
-
-def split_skip(faces_dy, faces_st, y4, yref4, xs4, cap, vt_st, vt_dy, tv_st, beta, far):
-    """Far slots none of whose dynamic vertices moved by beta (L1 test of the
-    CUDA sweep's motion flags) between yref4 and y4: the slots
-    sx_contact_pairs_project_moved leaves out."""
-    Vd = y4.shape[0]
-    Vs = xs4.shape[0] if xs4 is not None else 0
-    fs, xs, c = _slot_args(faces_dy, faces_st, xs4, vt_st, vt_dy, tv_st)
-    skip = np.zeros_like(far)
-    lib().or_split_skip(Vd, Vs, _p(i32(faces_dy)), _p(fs), _p(y4), _p(yref4), _p(xs), cap, *c, beta, _p(far),
-                        _p(skip))
-    return skip
 
 
 def edge_query_boxes(p4, edges, padding):
@@ -610,13 +575,8 @@ class OracleSolver:
                  damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
                  compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True,
                  contact_cull=False, tol=None, check_every=4, tol_relative=False, sewing=None,
-                 velocity_update=False, mu=0.8, edge_edge=False, scatter_atomics=False, motion_budget=None):
+                 velocity_update=False, mu=0.8, edge_edge=False, scatter_atomics=False):
         self.d = mesh_dy
-        # the CUDA contact-pair split (absolute budget; needs contact_cull):
-        # far slots found at the first iteration's positions are left out of
-        # later iterations while none of their vertices moved by the budget
-        self.motion_budget = motion_budget
-        self.split_skipped = 0
         # multithreaded spring sweeps: a deterministic per-vertex gather (equal
         # to the serial sweep bit for bit) unless scatter_atomics, which runs
         # the reference's scatter with float atomics (order dependent), the
@@ -752,18 +712,6 @@ class OracleSolver:
                 if it == 0:
                     cands = self._broad(y4)
                 vt_st, vt_dy, tv_st = cands
-                skip = None
-                if self.motion_budget and self.cull_d2 > 0:
-                    has_st = self.s is not None
-                    args = (self.faces, self.faces_st if has_st else None)
-                    if it == 0:
-                        far = split_far(*args, y4, self.xs4 if has_st else None, self.cap, vt_st[:2], vt_dy[:2],
-                                        tv_st[:2], np.float32(self.cull_d2), np.float32(self.motion_budget))
-                        yref = y4.copy()
-                    else:
-                        skip = split_skip(*args, y4, yref, self.xs4 if has_st else None, self.cap, vt_st[:2],
-                                          vt_dy[:2], tv_st[:2], np.float32(self.motion_budget), far)
-                        self.split_skipped += int(skip.sum())
                 acc = None
                 if self.edge_edge:
                     Vd = y4.shape[0]
@@ -780,7 +728,7 @@ class OracleSolver:
                                     self.xs4 if self.s is not None else None, self.fixed, self.m_inv, self.dHat,
                                     self.compliance, self.cap, vt_st[:2], vt_dy[:2], tv_st[:2],
                                     nthreads=self.nthreads, cull_d2=self.cull_d2,
-                                    want_pairs=self.velocity_update, acc=acc, skip=skip)
+                                    want_pairs=self.velocity_update, acc=acc)
                 self.last_status |= r["status"]
                 if self.velocity_update:
                     self._records = r

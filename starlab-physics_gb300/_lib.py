@@ -40,8 +40,7 @@ SIGNATURES = {
     "sx_jacobi_sweep_variant_info": ([I, P, P], I),
     "sx_set_programmatic_launch": ([I], I),
     "sx_jacobi_sweep_v": ([P, P, P, P, P, P, I, F, F, I, I, P], I),
-    "sx_jacobi_sweep_tracked": ([P, P, P, P, P, P, I, F, F, I, I, I, P, P, F, I, P], I),
-    "sx_motion_buffer_bytes": ([I], Z),
+    "sx_jacobi_sweep_mode": ([P, P, P, P, P, P, I, F, F, I, I, I, P], I),
     "sx_velocity_update": ([P, P, P, P, I, F, F, P], I),
     "sx_compute_velocity": ([P, P, P, P, I, F, F, P], I),
     "sx_update_x": ([P, P, I, F, P], I),
@@ -51,8 +50,8 @@ SIGNATURES = {
     "sx_constraint_residual": ([P, P, P, I, P, P, Z, P], I),
     "sx_convergence_begin": ([P, I, I, P], I),
     "sx_jacobi_sweep_checked": ([P, P, P, P, P, P, I, F, F, I, I, C.c_double, P, P, P, P, Z, C.c_ulonglong, I, P], I),
-    "sx_jacobi_sweep_checked_tracked": ([P, P, P, P, P, P, I, F, F, I, I, C.c_double, P, P, P, P, Z, C.c_ulonglong, I,
-                                         I, P, P, F, P], I),
+    "sx_jacobi_sweep_checked_mode": ([P, P, P, P, P, P, I, F, F, I, I, C.c_double, P, P, P, P, Z, C.c_ulonglong, I,
+                                      I, P], I),
     "sx_loop_begin": ([P, P, P, P], I),
     "sx_loop_end": ([P], I),
     "sx_face_aabbs": ([P, P, I, F, P, P, P], I),
@@ -80,12 +79,6 @@ SIGNATURES = {
     "sx_contact_pairs_project_variant_info": ([I, P, P], I),
     "sx_contact_pairs_project_v": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, I, P], I),
     "sx_contact_apply": ([I, P, P, P, P, P, I, P], I),
-    "sx_contact_split_workspace_bytes": ([I, C.c_longlong], Z),
-    "sx_contact_pairs_split": ([I, I, P, P, P, C.c_longlong, P, Z, P, P, P, P, P, F, F, F, F, P, P, P, P, I, I, P],
-                               I),
-    "sx_contact_pairs_project_moved": ([I, I, P, P, P, C.c_longlong, P, P, P, P, P, F, F, F, P, P, P, P, I, I, P],
-                                       I),
-    "sx_contact_pairs_counts": ([P, I, I, P, P], I),
     "sx_edge_edge_sweep": ([I, P, P, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, I, P], I),
     "sx_edge_edge_classify": ([I, P, F, P, P, P, P], I),
     "sx_cell_bvh_traverse_edges": ([P, I, P, F, P, P, P, P, P, P, I, P, P, P, P], I),

@@ -254,16 +254,14 @@ class BatchedSolver:
         handle, given with the body's checked sweep."""
         fast = 1 if self.fast_math else 0
         if conv is not None:
-            sx.sx_jacobi_sweep_checked_tracked(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
-                                               ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend, it,
-                                               1 if check else 0, float(self.tol), ref, conv, ptr(self._res3),
-                                               ptr(self._res_ws), self._res_ws.numel(), loop, self.n_iter, fast, None,
-                                               None, 0.0, s)
+            sx.sx_jacobi_sweep_checked_mode(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
+                                            ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend, it,
+                                            1 if check else 0, float(self.tol), ref, conv, ptr(self._res3),
+                                            ptr(self._res_ws), self._res_ws.numel(), loop, self.n_iter, fast, s)
         else:
-            sx.sx_jacobi_sweep_tracked(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
-                                       ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend,
-                                       1 if self.bending_on == "y" else 0, self.sweep_variant, fast, None, None, 0.0, it,
-                                       s)
+            sx.sx_jacobi_sweep_mode(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
+                                    ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend,
+                                    1 if self.bending_on == "y" else 0, self.sweep_variant, fast, s)
         self._swap_y()
         if it == 0:
             sx.sx_batched_obstacle_broadphase(

@@ -147,13 +147,6 @@ inline int tile_grid(K kernel, int n_verts) {
 // fewer instructions per entry, results within float rounding of the exact
 // form but not bit-identical to it; validated against the oracle at the
 // position and residual tolerance of the substep instead.
-//
-// Motion tracking for the contact-pair split (optional, yref != nullptr):
-// with motion == nullptr the sweep also writes its output to yref (the
-// reference positions of a substep's pair-list split); otherwise bit v of the
-// motion buffer's flags is set when |out - yref|_1 >= beta or is NaN (one
-// 32-bit word per warp, written whole) and v is appended to its list
-// (count[iter & 1]).  The positions the sweep computes do not change.
 template <bool CHECK, int G = 2, int BLOCK = SW_BLOCK, bool BY = false, bool FAST = false>
 __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
                                                                 const float4* __restrict__ yin,
@@ -162,17 +155,14 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
                                                                 const int* __restrict__ ptr,
                                                                 const int2* __restrict__ adj, float ks, float kb,
                                                                 int bend_y, const int* conv, int iter,
-                                                                double* __restrict__ partial, float4* yref,
-                                                                unsigned* __restrict__ motion, float beta) {
+                                                                double* __restrict__ partial) {
     pdl_entry();
     if (iteration_skipped(conv, iter)) return;  // grid-uniform
     static_assert(!CHECK || BLOCK == SW_BLOCK, "residual partials are per SW_BLOCK tile");
-    static_assert(BLOCK % 32 == 0, "motion flags are written one word per warp");
     const int ntiles = (V + BLOCK - 1) / BLOCK;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int v = tile * BLOCK + threadIdx.x;
     float c2 = 0.0f;  // sum of C^2 over this vertex's entries (CHECK)
-    bool moved = false;
     if (v < V) {
         const float4 ps = __ldg(yin + v), xs = __ldg(x4 + v);
         const int b = __ldg(ptr + v), e = __ldg(ptr + v + 1);
@@ -237,29 +227,6 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
             }
         }
         yout[v] = out;
-        if (yref != nullptr) {
-            if (motion == nullptr) {
-                yref[v] = out;
-            } else {
-                const float4 r = yref[v];
-                const float d = (fabsf(out.x - r.x) + fabsf(out.y - r.y)) + fabsf(out.z - r.z);
-                moved = !(d < beta);
-            }
-        }
-    }
-    if (motion != nullptr) {  // block-uniform
-        const MotionBuf mb = motion_buf(motion, V);
-        const unsigned m = __ballot_sync(0xffffffffu, moved);
-        const int w0 = tile * BLOCK + (threadIdx.x & ~31);
-        const int lane = threadIdx.x & 31;
-        if (lane == 0 && w0 < V) mb.flags[w0 >> 5] = m;
-        if (m) {
-            int base = 0;
-            if (lane == 0) base = atomicAdd(mb.count + (iter & 1), __popc(m));
-            base = __shfl_sync(0xffffffffu, base, 0);
-            if (moved) mb.list[base + __popc(m & ((1u << lane) - 1u))] = v;
-        }
-        if (tile == 0 && threadIdx.x == 0) mb.count[(iter + 1) & 1] = 0;
     }
     if (CHECK) block_residual_partial(c2, partial, tile);
     }
@@ -500,23 +467,15 @@ extern "C" int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep: y_in4 and y_out4 must not alias");
     launch(bend_on_y ? jacobi_sweep_kernel<false, 2, SW_BLOCK, true> : jacobi_sweep_kernel<false>, sweep_blocks(n_verts),
            SW_BLOCK, 0, as_stream(stream), n_verts, (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed,
-           adj_ptr, (const int2*)adj, k_spring, k_bend, bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr,
-           (float4*)nullptr, (unsigned*)nullptr, 0.0f);
+           adj_ptr, (const int2*)adj, k_spring, k_bend, bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr);
     return check_launch("jacobi_sweep_kernel");
 }
-
-namespace sx {
-// The motion test compares a float L1 displacement (three float differences
-// and two sums, relative error below 4 * 2^-24) with the budget shrunk by
-// 1e-5, so a clear bit means a true displacement below the budget.
-float motion_beta_check(float budget) { return (float)((double)budget * (1.0 - 1e-5)); }
-}  // namespace sx
 
 // Launch configurations of the sweep for the autotuner: (entries per load
 // batch, threads per block).  All give bit-identical results.
 namespace sx {
 using SweepKernel = void (*)(int, const float4*, const float4*, float4*, const float*, const int*, const int2*, float,
-                            float, int, const int*, int, double*, float4*, unsigned*, float);
+                            float, int, const int*, int, double*);
 struct SweepVariant {
     int g, block;
     SweepKernel kern, kern_y;  // bending on x or y chosen at run time / bending on y
@@ -545,31 +504,23 @@ extern "C" int sx_jacobi_sweep_variant_info(int variant, int* g, int* block) {
 extern "C" int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
                                  const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
                                  int bend_on_y, int variant, void* stream) {
-    return sx_jacobi_sweep_tracked(x4, y_in4, y_out4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y,
-                                   variant, 0, nullptr, nullptr, 0.0f, 0, stream);
+    return sx_jacobi_sweep_mode(x4, y_in4, y_out4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y, variant,
+                                0, stream);
 }
 
-extern "C" size_t sx_motion_buffer_bytes(int n_verts) { return motion_buf_bytes(n_verts > 0 ? n_verts : 1); }
-
-extern "C" int sx_jacobi_sweep_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
-                                       const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
-                                       int bend_on_y, int variant, int fast, float* yref4, unsigned* motion_flags,
-                                       float motion_budget, int iteration, void* stream) {
+extern "C" int sx_jacobi_sweep_mode(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                                    const int* adj_ptr, const int* adj, int n_verts, float k_spring, float k_bend,
+                                    int bend_on_y, int variant, int fast, void* stream) {
     SX_REQUIRE(n_verts >= 0, "sx_jacobi_sweep_v: n_verts < 0");
     SX_REQUIRE(variant >= 0 && variant < kNumSweepVariants, "sx_jacobi_sweep_v: bad variant");
     if (n_verts == 0) return SX_OK;
     SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj, "sx_jacobi_sweep_v: null pointer");
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_v: y_in4 and y_out4 must not alias");
-    SX_REQUIRE(!motion_flags || (yref4 && motion_budget > 0.0f),
-               "sx_jacobi_sweep_tracked: motion flags need reference positions and a positive budget");
-    SX_REQUIRE(!yref4 || (yref4 != y_in4 && yref4 != y_out4), "sx_jacobi_sweep_tracked: yref4 must not alias y");
     const SweepVariant& sv = kSweepVariants[variant];
     const SweepKernel k = fast ? (bend_on_y ? sv.fast_y : sv.fast) : (bend_on_y ? sv.kern_y : sv.kern);
-    launch(k, grid_for(n_verts, sv.block), sv.block, 0, as_stream(stream), n_verts,
-           (const float4*)x4,
+    launch(k, grid_for(n_verts, sv.block), sv.block, 0, as_stream(stream), n_verts, (const float4*)x4,
            (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring, k_bend,
-           bend_on_y ? 1 : 0, (const int*)nullptr, iteration, (double*)nullptr, (float4*)yref4, motion_flags,
-           motion_flags ? motion_beta_check(motion_budget) : 0.0f);
+           bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr);
     return check_launch("jacobi_sweep_kernel");
 }
 
@@ -809,23 +760,16 @@ extern "C" int sx_jacobi_sweep_checked(const float* x4, const float* y_in4, floa
                                        float k_bend, int iter, int check, double tol, const double* ref3,
                                        int* conv, double* res3, void* ws, size_t ws_bytes,
                                        unsigned long long loop, int n_iter, void* stream) {
-    return sx_jacobi_sweep_checked_tracked(x4, y_in4, y_out4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, iter,
-                                           check, tol, ref3, conv, res3, ws, ws_bytes, loop, n_iter, 0, nullptr,
-                                           nullptr, 0.0f, stream);
+    return sx_jacobi_sweep_checked_mode(x4, y_in4, y_out4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, iter,
+                                        check, tol, ref3, conv, res3, ws, ws_bytes, loop, n_iter, 0, stream);
 }
 
-extern "C" int sx_jacobi_sweep_checked_tracked(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
-                                               const int* adj_ptr, const int* adj, int n_verts, float k_spring,
-                                               float k_bend, int iter, int check, double tol, const double* ref3,
-                                               int* conv, double* res3, void* ws, size_t ws_bytes,
-                                               unsigned long long loop, int n_iter, int fast, float* yref4,
-                                               unsigned* motion_flags, float motion_budget, void* stream) {
+extern "C" int sx_jacobi_sweep_checked_mode(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                                            const int* adj_ptr, const int* adj, int n_verts, float k_spring,
+                                            float k_bend, int iter, int check, double tol, const double* ref3,
+                                            int* conv, double* res3, void* ws, size_t ws_bytes,
+                                            unsigned long long loop, int n_iter, int fast, void* stream) {
     SX_REQUIRE(n_verts > 0, "sx_jacobi_sweep_checked: n_verts must be positive");
-    SX_REQUIRE(!motion_flags || (yref4 && motion_budget > 0.0f),
-               "sx_jacobi_sweep_checked_tracked: motion flags need reference positions and a positive budget");
-    SX_REQUIRE(!yref4 || (yref4 != y_in4 && yref4 != y_out4),
-               "sx_jacobi_sweep_checked_tracked: yref4 must not alias y");
-    const float beta = motion_flags ? motion_beta_check(motion_budget) : 0.0f;
     SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && adj && conv, "sx_jacobi_sweep_checked: null pointer");
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_checked: y_in4 and y_out4 must not alias");
     SX_REQUIRE(iter >= 0, "sx_jacobi_sweep_checked: iter < 0");
@@ -841,7 +785,7 @@ extern "C" int sx_jacobi_sweep_checked_tracked(const float* x4, const float* y_i
                              : jacobi_sweep_kernel<true, 2, SW_BLOCK, true>;
         launch(kc, gate ? tile_grid(kc, n_verts) : sweep_blocks(n_verts), SW_BLOCK, 0, s, n_verts,
                (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
-               k_bend, 1, gate, iter, (double*)ws, (float4*)yref4, motion_flags, beta);
+               k_bend, 1, gate, iter, (double*)ws);
         int rc = check_launch("jacobi_sweep_kernel");
         if (rc) return rc;
         return residual_finish(n_verts, adj_ptr, ws, res3, conv, iter, tol, ref3, loop, n_iter, s);
@@ -850,7 +794,7 @@ extern "C" int sx_jacobi_sweep_checked_tracked(const float* x4, const float* y_i
                          : jacobi_sweep_kernel<false, 2, SW_BLOCK, true>;
     launch(kp, gate ? tile_grid(kp, n_verts) : sweep_blocks(n_verts), SW_BLOCK, 0, s, n_verts,
            (const float4*)x4, (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring,
-           k_bend, 1, gate, iter, (double*)nullptr, (float4*)yref4, motion_flags, beta);
+           k_bend, 1, gate, iter, (double*)nullptr);
     return check_launch("jacobi_sweep_kernel");
 }
 

@@ -131,25 +131,6 @@ constexpr int kNumCells = kGridRes * kGridRes * kGridRes;
 constexpr int kGridHeader = 8;
 constexpr int kGridWords = kGridHeader + kGridRes * kGridRes;
 
-// ---- motion buffer of the contact-pair split ----------------------------------
-// One bit per vertex (flags), two list counters (count[iteration & 1]) and
-// the list of the vertices flagged in that iteration; a sweep of iteration k
-// appends to count[k & 1] and clears count[(k + 1) & 1] for the next one.
-struct MotionBuf {
-    unsigned* flags;
-    int* count;
-    int* list;
-};
-__host__ __device__ inline int motion_words(int n_verts) { return ((n_verts + 31) / 32 + 63) & ~63; }
-__host__ __device__ inline MotionBuf motion_buf(unsigned* base, int n_verts) {
-    MotionBuf m;
-    m.flags = base;
-    m.count = (int*)(base + motion_words(n_verts));
-    m.list = m.count + 64;
-    return m;
-}
-inline size_t motion_buf_bytes(int n_verts) { return ((size_t)motion_words(n_verts) + 64 + (size_t)n_verts) * 4; }
-
 // ---- convergence control -------------------------------------------------------
 // conv[0] = stop iteration of the current substep: -1 while it has not
 // converged, else the iteration j (a multiple of the check interval

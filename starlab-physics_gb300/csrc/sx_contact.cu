@@ -6,8 +6,6 @@
 // Corrections are accumulated in 64-bit fixed point (40 fractional bits) with
 // integer atomics, so the sum does not depend on the order in which threads
 // arrive (the reference uses float atomics, whose result does).
-#include <cmath>
-
 #include "sx_common.cuh"
 
 namespace sx {
@@ -576,10 +574,6 @@ __global__ void __launch_bounds__(PB) pairs_fill_kernel(int Vd, int Vs, int cap,
     if (q == Vd) meta[0] = off;
     if (q == 2 * Vd) meta[1] = off;
     if (q == Q) meta[2] = off;
-    if (q == 0) {  // near / far counters of sx_contact_pairs_split
-        meta[4] = 0;
-        meta[5] = 0;
-    }
     if (q >= Q || c == 0) return;
     int k = off;
     if (q < Vd) {
@@ -808,412 +802,6 @@ __global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_kernel(const int
         if (n1 > 0) sat_stage(n1);
         if (lane < n2) project_pair(c, s2[lane], &bad);
     }
-    if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
-}
-
-// ---------------------------------------------------------------------------
-// The pair list split by motion.  Within a substep the candidate lists are
-// fixed and the Jacobi iterations move the vertices only a little (on the
-// drape, 99 % of vertices by under 0.1 mm over 30 iterations, against pair
-// distances of millimetres), so the first iteration sorts the pairs into a
-// NEAR part and a FAR part.  A far pair's point-triangle distance at the
-// reference positions (the sweep's output in that iteration, saved by
-// sx_jacobi_sweep_tracked) exceeds sqrt(cull_d2) + 2 beta, and its triangle
-// stays classifiable while each vertex moves less than beta.  Every point of
-// a triangle whose vertices each moved less than beta lies within beta of
-// the old triangle, so while no vertex of a far pair has moved by beta the
-// pair's distance stays above sqrt(cull_d2) and -- exactly as for a pair the
-// regular cull skips -- its projection adds nothing.  Later iterations test
-// the near pairs as before and a far pair only when the sweep flagged one of
-// its dynamic vertices.  The sums are the same as the full list's.
-// Split records carry their kind (0 vt_st, 1 vt_dy, 2 tv_st) in bits 30-31 of
-// the query index.
-// ---------------------------------------------------------------------------
-constexpr int M_NEAR = 4, M_FAR = 5;  // meta slots: near / far counters
-constexpr unsigned KIND_SHIFT = 30;
-
-__device__ __forceinline__ int rec_kind(int4 r) { return (int)((unsigned)r.x >> KIND_SHIFT); }
-__device__ __forceinline__ int rec_query(int4 r) { return r.x & 0x3fffffff; }
-__device__ __forceinline__ int pos_kind(int t, int st_end, int dy_end) { return t < st_end ? 0 : t < dy_end ? 1 : 2; }
-__device__ __forceinline__ int4 make_rec(int4 pr, int kind) {
-    return make_int4((int)((unsigned)pr.x | ((unsigned)kind << KIND_SHIFT)), pr.y, pr.z, pr.w);
-}
-
-struct RecCtx {
-    const float4* __restrict__ y4;
-    const float4* __restrict__ xs4;
-    const float* __restrict__ fixed;
-    const float* __restrict__ m_inv;
-    float dHat, compliance;
-    long long* dx;
-    int* nc;
-};
-
-__device__ __forceinline__ void rec_points(const RecCtx& c, int4 r, V3 x[4]) {
-    const int k = rec_kind(r);
-    x[0] = mk((k == 2 ? c.xs4 : c.y4)[rec_query(r)]);
-    const float4* tri = k == 0 ? c.xs4 : c.y4;
-    x[1] = mk(tri[r.y]);
-    x[2] = mk(tri[r.z]);
-    x[3] = mk(tri[r.w]);
-}
-
-// project_pair for a split record
-__device__ __forceinline__ void project_rec(const RecCtx& c, int4 r, int* bad) {
-    V3 x[4];
-    rec_points(c, r, x);
-    V3 g[4] = SX_ZERO_G;
-    int dt;
-    float schur;
-    const int k = rec_kind(r), q = rec_query(r);
-    if (k == 0) {
-        project_vt_st(q, x[0], x[1], x[2], x[3], c.m_inv[q], c.dHat, c.compliance, c.dx, c.nc, bad, g, &dt, &schur);
-    } else if (k == 1) {
-        const int vv[4] = {q, r.y, r.z, r.w};
-        project_vt_dy(vv, x, c.fixed, c.m_inv, c.dHat, c.dx, c.nc, bad, g, &dt, &schur);
-    } else {
-        const int vv[4] = {-1, r.y, r.z, r.w};
-        project_tv_st(vv, x, c.fixed, c.m_inv, c.dHat, c.compliance, c.dx, c.nc, bad, g, &dt, &schur);
-    }
-}
-
-__device__ __forceinline__ bool flag_bit(const unsigned* __restrict__ f, int v) {
-    return (__ldg(f + (v >> 5)) >> (v & 31)) & 1u;
-}
-// a dynamic vertex of the record moved by beta or more (static ones never move)
-__device__ __forceinline__ bool rec_moved(const unsigned* __restrict__ f, int4 r) {
-    const int k = rec_kind(r);
-    const bool q = k != 2 && flag_bit(f, rec_query(r));
-    const bool t = k != 0 && (flag_bit(f, r.y) || flag_bit(f, r.z) || flag_bit(f, r.w));
-    return q || t;
-}
-
-// classifiable() keeps holding after each vertex moves by less than beta.
-// With lo / hi the smallest / largest squared edge length, M = sqrt(hi) and
-// n the (doubled-area) normal: if every edge is at least 4 beta long and
-// |n| >= 8 beta M + 8 beta^2, a move of the vertices by under beta changes
-// each edge by under 2 beta (so lo' >= lo / 4, hi' <= 2.25 hi) and n by under
-// 4 beta M + 4 beta^2 (so nn / 4 <= nn' <= 2.25 nn); then nn' lo'^2 >=
-// nn lo^2 / 64 and nn' hi'^2 <= 11.4 nn hi^2, and the thresholds below keep
-// both inside classifiable()'s 1e-30 .. 1e30.  Every test has a margin of at
-// least 1 %, far above the float rounding of its operands.
-__device__ __forceinline__ bool robust_classifiable(V3 a, V3 b, V3 c, float beta) {
-    const V3 e0 = sub(b, a), e1 = sub(c, b), e2 = sub(a, c);
-    const V3 n = cross(e0, sub(c, a));
-    const float nn = dot(n, n);
-    const float l0 = dot(e0, e0), l1 = dot(e1, e1), l2 = dot(e2, e2);
-    const float lo = fminf(fminf(l0, l1), l2), hi = fmaxf(fmaxf(l0, l1), l2);
-    const float nmin = 8.0f * beta * sqrtf(hi) + 8.0f * beta * beta;
-    return lo > 16.16f * beta * beta && nn > 1.01f * nmin * nmin && (nn * lo) * lo > 6.5e-29f &&
-           (nn * hi) * hi < 8.0e28f;
-}
-
-// The first projection of a substep, splitting the list.  Stage 1 (every
-// pair): box distance at the far radius on a robustly classifiable triangle
-// -> far; the rest go through stage 2: the separating-axis bound at the far
-// radius -> far, otherwise near, and a near pair goes on through this
-// iteration's regular cull (box and separating axis at cull_d2) to the
-// projection.  Appends are warp-aggregated: near records from the front,
-// far records from the back of split[0 .. P).
-template <int U, int MINB>
-__global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_split_kernel(int* meta, const int4* __restrict__ pairs,
-                                                                     int4* __restrict__ split, int max_split,
-                                                                     RecCtx rc, float cull_d2, float cull_far_d2,
-                                                                     float beta, int* status, const int* conv,
-                                                                     int iter) {
-    pdl_entry();
-    if (iteration_skipped(conv, iter)) return;
-    const int st_end = meta[0], dy_end = meta[1], P = meta[2];
-    if (P > max_split) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, SX_STATUS_CAND_OVERFLOW);
-        return;
-    }
-    const PairCtx c{pairs, rc.y4, rc.xs4, rc.fixed, rc.m_inv, rc.dHat, rc.compliance, rc.dx, rc.nc, st_end, dy_end};
-    __shared__ int box_stack[PP_BLOCK / 32][32 * U + 32];
-    __shared__ int sat_stack[PP_BLOCK / 32][64];
-    const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
-    int* s1 = box_stack[threadIdx.x >> 5];
-    int* s2 = sat_stack[threadIdx.x >> 5];
-    int n1 = 0, n2 = 0;  // warp-uniform
-    int bad = 0;
-    // warp-collective append of the lanes' records to the near / far parts
-    auto emit = [&](bool near_, bool far_, int4 rec) {
-        const unsigned mn = __ballot_sync(0xffffffffu, near_), mf = __ballot_sync(0xffffffffu, far_);
-        int bn = 0, bf = 0;
-        if (lane == 0) {
-            if (mn) bn = atomicAdd(meta + M_NEAR, __popc(mn));
-            if (mf) bf = atomicAdd(meta + M_FAR, __popc(mf));
-        }
-        bn = __shfl_sync(0xffffffffu, bn, 0);
-        bf = __shfl_sync(0xffffffffu, bf, 0);
-        if (near_) {
-            const int slot = bn + __popc(mn & below);
-            if (slot < P) split[slot] = rec;
-            else bad |= 2;
-        }
-        if (far_) {
-            const int slot = P - 1 - (bf + __popc(mf & below));
-            if (slot >= 0) split[slot] = rec;
-            else bad |= 2;
-        }
-    };
-    auto sat_stage = [&](int cnt) {
-        const int t = lane < cnt ? s1[n1 - cnt + lane] : -1;
-        bool near_ = false, far_ = false, keep = false;
-        int4 rec = make_int4(0, 0, 0, 0);
-        if (t >= 0) {
-            const int4 pr = pairs[t];
-            V3 x[4];
-            pair_points(c, t, pr, x);
-            rec = make_rec(pr, pos_kind(t, st_end, dy_end));
-            far_ = robust_classifiable(x[1], x[2], x[3], beta) && sat_far(x[0], x[1], x[2], x[3], cull_far_d2);
-            near_ = !far_;
-            keep = near_ && !box_far(x[0], x[1], x[2], x[3], cull_d2) && !sat_far(x[0], x[1], x[2], x[3], cull_d2);
-        }
-        n1 -= cnt;
-        emit(near_, far_, rec);
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (keep) s2[n2 + __popc(m & below)] = t;
-        n2 += __popc(m);
-        __syncwarp();
-        if (n2 >= 32) {
-            project_pair(c, s2[n2 - 32 + lane], &bad);
-            n2 -= 32;
-            __syncwarp();
-        }
-    };
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    for (int base = gw * 32 * U; base < P; base += nw * 32 * U) {
-        int4 pr[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int t = base + 32 * u + lane;
-            pr[u] = t < P ? pairs[t] : make_int4(0, 0, 0, 0);
-        }
-        V3 x[U][4];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int t = base + 32 * u + lane;
-            if (t < P) pair_points(c, t, pr[u], x[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int t = base + 32 * u + lane;
-            const bool valid = t < P;
-            const bool far_ = valid && box_d2(x[u][0], x[u][1], x[u][2], x[u][3]) > cull_far_d2 &&
-                              robust_classifiable(x[u][1], x[u][2], x[u][3], beta);
-            emit(false, far_, valid ? make_rec(pr[u], pos_kind(t, st_end, dy_end)) : make_int4(0, 0, 0, 0));
-            const bool keep = valid && !far_;
-            const unsigned m = __ballot_sync(0xffffffffu, keep);
-            if (keep) s1[n1 + __popc(m & below)] = t;
-            n1 += __popc(m);
-        }
-        __syncwarp();
-        while (n1 >= 32) sat_stage(32);
-    }
-    if (n1 > 0) sat_stage(n1);
-    if (lane < n2) project_pair(c, s2[lane], &bad);
-    if (bad & 1) atomicOr(status, SX_STATUS_FIXED_RANGE);
-    if (bad & 2) atomicOr(status, SX_STATUS_CAND_OVERFLOW);
-}
-
-// Vertex -> far-pair incidence, built once per substep after the split
-// (counting sort by vertex): a later iteration visits only the far pairs of
-// the vertices flagged as moved instead of testing every far pair's flags.
-// Arrays (split workspace): cnt[V] (zero between substeps), cur[V], count[V],
-// start[V] (block-local exclusive prefix), btot[nb] (block offsets), then the
-// incidence list inc[] of far-pair indices into split.
-struct IncWs {
-    int *cnt, *cur, *count, *start, *btot, *inc;
-    long long inc_cap;
-    size_t bytes;
-};
-constexpr int INC_BLOCK = 256;
-
-__device__ __forceinline__ int rec_dyn(int4 r, int k, int* v) {  // dynamic vertex k (0..3) of record r, or -1
-    const int kind = rec_kind(r);
-    const int id = k == 0 ? (kind == 2 ? -1 : rec_query(r)) : (kind == 0 ? -1 : (k == 1 ? r.y : k == 2 ? r.z : r.w));
-    *v = id;
-    return id;
-}
-
-__global__ void inc_count_kernel(const int* __restrict__ meta, const int4* __restrict__ split, int max_split,
-                                 int* cnt) {
-    pdl_entry();
-    const int P = min(meta[2], max_split), NN = meta[M_NEAR];
-    for (int t = NN + blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
-        const int4 r = split[t];
-        for (int k = 0; k < 4; ++k) {
-            int v;
-            if (rec_dyn(r, k, &v) >= 0) atomicAdd(cnt + v, 1);
-        }
-    }
-}
-
-// count -> block-local exclusive prefix; clears cnt for the next substep and
-// the fill cursors
-__global__ void __launch_bounds__(INC_BLOCK) inc_block_scan_kernel(int V, int* cnt, int* cur, int* count, int* start,
-                                                                   int* btot, int* motion_count) {
-    pdl_entry();
-    if (blockIdx.x == 0 && threadIdx.x < 2) motion_count[threadIdx.x] = 0;  // flagged lists of the iterations to come
-    __shared__ int warp_tot[INC_BLOCK / 32];
-    const int v = blockIdx.x * INC_BLOCK + threadIdx.x;
-    const int c = v < V ? cnt[v] : 0;
-    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-    int incl = c;
-    for (int o = 1; o < 32; o <<= 1) {
-        const int t = __shfl_up_sync(0xffffffffu, incl, o);
-        if (lane >= o) incl += t;
-    }
-    if (lane == 31) warp_tot[w] = incl;
-    __syncthreads();
-    int base = 0, tot = 0;
-    for (int k = 0; k < INC_BLOCK / 32; ++k) {
-        if (k < w) base += warp_tot[k];
-        tot += warp_tot[k];
-    }
-    if (v < V) {
-        count[v] = c;
-        start[v] = base + incl - c;
-        cnt[v] = 0;
-        cur[v] = 0;
-    }
-    if (threadIdx.x == 0) btot[blockIdx.x] = tot;
-}
-
-__global__ void inc_fill_kernel(const int* __restrict__ meta, const int4* __restrict__ split, int max_split,
-                                int* cur, const int* __restrict__ start, const int* __restrict__ btot, int* inc,
-                                long long inc_cap, int* status) {
-    pdl_entry();
-    const int P = min(meta[2], max_split), NN = meta[M_NEAR];
-    for (int t = NN + blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x) {
-        const int4 r = split[t];
-        for (int k = 0; k < 4; ++k) {
-            int v;
-            if (rec_dyn(r, k, &v) < 0) continue;
-            const long long slot = (long long)start[v] + btot[v / INC_BLOCK] + atomicAdd(cur + v, 1);
-            if (slot < inc_cap) inc[slot] = t;
-            else atomicOr(status, SX_STATUS_CAND_OVERFLOW);
-        }
-    }
-}
-
-// the record's smallest flagged dynamic vertex (INT_MAX if none)
-__device__ __forceinline__ int lowest_flagged(const unsigned* __restrict__ f, int4 r) {
-    int lo = 0x7fffffff;
-    for (int k = 0; k < 4; ++k) {
-        int v;
-        if (rec_dyn(r, k, &v) >= 0 && flag_bit(f, v) && v < lo) lo = v;
-    }
-    return lo;
-}
-
-// A later projection of the substep over the split list: near pairs through
-// the regular two-stage cull; far pairs only when a dynamic vertex of theirs
-// is flagged as moved, found through the flagged vertices' incidence lists
-// (a pair met from several flagged vertices is taken from the smallest), then
-// the same cull.  Stacks per warp: s0 flagged far pairs awaiting the box
-// test, s1 box survivors awaiting the separating-axis test, s2 pairs to
-// project.
-template <int U, int MINB>
-__global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_moved_kernel(
-    const int* __restrict__ meta, const int4* __restrict__ split, const unsigned* __restrict__ motion, int n_dy,
-    const int* __restrict__ count, const int* __restrict__ start, const int* __restrict__ btot,
-    const int* __restrict__ inc, RecCtx rc, float cull_d2, int* status, const int* conv, int iter) {
-    pdl_entry();
-    if (iteration_skipped(conv, iter)) return;
-    const int NN = min(meta[M_NEAR], meta[2]);
-    __shared__ int far_stack[PP_BLOCK / 32][64];
-    __shared__ int box_stack[PP_BLOCK / 32][32 * U + 32];
-    __shared__ int sat_stack[PP_BLOCK / 32][64];
-    const int lane = threadIdx.x & 31;
-    const unsigned below = (1u << lane) - 1u;
-    int* s0 = far_stack[threadIdx.x >> 5];
-    int* s1 = box_stack[threadIdx.x >> 5];
-    int* s2 = sat_stack[threadIdx.x >> 5];
-    int n0 = 0, n1 = 0, n2 = 0;  // warp-uniform
-    int bad = 0;
-    auto sat_stage = [&](int cnt) {
-        const int t = lane < cnt ? s1[n1 - cnt + lane] : -1;
-        bool keep = false;
-        if (t >= 0) {
-            V3 x[4];
-            rec_points(rc, split[t], x);
-            keep = !sat_far(x[0], x[1], x[2], x[3], cull_d2);
-        }
-        n1 -= cnt;
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (keep) s2[n2 + __popc(m & below)] = t;
-        n2 += __popc(m);
-        __syncwarp();
-        if (n2 >= 32) {
-            project_rec(rc, split[s2[n2 - 32 + lane]], &bad);
-            n2 -= 32;
-            __syncwarp();
-        }
-    };
-    auto box_stage = [&](int cnt) {
-        const int t = lane < cnt ? s0[n0 - cnt + lane] : -1;
-        bool keep = false;
-        if (t >= 0) {
-            V3 x[4];
-            rec_points(rc, split[t], x);
-            keep = !box_far(x[0], x[1], x[2], x[3], cull_d2);
-        }
-        n0 -= cnt;
-        const unsigned m = __ballot_sync(0xffffffffu, keep);
-        if (keep) s1[n1 + __popc(m & below)] = t;
-        n1 += __popc(m);
-        __syncwarp();
-        while (n1 >= 32) sat_stage(32);
-    };
-    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
-    for (int base = gw * 32 * U; base < NN; base += nw * 32 * U) {
-        int4 r[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int t = base + 32 * u + lane;
-            r[u] = t < NN ? split[t] : make_int4(0, 0, 0, 0);
-        }
-        V3 x[U][4];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int t = base + 32 * u + lane;
-            if (t < NN) rec_points(rc, r[u], x[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const int t = base + 32 * u + lane;
-            const bool keep = t < NN && !box_far(x[u][0], x[u][1], x[u][2], x[u][3], cull_d2);
-            const unsigned m = __ballot_sync(0xffffffffu, keep);
-            if (keep) s1[n1 + __popc(m & below)] = t;
-            n1 += __popc(m);
-        }
-        __syncwarp();
-        while (n1 >= 32) sat_stage(32);
-    }
-    // the vertices flagged in this iteration, one per warp
-    const MotionBuf mb = motion_buf(const_cast<unsigned*>(motion), n_dy);
-    const unsigned* mflags = mb.flags;
-    const int nflag = mb.count[iter & 1];
-    for (int h = gw; h < nflag; h += nw) {
-        const int v = mb.list[h];
-        const int s = start[v] + btot[v / INC_BLOCK], n = count[v];
-        for (int b = 0; b < n; b += 32) {
-            const int t = b + lane < n ? inc[s + b + lane] : -1;
-            const bool take = t >= 0 && lowest_flagged(mflags, split[t]) == v;
-            const unsigned m = __ballot_sync(0xffffffffu, take);
-            if (take) s0[n0 + __popc(m & below)] = t;
-            n0 += __popc(m);
-            __syncwarp();
-            if (n0 >= 32) box_stage(32);
-        }
-    }
-    if (n0 > 0) box_stage(n0);
-    while (n1 >= 32) sat_stage(32);
-    if (n1 > 0) sat_stage(n1);
-    if (lane < n2) project_rec(rc, split[s2[lane]], &bad);
     if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
 }
 
@@ -1853,127 +1441,6 @@ extern "C" int sx_contact_apply(int n_dy, float* y4, const float* fixed, long lo
     launch(collision_apply_kernel, conv ? capped_grid(collision_apply_kernel, n_dy, 256) : grid_for(n_dy, 256), 256, 0,
            as_stream(stream), n_dy, (float4*)y4, fixed, dx_fix, nc, conv, iter);
     return check_launch("collision_apply_kernel");
-}
-
-// The split kernels in the launch configurations of kPairsProjectVariants
-// (the same index means the same configuration).
-struct PairsSplitVariant {
-    decltype(&pairs_split_kernel<1, 4>) split;
-    decltype(&pairs_project_moved_kernel<1, 4>) moved;
-};
-static const PairsSplitVariant kPairsSplitVariants[] = {
-    {pairs_split_kernel<2, 3>, pairs_project_moved_kernel<2, 3>},
-    {pairs_split_kernel<1, 4>, pairs_project_moved_kernel<1, 4>},
-    {pairs_split_kernel<2, 3>, pairs_project_moved_kernel<2, 3>},
-    {pairs_split_kernel<4, 2>, pairs_project_moved_kernel<4, 2>},
-};
-static_assert(sizeof(kPairsSplitVariants) / sizeof(kPairsSplitVariants[0]) == kNumPairsProjectVariants,
-              "one split configuration per projection configuration");
-
-// squared far radius (sqrt(cull_d2) + 2 beta)^2, rounded up with a 1e-5
-// relative margin (the box and separating-axis tests compare float values
-// with it)
-static float far_radius_d2(float cull_d2, float beta) {
-    const double r = (std::sqrt((double)cull_d2) + 2.0 * (double)beta) * (1.0 + 1e-5);
-    return std::nextafter((float)(r * r), INFINITY);
-}
-
-static IncWs inc_ws(void* ws, int n_dy, long long max_split) {
-    IncWs w;
-    char* p = (char*)ws;
-    char* p0 = p;
-    const size_t vb = a256((size_t)(n_dy > 0 ? n_dy : 1) * 4);
-    w.cnt = (int*)p; p += vb;
-    w.cur = (int*)p; p += vb;
-    w.count = (int*)p; p += vb;
-    w.start = (int*)p; p += vb;
-    w.btot = (int*)p; p += a256((size_t)((n_dy + INC_BLOCK - 1) / INC_BLOCK + 1) * 4);
-    w.inc = (int*)p;
-    w.inc_cap = 4 * (max_split > 0 ? max_split : 1);
-    p += a256((size_t)w.inc_cap * 4);
-    w.bytes = (size_t)(p - p0);
-    return w;
-}
-
-extern "C" size_t sx_contact_split_workspace_bytes(int n_dy, long long max_split) {
-    return inc_ws(nullptr, n_dy, max_split).bytes;
-}
-
-extern "C" int sx_contact_pairs_split(int n_dy, int n_st, const int* pairs, void* ws, int* split,
-                                      long long max_split, void* split_ws, size_t split_ws_bytes, unsigned* motion,
-                                      const float* y4,
-                                      const float* xs4, const float* fixed, const float* m_inv, float dHat,
-                                      float compliance, float cull_d2, float motion_budget, long long* dx_fix,
-                                      int* nc, int* status, const int* conv, int iter, int variant, void* stream) {
-    SX_REQUIRE(variant >= 0 && variant < kNumPairsProjectVariants, "sx_contact_pairs_split: bad variant");
-    SX_REQUIRE(n_dy >= 0 && n_st >= 0 && max_split >= 0, "sx_contact_pairs_split: bad sizes");
-    SX_REQUIRE(cull_d2 > 0.0f && motion_budget > 0.0f, "sx_contact_pairs_split: needs cull_d2 > 0 and a positive "
-                                                       "motion budget");
-    if (n_dy == 0) return SX_OK;
-    SX_REQUIRE(pairs && ws && split && split_ws && motion && y4 && fixed && m_inv && dx_fix && nc && status,
-               "sx_contact_pairs_split: null pointer");
-    SX_REQUIRE(split_ws_bytes >= sx_contact_split_workspace_bytes(n_dy, max_split),
-               "sx_contact_pairs_split: split workspace too small");
-    SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_split: null static positions");
-    SX_REQUIRE((const void*)pairs != (const void*)split, "sx_contact_pairs_split: split must not alias pairs");
-    cudaStream_t st = as_stream(stream);
-    PairsWs w = pairs_ws(ws, n_dy, n_st);
-    IncWs iw = inc_ws(split_ws, n_dy, max_split);
-    const PairsProjectVariant& pv = kPairsProjectVariants[variant];
-    const RecCtx rc{(const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, dx_fix, nc};
-    const int ms = max_split > 0x7fffffffLL ? 0x7fffffff : (int)max_split;
-    launch(kPairsSplitVariants[variant].split, sm_count() * pv.blocks_per_sm, PP_BLOCK, 0, st, w.meta,
-           (const int4*)pairs, (int4*)split, ms, rc, cull_d2, far_radius_d2(cull_d2, motion_budget), motion_budget,
-           status, conv, iter);
-    int rc_ = check_launch("pairs_split_kernel");
-    if (rc_) return rc_;
-    // vertex -> far-pair incidence for the later iterations
-    const int nb = (n_dy + INC_BLOCK - 1) / INC_BLOCK;
-    const int gf = sm_count() * 8;
-    launch(inc_count_kernel, gf, 256, 0, st, (const int*)w.meta, (const int4*)split, ms, iw.cnt);
-    launch(inc_block_scan_kernel, nb, INC_BLOCK, 0, st, n_dy, iw.cnt, iw.cur, iw.count, iw.start, iw.btot,
-           motion_buf(motion, n_dy).count);
-    launch(pairs_scan_kernel, 1, 1024, 0, st, nb, iw.btot);
-    launch(inc_fill_kernel, gf, 256, 0, st, (const int*)w.meta, (const int4*)split, ms, iw.cur, (const int*)iw.start,
-           (const int*)iw.btot, iw.inc, iw.inc_cap, status);
-    return check_launch("sx_contact_pairs_split incidence");
-}
-
-extern "C" int sx_contact_pairs_project_moved(int n_dy, int n_st, const int* split, const void* ws,
-                                              const void* split_ws, long long max_split,
-                                              const unsigned* motion, const float* y4, const float* xs4,
-                                              const float* fixed, const float* m_inv, float dHat, float compliance,
-                                              float cull_d2, long long* dx_fix, int* nc, int* status,
-                                              const int* conv, int iter, int variant, void* stream) {
-    SX_REQUIRE(variant >= 0 && variant < kNumPairsProjectVariants, "sx_contact_pairs_project_moved: bad variant");
-    SX_REQUIRE(n_dy >= 0 && n_st >= 0 && max_split >= 0, "sx_contact_pairs_project_moved: bad sizes");
-    SX_REQUIRE(cull_d2 > 0.0f, "sx_contact_pairs_project_moved: needs cull_d2 > 0");
-    if (n_dy == 0) return SX_OK;
-    SX_REQUIRE(split && ws && split_ws && motion && y4 && fixed && m_inv && dx_fix && nc && status,
-               "sx_contact_pairs_project_moved: null pointer");
-    SX_REQUIRE(n_st == 0 || xs4, "sx_contact_pairs_project_moved: null static positions");
-    PairsWs w = pairs_ws(const_cast<void*>(ws), n_dy, n_st);
-    IncWs iw = inc_ws(const_cast<void*>(split_ws), n_dy, max_split);
-    const PairsProjectVariant& pv = kPairsProjectVariants[variant];
-    const RecCtx rc{(const float4*)y4, (const float4*)xs4, fixed, m_inv, dHat, compliance, dx_fix, nc};
-    launch(kPairsSplitVariants[variant].moved, sm_count() * pv.blocks_per_sm, PP_BLOCK, 0, as_stream(stream),
-           (const int*)w.meta, (const int4*)split, motion, n_dy, (const int*)iw.count,
-           (const int*)iw.start, (const int*)iw.btot, (const int*)iw.inc, rc, cull_d2, status, conv, iter);
-    return check_launch("pairs_project_moved_kernel");
-}
-
-extern "C" int sx_contact_pairs_counts(const void* ws, int n_dy, int n_st, int* counts4, void* stream) {
-    SX_REQUIRE(ws && counts4 && n_dy >= 0 && n_st >= 0, "sx_contact_pairs_counts: bad argument");
-    PairsWs w = pairs_ws(const_cast<void*>(ws), n_dy, n_st);
-    int meta[6];
-    cudaStream_t s = as_stream(stream);
-    SX_CUDA(cudaMemcpyAsync(meta, w.meta, sizeof(meta), cudaMemcpyDeviceToHost, s));
-    SX_CUDA(cudaStreamSynchronize(s));
-    counts4[0] = meta[0];
-    counts4[1] = meta[1];
-    counts4[2] = meta[2];
-    counts4[3] = meta[M_NEAR];
-    return SX_OK;
 }
 
 extern "C" int sx_contact_pairs_sweep(int n_dy, int n_st, const int* pairs, const void* ws, float* y4,

@@ -48,14 +48,10 @@ Options beyond the reference (keyword-only, defaults reproduce the reference):
   before classifying its region.  The distance of every region is at least the
   box distance, so such a pair adds no correction; the skip only saves the
   classification.  Off, every pair is classified as the reference does.
-* ``contact_motion_budget`` (attribute, default 0.05; needs ``contact_cull``)
-  -- the first contact projection of a substep splits the pair list into near
-  pairs and far pairs that provably stay out of contact while none of their
-  vertices moves by ``budget = contact_motion_budget * sqrt(dHat * 1.0625)``;
-  the sweeps flag the vertices that move that far, and later iterations
-  re-test a far pair only when one of its vertices is flagged
-  (``sx_contact_pairs_split`` / ``sx_contact_pairs_project_moved``).  The
-  positions are identical with any budget; 0 tests every pair every iteration.
+* ``fast_math`` (attribute, default off) -- the sweep's fast arithmetic
+  (``sx_jacobi_sweep_mode``: fused multiply-adds, the hardware reciprocal
+  square root): within float rounding of the exact sweep, held to the
+  substep's position and residual tolerance instead of bit-equality.
 
 Reference quirks kept on purpose: the stretch springs use
 ``stiffness_bending * dt^2`` and the bending pairs ``stiffness_stretch * dt^2``
@@ -103,8 +99,6 @@ class Solver:
         # when collisions are on
         self.self_collision = True
         self.contact_cull = True
-        self.contact_motion_budget = 0.05
-        self._split = self._yref4 = self._mflags = None
         # the sweep's fast arithmetic (FMA, hardware reciprocal square root):
         # within float rounding of the exact sweep, held to the substep's
         # position and residual tolerance rather than bit-equality
@@ -195,54 +189,23 @@ class Solver:
         """init_variables + solve_spring_constraints_x + update_dx
         (XPBD.py:345-348, :141-184, :384-387); ping-pongs ``y``.  In tolerance
         mode the sweep of every check_every-th iteration measures the residual;
-        ``loop`` is the handle of a device-side loop whose body this is.  With
-        the contact-pair split the sweep of a substep's first iteration saves
-        its output as the reference positions and later sweeps flag the
-        vertices that moved by the motion budget."""
+        ``loop`` is the handle of a device-side loop whose body this is."""
         m = self.mesh_dy
         k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
         k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
-        track = self._split_active()
-        if track:
-            self._ensure_split()
-        yref = ptr(self._yref4) if track else None
-        mfl = ptr(self._mflags) if track and iteration > 0 else None
-        beta = self.motion_budget() if track else 0.0
+        fast = 1 if self.fast_math else 0
         if self.tol is None:
-            sx.sx_jacobi_sweep_tracked(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
-                                       ptr(m.adj), m.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0,
-                                       self.sweep_variant, 1 if self.fast_math else 0, yref, mfl, beta, iteration,
-                                       stream_handle())
+            sx.sx_jacobi_sweep_mode(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
+                                    ptr(m.adj), m.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0,
+                                    self.sweep_variant, fast, stream_handle())
         else:
             check = 1 if iteration > 0 and iteration % self.check_every == 0 else 0
-            sx.sx_jacobi_sweep_checked_tracked(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed),
-                                               ptr(m.adj_ptr), ptr(m.adj), m.num_verts, k_spring, k_bend, iteration,
-                                               check, float(self.tol),
-                                               ptr(self._res_ref) if self.tol_relative else None, ptr(self._conv),
-                                               ptr(self._res3), ptr(self._res_ws), self._res_ws.numel(), loop,
-                                               self.n_iter, 1 if self.fast_math else 0, yref, mfl, beta,
-                                               stream_handle())
+            sx.sx_jacobi_sweep_checked_mode(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
+                                            ptr(m.adj), m.num_verts, k_spring, k_bend, iteration, check,
+                                            float(self.tol), ptr(self._res_ref) if self.tol_relative else None,
+                                            ptr(self._conv), ptr(self._res3), ptr(self._res_ws), self._res_ws.numel(),
+                                            loop, self.n_iter, fast, stream_handle())
         self._swap_y()
-
-    def _split_active(self) -> bool:
-        return bool(self.enable_collision_handling and not self.record_pairs and self.contact_cull
-                    and self.contact_motion_budget and self.contact_motion_budget > 0)
-
-    def motion_budget(self) -> float:
-        """Absolute motion budget of the contact-pair split (world units)."""
-        return float(self.contact_motion_budget) * float(np.sqrt(self.contact_cull_d2()))
-
-    def _ensure_split(self):
-        """Buffers of the contact-pair split: the split list (as large as the
-        pair list), reference positions and one motion bit per vertex."""
-        if self._split is None:
-            Vd = self.mesh_dy.num_verts
-            self._split = torch.empty_like(self._pairs)
-            self._split_ws = torch.zeros(int(sx.sx_contact_split_workspace_bytes(Vd, self._split.shape[0])),
-                                         dtype=torch.uint8, device=self.device)
-            self._yref4 = torch.zeros_like(self.mesh_dy.y4)
-            self._mflags = torch.zeros(int(sx.sx_motion_buffer_bytes(Vd)) // 4, dtype=torch.int32,
-                                       device=self.device)
 
     def _swap_y(self):
         m = self.mesh_dy
@@ -352,29 +315,6 @@ class Solver:
             self.solve_edge_edge_constraints_x(c, iteration, gated)
         if not self.record_pairs:
             conv = ptr(self._conv) if self.tol is not None and gated else None
-            if self._split_active():
-                self._ensure_split()
-                xs = ptr(s.x4) if s is not None else None
-                variant = 0 if self.pairs_variant is None else int(self.pairs_variant)
-                if iteration == 0:
-                    sx.sx_contact_pairs_split(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
-                                              ptr(self._pairs_ws), ptr(self._split), self._split.shape[0],
-                                              ptr(self._split_ws), self._split_ws.numel(), ptr(self._mflags),
-                                              ptr(m.y4),
-                                              xs, ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c),
-                                              self.contact_cull_d2(), self.motion_budget(), ptr(self._dx_fix),
-                                              ptr(self._nc), ptr(self.status), conv, iteration, variant,
-                                              stream_handle())
-                else:
-                    sx.sx_contact_pairs_project_moved(m.num_verts, s.num_verts if s is not None else 0,
-                                                      ptr(self._split), ptr(self._pairs_ws), ptr(self._split_ws),
-                                                      self._split.shape[0], ptr(self._mflags),
-                                                      ptr(m.y4), xs, ptr(m.fixed), ptr(m.m_inv), self.dHat, float(c),
-                                                      self.contact_cull_d2(), ptr(self._dx_fix), ptr(self._nc),
-                                                      ptr(self.status), conv, iteration, variant, stream_handle())
-                sx.sx_contact_apply(m.num_verts, ptr(m.y4), ptr(m.fixed), ptr(self._dx_fix), ptr(self._nc), conv,
-                                    iteration, stream_handle())
-                return
             if self.pairs_variant is None:
                 sx.sx_contact_pairs_sweep(m.num_verts, s.num_verts if s is not None else 0, ptr(self._pairs),
                                           ptr(self._pairs_ws), ptr(m.y4), ptr(s.x4) if s is not None else None,
@@ -507,8 +447,6 @@ class Solver:
         replayed on later calls; results are identical to the eager path."""
         if self.enable_edge_edge and self.enable_collision_handling:
             self._ensure_ee()  # allocated outside any capture
-        if self._split_active():
-            self._ensure_split()
         if not self.use_graph:
             self._forward_eager(n_substeps)
             return
@@ -570,8 +508,8 @@ class Solver:
     def _graph_key(self, n_substeps):
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
-                self.compliance_collision, self.self_collision, self.contact_cull, self.contact_motion_budget,
-                self.fast_math, self.sweep_variant,
+                self.compliance_collision, self.self_collision, self.contact_cull, self.fast_math,
+                self.sweep_variant,
                 self.pairs_variant, self.enable_edge_edge,
                 self.enable_velocity_update, self.mu, self.tol,
                 self.tol_relative,
@@ -622,15 +560,6 @@ class Solver:
         the last 256 bytes of the pair-list workspace, {end of vertex-vs-static
         pairs, end of vertex-vs-cloth pairs, total}."""
         return int(self._pairs_ws[-256:].view(torch.int32)[2].item())
-
-    def contact_pair_counts(self) -> dict:
-        """Pair counts of the last pair list (host sync): the total and, after
-        a split, how many pairs are near."""
-        c = (C.c_int * 4)()
-        sx.sx_contact_pairs_counts(ptr(self._pairs_ws), self.mesh_dy.num_verts,
-                                   self.mesh_st.num_verts if self.mesh_st is not None else 0, C.addressof(c),
-                                   stream_handle())
-        return {"vt_st": c[0], "vt_dy": c[1] - c[0], "tv_st": c[2] - c[1], "total": c[2], "near": c[3]}
 
     def status_flags(self) -> int:
         """Accumulated device status bits (host sync)."""

@@ -161,3 +161,66 @@ def test_batched512_sampled_instances(pkg, po):
         touched += int((orc.x4[:, 2] > 1.0 - 0.5 * 9.81 * (frames / 60) ** 2 + 0.01).sum() > 0)
     assert touched >= 1
     assert int(sim.status.item()) & 4 == 0
+
+
+def _check_tol(po, got4, orc_x4, adj_ptr, adj, diag, what):
+    """The tolerance criteria alone (for the fast arithmetic, which is not
+    bit-identical): max |dx| <= 1e-4 x diagonal, residual within 1 %."""
+    got, ref = got4[:, :3], orc_x4[:, :3]
+    assert np.isfinite(got).all(), what
+    dmax = float(np.abs(got.astype(np.float64) - ref).max())
+    assert dmax <= POS_TOL * diag, f"{what}: max |dx| {dmax:.3e} > {POS_TOL} x diagonal {diag:.4f}"
+    r_got = po.residual(np.ascontiguousarray(got4), adj_ptr, adj)
+    r_ref = po.residual(np.ascontiguousarray(orc_x4), adj_ptr, adj)
+    rms_got, rms_ref = np.sqrt(r_got[0] / r_got[1]), np.sqrt(r_ref[0] / r_ref[1])
+    assert abs(rms_got - rms_ref) <= RES_TOL * rms_ref, f"{what}: residual {rms_got:.6e} vs {rms_ref:.6e}"
+    return dmax
+
+
+def test_fast_math_within_tolerance(pkg, po):
+    """The sweep's fast arithmetic (fused multiply-adds, hardware reciprocal
+    square root; not bit-identical) against the exact oracle: the 64 x 64 box
+    scene for 60 frames and four batched instances for 10 frames stay within
+    1e-4 x the bounding-box diagonal with the residual within 1 %, and differ
+    from the exact run (the fast kernels ran)."""
+    from starlab_physics_gb300 import mesh as M
+
+    scene = pkg.scenes.plain64()
+    sim = pkg.scenes.make_solver(scene, device="cuda")
+    sim.bending_on = "y"
+    sim.use_graph = True
+    sim.fast_math = True
+    orc = _oracle_for(pkg, po, scene, sim)
+    for _ in range(60):
+        sim.forward(scene.n_substeps)
+        orc.forward(scene.n_substeps)
+    torch.cuda.synchronize()
+    got = _np(sim.mesh_dy.x4)
+    d = _check_tol(po, got, orc.x4, orc.adj_ptr, orc.adj, sim.mesh_dy.bbox_diagonal(), "plain64 fast")
+    assert d > 0.0
+    insts = pkg.batched_scene(512, seed=0)
+    kw = dict(dt=1 / 60, g=(0.0, 0.0, -9.81), k_stretch_stiffness=1e5, k_bend_stiffness=1e8, dHat=(4e-3) ** 2,
+              damping=0.001, padding=8e-3, n_iter=20, cap=40)
+    bs = pkg.BatchedSolver(insts, dHat=kw["dHat"], stiffness_stretch=1e5, stiffness_bending=1e8, g=kw["g"],
+                           dt=kw["dt"], n_iter=20, padding=8e-3)
+    bs.use_graph = True
+    bs.fast_math = True
+    for _ in range(10):
+        bs.forward(10)
+    torch.cuda.synchronize()
+    sides = np.array([int(round(np.sqrt(i.x.shape[0]))) for i in insts])
+    box_top = np.array([float(i.obstacle_x[:, 2].max()) for i in insts])
+    for i in (int(np.argmin(sides)), int(np.argmax(sides)), int(np.argmax(box_top)), 100):
+        inst = insts[i]
+        cl = M.TriMesh(inst.x, inst.faces, device="cpu")
+        cl.fixed[np.asarray(inst.pinned)] = 0.0
+        ob = M.TriMesh(inst.obstacle_x, inst.obstacle_faces, device="cpu")
+        o = po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob), collisions=True,
+                            rebuild="substep", self_collision=False, bending_on="y", nthreads=NTHREADS, **kw)
+        for _ in range(10):
+            o.forward(10)
+        g4 = np.zeros_like(o.x4)
+        g4[:, :3] = _np(bs.instance_positions(i))
+        g4[:, 3] = o.x4[:, 3]
+        p = inst.x.astype(np.float64)
+        _check_tol(po, g4, o.x4, o.adj_ptr, o.adj, float(np.linalg.norm(p.max(0) - p.min(0))), f"instance {i} fast")

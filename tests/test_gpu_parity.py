@@ -671,37 +671,3 @@ def test_programmatic_launch_gives_the_same_frames(pkg, sxm, use_graph):
     finally:
         lib.sx_set_programmatic_launch(prev)
     assert np.array_equal(res[0][0], res[1][0]) and np.array_equal(res[0][1], res[1][1])
-
-
-def test_contact_split_equals_full_list(pkg):
-    """The contact-pair split (far pairs re-tested only after their vertices
-    move by the budget) gives the same frames as projecting every pair in
-    every iteration, bit for bit: budgets 0.02 / 0.05 / 0.5 of the cull
-    distance, every launch configuration, eager and graph."""
-    def run(budget, variant=None, use_graph=True):
-        scene = pkg.scenes.drape256(n=64, sphere_subdiv=3)
-        scene.n_iter = 8
-        sim = pkg.scenes.make_solver(scene, device=DEV)
-        sim.bending_on = "y"
-        sim.use_graph = use_graph
-        sim.contact_motion_budget = budget
-        sim.pairs_variant = variant
-        for _ in range(4):
-            sim.forward(scene.n_substeps)
-        torch.cuda.synchronize()
-        return sim
-
-    ref = run(0.0)
-    x_ref = _np(ref.mesh_dy.x4)
-    assert ref.status_flags() & 4 == 0
-    from starlab_physics_gb300._lib import sx
-
-    runs = [(b, None, True) for b in (0.02, 0.05, 0.5)] + [(0.05, v, True) for v in
-                                                            range(sx.sx_contact_pairs_project_variants())]
-    runs.append((0.05, None, False))
-    for b, v, g in runs:
-        sim = run(b, v, g)
-        assert np.array_equal(_np(sim.mesh_dy.x4), x_ref), (b, v, g)
-        assert sim.status_flags() == ref.status_flags()
-    c = sim.contact_pair_counts()
-    assert 0 < c["near"] < c["total"] // 4, c
