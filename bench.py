@@ -27,6 +27,7 @@ replicas' work divided by the slowest rank's time.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import os
 import subprocess
@@ -376,32 +377,53 @@ def batched512(pkg, steps=5, warmup=2):
 
     exact_sweep = sweep_roofline(False)
     status = int(sim.status.item())
+
+    def timed_frames():
+        sim.x4.copy_(x0)
+        sim.v4.copy_(v0)
+        sim.forward(S)  # capture
+        tot_ = 0.0
+        for _ in range(steps):
+            sim.x4.copy_(x0)
+            sim.v4.copy_(v0)
+            flush.zero_()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            sim.forward(S)
+            b.record(stream)
+            torch.cuda.synchronize()
+            tot_ += a.elapsed_time(b)
+        return {"value": V * S * steps / (tot_ / 1e3), "unit": UNIT, "ms_per_step": tot_ / steps}
+
     # the same frames with the sweep's fast arithmetic (tolerance-validated,
     # not bit-identical)
     sim.fast_math = True
+    fast = timed_frames() | {"sweep_roofline": sweep_roofline(True)}
+    # one persistent launch per substep (an instance per CTA), exact and fast
+    sim.fast_math = False
+    sim.persistent = True
     sim.x4.copy_(x0)
     sim.v4.copy_(v0)
-    sim.forward(S)
-    tot_f = 0.0
-    for _ in range(steps):
-        sim.x4.copy_(x0)
-        sim.v4.copy_(v0)
-        flush.zero_()
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        sim.forward(S)
-        b.record(stream)
-        torch.cuda.synchronize()
-        tot_f += a.elapsed_time(b)
-    fast = {"value": V * S * steps / (tot_f / 1e3), "unit": UNIT, "ms_per_step": tot_f / steps,
-            "sweep_roofline": sweep_roofline(True)}
+    pv, ptimes = sim.autotune_persistent()
+    from starlab_physics_gb300._lib import load as _load
+
+    blk, bps = C.c_int(0), C.c_int(0)
+    _load().sx_batched_substep_variant_info(pv, C.addressof(blk), C.addressof(bps))
+    persistent = timed_frames() | {"launch": {"threads_per_cta": blk.value, "ctas_per_sm": bps.value,
+                                              "picked_by": "autotuner (fastest of %d identical variants, one "
+                                                           "substep each)" % len(ptimes)}}
+    sim.fast_math = True
+    persistent_fast = timed_frames()
     sim.fast_math = False
+    sim.persistent = False
     return {"workload": f"512 cloths, {V} vertices, {sim.num_faces} faces, 10 substeps x 20 iterations, "
                         "obstacle contacts", "value": V * S * steps / (tot / 1e3), "unit": UNIT,
             "ms_per_step": tot / steps, "steps": steps, "warmup": warmup,
             "sweep_variant": sim.sweep_variant,
             "sweep_roofline": exact_sweep,
             "fast_math": fast,
+            "persistent": persistent,
+            "persistent_fast_math": persistent_fast,
             "status_flags": status}
 
 

@@ -378,6 +378,45 @@ int sx_edge_edge_sweep(int n_edges_dy, const int* edges_dy, const int* edges_st,
  * (edge 0), x2, x3 (edge 1): dtype[n], d[n], g12[12 n]. */
 int sx_edge_edge_classify(int n, const float* p12, float dHat, int* dtype, float* d, float* g12, void* stream);
 
+/* Persistent batched substep (no counterpart in the reference, whose batching
+ * is mesh concatenation, framework/meshio/concat.py:11-58): one launch runs a
+ * whole substep of every instance of a batch.  Each CTA takes instances from
+ * a queue in the order `order` (largest first), and for its instance alone
+ * computes the cloth box (sx_segment_aabbs) and padded face boxes on x, with
+ * predict != 0 the prediction y = compute_y(x, v) (sx_predict; 0: y already
+ * holds the start, e.g. a learned warm start), n_iter Jacobi iterations --
+ * the sweep with bending on y (sx_jacobi_sweep_v / sx_jacobi_sweep_mode with
+ * `fast`), in the first iteration the obstacle broad phase
+ * (sx_batched_obstacle_broadphase), then the obstacle contacts and update_dx
+ * (sx_batched_obstacle_contacts) -- and the velocity update
+ * (sx_velocity_update), with block barriers between the phases.  y and
+ * y_other ping-pong: after an even n_iter the final positions are in y, after
+ * an odd one in y_other.  The result equals those grid-wide launches bit for
+ * bit.  Chunk boxes are per instance: cmin4 / cmax4 hold cptr[n_inst] boxes,
+ * instance i's chunks of 32 faces at cptr[i] .. cptr[i+1].  queue: two ints,
+ * zero before the first launch and left zero by every launch.  Fixed
+ * iteration counts only (iterating to a residual uses the grid-wide
+ * launches). */
+typedef struct SxBatchedSubstep {
+    int n_inst, n_iter, predict, cap;
+    const int *order, *vptr, *fptr, *cptr, *optr, *ob_fptr;
+    float *x4, *y4, *y_other4, *v4;
+    const float *fixed, *m_inv;
+    const int *adj_ptr, *adj;
+    const int *faces, *ob_faces;
+    const float* xs4;
+    float *fmin4, *fmax4, *cmin4, *cmax4, *cl_box6;
+    const float *ob_box6, *ob_fmin4, *ob_fmax4;
+    unsigned* vmask;
+    int *tv_cand, *tv_num;
+    long long* dx_fix;
+    int *nc, *status, *queue;
+    float padding, dt, gx, gy, gz, k_spring, k_bend, dHat, compliance, damping;
+} SxBatchedSubstep;
+int sx_batched_substep_variants(void);
+int sx_batched_substep_variant_info(int variant, int* block, int* blocks_per_sm);
+int sx_batched_substep(const SxBatchedSubstep* args, int variant, int fast, void* stream);
+
 /* solve_constraints_v (XPBD.py:374-381, :398-404; collision_constraints_v.py
  * __vt_st :6-133, __tv_st :137-330, __vt_dy :334-570): velocity-level contact
  * and friction over the pair records of the last sx_collision_sweep (pair,

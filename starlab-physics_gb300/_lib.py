@@ -29,6 +29,18 @@ STATUS_STACK_OVERFLOW = 2
 STATUS_FIXED_RANGE = 4
 STATUS_CLIMB_LIMIT = 8
 
+class SxBatchedSubstep(C.Structure):
+    """The argument block of sx_batched_substep (include/starxpbd.h)."""
+
+    _fields_ = [(n, I) for n in ("n_inst", "n_iter", "predict", "cap")] + \
+               [(n, P) for n in ("order", "vptr", "fptr", "cptr", "optr", "ob_fptr", "x4", "y4", "y_other4", "v4",
+                                 "fixed", "m_inv", "adj_ptr", "adj", "faces", "ob_faces", "xs4", "fmin4", "fmax4",
+                                 "cmin4", "cmax4", "cl_box6", "ob_box6", "ob_fmin4", "ob_fmax4", "vmask", "tv_cand",
+                                 "tv_num", "dx_fix", "nc", "status", "queue")] + \
+               [(n, F) for n in ("padding", "dt", "gx", "gy", "gz", "k_spring", "k_bend", "dHat", "compliance",
+                                 "damping")]
+
+
 # name -> (argtypes, restype)
 SIGNATURES = {
     "sx_version": ([], I),
@@ -79,6 +91,9 @@ SIGNATURES = {
     "sx_contact_pairs_project_variant_info": ([I, P, P], I),
     "sx_contact_pairs_project_v": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, I, P], I),
     "sx_contact_apply": ([I, P, P, P, P, P, I, P], I),
+    "sx_batched_substep_variants": ([], I),
+    "sx_batched_substep_variant_info": ([I, P, P], I),
+    "sx_batched_substep": ([P, I, I, P], I),
     "sx_edge_edge_sweep": ([I, P, P, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, I, P], I),
     "sx_edge_edge_classify": ([I, P, F, P, P, P, P], I),
     "sx_cell_bvh_traverse_edges": ([P, I, P, F, P, P, P, P, P, P, I, P, P, P, P], I),

@@ -170,6 +170,14 @@ class BatchedSolver:
         self.sweep_variant = 0
         # the sweep's fast arithmetic (Solver.fast_math)
         self.fast_math = False
+        # one persistent launch per substep (sx_batched_substep) instead of a
+        # graph of grid-wide launches; fixed iteration counts only (iterating
+        # to a residual keeps the grid-wide form).  persistent_variant: its
+        # launch configuration (autotune_persistent() picks one)
+        self.persistent = False
+        self.persistent_variant = 0
+        self._pargs = None
+        self._vsizes = np.diff(self.vptr_np)
         # iterate to a residual (Solver.tol): n_iter is then the cap
         self.tol = None
         self.tol_relative = False
@@ -190,7 +198,64 @@ class BatchedSolver:
     def _swap_y(self):
         self.y4, self._y_other = self._y_other, self.y4
 
+    def _persistent_buffers(self):
+        """Instance order (largest first), per-instance chunk offsets, their
+        chunk boxes and the work queue of the persistent substep."""
+        if self._pargs is None:
+            dev = self.device
+            t = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)  # noqa: E731
+            nf = np.diff(self.fptr_np)
+            cptr = np.zeros(self.n_instances + 1, np.int32)
+            cptr[1:] = np.cumsum((nf + 31) // 32)
+            order = np.argsort(-self._vsizes, kind="stable").astype(np.int32)
+            self._p_order, self._p_cptr = t(order), t(cptr)
+            self._p_cmin4 = torch.zeros((max(int(cptr[-1]), 1), 4), dtype=torch.float32, device=dev)
+            self._p_cmax4 = torch.zeros_like(self._p_cmin4)
+            self._p_queue = torch.zeros(2, dtype=torch.int32, device=dev)
+            self._pargs = True
+
+    def _persistent_substep(self, dt, predict: bool):
+        """One substep as a single persistent launch (sx_batched_substep)."""
+        from ._lib import SxBatchedSubstep
+
+        self._persistent_buffers()
+        g = self.g
+        a = SxBatchedSubstep()
+        a.n_inst, a.n_iter, a.predict, a.cap = self.n_instances, self.n_iter, 1 if predict else 0, self.cap
+        for name, tns in (("order", self._p_order), ("vptr", self.vptr), ("fptr", self.fptr), ("cptr", self._p_cptr),
+                          ("optr", self.optr), ("ob_fptr", self.ob_fptr), ("x4", self.x4), ("y4", self.y4),
+                          ("y_other4", self._y_other), ("v4", self.v4), ("fixed", self.fixed), ("m_inv", self.m_inv),
+                          ("adj_ptr", self.adj_ptr), ("adj", self.adj), ("faces", self.faces),
+                          ("ob_faces", self.ob_faces), ("xs4", self.xs4), ("fmin4", self.fmin4),
+                          ("fmax4", self.fmax4), ("cmin4", self._p_cmin4), ("cmax4", self._p_cmax4),
+                          ("cl_box6", self.cl_box6), ("ob_box6", self.ob_box6), ("ob_fmin4", self.ob_fmin4),
+                          ("ob_fmax4", self.ob_fmax4), ("vmask", self.vmask), ("tv_cand", self.tv_cand),
+                          ("tv_num", self.tv_num), ("dx_fix", self._dx_fix), ("nc", self._nc),
+                          ("status", self.status), ("queue", self._p_queue)):
+            setattr(a, name, ptr(tns))
+        a.padding, a.dt, a.gx, a.gy, a.gz = self.padding, float(dt), g[0], g[1], g[2]
+        a.k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
+        a.k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
+        a.dHat, a.compliance, a.damping = self.dHat, self.compliance_collision, self.damping
+        sx.sx_batched_substep(C.addressof(a), int(self.persistent_variant), 1 if self.fast_math else 0,
+                              stream_handle())
+        if self.n_iter % 2:
+            self._swap_y()
+
     def substep(self, dt):
+        if self.persistent and self.tol is None:
+            if self.bending_on != "y":
+                raise ValueError("the persistent substep evaluates bending on y")
+            if self.warm is None:
+                self._persistent_substep(dt, predict=True)
+                return
+            g = self.g
+            sx.sx_predict(ptr(self.x4), ptr(self.v4), ptr(self.fixed), ptr(self.y4), self.num_verts, float(dt), g[0],
+                          g[1], g[2], stream_handle())
+            self.warm.begin(self, dt)
+            self._persistent_substep(dt, predict=False)
+            self.warm.end(self)
+            return
         s = stream_handle()
         # per-instance cloth grids and face boxes on x (the substep's BVH build)
         sx.sx_face_aabbs_chunked(ptr(self.x4), ptr(self.faces), self.num_faces, self.padding, ptr(self.fmin4),
@@ -291,7 +356,7 @@ class BatchedSolver:
             return
         key = (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                self.stiffness_bending, self.n_iter, self.bending_on, self.sweep_variant, self.fast_math, self.tol,
-               self.tol_relative,
+               self.tol_relative, self.persistent, self.persistent_variant,
                self.check_every,
                id(self.warm) if self.warm is not None else None,
                self.warm.mode if self.warm is not None else None, self.y4.data_ptr())
@@ -325,6 +390,38 @@ class BatchedSolver:
                                  1 if self.bending_on == "y" else 0)
         self.sweep_variant = best
         return best, times
+
+    def autotune_persistent(self, reps: int = 3):
+        """Time every launch configuration of the persistent substep on this
+        batch (from the current state, restored after each run) and keep the
+        fastest; identical results.  Returns (variant, times in ms)."""
+        if self._ob_built_for != self.padding:
+            self._static_obstacles()
+        n = int(sx.sx_batched_substep_variants())
+        x0, v0, y0 = self.x4.clone(), self.v4.clone(), self.y4.clone()
+        dt = self.dt / 10
+        times = []
+        for v in range(n):
+            self.persistent_variant = v
+            self._persistent_substep(dt, predict=True)
+            best = None
+            for _ in range(reps):
+                self.x4.copy_(x0)
+                self.v4.copy_(v0)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                self._persistent_substep(dt, predict=True)
+                b.record()
+                torch.cuda.synchronize()
+                ms = a.elapsed_time(b)
+                best = ms if best is None else min(best, ms)
+            times.append(best)
+        self.x4.copy_(x0)
+        self.v4.copy_(v0)
+        self.y4.copy_(y0)
+        self.persistent_variant = int(np.argmin(times))
+        self._graphs.clear()
+        return self.persistent_variant, times
 
     def constraint_residual(self, positions: str = "x", out=None):
         """Solver.constraint_residual over every instance's constraints."""

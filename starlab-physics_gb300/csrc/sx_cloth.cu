@@ -7,6 +7,7 @@
 #include <mutex>
 
 #include "sx_common.cuh"
+#include "sx_sweep.cuh"
 
 namespace sx {
 
@@ -87,15 +88,9 @@ __global__ void predict_kernel(int V, const float4* __restrict__ x4, const float
 }
 
 // ---------------------------------------------------------------------------
-// One Jacobi sweep (XPBD.py:141-184 + :384-387), gathered per vertex.
-//
-// For a constraint (v0, v1) the reference computes x10 = p0 - p1,
-// n = x10 * (1/|x10|), ld = k*C/(k*(w0+w1)*(n.n) + 1) and scatters
-// dx0 -= (w0*ld)*n, dx1 += (w1*ld)*n with float atomics.  From v1's side
-// p1 - p0 = -x10 exactly, so n flips sign exactly and
-// dx1 - (w1*ld)*(-n) == dx1 + (w1*ld)*n bit for bit: every vertex evaluates
-// dx -= (w_self*ld) * normalize(p_self - p_other) over its incident constraints
-// in ascending constraint index, which equals a serial run of the reference.
+// One Jacobi sweep (XPBD.py:141-184 + :384-387), gathered per vertex
+// (sweep_vertex, sx_sweep.cuh, states why the gather equals a serial run of
+// the reference's scatter).
 // ---------------------------------------------------------------------------
 constexpr int SW_BLOCK = 256;  // one vertex per thread
 inline int sweep_blocks(int n_verts) { return grid_for(n_verts, SW_BLOCK); }
@@ -163,71 +158,7 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int v = tile * BLOCK + threadIdx.x;
     float c2 = 0.0f;  // sum of C^2 over this vertex's entries (CHECK)
-    if (v < V) {
-        const float4 ps = __ldg(yin + v), xs = __ldg(x4 + v);
-        const int b = __ldg(ptr + v), e = __ldg(ptr + v + 1);
-        float dx = 0.0f, dy = 0.0f, dz = 0.0f;
-        for (int k0 = b; k0 < e; k0 += G) {
-            int2 a[G];
-            float4 o[G];
-#pragma unroll
-            for (int g = 0; g < G; ++g) a[g] = k0 + g < e ? __ldg(adj + k0 + g) : make_int2(0, 0);
-#pragma unroll
-            for (int g = 0; g < G; ++g) {
-                const bool use_x = !BY && a[g].x < 0 && !bend_y;
-                o[g] = k0 + g < e ? __ldg((use_x ? x4 : yin) + (a[g].x & 0x7fffffff)) : ps;
-            }
-#pragma unroll
-            for (int g = 0; g < G; ++g) {
-                if (k0 + g >= e) break;
-                const bool bend = a[g].x < 0;
-                const float rest = __int_as_float(a[g].y);
-                const bool use_x = !BY && bend && !bend_y;
-                const float4 self = use_x ? xs : ps;
-                const float kk = bend ? kb : ks;
-                const float ex = self.x - o[g].x, ey = self.y - o[g].y, ez = self.z - o[g].z;
-                if (FAST) {
-                    const float d2 = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, ez * ez));
-                    const float inv = rsqrtf(d2);
-                    const float C = d2 * inv - rest;
-                    if (CHECK) c2 = __fmaf_rn(C, C, c2);
-                    const float ld = __fdividef(kk * C, __fmaf_rn(kk, self.w + o[g].w, 1.0f));
-                    const float a0 = (self.w * ld) * inv;  // times the unnormalised difference
-                    dx = __fmaf_rn(-a0, ex, dx);
-                    dy = __fmaf_rn(-a0, ey, dy);
-                    dz = __fmaf_rn(-a0, ez, dz);
-                } else {
-                const float lij = sqrtf((ex * ex + ey * ey) + ez * ez);
-                const float C = lij - rest;
-                if (CHECK) c2 = c2 + C * C;
-                const float inv = 1.0f / lij;
-                const float nx = inv * ex, ny = inv * ey, nz = inv * ez;
-                const float schur = (self.w + o[g].w) * ((nx * nx + ny * ny) + nz * nz);
-                const float ld = (kk * C) / (kk * schur + 1.0f);
-                const float a0 = self.w * ld;
-                dx = dx - a0 * nx;
-                dy = dy - a0 * ny;
-                dz = dz - a0 * nz;
-                }
-            }
-        }
-        float4 out = ps;
-        const float nc = (float)(e - b);
-        if (nc > 0.0f) {
-            const float f = fixed[v];
-            if (FAST) {
-                const float fs = __fdividef(f, nc);
-                out.x = __fmaf_rn(fs, dx, ps.x);
-                out.y = __fmaf_rn(fs, dy, ps.y);
-                out.z = __fmaf_rn(fs, dz, ps.z);
-            } else {
-            out.x = ps.x + f * (dx / nc);
-            out.y = ps.y + f * (dy / nc);
-            out.z = ps.z + f * (dz / nc);
-            }
-        }
-        yout[v] = out;
-    }
+    if (v < V) yout[v] = sweep_vertex<G, BY, FAST, CHECK, true>(v, x4, yin, fixed, ptr, adj, ks, kb, bend_y, &c2);
     if (CHECK) block_residual_partial(c2, partial, tile);
     }
 }

@@ -7,6 +7,7 @@
 // integer atomics, so the sum does not depend on the order in which threads
 // arrive (the reference uses float atomics, whose result does).
 #include "sx_common.cuh"
+#include "sx_sweep.cuh"
 
 namespace sx {
 
@@ -1005,6 +1006,263 @@ __global__ void __launch_bounds__(256) batched_contacts_kernel(
 }
 
 // ---------------------------------------------------------------------------
+// Persistent batched substep.  One launch runs a whole substep of every
+// instance: each CTA takes instances from a queue (largest first) and runs,
+// for its instance alone, the cloth box and face boxes on x, optionally the
+// prediction, all Jacobi iterations (sweep; in the first, the obstacle broad
+// phase; obstacle contacts; update_dx) and the velocity update, with block
+// barriers between the phases -- an instance never reads another's vertices,
+// so no grid-wide synchronisation is needed.  The instance's positions and
+// adjacency stay in L1/L2 across its iterations instead of streaming the
+// whole batch from HBM in every sweep.  Every phase evaluates the same
+// expressions as the grid-wide kernels (sweep_vertex, project_vt_st /
+// project_tv_st, the broad-phase tests, update_dx, compute_velocity +
+// update_x), and contact sums are order independent, so the result equals the
+// graph of grid-wide launches bit for bit.  Chunk boxes (32 faces) are
+// aligned to each instance's first face (cptr); they only select which faces
+// are tested, and the faces are tested in ascending order either way.
+// The queue counter is reset by the last CTA to finish.
+// ---------------------------------------------------------------------------
+struct BatchedSubstepArgs {
+    int n_inst, n_iter, predict, cap;
+    const int *order, *vptr, *fptr, *cptr, *optr, *ob_fptr;
+    float4 *x4, *ya, *yb, *v4;
+    const float *fixed, *m_inv;
+    const int* adj_ptr;
+    const int2* adj;
+    const int *faces, *ob_faces;
+    const float4* xs4;
+    float4 *fmin4, *fmax4, *cmin4, *cmax4;
+    float* cl_box6;
+    const float* ob_box6;
+    const float4 *ob_fmin4, *ob_fmax4;
+    unsigned* vmask;
+    int *tv_cand, *tv_num;
+    long long* dx;
+    int* nc;
+    int *status, *queue;
+    float pad, dt, gx, gy, gz, ks, kb, dHat, compliance, damping;
+};
+
+template <int BLOCK, int MINB, bool FAST>
+__global__ void __launch_bounds__(BLOCK, MINB) batched_substep_kernel(BatchedSubstepArgs A) {
+    pdl_entry();
+    constexpr int NW = BLOCK / 32;
+    __shared__ int s_inst;
+    __shared__ unsigned s_box[6];
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    int bad = 0, overflow = 0;
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) {
+            const int k = atomicAdd(A.queue, 1);
+            s_inst = k < A.n_inst ? A.order[k] : -1;
+        }
+        if (tid < 6) s_box[tid] = tid < 3 ? f2ord_c(1e5f) : f2ord_c(-1e5f);
+        __syncthreads();
+        const int i = s_inst;
+        if (i < 0) break;
+        const int v0 = A.vptr[i], v1 = A.vptr[i + 1], f0 = A.fptr[i], f1 = A.fptr[i + 1], c0 = A.cptr[i];
+        const int o0 = A.optr[i], o1 = A.optr[i + 1];
+        // the cloth box on x (segment_aabb_kernel) ...
+        {
+            float lo[3] = {1e5f, 1e5f, 1e5f}, hi[3] = {-1e5f, -1e5f, -1e5f};
+            for (int v = v0 + tid; v < v1; v += BLOCK) {
+                const float4 p = A.x4[v];
+                lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
+                hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
+            }
+            for (int k = 0; k < 3; ++k) {
+                atomicMin(s_box + k, f2ord_c(lo[k]));
+                atomicMax(s_box + 3 + k, f2ord_c(hi[k]));
+            }
+        }
+        // ... padded face boxes on x (face_aabb_kernel) and the unions of
+        // chunks of 32 of them (warp w of a pass: chunk w)
+        for (int fb = f0 + 32 * warp; fb < f1; fb += BLOCK) {
+            const int f = fb + lane;
+            V3 lo{INFINITY, INFINITY, INFINITY}, hi{-INFINITY, -INFINITY, -INFINITY};
+            if (f < f1) {
+                const V3 a = mk(A.x4[A.faces[3 * f]]), b = mk(A.x4[A.faces[3 * f + 1]]),
+                         c = mk(A.x4[A.faces[3 * f + 2]]);
+                const V3 l = vmin(vmin(a, b), c), h = vmax(vmax(a, b), c);
+                lo = V3{l.x - A.pad, l.y - A.pad, l.z - A.pad};
+                hi = V3{h.x + A.pad, h.y + A.pad, h.z + A.pad};
+                A.fmin4[f] = make_float4(lo.x, lo.y, lo.z, 0.0f);
+                A.fmax4[f] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+            }
+            for (int o = 16; o > 0; o >>= 1) {
+                lo.x = fminf(lo.x, __shfl_xor_sync(0xffffffffu, lo.x, o));
+                lo.y = fminf(lo.y, __shfl_xor_sync(0xffffffffu, lo.y, o));
+                lo.z = fminf(lo.z, __shfl_xor_sync(0xffffffffu, lo.z, o));
+                hi.x = fmaxf(hi.x, __shfl_xor_sync(0xffffffffu, hi.x, o));
+                hi.y = fmaxf(hi.y, __shfl_xor_sync(0xffffffffu, hi.y, o));
+                hi.z = fmaxf(hi.z, __shfl_xor_sync(0xffffffffu, hi.z, o));
+            }
+            if (lane == 0) {
+                const int c = c0 + (fb - f0) / 32;
+                A.cmin4[c] = make_float4(lo.x, lo.y, lo.z, 0.0f);
+                A.cmax4[c] = make_float4(hi.x, hi.y, hi.z, 0.0f);
+            }
+        }
+        // compute_y (predict_kernel)
+        if (A.predict) {
+            for (int v = v0 + tid; v < v1; v += BLOCK) {
+                const float4 x = A.x4[v], vel = A.v4[v];
+                const float f = A.fixed[v];
+                float4 y;
+                y.x = (x.x + (f * vel.x) * A.dt) + (A.gx * A.dt) * A.dt;
+                y.y = (x.y + (f * vel.y) * A.dt) + (A.gy * A.dt) * A.dt;
+                y.z = (x.z + (f * vel.z) * A.dt) + (A.gz * A.dt) * A.dt;
+                y.w = x.w;
+                A.ya[v] = y;
+            }
+        }
+        __syncthreads();
+        if (tid < 6) {
+            const float b = ord2f_c(s_box[tid]);
+            A.cl_box6[6 * i + tid] = tid < 3 ? b - A.pad : b + A.pad;
+        }
+        float4* yin = A.ya;
+        float4* yout = A.yb;
+        for (int it = 0; it < A.n_iter; ++it) {
+            for (int v = v0 + tid; v < v1; v += BLOCK)
+                yout[v] = sweep_vertex<2, true, FAST, false, false>(v, A.x4, yin, A.fixed, A.adj_ptr, A.adj, A.ks,
+                                                                    A.kb, 1, nullptr);
+            __syncthreads();
+            if (it == 0) {
+                // broad phase (batched_vt_st_broad_kernel, batched_tv_st_broad_kernel)
+                const int of0 = A.ob_fptr[i], of1 = A.ob_fptr[i + 1];
+                const float* ob6 = A.ob_box6 + 6 * i;
+                for (int v = v0 + tid; v < v1; v += BLOCK) {
+                    const V3 p = mk(yout[v]);
+                    const V3 a{p.x - A.pad, p.y - A.pad, p.z - A.pad}, b{p.x + A.pad, p.y + A.pad, p.z + A.pad};
+                    unsigned m = 0;
+                    if (!query_skipped(a, b, ob6))
+                        for (int f = of0; f < of1; ++f)
+                            if (overlap(a, b, mk(A.ob_fmin4[f]), mk(A.ob_fmax4[f]))) m |= 1u << (f - of0);
+                    A.vmask[v] = m;
+                }
+                const float* cb6 = A.cl_box6 + 6 * i;
+                const int nch = (f1 - f0 + 31) / 32;
+                for (int s = o0 + warp; s < o1; s += NW) {
+                    const V3 p = mk(A.xs4[s]);
+                    const V3 a{p.x - A.pad, p.y - A.pad, p.z - A.pad}, b{p.x + A.pad, p.y + A.pad, p.z + A.pad};
+                    int count = 0;
+                    if (!query_skipped(a, b, cb6)) {
+                        for (int cb = 0; cb < nch; cb += 32) {
+                            const int c = cb + lane;
+                            const bool near_ = c < nch && overlap(a, b, mk(A.cmin4[c0 + c]), mk(A.cmax4[c0 + c]));
+                            unsigned hits = __ballot_sync(0xffffffffu, near_);
+                            while (hits) {
+                                const int ch = cb + __ffs(hits) - 1;
+                                hits &= hits - 1u;
+                                const int f = f0 + 32 * ch + lane;
+                                const bool hit = f < f1 && overlap(a, b, mk(A.fmin4[f]), mk(A.fmax4[f]));
+                                const unsigned ball = __ballot_sync(0xffffffffu, hit);
+                                const int slot = count + __popc(ball & ((1u << lane) - 1u));
+                                if (hit && slot < A.cap) A.tv_cand[(size_t)s * A.cap + slot] = f;
+                                count += __popc(ball);
+                            }
+                        }
+                    }
+                    if (lane == 0) {
+                        A.tv_num[s] = count;
+                        if (count > A.cap) overflow = 1;
+                    }
+                }
+                __syncthreads();
+            }
+            // obstacle contacts (batched_contacts_kernel)
+            const int nv = v1 - v0;
+            for (int k = tid; k < nv + (o1 - o0); k += BLOCK) {
+                if (k < nv) {
+                    const int v = v0 + k;
+                    unsigned m = A.vmask[v];
+                    if (m) {
+                        const int of0 = A.ob_fptr[i];
+                        const V3 x0 = mk(yout[v]);
+                        const float wv = A.m_inv[v];
+                        while (m) {
+                            const int kk = __ffs(m) - 1;
+                            m &= m - 1;
+                            const int f = of0 + kk;
+                            V3 g[4] = SX_ZERO_G;
+                            int dt_;
+                            float schur;
+                            project_vt_st(v, x0, mk(A.xs4[A.ob_faces[3 * f]]), mk(A.xs4[A.ob_faces[3 * f + 1]]),
+                                          mk(A.xs4[A.ob_faces[3 * f + 2]]), wv, A.dHat, A.compliance, A.dx, A.nc,
+                                          &bad, g, &dt_, &schur);
+                        }
+                    }
+                } else {
+                    const int s = o0 + (k - nv);
+                    const int n = min(A.tv_num[s], A.cap);
+                    for (int j = 0; j < n; ++j) {
+                        const int fd = A.tv_cand[(size_t)s * A.cap + j];
+                        const int vv[4] = {-1, A.faces[3 * fd], A.faces[3 * fd + 1], A.faces[3 * fd + 2]};
+                        const V3 x[4] = {mk(A.xs4[s]), mk(yout[vv[1]]), mk(yout[vv[2]]), mk(yout[vv[3]])};
+                        V3 g[4] = SX_ZERO_G;
+                        int dt_;
+                        float schur;
+                        project_tv_st(vv, x, A.fixed, A.m_inv, A.dHat, A.compliance, A.dx, A.nc, &bad, g, &dt_,
+                                      &schur);
+                    }
+                }
+            }
+            __syncthreads();
+            // update_dx (collision_apply_kernel)
+            for (int v = v0 + tid; v < v1; v += BLOCK) {
+                const int c = A.nc[v];
+                if (c > 0) {
+                    const float cf = (float)c;
+                    const float f = A.fixed[v];
+                    float4 y = yout[v];
+                    y.x = y.x + f * (from_fix(A.dx[3 * v]) / cf);
+                    y.y = y.y + f * (from_fix(A.dx[3 * v + 1]) / cf);
+                    y.z = y.z + f * (from_fix(A.dx[3 * v + 2]) / cf);
+                    yout[v] = y;
+                    A.dx[3 * v] = 0;
+                    A.dx[3 * v + 1] = 0;
+                    A.dx[3 * v + 2] = 0;
+                    A.nc[v] = 0;
+                }
+            }
+            __syncthreads();
+            float4* t = yin;
+            yin = yout;
+            yout = t;
+        }
+        // compute_velocity + update_x (velocity_update_kernel) from the final y
+        for (int v = v0 + tid; v < v1; v += BLOCK) {
+            float4 x = A.x4[v];
+            const float4 y = yin[v];
+            const float sfac = (1.0f - A.damping) * A.fixed[v];
+            float4 vel;
+            vel.x = (sfac * (y.x - x.x)) / A.dt;
+            vel.y = (sfac * (y.y - x.y)) / A.dt;
+            vel.z = (sfac * (y.z - x.z)) / A.dt;
+            vel.w = 0.0f;
+            A.v4[v] = vel;
+            x.x = x.x + A.dt * vel.x;
+            x.y = x.y + A.dt * vel.y;
+            x.z = x.z + A.dt * vel.z;
+            A.x4[v] = x;
+        }
+    }
+    if (bad) atomicOr(A.status, SX_STATUS_FIXED_RANGE);
+    if (overflow) atomicOr(A.status, SX_STATUS_CAND_OVERFLOW);
+    // the last CTA out resets the queue for the next launch
+    if (tid == 0) {
+        __threadfence();
+        if (atomicAdd(A.queue + 1, 1) == (int)gridDim.x - 1) {
+            A.queue[0] = 0;
+            A.queue[1] = 0;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Velocity-level contact and friction (solve_constraints_v, XPBD.py:374-381
 // and :398-404; collision_constraints_v.py __vt_st :6-133, __tv_st :137-330,
 // __vt_dy :334-570), over the pair records of the last position-level contact
@@ -1510,6 +1768,59 @@ extern "C" int sx_batched_obstacle_contacts(int n_verts, float* y4, const float*
            256, 0, s, n_verts, (float4*)y4, fixed, dx_fix, nc, conv,
            iter);
     return check_launch("collision_apply_kernel");
+}
+
+// Launch configurations of the persistent batched substep: threads per CTA
+// and CTAs per SM (the grid is that many per SM); all give identical results.
+struct BatchedSubstepVariant {
+    int block, blocks_per_sm;
+    decltype(&batched_substep_kernel<256, 4, false>) exact, fast;
+};
+#define SX_BS_VARIANT(B, M) {B, M, batched_substep_kernel<B, M, false>, batched_substep_kernel<B, M, true>}
+static const BatchedSubstepVariant kBatchedSubstepVariants[] = {
+    SX_BS_VARIANT(512, 2), SX_BS_VARIANT(256, 4), SX_BS_VARIANT(1024, 1), SX_BS_VARIANT(256, 2),
+    SX_BS_VARIANT(512, 1), SX_BS_VARIANT(128, 8),
+};
+#undef SX_BS_VARIANT
+constexpr int kNumBatchedSubstepVariants = sizeof(kBatchedSubstepVariants) / sizeof(kBatchedSubstepVariants[0]);
+
+extern "C" int sx_batched_substep_variants(void) { return kNumBatchedSubstepVariants; }
+
+extern "C" int sx_batched_substep_variant_info(int variant, int* block, int* blocks_per_sm) {
+    SX_REQUIRE(variant >= 0 && variant < kNumBatchedSubstepVariants && block && blocks_per_sm,
+               "sx_batched_substep_variant_info: bad variant");
+    *block = kBatchedSubstepVariants[variant].block;
+    *blocks_per_sm = kBatchedSubstepVariants[variant].blocks_per_sm;
+    return SX_OK;
+}
+
+extern "C" int sx_batched_substep(const SxBatchedSubstep* b, int variant, int fast, void* stream) {
+    SX_REQUIRE(b, "sx_batched_substep: null argument block");
+    SX_REQUIRE(variant >= 0 && variant < kNumBatchedSubstepVariants, "sx_batched_substep: bad variant");
+    SX_REQUIRE(b->n_inst >= 0 && b->n_iter >= 0 && b->cap >= 1, "sx_batched_substep: bad sizes");
+    if (b->n_inst == 0) return SX_OK;
+    SX_REQUIRE(b->order && b->vptr && b->fptr && b->cptr && b->optr && b->ob_fptr && b->x4 && b->y4 && b->y_other4 &&
+                   b->v4 && b->fixed && b->m_inv && b->adj_ptr && b->adj && b->faces && b->ob_faces && b->xs4 &&
+                   b->fmin4 && b->fmax4 && b->cmin4 && b->cmax4 && b->cl_box6 && b->ob_box6 && b->ob_fmin4 &&
+                   b->ob_fmax4 && b->vmask && b->tv_cand && b->tv_num && b->dx_fix && b->nc && b->status && b->queue,
+               "sx_batched_substep: null pointer");
+    BatchedSubstepArgs A;
+    A.n_inst = b->n_inst; A.n_iter = b->n_iter; A.predict = b->predict; A.cap = b->cap;
+    A.order = b->order; A.vptr = b->vptr; A.fptr = b->fptr; A.cptr = b->cptr; A.optr = b->optr;
+    A.ob_fptr = b->ob_fptr;
+    A.x4 = (float4*)b->x4; A.ya = (float4*)b->y4; A.yb = (float4*)b->y_other4; A.v4 = (float4*)b->v4;
+    A.fixed = b->fixed; A.m_inv = b->m_inv; A.adj_ptr = b->adj_ptr; A.adj = (const int2*)b->adj;
+    A.faces = b->faces; A.ob_faces = b->ob_faces; A.xs4 = (const float4*)b->xs4;
+    A.fmin4 = (float4*)b->fmin4; A.fmax4 = (float4*)b->fmax4; A.cmin4 = (float4*)b->cmin4;
+    A.cmax4 = (float4*)b->cmax4; A.cl_box6 = b->cl_box6; A.ob_box6 = b->ob_box6;
+    A.ob_fmin4 = (const float4*)b->ob_fmin4; A.ob_fmax4 = (const float4*)b->ob_fmax4;
+    A.vmask = b->vmask; A.tv_cand = b->tv_cand; A.tv_num = b->tv_num; A.dx = b->dx_fix; A.nc = b->nc;
+    A.status = b->status; A.queue = b->queue;
+    A.pad = b->padding; A.dt = b->dt; A.gx = b->gx; A.gy = b->gy; A.gz = b->gz; A.ks = b->k_spring;
+    A.kb = b->k_bend; A.dHat = b->dHat; A.compliance = b->compliance; A.damping = b->damping;
+    const BatchedSubstepVariant& bv = kBatchedSubstepVariants[variant];
+    launch(fast ? bv.fast : bv.exact, sm_count() * bv.blocks_per_sm, bv.block, 0, as_stream(stream), A);
+    return check_launch("batched_substep_kernel");
 }
 
 extern "C" int sx_velocity_contacts(int n_dy, int n_st, const int* faces_dy, const int* faces_st, int cap,

@@ -91,3 +91,63 @@ def test_batched_tolerance_mode(pkg):
     assert 0 < n < 20
     assert torch.equal(mid.x4, mid_g.x4)
     assert mid_g.convergence_stats()["converged_substeps"] == n
+
+
+@pytest.mark.parametrize("fast", [False, True])
+def test_persistent_substep_equals_grid_launches(pkg, fast):
+    """One persistent launch per substep (sx_batched_substep: an instance per
+    CTA, block barriers between the phases) gives the same frames as the graph
+    of grid-wide launches, bit for bit, in every launch configuration, with the
+    exact and with the fast arithmetic, for an even and an odd iteration
+    count."""
+    from starlab_physics_gb300._lib import sx
+
+    insts = _instances(pkg, seed=7, n_inst=9)
+    for n_iter in (4, 3):
+        def run(persistent, variant=0):
+            sim = pkg.BatchedSolver(insts, dHat=(4e-3) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8,
+                                    g=(0.0, 0.0, -9.81), dt=1 / 60, n_iter=n_iter, padding=8e-3)
+            sim.fast_math = fast
+            sim.persistent = persistent
+            sim.persistent_variant = variant
+            sim.use_graph = True
+            for _ in range(5):
+                sim.forward(10)
+            torch.cuda.synchronize()
+            return sim
+
+        ref = run(False)
+        for v in range(int(sx.sx_batched_substep_variants())):
+            got = run(True, v)
+            assert torch.equal(got.x4, ref.x4) and torch.equal(got.v4, ref.v4), (n_iter, v)
+            assert int(got.status.item()) == int(ref.status.item())
+            assert int(got._p_queue.abs().sum().item()) == 0
+
+
+def test_persistent_substep_batched512(pkg):
+    """The 512-cloth batch (3.2 M vertices): two frames of persistent launches
+    equal two frames of grid-wide launches bit for bit; the autotuner's pick
+    gives the same result."""
+    insts = pkg.batched_scene(512, seed=0)
+
+    def make():
+        return pkg.BatchedSolver(insts, dHat=(4e-3) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8,
+                                 g=(0.0, 0.0, -9.81), dt=1 / 60, n_iter=20, padding=8e-3)
+
+    a = make()
+    a.use_graph = True
+    for _ in range(2):
+        a.forward(10)
+    b = make()
+    b.persistent = True
+    b.use_graph = True
+    for _ in range(2):
+        b.forward(10)
+    torch.cuda.synchronize()
+    assert torch.equal(a.x4, b.x4) and torch.equal(a.v4, b.v4)
+    variant, times = b.autotune_persistent(reps=1)
+    assert 0 <= variant < len(times)
+    b.forward(10)
+    a.forward(10)
+    torch.cuda.synchronize()
+    assert torch.equal(a.x4, b.x4)
