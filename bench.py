@@ -427,45 +427,97 @@ def batched512(pkg, steps=5, warmup=2):
             "status_flags": status}
 
 
-def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2, check_every=4, train_frames=10,
-                    train_steps=6000):
-    """Learned warm start against the plain cold start on the 512-cloth batched
-    workload, at a fixed residual.
+def coloring_timing(pkg, reps=5, with_cpu=True):
+    """Constraint-graph colouring (sx_color_edges_greedy: first-fit in edge-id
+    order, all parallel rounds in one cooperative launch, then the stable sort
+    by colour) on the edges of the 64 x 64 and 256 x 256 cloths: ms per call
+    (CUDA events, median of `reps`), colours, and the oracle's serial time."""
+    import numpy as np
+    import torch
+    from starlab_physics_gb300._lib import ptr, stream_handle, sx
 
-    Training: the plain solver (``target_iters`` Jacobi iterations per substep)
-    runs ``train_frames`` frames of the seed-0 scene (10 frames: 51 200
-    cloth-substeps); 262 144 random free vertices per substep give (features,
-    correction) samples, and the MLP trains on them for ``train_steps`` Adam
-    steps of 65 536 rows with the library's kernels.  Evaluation on the held-out seed-1 scene: from one snapshot, the
-    plain solver runs a frame with ``cal_iters`` iterations per substep and the
-    largest end-of-substep residual of that frame becomes the tolerance.  Both
-    solvers then run frames from the same snapshot, iterating every substep
-    until the residual is at most that tolerance (cap 4 x cal_iters, checks
-    every 4 iterations); the learned one starts from the network's prediction
-    unless that raises the residual."""
+    out = {}
+    for n in (64, 256):
+        _, f = pkg.grid_cloth(n)
+        e = pkg.mesh.edges_from_faces(f)
+        E, V = e.shape[0], n * n
+        et = torch.from_numpy(np.ascontiguousarray(e.astype(np.int32))).cuda()
+        color = torch.empty(E, dtype=torch.int32, device="cuda")
+        srt = torch.empty(E, dtype=torch.int32, device="cuda")
+        prefix = torch.empty(100, dtype=torch.int32, device="cuda")
+        wsb = int(sx.sx_color_workspace_bytes(V, E))
+        ws = torch.empty(wsb, dtype=torch.uint8, device="cuda")
+
+        def call():
+            sx.sx_color_edges_greedy(ptr(et), E, V, 100, ptr(color), ptr(srt), ptr(prefix), ptr(ws), wsb,
+                                     stream_handle())
+
+        call()
+        ts = []
+        for _ in range(reps):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            call()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b))
+        r = {"edges": E, "ms": round(sorted(ts)[reps // 2], 4), "colours": int(color.max().item()) + 1,
+             "status": int(ws[:4].view(torch.int32).item())}
+        if with_cpu:
+            from oracle import pyoracle as po
+
+            t0 = time.perf_counter()
+            c_ref, s_ref, p_ref = po.color_edges(V, e)
+            r["cpu_baseline_ms"] = round(1e3 * (time.perf_counter() - t0), 2)
+            r["matches_oracle"] = bool(np.array_equal(color.cpu().numpy(), c_ref) and
+                                       np.array_equal(srt.cpu().numpy(), s_ref))
+        out[f"grid{n}"] = r
+    return out
+
+
+def learned_batched(pkg, target_iters=100, train_frames=40, train_rows=65536, val_frames=40, val_rows=8192,
+                    train_steps=6000, eval_start=10, eval_frames=6, rho=0.995, check_every=4, cap=400):
+    """Learned warm start against the plain cold start on the 512-cloth batched
+    workload, iterating every substep to the same relative residual.
+
+    Training data: the plain solver (``target_iters`` Jacobi iterations per
+    substep) runs the seed-0 scene from rest for ``train_frames`` frames (40
+    frames x 10 substeps x 512 cloths = 204 800 cloth-substeps); every substep
+    gives ``train_rows`` random free vertices (features, correction).  The MLP
+    trains on them for ``train_steps`` Adam steps of 65 536 rows with the
+    library's kernels.  Validation: the held-out seed-1 scene over the same
+    frame range; the loss of predicting no correction is evaluated by the same
+    masked loss.  Evaluation: the held-out seed-2 scene, from its state after
+    ``eval_start`` frames, ``eval_frames`` consecutive frames for each solver,
+    every substep iterated until the constraint residual is at most ``rho``
+    times the residual of that substep's cold start (cap ``cap``, checks every
+    ``check_every`` iterations, device-side loops); the learned solver starts
+    from the network's prediction unless that raises the residual.  Reported:
+    ms per frame, iterations, the end-state distance between the two runs.
+    Why a relative tolerance: on these scenes Jacobi lowers the residual by
+    0.5-2 % per 100 iterations once the cloths rest on their boxes (the
+    compliant bending pairs hold it up), so an absolute 1e-5 is met before any
+    iteration in free fall and never in contact."""
+    import numpy as np
     import torch
 
     L = pkg.learned
     kw = dict(dHat=(4e-3) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8, g=(0.0, 0.0, -9.81), dt=1.0 / 60.0,
               n_iter=20, padding=8e-3)
     A = pkg.BatchedSolver(pkg.batched_scene(512, seed=0), **kw)
-    for _ in range(2):
-        A.forward(10)
-    A.n_iter = target_iters
+    A.n_iter, A.persistent = target_iters, True
     t0 = time.time()
-    feat, tgt = L.collect_samples(A, frames=train_frames, rows_per_substep=262144)
+    feat, tgt = L.collect_samples(A, frames=train_frames, rows_per_substep=train_rows)
     torch.cuda.synchronize()
     collect_s = time.time() - t0
+    n_train_substeps = train_frames * 10 * A.n_instances
     del A
-    B = pkg.BatchedSolver(pkg.batched_scene(512, seed=1), **kw)
-    rec = L.WarmStart(B, mode="record")
-    B.warm = rec
-    for _ in range(2):
-        B.forward(10)
-    B.warm = None
-    vf, vt = L.collect_samples(B, frames=1, rows_per_substep=65536, seed=5)
-    snap = (B.x4.clone(), B.v4.clone(), rec.c4.clone())
+    Bv = pkg.BatchedSolver(pkg.batched_scene(512, seed=1), **kw)
+    Bv.n_iter, Bv.persistent = target_iters, True
+    vf, vt = L.collect_samples(Bv, frames=val_frames, rows_per_substep=val_rows, seed=5)
+    del Bv
     mlp = pkg.WarmStartMLP(seed=0)
+    zero_net = pkg.WarmStartMLP(params=L.zero_output_params())  # predicts no correction
     loss0 = L.evaluate_loss(mlp, vf, vt)
     t0 = time.time()
     h1 = L.train(mlp, feat, tgt, train_steps // 2, batch=65536, lr=2e-3)
@@ -473,11 +525,13 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2, check_e
     torch.cuda.synchronize()
     train_s = time.time() - t0
     val = L.evaluate_loss(mlp, vf, vt)
-    zero_val = float(vt[:, :3].pow(2).sum(1).mean().item())
+    zero_val = L.evaluate_loss(zero_net, vf, vt)
+    n_train_rows = int(feat.shape[0])
     del feat, tgt
     # inference alone, eager launches: the validation rows repeated to a batch
     # larger than L2, on the tcgen05 kernel and on the mma.sync kernel
-    big = torch.cat([vf] * 5)
+    reps_ = max(1, (3 << 20) // vf.shape[0] + 1)
+    big = torch.cat([vf] * reps_)
     n_big = big.shape[0]
     out_big = torch.empty((n_big, 4), dtype=torch.float32, device="cuda")
     flush_inf = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
@@ -501,6 +555,14 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2, check_e
     mlp.tcgen05 = True
     inf["tcgen05_status"] = int(mlp.status.item())
     del big, out_big, flush_inf
+    # evaluation scene: seed 2, state after eval_start plain frames
+    B = pkg.BatchedSolver(pkg.batched_scene(512, seed=2), **kw)
+    rec = L.WarmStart(B, mode="record")
+    B.warm, B.persistent = rec, True
+    for _ in range(eval_start):
+        B.forward(10)
+    B.warm, B.persistent = None, False
+    snap = (B.x4.clone(), B.v4.clone(), rec.c4.clone())
 
     def restore(warm=None):
         B.x4.copy_(snap[0])
@@ -508,36 +570,30 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2, check_e
         if warm is not None:
             warm.c4.copy_(snap[2])
 
-    # calibration: residual after cal_iters iterations, every substep of a frame
-    restore()
-    B.tol, B.tol_relative, B.check_every, B.n_iter, B.use_graph = 0.0, False, check_every, cal_iters + check_every, False
-    res = []
-    for _ in range(10):
-        B.substep(B.dt / 10)
-        res.append(float(B._res3[2].item()))
-    tol = max(res)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
-    out = {"workload": f"512 cloths ({B.num_verts} vertices), held-out seed, frames from one snapshot, "
-                       f"10 substeps, iterate to residual <= {tol:.4e} (cap {4 * cal_iters}, checks every "
-                       f"{check_every} iterations)",
-           "training": {"samples": train_frames * 10 * 262144, "cloth_substeps": train_frames * 10 * 512,
+    out = {"workload": f"512 cloths ({B.num_verts} vertices), held-out seed 2, frames {eval_start + 1}-"
+                       f"{eval_start + eval_frames} run in sequence, 10 substeps, each iterated to residual <= "
+                       f"{rho} x its cold-start residual (cap {cap}, checks every {check_every} iterations)",
+           "training": {"cloth_substeps": n_train_substeps, "frames": train_frames, "samples": n_train_rows,
                         "target_iterations": target_iters, "adam_steps": train_steps, "batch": 65536,
                         "collect_s": round(collect_s, 2), "train_s": round(train_s, 2),
                         "train_loss_first": float(h1[:10].mean()), "train_loss_last": float(h2[-100:].mean()),
-                        "val_loss_untrained": loss0, "val_loss": val, "val_loss_zero_prediction": zero_val},
-           "inference": inf, "tolerance": tol, "calibration_residuals": [round(r, 9) for r in res]}
+                        "validation": f"held-out seed 1, frames 1-{val_frames}, {int(vf.shape[0])} rows",
+                        "val_loss_untrained": loss0, "val_loss": val, "val_loss_zero_prediction": zero_val,
+                        "val_loss_vs_zero": val / zero_val if zero_val > 0 else None},
+           "inference": inf, "tolerance": {"relative_to_cold_start": rho}}
+    finals = {}
     for mode in ("plain", "learned"):
-        restore()
-        B.tol, B.n_iter, B.use_graph = tol, 4 * cal_iters, True
+        B.tol, B.tol_relative, B.check_every, B.n_iter, B.use_graph = rho, True, check_every, cap, True
         B.warm = L.WarmStart(B, mlp) if mode == "learned" else None
         restore(B.warm)
         B.forward(10)  # capture
-        times = []
+        restore(B.warm)
         B.convergence_stats(reset=True)
         if B.warm is not None:
             B.warm.flags.zero_()
+        times = []
         for _ in range(eval_frames):
-            restore(B.warm)
             flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record()
@@ -547,6 +603,7 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2, check_e
             times.append(a.elapsed_time(b))
         st = B.convergence_stats()
         ms = sum(times) / len(times)
+        finals[mode] = B.x4[:, :3].clone()
         out[mode] = {"ms_per_frame": round(ms, 3), "value": B.num_verts * 10 / (ms / 1e3), "unit": UNIT,
                      "converged_substeps": st["converged_substeps"], "substeps": 10 * eval_frames,
                      "mean_stop_iteration": st["mean_stop_iteration"],
@@ -554,6 +611,10 @@ def learned_batched(pkg, target_iters=100, cal_iters=100, eval_frames=2, check_e
         if B.warm is not None:
             out[mode].update(B.warm.fallback_counts())
     B.warm = None
+    d = (finals["learned"] - finals["plain"]).norm(dim=1)
+    diag = float(np.sqrt(2.0))  # every instance is a unit square cloth
+    out["end_state"] = {"max_abs_dx": float(d.max()), "rms_dx": float(d.pow(2).mean().sqrt()),
+                        "max_over_diagonal": float(d.max()) / diag, "criterion": 1e-4}
     out["speedup"] = out["learned"]["value"] / out["plain"]["value"]
     return out
 
@@ -848,6 +909,8 @@ def main():
         line["lbvh_soup"] = lbvh_soup(pkg, with_cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_batched:
         line["batched512"] = batched512(pkg)
+    if rank == 0:
+        line["coloring"] = coloring_timing(pkg, with_cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_learned:
         line["learned_batched512"] = learned_batched(pkg)
     if rank == 0 and world >= 1 and not args.no_cpu_baseline and world == 1:

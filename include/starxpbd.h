@@ -469,7 +469,11 @@ int sx_batched_obstacle_contacts(int n_verts, float* y4, const float* fixed, con
  * adjacent; all max_colors forbidden -> 0), computed in parallel rounds in
  * which an edge is coloured once all its lower-id neighbours are; then a
  * stable sort by colour.  prefix[max_colors] = start offset of each colour.
- * Synchronises `stream` (it polls the number of uncoloured edges). */
+ * All rounds run in one cooperative launch with a bounded grid barrier
+ * between them; the loop ends on the device (no host synchronisation).  After
+ * the call the first int of ws holds status bits: SX_STATUS_WAIT_TIMEOUT if a
+ * barrier wait or the round bound (n_edges + 1) ran out, the colours then
+ * being incomplete. */
 size_t sx_color_workspace_bytes(int n_verts, int n_edges);
 int sx_color_edges_greedy(const int* edges, int n_edges, int n_verts, int max_colors, int* color, int* sorted_edges,
                           int* prefix, void* ws, size_t ws_bytes, void* stream);

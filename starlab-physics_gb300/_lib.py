@@ -179,7 +179,8 @@ class _Calls:
             raise AttributeError(name)
         if SIGNATURES[name][1] is I and name not in ("sx_version", "sx_mlp_param_count", "sx_mlp_bf16_count",
                                                      "sx_jacobi_sweep_variants",
-                                                     "sx_contact_pairs_project_variants"):
+                                                     "sx_contact_pairs_project_variants",
+                                                     "sx_batched_substep_variants"):
             return lambda *a: _call(name, *a)
         return getattr(load(), name)
 

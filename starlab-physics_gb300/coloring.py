@@ -45,6 +45,10 @@ class GraphColoring:
         sx.sx_color_edges_greedy(ptr(e), self.num_edges, self.num_verts, self.max_num_colors, ptr(self.edges_color),
                                  ptr(self.sorted_edges_sequence_for_color), ptr(self.color_prefix_sum), ptr(ws),
                                  ws_bytes, stream_handle())
+        # device-side status of the colouring rounds (first int of the workspace)
+        status = int(ws[:4].view(torch.int32).item()) if self.num_edges else 0
+        if status:
+            raise RuntimeError(f"sx_color_edges_greedy: status {status:#x} (a bounded wait gave up)")
         if cache_dir and mesh_name:
             self.exportColorResult()
 

@@ -7,7 +7,10 @@
 // the dense matrix, and the sequential first-fit is reproduced exactly by
 // parallel rounds in which an edge takes its colour as soon as every adjacent
 // edge with a smaller id has one (those are exactly the edges a sequential pass
-// would have coloured before it).  The stable sort is the library's radix sort.
+// would have coloured before it).  All rounds run in one cooperative launch
+// with a grid barrier between them, and the loop ends on the device when a
+// round leaves nothing uncoloured (no host synchronisation).  The stable sort
+// is the library's radix sort.
 #include "sx_common.cuh"
 
 extern "C" size_t sx_radix_sort_workspace_bytes(int n);
@@ -17,7 +20,7 @@ extern "C" int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, v
 namespace sx {
 
 constexpr int kMaxColorWords = 4;  // up to 128 colours
-constexpr int kRoundsPerPoll = 16;
+constexpr long long kBarrierPolls = 1LL << 24;  // about 1 s of 64 ns sleeps
 
 static inline size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 
@@ -47,13 +50,14 @@ __global__ void color_init_kernel(int E, int* color, unsigned* keys, int* ids) {
     ids[e] = e;
 }
 
-__global__ void color_round_kernel(int E, const int* __restrict__ edges, const int* __restrict__ ptr,
-                                   const int* __restrict__ inc, int max_colors, int* color, int* remaining) {
-    pdl_entry();
-    int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e >= E) return;
+// Tries to colour edge e: false if an adjacent edge with a smaller id has no
+// colour yet; otherwise e gets the smallest colour none of them has (or keeps
+// the one it has).  Colours once set never change, so reading a neighbour's
+// colour set earlier in the same round gives the same choice.
+__device__ __forceinline__ bool color_try(int e, const int* __restrict__ edges, const int* __restrict__ ptr,
+                                          const int* __restrict__ inc, int max_colors, int* color) {
     volatile int* vc = color;
-    if (vc[e] != -1) return;
+    if (vc[e] != -1) return true;
     unsigned forbid[kMaxColorWords] = {0u, 0u, 0u, 0u};
     for (int s = 0; s < 2; ++s) {
         const int v = edges[2 * e + s];
@@ -61,10 +65,7 @@ __global__ void color_round_kernel(int E, const int* __restrict__ edges, const i
             const int o = inc[k];
             if (o >= e) continue;
             const int c = vc[o];
-            if (c < 0) {
-                atomicAdd(remaining, 1);
-                return;
-            }
+            if (c < 0) return false;
             forbid[c >> 5] |= 1u << (c & 31);
         }
     }
@@ -76,14 +77,83 @@ __global__ void color_round_kernel(int E, const int* __restrict__ edges, const i
         }
     }
     vc[e] = pick;
+    return true;
+}
+
+// Sense-reversing barrier over the blocks of a cooperative launch (all of
+// them resident), bounded: a block that waits longer than kBarrierPolls polls
+// returns false (the caller sets a status bit and leaves).  sync[0] counts
+// arrivals, sync[1] is the generation.
+__device__ bool grid_barrier(unsigned* sync) {
+    __shared__ int s_ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* gen = sync + 1;
+        const unsigned g = *gen;
+        __threadfence();
+        int ok = 1;
+        if (atomicAdd(sync, 1u) == gridDim.x - 1) {
+            atomicExch(sync, 0u);
+            __threadfence();
+            atomicAdd(sync + 1, 1u);
+        } else {
+            long long n = 0;
+            while (*gen == g) {
+                if (++n > kBarrierPolls) {
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(64);
+            }
+        }
+        __threadfence();
+        s_ok = ok;
+    }
+    __syncthreads();
+    return s_ok != 0;
+}
+
+// Every round in one cooperative launch: each thread tries its edges (grid
+// stride), blocks add the edges still uncoloured to rem[r % 3], and after the
+// barrier every block reads it; 0 ends the loop.  rem[(r + 1) % 3] is cleared
+// during round r: it was last read right after barrier r - 2, which every
+// block has left since it arrived at barrier r - 1.  E + 1 rounds bound the
+// loop (each round colours at least the smallest uncoloured edge).
+// sync = {arrivals, generation, rem[3]}, zero on entry; status bit
+// SX_STATUS_WAIT_TIMEOUT if a barrier wait or the round bound ran out.
+__global__ void __launch_bounds__(256) color_rounds_kernel(int E, const int* __restrict__ edges,
+                                                           const int* __restrict__ ptr, const int* __restrict__ inc,
+                                                           int max_colors, int* color, unsigned* sync, int max_rounds,
+                                                           int* status) {
+    pdl_entry();
+    __shared__ int s_left;
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (int r = 0; r < max_rounds; ++r) {
+        if (threadIdx.x == 0) s_left = 0;
+        if (blockIdx.x == 0 && threadIdx.x == 0) sync[2 + (r + 1) % 3] = 0u;
+        __syncthreads();
+        int left = 0;
+        for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride)
+            left += color_try((int)e, edges, ptr, inc, max_colors, color) ? 0 : 1;
+        if (left) atomicAdd(&s_left, left);
+        __syncthreads();
+        if (threadIdx.x == 0 && s_left) atomicAdd(sync + 2 + r % 3, (unsigned)s_left);
+        if (!grid_barrier(sync)) {
+            if (threadIdx.x == 0) atomicOr(status, SX_STATUS_WAIT_TIMEOUT);
+            return;
+        }
+        if (*(volatile unsigned*)(sync + 2 + r % 3) == 0u) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, SX_STATUS_WAIT_TIMEOUT);
 }
 
 __global__ void color_hist_kernel(int E, const int* __restrict__ color, unsigned* keys, unsigned* hist) {
     pdl_entry();
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
-    keys[e] = (unsigned)color[e];
-    atomicAdd(hist + color[e], 1u);
+    const int c = color[e];  // -1 only if the rounds stopped early (status bit set)
+    keys[e] = c < 0 ? 255u : (unsigned)c;
+    if (c >= 0) atomicAdd(hist + c, 1u);
 }
 
 // exclusive scan of the colour histogram (max_colors <= 128) -> start offsets
@@ -112,10 +182,10 @@ __global__ void scan_excl_small(int n, int* data) {
 
 using namespace sx;
 
-// workspace: [ptr V+1][cursor V][inc 2E][remaining kRoundsPerPoll][keys E][hist 128][radix ws E]
+// workspace: [status 1][sync 5][ptr V+1][cursor V][inc 2E][keys E][hist 128][radix ws E]
 extern "C" size_t sx_color_workspace_bytes(int n_verts, int n_edges) {
     size_t V = (size_t)(n_verts > 0 ? n_verts : 1), E = (size_t)(n_edges > 0 ? n_edges : 1);
-    return a256((V + 1) * 4) + a256(V * 4) + a256(2 * E * 4) + a256(kRoundsPerPoll * 4) + a256(E * 4) +
+    return a256(4) + a256(5 * 4) + a256((V + 1) * 4) + a256(V * 4) + a256(2 * E * 4) + a256(E * 4) +
            a256(128 * 4) + sx_radix_sort_workspace_bytes(n_edges);
 }
 
@@ -160,14 +230,16 @@ extern "C" int sx_color_edges_greedy(const int* edges, int n_edges, int n_verts,
                "sx_color_edges_greedy: workspace too small");
     const size_t V = (size_t)(n_verts > 0 ? n_verts : 1), E = (size_t)n_edges;
     char* p = (char*)ws;
+    int* status = (int*)p; p += a256(4);
+    unsigned* sync = (unsigned*)p; p += a256(5 * 4);
     int* ptr = (int*)p; p += a256((V + 1) * 4);
     int* cursor = (int*)p; p += a256(V * 4);
     int* inc = (int*)p; p += a256(2 * E * 4);
-    int* remaining = (int*)p; p += a256(kRoundsPerPoll * 4);
     unsigned* keys = (unsigned*)p; p += a256(E * 4);
     unsigned* hist = (unsigned*)p; p += a256(128 * 4);
     void* rws = p;
 
+    SX_CUDA(cudaMemsetAsync(ws, 0, a256(4) + a256(5 * 4), s));
     SX_CUDA(cudaMemsetAsync(ptr, 0, (V + 1) * 4, s));
     SX_CUDA(cudaMemsetAsync(cursor, 0, V * 4, s));
     launch(inc_count_kernel, grid_for(n_edges, 256), 256, 0, s, n_edges, edges, ptr);
@@ -176,25 +248,22 @@ extern "C" int sx_color_edges_greedy(const int* edges, int n_edges, int n_verts,
     launch(color_init_kernel, grid_for(n_edges, 256), 256, 0, s, n_edges, color, keys, sorted_edges);
     int rc = check_launch("colour setup");
     if (rc) return rc;
-    // Each round colours at least the smallest uncoloured edge, so E rounds bound
-    // the loop; poll the remaining count every kRoundsPerPoll rounds.
-    long long rounds = 0;
-    for (;;) {
-        SX_CUDA(cudaMemsetAsync(remaining, 0, kRoundsPerPoll * 4, s));
-        for (int r = 0; r < kRoundsPerPoll; ++r)
-            launch(color_round_kernel, grid_for(n_edges, 256), 256, 0, s, n_edges, edges, ptr, inc, max_colors, color,
-                                                                      remaining + r);
-        rc = check_launch("color_round_kernel");
-        if (rc) return rc;
-        rounds += kRoundsPerPoll;
-        int left = 0;
-        SX_CUDA(cudaMemcpyAsync(&left, remaining + kRoundsPerPoll - 1, 4, cudaMemcpyDeviceToHost, s));
-        SX_CUDA(cudaStreamSynchronize(s));
-        if (left == 0) break;
-        if (rounds > (long long)n_edges + kRoundsPerPoll) {
-            set_error("sx_color_edges_greedy: no progress after %lld rounds", rounds);
-            return SX_ERR_TIMEOUT;
-        }
+    // all rounds in one cooperative launch (every block resident)
+    {
+        const int cap = resident_blocks(color_rounds_kernel, 256);
+        const int g = grid_for(n_edges, 256) < cap ? grid_for(n_edges, 256) : cap;
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(g);
+        cfg.blockDim = dim3(256);
+        cfg.stream = s;
+        cudaLaunchAttribute attr[1];
+        attr[0].id = cudaLaunchAttributeCooperative;
+        attr[0].val.cooperative = 1;
+        cfg.attrs = attr;
+        cfg.numAttrs = 1;
+        SX_CUDA(cudaLaunchKernelEx(&cfg, color_rounds_kernel, n_edges, edges, (const int*)ptr, (const int*)inc,
+                                   max_colors, color, sync, n_edges + 1, status));
+        note_launch();
     }
     SX_CUDA(cudaMemsetAsync(hist, 0, 128 * 4, s));
     launch(color_hist_kernel, grid_for(n_edges, 256), 256, 0, s, n_edges, color, keys, hist);

@@ -51,6 +51,20 @@ def init_params(seed: int = 0) -> np.ndarray:
     return np.concatenate(parts).astype(np.float32)
 
 
+def zero_output_params(seed: int = 0) -> np.ndarray:
+    """init_params with the output layer zeroed: a network that predicts no
+    correction, whose evaluate_loss is the loss of the cold start under the
+    same masked loss function."""
+    p = init_params(seed)
+    o = 0
+    for name, shape in SHAPES:
+        n = int(np.prod(shape))
+        if name in ("W3", "b3"):
+            p[o:o + n] = 0.0
+        o += n
+    return p
+
+
 def mean_spring_rest(adj_ptr: np.ndarray, adj: np.ndarray) -> np.ndarray:
     """L per vertex: mean rest length of its springs (of all its constraints if
     it has none, 1 if it has no constraint)."""

@@ -348,7 +348,7 @@ def test_solver_end_to_end(pkg, po, mode):
 
 
 def test_coloring(pkg, po):
-    for n in (9, 33):
+    for n in (9, 33, 256):
         x, f = pkg.grid_cloth(n)
         e = pkg.mesh.edges_from_faces(f)
         gc = pkg.GraphColoring(n * n, e, device=DEV)

@@ -288,7 +288,8 @@ def test_training_reduces_loss(pkg, trained):
     L = pkg.learned
     mlp, hist, before, vf, vt = trained
     after = L.evaluate_loss(mlp, vf, vt)
-    zero = float(vt[:, :3].pow(2).sum(1).mean().item())
+    zero = L.evaluate_loss(pkg.WarmStartMLP(params=L.zero_output_params()), vf, vt)
+    assert zero == pytest.approx(float(vt[:, :3].pow(2).sum(1).mean().item()), rel=1e-3)
     assert np.all(np.isfinite(hist))
     assert hist[-50:].mean() < 0.1 * hist[:10].mean()
     assert after < 0.1 * before
