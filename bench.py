@@ -200,52 +200,56 @@ def ncu_traffic(kernel_file):
     return None
 
 
-def cpu_baseline(scene, rank):
-    """Oracle port on all host cores, one substep of the same scene."""
-    import numpy as np  # noqa: F401
-
+def _oracle_solver(pkg, scene, nthreads):
     from oracle import pyoracle as po
-    import __graft_entry__ as ge
-
-    pkg = ge.load_package()
     from starlab_physics_gb300 import mesh as M
 
     cl = M.TriMesh(scene.cloth_x, scene.cloth_faces, device="cpu")
     ob = M.TriMesh(scene.obstacle_x, scene.obstacle_faces, device="cpu") if scene.obstacle_x is not None else None
     if len(scene.pinned):
         cl.fixed[scene.pinned] = 0.0
+    return po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob) if ob else None, dt=scene.dt,
+                           g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
+                           k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
+                           padding=scene.padding, n_iter=scene.n_iter, collisions=scene.collisions,
+                           rebuild=scene.rebuild, cap=scene.cap, nthreads=nthreads, bending_on="y",
+                           contact_cull=True)
+
+
+def cpu_baseline(pkg, scene, x0, v0, gpu_x_after, frame):
+    """The oracle port on all host cores, on the state the GPU arm times (the
+    snapshot before frame `frame`): the whole frame (its 10 substeps) timed, and
+    its end state compared with the GPU's frame from the same snapshot; then one
+    substep on one core."""
+    import numpy as np
+
     cores = os.cpu_count() or 1
-    orc = po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob) if ob else None, dt=scene.dt,
-                          g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
-                          k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
-                          padding=scene.padding, n_iter=scene.n_iter, collisions=scene.collisions,
-                          rebuild=scene.rebuild, cap=scene.cap, nthreads=cores, bending_on="y")
+    orc = _oracle_solver(pkg, scene, cores)
+    orc.x4[:] = x0
+    orc.v4[:] = v0
     dt_sub = scene.dt / scene.n_substeps
-    orc.substep(dt_sub)  # warm-up
-    n = 0
     t0 = time.perf_counter()
-    while True:
+    for _ in range(scene.n_substeps):
         orc.substep(dt_sub)
-        n += 1
-        el = time.perf_counter() - t0
-        if el > 8.0 or n >= 10:
-            break
+    el = time.perf_counter() - t0
+    d = np.abs(orc.x4[:, :3].astype(np.float64) - gpu_x_after[:, :3])
+    p = scene.cloth_x.astype(np.float64)
+    diag = float(np.linalg.norm(p.max(0) - p.min(0)))
     V = scene.cloth_x.shape[0]
-    # the same port on one core, one or two substeps
-    orc.nthreads = 1
-    n1 = 0
+    n = scene.n_substeps
+    orc1 = _oracle_solver(pkg, scene, 1)
+    orc1.x4[:] = x0
+    orc1.v4[:] = v0
     t0 = time.perf_counter()
-    while True:
-        orc.substep(dt_sub)
-        n1 += 1
-        el1 = time.perf_counter() - t0
-        if el1 > 4.0 or n1 >= 2:
-            break
+    orc1.substep(dt_sub)
+    el1 = time.perf_counter() - t0
     return {"value": V * n / el, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{n} substep(s) of the same scene on the CPU oracle (OpenMP, {cores} threads), "
-                      f"{el:.2f} s",
-            "one_core": {"value": V * n1 / el1, "unit": UNIT, "cores": 1,
-                         "sample": f"{n1} substep(s) of the same scene, 1 thread, {el1:.2f} s"}}
+            "sample": f"frame {frame} of the scene ({n} substeps) from the GPU arm's snapshot on the CPU oracle "
+                      f"(OpenMP, {cores} threads), {el:.2f} s",
+            "max_abs_dx_vs_gpu": float(d.max()), "max_abs_dx_over_diagonal": float(d.max()) / diag,
+            "bit_exact_vs_gpu": bool(d.max() == 0.0),
+            "one_core": {"value": V / el1, "unit": UNIT, "cores": 1,
+                         "sample": f"1 substep of the same frame, 1 thread, {el1:.2f} s"}}
 
 
 def lbvh_soup(pkg, reps=10, with_cpu=True):
@@ -318,7 +322,7 @@ def lbvh_soup(pkg, reps=10, with_cpu=True):
     return out
 
 
-def batched512(pkg, steps=5, warmup=2):
+def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
     """Batched workload: 512 independent cloths (grid side uniform in [16,128],
     about 3.2M vertices) each over its own box, 10 substeps x 20 Jacobi
     iterations, obstacle contacts; one CUDA graph per frame.  Also times the
@@ -328,6 +332,8 @@ def batched512(pkg, steps=5, warmup=2):
     from starlab_physics_gb300._lib import ptr, stream_handle, sx
 
     insts = pkg.batched_scene(512, seed=0)
+    if world > 1:  # independent instances: each rank takes a balanced share, nothing is exchanged
+        insts = [insts[i] for i in pkg.shard_instances(insts, rank, world)]
     sim = pkg.BatchedSolver(insts, dHat=(4e-3) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8,
                             g=(0.0, 0.0, -9.81), dt=1.0 / 60.0, n_iter=20, padding=8e-3)
     sim.use_graph = True
@@ -416,9 +422,18 @@ def batched512(pkg, steps=5, warmup=2):
     persistent_fast = timed_frames()
     sim.fast_math = False
     sim.persistent = False
-    return {"workload": f"512 cloths, {V} vertices, {sim.num_faces} faces, 10 substeps x 20 iterations, "
-                        "obstacle contacts", "value": V * S * steps / (tot / 1e3), "unit": UNIT,
-            "ms_per_step": tot / steps, "steps": steps, "warmup": warmup,
+    value, ms_job = replica_throughput(V * S * steps, tot, world)  # units summed over ranks / slowest rank
+    if world > 1:
+        import torch.distributed as dist
+
+        t = torch.tensor([V], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t)
+        value = float(t.item()) * S * steps / (ms_job / 1e3)
+    return {"workload": f"512 cloths, {V} vertices on this rank, {sim.num_faces} faces, 10 substeps x 20 "
+                        "iterations, obstacle contacts" + (f", instances split over {world} ranks" if world > 1
+                                                            else ""),
+            "value": value, "unit": UNIT,
+            "ms_per_step": ms_job / steps, "steps": steps, "warmup": warmup,
             "sweep_variant": sim.sweep_variant,
             "sweep_roofline": exact_sweep,
             "fast_math": fast,
@@ -620,27 +635,23 @@ def learned_batched(pkg, target_iters=100, train_frames=40, train_rows=65536, va
 
 
 def run_reference(args):
+    """The reference arm: the CPU port of the reference's substep (the
+    reference's Taichi path cannot run here) on all host cores, on the state
+    the GPU arm times: the scene advanced by `warmup` frames, then `steps`
+    substeps of the next frame(s) timed one by one (a bounded sample; at most
+    about 150 s of timing)."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
     pkg, scene = build_scene(args.workload)
-    from oracle import pyoracle as po
-    from starlab_physics_gb300 import mesh as M
-
-    cl = M.TriMesh(scene.cloth_x, scene.cloth_faces, device="cpu")
-    ob = M.TriMesh(scene.obstacle_x, scene.obstacle_faces, device="cpu") if scene.obstacle_x is not None else None
-    if len(scene.pinned):
-        cl.fixed[scene.pinned] = 0.0
     cores = os.cpu_count() or 1
-    orc = po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob) if ob else None, dt=scene.dt,
-                          g=scene.gravity, k_stretch_stiffness=scene.stiffness_stretch,
-                          k_bend_stiffness=scene.stiffness_bending, dHat=scene.dHat, damping=scene.damping,
-                          padding=scene.padding, n_iter=scene.n_iter, collisions=scene.collisions,
-                          rebuild=scene.rebuild, cap=scene.cap, nthreads=cores, bending_on="y")
+    orc = _oracle_solver(pkg, scene, cores)
+    t0 = time.perf_counter()
+    for _ in range(args.warmup):
+        orc.forward(scene.n_substeps)
+    warm_s = time.perf_counter() - t0
     dt_sub = scene.dt / scene.n_substeps
-    for _ in range(max(1, min(args.warmup, 2))):
-        orc.substep(dt_sub)
     times = []
     budget = 150.0
     t_all = time.perf_counter()
@@ -657,10 +668,12 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
         "steps": len(times), "warmup": args.warmup, "ms_per_step": 1e3 * tot / len(times),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": workload_config(scene, args.workload) | {"step": "one substep (bounded CPU sample)"},
+        "config": workload_config(scene, args.workload) | {
+            "step": f"one substep of frame {args.warmup + 1} onward (the state the GPU arm times, reached by "
+                    f"{args.warmup} untimed frames, {warm_s:.1f} s)"},
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
-                         "sample": f"{len(times)} substeps of the same scene on the CPU oracle, {cores} threads "
-                                   "(the reference's Taichi path cannot run here)"},
+                         "sample": f"{len(times)} substeps from frame {args.warmup + 1} of the same scene on the "
+                                   f"CPU oracle, {cores} threads (the reference's Taichi path cannot run here)"},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
@@ -907,14 +920,23 @@ def main():
     line["clocks_e2e"] = clk2.summary()
     if rank == 0 and not args.no_lbvh:
         line["lbvh_soup"] = lbvh_soup(pkg, with_cpu=not args.no_cpu_baseline)
-    if rank == 0 and not args.no_batched:
-        line["batched512"] = batched512(pkg)
+    if not args.no_batched:
+        b512 = batched512(pkg, world=world, rank=rank)
+        if rank == 0:
+            line["batched512"] = b512
     if rank == 0:
         line["coloring"] = coloring_timing(pkg, with_cpu=not args.no_cpu_baseline)
     if rank == 0 and not args.no_learned:
         line["learned_batched512"] = learned_batched(pkg)
     if rank == 0 and world >= 1 and not args.no_cpu_baseline and world == 1:
-        line["cpu_baseline"] = cpu_baseline(scene, rank)
+        # the GPU's frame from the timed snapshot, for the comparison
+        sim.use_graph = True
+        sim.mesh_dy.x4.copy_(x0)
+        sim.mesh_dy.v4.copy_(v0)
+        sim.forward(S)
+        torch.cuda.synchronize()
+        line["cpu_baseline"] = cpu_baseline(pkg, scene, x0.cpu().numpy(), v0.cpu().numpy(),
+                                            sim.mesh_dy.x4.cpu().numpy(), args.warmup + 1)
     if rank == 0:
         print(json.dumps(line))
     if world > 1:

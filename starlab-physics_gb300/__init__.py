@@ -12,12 +12,12 @@ from .coloring import GraphColoring
 from .lbvh import LBVH, LBVH_CELL
 from .mesh import TriMesh, box_mesh, grid_cloth, icosphere
 from .solver import Solver
-from .batched import BatchedSolver, Instance, batched_scene
+from .batched import BatchedSolver, Instance, batched_scene, shard_instances
 from . import scenes
 from . import learned
 from . import meshio
 from .learned import WarmStart, WarmStartMLP
 
-__all__ = ["Solver", "BatchedSolver", "Instance", "batched_scene", "LBVH_CELL", "LBVH", "GraphColoring", "TriMesh",
+__all__ = ["Solver", "BatchedSolver", "Instance", "batched_scene", "shard_instances", "LBVH_CELL", "LBVH", "GraphColoring", "TriMesh",
            "grid_cloth", "box_mesh", "icosphere", "scenes", "learned", "meshio", "WarmStart", "WarmStartMLP", "SxError",
            "load_library", "library_path"]

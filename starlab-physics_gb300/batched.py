@@ -58,6 +58,28 @@ def batched_scene(n_instances: int = 512, seed: int = 0, n_min: int = 16, n_max:
     return out
 
 
+def shard_instances(instances, rank: int, world: int):
+    """The instances rank `rank` of `world` simulates: a greedy split by
+    weight V + constraints (springs and bending pairs, about 6 V for a grid
+    cloth), largest first onto the lightest rank.  Instances are independent,
+    so ranks exchange nothing per substep.  Returns the instance indices in
+    ascending order."""
+    if not 0 <= rank < world:
+        raise ValueError("rank out of range")
+    w = []
+    for inst in instances:
+        V = int(np.asarray(inst.x).shape[0])
+        F = int(np.asarray(inst.faces).shape[0])
+        w.append(V + 3 * F)  # V + springs (~1.5 F) + bending pairs (~1.5 F)
+    load = [0] * world
+    owner = [0] * len(instances)
+    for i in sorted(range(len(instances)), key=lambda k: (-w[k], k)):
+        r = min(range(world), key=lambda k: (load[k], k))
+        owner[i] = r
+        load[r] += w[i]
+    return [i for i in range(len(instances)) if owner[i] == rank]
+
+
 class BatchedSolver:
     """XPBD substep for a batch of independent cloths with obstacles."""
 
