@@ -373,6 +373,8 @@ class BatchedSolver:
     def forward(self, n_substeps: int):
         """One frame for every instance (a CUDA graph per frame with
         ``use_graph``)."""
+        if self.persistent:
+            self._persistent_buffers()  # allocated and uploaded outside any capture
         if not self.use_graph:
             self._forward_eager(n_substeps)
             return
