@@ -466,14 +466,13 @@ int sx_batched_obstacle_contacts(int n_verts, float* y4, const float* fixed, con
 
 /* initAdjEdges + colorEdgesGreedy + colorCountingSort, graph_coloring.py:112-201:
  * colour = first-fit over edges in id order (edges sharing a vertex are
- * adjacent; all max_colors forbidden -> 0), computed in parallel rounds in
- * which an edge is coloured once all its lower-id neighbours are; then a
+ * adjacent; all max_colors forbidden -> 0), computed in parallel: an edge is
+ * coloured once all its lower-id neighbours are; then a
  * stable sort by colour.  prefix[max_colors] = start offset of each colour.
- * All rounds run in one cooperative launch with a bounded grid barrier
- * between them; the loop ends on the device (no host synchronisation).  After
+ * One cooperative launch colours every edge as soon as its lower-id
+ * neighbours have colours (bounded waits, no host synchronisation).  After
  * the call the first int of ws holds status bits: SX_STATUS_WAIT_TIMEOUT if a
- * barrier wait or the round bound (n_edges + 1) ran out, the colours then
- * being incomplete. */
+ * wait gave up, the colours then being incomplete. */
 size_t sx_color_workspace_bytes(int n_verts, int n_edges);
 int sx_color_edges_greedy(const int* edges, int n_edges, int n_verts, int max_colors, int* color, int* sorted_edges,
                           int* prefix, void* ws, size_t ws_bytes, void* stream);

@@ -7,10 +7,9 @@
 // the dense matrix, and the sequential first-fit is reproduced exactly by
 // parallel rounds in which an edge takes its colour as soon as every adjacent
 // edge with a smaller id has one (those are exactly the edges a sequential pass
-// would have coloured before it).  All rounds run in one cooperative launch
-// with a grid barrier between them, and the loop ends on the device when a
-// round leaves nothing uncoloured (no host synchronisation).  The stable sort
-// is the library's radix sort.
+// would have coloured before it).  One cooperative launch colours every edge,
+// each as soon as its lower-id neighbours have colours (no rounds, no host
+// synchronisation).  The stable sort is the library's radix sort.
 #include "sx_common.cuh"
 
 extern "C" size_t sx_radix_sort_workspace_bytes(int n);
@@ -20,7 +19,6 @@ extern "C" int sx_radix_sort_pairs(unsigned* keys, int* vals, int n, int bits, v
 namespace sx {
 
 constexpr int kMaxColorWords = 4;  // up to 128 colours
-constexpr long long kBarrierPolls = 1LL << 24;  // about 1 s of 64 ns sleeps
 
 static inline size_t a256(size_t b) { return (b + 255) & ~(size_t)255; }
 
@@ -55,7 +53,7 @@ __global__ void color_init_kernel(int E, int* color, unsigned* keys, int* ids) {
 // the one it has).  Colours once set never change, so reading a neighbour's
 // colour set earlier in the same round gives the same choice.
 __device__ __forceinline__ bool color_try(int e, const int* __restrict__ edges, const int* __restrict__ ptr,
-                                          const int* __restrict__ inc, int max_colors, int* color) {
+                                          const int* __restrict__ inc, int max_colors, int* color, int* blocker) {
     volatile int* vc = color;
     if (vc[e] != -1) return true;
     unsigned forbid[kMaxColorWords] = {0u, 0u, 0u, 0u};
@@ -65,7 +63,10 @@ __device__ __forceinline__ bool color_try(int e, const int* __restrict__ edges, 
             const int o = inc[k];
             if (o >= e) continue;
             const int c = vc[o];
-            if (c < 0) return false;
+            if (c < 0) {
+                *blocker = o;
+                return false;
+            }
             forbid[c >> 5] |= 1u << (c & 31);
         }
     }
@@ -80,78 +81,47 @@ __device__ __forceinline__ bool color_try(int e, const int* __restrict__ edges, 
     return true;
 }
 
-// Sense-reversing barrier over the blocks of a cooperative launch (all of
-// them resident), bounded: a block that waits longer than kBarrierPolls polls
-// returns false (the caller sets a status bit and leaves).  sync[0] counts
-// arrivals, sync[1] is the generation.
-__device__ bool grid_barrier(unsigned* sync) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        volatile unsigned* gen = sync + 1;
-        const unsigned g = *gen;
-        __threadfence();
-        int ok = 1;
-        if (atomicAdd(sync, 1u) == gridDim.x - 1) {
-            atomicExch(sync, 0u);
-            __threadfence();
-            atomicAdd(sync + 1, 1u);
-        } else {
-            long long n = 0;
-            while (*gen == g) {
-                if (++n > kBarrierPolls) {
-                    ok = 0;
+// Every edge in one cooperative launch (all threads resident), without
+// rounds: a thread takes its edges in ascending id order (grid stride) and
+// colours each as soon as every adjacent edge with a smaller id has a
+// colour, re-reading them with a short sleep in between.  The smallest
+// uncoloured edge never waits (its thread has finished all its smaller
+// edges), so the colouring always progresses; its critical path is the
+// longest chain of adjacent edges with increasing ids.  Each wait is bounded:
+// after kColorPolls re-reads the edge stays uncoloured and
+// SX_STATUS_WAIT_TIMEOUT is set, which makes the edges waiting on it give up
+// in turn.
+constexpr int kColorPolls = 1 << 21;
+
+__global__ void __launch_bounds__(256) color_edges_kernel(int E, const int* __restrict__ edges,
+                                                          const int* __restrict__ ptr, const int* __restrict__ inc,
+                                                          int max_colors, int* color, int* status) {
+    pdl_entry();
+    const long long stride = (long long)gridDim.x * blockDim.x;
+    for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride) {
+        int polls = 0, blocker = -1;
+        bool done = false, timed_out = false;
+        while (!done && !timed_out) {
+            done = color_try((int)e, edges, ptr, inc, max_colors, color, &blocker);
+            // wait on the neighbour that blocked, one load per poll
+            const volatile int* vb = color + blocker;
+            while (!done && *vb < 0) {
+                if (++polls > kColorPolls) {
+                    timed_out = true;
                     break;
                 }
-                __nanosleep(64);
+                __nanosleep(32);
             }
         }
-        __threadfence();
-        s_ok = ok;
+        if (timed_out) atomicOr(status, SX_STATUS_WAIT_TIMEOUT);
     }
-    __syncthreads();
-    return s_ok != 0;
-}
-
-// Every round in one cooperative launch: each thread tries its edges (grid
-// stride), blocks add the edges still uncoloured to rem[r % 3], and after the
-// barrier every block reads it; 0 ends the loop.  rem[(r + 1) % 3] is cleared
-// during round r: it was last read right after barrier r - 2, which every
-// block has left since it arrived at barrier r - 1.  E + 1 rounds bound the
-// loop (each round colours at least the smallest uncoloured edge).
-// sync = {arrivals, generation, rem[3]}, zero on entry; status bit
-// SX_STATUS_WAIT_TIMEOUT if a barrier wait or the round bound ran out.
-__global__ void __launch_bounds__(256) color_rounds_kernel(int E, const int* __restrict__ edges,
-                                                           const int* __restrict__ ptr, const int* __restrict__ inc,
-                                                           int max_colors, int* color, unsigned* sync, int max_rounds,
-                                                           int* status) {
-    pdl_entry();
-    __shared__ int s_left;
-    const long long stride = (long long)gridDim.x * blockDim.x;
-    for (int r = 0; r < max_rounds; ++r) {
-        if (threadIdx.x == 0) s_left = 0;
-        if (blockIdx.x == 0 && threadIdx.x == 0) sync[2 + (r + 1) % 3] = 0u;
-        __syncthreads();
-        int left = 0;
-        for (long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x; e < E; e += stride)
-            left += color_try((int)e, edges, ptr, inc, max_colors, color) ? 0 : 1;
-        if (left) atomicAdd(&s_left, left);
-        __syncthreads();
-        if (threadIdx.x == 0 && s_left) atomicAdd(sync + 2 + r % 3, (unsigned)s_left);
-        if (!grid_barrier(sync)) {
-            if (threadIdx.x == 0) atomicOr(status, SX_STATUS_WAIT_TIMEOUT);
-            return;
-        }
-        if (*(volatile unsigned*)(sync + 2 + r % 3) == 0u) return;
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(status, SX_STATUS_WAIT_TIMEOUT);
 }
 
 __global__ void color_hist_kernel(int E, const int* __restrict__ color, unsigned* keys, unsigned* hist) {
     pdl_entry();
     int e = blockIdx.x * blockDim.x + threadIdx.x;
     if (e >= E) return;
-    const int c = color[e];  // -1 only if the rounds stopped early (status bit set)
+    const int c = color[e];  // -1 only if a bounded wait gave up (status bit set)
     keys[e] = c < 0 ? 255u : (unsigned)c;
     if (c >= 0) atomicAdd(hist + c, 1u);
 }
@@ -182,7 +152,7 @@ __global__ void scan_excl_small(int n, int* data) {
 
 using namespace sx;
 
-// workspace: [status 1][sync 5][ptr V+1][cursor V][inc 2E][keys E][hist 128][radix ws E]
+// workspace: [status 1][unused 5][ptr V+1][cursor V][inc 2E][keys E][hist 128][radix ws E]
 extern "C" size_t sx_color_workspace_bytes(int n_verts, int n_edges) {
     size_t V = (size_t)(n_verts > 0 ? n_verts : 1), E = (size_t)(n_edges > 0 ? n_edges : 1);
     return a256(4) + a256(5 * 4) + a256((V + 1) * 4) + a256(V * 4) + a256(2 * E * 4) + a256(E * 4) +
@@ -231,7 +201,7 @@ extern "C" int sx_color_edges_greedy(const int* edges, int n_edges, int n_verts,
     const size_t V = (size_t)(n_verts > 0 ? n_verts : 1), E = (size_t)n_edges;
     char* p = (char*)ws;
     int* status = (int*)p; p += a256(4);
-    unsigned* sync = (unsigned*)p; p += a256(5 * 4);
+    p += a256(5 * 4);  // unused
     int* ptr = (int*)p; p += a256((V + 1) * 4);
     int* cursor = (int*)p; p += a256(V * 4);
     int* inc = (int*)p; p += a256(2 * E * 4);
@@ -248,9 +218,9 @@ extern "C" int sx_color_edges_greedy(const int* edges, int n_edges, int n_verts,
     launch(color_init_kernel, grid_for(n_edges, 256), 256, 0, s, n_edges, color, keys, sorted_edges);
     int rc = check_launch("colour setup");
     if (rc) return rc;
-    // all rounds in one cooperative launch (every block resident)
+    // every edge in one cooperative launch (every block resident)
     {
-        const int cap = resident_blocks(color_rounds_kernel, 256);
+        const int cap = resident_blocks(color_edges_kernel, 256);
         const int g = grid_for(n_edges, 256) < cap ? grid_for(n_edges, 256) : cap;
         cudaLaunchConfig_t cfg = {};
         cfg.gridDim = dim3(g);
@@ -261,8 +231,8 @@ extern "C" int sx_color_edges_greedy(const int* edges, int n_edges, int n_verts,
         attr[0].val.cooperative = 1;
         cfg.attrs = attr;
         cfg.numAttrs = 1;
-        SX_CUDA(cudaLaunchKernelEx(&cfg, color_rounds_kernel, n_edges, edges, (const int*)ptr, (const int*)inc,
-                                   max_colors, color, sync, n_edges + 1, status));
+        SX_CUDA(cudaLaunchKernelEx(&cfg, color_edges_kernel, n_edges, edges, (const int*)ptr, (const int*)inc,
+                                   max_colors, color, status));
         note_launch();
     }
     SX_CUDA(cudaMemsetAsync(hist, 0, 128 * 4, s));
