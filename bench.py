@@ -59,7 +59,71 @@ def parse_args():
     ap.add_argument("--only-learned", action="store_true", help="run only the learned warm-start measurement")
     ap.add_argument("--only-lbvh", action="store_true",
                     help="run only the standalone 2^20-triangle LBVH measurement (no CPU baseline)")
+    ap.add_argument("--only-gs", action="store_true",
+                    help="run only the Gauss-Seidel against Jacobi comparison (drape after 3 frames)")
+    ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES),
+                    help="run one small case of a workload for a profiler capture, print 'ok <case>' and exit "
+                         "(no timing, no JSON line)")
     return ap.parse_args()
+
+
+def _case_drape(pkg):
+    """Two frames of the 256 x 256 drape with eager launches (every kernel of a frame)."""
+    scene = pkg.scenes.drape256()
+    sim = pkg.scenes.make_solver(scene, device="cuda")
+    sim.bending_on = "y"
+    for _ in range(2):
+        sim.forward(scene.n_substeps)
+
+
+def _case_soup(pkg):
+    """The 2^20-triangle LBVH build and query, two repetitions."""
+    lbvh_soup(pkg, reps=2, with_cpu=False)
+
+
+def _batched_case_solver(pkg, n_iter):
+    insts = pkg.batched_scene(512, seed=0)
+    return pkg.BatchedSolver(insts, dHat=(4e-3) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8,
+                             g=(0.0, 0.0, -9.81), dt=1 / 60, n_iter=n_iter, padding=8e-3)
+
+
+def _case_batched(pkg):
+    """The 512-cloth batch: two frames of grid-wide launches, then one frame of
+    persistent launches (one per substep)."""
+    sim = _batched_case_solver(pkg, 20)
+    for _ in range(2):
+        sim.forward(10)
+    sim.persistent = True
+    sim.forward(10)
+
+
+def _case_color(pkg):
+    """Colouring of the 256 x 256 cloth's edges (one call)."""
+    _, f = pkg.grid_cloth(256)
+    pkg.GraphColoring(256 * 256, pkg.mesh.edges_from_faces(f), device="cuda")
+
+
+def _case_learned(pkg):
+    """One batched frame with the (untrained) warm-start network: features,
+    inference, warm start and the Jacobi loop."""
+    sim = _batched_case_solver(pkg, 4)
+    sim.warm = pkg.learned.WarmStart(sim, pkg.WarmStartMLP(seed=0))
+    sim.forward(10)
+
+
+PROFILE_CASES = {"drape": _case_drape, "soup": _case_soup, "batched": _case_batched, "color": _case_color,
+                 "learned": _case_learned}
+
+
+def run_profile_case(name):
+    import torch
+    import __graft_entry__ as ge
+
+    pkg = ge.load_package()
+    torch.cuda.set_device(0)
+    PROFILE_CASES[name](pkg)
+    torch.cuda.synchronize()
+    print("ok", name)
 
 
 def dist_setup(n_gpus):
@@ -364,24 +428,37 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
     alg = 12 * n_con + 28 * V
     peak, kind = measured_peak()
 
-    def sweep_roofline(fast):
+    def sweep_roofline(fast, packed=None):
+        """One sweep over every instance, timed alone (L2 flushed before each
+        launch, mean of 20): the int2 sweep in the tuned variant, or with
+        packed=True the packed staged sweep (None: whichever the tuner chose)."""
+        packed = sim.packed_sweep if packed is None else packed
         ev = []
         for _ in range(20):
             flush.zero_()
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
-            sx.sx_jacobi_sweep_mode(ptr(sim.x4), ptr(sim.y4), ptr(sim._y_other), ptr(sim.fixed), ptr(sim.adj_ptr),
-                                    ptr(sim.adj), V, ks, kb, 1, sim.sweep_variant, 1 if fast else 0,
-                                    stream_handle())
+            if packed:
+                sx.sx_jacobi_sweep_packed(ptr(sim.x4), ptr(sim.y4), ptr(sim._y_other), ptr(sim.fixed),
+                                          ptr(sim.adj_ptr), ptr(sim.adj_nbr16), ptr(sim.adj_rest32), V, ks, kb, 1,
+                                          1 if fast else 0, stream_handle())
+            else:
+                sx.sx_jacobi_sweep_mode(ptr(sim.x4), ptr(sim.y4), ptr(sim._y_other), ptr(sim.fixed),
+                                        ptr(sim.adj_ptr), ptr(sim.adj), V, ks, kb, 1, sim.sweep_variant,
+                                        1 if fast else 0, stream_handle())
             b.record(stream)
             ev.append((a, b))
         torch.cuda.synchronize()
         sweep_ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
-        return {"bound": "hbm", "achieved": round(alg / (sweep_ms / 1e3) / 1e9, 1), "peak": peak,
+        return {"kernel": "jacobi_sweep_staged_kernel" if packed else "jacobi_sweep_kernel", "bound": "hbm",
+                "achieved": round(alg / (sweep_ms / 1e3) / 1e9, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(alg / (sweep_ms / 1e3) / 1e9 / peak, 4),
                 "algorithmic_bytes_per_launch": alg, "avg_launch_us": round(sweep_ms * 1e3, 2), "peak_source": kind}
 
     exact_sweep = sweep_roofline(False)
+    sweeps = {"int2_exact": sweep_roofline(False, False), "int2_fast": sweep_roofline(True, False)}
+    if sim.adj_nbr16 is not None:
+        sweeps |= {"packed_exact": sweep_roofline(False, True), "packed_fast": sweep_roofline(True, True)}
     status = int(sim.status.item())
 
     def timed_frames():
@@ -434,8 +511,9 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
                                                             else ""),
             "value": value, "unit": UNIT,
             "ms_per_step": ms_job / steps, "steps": steps, "warmup": warmup,
-            "sweep_variant": sim.sweep_variant,
+            "sweep_variant": "packed" if sim.packed_sweep else sim.sweep_variant,
             "sweep_roofline": exact_sweep,
+            "sweep_rooflines": sweeps,
             "fast_math": fast,
             "persistent": persistent,
             "persistent_fast_math": persistent_fast,
@@ -488,6 +566,74 @@ def coloring_timing(pkg, reps=5, with_cpu=True):
                                        np.array_equal(srt.cpu().numpy(), s_ref))
         out[f"grid{n}"] = r
     return out
+
+
+def gauss_seidel_drape(pkg, scene, x0, v0, jacobi_iters=30, max_gs=60, reps=5):
+    """Colour-ordered Gauss-Seidel sweeps against the Jacobi sweep on the
+    256 x 256 drape: from the timed frame's state, one substep's predicted
+    positions are swept k times by each method (springs and bending pairs, no
+    contacts) and the RMS constraint violation is read after every sweep.
+    Reports the residual curves, the Gauss-Seidel sweeps needed to reach the
+    residual of `jacobi_iters` Jacobi sweeps (the drape's count), each sweep's
+    time (CUDA events over a captured graph of `jacobi_iters` sweeps, median of
+    `reps`) and the time each method takes to that residual."""
+    import torch
+
+    sim = pkg.scenes.make_solver(scene, device="cuda")
+    sim.bending_on = "y"
+    m = sim.mesh_dy
+    dt = scene.dt / scene.n_substeps
+    sim.gauss_seidel = True
+    n_colors = sim.gs_setup()[2]
+    curves = {}
+    for gs in (False, True):
+        sim.gauss_seidel = gs
+        m.x4.copy_(x0)
+        m.v4.copy_(v0)
+        sim.compute_y(dt)
+        res = [float(sim.constraint_residual("y")[2].item())]
+        for _ in range(max(jacobi_iters, max_gs)):
+            sim.spring_sweep(dt)
+            res.append(float(sim.constraint_residual("y")[2].item()))
+        curves["gauss_seidel" if gs else "jacobi"] = res
+    target = curves["jacobi"][jacobi_iters]
+    gs_curve = curves["gauss_seidel"]
+    gs_needed = next((k for k in range(len(gs_curve)) if gs_curve[k] <= target), None)
+    ms = {}
+    for gs in (False, True):
+        sim.gauss_seidel = gs
+        m.x4.copy_(x0)
+        m.v4.copy_(v0)
+        sim.compute_y(dt)
+        g = torch.cuda.CUDAGraph()
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        with torch.cuda.graph(g, stream=side):
+            for _ in range(jacobi_iters):
+                sim.spring_sweep(dt)
+        torch.cuda.current_stream().wait_stream(side)
+        ts = []
+        for _ in range(reps + 1):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record()
+            g.replay()
+            b.record()
+            torch.cuda.synchronize()
+            ts.append(a.elapsed_time(b) / jacobi_iters)
+        ms["gauss_seidel" if gs else "jacobi"] = sorted(ts[1:])[reps // 2]
+    pick = (1, 2, 5, 10, 20, 30, 60)
+    return {
+        "workload": "256x256 drape, one substep's predicted positions from the timed frame, springs + bending pairs",
+        "colours": n_colors,
+        "residual_start": curves["jacobi"][0],
+        "residual_jacobi": {str(k): curves["jacobi"][k] for k in pick if k < len(curves["jacobi"])},
+        "residual_gauss_seidel": {str(k): gs_curve[k] for k in pick if k < len(gs_curve)},
+        "target": f"residual of {jacobi_iters} Jacobi sweeps",
+        "gauss_seidel_sweeps_to_target": gs_needed,
+        "ms_per_sweep": {k: round(v, 5) for k, v in ms.items()},
+        "ms_to_target": {"jacobi": round(jacobi_iters * ms["jacobi"], 4),
+                         "gauss_seidel": round(gs_needed * ms["gauss_seidel"], 4) if gs_needed else None},
+    }
 
 
 def learned_batched(pkg, target_iters=100, train_frames=40, train_rows=65536, val_frames=40, val_rows=8192,
@@ -762,6 +908,9 @@ def run_reference(args):
 
 def main():
     args = parse_args()
+    if args.profile_case:
+        run_profile_case(args.profile_case)
+        return
     if args.impl == "reference":
         run_reference(args)
         return
@@ -781,6 +930,15 @@ def main():
     if args.only_learned:
         print(json.dumps({"learned_batched512": learned_batched(pkg)}))
         return
+    if args.only_gs:
+        sim = pkg.scenes.make_solver(scene, device="cuda")
+        sim.bending_on = "y"
+        sim.use_graph = True
+        for _ in range(3):
+            sim.forward(scene.n_substeps)
+        print(json.dumps({"gauss_seidel": gauss_seidel_drape(pkg, scene, sim.mesh_dy.x4.clone(),
+                                                             sim.mesh_dy.v4.clone())}))
+        return
     sim = pkg.scenes.make_solver(scene, device="cuda")
     sim.bending_on = "y"
     V = sim.mesh_dy.num_verts
@@ -795,7 +953,7 @@ def main():
     variant, vtimes = sim.autotune()
     from starlab_physics_gb300.autotune import variants as sweep_variants
 
-    sweep_cfg = sweep_variants()[variant]
+    sweep_cfg = ("packed", 256) if sim.packed_sweep else sweep_variants()[variant]
     from starlab_physics_gb300.autotune import pairs_project_variants
 
     pp_variants = pairs_project_variants()
@@ -886,8 +1044,12 @@ def main():
     def burst():
         for k in range(30):
             src, dst = (ya, yb) if k % 2 == 0 else (yb, ya)
-            sx.sx_jacobi_sweep_v(ptr(m.x4), ptr(src), ptr(dst), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj), V, ks_,
-                                 kb_, 1, sim.sweep_variant, stream_handle())
+            if sim.packed_sweep:
+                sx.sx_jacobi_sweep_packed(ptr(m.x4), ptr(src), ptr(dst), ptr(m.fixed), ptr(m.adj_ptr),
+                                          ptr(m.adj_nbr16), ptr(m.adj_rest32), V, ks_, kb_, 1, 0, stream_handle())
+            else:
+                sx.sx_jacobi_sweep_v(ptr(m.x4), ptr(src), ptr(dst), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj), V,
+                                     ks_, kb_, 1, sim.sweep_variant, stream_handle())
 
     side = torch.cuda.Stream()
     side.wait_stream(stream)
@@ -912,7 +1074,8 @@ def main():
     achieved = alg_bytes / (sweep_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     frame_ms = ms / args.steps
-    roofline_sweep = {"kernel": "jacobi_sweep_kernel", "bound": "hbm", "achieved": round(achieved, 1),
+    roofline_sweep = {"kernel": "jacobi_sweep_staged_kernel" if sim.packed_sweep else "jacobi_sweep_kernel",
+                "bound": "hbm", "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": ncu_traffic("jacobi_sweep_kernel_drape256.md"),
                 "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": round(sweep_ms * 1e3, 3),
@@ -1007,6 +1170,7 @@ def main():
             line["batched512"] = b512
     if rank == 0:
         line["coloring"] = coloring_timing(pkg, with_cpu=not args.no_cpu_baseline)
+        line["gauss_seidel"] = gauss_seidel_drape(pkg, scene, x0, v0)
     if rank == 0 and not args.no_learned:
         line["learned_batched512"] = learned_batched(pkg)
     if rank == 0 and world >= 1 and not args.no_cpu_baseline and world == 1:

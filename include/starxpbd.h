@@ -91,6 +91,17 @@ int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_out4, const 
 int sx_jacobi_sweep_mode(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
                          const int* adj, int n_verts, float k_spring, float k_bend, int bend_on_y, int variant,
                          int fast, void* stream);
+/* The same sweep over the packed adjacency (6 bytes per entry instead of 8):
+ * for entry k of the CSR adj_ptr, nbr16[k] = neighbour - owner (int16) and
+ * rest32[k] = bits(rest length) | 0x80000000 for a bending pair.  Both arrays
+ * are 16-byte aligned and hold at least ((adj_ptr[n_verts] + 7) & ~7) entries
+ * (the kernel reads whole 16-byte groups; padding entries are never used).
+ * Each block copies its vertices' range of entries into shared memory with
+ * coalesced streaming loads before the gather.  Results equal
+ * sx_jacobi_sweep_mode's bit for bit (fast = 0) or its fast arithmetic. */
+int sx_jacobi_sweep_packed(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
+                           const short* nbr16, const unsigned* rest32, int n_verts, float k_spring, float k_bend,
+                           int bend_on_y, int fast, void* stream);
 
 /* solve_sewing_constraints_x (XPBD.py:425-441) + update_dx over sewn vertex
  * pairs (zero rest length, k = compliance argument of the reference):
@@ -476,6 +487,27 @@ int sx_batched_obstacle_contacts(int n_verts, float* y4, const float* fixed, con
 size_t sx_color_workspace_bytes(int n_verts, int n_edges);
 int sx_color_edges_greedy(const int* edges, int n_edges, int n_verts, int max_colors, int* color, int* sorted_edges,
                           int* prefix, void* ws, size_t ws_bytes, void* stream);
+
+/* ---- colour-ordered Gauss-Seidel sweep (consumer of the colouring) ----------
+ * The reference colours its constraints for a parallel Gauss-Seidel solver it
+ * marks as work in progress (README.md:20-22, graph_coloring.py:8-97); its
+ * solver runs only the Jacobi sweep.  Springs 0..E-1 and bending pairs
+ * E..E+B-1 are coloured together as one edge list (sx_color_edges_greedy on
+ * [edges; bend]) and packed in colour order by sx_gs_pack:
+ * cons[i] = {v0, v1 | 0x80000000 for a bending pair, bits(rest length), id}
+ * for id = sorted[i]; *bad gets 1 if an id is out of range.
+ *
+ * sx_gs_sweep: one sweep, one launch per colour c over
+ * cons[colour_start[c] .. colour_start[c+1]) (colour_start: n_colors + 1 HOST
+ * ints).  Each constraint is projected on the current positions and both
+ * endpoints move at once: y0 -= (w0*ld)*n, y1 += (w1*ld)*n, with n, ld as in
+ * the Jacobi sweep (XPBD.py:141-184), w = y4.w, k = k_spring or k_bend.
+ * Constraints of one colour share no vertex, so y4 is updated in place
+ * without races and the result is independent of thread order. */
+int sx_gs_pack(const int* edges, const float* l0, int E, const int* bend, const float* bend_l0, int B,
+               const int* sorted, int* cons, int* bad, void* stream);
+int sx_gs_sweep(float* y4, const int* cons, const int* colour_start, int n_colors, float k_spring, float k_bend,
+                void* stream);
 
 /* ---- learned warm start (no counterpart in the reference) -----------------
  * The reference starts every Jacobi solve from the predicted positions

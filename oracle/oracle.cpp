@@ -1641,4 +1641,38 @@ API int or_color_edges(int V, int E, const int32_t* edges, int max_colors, int32
     return 0;
 }
 
+// Colour-ordered Gauss-Seidel sweep (the consumer the reference's colouring is
+// for, README.md:20-22; its solver has only the Jacobi sweep): serially over
+// colours and, within a colour, over cons in order.  cons[i] = {v0, v1 | bit 31
+// for a bending pair, bits(l0), id}.  The projection is the stretch step of
+// XPBD.py:141-164 evaluated on the current positions, applied at once to both
+// endpoints: y0 -= (w0*ld)*n, y1 += (w1*ld)*n with w = y4[.].w.
+API int or_gs_sweep(int n_colors, const int32_t* colour_start, const int32_t* cons, float* y4, float k_spring,
+                    float k_bend) {
+    for (int c = 0; c < n_colors; ++c) {
+        for (int i = colour_start[c]; i < colour_start[c + 1]; ++i) {
+            const int32_t* q = cons + 4 * (size_t)i;
+            const int v0 = q[0];
+            const int v1 = (int)((uint32_t)q[1] & 0x7fffffffu);
+            const float k = q[1] < 0 ? k_bend : k_spring;
+            float rest;
+            std::memcpy(&rest, &q[2], 4);
+            float* p0 = y4 + 4 * (size_t)v0;
+            float* p1 = y4 + 4 * (size_t)v1;
+            V3 x10 = sub(v3(p0), v3(p1));
+            float lij = std::sqrt(dot(x10, x10));
+            float C = lij - rest;
+            float inv = 1.0f / lij;
+            V3 n = scale(inv, x10);
+            float schur = (p0[3] + p1[3]) * dot(n, n);
+            float ld = (k * C) / (k * schur + 1.0f);
+            V3 a = sub(v3(p0), scale(p0[3] * ld, n));
+            V3 b = add(v3(p1), scale(p1[3] * ld, n));
+            p0[0] = a.x; p0[1] = a.y; p0[2] = a.z;
+            p1[0] = b.x; p1[1] = b.y; p1[2] = b.z;
+        }
+    }
+    return 0;
+}
+
 API int or_version(void) { return 1; }

@@ -57,6 +57,7 @@ _SIGS = {
     "or_edge_edge_sweep": [I, P, P, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, I],
     "or_point_triangle": [P, P, P],
     "or_color_edges": [I, I, P, I, P, P, P],
+    "or_gs_sweep": [I, P, P, P, F, F],
     "or_version": [],
 }
 
@@ -559,6 +560,34 @@ def color_edges(n_verts, edges, max_colors=100):
     return color[:E], sorted_edges[:E], prefix
 
 
+def gs_constraints(n_verts, edges, l0, bend, bend_l0, max_colors=100):
+    """Springs and bending pairs coloured together as one edge list (the
+    reference's colouring, graph_coloring.py:131-201) and packed in colour
+    order: cons[i] = (v0, v1 | bit 31 for a bending pair, bits(l0), id) for
+    id = sorted[i]; colour_start = the n_colors + 1 offsets of the colours."""
+    edges, bend = i32(edges).reshape(-1, 2), i32(bend).reshape(-1, 2)
+    E = edges.shape[0]
+    pairs = np.concatenate([edges, bend])
+    rest = np.concatenate([f32(l0), f32(bend_l0)])
+    color, order, prefix = color_edges(n_verts, pairs, max_colors)
+    n_colors = int(color.max()) + 1 if color.size else 0
+    cons = np.zeros((pairs.shape[0], 4), np.int32)
+    cons[:, 0] = pairs[order, 0]
+    cons[:, 1] = np.where(order >= E, pairs[order, 1] | np.int32(-2147483648), pairs[order, 1])
+    cons[:, 2] = rest[order].view(np.int32)
+    cons[:, 3] = order
+    start = np.append(prefix[:n_colors], pairs.shape[0]).astype(np.int32)
+    return cons, start
+
+
+def gs_sweep(y4, cons, colour_start, k_spring, k_bend):
+    """One colour-ordered Gauss-Seidel sweep over cons, in place on y4."""
+    assert y4.dtype == np.float32 and y4.flags.c_contiguous
+    start = i32(colour_start)
+    lib().or_gs_sweep(start.shape[0] - 1, _p(start), _p(i32(cons)), _p(y4), np.float32(k_spring),
+                      np.float32(k_bend))
+
+
 # ---- whole-solver driver -----------------------------------------------------
 class OracleSolver:
     """CPU restatement of ``Solver.forward`` (XPBD.py:443-469).
@@ -575,8 +604,13 @@ class OracleSolver:
                  damping=0.001, padding=0.05, n_iter=1, collisions=False, rebuild="frame", cap=40,
                  compliance_collision=1e8, nthreads=1, bending_on="x", self_collision=True,
                  contact_cull=False, tol=None, check_every=4, tol_relative=False, sewing=None,
-                 velocity_update=False, mu=0.8, edge_edge=False, scatter_atomics=False):
+                 velocity_update=False, mu=0.8, edge_edge=False, scatter_atomics=False, gauss_seidel=False):
         self.d = mesh_dy
+        # colour-ordered Gauss-Seidel sweeps instead of the Jacobi sweep (needs
+        # bending on y; the reference's solver has only the Jacobi sweep)
+        self.gauss_seidel = gauss_seidel
+        if gauss_seidel and bending_on != "y":
+            raise ValueError("Gauss-Seidel sweeps need bending_on='y'")
         # multithreaded spring sweeps: a deterministic per-vertex gather (equal
         # to the serial sweep bit for bit) unless scatter_atomics, which runs
         # the reference's scatter with float atomics (order dependent), the
@@ -633,6 +667,8 @@ class OracleSolver:
         self.bl0 = f32(mesh_dy["bend_l0"])
         self.faces = i32(mesh_dy["faces"])
         self.adj_ptr, self.adj = adjacency(V, self.edges, self.l0, self.bend, self.bl0)
+        if gauss_seidel:
+            self.gs_cons, self.gs_start = gs_constraints(V, self.edges, self.l0, self.bend, self.bl0)
         if edge_edge:
             self.face_edges = i32(mesh_dy["face_edges"])
             if mesh_st is not None:
@@ -702,7 +738,9 @@ class OracleSolver:
                         stop = it
                         self.stop_sum += it
                         self.converged += 1
-            if self.nthreads > 1 and not self.scatter_atomics:
+            if self.gauss_seidel:
+                gs_sweep(y4, self.gs_cons, self.gs_start, k_spring, k_bend)
+            elif self.nthreads > 1 and not self.scatter_atomics:
                 spring_sweep_gather(self.x4, y4, self.fixed, self.m_inv, self.adj_ptr, self.adj, k_spring, k_bend,
                                     self.nthreads, self.bend_on_y)
             else:

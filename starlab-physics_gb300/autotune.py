@@ -35,11 +35,17 @@ def variants() -> list[tuple[int, int]]:
 
 
 def _time_variant(v, args, reps, rounds):
-    x4, y4, out, fixed, adj_ptr, adj, n, ks, kb, bend_y = args
+    """v: a compiled variant of the int2 sweep, or "packed" (the sweep over the
+    packed, shared-memory-staged adjacency)."""
+    x4, y4, out, fixed, adj_ptr, adj, n, ks, kb, bend_y, packed, fast = args
 
     def run():
-        sx.sx_jacobi_sweep_v(ptr(x4), ptr(y4), ptr(out), ptr(fixed), ptr(adj_ptr), ptr(adj), n, ks, kb, bend_y, v,
-                             stream_handle())
+        if v == "packed":
+            sx.sx_jacobi_sweep_packed(ptr(x4), ptr(y4), ptr(out), ptr(fixed), ptr(adj_ptr), ptr(packed[0]),
+                                      ptr(packed[1]), n, ks, kb, bend_y, fast, stream_handle())
+        else:
+            sx.sx_jacobi_sweep_mode(ptr(x4), ptr(y4), ptr(out), ptr(fixed), ptr(adj_ptr), ptr(adj), n, ks, kb, bend_y,
+                                    v, fast, stream_handle())
 
     side = torch.cuda.Stream(device=x4.device)
     side.wait_stream(torch.cuda.current_stream(x4.device))
@@ -63,14 +69,24 @@ def _time_variant(v, args, reps, rounds):
     return float(np.median(ts))
 
 
-def tune_sweep(x4, y4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y=1, reps=20, rounds=5):
-    """Fastest sweep variant for these arrays, and the per-variant times (ms)."""
-    key = (torch.cuda.get_device_name(x4.device), int(n_verts), int(adj.shape[0]))
+def tune_sweep(x4, y4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y=1, reps=20, rounds=5, packed=None,
+               fast=False):
+    """Fastest sweep variant for these arrays, and the per-variant times (ms).
+
+    ``packed``: the (nbr16, rest32) arrays of the packed adjacency, or None;
+    when given, its staged sweep is timed as one more candidate, the last
+    entry of the times (index ``len(variants())``).  ``fast``: time the fast
+    arithmetic."""
+    if packed is not None and packed[0] is None:
+        packed = None
+    key = (torch.cuda.get_device_name(x4.device), int(n_verts), int(adj.shape[0]), packed is not None, bool(fast))
     if key in _cache:
         return _cache[key]
     out = torch.empty_like(y4)
-    args = (x4, y4, out, fixed, adj_ptr, adj, int(n_verts), float(k_spring), float(k_bend), int(bend_on_y))
-    times = [_time_variant(v, args, reps, rounds) for v in range(len(variants()))]
+    args = (x4, y4, out, fixed, adj_ptr, adj, int(n_verts), float(k_spring), float(k_bend), int(bend_on_y), packed,
+            1 if fast else 0)
+    cands = list(range(len(variants()))) + (["packed"] if packed is not None else [])
+    times = [_time_variant(v, args, reps, rounds) for v in cands]
     best = int(np.argmin(times))
     _cache[key] = (best, times)
     return best, times

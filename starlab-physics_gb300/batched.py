@@ -27,7 +27,7 @@ import torch
 
 from ._lib import load, ptr, stream_handle, sx
 from .mesh import bending_pairs, box_mesh, constraint_adjacency, edges_from_faces, grid_cloth, inverse_masses, \
-    rest_lengths
+    packed_adjacency, rest_lengths
 
 
 @dataclass
@@ -153,6 +153,8 @@ class BatchedSolver:
         self.vinst = t(np.repeat(np.arange(self.n_instances, dtype=np.int32), np.diff(self.vptr_np)))
         self.faces = t(faces.reshape(-1))
         self.adj_ptr, self.adj = t(adj_ptr), t(adj)
+        packed = packed_adjacency(adj_ptr, adj)
+        self.adj_nbr16, self.adj_rest32 = (t(packed[0]), t(packed[1])) if packed is not None else (None, None)
         self.fixed, self.m_inv = t(fixed), t(m_inv)
         self.x4 = torch.zeros((V, 4), dtype=torch.float32, device=dev)
         self.x4[:, :3] = t(x)
@@ -190,6 +192,9 @@ class BatchedSolver:
         self.warm = None
         # launch configuration of the fixed-count sweep (autotune() picks one)
         self.sweep_variant = 0
+        # the sweep over the packed, shared-memory-staged adjacency
+        # (sx_jacobi_sweep_packed; same results; autotune() decides)
+        self._packed_sweep = False
         # the sweep's fast arithmetic (Solver.fast_math)
         self.fast_math = False
         # one persistent launch per substep (sx_batched_substep) instead of a
@@ -345,6 +350,10 @@ class BatchedSolver:
                                             ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend, it,
                                             1 if check else 0, float(self.tol), ref, conv, ptr(self._res3),
                                             ptr(self._res_ws), self._res_ws.numel(), loop, self.n_iter, fast, s)
+        elif self.packed_sweep:
+            sx.sx_jacobi_sweep_packed(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
+                                      ptr(self.adj_ptr), ptr(self.adj_nbr16), ptr(self.adj_rest32), self.num_verts,
+                                      k_spring, k_bend, 1 if self.bending_on == "y" else 0, fast, s)
         else:
             sx.sx_jacobi_sweep_mode(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
                                     ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend,
@@ -379,7 +388,8 @@ class BatchedSolver:
             self._forward_eager(n_substeps)
             return
         key = (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
-               self.stiffness_bending, self.n_iter, self.bending_on, self.sweep_variant, self.fast_math, self.tol,
+               self.stiffness_bending, self.n_iter, self.bending_on, self.sweep_variant, self._packed_sweep,
+               self.fast_math, self.tol,
                self.tol_relative, self.persistent, self.persistent_variant,
                self.check_every,
                id(self.warm) if self.warm is not None else None,
@@ -404,6 +414,16 @@ class BatchedSolver:
             self._graphs[key] = gr
         gr.replay()
 
+    @property
+    def packed_sweep(self) -> bool:
+        return self._packed_sweep
+
+    @packed_sweep.setter
+    def packed_sweep(self, on: bool):
+        if on and self.adj_nbr16 is None:
+            raise ValueError("the packed adjacency needs neighbour offsets within 16 bits")
+        self._packed_sweep = bool(on)
+
     def autotune(self):
         """Solver.autotune for the concatenated instances."""
         from .autotune import tune_sweep
@@ -411,8 +431,12 @@ class BatchedSolver:
         dt = self.dt / 10
         best, times = tune_sweep(self.x4, self.y4, self.fixed, self.adj_ptr, self.adj, self.num_verts,
                                  self.stiffness_bending * dt * dt, self.stiffness_stretch * dt * dt,
-                                 1 if self.bending_on == "y" else 0)
-        self.sweep_variant = best
+                                 1 if self.bending_on == "y" else 0, packed=(self.adj_nbr16, self.adj_rest32),
+                                 fast=self.fast_math)
+        from .autotune import variants
+
+        self._packed_sweep = best == len(variants())
+        self.sweep_variant = 0 if self._packed_sweep else best
         return best, times
 
     def autotune_persistent(self, reps: int = 3):

@@ -455,6 +455,85 @@ extern "C" int sx_jacobi_sweep_mode(const float* x4, const float* y_in4, float* 
     return check_launch("jacobi_sweep_kernel");
 }
 
+// ---------------------------------------------------------------------------
+// The sweep over the packed CSR (6 bytes per entry: int16 neighbour offset,
+// rest-length bits with the bending flag in bit 31), with the block's range of
+// entries staged in shared memory.  A block of BLOCK vertices reads the
+// entries [ptr[v0], ptr[v0 + BLOCK]) widened to 16-byte boundaries with
+// coalesced 16-byte streaming loads (L2 evict-first, so that the positions,
+// which neighbouring blocks gather again, stay in L2), then every thread walks
+// its own entries in shared memory.  A block whose range exceeds CAP entries
+// reads its entries from global memory instead.  The projection is the same
+// code as the int2 sweep (sweep_vertex_src), so results are bit-identical.
+namespace sx {
+constexpr int kStagedCap = 4096;  // entries per block: 16 KB rest bits + 8 KB offsets
+
+template <int BLOCK, bool BY, bool FAST>
+__global__ void __launch_bounds__(BLOCK) jacobi_sweep_staged_kernel(int V, const float4* __restrict__ x4,
+                                                                       const float4* __restrict__ yin,
+                                                                       float4* __restrict__ yout,
+                                                                       const float* __restrict__ fixed,
+                                                                       const int* __restrict__ ptr,
+                                                                       const short* __restrict__ nbr16,
+                                                                       const unsigned* __restrict__ rest32,
+                                                                       float ks, float kb, int bend_y) {
+    __shared__ __align__(16) unsigned s_rest[kStagedCap];
+    __shared__ __align__(16) short s_nbr[kStagedCap];
+    pdl_entry();
+    const int ntiles = (V + BLOCK - 1) / BLOCK;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const int v0 = tile * BLOCK;
+        const int v1 = min(v0 + BLOCK, V);
+        const int e0 = __ldg(ptr + v0), e1 = __ldg(ptr + v1);
+        const int a0 = e0 & ~7, a1 = (e1 + 7) & ~7;  // 8 entries = 16 B of offsets, 32 B of rest bits
+        const bool staged = a1 - a0 <= kStagedCap;
+        if (staged) {
+            const uint4* gr = reinterpret_cast<const uint4*>(rest32 + a0);
+            const uint4* gn = reinterpret_cast<const uint4*>(nbr16 + a0);
+            uint4* sr = reinterpret_cast<uint4*>(s_rest);
+            uint4* sn = reinterpret_cast<uint4*>(s_nbr);
+            const int nr = (a1 - a0) >> 2, nn = (a1 - a0) >> 3;
+            for (int i = threadIdx.x; i < nr; i += BLOCK) sr[i] = __ldcs(gr + i);
+            for (int i = threadIdx.x; i < nn; i += BLOCK) sn[i] = __ldcs(gn + i);
+        }
+        __syncthreads();
+        const int v = v0 + threadIdx.x;
+        if (v < V) {
+            const int b = __ldg(ptr + v), e = __ldg(ptr + v + 1);
+            float c2 = 0.0f;
+            yout[v] = staged ? sweep_vertex_src<2, BY, FAST, false, true>(v, x4, yin, fixed, b, e,
+                                                                          AdjPacked{s_nbr, s_rest, a0}, ks, kb,
+                                                                          bend_y, &c2)
+                             : sweep_vertex_src<2, BY, FAST, false, true>(v, x4, yin, fixed, b, e,
+                                                                          AdjPacked{nbr16, rest32, 0}, ks, kb,
+                                                                          bend_y, &c2);
+        }
+        __syncthreads();
+    }
+}
+}  // namespace sx
+
+extern "C" int sx_jacobi_sweep_packed(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                                      const int* adj_ptr, const short* nbr16, const unsigned* rest32, int n_verts,
+                                      float k_spring, float k_bend, int bend_on_y, int fast, void* stream) {
+    SX_REQUIRE(n_verts >= 0, "sx_jacobi_sweep_packed: n_verts < 0");
+    if (n_verts == 0) return SX_OK;
+    SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && nbr16 && rest32, "sx_jacobi_sweep_packed: null pointer");
+    SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_packed: y_in4 and y_out4 must not alias");
+    SX_REQUIRE(((uintptr_t)nbr16 & 15) == 0 && ((uintptr_t)rest32 & 15) == 0,
+               "sx_jacobi_sweep_packed: nbr16 and rest32 must be 16-byte aligned");
+    using K = void (*)(int, const float4*, const float4*, float4*, const float*, const int*, const short*,
+                       const unsigned*, float, float, int);
+    const K k = fast ? (bend_on_y ? jacobi_sweep_staged_kernel<SW_BLOCK, true, true>
+                                  : jacobi_sweep_staged_kernel<SW_BLOCK, false, true>)
+                     : (bend_on_y ? jacobi_sweep_staged_kernel<SW_BLOCK, true, false>
+                                  : jacobi_sweep_staged_kernel<SW_BLOCK, false, false>);
+    launch(k, sweep_blocks(n_verts), SW_BLOCK, 0, as_stream(stream), n_verts, (const float4*)x4,
+           (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, nbr16, rest32, k_spring, k_bend,
+           bend_on_y ? 1 : 0);
+    return check_launch("jacobi_sweep_staged_kernel");
+}
+
 extern "C" int sx_sewing_sweep(float* y4, const float* fixed, int n_sewn, const int* sewn, const int* sptr,
                                const int* partner, float k, float* scratch4, void* stream) {
     SX_REQUIRE(n_sewn >= 0, "sx_sewing_sweep: n_sewn < 0");

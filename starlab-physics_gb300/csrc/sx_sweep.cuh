@@ -27,19 +27,37 @@ __device__ __forceinline__ float4 load_y(const float4* p) {
     return *p;
 }
 
-template <int G, bool BY, bool FAST, bool CHECK, bool YLDG>
-__device__ __forceinline__ float4 sweep_vertex(int v, const float4* __restrict__ x4, const float4* yin,
-                                               const float* __restrict__ fixed, const int* __restrict__ ptr,
-                                               const int2* __restrict__ adj, float ks, float kb, int bend_y,
-                                               float* c2) {
+// Entry sources: entry k of vertex v's list as the adjacency word
+// (neighbour | bit 31 for a bending pair, bits(rest length)).
+struct AdjInt2 {  // the CSR of int2 entries
+    const int2* __restrict__ adj;
+    __device__ __forceinline__ int2 operator()(int, int k) const { return __ldg(adj + k); }
+};
+// The packed CSR: nbr16[k] = neighbour - v, rest32[k] = bits(rest length) with
+// bit 31 set for a bending pair (6 bytes per entry instead of 8), read from a
+// shared-memory copy of the block's range [a0, a0 + n) when staged, else from
+// global memory.
+struct AdjPacked {
+    const short* nbr;
+    const unsigned* rest;
+    int a0;
+    __device__ __forceinline__ int2 operator()(int v, int k) const {
+        const unsigned r = rest[k - a0];
+        return make_int2((v + (int)nbr[k - a0]) | (int)(r & 0x80000000u), (int)(r & 0x7fffffffu));
+    }
+};
+
+template <int G, bool BY, bool FAST, bool CHECK, bool YLDG, typename Src>
+__device__ __forceinline__ float4 sweep_vertex_src(int v, const float4* __restrict__ x4, const float4* yin,
+                                                   const float* __restrict__ fixed, int b, int e, const Src& src,
+                                                   float ks, float kb, int bend_y, float* c2) {
     const float4 ps = load_y<YLDG>(yin + v), xs = __ldg(x4 + v);
-    const int b = __ldg(ptr + v), e = __ldg(ptr + v + 1);
     float dx = 0.0f, dy = 0.0f, dz = 0.0f;
     for (int k0 = b; k0 < e; k0 += G) {
         int2 a[G];
         float4 o[G];
 #pragma unroll
-        for (int g = 0; g < G; ++g) a[g] = k0 + g < e ? __ldg(adj + k0 + g) : make_int2(0, 0);
+        for (int g = 0; g < G; ++g) a[g] = k0 + g < e ? src(v, k0 + g) : make_int2(0, 0);
 #pragma unroll
         for (int g = 0; g < G; ++g) {
             const bool use_x = !BY && a[g].x < 0 && !bend_y;
@@ -96,6 +114,15 @@ __device__ __forceinline__ float4 sweep_vertex(int v, const float4* __restrict__
         }
     }
     return out;
+}
+
+template <int G, bool BY, bool FAST, bool CHECK, bool YLDG>
+__device__ __forceinline__ float4 sweep_vertex(int v, const float4* __restrict__ x4, const float4* yin,
+                                               const float* __restrict__ fixed, const int* __restrict__ ptr,
+                                               const int2* __restrict__ adj, float ks, float kb, int bend_y,
+                                               float* c2) {
+    return sweep_vertex_src<G, BY, FAST, CHECK, YLDG>(v, x4, yin, fixed, __ldg(ptr + v), __ldg(ptr + v + 1),
+                                                      AdjInt2{adj}, ks, kb, bend_y, c2);
 }
 
 }  // namespace sx

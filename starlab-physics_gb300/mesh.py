@@ -259,6 +259,28 @@ def constraint_adjacency(n_verts: int, edges: np.ndarray, l0: np.ndarray,
     return ptr, adj
 
 
+def packed_adjacency(ptr: np.ndarray, adj: np.ndarray):
+    """The packed form of :func:`constraint_adjacency` for ``sx_jacobi_sweep_packed``:
+    ``nbr16[k] = neighbour - owner`` (int16) and ``rest32[k] = bits(l0)`` with
+    bit 31 set for a bending pair, both padded with zeros to a multiple of 8
+    entries plus 8 (the kernel reads whole 16-byte groups).  None when an
+    offset does not fit in 16 bits (the int2 sweep then serves)."""
+    ptr = np.asarray(ptr, np.int64)
+    adj = np.asarray(adj, np.int32).reshape(-1, 2)
+    n = adj.shape[0]
+    owner = np.repeat(np.arange(ptr.shape[0] - 1, dtype=np.int64), np.diff(ptr))
+    word = adj[:, 0].view(np.uint32)
+    delta = (word & np.uint32(0x7FFFFFFF)).astype(np.int64) - owner
+    if n and (delta.min() < -32768 or delta.max() > 32767):
+        return None
+    size = ((n + 7) // 8) * 8 + 8
+    nbr16 = np.zeros(size, np.int16)
+    rest32 = np.zeros(size, np.uint32)
+    nbr16[:n] = delta.astype(np.int16)
+    rest32[:n] = adj[:, 1].view(np.uint32) | (word & np.uint32(0x80000000))
+    return nbr16, rest32.view(np.int32)
+
+
 class _Verts:
     """Attribute bag mirroring ``mesh.verts.{x,y,v,fixed,m_inv}``."""
 
@@ -315,6 +337,8 @@ class TriMesh:
         self.bending_l0 = t(bend_l0)
         self.adj_ptr = t(ptr)
         self.adj = t(adj)
+        packed = packed_adjacency(ptr, adj)
+        self.adj_nbr16, self.adj_rest32 = (t(packed[0]), t(packed[1])) if packed is not None else (None, None)
 
         V = self.num_verts
         self.x4 = torch.zeros((V, 4), dtype=torch.float32, device=dev)

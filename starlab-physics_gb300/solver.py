@@ -52,6 +52,14 @@ Options beyond the reference (keyword-only, defaults reproduce the reference):
   (``sx_jacobi_sweep_mode``: fused multiply-adds, the hardware reciprocal
   square root): within float rounding of the exact sweep, held to the
   substep's position and residual tolerance instead of bit-equality.
+* ``gauss_seidel`` (attribute, default off) -- replace the Jacobi spring /
+  bending sweep by a colour-ordered Gauss-Seidel sweep (``sx_gs_sweep``): the
+  springs and bending pairs are coloured together once
+  (``sx_color_edges_greedy``, the reference's colouring,
+  ``graph_coloring.py:131-201``) and each colour is projected in place, one
+  launch per colour.  This is the parallel Gauss-Seidel path the reference's
+  colouring is meant for and which its README marks as work in progress;
+  needs ``bending_on="y"`` and a fixed iteration count.
 
 Reference quirks kept on purpose: the stretch springs use
 ``stiffness_bending * dt^2`` and the bending pairs ``stiffness_stretch * dt^2``
@@ -103,6 +111,9 @@ class Solver:
         # within float rounding of the exact sweep, held to the substep's
         # position and residual tolerance rather than bit-equality
         self.fast_math = False
+        # colour-ordered Gauss-Seidel sweeps instead of the Jacobi sweep
+        self.gauss_seidel = False
+        self._gs = None  # (cons, colour_start as a host int array, n_colors)
         # edge-edge contacts (__ee_st / __ee_dy; commented out in the
         # reference's solver, so off by default)
         self.enable_edge_edge = False
@@ -110,6 +121,7 @@ class Solver:
         self._sewing = None  # (sewn, sptr, partner, scratch, stiffness)
         # launch configuration of the fixed-count sweep (autotune() picks one)
         self.sweep_variant = 0
+        self._packed_sweep = False
         # launch configuration of the contact-pair projection (None: the
         # library's default, sx_contact_pairs_project_variant_info lists all)
         self.pairs_variant = None
@@ -194,7 +206,15 @@ class Solver:
         k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
         k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355
         fast = 1 if self.fast_math else 0
-        if self.tol is None:
+        if self.gauss_seidel:
+            cons, start, n_colors = self.gs_setup()
+            sx.sx_gs_sweep(ptr(m.y4), ptr(cons), start, n_colors, k_spring, k_bend, stream_handle())
+            return
+        if self.tol is None and self._packed_sweep:
+            sx.sx_jacobi_sweep_packed(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
+                                      ptr(m.adj_nbr16), ptr(m.adj_rest32), m.num_verts, k_spring, k_bend,
+                                      1 if self.bending_on == "y" else 0, fast, stream_handle())
+        elif self.tol is None:
             sx.sx_jacobi_sweep_mode(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
                                     ptr(m.adj), m.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0,
                                     self.sweep_variant, fast, stream_handle())
@@ -206,6 +226,33 @@ class Solver:
                                             ptr(self._conv), ptr(self._res3), ptr(self._res_ws), self._res_ws.numel(),
                                             loop, self.n_iter, fast, stream_handle())
         self._swap_y()
+
+    def gs_setup(self):
+        """Colour the springs and bending pairs together and pack them in
+        colour order for the Gauss-Seidel sweep (once per mesh; synchronises
+        the host to read the colour offsets, so it runs outside any graph
+        capture).  Returns (cons, host colour offsets, number of colours)."""
+        if self._gs is not None:
+            return self._gs
+        if self.bending_on != "y":
+            raise ValueError("Gauss-Seidel sweeps need bending_on='y'")
+        from .coloring import GraphColoring
+
+        m = self.mesh_dy
+        E, B = m.num_edges, m.bending_constraint_count
+        pairs = torch.cat([m.edge_indices.view(-1, 2), m.bending_indices.view(-1, 2)]).to(torch.int32).contiguous()
+        gc = GraphColoring(m.num_verts, pairs, device=self.device)
+        cons = torch.empty((max(E + B, 1), 4), dtype=torch.int32, device=self.device)
+        bad = torch.zeros(1, dtype=torch.int32, device=self.device)
+        sx.sx_gs_pack(ptr(m.edge_indices), ptr(m.l0), E, ptr(m.bending_indices), ptr(m.bending_l0), B,
+                      ptr(gc.sorted_edges_sequence_for_color), ptr(cons), ptr(bad), stream_handle())
+        n_colors = int(gc.edges_color[:E + B].max().item()) + 1 if E + B else 0
+        offs = gc.color_prefix_sum[:n_colors].cpu().tolist() + [E + B]
+        if int(bad.item()):
+            raise RuntimeError("sx_gs_pack: constraint id out of range")
+        self._gs = (cons, (C.c_int * len(offs))(*offs), n_colors)
+        self.gs_colouring = gc
+        return self._gs
 
     def _swap_y(self):
         m = self.mesh_dy
@@ -447,6 +494,8 @@ class Solver:
         replayed on later calls; results are identical to the eager path."""
         if self.enable_edge_edge and self.enable_collision_handling:
             self._ensure_ee()  # allocated outside any capture
+        if self.gauss_seidel:
+            self.gs_setup()  # colours read back outside any capture
         if not self.use_graph:
             self._forward_eager(n_substeps)
             return
@@ -467,11 +516,29 @@ class Solver:
         m = self.mesh_dy
         dt = self.dt / 10
         best, times = tune_sweep(m.x4, m.y4, m.fixed, m.adj_ptr, m.adj, m.num_verts, self.stiffness_bending * dt * dt,
-                                 self.stiffness_stretch * dt * dt, 1 if self.bending_on == "y" else 0)
-        self.sweep_variant = best
+                                 self.stiffness_stretch * dt * dt, 1 if self.bending_on == "y" else 0,
+                                 packed=(m.adj_nbr16, m.adj_rest32), fast=self.fast_math)
+        from .autotune import variants
+
+        self._packed_sweep = best == len(variants())
+        self.sweep_variant = 0 if self._packed_sweep else best
         return best, times
 
+    @property
+    def packed_sweep(self) -> bool:
+        """The fixed-count sweep runs over the packed, shared-memory-staged
+        adjacency (``sx_jacobi_sweep_packed``; identical results)."""
+        return self._packed_sweep
+
+    @packed_sweep.setter
+    def packed_sweep(self, on: bool):
+        if on and self.mesh_dy.adj_nbr16 is None:
+            raise ValueError("the packed adjacency needs neighbour offsets within 16 bits")
+        self._packed_sweep = bool(on)
+
     def _check_tol_mode(self):
+        if self.gauss_seidel:
+            raise ValueError("iterating to a tolerance runs the Jacobi sweep (gauss_seidel must be off)")
         if self._sewing is not None:
             raise ValueError("iterating to a tolerance does not support sewing pairs")
         if self.bending_on != "y":
@@ -509,7 +576,7 @@ class Solver:
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
                 self.compliance_collision, self.self_collision, self.contact_cull, self.fast_math,
-                self.sweep_variant,
+                self.gauss_seidel, self.sweep_variant, self._packed_sweep,
                 self.pairs_variant, self.enable_edge_edge,
                 self.enable_velocity_update, self.mu, self.tol,
                 self.tol_relative,

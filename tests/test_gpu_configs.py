@@ -182,13 +182,15 @@ def test_fast_math_within_tolerance(pkg, po):
     square root; not bit-identical) against the exact oracle over the stated
     horizon of 60 substeps: the 64 x 64 box scene after 10 exact frames
     (falling), the drape after 3 (on the sphere, self contact) and four batched
-    instances after 10 (some on their boxes).  Positions stay within 1e-4 x the
-    bounding-box diagonal and the residual within 1 %, and differ from the
-    exact run (the fast kernels ran).  Not from the box scene's contact phase:
-    there the vertices on the box's top edges have more candidates than the
-    reference's 40 slots, which candidates survive the truncation flips with
-    the last bit of a position, and any change of rounding (the reference's own
-    float atomics included) moves the cloth by centimetres within 60 substeps."""
+    instances after 8 (instance 78, the one with the highest box, lands on it
+    within the window).  Positions stay within 1e-4 x the bounding-box diagonal
+    and the residual within 1 %, and differ from the exact run (the fast
+    kernels ran).  Only over windows where no query overflows the reference's
+    40 candidate slots (asserted through the oracle's status): there which
+    candidates survive the truncation flips with the last bit of a position,
+    and any change of rounding (the reference's own float atomics included)
+    moves the cloth by centimetres within 60 substeps -- the box scene's
+    contact phase, and instance 78 from its 14th frame on."""
     from starlab_physics_gb300 import mesh as M
 
     for scene, warm in ((pkg.scenes.plain64(), 10), (pkg.scenes.drape256(), 3)):
@@ -215,17 +217,18 @@ def test_fast_math_within_tolerance(pkg, po):
     bs = pkg.BatchedSolver(insts, dHat=kw["dHat"], stiffness_stretch=1e5, stiffness_bending=1e8, g=kw["g"],
                            dt=kw["dt"], n_iter=20, padding=8e-3)
     bs.use_graph = True
-    for _ in range(10):
+    for _ in range(8):
         bs.forward(10)
     torch.cuda.synchronize()
-    x10, v10 = _np(bs.x4).copy(), _np(bs.v4).copy()
+    x8, v8 = _np(bs.x4).copy(), _np(bs.v4).copy()
     bs.fast_math = True
     for _ in range(6):
         bs.forward(10)
     torch.cuda.synchronize()
     sides = np.array([int(round(np.sqrt(i.x.shape[0]))) for i in insts])
     box_top = np.array([float(i.obstacle_x[:, 2].max()) for i in insts])
-    for i in (int(np.argmin(sides)), int(np.argmax(sides)), int(np.argmax(box_top)), 100):
+    assert int(np.argmax(box_top)) == 78
+    for i in (int(np.argmin(sides)), int(np.argmax(sides)), 78, 100):
         inst = insts[i]
         cl = M.TriMesh(inst.x, inst.faces, device="cpu")
         cl.fixed[np.asarray(inst.pinned)] = 0.0
@@ -233,10 +236,14 @@ def test_fast_math_within_tolerance(pkg, po):
         o = po.OracleSolver(pkg.scenes.oracle_inputs(cl), pkg.scenes.oracle_inputs(ob), collisions=True,
                             rebuild="substep", self_collision=False, bending_on="y", nthreads=NTHREADS, **kw)
         a, b = bs.vptr_np[i], bs.vptr_np[i + 1]
-        o.x4[:] = x10[a:b]
-        o.v4[:] = v10[a:b]
+        o.x4[:] = x8[a:b]
+        o.v4[:] = v8[a:b]
+        o.last_status = 0
         for _ in range(6):
             o.forward(10)
+        assert o.last_status & 1 == 0, f"instance {i}: a query overflowed the candidate slots"
+        if i == 78:
+            assert o.x4[:, 2].min() < box_top[i], "instance 78 reached its box"
         g4 = np.zeros_like(o.x4)
         g4[:, :3] = _np(bs.instance_positions(i))
         g4[:, 3] = o.x4[:, 3]
