@@ -493,6 +493,7 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
     blk, bps = C.c_int(0), C.c_int(0)
     _load().sx_batched_substep_variant_info(pv, C.addressof(blk), C.addressof(bps))
     persistent = timed_frames() | {"launch": {"threads_per_cta": blk.value, "ctas_per_sm": bps.value,
+                                              "ctas_per_instance": int(_load().sx_batched_substep_variant_cluster(pv)),
                                               "picked_by": "autotuner (fastest of %d identical variants, one "
                                                            "substep each)" % len(ptimes)}}
     sim.fast_math = True

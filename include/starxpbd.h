@@ -391,8 +391,9 @@ int sx_edge_edge_classify(int n, const float* p12, float dHat, int* dtype, float
 
 /* Persistent batched substep (no counterpart in the reference, whose batching
  * is mesh concatenation, framework/meshio/concat.py:11-58): one launch runs a
- * whole substep of every instance of a batch.  Each CTA takes instances from
- * a queue in the order `order` (largest first), and for its instance alone
+ * whole substep of every instance of a batch.  Each CTA (or, in the cluster
+ * variants, each thread-block cluster) takes instances from a queue in the
+ * order `order` (largest first), and for its instance alone
  * computes the cloth box (sx_segment_aabbs) and padded face boxes on x, with
  * predict != 0 the prediction y = compute_y(x, v) (sx_predict; 0: y already
  * holds the start, e.g. a learned warm start), n_iter Jacobi iterations --
@@ -400,20 +401,23 @@ int sx_edge_edge_classify(int n, const float* p12, float dHat, int* dtype, float
  * `fast`), in the first iteration the obstacle broad phase
  * (sx_batched_obstacle_broadphase), then the obstacle contacts and update_dx
  * (sx_batched_obstacle_contacts) -- and the velocity update
- * (sx_velocity_update), with block barriers between the phases.  y and
+ * (sx_velocity_update), with block (cluster) barriers between the phases.  y and
  * y_other ping-pong: after an even n_iter the final positions are in y, after
  * an odd one in y_other.  The result equals those grid-wide launches bit for
  * bit.  Chunk boxes are per instance: cmin4 / cmax4 hold cptr[n_inst] boxes,
  * instance i's chunks of 32 faces at cptr[i] .. cptr[i+1].  queue: two ints,
  * zero before the first launch and left zero by every launch.  Fixed
  * iteration counts only (iterating to a residual uses the grid-wide
- * launches). */
+ * launches).  adj_nbr16 / adj_rest32: the packed adjacency
+ * (sx_jacobi_sweep_packed) or both null. */
 typedef struct SxBatchedSubstep {
     int n_inst, n_iter, predict, cap;
     const int *order, *vptr, *fptr, *cptr, *optr, *ob_fptr;
     float *x4, *y4, *y_other4, *v4;
     const float *fixed, *m_inv;
     const int *adj_ptr, *adj;
+    const short* adj_nbr16;      /* the packed adjacency (sx_jacobi_sweep_packed), or */
+    const unsigned* adj_rest32;  /* null: the sweep then reads adj                    */
     const int *faces, *ob_faces;
     const float* xs4;
     float *fmin4, *fmax4, *cmin4, *cmax4, *cl_box6;
@@ -426,6 +430,11 @@ typedef struct SxBatchedSubstep {
 } SxBatchedSubstep;
 int sx_batched_substep_variants(void);
 int sx_batched_substep_variant_info(int variant, int* block, int* blocks_per_sm);
+/* CTAs per instance of a variant: 1 = an instance per CTA (block barriers);
+ * more = an instance per thread-block cluster of that many CTAs (hardware
+ * cluster barriers; fewer instances in flight, so their working set stays in
+ * L2 across the iterations).  Results are identical for every variant. */
+int sx_batched_substep_variant_cluster(int variant);
 int sx_batched_substep(const SxBatchedSubstep* args, int variant, int fast, void* stream);
 
 /* solve_constraints_v (XPBD.py:374-381, :398-404; collision_constraints_v.py

@@ -34,9 +34,9 @@ class SxBatchedSubstep(C.Structure):
 
     _fields_ = [(n, I) for n in ("n_inst", "n_iter", "predict", "cap")] + \
                [(n, P) for n in ("order", "vptr", "fptr", "cptr", "optr", "ob_fptr", "x4", "y4", "y_other4", "v4",
-                                 "fixed", "m_inv", "adj_ptr", "adj", "faces", "ob_faces", "xs4", "fmin4", "fmax4",
-                                 "cmin4", "cmax4", "cl_box6", "ob_box6", "ob_fmin4", "ob_fmax4", "vmask", "tv_cand",
-                                 "tv_num", "dx_fix", "nc", "status", "queue")] + \
+                                 "fixed", "m_inv", "adj_ptr", "adj", "adj_nbr16", "adj_rest32", "faces", "ob_faces",
+                                 "xs4", "fmin4", "fmax4", "cmin4", "cmax4", "cl_box6", "ob_box6", "ob_fmin4",
+                                 "ob_fmax4", "vmask", "tv_cand", "tv_num", "dx_fix", "nc", "status", "queue")] + \
                [(n, F) for n in ("padding", "dt", "gx", "gy", "gz", "k_spring", "k_bend", "dHat", "compliance",
                                  "damping")]
 
@@ -92,6 +92,7 @@ SIGNATURES = {
     "sx_contact_pairs_project_v": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, I, P], I),
     "sx_contact_apply": ([I, P, P, P, P, P, I, P], I),
     "sx_batched_substep_variants": ([], I),
+    "sx_batched_substep_variant_cluster": ([I], I),
     "sx_batched_substep_variant_info": ([I, P, P], I),
     "sx_batched_substep": ([P, I, I, P], I),
     "sx_edge_edge_sweep": ([I, P, P, P, P, P, P, P, P, F, F, I, P, P, P, P, P, P, P, P, P, P, P, P, I, P], I),
@@ -183,7 +184,8 @@ class _Calls:
         if SIGNATURES[name][1] is I and name not in ("sx_version", "sx_mlp_param_count", "sx_mlp_bf16_count",
                                                      "sx_jacobi_sweep_variants",
                                                      "sx_contact_pairs_project_variants",
-                                                     "sx_batched_substep_variants"):
+                                                     "sx_batched_substep_variants",
+                                                     "sx_batched_substep_variant_cluster"):
             return lambda *a: _call(name, *a)
         return getattr(load(), name)
 

@@ -260,6 +260,8 @@ class BatchedSolver:
                           ("tv_num", self.tv_num), ("dx_fix", self._dx_fix), ("nc", self._nc),
                           ("status", self.status), ("queue", self._p_queue)):
             setattr(a, name, ptr(tns))
+        if self._packed_sweep:
+            a.adj_nbr16, a.adj_rest32 = ptr(self.adj_nbr16), ptr(self.adj_rest32)
         a.padding, a.dt, a.gx, a.gy, a.gz = self.padding, float(dt), g[0], g[1], g[2]
         a.k_spring = self.stiffness_bending * dt * dt  # XPBD.py:354
         a.k_bend = self.stiffness_stretch * dt * dt    # XPBD.py:355

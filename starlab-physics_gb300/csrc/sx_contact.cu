@@ -1030,6 +1030,8 @@ struct BatchedSubstepArgs {
     const float *fixed, *m_inv;
     const int* adj_ptr;
     const int2* adj;
+    const short* nbr16;      // packed adjacency, or null
+    const unsigned* rest32;
     const int *faces, *ob_faces;
     const float4* xs4;
     float4 *fmin4, *fmax4, *cmin4, *cmax4;
@@ -1044,42 +1046,102 @@ struct BatchedSubstepArgs {
     float pad, dt, gx, gy, gz, ks, kb, dHat, compliance, damping;
 };
 
-template <int BLOCK, int MINB, bool FAST>
+// Cluster plumbing of the persistent substep: with CL > 1 an instance is
+// processed by a thread-block cluster of CL CTAs (one instance per cluster
+// instead of per CTA, so CL times fewer instances are in flight and their
+// positions and adjacency stay in L2 across the iterations).  The phases are
+// separated by the hardware cluster barrier (release / acquire at cluster
+// scope, so global writes of one CTA are visible to the others after it);
+// the instance index and the cloth box live in the leader CTA's shared
+// memory and are reached through distributed shared memory.
+template <int CL>
+__device__ __forceinline__ void inst_sync() {
+    if constexpr (CL == 1) {
+        __syncthreads();
+    } else {
+        asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
+    }
+}
+__device__ __forceinline__ unsigned cluster_rank() {
+    unsigned r;
+    asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+    return r;
+}
+// shared::cluster address of `p` (this CTA's shared memory) in CTA `rank`
+__device__ __forceinline__ unsigned leader_addr(const void* p, unsigned rank) {
+    unsigned r;
+    asm volatile("mapa.shared::cluster.u32 %0, %1, %2;"
+                 : "=r"(r)
+                 : "r"((unsigned)__cvta_generic_to_shared(p)), "r"(rank));
+    return r;
+}
+__device__ __forceinline__ int ld_cluster_s32(unsigned addr) {
+    int v;
+    asm volatile("ld.shared::cluster.s32 %0, [%1];" : "=r"(v) : "r"(addr) : "memory");
+    return v;
+}
+__device__ __forceinline__ void red_cluster_min(unsigned addr, unsigned v) {
+    asm volatile("red.shared::cluster.min.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_cluster_max(unsigned addr, unsigned v) {
+    asm volatile("red.shared::cluster.max.u32 [%0], %1;" ::"r"(addr), "r"(v) : "memory");
+}
+
+template <int BLOCK, int MINB, int CL, bool FAST>
 __global__ void __launch_bounds__(BLOCK, MINB) batched_substep_kernel(BatchedSubstepArgs A) {
     pdl_entry();
     constexpr int NW = BLOCK / 32;
+    constexpr int STRIDE = CL * BLOCK;  // threads working on one instance
+    constexpr int NWI = CL * NW;        // warps working on one instance
     __shared__ int s_inst;
     __shared__ unsigned s_box[6];
     const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const unsigned rank = CL == 1 ? 0u : cluster_rank();
+    const int gtid = (int)rank * BLOCK + tid, gwarp = (int)rank * NW + warp;
     int bad = 0, overflow = 0;
     for (;;) {
-        __syncthreads();
-        if (tid == 0) {
-            const int k = atomicAdd(A.queue, 1);
-            s_inst = k < A.n_inst ? A.order[k] : -1;
+        inst_sync<CL>();
+        if (rank == 0) {
+            if (tid == 0) {
+                const int k = atomicAdd(A.queue, 1);
+                s_inst = k < A.n_inst ? A.order[k] : -1;
+            }
+            if (tid < 6) s_box[tid] = tid < 3 ? f2ord_c(1e5f) : f2ord_c(-1e5f);
         }
-        if (tid < 6) s_box[tid] = tid < 3 ? f2ord_c(1e5f) : f2ord_c(-1e5f);
-        __syncthreads();
-        const int i = s_inst;
+        inst_sync<CL>();
+        const int i = CL == 1 ? s_inst : ld_cluster_s32(leader_addr(&s_inst, 0));
         if (i < 0) break;
         const int v0 = A.vptr[i], v1 = A.vptr[i + 1], f0 = A.fptr[i], f1 = A.fptr[i + 1], c0 = A.cptr[i];
         const int o0 = A.optr[i], o1 = A.optr[i + 1];
         // the cloth box on x (segment_aabb_kernel) ...
         {
             float lo[3] = {1e5f, 1e5f, 1e5f}, hi[3] = {-1e5f, -1e5f, -1e5f};
-            for (int v = v0 + tid; v < v1; v += BLOCK) {
+            for (int v = v0 + gtid; v < v1; v += STRIDE) {
                 const float4 p = A.x4[v];
                 lo[0] = fminf(lo[0], p.x); lo[1] = fminf(lo[1], p.y); lo[2] = fminf(lo[2], p.z);
                 hi[0] = fmaxf(hi[0], p.x); hi[1] = fmaxf(hi[1], p.y); hi[2] = fmaxf(hi[2], p.z);
             }
             for (int k = 0; k < 3; ++k) {
-                atomicMin(s_box + k, f2ord_c(lo[k]));
-                atomicMax(s_box + 3 + k, f2ord_c(hi[k]));
+                for (int o = 16; o > 0; o >>= 1) {
+                    lo[k] = fminf(lo[k], __shfl_xor_sync(0xffffffffu, lo[k], o));
+                    hi[k] = fmaxf(hi[k], __shfl_xor_sync(0xffffffffu, hi[k], o));
+                }
+            }
+            if (lane == 0) {
+                for (int k = 0; k < 3; ++k) {
+                    if (CL == 1) {
+                        atomicMin(s_box + k, f2ord_c(lo[k]));
+                        atomicMax(s_box + 3 + k, f2ord_c(hi[k]));
+                    } else {
+                        red_cluster_min(leader_addr(s_box + k, 0), f2ord_c(lo[k]));
+                        red_cluster_max(leader_addr(s_box + 3 + k, 0), f2ord_c(hi[k]));
+                    }
+                }
             }
         }
         // ... padded face boxes on x (face_aabb_kernel) and the unions of
         // chunks of 32 of them (warp w of a pass: chunk w)
-        for (int fb = f0 + 32 * warp; fb < f1; fb += BLOCK) {
+        for (int fb = f0 + 32 * gwarp; fb < f1; fb += 32 * NWI) {
             const int f = fb + lane;
             V3 lo{INFINITY, INFINITY, INFINITY}, hi{-INFINITY, -INFINITY, -INFINITY};
             if (f < f1) {
@@ -1107,7 +1169,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_substep_kernel(BatchedSub
         }
         // compute_y (predict_kernel)
         if (A.predict) {
-            for (int v = v0 + tid; v < v1; v += BLOCK) {
+            for (int v = v0 + gtid; v < v1; v += STRIDE) {
                 const float4 x = A.x4[v], vel = A.v4[v];
                 const float f = A.fixed[v];
                 float4 y;
@@ -1118,23 +1180,30 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_substep_kernel(BatchedSub
                 A.ya[v] = y;
             }
         }
-        __syncthreads();
-        if (tid < 6) {
+        inst_sync<CL>();
+        if (rank == 0 && tid < 6) {
             const float b = ord2f_c(s_box[tid]);
             A.cl_box6[6 * i + tid] = tid < 3 ? b - A.pad : b + A.pad;
         }
         float4* yin = A.ya;
         float4* yout = A.yb;
         for (int it = 0; it < A.n_iter; ++it) {
-            for (int v = v0 + tid; v < v1; v += BLOCK)
-                yout[v] = sweep_vertex<2, true, FAST, false, false>(v, A.x4, yin, A.fixed, A.adj_ptr, A.adj, A.ks,
-                                                                    A.kb, 1, nullptr);
-            __syncthreads();
+            if (A.nbr16 != nullptr) {
+                for (int v = v0 + gtid; v < v1; v += STRIDE)
+                    yout[v] = sweep_vertex_src<2, true, FAST, false, false>(
+                        v, A.x4, yin, A.fixed, __ldg(A.adj_ptr + v), __ldg(A.adj_ptr + v + 1),
+                        AdjPacked{A.nbr16, A.rest32, 0}, A.ks, A.kb, 1, nullptr);
+            } else {
+                for (int v = v0 + gtid; v < v1; v += STRIDE)
+                    yout[v] = sweep_vertex<2, true, FAST, false, false>(v, A.x4, yin, A.fixed, A.adj_ptr, A.adj,
+                                                                        A.ks, A.kb, 1, nullptr);
+            }
+            inst_sync<CL>();
             if (it == 0) {
                 // broad phase (batched_vt_st_broad_kernel, batched_tv_st_broad_kernel)
                 const int of0 = A.ob_fptr[i], of1 = A.ob_fptr[i + 1];
                 const float* ob6 = A.ob_box6 + 6 * i;
-                for (int v = v0 + tid; v < v1; v += BLOCK) {
+                for (int v = v0 + gtid; v < v1; v += STRIDE) {
                     const V3 p = mk(yout[v]);
                     const V3 a{p.x - A.pad, p.y - A.pad, p.z - A.pad}, b{p.x + A.pad, p.y + A.pad, p.z + A.pad};
                     unsigned m = 0;
@@ -1145,7 +1214,7 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_substep_kernel(BatchedSub
                 }
                 const float* cb6 = A.cl_box6 + 6 * i;
                 const int nch = (f1 - f0 + 31) / 32;
-                for (int s = o0 + warp; s < o1; s += NW) {
+                for (int s = o0 + gwarp; s < o1; s += NWI) {
                     const V3 p = mk(A.xs4[s]);
                     const V3 a{p.x - A.pad, p.y - A.pad, p.z - A.pad}, b{p.x + A.pad, p.y + A.pad, p.z + A.pad};
                     int count = 0;
@@ -1171,11 +1240,11 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_substep_kernel(BatchedSub
                         if (count > A.cap) overflow = 1;
                     }
                 }
-                __syncthreads();
+                inst_sync<CL>();
             }
             // obstacle contacts (batched_contacts_kernel)
             const int nv = v1 - v0;
-            for (int k = tid; k < nv + (o1 - o0); k += BLOCK) {
+            for (int k = gtid; k < nv + (o1 - o0); k += STRIDE) {
                 if (k < nv) {
                     const int v = v0 + k;
                     unsigned m = A.vmask[v];
@@ -1210,9 +1279,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_substep_kernel(BatchedSub
                     }
                 }
             }
-            __syncthreads();
+            inst_sync<CL>();
             // update_dx (collision_apply_kernel)
-            for (int v = v0 + tid; v < v1; v += BLOCK) {
+            for (int v = v0 + gtid; v < v1; v += STRIDE) {
                 const int c = A.nc[v];
                 if (c > 0) {
                     const float cf = (float)c;
@@ -1228,13 +1297,13 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_substep_kernel(BatchedSub
                     A.nc[v] = 0;
                 }
             }
-            __syncthreads();
+            inst_sync<CL>();
             float4* t = yin;
             yin = yout;
             yout = t;
         }
         // compute_velocity + update_x (velocity_update_kernel) from the final y
-        for (int v = v0 + tid; v < v1; v += BLOCK) {
+        for (int v = v0 + gtid; v < v1; v += STRIDE) {
             float4 x = A.x4[v];
             const float4 y = yin[v];
             const float sfac = (1.0f - A.damping) * A.fixed[v];
@@ -1250,6 +1319,9 @@ __global__ void __launch_bounds__(BLOCK, MINB) batched_substep_kernel(BatchedSub
             A.x4[v] = x;
         }
     }
+    // no CTA leaves while another CTA of its cluster may still read its
+    // shared memory (the final instance index)
+    if (CL > 1) inst_sync<CL>();
     if (bad) atomicOr(A.status, SX_STATUS_FIXED_RANGE);
     if (overflow) atomicOr(A.status, SX_STATUS_CAND_OVERFLOW);
     // the last CTA out resets the queue for the next launch
@@ -1773,13 +1845,16 @@ extern "C" int sx_batched_obstacle_contacts(int n_verts, float* y4, const float*
 // Launch configurations of the persistent batched substep: threads per CTA
 // and CTAs per SM (the grid is that many per SM); all give identical results.
 struct BatchedSubstepVariant {
-    int block, blocks_per_sm;
-    decltype(&batched_substep_kernel<256, 4, false>) exact, fast;
+    int block, blocks_per_sm, cluster;
+    decltype(&batched_substep_kernel<256, 4, 1, false>) exact, fast;
 };
-#define SX_BS_VARIANT(B, M) {B, M, batched_substep_kernel<B, M, false>, batched_substep_kernel<B, M, true>}
+#define SX_BS_VARIANT(B, M, CL) \
+    {B, M, CL, batched_substep_kernel<B, M, CL, false>, batched_substep_kernel<B, M, CL, true>}
+// (threads per CTA, CTAs per SM, CTAs per instance)
 static const BatchedSubstepVariant kBatchedSubstepVariants[] = {
-    SX_BS_VARIANT(512, 2), SX_BS_VARIANT(256, 4), SX_BS_VARIANT(1024, 1), SX_BS_VARIANT(256, 2),
-    SX_BS_VARIANT(512, 1), SX_BS_VARIANT(128, 8),
+    SX_BS_VARIANT(512, 2, 1), SX_BS_VARIANT(256, 4, 1), SX_BS_VARIANT(1024, 1, 1), SX_BS_VARIANT(256, 2, 1),
+    SX_BS_VARIANT(512, 1, 1), SX_BS_VARIANT(128, 8, 1), SX_BS_VARIANT(512, 2, 8), SX_BS_VARIANT(512, 2, 4),
+    SX_BS_VARIANT(256, 4, 8), SX_BS_VARIANT(1024, 1, 8), SX_BS_VARIANT(512, 2, 2),
 };
 #undef SX_BS_VARIANT
 constexpr int kNumBatchedSubstepVariants = sizeof(kBatchedSubstepVariants) / sizeof(kBatchedSubstepVariants[0]);
@@ -1792,6 +1867,11 @@ extern "C" int sx_batched_substep_variant_info(int variant, int* block, int* blo
     *block = kBatchedSubstepVariants[variant].block;
     *blocks_per_sm = kBatchedSubstepVariants[variant].blocks_per_sm;
     return SX_OK;
+}
+
+extern "C" int sx_batched_substep_variant_cluster(int variant) {
+    SX_REQUIRE(variant >= 0 && variant < kNumBatchedSubstepVariants, "sx_batched_substep_variant_cluster: bad variant");
+    return kBatchedSubstepVariants[variant].cluster;
 }
 
 extern "C" int sx_batched_substep(const SxBatchedSubstep* b, int variant, int fast, void* stream) {
@@ -1809,7 +1889,10 @@ extern "C" int sx_batched_substep(const SxBatchedSubstep* b, int variant, int fa
     A.order = b->order; A.vptr = b->vptr; A.fptr = b->fptr; A.cptr = b->cptr; A.optr = b->optr;
     A.ob_fptr = b->ob_fptr;
     A.x4 = (float4*)b->x4; A.ya = (float4*)b->y4; A.yb = (float4*)b->y_other4; A.v4 = (float4*)b->v4;
+    SX_REQUIRE((b->adj_nbr16 == nullptr) == (b->adj_rest32 == nullptr),
+               "sx_batched_substep: give both packed adjacency arrays or neither");
     A.fixed = b->fixed; A.m_inv = b->m_inv; A.adj_ptr = b->adj_ptr; A.adj = (const int2*)b->adj;
+    A.nbr16 = b->adj_nbr16; A.rest32 = b->adj_rest32;
     A.faces = b->faces; A.ob_faces = b->ob_faces; A.xs4 = (const float4*)b->xs4;
     A.fmin4 = (float4*)b->fmin4; A.fmax4 = (float4*)b->fmax4; A.cmin4 = (float4*)b->cmin4;
     A.cmax4 = (float4*)b->cmax4; A.cl_box6 = b->cl_box6; A.ob_box6 = b->ob_box6;
@@ -1819,7 +1902,33 @@ extern "C" int sx_batched_substep(const SxBatchedSubstep* b, int variant, int fa
     A.pad = b->padding; A.dt = b->dt; A.gx = b->gx; A.gy = b->gy; A.gz = b->gz; A.ks = b->k_spring;
     A.kb = b->k_bend; A.dHat = b->dHat; A.compliance = b->compliance; A.damping = b->damping;
     const BatchedSubstepVariant& bv = kBatchedSubstepVariants[variant];
-    launch(fast ? bv.fast : bv.exact, sm_count() * bv.blocks_per_sm, bv.block, 0, as_stream(stream), A);
+    const auto kern = fast ? bv.fast : bv.exact;
+    if (bv.cluster == 1) {
+        launch(kern, sm_count() * bv.blocks_per_sm, bv.block, 0, as_stream(stream), A);
+        return check_launch("batched_substep_kernel");
+    }
+    // clusters of bv.cluster CTAs, one instance per cluster
+    const int clusters = max(1, sm_count() * bv.blocks_per_sm / bv.cluster);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(clusters * bv.cluster);
+    cfg.blockDim = dim3(bv.block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = as_stream(stream);
+    cudaLaunchAttribute attr[2];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = bv.cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    int na = 1;
+    if (pdl_enabled()) {
+        attr[1].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[1].val.programmaticStreamSerializationAllowed = 1;
+        na = 2;
+    }
+    cfg.attrs = attr;
+    cfg.numAttrs = na;
+    SX_CUDA(cudaLaunchKernelEx(&cfg, kern, A));
+    note_launch();
     return check_launch("batched_substep_kernel");
 }
 

@@ -96,10 +96,10 @@ def test_batched_tolerance_mode(pkg):
 @pytest.mark.parametrize("fast", [False, True])
 def test_persistent_substep_equals_grid_launches(pkg, fast):
     """One persistent launch per substep (sx_batched_substep: an instance per
-    CTA, block barriers between the phases) gives the same frames as the graph
-    of grid-wide launches, bit for bit, in every launch configuration, with the
-    exact and with the fast arithmetic, for an even and an odd iteration
-    count."""
+    CTA with block barriers, or per thread-block cluster with cluster barriers)
+    gives the same frames as the graph of grid-wide launches, bit for bit, in
+    every launch configuration, with the exact and with the fast arithmetic,
+    for an even and an odd iteration count."""
     from starlab_physics_gb300._lib import sx
 
     insts = _instances(pkg, seed=7, n_inst=9)
@@ -151,3 +151,13 @@ def test_persistent_substep_batched512(pkg):
     a.forward(10)
     torch.cuda.synchronize()
     assert torch.equal(a.x4, b.x4)
+    # an instance per 8-CTA cluster, reading the packed adjacency
+    from starlab_physics_gb300._lib import sx
+
+    b.persistent_variant = next(v for v in range(int(sx.sx_batched_substep_variants()))
+                                if int(sx.sx_batched_substep_variant_cluster(v)) == 8)
+    b.packed_sweep = True
+    b.forward(10)
+    a.forward(10)
+    torch.cuda.synchronize()
+    assert torch.equal(a.x4, b.x4) and torch.equal(a.v4, b.v4)

@@ -101,17 +101,20 @@ def test_packed_sweep_equals_int2_sweep(pkg, fast):
 
 @pytest.mark.gpu
 def test_packed_sweep_in_solver_frames(pkg):
-    """A batched frame with the packed sweep equals the frame with the int2 sweep."""
+    """Batched frames with the packed sweep (grid-wide launches, and the
+    persistent substep reading the packed arrays) equal the frames with the
+    int2 sweep."""
     bs = pkg.BatchedSolver(pkg.batched_scene(64, seed=3), dHat=(4e-3) ** 2, stiffness_stretch=1e5,
                            stiffness_bending=1e8, g=(0.0, 0.0, -9.81), dt=1 / 60, n_iter=20, padding=8e-3)
     bs.use_graph = True
     x0, v0 = bs.x4.clone(), bs.v4.clone()
     out = []
-    for packed in (False, True):
+    for persistent, packed in ((False, False), (False, True), (True, True)):
         bs.x4.copy_(x0)
         bs.v4.copy_(v0)
+        bs.persistent = persistent
         bs.packed_sweep = packed
         for _ in range(3):
             bs.forward(10)
         out.append(bs.x4.clone())
-    assert torch.equal(out[0], out[1])
+    assert torch.equal(out[0], out[1]) and torch.equal(out[0], out[2])
