@@ -59,6 +59,7 @@ def parse_args():
     ap.add_argument("--only-learned", action="store_true", help="run only the learned warm-start measurement")
     ap.add_argument("--only-lbvh", action="store_true",
                     help="run only the standalone 2^20-triangle LBVH measurement (no CPU baseline)")
+    ap.add_argument("--only-color", action="store_true", help="run only the colouring measurement")
     ap.add_argument("--only-gs", action="store_true",
                     help="run only the Gauss-Seidel against Jacobi comparison (drape after 3 frames)")
     ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES),
@@ -97,6 +98,25 @@ def _case_batched(pkg):
     sim.forward(10)
 
 
+def _case_sweeps(pkg):
+    """One sweep of each kind over the 512-cloth batch from its rest state:
+    int2 exact, int2 fast, packed exact, packed fast."""
+    import torch
+    from starlab_physics_gb300._lib import ptr, stream_handle, sx
+
+    sim = _batched_case_solver(pkg, 20)
+    dt = 1.0 / 600.0
+    ks, kb = 1e8 * dt * dt, 1e5 * dt * dt
+    out = torch.empty_like(sim.y4)
+    for fast in (0, 1):
+        sx.sx_jacobi_sweep_mode(ptr(sim.x4), ptr(sim.x4), ptr(out), ptr(sim.fixed), ptr(sim.adj_ptr), ptr(sim.adj),
+                                sim.num_verts, ks, kb, 1, 0, fast, stream_handle())
+    for fast in (0, 1):
+        sx.sx_jacobi_sweep_packed(ptr(sim.x4), ptr(sim.x4), ptr(out), ptr(sim.fixed), ptr(sim.adj_ptr),
+                                  ptr(sim.adj_nbr16), ptr(sim.adj_rest32), sim.num_verts, ks, kb, 1, fast,
+                                  stream_handle())
+
+
 def _case_color(pkg):
     """Colouring of the 256 x 256 cloth's edges (one call)."""
     _, f = pkg.grid_cloth(256)
@@ -112,7 +132,7 @@ def _case_learned(pkg):
 
 
 PROFILE_CASES = {"drape": _case_drape, "soup": _case_soup, "batched": _case_batched, "color": _case_color,
-                 "learned": _case_learned}
+                 "learned": _case_learned, "sweeps": _case_sweeps}
 
 
 def run_profile_case(name):
@@ -930,6 +950,9 @@ def main():
         return
     if args.only_learned:
         print(json.dumps({"learned_batched512": learned_batched(pkg)}))
+        return
+    if args.only_color:
+        print(json.dumps({"coloring": coloring_timing(pkg, with_cpu=not args.no_cpu_baseline)}))
         return
     if args.only_gs:
         sim = pkg.scenes.make_solver(scene, device="cuda")
