@@ -79,6 +79,13 @@ int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out4, const fl
 int sx_set_programmatic_launch(int enable);
 int sx_jacobi_sweep_variants(void);
 int sx_jacobi_sweep_variant_info(int variant, int* g, int* block);
+/* The form of that variant: *lanes = lanes of a warp that evaluate one vertex
+ * (1, or 2/4/8: the vertex's entries are split across the lanes and their
+ * terms added in ascending entry order through shuffles, for meshes with too
+ * few vertices to fill the SMs); *streaming = 1 if the adjacency entries are
+ * read with the evict-first cache policy (for batches larger than L2).  Every
+ * form gives the same result bit for bit. */
+int sx_jacobi_sweep_variant_form(int variant, int* lanes, int* streaming);
 int sx_jacobi_sweep_v(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
                       const int* adj, int n_verts, float k_spring, float k_bend, int bend_on_y, int variant,
                       void* stream);
@@ -355,6 +362,11 @@ int sx_contact_pairs_project(int n_dy, int n_st, const int* pairs, const void* w
  * blocks per SM, as sx_contact_pairs_project_variant_info reports. */
 int sx_contact_pairs_project_variants(void);
 int sx_contact_pairs_project_variant_info(int variant, int* unroll, int* blocks_per_sm);
+/* 1 if that variant is the pipelined form: the vertex-vs-obstacle and
+ * obstacle-vertex pairs one per lane with their positions kept in registers,
+ * and the next step's pair records loaded while the current step's positions
+ * are gathered; 0 for the stacked form.  Same sums either way. */
+int sx_contact_pairs_project_variant_pipelined(int variant);
 int sx_contact_pairs_project_v(int n_dy, int n_st, const int* pairs, const void* ws, const float* y4,
                                const float* xs4, const float* fixed, const float* m_inv, float dHat, float compliance,
                                float cull_d2, long long* dx_fix, int* nc, int* status, const int* conv, int iter,

@@ -50,6 +50,7 @@ SIGNATURES = {
     "sx_jacobi_sweep": ([P, P, P, P, P, P, I, F, F, I, P], I),
     "sx_jacobi_sweep_variants": ([], I),
     "sx_jacobi_sweep_variant_info": ([I, P, P], I),
+    "sx_jacobi_sweep_variant_form": ([I, P, P], I),
     "sx_set_programmatic_launch": ([I], I),
     "sx_jacobi_sweep_v": ([P, P, P, P, P, P, I, F, F, I, I, P], I),
     "sx_jacobi_sweep_mode": ([P, P, P, P, P, P, I, F, F, I, I, I, P], I),
@@ -88,6 +89,7 @@ SIGNATURES = {
     "sx_contact_pairs_sweep": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, P], I),
     "sx_contact_pairs_project": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, P], I),
     "sx_contact_pairs_project_variants": ([], I),
+    "sx_contact_pairs_project_variant_pipelined": ([I], I),
     "sx_contact_pairs_project_variant_info": ([I, P, P], I),
     "sx_contact_pairs_project_v": ([I, I, P, P, P, P, P, P, F, F, F, P, P, P, P, I, I, P], I),
     "sx_contact_apply": ([I, P, P, P, P, P, I, P], I),
@@ -184,6 +186,7 @@ class _Calls:
         if SIGNATURES[name][1] is I and name not in ("sx_version", "sx_mlp_param_count", "sx_mlp_bf16_count",
                                                      "sx_jacobi_sweep_variants",
                                                      "sx_contact_pairs_project_variants",
+                                                     "sx_contact_pairs_project_variant_pipelined",
                                                      "sx_batched_substep_variants",
                                                      "sx_batched_substep_variant_cluster"):
             return lambda *a: _call(name, *a)

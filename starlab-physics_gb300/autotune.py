@@ -2,9 +2,10 @@
 of the contact-pair projection's configurations).
 
 The sweep kernel is compiled in several configurations -- how many adjacency
-entries a thread loads before it computes, and how many threads (= vertices) a
-block holds (``sx_jacobi_sweep_variant_info``); all give bit-identical
-results.  The best one depends on the mesh: a 65 536-vertex cloth whose sweep
+entries a thread loads before it computes, how many threads a block holds
+(``sx_jacobi_sweep_variant_info``), how many lanes share one vertex and
+whether the adjacency is read with the streaming cache policy
+(``sx_jacobi_sweep_variant_form``); all give bit-identical results.  The best one depends on the mesh: a 65 536-vertex cloth whose sweep
 is L2-resident and latency-bound wants more loads in flight per thread, a
 3.2 M-vertex batch that streams from HBM wants more resident threads.
 :func:`tune_sweep` times every configuration on the caller's own arrays (a
@@ -31,6 +32,17 @@ def variants() -> list[tuple[int, int]]:
         g, b = C.c_int(0), C.c_int(0)
         sx.sx_jacobi_sweep_variant_info(k, C.addressof(g), C.addressof(b))
         out.append((g.value, b.value))
+    return out
+
+
+def variant_forms() -> list[tuple[int, int]]:
+    """(lanes per vertex, streaming adjacency loads) of every compiled variant."""
+    L = load()
+    out = []
+    for k in range(int(L.sx_jacobi_sweep_variants())):
+        lanes, st = C.c_int(0), C.c_int(0)
+        sx.sx_jacobi_sweep_variant_form(k, C.addressof(lanes), C.addressof(st))
+        out.append((lanes.value, st.value))
     return out
 
 

@@ -142,7 +142,8 @@ inline int tile_grid(K kernel, int n_verts) {
 // fewer instructions per entry, results within float rounding of the exact
 // form but not bit-identical to it; validated against the oracle at the
 // position and residual tolerance of the substep instead.
-template <bool CHECK, int G = 2, int BLOCK = SW_BLOCK, bool BY = false, bool FAST = false>
+// STREAM: adjacency entries read with the evict-first policy (AdjInt2Stream).
+template <bool CHECK, int G = 2, int BLOCK = SW_BLOCK, bool BY = false, bool FAST = false, bool STREAM = false>
 __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4* __restrict__ x4,
                                                                 const float4* __restrict__ yin,
                                                                 float4* __restrict__ yout,
@@ -158,9 +159,42 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_kernel(int V, const float4
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     const int v = tile * BLOCK + threadIdx.x;
     float c2 = 0.0f;  // sum of C^2 over this vertex's entries (CHECK)
-    if (v < V) yout[v] = sweep_vertex<G, BY, FAST, CHECK, true>(v, x4, yin, fixed, ptr, adj, ks, kb, bend_y, &c2);
+    if (v < V) {
+        if (STREAM)
+            yout[v] = sweep_vertex_src<G, BY, FAST, CHECK, true>(v, x4, yin, fixed, __ldg(ptr + v), __ldg(ptr + v + 1),
+                                                                 AdjInt2Stream{adj}, ks, kb, bend_y, &c2);
+        else
+            yout[v] = sweep_vertex<G, BY, FAST, CHECK, true>(v, x4, yin, fixed, ptr, adj, ks, kb, bend_y, &c2);
+    }
     if (CHECK) block_residual_partial(c2, partial, tile);
     }
+}
+
+// L lanes per vertex (sweep_vertex_lanes): for meshes whose vertices alone
+// leave the SMs short of warps (65 536 vertices are 13 warps per SM), L times
+// the threads and a shorter chain of dependent loads per thread; the same
+// sums in the same order, so bit-identical to jacobi_sweep_kernel.
+template <int L, int G, int BLOCK, bool BY = false, bool FAST = false>
+__global__ void __launch_bounds__(BLOCK) jacobi_sweep_lanes_kernel(int V, const float4* __restrict__ x4,
+                                                                      const float4* __restrict__ yin,
+                                                                      float4* __restrict__ yout,
+                                                                      const float* __restrict__ fixed,
+                                                                      const int* __restrict__ ptr,
+                                                                      const int2* __restrict__ adj, float ks,
+                                                                      float kb, int bend_y, const int* conv, int iter,
+                                                                      double* __restrict__ partial) {
+    pdl_entry();
+    if (iteration_skipped(conv, iter)) return;  // grid-uniform
+    const long long t = (long long)blockIdx.x * BLOCK + threadIdx.x;
+    const int v = (int)(t / L);
+    const bool valid = v < V;
+    int b = 0, e = 0;
+    if (valid) {
+        b = __ldg(ptr + v);
+        e = __ldg(ptr + v + 1);
+    }
+    const float4 out = sweep_vertex_lanes<L, G, BY, FAST, true>(v, valid, x4, yin, fixed, b, e, adj, ks, kb, bend_y);
+    if (valid && (threadIdx.x & (L - 1)) == 0) yout[v] = out;
 }
 
 // ---------------------------------------------------------------------------
@@ -402,24 +436,37 @@ extern "C" int sx_jacobi_sweep(const float* x4, const float* y_in4, float* y_out
     return check_launch("jacobi_sweep_kernel");
 }
 
-// Launch configurations of the sweep for the autotuner: (entries per load
-// batch, threads per block).  All give bit-identical results.
+// Launch configurations of the sweep for the autotuner: entries per load
+// batch, threads per block, lanes per vertex, and whether the adjacency is
+// read with the streaming cache policy.  All give bit-identical results.
 namespace sx {
 using SweepKernel = void (*)(int, const float4*, const float4*, float4*, const float*, const int*, const int2*, float,
                             float, int, const int*, int, double*);
 struct SweepVariant {
-    int g, block;
+    int g, block, lanes, stream;
     SweepKernel kern, kern_y;  // bending on x or y chosen at run time / bending on y
     SweepKernel fast, fast_y;  // the FAST arithmetic
 };
 #define SX_SWEEP_VARIANT(G, B)                                                                                  \
-    {G, B, jacobi_sweep_kernel<false, G, B>, jacobi_sweep_kernel<false, G, B, true>,                           \
+    {G, B, 1, 0, jacobi_sweep_kernel<false, G, B>, jacobi_sweep_kernel<false, G, B, true>,                     \
      jacobi_sweep_kernel<false, G, B, false, true>, jacobi_sweep_kernel<false, G, B, true, true>}
+#define SX_SWEEP_LANES(L, G, B)                                                                                 \
+    {G, B, L, 0, jacobi_sweep_lanes_kernel<L, G, B>, jacobi_sweep_lanes_kernel<L, G, B, true>,                 \
+     jacobi_sweep_lanes_kernel<L, G, B, false, true>, jacobi_sweep_lanes_kernel<L, G, B, true, true>}
+#define SX_SWEEP_STREAM(G, B)                                                                                   \
+    {G, B, 1, 1, jacobi_sweep_kernel<false, G, B, false, false, true>,                                         \
+     jacobi_sweep_kernel<false, G, B, true, false, true>, jacobi_sweep_kernel<false, G, B, false, true, true>,   \
+     jacobi_sweep_kernel<false, G, B, true, true, true>}
 static const SweepVariant kSweepVariants[] = {
     SX_SWEEP_VARIANT(2, 256), SX_SWEEP_VARIANT(1, 256), SX_SWEEP_VARIANT(4, 256), SX_SWEEP_VARIANT(2, 128),
     SX_SWEEP_VARIANT(2, 512), SX_SWEEP_VARIANT(4, 128), SX_SWEEP_VARIANT(1, 128), SX_SWEEP_VARIANT(3, 256),
+    SX_SWEEP_LANES(2, 2, 256), SX_SWEEP_LANES(2, 3, 256), SX_SWEEP_LANES(4, 1, 256), SX_SWEEP_LANES(4, 2, 256),
+    SX_SWEEP_LANES(4, 3, 256), SX_SWEEP_LANES(8, 1, 256), SX_SWEEP_LANES(8, 2, 256),
+    SX_SWEEP_STREAM(2, 128), SX_SWEEP_STREAM(3, 256), SX_SWEEP_STREAM(2, 256),
 };
 #undef SX_SWEEP_VARIANT
+#undef SX_SWEEP_LANES
+#undef SX_SWEEP_STREAM
 constexpr int kNumSweepVariants = sizeof(kSweepVariants) / sizeof(kSweepVariants[0]);
 }  // namespace sx
 
@@ -429,6 +476,14 @@ extern "C" int sx_jacobi_sweep_variant_info(int variant, int* g, int* block) {
     SX_REQUIRE(variant >= 0 && variant < kNumSweepVariants && g && block, "sx_jacobi_sweep_variant_info: bad variant");
     *g = kSweepVariants[variant].g;
     *block = kSweepVariants[variant].block;
+    return SX_OK;
+}
+
+extern "C" int sx_jacobi_sweep_variant_form(int variant, int* lanes, int* streaming) {
+    SX_REQUIRE(variant >= 0 && variant < kNumSweepVariants && lanes && streaming,
+               "sx_jacobi_sweep_variant_form: bad variant");
+    *lanes = kSweepVariants[variant].lanes;
+    *streaming = kSweepVariants[variant].stream;
     return SX_OK;
 }
 
@@ -449,7 +504,7 @@ extern "C" int sx_jacobi_sweep_mode(const float* x4, const float* y_in4, float* 
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_v: y_in4 and y_out4 must not alias");
     const SweepVariant& sv = kSweepVariants[variant];
     const SweepKernel k = fast ? (bend_on_y ? sv.fast_y : sv.fast) : (bend_on_y ? sv.kern_y : sv.kern);
-    launch(k, grid_for(n_verts, sv.block), sv.block, 0, as_stream(stream), n_verts, (const float4*)x4,
+    launch(k, grid_for((long long)n_verts * sv.lanes, sv.block), sv.block, 0, as_stream(stream), n_verts, (const float4*)x4,
            (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, (const int2*)adj, k_spring, k_bend,
            bend_on_y ? 1 : 0, (const int*)nullptr, 0, (double*)nullptr);
     return check_launch("jacobi_sweep_kernel");

@@ -698,10 +698,7 @@ __device__ __forceinline__ void pair_points(const PairCtx& c, int t, int4 pr, V3
     x[3] = mk(tri[pr.w]);
 }
 
-__device__ __forceinline__ void project_pair(const PairCtx& c, int t, int* bad) {
-    const int4 pr = c.pairs[t];
-    V3 x[4];
-    pair_points(c, t, pr, x);
+__device__ __forceinline__ void project_pair_x(const PairCtx& c, int t, int4 pr, const V3 x[4], int* bad) {
     V3 g[4] = SX_ZERO_G;
     int dt;
     float schur;
@@ -715,6 +712,13 @@ __device__ __forceinline__ void project_pair(const PairCtx& c, int t, int* bad) 
         const int vv[4] = {-1, pr.y, pr.z, pr.w};
         project_tv_st(vv, x, c.fixed, c.m_inv, c.dHat, c.compliance, c.dx, c.nc, bad, g, &dt, &schur);
     }
+}
+
+__device__ __forceinline__ void project_pair(const PairCtx& c, int t, int* bad) {
+    const int4 pr = c.pairs[t];
+    V3 x[4];
+    pair_points(c, t, pr, x);
+    project_pair_x(c, t, pr, x, bad);
 }
 
 constexpr int PP_BLOCK = 256;
@@ -803,6 +807,117 @@ __global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_kernel(const int
         if (n1 > 0) sat_stage(n1);
         if (lane < n2) project_pair(c, s2[lane], &bad);
     }
+    if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
+}
+
+// Pipelined form of pairs_project_kernel (same sums).  The two kinds against
+// the obstacle (vertex vs obstacle face, obstacle vertex vs cloth face) are
+// few pairs of which most reach the classification; the first warps take them
+// one per lane and run box test, separating-axis test and projection on the
+// positions already in registers, without re-loading them through the
+// stacks.  The vertex-vs-cloth pairs then go through the stacked stages as in
+// pairs_project_kernel, with the next step's pair records loaded while the
+// current step's positions are gathered, so that a warp waits on one round
+// trip per step instead of two.
+template <int U, int MINB>
+__global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_pipe_kernel(const int* __restrict__ meta,
+                                                                            const int4* __restrict__ pairs,
+                                                                            const float4* __restrict__ y4,
+                                                                            const float4* __restrict__ xs4,
+                                                                            const float* __restrict__ fixed,
+                                                                            const float* __restrict__ m_inv,
+                                                                            float dHat, float compliance,
+                                                                            float cull_d2, long long* dx, int* nc,
+                                                                            int* status, const int* conv, int iter) {
+    pdl_entry();
+    if (iteration_skipped(conv, iter)) return;
+    const PairCtx c{pairs, y4, xs4, fixed, m_inv, dHat, compliance, dx, nc, meta[0], meta[1]};
+    const int P = meta[2], st_end = c.st_end, dy_end = c.dy_end;
+    const int lane = threadIdx.x & 31;
+    const int gw = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, nw = (gridDim.x * blockDim.x) >> 5;
+    int bad = 0;
+    if (!(cull_d2 > 0.0f)) {  // no cull: every pair is classified
+        for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < P; t += gridDim.x * blockDim.x)
+            project_pair(c, t, &bad);
+        if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
+        return;
+    }
+    // the obstacle kinds, one pair per lane
+    const int H = st_end + (P - dy_end);
+    for (int h0 = gw * 32; h0 < H; h0 += nw * 32) {
+        const int h = h0 + lane;
+        if (h < H) {
+            const int t = h < st_end ? h : dy_end + (h - st_end);
+            const int4 pr = pairs[t];
+            V3 x[4];
+            pair_points(c, t, pr, x);
+            if (!box_far(x[0], x[1], x[2], x[3], cull_d2) && !sat_far(x[0], x[1], x[2], x[3], cull_d2))
+                project_pair_x(c, t, pr, x, &bad);
+        }
+    }
+    // the vertex-vs-cloth pairs [st_end, dy_end)
+    __shared__ int box_stack[PP_BLOCK / 32][32 * U + 32];
+    __shared__ int sat_stack[PP_BLOCK / 32][64];
+    const unsigned below = (1u << lane) - 1u;
+    int* s1 = box_stack[threadIdx.x >> 5];
+    int* s2 = sat_stack[threadIdx.x >> 5];
+    int n1 = 0, n2 = 0;  // warp-uniform
+    auto sat_stage = [&](int cnt) {
+        const int t = lane < cnt ? s1[n1 - cnt + lane] : -1;
+        bool keep = false;
+        if (t >= 0) {
+            V3 x[4];
+            pair_points(c, t, pairs[t], x);
+            keep = !sat_far(x[0], x[1], x[2], x[3], cull_d2);
+        }
+        n1 -= cnt;
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) s2[n2 + __popc(m & below)] = t;
+        n2 += __popc(m);
+        __syncwarp();
+        if (n2 >= 32) {
+            project_pair(c, s2[n2 - 32 + lane], &bad);
+            n2 -= 32;
+            __syncwarp();
+        }
+    };
+    const int step = nw * 32 * U;
+    int4 nx[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+        const int t = st_end + gw * 32 * U + 32 * u + lane;
+        nx[u] = t < dy_end ? pairs[t] : make_int4(0, 0, 0, 0);
+    }
+    for (int base = st_end + gw * 32 * U; base < dy_end; base += step) {
+        V3 x[U][4];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int t = base + 32 * u + lane;
+            if (t < dy_end) {
+                x[u][0] = mk(y4[nx[u].x]);
+                x[u][1] = mk(y4[nx[u].y]);
+                x[u][2] = mk(y4[nx[u].z]);
+                x[u][3] = mk(y4[nx[u].w]);
+            }
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int t = base + step + 32 * u + lane;
+            nx[u] = t < dy_end ? pairs[t] : make_int4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const int t = base + 32 * u + lane;
+            const bool keep = t < dy_end && !box_far(x[u][0], x[u][1], x[u][2], x[u][3], cull_d2);
+            const unsigned m = __ballot_sync(0xffffffffu, keep);
+            if (keep) s1[n1 + __popc(m & below)] = t;
+            n1 += __popc(m);
+        }
+        __syncwarp();
+        while (n1 >= 32) sat_stage(32);
+    }
+    if (n1 > 0) sat_stage(n1);
+    if (lane < n2) project_pair(c, s2[lane], &bad);
     if (bad) atomicOr(status, SX_STATUS_FIXED_RANGE);
 }
 
@@ -1715,14 +1830,17 @@ static int sm_count() {
 // results.  The default was the fastest inside the drape256 frame; timed
 // alone on a fixed state the ranking differs, so it is not autotuned.
 struct PairsProjectVariant {
-    int unroll, blocks_per_sm;
+    int unroll, blocks_per_sm, pipelined;
     decltype(&pairs_project_kernel<1, 4>) kern;
 };
 static const PairsProjectVariant kPairsProjectVariants[] = {
-    {2, 3, pairs_project_kernel<2, 3>},
-    {1, 4, pairs_project_kernel<1, 4>},
-    {2, 6, pairs_project_kernel<2, 3>},
-    {4, 2, pairs_project_kernel<4, 2>},
+    {2, 3, 0, pairs_project_kernel<2, 3>},
+    {1, 4, 0, pairs_project_kernel<1, 4>},
+    {2, 6, 0, pairs_project_kernel<2, 3>},
+    {4, 2, 0, pairs_project_kernel<4, 2>},
+    {2, 3, 1, pairs_project_pipe_kernel<2, 3>},
+    {1, 4, 1, pairs_project_pipe_kernel<1, 4>},
+    {2, 4, 1, pairs_project_pipe_kernel<2, 4>},
 };
 constexpr int kNumPairsProjectVariants = sizeof(kPairsProjectVariants) / sizeof(kPairsProjectVariants[0]);
 constexpr int kPairsProjectDefault = 0;
@@ -1735,6 +1853,12 @@ extern "C" int sx_contact_pairs_project_variant_info(int variant, int* unroll, i
     *unroll = kPairsProjectVariants[variant].unroll;
     *blocks_per_sm = kPairsProjectVariants[variant].blocks_per_sm;
     return SX_OK;
+}
+
+extern "C" int sx_contact_pairs_project_variant_pipelined(int variant) {
+    SX_REQUIRE(variant >= 0 && variant < kNumPairsProjectVariants,
+               "sx_contact_pairs_project_variant_pipelined: bad variant");
+    return kPairsProjectVariants[variant].pipelined;
 }
 
 extern "C" int sx_contact_pairs_project_v(int n_dy, int n_st, const int* pairs, const void* ws, const float* y4,

@@ -524,6 +524,37 @@ class Solver:
         self.sweep_variant = 0 if self._packed_sweep else best
         return best, times
 
+    def autotune_contacts(self, n_substeps: int, reps: int = 3):
+        """Time whole frames with every launch configuration of the contact-pair
+        projection (identical results) and keep the fastest: timed alone on one
+        state the ranking differs from the frame's.  The state is restored after
+        every frame.  Returns (variant, frame times in ms)."""
+        if not (self.enable_collision_handling and not self.record_pairs):
+            return self.pairs_variant, []
+        m = self.mesh_dy
+        x0, v0 = m.x4.clone(), m.v4.clone()
+        times = []
+        for v in range(int(sx.sx_contact_pairs_project_variants())):
+            self.pairs_variant = v
+            self.forward(n_substeps)  # captures the frame's graph for this variant when use_graph is set
+            best = None
+            for _ in range(reps):
+                m.x4.copy_(x0)
+                m.v4.copy_(v0)
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record()
+                self.forward(n_substeps)
+                b.record()
+                torch.cuda.synchronize()
+                t = a.elapsed_time(b)
+                best = t if best is None else min(best, t)
+            times.append(best)
+            m.x4.copy_(x0)
+            m.v4.copy_(v0)
+        self.pairs_variant = int(np.argmin(times))
+        torch.cuda.synchronize()
+        return self.pairs_variant, times
+
     @property
     def packed_sweep(self) -> bool:
         """The fixed-count sweep runs over the packed, shared-memory-staged
