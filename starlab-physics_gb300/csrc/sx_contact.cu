@@ -1827,8 +1827,10 @@ static int sm_count() {
 // Launch configurations of the pair projection: pair batches box-tested per
 // warp step (U) and resident blocks per SM (the grid is that many blocks per
 // SM; registers are capped to keep them resident).  All give identical
-// results.  The default was the fastest inside the drape256 frame; timed
-// alone on a fixed state the ranking differs, so it is not autotuned.
+// results.  The default (the pipelined form, one pair batch per warp step, 4
+// blocks per SM) was the fastest inside the drape256 frame; timed alone on a
+// fixed state the ranking differs, so Solver.autotune_contacts times whole
+// frames.
 struct PairsProjectVariant {
     int unroll, blocks_per_sm, pipelined;
     decltype(&pairs_project_kernel<1, 4>) kern;
@@ -1843,7 +1845,7 @@ static const PairsProjectVariant kPairsProjectVariants[] = {
     {2, 4, 1, pairs_project_pipe_kernel<2, 4>},
 };
 constexpr int kNumPairsProjectVariants = sizeof(kPairsProjectVariants) / sizeof(kPairsProjectVariants[0]);
-constexpr int kPairsProjectDefault = 0;
+constexpr int kPairsProjectDefault = 5;
 
 extern "C" int sx_contact_pairs_project_variants(void) { return kNumPairsProjectVariants; }
 
