@@ -60,6 +60,7 @@ def parse_args():
     ap.add_argument("--only-lbvh", action="store_true",
                     help="run only the standalone 2^20-triangle LBVH measurement (no CPU baseline)")
     ap.add_argument("--only-color", action="store_true", help="run only the colouring measurement")
+    ap.add_argument("--only-plain64", action="store_true", help="run only the 64x64 box-scene measurement")
     ap.add_argument("--only-gs", action="store_true",
                     help="run only the Gauss-Seidel against Jacobi comparison (drape after 3 frames)")
     ap.add_argument("--profile-case", choices=sorted(PROFILE_CASES),
@@ -334,6 +335,64 @@ def cpu_baseline(pkg, scene, x0, v0, gpu_x_after, frame):
             "bit_exact_vs_gpu": bool(d.max() == 0.0),
             "one_core": {"value": V / el1, "unit": UNIT, "cores": 1,
                          "sample": f"1 substep of the same frame, 1 thread, {el1:.2f} s"}}
+
+
+def plain64_timing(pkg, warm_frames=20, frames=20, with_cpu=True):
+    """Configuration 0: the 64 x 64 cloth over the box (10 substeps x 20
+    iterations), one CUDA graph per frame, sweep and contact launch
+    configurations autotuned; after `warm_frames` frames (the cloth reaches the
+    box at about frame 18), `frames` consecutive frames timed with CUDA events
+    (the working set is L2-resident).  The CPU leg runs the oracle over the same
+    frames from the same state on all host cores and compares end states."""
+    import numpy as np
+    import torch
+
+    scene = pkg.scenes.plain64()
+    sim = pkg.scenes.make_solver(scene, device="cuda")
+    sim.bending_on = "y"
+    sim.use_graph = True
+    S = scene.n_substeps
+    sim.forward(S)
+    variant, _ = sim.autotune()
+    pp_variant, _ = sim.autotune_contacts(S)
+    for _ in range(warm_frames - 1):
+        sim.forward(S)
+    torch.cuda.synchronize()
+    x0 = sim.mesh_dy.x4.cpu().numpy().copy()
+    v0 = sim.mesh_dy.v4.cpu().numpy().copy()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(frames):
+        sim.forward(S)
+    b.record()
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(b)
+    V = sim.mesh_dy.num_verts
+    from starlab_physics_gb300.autotune import variant_forms, variants
+
+    out = {"workload": f"plain64: 64x64 cloth over a 12-face box, {S} substeps x {scene.n_iter} iterations, "
+                       f"frames {warm_frames + 1}-{warm_frames + frames}",
+           "value": V * S * frames / (ms / 1e3), "unit": UNIT, "ms_per_frame": ms / frames,
+           "sweep_config": {"entries_per_load_batch": variants()[variant][0] if variant < len(variants()) else None,
+                            "lanes_per_vertex": variant_forms()[variant][0] if variant < len(variants()) else 1,
+                            "packed": bool(sim.packed_sweep)},
+           "pairs_project_variant": pp_variant, "status_flags": sim.status_flags()}
+    if with_cpu:
+        cores = os.cpu_count() or 1
+        orc = _oracle_solver(pkg, scene, cores)
+        orc.x4[:] = x0
+        orc.v4[:] = v0
+        dt_sub = scene.dt / S
+        t0 = time.perf_counter()
+        for _ in range(frames * S):
+            orc.substep(dt_sub)
+        el = time.perf_counter() - t0
+        d = np.abs(orc.x4[:, :3].astype(np.float64) - sim.mesh_dy.x4.cpu().numpy()[:, :3])
+        out["cpu_baseline"] = {"value": V * S * frames / el, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"the same {frames} frames from the same state on the CPU oracle "
+                                         f"(OpenMP, {cores} threads), {el:.2f} s",
+                               "max_abs_dx_vs_gpu": float(d.max()), "bit_exact_vs_gpu": bool(d.max() == 0.0)}
+    return out
 
 
 def lbvh_soup(pkg, reps=10, with_cpu=True):
@@ -958,6 +1017,9 @@ def main():
     if args.only_learned:
         print(json.dumps({"learned_batched512": learned_batched(pkg)}))
         return
+    if args.only_plain64:
+        print(json.dumps({"plain64": plain64_timing(pkg, with_cpu=not args.no_cpu_baseline)}))
+        return
     if args.only_color:
         print(json.dumps({"coloring": coloring_timing(pkg, with_cpu=not args.no_cpu_baseline)}))
         return
@@ -1045,6 +1107,35 @@ def main():
     e2e_val, ms_e2e = replica_throughput(V * S * args.steps, sum(s.elapsed_time(e) for s, e in zip(e_st, e_en)),
                                          world)
     bytes_io = 2 * V * 16
+
+    # ---- the same frame with the sweep's fast arithmetic (not bit-identical;
+    # held to the substep tolerance by the GPU tests), sweep re-tuned for it ----
+    exact_sweep = (sim.sweep_variant, sim.packed_sweep)
+    sim.fast_math = True
+    sim.mesh_dy.x4.copy_(x0)
+    sim.mesh_dy.v4.copy_(v0)
+    fast_variant, _ = sim.autotune()
+    sim.forward(S)  # captures the fast frame
+    f_st = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    f_en = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        sim.mesh_dy.x4.copy_(x0)
+        sim.mesh_dy.v4.copy_(v0)
+        flush.zero_()
+        f_st[k].record(stream)
+        sim.forward(S)
+        f_en[k].record(stream)
+    torch.cuda.synchronize()
+    f_ms = sum(s_.elapsed_time(e_) for s_, e_ in zip(f_st, f_en))
+    drape_fast = {"value": V * S * args.steps / (f_ms / 1e3), "unit": UNIT, "ms_per_step": f_ms / args.steps,
+                  "sweep_config": {"variant": "packed" if sim.packed_sweep else fast_variant,
+                                   "lanes_per_vertex": 1 if sim.packed_sweep else variant_forms()[fast_variant][0]},
+                  "note": "the sweep with fused multiply-adds, rsqrtf and a fast divide; contacts unchanged"}
+    sim.fast_math = False
+    sim.sweep_variant, sim.packed_sweep = exact_sweep
+    sim.mesh_dy.x4.copy_(x0)
+    sim.mesh_dy.v4.copy_(v0)
 
     # ---- dominant kernel: Jacobi sweep, instrumented pass ----
     from starlab_physics_gb300._lib import ptr, stream_handle, sx
@@ -1196,6 +1287,7 @@ def main():
         "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": bytes_io, "d2h_bytes_per_step": bytes_io},
         "roofline": roofline,
         "roofline_sweep": roofline_sweep,
+        "fast_math": drape_fast,
         "clocks": clk.summary(),
         "status_flags": status,
     }
@@ -1208,6 +1300,7 @@ def main():
             line["batched512"] = b512
     if rank == 0:
         line["coloring"] = coloring_timing(pkg, with_cpu=not args.no_cpu_baseline)
+        line["plain64"] = plain64_timing(pkg, with_cpu=not args.no_cpu_baseline)
         line["gauss_seidel"] = gauss_seidel_drape(pkg, scene, x0, v0)
     if rank == 0 and not args.no_learned:
         line["learned_batched512"] = learned_batched(pkg)

@@ -881,19 +881,19 @@ __global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_pipe_kernel(cons
             __syncwarp();
         }
     };
-    const int step = nw * 32 * U;
+    const int step = nw * 32 * U, first = st_end + gw * 32 * U, last = dy_end;
     int4 nx[U];
 #pragma unroll
     for (int u = 0; u < U; ++u) {
-        const int t = st_end + gw * 32 * U + 32 * u + lane;
-        nx[u] = t < dy_end ? pairs[t] : make_int4(0, 0, 0, 0);
+        const int t = first + 32 * u + lane;
+        nx[u] = t < last ? pairs[t] : make_int4(0, 0, 0, 0);
     }
-    for (int base = st_end + gw * 32 * U; base < dy_end; base += step) {
+    for (int base = first; base < last; base += step) {
         V3 x[U][4];
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int t = base + 32 * u + lane;
-            if (t < dy_end) {
+            if (t < last) {
                 x[u][0] = mk(y4[nx[u].x]);
                 x[u][1] = mk(y4[nx[u].y]);
                 x[u][2] = mk(y4[nx[u].z]);
@@ -903,12 +903,12 @@ __global__ void __launch_bounds__(PP_BLOCK, MINB) pairs_project_pipe_kernel(cons
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int t = base + step + 32 * u + lane;
-            nx[u] = t < dy_end ? pairs[t] : make_int4(0, 0, 0, 0);
+            nx[u] = t < last ? pairs[t] : make_int4(0, 0, 0, 0);
         }
 #pragma unroll
         for (int u = 0; u < U; ++u) {
             const int t = base + 32 * u + lane;
-            const bool keep = t < dy_end && !box_far(x[u][0], x[u][1], x[u][2], x[u][3], cull_d2);
+            const bool keep = t < last && !box_far(x[u][0], x[u][1], x[u][2], x[u][3], cull_d2);
             const unsigned m = __ballot_sync(0xffffffffu, keep);
             if (keep) s1[n1 + __popc(m & below)] = t;
             n1 += __popc(m);

@@ -125,6 +125,10 @@ class Solver:
         # launch configuration of the contact-pair projection (None: the
         # library's default, sx_contact_pairs_project_variant_info lists all)
         self.pairs_variant = None
+        # the three broad-phase query sets on parallel streams
+        self.concurrent_broadphase = True
+        self._bp_streams = ((torch.cuda.Stream(device=mesh_dy.device), torch.cuda.Stream(device=mesh_dy.device))
+                            if torch.device(mesh_dy.device).type == "cuda" else None)
 
         self.max_num_verts_dy = mesh_dy.num_verts
         self.max_num_edges_dy = mesh_dy.num_edges
@@ -283,19 +287,33 @@ class Solver:
         self._graphs.clear()
 
     def broadphase_lbvh(self):
-        """XPBD.py:187-215: three query sets."""
+        """XPBD.py:187-215: three query sets.  They are independent (each
+        writes its own candidate lists; the status word takes atomic ORs), so
+        the two obstacle query sets run on side streams next to the self
+        query set (parallel branches in a captured frame)."""
         m = self.mesh_dy
         cap = self.cache_size
+        cur = torch.cuda.current_stream(self.device)
+        side = self.concurrent_broadphase and self.mesh_st is not None and self._bp_streams is not None
+        if side:
+            s1, s2 = self._bp_streams
+            s1.wait_stream(cur)
+            s2.wait_stream(cur)
         if self.mesh_st is not None:
-            self.lbvh_st.traverse(m.y4, self.padding, cap, self.vt_st_candidates, self.vt_st_candidates_num,
-                                  self.status)
-            self.lbvh_dy.traverse(self.mesh_st.x4, self.padding, cap, self.tv_st_candidates,
-                                  self.tv_st_candidates_num, self.status)
+            with torch.cuda.stream(s1 if side else cur):
+                self.lbvh_st.traverse(m.y4, self.padding, cap, self.vt_st_candidates, self.vt_st_candidates_num,
+                                      self.status)
+            with torch.cuda.stream(s2 if side else cur):
+                self.lbvh_dy.traverse(self.mesh_st.x4, self.padding, cap, self.tv_st_candidates,
+                                      self.tv_st_candidates_num, self.status)
         if self.self_collision:
             self.lbvh_dy.traverse(m.y4, self.padding, cap, self.vt_dy_candidates, self.vt_dy_candidates_num,
                                   self.status)
         else:
             self.vt_dy_candidates_num.zero_()
+        if side:
+            cur.wait_stream(s1)
+            cur.wait_stream(s2)
         if self.enable_edge_edge:
             ee = self._ensure_ee()
             cap = self.cache_size
@@ -608,7 +626,7 @@ class Solver:
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
                 self.compliance_collision, self.self_collision, self.contact_cull, self.fast_math,
                 self.gauss_seidel, self.sweep_variant, self._packed_sweep,
-                self.pairs_variant, self.enable_edge_edge,
+                self.pairs_variant, self.concurrent_broadphase, self.enable_edge_edge,
                 self.enable_velocity_update, self.mu, self.tol,
                 self.tol_relative,
                 self.check_every,

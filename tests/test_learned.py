@@ -260,23 +260,24 @@ def _small_batch(pkg, seed, n_inst=96):
 @pytest.fixture(scope="module")
 def trained(pkg):
     """A network trained on samples of the plain solver (seed-0 scene, 80
-    iterations per substep), with its loss history and held-out samples of
-    another scene."""
+    iterations per substep, frames 2-15: free fall and the first contacts
+    with the boxes), with its loss history and held-out samples of another
+    scene over the same frames."""
     if not torch.cuda.is_available():
         pytest.skip("needs a GPU")
     L = pkg.learned
     A = _small_batch(pkg, 0)
     A.forward(10)
     A.n_iter = 80
-    feat, tgt = L.collect_samples(A, frames=3, rows_per_substep=32768)
+    feat, tgt = L.collect_samples(A, frames=14, rows_per_substep=8192)
     B = _small_batch(pkg, 1)
     B.forward(10)
     B.n_iter = 80
-    vf, vt = L.collect_samples(B, frames=1, rows_per_substep=16384, seed=3)
+    vf, vt = L.collect_samples(B, frames=14, rows_per_substep=2048, seed=3)
     mlp = pkg.WarmStartMLP(seed=0)
     before = L.evaluate_loss(mlp, vf, vt)
-    h1 = L.train(mlp, feat, tgt, 1500, batch=16384, lr=2e-3)
-    h2 = L.train(mlp, feat, tgt, 500, batch=16384, lr=5e-4)
+    h1 = L.train(mlp, feat, tgt, 3000, batch=16384, lr=2e-3)
+    h2 = L.train(mlp, feat, tgt, 1000, batch=16384, lr=5e-4)
     return mlp, np.concatenate([h1, h2]), before, vf, vt
 
 
@@ -291,9 +292,11 @@ def test_training_reduces_loss(pkg, trained):
     zero = L.evaluate_loss(pkg.WarmStartMLP(params=L.zero_output_params()), vf, vt)
     assert zero == pytest.approx(float(vt[:, :3].pow(2).sum(1).mean().item()), rel=1e-3)
     assert np.all(np.isfinite(hist))
-    assert hist[-50:].mean() < 0.1 * hist[:10].mean()
-    assert after < 0.1 * before
-    assert after < 0.8 * zero, (after, zero)
+    # the samples span free fall and contact, whose corrections the features
+    # only partly determine: the loss falls severalfold, not to zero
+    assert hist[-50:].mean() < 0.5 * hist[:10].mean(), (hist[-50:].mean(), hist[:10].mean())
+    assert after < 0.3 * before, (after, before)
+    assert after < 0.9 * zero, (after, zero)
 
 
 @pytest.mark.gpu
