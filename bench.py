@@ -507,10 +507,12 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
     alg = 12 * n_con + 28 * V
     peak, kind = measured_peak()
 
-    def sweep_roofline(fast, packed=None):
+    def sweep_roofline(fast, packed=None, form=None):
         """One sweep over every instance, timed alone (L2 flushed before each
         launch, mean of 20): the int2 sweep in the tuned variant, or with
-        packed=True the packed staged sweep (None: whichever the tuner chose)."""
+        packed=True the packed sweep, staged (form 0) or direct (form 1) (None:
+        whichever the tuner chose)."""
+        form = sim.packed_form if packed is None and form is None else (form or 0)
         packed = sim.packed_sweep if packed is None else packed
         ev = []
         for _ in range(20):
@@ -518,9 +520,9 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
             a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
             a.record(stream)
             if packed:
-                sx.sx_jacobi_sweep_packed(ptr(sim.x4), ptr(sim.y4), ptr(sim._y_other), ptr(sim.fixed),
-                                          ptr(sim.adj_ptr), ptr(sim.adj_nbr16), ptr(sim.adj_rest32), V, ks, kb, 1,
-                                          1 if fast else 0, stream_handle())
+                sx.sx_jacobi_sweep_packed_v(ptr(sim.x4), ptr(sim.y4), ptr(sim._y_other), ptr(sim.fixed),
+                                            ptr(sim.adj_ptr), ptr(sim.adj_nbr16), ptr(sim.adj_rest32), V, ks, kb, 1,
+                                            form, 1 if fast else 0, stream_handle())
             else:
                 sx.sx_jacobi_sweep_mode(ptr(sim.x4), ptr(sim.y4), ptr(sim._y_other), ptr(sim.fixed),
                                         ptr(sim.adj_ptr), ptr(sim.adj), V, ks, kb, 1, sim.sweep_variant,
@@ -529,7 +531,9 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
             ev.append((a, b))
         torch.cuda.synchronize()
         sweep_ms = sum(a.elapsed_time(b) for a, b in ev) / len(ev)
-        return {"kernel": "jacobi_sweep_staged_kernel" if packed else "jacobi_sweep_kernel", "bound": "hbm",
+        kname = (("jacobi_sweep_packed_kernel" if form else "jacobi_sweep_staged_kernel") if packed
+                 else "jacobi_sweep_kernel")
+        return {"kernel": kname, "bound": "hbm",
                 "achieved": round(alg / (sweep_ms / 1e3) / 1e9, 1), "peak": peak,
                 "unit": "GB/s", "frac": round(alg / (sweep_ms / 1e3) / 1e9 / peak, 4),
                 "algorithmic_bytes_per_launch": alg, "avg_launch_us": round(sweep_ms * 1e3, 2), "peak_source": kind}
@@ -537,7 +541,9 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
     exact_sweep = sweep_roofline(False)
     sweeps = {"int2_exact": sweep_roofline(False, False), "int2_fast": sweep_roofline(True, False)}
     if sim.adj_nbr16 is not None:
-        sweeps |= {"packed_exact": sweep_roofline(False, True), "packed_fast": sweep_roofline(True, True)}
+        sweeps |= {"packed_exact": sweep_roofline(False, True, 0), "packed_fast": sweep_roofline(True, True, 0),
+                   "packed_direct_exact": sweep_roofline(False, True, 1),
+                   "packed_direct_fast": sweep_roofline(True, True, 1)}
     status = int(sim.status.item())
 
     def timed_frames():
@@ -560,14 +566,15 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
     # the same frames with the sweep's fast arithmetic (tolerance-validated,
     # not bit-identical)
     sim.fast_math = True
-    exact_choice = (sim.sweep_variant, sim.packed_sweep)
+    exact_choice = (sim.sweep_variant, sim.packed_sweep, sim.packed_form)
     sim.x4.copy_(x0)
     sim.v4.copy_(v0)
     sim.forward(S)
     fast_variant, _ = sim.autotune()  # tuned for the fast arithmetic on the same batch
     fast = timed_frames() | {"sweep_roofline": sweep_roofline(True),
-                             "sweep_variant": "packed" if sim.packed_sweep else sim.sweep_variant}
-    sim.sweep_variant, sim.packed_sweep = exact_choice
+                             "sweep_variant": (("packed_direct" if sim.packed_form else "packed") if sim.packed_sweep
+                                               else sim.sweep_variant)}
+    sim.sweep_variant, sim.packed_sweep, sim.packed_form = exact_choice
     # one persistent launch per substep (an instance per CTA), exact and fast
     sim.fast_math = False
     sim.persistent = True
@@ -598,7 +605,8 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
                                                             else ""),
             "value": value, "unit": UNIT,
             "ms_per_step": ms_job / steps, "steps": steps, "warmup": warmup,
-            "sweep_variant": "packed" if sim.packed_sweep else sim.sweep_variant,
+            "sweep_variant": (("packed_direct" if sim.packed_form else "packed") if sim.packed_sweep
+                              else sim.sweep_variant),
             "sweep_roofline": exact_sweep,
             "sweep_rooflines": sweeps,
             "fast_math": fast,
@@ -1048,7 +1056,8 @@ def main():
 
     from starlab_physics_gb300.autotune import variant_forms
 
-    sweep_cfg = ("packed", 256, 1, 0) if sim.packed_sweep else sweep_variants()[variant] + variant_forms()[variant]
+    sweep_cfg = ((("packed_direct" if sim.packed_form else "packed"), 256, 1, 0) if sim.packed_sweep
+                 else sweep_variants()[variant] + variant_forms()[variant])
     from starlab_physics_gb300.autotune import pairs_project_variants
 
     pp_variants = pairs_project_variants()
@@ -1110,7 +1119,7 @@ def main():
 
     # ---- the same frame with the sweep's fast arithmetic (not bit-identical;
     # held to the substep tolerance by the GPU tests), sweep re-tuned for it ----
-    exact_sweep = (sim.sweep_variant, sim.packed_sweep)
+    exact_sweep = (sim.sweep_variant, sim.packed_sweep, sim.packed_form)
     sim.fast_math = True
     sim.mesh_dy.x4.copy_(x0)
     sim.mesh_dy.v4.copy_(v0)
@@ -1129,11 +1138,12 @@ def main():
     torch.cuda.synchronize()
     f_ms = sum(s_.elapsed_time(e_) for s_, e_ in zip(f_st, f_en))
     drape_fast = {"value": V * S * args.steps / (f_ms / 1e3), "unit": UNIT, "ms_per_step": f_ms / args.steps,
-                  "sweep_config": {"variant": "packed" if sim.packed_sweep else fast_variant,
+                  "sweep_config": {"variant": (("packed_direct" if sim.packed_form else "packed") if sim.packed_sweep
+                                               else fast_variant),
                                    "lanes_per_vertex": 1 if sim.packed_sweep else variant_forms()[fast_variant][0]},
                   "note": "the sweep with fused multiply-adds, rsqrtf and a fast divide; contacts unchanged"}
     sim.fast_math = False
-    sim.sweep_variant, sim.packed_sweep = exact_sweep
+    sim.sweep_variant, sim.packed_sweep, sim.packed_form = exact_sweep
     sim.mesh_dy.x4.copy_(x0)
     sim.mesh_dy.v4.copy_(v0)
 
@@ -1170,8 +1180,9 @@ def main():
         for k in range(30):
             src, dst = (ya, yb) if k % 2 == 0 else (yb, ya)
             if sim.packed_sweep:
-                sx.sx_jacobi_sweep_packed(ptr(m.x4), ptr(src), ptr(dst), ptr(m.fixed), ptr(m.adj_ptr),
-                                          ptr(m.adj_nbr16), ptr(m.adj_rest32), V, ks_, kb_, 1, 0, stream_handle())
+                sx.sx_jacobi_sweep_packed_v(ptr(m.x4), ptr(src), ptr(dst), ptr(m.fixed), ptr(m.adj_ptr),
+                                            ptr(m.adj_nbr16), ptr(m.adj_rest32), V, ks_, kb_, 1, sim.packed_form, 0,
+                                            stream_handle())
             else:
                 sx.sx_jacobi_sweep_v(ptr(m.x4), ptr(src), ptr(dst), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj), V,
                                      ks_, kb_, 1, sim.sweep_variant, stream_handle())
@@ -1199,7 +1210,8 @@ def main():
     achieved = alg_bytes / (sweep_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     frame_ms = ms / args.steps
-    roofline_sweep = {"kernel": "jacobi_sweep_staged_kernel" if sim.packed_sweep else "jacobi_sweep_kernel",
+    roofline_sweep = {"kernel": ((("jacobi_sweep_packed_kernel" if sim.packed_form else "jacobi_sweep_staged_kernel")
+                                 if sim.packed_sweep else "jacobi_sweep_kernel")),
                 "bound": "hbm", "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                 "traffic": ncu_traffic("jacobi_sweep_kernel_drape256.md"),

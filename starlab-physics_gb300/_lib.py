@@ -118,6 +118,7 @@ SIGNATURES = {
     "sx_color_workspace_bytes": ([I, I], Z),
     "sx_color_edges_greedy": ([P, I, I, I, P, P, P, P, Z, P], I),
     "sx_jacobi_sweep_packed": ([P, P, P, P, P, P, P, I, F, F, I, I, P], I),
+    "sx_jacobi_sweep_packed_v": ([P, P, P, P, P, P, P, I, F, F, I, I, I, P], I),
     "sx_gs_pack": ([P, P, I, P, P, I, P, P, P, P], I),
     "sx_gs_sweep": ([P, P, P, I, F, F, P], I),
 }

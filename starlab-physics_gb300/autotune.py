@@ -47,14 +47,16 @@ def variant_forms() -> list[tuple[int, int]]:
 
 
 def _time_variant(v, args, reps, rounds):
-    """v: a compiled variant of the int2 sweep, or "packed" (the sweep over the
-    packed, shared-memory-staged adjacency)."""
+    """v: a compiled variant of the int2 sweep, "packed" (the sweep over the
+    packed adjacency, staged per block in shared memory) or "packed_direct"
+    (the packed adjacency read from global memory)."""
     x4, y4, out, fixed, adj_ptr, adj, n, ks, kb, bend_y, packed, fast = args
 
     def run():
-        if v == "packed":
-            sx.sx_jacobi_sweep_packed(ptr(x4), ptr(y4), ptr(out), ptr(fixed), ptr(adj_ptr), ptr(packed[0]),
-                                      ptr(packed[1]), n, ks, kb, bend_y, fast, stream_handle())
+        if v in ("packed", "packed_direct"):
+            sx.sx_jacobi_sweep_packed_v(ptr(x4), ptr(y4), ptr(out), ptr(fixed), ptr(adj_ptr), ptr(packed[0]),
+                                        ptr(packed[1]), n, ks, kb, bend_y, 0 if v == "packed" else 1, fast,
+                                        stream_handle())
         else:
             sx.sx_jacobi_sweep_mode(ptr(x4), ptr(y4), ptr(out), ptr(fixed), ptr(adj_ptr), ptr(adj), n, ks, kb, bend_y,
                                     v, fast, stream_handle())
@@ -86,9 +88,9 @@ def tune_sweep(x4, y4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y
     """Fastest sweep variant for these arrays, and the per-variant times (ms).
 
     ``packed``: the (nbr16, rest32) arrays of the packed adjacency, or None;
-    when given, its staged sweep is timed as one more candidate, the last
-    entry of the times (index ``len(variants())``).  ``fast``: time the fast
-    arithmetic."""
+    when given, its staged and its direct sweep are timed as two more
+    candidates, the last entries of the times (indices ``len(variants())`` and
+    ``len(variants()) + 1``).  ``fast``: time the fast arithmetic."""
     if packed is not None and packed[0] is None:
         packed = None
     key = (torch.cuda.get_device_name(x4.device), int(n_verts), int(adj.shape[0]), packed is not None, bool(fast))
@@ -97,7 +99,7 @@ def tune_sweep(x4, y4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y
     out = torch.empty_like(y4)
     args = (x4, y4, out, fixed, adj_ptr, adj, int(n_verts), float(k_spring), float(k_bend), int(bend_on_y), packed,
             1 if fast else 0)
-    cands = list(range(len(variants()))) + (["packed"] if packed is not None else [])
+    cands = list(range(len(variants()))) + (["packed", "packed_direct"] if packed is not None else [])
     times = [_time_variant(v, args, reps, rounds) for v in cands]
     best = int(np.argmin(times))
     _cache[key] = (best, times)

@@ -195,6 +195,7 @@ class BatchedSolver:
         # the sweep over the packed, shared-memory-staged adjacency
         # (sx_jacobi_sweep_packed; same results; autotune() decides)
         self._packed_sweep = False
+        self.packed_form = 0  # the packed sweep staged per block (0) or read from global memory (1)
         # the sweep's fast arithmetic (Solver.fast_math)
         self.fast_math = False
         # one persistent launch per substep (sx_batched_substep) instead of a
@@ -353,9 +354,10 @@ class BatchedSolver:
                                             1 if check else 0, float(self.tol), ref, conv, ptr(self._res3),
                                             ptr(self._res_ws), self._res_ws.numel(), loop, self.n_iter, fast, s)
         elif self.packed_sweep:
-            sx.sx_jacobi_sweep_packed(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
-                                      ptr(self.adj_ptr), ptr(self.adj_nbr16), ptr(self.adj_rest32), self.num_verts,
-                                      k_spring, k_bend, 1 if self.bending_on == "y" else 0, fast, s)
+            sx.sx_jacobi_sweep_packed_v(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
+                                        ptr(self.adj_ptr), ptr(self.adj_nbr16), ptr(self.adj_rest32), self.num_verts,
+                                        k_spring, k_bend, 1 if self.bending_on == "y" else 0, self.packed_form, fast,
+                                        s)
         else:
             sx.sx_jacobi_sweep_mode(ptr(self.x4), ptr(self.y4), ptr(self._y_other), ptr(self.fixed),
                                     ptr(self.adj_ptr), ptr(self.adj), self.num_verts, k_spring, k_bend,
@@ -390,7 +392,7 @@ class BatchedSolver:
             self._forward_eager(n_substeps)
             return
         key = (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
-               self.stiffness_bending, self.n_iter, self.bending_on, self.sweep_variant, self._packed_sweep,
+               self.stiffness_bending, self.n_iter, self.bending_on, self.sweep_variant, self._packed_sweep, self.packed_form,
                self.fast_math, self.tol,
                self.tol_relative, self.persistent, self.persistent_variant,
                self.check_every,
@@ -437,7 +439,8 @@ class BatchedSolver:
                                  fast=self.fast_math)
         from .autotune import variants
 
-        self._packed_sweep = best == len(variants())
+        self._packed_sweep = best >= len(variants())
+        self.packed_form = best - len(variants()) if self._packed_sweep else 0
         self.sweep_variant = 0 if self._packed_sweep else best
         return best, times
 

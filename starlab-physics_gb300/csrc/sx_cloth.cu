@@ -566,6 +566,27 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_staged_kernel(int V, const
         __syncthreads();
     }
 }
+
+// The packed adjacency read straight from global memory, one vertex per
+// thread, G entries' loads issued together: 6 bytes per entry (two loads)
+// instead of the int2 entry's 8 and none of the staging's barriers.  Same
+// projection code, so bit-identical.
+template <int G, int BLOCK, bool BY, bool FAST>
+__global__ void __launch_bounds__(BLOCK) jacobi_sweep_packed_kernel(int V, const float4* __restrict__ x4,
+                                                                       const float4* __restrict__ yin,
+                                                                       float4* __restrict__ yout,
+                                                                       const float* __restrict__ fixed,
+                                                                       const int* __restrict__ ptr,
+                                                                       const short* __restrict__ nbr16,
+                                                                       const unsigned* __restrict__ rest32,
+                                                                       float ks, float kb, int bend_y) {
+    pdl_entry();
+    const int v = blockIdx.x * BLOCK + threadIdx.x;
+    if (v >= V) return;
+    float c2 = 0.0f;
+    yout[v] = sweep_vertex_src<G, BY, FAST, false, true>(v, x4, yin, fixed, __ldg(ptr + v), __ldg(ptr + v + 1),
+                                                         AdjPackedGlobal{nbr16, rest32}, ks, kb, bend_y, &c2);
+}
 }  // namespace sx
 
 extern "C" int sx_jacobi_sweep_packed(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
@@ -587,6 +608,29 @@ extern "C" int sx_jacobi_sweep_packed(const float* x4, const float* y_in4, float
            (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, nbr16, rest32, k_spring, k_bend,
            bend_on_y ? 1 : 0);
     return check_launch("jacobi_sweep_staged_kernel");
+}
+
+extern "C" int sx_jacobi_sweep_packed_v(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
+                                        const int* adj_ptr, const short* nbr16, const unsigned* rest32, int n_verts,
+                                        float k_spring, float k_bend, int bend_on_y, int form, int fast,
+                                        void* stream) {
+    SX_REQUIRE(form == 0 || form == 1, "sx_jacobi_sweep_packed_v: form is 0 (staged) or 1 (direct)");
+    if (form == 0)
+        return sx_jacobi_sweep_packed(x4, y_in4, y_out4, fixed, adj_ptr, nbr16, rest32, n_verts, k_spring, k_bend,
+                                      bend_on_y, fast, stream);
+    SX_REQUIRE(n_verts >= 0, "sx_jacobi_sweep_packed_v: n_verts < 0");
+    if (n_verts == 0) return SX_OK;
+    SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && nbr16 && rest32, "sx_jacobi_sweep_packed_v: null pointer");
+    SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_packed_v: y_in4 and y_out4 must not alias");
+    using K = void (*)(int, const float4*, const float4*, float4*, const float*, const int*, const short*,
+                       const unsigned*, float, float, int);
+    const K k = fast ? (bend_on_y ? jacobi_sweep_packed_kernel<4, 256, true, true>
+                                  : jacobi_sweep_packed_kernel<4, 256, false, true>)
+                     : (bend_on_y ? jacobi_sweep_packed_kernel<4, 256, true, false>
+                                  : jacobi_sweep_packed_kernel<4, 256, false, false>);
+    launch(k, grid_for(n_verts, 256), 256, 0, as_stream(stream), n_verts, (const float4*)x4, (const float4*)y_in4,
+           (float4*)y_out4, fixed, adj_ptr, nbr16, rest32, k_spring, k_bend, bend_on_y ? 1 : 0);
+    return check_launch("jacobi_sweep_packed_kernel");
 }
 
 extern "C" int sx_sewing_sweep(float* y4, const float* fixed, int n_sewn, const int* sewn, const int* sptr,

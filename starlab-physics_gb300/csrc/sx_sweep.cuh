@@ -54,6 +54,16 @@ struct AdjPacked {
     }
 };
 
+// The packed CSR read from global memory through the read-only path.
+struct AdjPackedGlobal {
+    const short* __restrict__ nbr;
+    const unsigned* __restrict__ rest;
+    __device__ __forceinline__ int2 operator()(int v, int k) const {
+        const unsigned r = __ldg(rest + k);
+        return make_int2((v + (int)__ldg(nbr + k)) | (int)(r & 0x80000000u), (int)(r & 0x7fffffffu));
+    }
+};
+
 template <int G, bool BY, bool FAST, bool CHECK, bool YLDG, typename Src>
 __device__ __forceinline__ float4 sweep_vertex_src(int v, const float4* __restrict__ x4, const float4* yin,
                                                    const float* __restrict__ fixed, int b, int e, const Src& src,

@@ -122,6 +122,7 @@ class Solver:
         # launch configuration of the fixed-count sweep (autotune() picks one)
         self.sweep_variant = 0
         self._packed_sweep = False
+        self.packed_form = 0  # the packed sweep staged per block (0) or read from global memory (1)
         # launch configuration of the contact-pair projection (None: the
         # library's default, sx_contact_pairs_project_variant_info lists all)
         self.pairs_variant = None
@@ -215,9 +216,9 @@ class Solver:
             sx.sx_gs_sweep(ptr(m.y4), ptr(cons), start, n_colors, k_spring, k_bend, stream_handle())
             return
         if self.tol is None and self._packed_sweep:
-            sx.sx_jacobi_sweep_packed(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
-                                      ptr(m.adj_nbr16), ptr(m.adj_rest32), m.num_verts, k_spring, k_bend,
-                                      1 if self.bending_on == "y" else 0, fast, stream_handle())
+            sx.sx_jacobi_sweep_packed_v(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
+                                        ptr(m.adj_nbr16), ptr(m.adj_rest32), m.num_verts, k_spring, k_bend,
+                                        1 if self.bending_on == "y" else 0, self.packed_form, fast, stream_handle())
         elif self.tol is None:
             sx.sx_jacobi_sweep_mode(ptr(m.x4), ptr(m.y4), ptr(self._y_other), ptr(m.fixed), ptr(m.adj_ptr),
                                     ptr(m.adj), m.num_verts, k_spring, k_bend, 1 if self.bending_on == "y" else 0,
@@ -538,7 +539,8 @@ class Solver:
                                  packed=(m.adj_nbr16, m.adj_rest32), fast=self.fast_math)
         from .autotune import variants
 
-        self._packed_sweep = best == len(variants())
+        self._packed_sweep = best >= len(variants())
+        self.packed_form = best - len(variants()) if self._packed_sweep else 0
         self.sweep_variant = 0 if self._packed_sweep else best
         return best, times
 
@@ -625,7 +627,7 @@ class Solver:
         return (n_substeps, self.dt, self.dHat, self.damping, self.padding, self.g, self.stiffness_stretch,
                 self.stiffness_bending, self.enable_collision_handling, self.n_iter, self.bending_on, self.rebuild,
                 self.compliance_collision, self.self_collision, self.contact_cull, self.fast_math,
-                self.gauss_seidel, self.sweep_variant, self._packed_sweep,
+                self.gauss_seidel, self.sweep_variant, self._packed_sweep, self.packed_form,
                 self.pairs_variant, self.concurrent_broadphase, self.enable_edge_edge,
                 self.enable_velocity_update, self.mu, self.tol,
                 self.tol_relative,

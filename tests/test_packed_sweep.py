@@ -50,13 +50,17 @@ def test_packed_adjacency_round_trip(pkg):
 def _both(L, x4, y4, fixed, ptr, adj, nbr16, rest32, V, fast, bend_y=1):
     from starlab_physics_gb300._lib import ptr as P, stream_handle
 
-    o1, o2 = torch.empty_like(y4), torch.empty_like(y4)
+    o1, o2, o3 = torch.empty_like(y4), torch.empty_like(y4), torch.empty_like(y4)
     ks, kb = 1e8 / 3.6e5, 1e5 / 3.6e5
     assert L.sx_jacobi_sweep_mode(P(x4), P(y4), P(o1), P(fixed), P(ptr), P(adj), V, ks, kb, bend_y, 0, fast,
                                   stream_handle()) == 0
     assert L.sx_jacobi_sweep_packed(P(x4), P(y4), P(o2), P(fixed), P(ptr), P(nbr16), P(rest32), V, ks, kb, bend_y,
                                     fast, stream_handle()) == 0
+    # the direct form (entries read from global memory) gives the same sums
+    assert L.sx_jacobi_sweep_packed_v(P(x4), P(y4), P(o3), P(fixed), P(ptr), P(nbr16), P(rest32), V, ks, kb, bend_y,
+                                      1, fast, stream_handle()) == 0
     torch.cuda.synchronize()
+    assert torch.equal(o2, o3)
     return o1, o2
 
 
