@@ -101,7 +101,8 @@ def _case_batched(pkg):
 
 def _case_sweeps(pkg):
     """One sweep of each kind over the 512-cloth batch from its rest state:
-    int2 exact, int2 fast, packed exact, packed fast."""
+    int2 exact, int2 fast, packed staged exact and fast, packed direct exact
+    and fast."""
     import torch
     from starlab_physics_gb300._lib import ptr, stream_handle, sx
 
@@ -112,10 +113,11 @@ def _case_sweeps(pkg):
     for fast in (0, 1):
         sx.sx_jacobi_sweep_mode(ptr(sim.x4), ptr(sim.x4), ptr(out), ptr(sim.fixed), ptr(sim.adj_ptr), ptr(sim.adj),
                                 sim.num_verts, ks, kb, 1, 0, fast, stream_handle())
-    for fast in (0, 1):
-        sx.sx_jacobi_sweep_packed(ptr(sim.x4), ptr(sim.x4), ptr(out), ptr(sim.fixed), ptr(sim.adj_ptr),
-                                  ptr(sim.adj_nbr16), ptr(sim.adj_rest32), sim.num_verts, ks, kb, 1, fast,
-                                  stream_handle())
+    for form in (0, 1):
+        for fast in (0, 1):
+            sx.sx_jacobi_sweep_packed_v(ptr(sim.x4), ptr(sim.x4), ptr(out), ptr(sim.fixed), ptr(sim.adj_ptr),
+                                        ptr(sim.adj_nbr16), ptr(sim.adj_rest32), sim.num_verts, ks, kb, 1, form, fast,
+                                        stream_handle())
 
 
 def _case_color(pkg):
@@ -541,9 +543,16 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
     exact_sweep = sweep_roofline(False)
     sweeps = {"int2_exact": sweep_roofline(False, False), "int2_fast": sweep_roofline(True, False)}
     if sim.adj_nbr16 is not None:
-        sweeps |= {"packed_exact": sweep_roofline(False, True, 0), "packed_fast": sweep_roofline(True, True, 0),
-                   "packed_direct_exact": sweep_roofline(False, True, 1),
-                   "packed_direct_fast": sweep_roofline(True, True, 1)}
+        sweeps |= {"packed_exact": sweep_roofline(False, True, 0), "packed_fast": sweep_roofline(True, True, 0)}
+        from starlab_physics_gb300.autotune import packed_forms
+
+        for fast_, name in ((False, "packed_direct_exact"), (True, "packed_direct_fast")):
+            best_ = None
+            for f_ in range(1, packed_forms()):
+                r_ = sweep_roofline(fast_, True, f_) | {"form": f_}
+                if best_ is None or r_["avg_launch_us"] < best_["avg_launch_us"]:
+                    best_ = r_
+            sweeps[name] = best_
     status = int(sim.status.item())
 
     def timed_frames():
@@ -572,7 +581,7 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
     sim.forward(S)
     fast_variant, _ = sim.autotune()  # tuned for the fast arithmetic on the same batch
     fast = timed_frames() | {"sweep_roofline": sweep_roofline(True),
-                             "sweep_variant": (("packed_direct" if sim.packed_form else "packed") if sim.packed_sweep
+                             "sweep_variant": ((f"packed_direct_{sim.packed_form}" if sim.packed_form else "packed") if sim.packed_sweep
                                                else sim.sweep_variant)}
     sim.sweep_variant, sim.packed_sweep, sim.packed_form = exact_choice
     # one persistent launch per substep (an instance per CTA), exact and fast
@@ -605,7 +614,7 @@ def batched512(pkg, steps=5, warmup=2, world=1, rank=0):
                                                             else ""),
             "value": value, "unit": UNIT,
             "ms_per_step": ms_job / steps, "steps": steps, "warmup": warmup,
-            "sweep_variant": (("packed_direct" if sim.packed_form else "packed") if sim.packed_sweep
+            "sweep_variant": ((f"packed_direct_{sim.packed_form}" if sim.packed_form else "packed") if sim.packed_sweep
                               else sim.sweep_variant),
             "sweep_roofline": exact_sweep,
             "sweep_rooflines": sweeps,
@@ -1056,7 +1065,7 @@ def main():
 
     from starlab_physics_gb300.autotune import variant_forms
 
-    sweep_cfg = ((("packed_direct" if sim.packed_form else "packed"), 256, 1, 0) if sim.packed_sweep
+    sweep_cfg = (((f"packed_direct_{sim.packed_form}" if sim.packed_form else "packed"), 256, 1, 0) if sim.packed_sweep
                  else sweep_variants()[variant] + variant_forms()[variant])
     from starlab_physics_gb300.autotune import pairs_project_variants
 
@@ -1138,7 +1147,7 @@ def main():
     torch.cuda.synchronize()
     f_ms = sum(s_.elapsed_time(e_) for s_, e_ in zip(f_st, f_en))
     drape_fast = {"value": V * S * args.steps / (f_ms / 1e3), "unit": UNIT, "ms_per_step": f_ms / args.steps,
-                  "sweep_config": {"variant": (("packed_direct" if sim.packed_form else "packed") if sim.packed_sweep
+                  "sweep_config": {"variant": ((f"packed_direct_{sim.packed_form}" if sim.packed_form else "packed") if sim.packed_sweep
                                                else fast_variant),
                                    "lanes_per_vertex": 1 if sim.packed_sweep else variant_forms()[fast_variant][0]},
                   "note": "the sweep with fused multiply-adds, rsqrtf and a fast divide; contacts unchanged"}

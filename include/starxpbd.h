@@ -109,9 +109,12 @@ int sx_jacobi_sweep_mode(const float* x4, const float* y_in4, float* y_out4, con
 int sx_jacobi_sweep_packed(const float* x4, const float* y_in4, float* y_out4, const float* fixed, const int* adj_ptr,
                            const short* nbr16, const unsigned* rest32, int n_verts, float k_spring, float k_bend,
                            int bend_on_y, int fast, void* stream);
-/* sx_jacobi_sweep_packed in one of two forms (bit-identical): form 0 stages
- * each block's entries in shared memory (sx_jacobi_sweep_packed); form 1 reads
- * them straight from global memory, four entries' loads issued together. */
+/* sx_jacobi_sweep_packed in one of sx_jacobi_sweep_packed_forms() forms
+ * (bit-identical): form 0 stages each block's entries in shared memory
+ * (sx_jacobi_sweep_packed); forms 1.. read them straight from global memory,
+ * one vertex per thread, in several launch configurations (entries whose loads
+ * are issued together, threads per block) for an autotuner. */
+int sx_jacobi_sweep_packed_forms(void);
 int sx_jacobi_sweep_packed_v(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
                              const int* adj_ptr, const short* nbr16, const unsigned* rest32, int n_verts,
                              float k_spring, float k_bend, int bend_on_y, int form, int fast, void* stream);

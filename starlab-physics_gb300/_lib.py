@@ -119,6 +119,7 @@ SIGNATURES = {
     "sx_color_edges_greedy": ([P, I, I, I, P, P, P, P, Z, P], I),
     "sx_jacobi_sweep_packed": ([P, P, P, P, P, P, P, I, F, F, I, I, P], I),
     "sx_jacobi_sweep_packed_v": ([P, P, P, P, P, P, P, I, F, F, I, I, I, P], I),
+    "sx_jacobi_sweep_packed_forms": ([], I),
     "sx_gs_pack": ([P, P, I, P, P, I, P, P, P, P], I),
     "sx_gs_sweep": ([P, P, P, I, F, F, P], I),
 }
@@ -185,7 +186,7 @@ class _Calls:
         if name not in SIGNATURES:
             raise AttributeError(name)
         if SIGNATURES[name][1] is I and name not in ("sx_version", "sx_mlp_param_count", "sx_mlp_bf16_count",
-                                                     "sx_jacobi_sweep_variants",
+                                                     "sx_jacobi_sweep_variants", "sx_jacobi_sweep_packed_forms",
                                                      "sx_contact_pairs_project_variants",
                                                      "sx_contact_pairs_project_variant_pipelined",
                                                      "sx_batched_substep_variants",

@@ -46,17 +46,21 @@ def variant_forms() -> list[tuple[int, int]]:
     return out
 
 
+def packed_forms() -> int:
+    """Forms of the packed sweep (0 staged, 1.. direct launch configurations)."""
+    return int(load().sx_jacobi_sweep_packed_forms())
+
+
 def _time_variant(v, args, reps, rounds):
-    """v: a compiled variant of the int2 sweep, "packed" (the sweep over the
-    packed adjacency, staged per block in shared memory) or "packed_direct"
-    (the packed adjacency read from global memory)."""
+    """v: a compiled variant of the int2 sweep, or ("packed", form): the sweep
+    over the packed adjacency, staged per block in shared memory (form 0) or
+    read from global memory (forms 1..)."""
     x4, y4, out, fixed, adj_ptr, adj, n, ks, kb, bend_y, packed, fast = args
 
     def run():
-        if v in ("packed", "packed_direct"):
+        if isinstance(v, tuple):
             sx.sx_jacobi_sweep_packed_v(ptr(x4), ptr(y4), ptr(out), ptr(fixed), ptr(adj_ptr), ptr(packed[0]),
-                                        ptr(packed[1]), n, ks, kb, bend_y, 0 if v == "packed" else 1, fast,
-                                        stream_handle())
+                                        ptr(packed[1]), n, ks, kb, bend_y, v[1], fast, stream_handle())
         else:
             sx.sx_jacobi_sweep_mode(ptr(x4), ptr(y4), ptr(out), ptr(fixed), ptr(adj_ptr), ptr(adj), n, ks, kb, bend_y,
                                     v, fast, stream_handle())
@@ -88,9 +92,9 @@ def tune_sweep(x4, y4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y
     """Fastest sweep variant for these arrays, and the per-variant times (ms).
 
     ``packed``: the (nbr16, rest32) arrays of the packed adjacency, or None;
-    when given, its staged and its direct sweep are timed as two more
-    candidates, the last entries of the times (indices ``len(variants())`` and
-    ``len(variants()) + 1``).  ``fast``: time the fast arithmetic."""
+    when given, every form of the packed sweep is timed as one more candidate,
+    the last entries of the times (index ``len(variants()) + form``).
+    ``fast``: time the fast arithmetic."""
     if packed is not None and packed[0] is None:
         packed = None
     key = (torch.cuda.get_device_name(x4.device), int(n_verts), int(adj.shape[0]), packed is not None, bool(fast))
@@ -99,7 +103,8 @@ def tune_sweep(x4, y4, fixed, adj_ptr, adj, n_verts, k_spring, k_bend, bend_on_y
     out = torch.empty_like(y4)
     args = (x4, y4, out, fixed, adj_ptr, adj, int(n_verts), float(k_spring), float(k_bend), int(bend_on_y), packed,
             1 if fast else 0)
-    cands = list(range(len(variants()))) + (["packed", "packed_direct"] if packed is not None else [])
+    cands = list(range(len(variants()))) + ([("packed", f) for f in range(packed_forms())] if packed is not None
+                                            else [])
     times = [_time_variant(v, args, reps, rounds) for v in cands]
     best = int(np.argmin(times))
     _cache[key] = (best, times)

@@ -587,6 +587,25 @@ __global__ void __launch_bounds__(BLOCK) jacobi_sweep_packed_kernel(int V, const
     yout[v] = sweep_vertex_src<G, BY, FAST, false, true>(v, x4, yin, fixed, __ldg(ptr + v), __ldg(ptr + v + 1),
                                                          AdjPackedGlobal{nbr16, rest32}, ks, kb, bend_y, &c2);
 }
+
+// Forms of the packed sweep: 0 staged (sx_jacobi_sweep_packed), then the
+// direct kernel in several (entries per load batch, threads per block).
+using PackedKernel = void (*)(int, const float4*, const float4*, float4*, const float*, const int*, const short*,
+                              const unsigned*, float, float, int);
+struct PackedForm {
+    int g, block;
+    PackedKernel kern, kern_y, fast, fast_y;
+};
+#define SX_PACKED_FORM(G, B)                                                                                    \
+    {G, B, jacobi_sweep_packed_kernel<G, B, false, false>, jacobi_sweep_packed_kernel<G, B, true, false>,       \
+     jacobi_sweep_packed_kernel<G, B, false, true>, jacobi_sweep_packed_kernel<G, B, true, true>}
+static const PackedForm kPackedForms[] = {
+    {0, SW_BLOCK, nullptr, nullptr, nullptr, nullptr},  // staged: sx_jacobi_sweep_packed
+    SX_PACKED_FORM(4, 256), SX_PACKED_FORM(2, 256), SX_PACKED_FORM(6, 256), SX_PACKED_FORM(4, 128),
+    SX_PACKED_FORM(3, 512),
+};
+#undef SX_PACKED_FORM
+constexpr int kNumPackedForms = sizeof(kPackedForms) / sizeof(kPackedForms[0]);
 }  // namespace sx
 
 extern "C" int sx_jacobi_sweep_packed(const float* x4, const float* y_in4, float* y_out4, const float* fixed,
@@ -614,7 +633,7 @@ extern "C" int sx_jacobi_sweep_packed_v(const float* x4, const float* y_in4, flo
                                         const int* adj_ptr, const short* nbr16, const unsigned* rest32, int n_verts,
                                         float k_spring, float k_bend, int bend_on_y, int form, int fast,
                                         void* stream) {
-    SX_REQUIRE(form == 0 || form == 1, "sx_jacobi_sweep_packed_v: form is 0 (staged) or 1 (direct)");
+    SX_REQUIRE(form >= 0 && form < kNumPackedForms, "sx_jacobi_sweep_packed_v: bad form");
     if (form == 0)
         return sx_jacobi_sweep_packed(x4, y_in4, y_out4, fixed, adj_ptr, nbr16, rest32, n_verts, k_spring, k_bend,
                                       bend_on_y, fast, stream);
@@ -622,16 +641,14 @@ extern "C" int sx_jacobi_sweep_packed_v(const float* x4, const float* y_in4, flo
     if (n_verts == 0) return SX_OK;
     SX_REQUIRE(x4 && y_in4 && y_out4 && fixed && adj_ptr && nbr16 && rest32, "sx_jacobi_sweep_packed_v: null pointer");
     SX_REQUIRE(y_in4 != y_out4, "sx_jacobi_sweep_packed_v: y_in4 and y_out4 must not alias");
-    using K = void (*)(int, const float4*, const float4*, float4*, const float*, const int*, const short*,
-                       const unsigned*, float, float, int);
-    const K k = fast ? (bend_on_y ? jacobi_sweep_packed_kernel<4, 256, true, true>
-                                  : jacobi_sweep_packed_kernel<4, 256, false, true>)
-                     : (bend_on_y ? jacobi_sweep_packed_kernel<4, 256, true, false>
-                                  : jacobi_sweep_packed_kernel<4, 256, false, false>);
-    launch(k, grid_for(n_verts, 256), 256, 0, as_stream(stream), n_verts, (const float4*)x4, (const float4*)y_in4,
-           (float4*)y_out4, fixed, adj_ptr, nbr16, rest32, k_spring, k_bend, bend_on_y ? 1 : 0);
+    const PackedForm& pf = kPackedForms[form];
+    const PackedKernel k = fast ? (bend_on_y ? pf.fast_y : pf.fast) : (bend_on_y ? pf.kern_y : pf.kern);
+    launch(k, grid_for(n_verts, pf.block), pf.block, 0, as_stream(stream), n_verts, (const float4*)x4,
+           (const float4*)y_in4, (float4*)y_out4, fixed, adj_ptr, nbr16, rest32, k_spring, k_bend, bend_on_y ? 1 : 0);
     return check_launch("jacobi_sweep_packed_kernel");
 }
+
+extern "C" int sx_jacobi_sweep_packed_forms(void) { return kNumPackedForms; }
 
 extern "C" int sx_sewing_sweep(float* y4, const float* fixed, int n_sewn, const int* sewn, const int* sptr,
                                const int* partner, float k, float* scratch4, void* stream) {

@@ -56,11 +56,13 @@ def _both(L, x4, y4, fixed, ptr, adj, nbr16, rest32, V, fast, bend_y=1):
                                   stream_handle()) == 0
     assert L.sx_jacobi_sweep_packed(P(x4), P(y4), P(o2), P(fixed), P(ptr), P(nbr16), P(rest32), V, ks, kb, bend_y,
                                     fast, stream_handle()) == 0
-    # the direct form (entries read from global memory) gives the same sums
-    assert L.sx_jacobi_sweep_packed_v(P(x4), P(y4), P(o3), P(fixed), P(ptr), P(nbr16), P(rest32), V, ks, kb, bend_y,
-                                      1, fast, stream_handle()) == 0
-    torch.cuda.synchronize()
-    assert torch.equal(o2, o3)
+    # every direct form (entries read from global memory) gives the same sums
+    for form in range(1, int(L.sx_jacobi_sweep_packed_forms())):
+        o3.fill_(float("nan"))
+        assert L.sx_jacobi_sweep_packed_v(P(x4), P(y4), P(o3), P(fixed), P(ptr), P(nbr16), P(rest32), V, ks, kb,
+                                          bend_y, form, fast, stream_handle()) == 0
+        torch.cuda.synchronize()
+        assert torch.equal(o2, o3), form
     return o1, o2
 
 
