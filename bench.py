@@ -447,9 +447,31 @@ def lbvh_soup(pkg, reps=10, with_cpu=True):
         torch.cuda.synchronize()
         tb.append(a.elapsed_time(b))
         tq.append(c.elapsed_time(d))
+    # the same build under the reference's rule for equal codes (lbvh_cell.py:256-264), whose hierarchy can be
+    # malformed where codes repeat, so its refit is the one-thread-per-leaf climb
+    bvh0 = pkg.LBVH(n, "cuda", tie=0)
+
+    def build0():
+        sx.sx_scene_aabb(ptr(V4), V4.shape[0], 0.0, ptr(box), stream_handle())
+        bvh0.build(fmn, fmx, box)
+
+    build0()
+    torch.cuda.synchronize()
+    t0s = []
+    for _ in range(reps):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        build0()
+        b.record(stream)
+        torch.cuda.synchronize()
+        t0s.append(a.elapsed_time(b))
+    codes = bvh0.codes.cpu().numpy()
     out = {"workload": "2^20-triangle soup, 2^20 queries, padding 2e-3", "build_ms": round(sum(tb) / reps, 4),
            "query_ms": round(sum(tq) / reps, 4), "candidates": int(num.sum().item()),
-           "sort_bytes_per_build": n * 64}
+           "sort_bytes_per_build": n * 64, "tie_rule": "equal codes ordered by index (always a valid tree)",
+           "build_ms_reference_tie_rule": round(sum(t0s) / reps, 4),
+           "repeated_codes": int(n - np.unique(codes).size)}
     if with_cpu:
         from oracle import pyoracle as po
 
@@ -461,6 +483,11 @@ def lbvh_soup(pkg, reps=10, with_cpu=True):
         t1 = time.perf_counter()
         ok = bool(np.array_equal(bvh.sorted_ids.cpu().numpy(), fb.sorted_ids)
                   and np.array_equal(bvh.child_a.cpu().numpy(), fb.child_a))
+        fb0 = po.FaceBVH(mn, mx, po.scene_aabb(vv, 0.0), tie=0)
+        out["matches_oracle_reference_tie_rule"] = bool(
+            np.array_equal(bvh0.sorted_ids.cpu().numpy(), fb0.sorted_ids)
+            and np.array_equal(bvh0.child_a.cpu().numpy(), fb0.child_a)
+            and np.array_equal(bvh0.child_b.cpu().numpy(), fb0.child_b))
         out["cpu_baseline_build_ms"] = round(1e3 * (t1 - t0), 1)
         out["cpu_baseline_kind"] = "port (serial oracle)"
         out["matches_oracle"] = ok
