@@ -427,9 +427,20 @@ __device__ __forceinline__ void tmem_ld16(unsigned taddr, unsigned (&r)[16]) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// SiLU with the fast exponential and division: the tensor-core path's hidden
-// activations are rounded to BF16, far coarser than these approximations
-__device__ __forceinline__ float silu_fast(float z) { return __fdividef(z, 1.0f + __expf(-z)); }
+// SiLU through the hardware tanh: z * sigmoid(z) = h + h * tanh(h) with
+// h = z / 2, one special-function instruction instead of an exponential and a
+// reciprocal (the epilogue's special-function unit was its limit).  The
+// tensor-core path's hidden activations are rounded to BF16, far coarser than
+// tanh.approx's error.
+__device__ __forceinline__ float tanh_hw(float x) {
+    float y;
+    asm("tanh.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+__device__ __forceinline__ float silu_fast(float z) {
+    const float h = 0.5f * z;
+    return __fmaf_rn(h, tanh_hw(h), h);
+}
 
 // 32 accumulator columns of this thread's row (at taddr) + bias -> SiLU ->
 // BF16 columns [c0, c0 + 32) of row `row` of A2
