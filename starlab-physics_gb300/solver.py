@@ -126,8 +126,10 @@ class Solver:
         # launch configuration of the contact-pair projection (None: the
         # library's default, sx_contact_pairs_project_variant_info lists all)
         self.pairs_variant = None
-        # the three broad-phase query sets on parallel streams
+        # the broad phase on side streams: the per-substep BVH build beside
+        # compute_y and the first sweep, the three query sets beside each other
         self.concurrent_broadphase = True
+        self._bvh_join = None  # side stream of a BVH build the broad phase must wait for
         self._bp_streams = ((torch.cuda.Stream(device=mesh_dy.device), torch.cuda.Stream(device=mesh_dy.device))
                             if torch.device(mesh_dy.device).type == "cuda" else None)
 
@@ -416,6 +418,9 @@ class Solver:
                 # the reference always has a static mesh when collisions are on
                 self.vt_st_candidates_num.zero_()
             if first_iteration:
+                if self._bvh_join is not None:
+                    torch.cuda.current_stream(self.device).wait_stream(self._bvh_join)
+                    self._bvh_join = None
                 self.broadphase_lbvh()
                 if not self.record_pairs:
                     self.build_contact_pairs()
@@ -468,7 +473,17 @@ class Solver:
 
     def substep(self, dt_sub):
         if self.enable_collision_handling and self.rebuild == "substep":
-            self.build_bvhs()
+            if self.concurrent_broadphase and self._bp_streams is not None:
+                # the build reads only x: it runs beside compute_y and the first
+                # sweep, and the broad phase waits for it
+                cur = torch.cuda.current_stream(self.device)
+                side = self._bp_streams[0]
+                side.wait_stream(cur)
+                with torch.cuda.stream(side):
+                    self.build_bvhs()
+                self._bvh_join = side
+            else:
+                self.build_bvhs()
         self.compute_y(dt_sub)
         ce = self.check_every
         if self.tol is not None:
