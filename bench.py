@@ -120,6 +120,26 @@ def _case_sweeps(pkg):
                                         stream_handle())
 
 
+def _case_drape_sweeps(pkg):
+    """One sweep of each storage form over the 256 x 256 drape's cloth from its
+    predicted state (int2, packed staged, packed direct forms), exact arithmetic."""
+    import torch
+    from starlab_physics_gb300._lib import ptr, stream_handle, sx
+
+    scene = pkg.scenes.drape256()
+    sim = pkg.scenes.make_solver(scene, device="cuda")
+    m = sim.mesh_dy
+    dt = scene.dt / scene.n_substeps
+    sim.compute_y(dt)
+    ks, kb = sim.stiffness_bending * dt * dt, sim.stiffness_stretch * dt * dt
+    out = torch.empty_like(m.y4)
+    sx.sx_jacobi_sweep_mode(ptr(m.x4), ptr(m.y4), ptr(out), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj), m.num_verts, ks,
+                            kb, 1, 7, 0, stream_handle())
+    for form in range(int(sx.sx_jacobi_sweep_packed_forms())):
+        sx.sx_jacobi_sweep_packed_v(ptr(m.x4), ptr(m.y4), ptr(out), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj_nbr16),
+                                    ptr(m.adj_rest32), m.num_verts, ks, kb, 1, form, 0, stream_handle())
+
+
 def _case_color(pkg):
     """Colouring of the 256 x 256 cloth's edges (one call)."""
     _, f = pkg.grid_cloth(256)
@@ -135,7 +155,7 @@ def _case_learned(pkg):
 
 
 PROFILE_CASES = {"drape": _case_drape, "soup": _case_soup, "batched": _case_batched, "color": _case_color,
-                 "learned": _case_learned, "sweeps": _case_sweeps}
+                 "learned": _case_learned, "sweeps": _case_sweeps, "drape_sweeps": _case_drape_sweeps}
 
 
 def run_profile_case(name):
@@ -1247,11 +1267,12 @@ def main():
     achieved = alg_bytes / (sweep_ms / 1e3) / 1e9
     peak, peak_kind = measured_peak()
     frame_ms = ms / args.steps
-    roofline_sweep = {"kernel": ((("jacobi_sweep_packed_kernel" if sim.packed_form else "jacobi_sweep_staged_kernel")
-                                 if sim.packed_sweep else "jacobi_sweep_kernel")),
+    sweep_kname = (("jacobi_sweep_packed_kernel" if sim.packed_form else "jacobi_sweep_staged_kernel")
+                   if sim.packed_sweep else "jacobi_sweep_kernel")
+    roofline_sweep = {"kernel": sweep_kname,
                 "bound": "hbm", "achieved": round(achieved, 1),
                 "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
-                "traffic": ncu_traffic("jacobi_sweep_kernel_drape256.md"),
+                "traffic": ncu_traffic(sweep_kname + "_drape256.md"),
                 "algorithmic_bytes_per_launch": alg_bytes, "avg_launch_us": round(sweep_ms * 1e3, 3),
                 "timing": "CUDA events around a graph of 30 back-to-back sweeps on the frame's state (L2 flushed "
                           "before each replay), median of 5; one eager launch between events: "
