@@ -145,6 +145,18 @@ size_t sx_residual_workspace_bytes(int n_verts);
 int sx_constraint_residual(const float* p4, const int* adj_ptr, const int* adj, int n_verts, double* out3, void* ws,
                            size_t ws_bytes, void* stream);
 
+/* System energy in FP64 (no counterpart in the reference): out3 (device) =
+ * {kinetic 1/2 sum m |v|^2, gravitational -sum m (g . x), elastic
+ * 1/2 sum k C^2} with m = 1/m_inv over vertices with m_inv > 0, C = |x_a - x_b|
+ * - l0 over the springs (k = k_spring) and bending pairs (k = k_bend) of the
+ * adjacency (adj_ptr/adj as for sx_jacobi_sweep).  Every term in double from
+ * the float inputs, sums in a fixed order (deterministic).  Workspace:
+ * sx_energy_workspace_bytes(n_verts). */
+size_t sx_energy_workspace_bytes(int n_verts);
+int sx_system_energy(const float* x4, const float* v4, const float* m_inv, const int* adj_ptr, const int* adj,
+                     int n_verts, float k_spring, float k_bend, float gx, float gy, float gz, double* out3, void* ws,
+                     size_t ws_bytes, void* stream);
+
 /* Iterating to a residual (no counterpart in the reference, which runs one
  * sweep per substep).  conv is a device int[8]:
  *   conv[0] stop iteration of the current substep (-1: not converged),

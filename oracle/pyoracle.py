@@ -431,6 +431,31 @@ def constraint_residual(p4, edges, l0, bend, bl0):
     return residual(p4, ptr, adj)
 
 
+def system_energy(x4, v4, m_inv, ptr, adj, ks, kb, g):
+    """Kinetic, gravitational and elastic energy in float64 (the library's
+    sx_system_energy; no counterpart in the reference): masses 1/m_inv where
+    m_inv > 0, elastic 1/2 k C^2 per constraint with every constraint seen from
+    both adjacency endpoints (1/4 per entry), k = kb for bending entries (bit 31
+    of the neighbour word) else ks."""
+    x = x4[:, :3].astype(np.float64)
+    v = v4[:, :3].astype(np.float64)
+    mi = m_inv.astype(np.float32)
+    has = mi > 0
+    m = np.zeros(x.shape[0])
+    m[has] = 1.0 / mi[has].astype(np.float64)
+    ek = 0.5 * float((m * (v * v).sum(1)).sum())
+    eg = -float((m * (x @ np.asarray(g, np.float32).astype(np.float64))).sum())  # g arrives as float32
+    ptr = np.asarray(ptr, np.int64)
+    a = np.asarray(adj, np.int32).reshape(-1, 2)
+    owner = np.repeat(np.arange(x.shape[0]), np.diff(ptr))
+    nbr = a[:, 0] & 0x7FFFFFFF
+    rest = a[:, 1].view(np.float32).astype(np.float64)
+    C = np.linalg.norm(x[owner] - x[nbr], axis=1) - rest
+    k = np.where(a[:, 0] < 0, kb, ks)
+    ee = float((0.25 * k * C * C).sum())
+    return ek, eg, ee
+
+
 # ---- learned warm start (no counterpart in the reference) --------------------
 # Parameter blob (FP32, 6792): W1[64][32] | b1[64] | W2[64][64] | b2[64] |
 # W3[8][64] | b3[8]; the BF16 copy holds the three weight matrices.

@@ -60,6 +60,8 @@ SIGNATURES = {
     "sx_velocity_contacts": ([I, I, P, P, I, P, P, P, P, P, P, P, P, P, F, P, P, P, P], I),
     "sx_sewing_sweep": ([P, P, I, P, P, P, F, P, P], I),
     "sx_residual_workspace_bytes": ([I], Z),
+    "sx_energy_workspace_bytes": ([I], Z),
+    "sx_system_energy": ([P, P, P, P, P, I, F, F, F, F, F, P, P, Z, P], I),
     "sx_constraint_residual": ([P, P, P, I, P, P, Z, P], I),
     "sx_convergence_begin": ([P, I, I, P], I),
     "sx_jacobi_sweep_checked": ([P, P, P, P, P, P, I, F, F, I, I, C.c_double, P, P, P, P, Z, C.c_ulonglong, I, P], I),

@@ -874,6 +874,94 @@ extern "C" int sx_constraint_residual(const float* p4, const int* adj_ptr, const
     return residual_finish(n_verts, adj_ptr, ws, out3, nullptr, 0, 0.0, nullptr, 0ull, 0, s);
 }
 
+// ---------------------------------------------------------------------------
+// System energy in FP64 (no counterpart in the reference): kinetic
+// 1/2 sum m |v|^2 and gravitational -sum m (g . x) over vertices with mass
+// (m = 1 / m_inv, m_inv > 0), and elastic 1/2 sum k C^2 over the springs and
+// bending pairs (C = |p_a - p_b| - l0, every constraint seen from both
+// endpoints, so the entries carry 1/4 each; k the spring or the bending
+// stiffness).  Every term is evaluated in double from the float positions;
+// per-block sums in a fixed order (thread, xor tree over the warp, warps in
+// index order), then the blocks in index order by one block: deterministic.
+// ---------------------------------------------------------------------------
+namespace sx {
+constexpr int EN_BLOCK = 256;
+
+__global__ void __launch_bounds__(EN_BLOCK) energy_partial_kernel(int V, const float4* __restrict__ x4,
+                                                               const float4* __restrict__ v4,
+                                                               const float* __restrict__ m_inv,
+                                                               const int* __restrict__ ptr,
+                                                               const int2* __restrict__ adj, double ks, double kb,
+                                                               double gx, double gy, double gz,
+                                                               double* __restrict__ partial) {
+    pdl_entry();
+    __shared__ double wsum[3][EN_BLOCK / 32];
+    const int v = blockIdx.x * EN_BLOCK + threadIdx.x;
+    double ek = 0.0, eg = 0.0, ee = 0.0;
+    if (v < V) {
+        const float4 p = x4[v];
+        const float mi = m_inv[v];
+        if (mi > 0.0f) {
+            const double m = 1.0 / (double)mi;
+            const float4 u = v4[v];
+            ek = 0.5 * m * (((double)u.x * u.x + (double)u.y * u.y) + (double)u.z * u.z);
+            eg = -m * ((gx * p.x + gy * p.y) + gz * p.z);
+        }
+        for (int k = ptr[v]; k < ptr[v + 1]; ++k) {
+            const int2 a = adj[k];
+            const float4 o = x4[a.x & 0x7fffffff];
+            const double ex = (double)p.x - o.x, ey = (double)p.y - o.y, ez = (double)p.z - o.z;
+            const double C = sqrt((ex * ex + ey * ey) + ez * ez) - (double)__int_as_float(a.y);
+            ee += 0.25 * (a.x < 0 ? kb : ks) * C * C;
+        }
+    }
+    double t[3] = {ek, eg, ee};
+#pragma unroll
+    for (int q = 0; q < 3; ++q) {
+        double w = t[q];
+        for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+        if ((threadIdx.x & 31) == 0) wsum[q][threadIdx.x >> 5] = w;
+    }
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        double a = 0.0;
+        for (int w = 0; w < EN_BLOCK / 32; ++w) a += wsum[threadIdx.x][w];
+        partial[3 * (size_t)blockIdx.x + threadIdx.x] = a;
+    }
+}
+
+__global__ void energy_finish_kernel(int nb, const double* __restrict__ partial, double* out3) {
+    pdl_entry();
+    if (threadIdx.x >= 3) return;
+    double a = 0.0;
+    for (int b = 0; b < nb; ++b) a += partial[3 * (size_t)b + threadIdx.x];
+    out3[threadIdx.x] = a;
+}
+}  // namespace sx
+
+extern "C" size_t sx_energy_workspace_bytes(int n_verts) {
+    return (size_t)3 * sizeof(double) * (size_t)grid_for(n_verts > 0 ? n_verts : 1, EN_BLOCK);
+}
+
+extern "C" int sx_system_energy(const float* x4, const float* v4, const float* m_inv, const int* adj_ptr,
+                                const int* adj, int n_verts, float k_spring, float k_bend, float gx, float gy,
+                                float gz, double* out3, void* ws, size_t ws_bytes, void* stream) {
+    SX_REQUIRE(n_verts >= 0, "sx_system_energy: n_verts < 0");
+    SX_REQUIRE(out3 && ws && (n_verts == 0 || (x4 && v4 && m_inv && adj_ptr && adj)),
+               "sx_system_energy: null pointer");
+    SX_REQUIRE(ws_bytes >= sx_energy_workspace_bytes(n_verts), "sx_system_energy: workspace too small");
+    cudaStream_t s = as_stream(stream);
+    if (n_verts == 0) {
+        SX_CUDA(cudaMemsetAsync(out3, 0, 3 * sizeof(double), s));
+        return SX_OK;
+    }
+    const int nb = grid_for(n_verts, EN_BLOCK);
+    launch(energy_partial_kernel, nb, EN_BLOCK, 0, s, n_verts, (const float4*)x4, (const float4*)v4, m_inv, adj_ptr,
+           (const int2*)adj, (double)k_spring, (double)k_bend, (double)gx, (double)gy, (double)gz, (double*)ws);
+    launch(energy_finish_kernel, 1, 32, 0, s, nb, (const double*)ws, out3);
+    return check_launch("energy_finish_kernel");
+}
+
 extern "C" int sx_convergence_begin(int* conv, int check_every, int reset_totals, void* stream) {
     SX_REQUIRE(conv, "sx_convergence_begin: null pointer");
     SX_REQUIRE(check_every >= 2 && check_every % 2 == 0, "sx_convergence_begin: check_every must be even and >= 2");

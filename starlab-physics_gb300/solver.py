@@ -716,6 +716,24 @@ class Solver:
                                   self._res_ws.numel(), stream_handle())
         return out
 
+    def system_energy(self, out=None):
+        """Kinetic, gravitational and elastic energy of the cloth in FP64
+        (``sx_system_energy``; no counterpart in the reference): a device
+        tensor of three doubles, from ``x`` and ``v``.  The elastic term uses the
+        stiffnesses the sweep applies to each constraint type (springs
+        ``stiffness_bending``, bending pairs ``stiffness_stretch``, the
+        reference's pairing, XPBD.py:354-355)."""
+        m = self.mesh_dy
+        if out is None:
+            out = torch.zeros(3, dtype=torch.float64, device=self.device)
+        if getattr(self, "_energy_ws", None) is None:
+            self._energy_ws = torch.zeros(int(sx.sx_energy_workspace_bytes(m.num_verts)), dtype=torch.uint8,
+                                          device=self.device)
+        sx.sx_system_energy(ptr(m.x4), ptr(m.v4), ptr(m.m_inv), ptr(m.adj_ptr), ptr(m.adj), m.num_verts,
+                            float(self.stiffness_bending), float(self.stiffness_stretch), *self.g, ptr(out),
+                            ptr(self._energy_ws), self._energy_ws.numel(), stream_handle())
+        return out
+
     def contact_pair_count(self) -> int:
         """Pairs in the current contact pair list (host sync): the counts sit in
         the last 256 bytes of the pair-list workspace, {end of vertex-vs-static

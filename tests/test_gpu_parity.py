@@ -446,6 +446,25 @@ def test_graph_replay_equals_eager(pkg, n_iter):
         assert np.array_equal(a, b)
 
 
+def test_system_energy(pkg, po):
+    """The FP64 energy reduction against the oracle's float64 sums (same
+    terms, another summation order: agreement to 1e-12 relative)."""
+    scene = pkg.scenes.drape256(n=48, seed=3, sphere_subdiv=3)
+    sim = pkg.scenes.make_solver(scene, device=DEV)
+    sim.bending_on = "y"
+    for _ in range(2):
+        sim.forward(scene.n_substeps)
+    e = sim.system_energy().cpu().numpy()
+    m = sim.mesh_dy
+    ref = po.system_energy(_np(m.x4), _np(m.v4), _np(m.m_inv), _np(m.adj_ptr), _np(m.adj), sim.stiffness_bending,
+                           sim.stiffness_stretch, sim.g)
+    for got, want in zip(e, ref):
+        assert abs(got - want) <= 1e-12 * max(abs(want), 1e-30), (got, want)
+    assert e[0] > 0 and e[2] > 0
+    # deterministic
+    assert np.array_equal(sim.system_energy().cpu().numpy(), e)
+
+
 def test_constraint_residual(pkg, po):
     """sx_constraint_residual equals the oracle's restatement of its summation
     order bit for bit, and the FP64 value agrees with a float64 evaluation."""
