@@ -140,6 +140,28 @@ def _case_drape_sweeps(pkg):
                                     ptr(m.adj_rest32), m.num_verts, ks, kb, 1, form, 0, stream_handle())
 
 
+def _case_lanes(pkg):
+    """One sweep in each lanes-per-vertex variant over the 64 x 64 cloth, and
+    one FP64 energy reduction of the 256 x 256 drape."""
+    import torch
+    from starlab_physics_gb300._lib import ptr, stream_handle, sx
+    from starlab_physics_gb300.autotune import variant_forms
+
+    scene = pkg.scenes.plain64()
+    sim = pkg.scenes.make_solver(scene, device="cuda")
+    m = sim.mesh_dy
+    dt = scene.dt / scene.n_substeps
+    sim.compute_y(dt)
+    ks, kb = sim.stiffness_bending * dt * dt, sim.stiffness_stretch * dt * dt
+    out = torch.empty_like(m.y4)
+    for v, (lanes, _) in enumerate(variant_forms()):
+        if lanes > 1:
+            sx.sx_jacobi_sweep_mode(ptr(m.x4), ptr(m.y4), ptr(out), ptr(m.fixed), ptr(m.adj_ptr), ptr(m.adj),
+                                    m.num_verts, ks, kb, 1, v, 0, stream_handle())
+    d = pkg.scenes.make_solver(pkg.scenes.drape256(), device="cuda")
+    d.system_energy()
+
+
 def _case_color(pkg):
     """Colouring of the 256 x 256 cloth's edges (one call)."""
     _, f = pkg.grid_cloth(256)
@@ -155,7 +177,8 @@ def _case_learned(pkg):
 
 
 PROFILE_CASES = {"drape": _case_drape, "soup": _case_soup, "batched": _case_batched, "color": _case_color,
-                 "learned": _case_learned, "sweeps": _case_sweeps, "drape_sweeps": _case_drape_sweeps}
+                 "learned": _case_learned, "sweeps": _case_sweeps, "drape_sweeps": _case_drape_sweeps,
+                 "lanes": _case_lanes}
 
 
 def run_profile_case(name):
