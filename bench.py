@@ -176,9 +176,74 @@ def _case_learned(pkg):
     sim.forward(10)
 
 
+def _case_widening(pkg):
+    """One substep of each optional path on a 128 x 128 drape (pair records +
+    velocity-level contacts and friction + edge-edge contacts; Gauss-Seidel
+    sweeps; iterating to a tolerance), sewing on the 64 x 64 cloth, 65 536
+    edge-edge classifications, one Adam step of the warm-start network on
+    65 536 rows, the FP64 energy, and a 2^18-face LBVH under the reference's tie
+    rule."""
+    import numpy as np
+    import torch
+    from starlab_physics_gb300._lib import ptr, stream_handle, sx
+
+    scene = pkg.scenes.drape256(n=128)
+    cl = pkg.TriMesh(scene.cloth_x, scene.cloth_faces, device="cuda")
+    ob = pkg.TriMesh(scene.obstacle_x, scene.obstacle_faces, device="cuda", is_static=True)
+    sim = pkg.Solver(cl, ob, dHat=scene.dHat, stiffness_stretch=scene.stiffness_stretch,
+                     stiffness_bending=scene.stiffness_bending, g=scene.gravity, dt=scene.dt, n_iter=2,
+                     rebuild=scene.rebuild, cap=scene.cap, record_pairs=True, bending_on="y")
+    sim.padding = scene.padding
+    sim.enable_collision_handling = True
+    sim.enable_velocity_update = True
+    sim.enable_edge_edge = True
+    sim.mu = 0.4
+    sim.forward(1)
+    sim.system_energy()
+    gs = pkg.scenes.make_solver(pkg.scenes.drape256(n=128), device="cuda")
+    gs.bending_on = "y"
+    gs.gauss_seidel = True
+    gs.n_iter = 1
+    gs.forward(1)
+    tol = pkg.scenes.make_solver(pkg.scenes.drape256(n=128), device="cuda")
+    tol.bending_on = "y"
+    tol.tol = 1e-9
+    tol.n_iter = 8
+    tol.forward(1)
+    sew_scene = pkg.scenes.plain64(collisions=False)
+    sw = pkg.scenes.make_solver(sew_scene, device="cuda")
+    sw.bending_on = "y"
+    sw.n_iter = 1
+    sw.set_sewing_pairs(np.array([[i, 63 * 64 + i] for i in range(2, 62)], np.int32), 1e5)
+    sw.forward(1)
+    rng = np.random.default_rng(0)
+    n = 1 << 16
+    p12 = torch.from_numpy(rng.normal(0, 0.01, (n, 12)).astype(np.float32)).cuda()
+    dtype = torch.empty(n, dtype=torch.int32, device="cuda")
+    d = torch.empty(n, dtype=torch.float32, device="cuda")
+    g12 = torch.empty((n, 12), dtype=torch.float32, device="cuda")
+    sx.sx_edge_edge_classify(n, ptr(p12), 1e-4, ptr(dtype), ptr(d), ptr(g12), stream_handle())
+    mlp = pkg.WarmStartMLP(seed=0)
+    feat = torch.randn((n, 32), device="cuda").to(torch.bfloat16)
+    target4 = 1e-4 * torch.randn((n, 4), device="cuda")
+    idx = torch.arange(n, dtype=torch.int32, device="cuda")
+    mlp.train_step(feat, target4, idx, n)
+    nf = 1 << 18
+    verts, faces, _ = pkg.scenes.triangle_soup(nf, seed=1)
+    V4 = torch.zeros((verts.shape[0], 4), dtype=torch.float32, device="cuda")
+    V4[:, :3] = torch.from_numpy(verts).cuda()
+    F = torch.from_numpy(faces.reshape(-1)).cuda()
+    fmn = torch.empty((nf, 4), dtype=torch.float32, device="cuda")
+    fmx = torch.empty_like(fmn)
+    box = torch.empty(6, dtype=torch.float32, device="cuda")
+    sx.sx_face_aabbs(ptr(V4), ptr(F), nf, 0.0, ptr(fmn), ptr(fmx), stream_handle())
+    sx.sx_scene_aabb(ptr(V4), V4.shape[0], 0.0, ptr(box), stream_handle())
+    pkg.LBVH(nf, "cuda", tie=0).build(fmn, fmx, box)
+
+
 PROFILE_CASES = {"drape": _case_drape, "soup": _case_soup, "batched": _case_batched, "color": _case_color,
                  "learned": _case_learned, "sweeps": _case_sweeps, "drape_sweeps": _case_drape_sweeps,
-                 "lanes": _case_lanes}
+                 "lanes": _case_lanes, "widening": _case_widening}
 
 
 def run_profile_case(name):

@@ -841,37 +841,55 @@ __global__ void __launch_bounds__(MLP_BLOCK) mlp_wgrad_kernel(int M, int rows_pe
 }
 
 // ---------------------------------------------------------------------------
-// Training, part 3: sum the block and warp partials in index order (one thread
-// per parameter) into grad; stats[0] = loss (sum over warps, in order).
+// Training, part 3: sum the block and warp partials in a fixed order into
+// grad; stats[0] = loss (sum over the warps' partials).
 // Part 4: Adam on the FP32 master weights, refreshing the BF16 copy.
 // Structurally zero parameters (W1 columns >= 24, W3/b3 rows >= 3) stay zero.
 // ---------------------------------------------------------------------------
-__global__ void mlp_reduce_kernel(int nblocks, const float* __restrict__ bpart, int nwarps,
-                                  const float* __restrict__ wpart, float* __restrict__ grad,
-                                  float* __restrict__ stats) {
+constexpr int RD_GROUPS = 16;  // partial groups per parameter column in mlp_reduce_kernel
+
+// Block = 32 parameter columns x RD_GROUPS groups: group y sums partials
+// y, y + RD_GROUPS, ... of its column (coalesced across the columns), then
+// the groups are added in order -- a fixed order, so the sums are
+// deterministic.  Column -1 is the loss.
+__global__ void __launch_bounds__(32 * RD_GROUPS) mlp_reduce_kernel(int nblocks, const float* __restrict__ bpart,
+                                                                   int nwarps, const float* __restrict__ wpart,
+                                                                   float* __restrict__ grad,
+                                                                   float* __restrict__ stats) {
     pdl_entry();
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i == 0) {
-        float l = 0.0f;
-        for (int w = 0; w < nwarps; ++w) l += wpart[(size_t)w * kWpart];
-        stats[0] = l;
-    }
-    if (i >= kParams) return;
-    float gsum = 0.0f;
-    if (i < ob1) {
-        for (int b = 0; b < nblocks; ++b) gsum += bpart[(size_t)b * kWgrad + (i - oW1)];
+    __shared__ float part[RD_GROUPS][33];
+    const int tx = threadIdx.x & 31, gy = threadIdx.x >> 5;
+    const int i = blockIdx.x * 32 + tx - 1;
+    const float* base = wpart;
+    size_t stride = kWpart;
+    int count = 0;
+    if (i == -1) {
+        count = nwarps;
+    } else if (i < ob1) {
+        base = bpart + (i - oW1), stride = kWgrad, count = nblocks;
     } else if (i < oW2) {
-        for (int w = 0; w < nwarps; ++w) gsum += wpart[(size_t)w * kWpart + 1 + (i - ob1)];
+        base = wpart + 1 + (i - ob1), count = nwarps;
     } else if (i < ob2) {
-        for (int b = 0; b < nblocks; ++b) gsum += bpart[(size_t)b * kWgrad + kHid * kFeat + (i - oW2)];
+        base = bpart + kHid * kFeat + (i - oW2), stride = kWgrad, count = nblocks;
     } else if (i < oW3) {
-        for (int w = 0; w < nwarps; ++w) gsum += wpart[(size_t)w * kWpart + 1 + kHid + (i - ob2)];
+        base = wpart + 1 + kHid + (i - ob2), count = nwarps;
     } else if (i < ob3) {
-        for (int b = 0; b < nblocks; ++b) gsum += bpart[(size_t)b * kWgrad + kHid * kFeat + kHid * kHid + (i - oW3)];
-    } else {
-        for (int w = 0; w < nwarps; ++w) gsum += wpart[(size_t)w * kWpart + 1 + 2 * kHid + (i - ob3)];
+        base = bpart + kHid * kFeat + kHid * kHid + (i - oW3), stride = kWgrad, count = nblocks;
+    } else if (i < kParams) {
+        base = wpart + 1 + 2 * kHid + (i - ob3), count = nwarps;
     }
-    grad[i] = gsum;
+    float sum = 0.0f;
+    for (int k = gy; k < count; k += RD_GROUPS) sum += base[(size_t)k * stride];
+    part[gy][tx] = sum;
+    __syncthreads();
+    if (gy == 0 && i < kParams) {
+        float t = part[0][tx];
+        for (int y = 1; y < RD_GROUPS; ++y) t += part[y][tx];
+        if (i < 0)
+            stats[0] = t;
+        else
+            grad[i] = t;
+    }
 }
 
 __device__ __forceinline__ bool structural_zero(int i) {
@@ -1004,12 +1022,9 @@ static void train_shape(int M, int* fb_blocks, int* nwarps, int* wg_blocks, int*
     if (b > 152 * 8) b = 152 * 8;
     *fb_blocks = b;
     *nwarps = b * (MLP_BLOCK / 32);
-    int rpb = 2048;
-    int wg = (M + rpb - 1) / rpb;
-    if (wg > 152 * 2) {
-        rpb = ((M + 152 * 2 - 1) / (152 * 2) + WG_ROWS - 1) / WG_ROWS * WG_ROWS;
-        wg = (M + rpb - 1) / rpb;
-    }
+    // about two blocks per SM, whole 64-row tiles each
+    const int rpb = ((M + 152 * 2 - 1) / (152 * 2) + WG_ROWS - 1) / WG_ROWS * WG_ROWS;
+    const int wg = (M + rpb - 1) / rpb;
     *wg_blocks = wg;
     *rows_per_block = rpb;
 }
@@ -1055,7 +1070,7 @@ static int mlp_grad_launches(const TrainWs& w, const void* feat, const float* ta
     launch(mlp_wgrad_kernel, w.wg, MLP_BLOCK, 0, s, n_rows, w.rpb, idx, (const unsigned short*)feat, w.tb, w.bpart);
     rc = check_launch("mlp_wgrad_kernel");
     if (rc) return rc;
-    launch(mlp_reduce_kernel, grid_for(kParams, 256), 256, 0, s, w.wg, (const float*)w.bpart, w.nw,
+    launch(mlp_reduce_kernel, (kParams + 1 + 31) / 32, 32 * RD_GROUPS, 0, s, w.wg, (const float*)w.bpart, w.nw,
            (const float*)w.tb.wpart, grad, stats);
     return check_launch("mlp_reduce_kernel");
 }
