@@ -384,6 +384,53 @@ def test_pair_list_sweep_equals_per_query_sweep(pkg, cull):
     assert np.array_equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("cap", [40, 64, 80])
+def test_contact_pair_list_layout(pkg, cap):
+    """The flattened pair list equals a host restatement of its definition:
+    queries in order (vertex vs obstacle, vertex vs cloth, obstacle vertex vs
+    cloth), each query's candidates in list order, vertex-vs-cloth candidates
+    incident to the query dropped, (query, triangle vertices) per pair; the
+    kind boundaries in the workspace's last 256 bytes."""
+    sc, cl, sp = _drape(pkg, n=40)
+    sim = pkg.Solver(cl, sp, dHat=(4e-2) ** 2, stiffness_stretch=1e5, stiffness_bending=1e8, g=(0, 0, -9.81),
+                     dt=1 / 60, cap=cap)
+    sim.padding = 0.06
+    sim.enable_collision_handling = True
+    x = _np(cl.x4).copy()
+    x[:, 2] = 0.5 + 0.3 + 0.01 * np.sin(13 * x[:, 0]) * np.cos(7 * x[:, 1])
+    cl.x4.copy_(_t(x))
+    sim.build_bvhs()
+    sim.compute_y(1 / 600)
+    sim.broadphase_lbvh()
+    sim.build_contact_pairs()
+    torch.cuda.synchronize()
+    fd, fs = cl.fid_np.reshape(-1, 3), sp.fid_np.reshape(-1, 3)
+    Vd, Vs = cl.num_verts, sp.num_verts
+    ref = []
+    c, n = _np(sim.vt_st_candidates), _np(sim.vt_st_candidates_num)
+    for q in range(Vd):
+        for f in c[q, :min(n[q], cap)]:
+            ref.append((q, *fs[f]))
+    st_end = len(ref)
+    c, n = _np(sim.vt_dy_candidates), _np(sim.vt_dy_candidates_num)
+    for q in range(Vd):
+        for f in c[q, :min(n[q], cap)]:
+            if q not in fd[f]:
+                ref.append((q, *fd[f]))
+    dy_end = len(ref)
+    c, n = _np(sim.tv_st_candidates), _np(sim.tv_st_candidates_num)
+    for q in range(Vs):
+        for f in c[q, :min(n[q], cap)]:
+            ref.append((q, *fd[f]))
+    ref = np.array(ref, np.int32).reshape(-1, 4)
+    P = sim.contact_pair_count()
+    meta = sim._pairs_ws[-256:].view(torch.int32)[:3].cpu().numpy()
+    assert P == ref.shape[0] and tuple(meta) == (st_end, dy_end, P)
+    assert st_end > 0 and dy_end > st_end and P > dy_end
+    assert int(_np(sim.vt_dy_candidates_num).max()) > 0
+    assert np.array_equal(_np(sim._pairs)[:P], ref)
+
+
 @pytest.mark.parametrize("cull", [False, True])
 def test_pair_projection_variants_agree(pkg, cull):
     """Every compiled launch configuration of the pair projection adds the same
