@@ -162,6 +162,15 @@ def _case_lanes(pkg):
     d.system_energy()
 
 
+def _case_plain64(pkg):
+    """Two frames of the 64 x 64 cloth over the box with eager launches."""
+    scene = pkg.scenes.plain64()
+    sim = pkg.scenes.make_solver(scene, device="cuda")
+    sim.bending_on = "y"
+    for _ in range(2):
+        sim.forward(scene.n_substeps)
+
+
 def _case_color(pkg):
     """Colouring of the 256 x 256 cloth's edges (one call)."""
     _, f = pkg.grid_cloth(256)
@@ -243,7 +252,7 @@ def _case_widening(pkg):
 
 PROFILE_CASES = {"drape": _case_drape, "soup": _case_soup, "batched": _case_batched, "color": _case_color,
                  "learned": _case_learned, "sweeps": _case_sweeps, "drape_sweeps": _case_drape_sweeps,
-                 "lanes": _case_lanes, "widening": _case_widening}
+                 "lanes": _case_lanes, "widening": _case_widening, "plain64": _case_plain64}
 
 
 def run_profile_case(name):

@@ -484,8 +484,11 @@ __device__ __forceinline__ NodeBox join_nodes(const NodeBox& l, const NodeBox& r
     return o;
 }
 
-// Block = one z-column (cells col*32 .. col*32+31), warp w = cell col*32 + w.
-__global__ void __launch_bounds__(1024) cell_column_refit_kernel(
+// Block = one z-column (cells col*32 .. col*32+31), a warp per cell: 8 warps
+// taking 4 cells each, so that the 1024 columns fit one wave of blocks.
+constexpr int kColumnRefitThreads = 256;
+
+__global__ void __launch_bounds__(kColumnRefitThreads) cell_column_refit_kernel(
     const float* __restrict__ box6, const int* __restrict__ prefix, const int* __restrict__ sorted_face_ids,
     const float4* __restrict__ fmn4, const float4* __restrict__ fmx4, int* __restrict__ num_faces,
     float4* __restrict__ nmin4, float4* __restrict__ nmax4, float4* __restrict__ frec, float* grid8) {
@@ -493,46 +496,49 @@ __global__ void __launch_bounds__(1024) cell_column_refit_kernel(
     __shared__ NodeBox tree[64];  // [32 + k]: leaf k; [16 + k], [8 + k], ...: levels above
     __shared__ unsigned ext_bits[3];
     const int col = blockIdx.x, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int i = col * kGridRes + w;
     if (threadIdx.x < 3) ext_bits[threadIdx.x] = 0u;
     const V3 lo{box6[0], box6[1], box6[2]};
     const V3 cs = cell_size_of(box6);
-    const int rl = i == 0 ? 0 : prefix[i - 1];
-    const int size = prefix[i] - rl;
-    const V3 c = cell_center(i, cs, lo);
-    V3 a = c, b = c;
-    for (int j = lane; j < size; j += 32) {
-        const int fid = sorted_face_ids[rl + j];
-        const float4 fa = fmn4[fid], fb = fmx4[fid];
-        a = vmin(a, mk(fa));
-        b = vmax(b, mk(fb));
-        frec[2 * (rl + j)] = make_float4(fa.x, fa.y, fa.z, __int_as_float(fid));
-        frec[2 * (rl + j) + 1] = make_float4(fb.x, fb.y, fb.z, 0.0f);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a = vmin(a, V3{__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o),
-                       __shfl_xor_sync(0xffffffffu, a.z, o)});
-        b = vmax(b, V3{__shfl_xor_sync(0xffffffffu, b.x, o), __shfl_xor_sync(0xffffffffu, b.y, o),
-                       __shfl_xor_sync(0xffffffffu, b.z, o)});
-    }
     __syncthreads();  // ext_bits initialised
-    if (lane == 0) {
-        const int leaf = i + kNumCells - 1;
-        num_faces[leaf] = size;
-        store_box(nmin4, nmax4, leaf, a, b, size);
-        tree[32 + w] = NodeBox{a, b, size};
-        // how far this leaf's box reaches beyond its cell (>= 0), maximised
-        // over the grid: the traversal scans the cells within that reach
-        if (size > 0) {
-            const int x0 = i / (kGridRes * kGridRes), y0 = (i % (kGridRes * kGridRes)) / kGridRes, z0 = w;
-            const float clo[3] = {lo.x + cs.x * (float)x0, lo.y + cs.y * (float)y0, lo.z + cs.z * (float)z0};
-            const float chi[3] = {lo.x + cs.x * (float)(x0 + 1), lo.y + cs.y * (float)(y0 + 1),
-                                  lo.z + cs.z * (float)(z0 + 1)};
-            const float am[3] = {a.x, a.y, a.z}, bm[3] = {b.x, b.y, b.z};
-            for (int k = 0; k < 3; ++k) {
-                const float ext = fmaxf(fmaxf(clo[k] - am[k], bm[k] - chi[k]), 0.0f);
-                if (ext > 0.0f) atomicMax(ext_bits + k, __float_as_uint(ext));
+    // warp w takes the column's cells w, w + warps, ... (one warp per cell)
+    for (int z = w; z < kGridRes; z += kColumnRefitThreads / 32) {
+        const int i = col * kGridRes + z;
+        const int rl = i == 0 ? 0 : prefix[i - 1];
+        const int size = prefix[i] - rl;
+        const V3 c = cell_center(i, cs, lo);
+        V3 a = c, b = c;
+        for (int j = lane; j < size; j += 32) {
+            const int fid = sorted_face_ids[rl + j];
+            const float4 fa = fmn4[fid], fb = fmx4[fid];
+            a = vmin(a, mk(fa));
+            b = vmax(b, mk(fb));
+            frec[2 * (rl + j)] = make_float4(fa.x, fa.y, fa.z, __int_as_float(fid));
+            frec[2 * (rl + j) + 1] = make_float4(fb.x, fb.y, fb.z, 0.0f);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            a = vmin(a, V3{__shfl_xor_sync(0xffffffffu, a.x, o), __shfl_xor_sync(0xffffffffu, a.y, o),
+                           __shfl_xor_sync(0xffffffffu, a.z, o)});
+            b = vmax(b, V3{__shfl_xor_sync(0xffffffffu, b.x, o), __shfl_xor_sync(0xffffffffu, b.y, o),
+                           __shfl_xor_sync(0xffffffffu, b.z, o)});
+        }
+        if (lane == 0) {
+            const int leaf = i + kNumCells - 1;
+            num_faces[leaf] = size;
+            store_box(nmin4, nmax4, leaf, a, b, size);
+            tree[32 + z] = NodeBox{a, b, size};
+            // how far this leaf's box reaches beyond its cell (>= 0), maximised
+            // over the grid: the traversal scans the cells within that reach
+            if (size > 0) {
+                const int x0 = i / (kGridRes * kGridRes), y0 = (i % (kGridRes * kGridRes)) / kGridRes, z0 = z;
+                const float clo[3] = {lo.x + cs.x * (float)x0, lo.y + cs.y * (float)y0, lo.z + cs.z * (float)z0};
+                const float chi[3] = {lo.x + cs.x * (float)(x0 + 1), lo.y + cs.y * (float)(y0 + 1),
+                                      lo.z + cs.z * (float)(z0 + 1)};
+                const float am[3] = {a.x, a.y, a.z}, bm[3] = {b.x, b.y, b.z};
+                for (int k = 0; k < 3; ++k) {
+                    const float ext = fmaxf(fmaxf(clo[k] - am[k], bm[k] - chi[k]), 0.0f);
+                    if (ext > 0.0f) atomicMax(ext_bits + k, __float_as_uint(ext));
+                }
             }
         }
     }
@@ -1084,7 +1090,7 @@ extern "C" int sx_cell_bvh_build(const float* fmin4, const float* fmax4, int n_f
         rc = radix_sort(keys, sorted_face_ids, n_faces, 15, rws, rs_ws_bytes(n_faces), s);
         if (rc) return rc;
     }
-    launch(cell_column_refit_kernel, kGridRes * kGridRes, 1024, 0, s, box6, (const int*)prefix,
+    launch(cell_column_refit_kernel, kGridRes * kGridRes, kColumnRefitThreads, 0, s, box6, (const int*)prefix,
            (const int*)sorted_face_ids, (const float4*)fmin4, (const float4*)fmax4, num_faces, (float4*)nmin4,
            (float4*)nmax4, (float4*)face_rec8, grid8);
     rc = check_launch("cell_column_refit_kernel");
